@@ -1,0 +1,323 @@
+"""Benchmark of the explicit shell time step on one GB300 (and N replicas).
+
+Workload (the single-shell FP64 configuration): level-6 icosphere (40,962
+nodes, 81,920 faces), orthotropic Koiter shell E1=1, E2=0.5, nu12=0.3,
+G12=0.35, h/R=0.01, density 1, Rayleigh damping 0.05, dt=1e-4, external
+pressure ramped from 0 to 2x the classical buckling pressure over 20,000
+steps, seeded Gaussian normal imperfection of amplitude 1e-3 R, linear
+self-contact with Coulomb friction mu=0.3 and linked cells of 2h.  Inputs are
+synthetic (generated icosphere and seeded imperfection); there is no dataset.
+
+A step is one Newmark step (ShellSystem::advance) of that shell; the metric is
+face-steps per second.  Reported:
+  value      device throughput of the timed steps, each step launched as one
+             CUDA graph and bracketed by CUDA events on the library's stream,
+             with L2 evicted (a 512 MB write) before every step;
+  e2e        the same steps through the C ABI with host buffers: per step the
+             state (u, v, a) is copied from pinned host memory, one step runs,
+             and the state is copied back;
+  roofline   the element-force kernel timed live (events, cold L2) against
+             its algorithmic bytes and FP64 flops;
+  cpu_baseline  the CPU oracle on this host's cores on a bounded sample.
+
+python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--level L]
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+E1, E2, NU12, G12, H, RHO, ALPHA, DT = 1.0, 0.5, 0.3, 0.35, 0.01, 1.0, 0.05, 1e-4
+RAMP_STEPS, RAMP_FACTOR, AMPL, SEED, MU = 20000, 2.0, 1e-3, 0, 0.3
+FLUSH_BYTES = 512 << 20
+# kernel launches per step of the library: predictor, element, contact force,
+# gather/corrector, volume/end-of-step, and two linked-cell passes of 22
+# kernels each (each pass returns at once when no rebuild is due)
+LAUNCHES_PER_STEP_CONTACT = 5 + 2 * 22
+# element kernel: per-face FP64 constants, patch ids, force shares, element
+# fields, face permutation (bytes); per-node predicted displacement (bytes)
+ELEM_BYTES_PER_FACE = 35 * 8 + 12 * 4 + 36 * 8 + 5 * 8 + 4
+ELEM_BYTES_PER_NODE = 24
+# FP64 flops of one regular face in the element kernel (count of the
+# arithmetic in element_force<12>, fused multiply-add = 2)
+ELEM_FLOPS_PER_FACE = 1372
+
+
+def classical_pressure():
+    E = np.sqrt(E1 * E2)
+    nu = np.sqrt(NU12 * NU12 * E2 / E1)
+    return 2 * E * H * H / np.sqrt(3 * (1 - nu * nu))
+
+
+def workload(L, level):
+    X, T = L.icosphere(level)
+    P = X[T]
+    cell_mult = 2 * H / (P.max(axis=1) - P.min(axis=1)).max(axis=1).mean()
+    p = L.default_params(shell_mass_density=RHO, shell_young_modulus=E1, shell_young_modulus2=E2,
+                         shell_poisson_ratio=NU12, shell_shear_modulus=G12, thickness=H, damping_alpha=ALPHA, dt=DT,
+                         shell_shell_contact=L.CONTACT_LINEAR, mu_s=MU, mu_d=MU, cell_size_mult=cell_mult)
+    u0 = L.gaussian_normal_imperfection(X, AMPL, SEED).reshape(-1)
+    return X, T, p, u0
+
+
+def pressure(step):
+    """p(t) at the end of step `step` (1-based): -s p_cl t / T."""
+    return -RAMP_FACTOR * classical_pressure() * np.asarray(step, dtype=np.float64) / RAMP_STEPS
+
+
+def cpu_sample(X, T, p, u0, seconds=10.0, threads=None):
+    """CPU oracle on the same workload: steps until about `seconds` elapsed."""
+    import oracle as O
+
+    threads = threads or os.cpu_count()
+    o = O.Oracle(X, T, p, threads=threads)
+    o.apply_initial_conditions(u0, 0.0, pressure(1))
+    o.step(1, pressure([1]))
+    t0 = time.perf_counter()
+    o.step(2, pressure([2, 3]))
+    per = (time.perf_counter() - t0) / 2
+    n = int(max(2, min(2000, seconds / max(per, 1e-6))))
+    t0 = time.perf_counter()
+    o.step(n, pressure(np.arange(4, 4 + n)))
+    dt = time.perf_counter() - t0
+    o.close()
+    return {"value": len(T) * n / dt, "unit": "face-steps/s", "cores": threads, "kind": "port",
+            "sample": "%d steps (steps 4-%d) of the level-%d workload, %.1f s, OpenMP %d threads"
+                      % (n, 3 + n, int(round(np.log(len(T) / 20) / np.log(4))), dt, threads)}
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples during the timed region."""
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + q,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx = float(f[1])
+            except ValueError:
+                continue
+            for nm, val in zip(names, f[4:8]):
+                if val.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def run_reference(args, rank, world):
+    """The reference arm: the CPU restatement of the reference's step (the
+    reference itself does not build), all host threads, same workload."""
+    import shell_gb300.lib as L
+
+    if rank != 0:
+        return
+    X, T, p, u0 = workload(L, args.level)
+    s = cpu_sample(X, T, p, u0, seconds=args.cpu_seconds)
+    line = {"metric": "shell face-steps/sec at 1 GB300", "value": s["value"], "unit": "face-steps/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "impl": "reference",
+            "config": {"workload": "single shell, level-%d icosphere (%d faces), FP64, self-contact + friction"
+                                   % (args.level, len(T)), "faces": int(len(T)), "nodes": int(len(X)),
+                       "parallelism": "replicas", "l2": "n/a (CPU)"},
+            "cpu_baseline": {"value": s["value"], "unit": s["unit"], "cores": s["cores"], "kind": "port",
+                             "sample": s["sample"]},
+            "e2e": {"value": s["value"], "unit": "face-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": "the reference needs an unpublished libMesh fork and muparser and misses Contact.C; "
+                    "its CPU step is timed through the oracle restatement"}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, rank, world, dist):
+    import torch
+
+    import shell_gb300.lib as L
+
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    X, T, p, u0 = workload(L, args.level)
+    F, V = len(T), len(X)
+    g = L.Shell(X, T, p)
+    g.apply_initial_conditions(u0, 0.0, pressure(1))
+    stream = torch.cuda.ExternalStream(g.stream_handle())
+    flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.int32, device="cuda")
+    W, K = args.warmup, args.steps
+    g.upload_pressure_table(pressure(np.arange(1, 1 + W + K)))
+    # warm-up (graph instantiation, first rebuilds)
+    g.step_enqueue(W)
+    torch.cuda.synchronize()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(K)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(K)]
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(dev) as clk:
+        with torch.cuda.stream(stream):
+            for k in range(K):
+                flush.fill_(k)
+                starts[k].record(stream)
+                g.step_enqueue(1)
+                ends[k].record(stream)
+        torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
+    report, status = g.step_collect()
+    if dist:
+        t = torch.tensor([ms], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = F * K * world / (ms * 1e-3)
+
+    # warm continuous throughput (informative): K steps back to back, one graph replay per 16 steps
+    g.upload_pressure_table(pressure(np.arange(1 + W + K, 1 + W + 2 * K)))
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        e0.record(stream)
+        g.step_enqueue(K)
+        e1.record(stream)
+    torch.cuda.synchronize()
+    warm = F * K / (e0.elapsed_time(e1) * 1e-3)
+    g.step_collect()
+
+    # e2e through the C ABI with pinned host buffers
+    u, v, a = g.get_state()
+    hu = torch.from_numpy(u).pin_memory()
+    hv = torch.from_numpy(v).pin_memory()
+    ha = torch.from_numpy(a).pin_memory()
+    nu_, nv_, na_ = hu.numpy(), hv.numpy(), ha.numpy()
+    Ke = max(8, K // 4)
+    pt = pressure(np.arange(1 + W + 2 * K, 1 + W + 2 * K + Ke))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for k in range(Ke):
+        g.set_state(nu_, nv_, na_)
+        g.step(1, pt[k:k + 1])
+        uu, vv, aa = g.get_state()
+        nu_[:], nv_[:], na_[:] = uu, vv, aa
+    e2e_s = time.perf_counter() - t0
+    e2e = F * Ke * world / e2e_s
+
+    # roofline of the element kernel (live, cold L2)
+    elem_ms = g.time_kernel(0, reps=20, flush_bytes=FLUSH_BYTES)
+    fp64_peak = L.measure_fp64_peak()
+    g.close()
+    bytes_elem = F * ELEM_BYTES_PER_FACE + V * ELEM_BYTES_PER_NODE
+    achieved_gbs = bytes_elem / (elem_ms * 1e-3) / 1e9
+    achieved_tf = F * ELEM_FLOPS_PER_FACE / (elem_ms * 1e-3) / 1e12
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    if rank != 0:
+        return
+    cpu = cpu_sample(X, T, p, u0, seconds=args.cpu_seconds) if args.cpu_seconds > 0 else None
+    line = {
+        "metric": "shell face-steps/sec at 1 GB300", "value": value, "unit": "face-steps/s", "n_gpus": world,
+        "steps": K, "warmup": W, "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "single shell, level-%d icosphere (%d faces, %d nodes), FP64 element forces and "
+                               "state, self-contact + Coulomb friction, pressure ramp to 2 p_cl over %d steps, "
+                               "steps %d-%d of the run" % (args.level, F, V, RAMP_STEPS, W + 1, W + K),
+                   "faces": F, "nodes": V, "parallelism": "replicas (one shell per GPU)" if world > 1 else "single",
+                   "l2": "evicted before every timed step (512 MB write)"},
+        "warm_value": warm,
+        "e2e": {"value": e2e, "unit": "face-steps/s", "h2d_bytes_per_step": 3 * 3 * V * 8,
+                "d2h_bytes_per_step": 3 * 3 * V * 8,
+                "how": "per step: shl_set_state from pinned host, shl_step(1), shl_get_state"},
+        "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm, "unit": "GB/s",
+                     "frac": achieved_gbs / hbm, "traffic": None, "kernel": "k_elements",
+                     "kernel_ms": elem_ms, "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)",
+                     "fp64": {"achieved_tflops": achieved_tf, "peak_tflops": fp64_peak,
+                              "frac": achieved_tf / fp64_peak,
+                              "peak_source": "DFMA register loop measured in this run"}},
+        "cpu_baseline": cpu,
+        "clocks": clk.summary(),
+        "gpu_launches": LAUNCHES_PER_STEP_CONTACT * K,
+        "status": {"worst_problem": report.worst_problem, "steps_done": report.steps_done,
+                   "n_rebuilds": report.n_rebuilds, "n_pairs": report.last.n_pairs},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=400)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--level", type=int, default=6)
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    dist = None
+    import __graft_entry__
+
+    __graft_entry__.build()
+    if world > 1:
+        import torch
+        import torch.distributed as tdist
+
+        if args.impl == "ours":
+            torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        tdist.init_process_group("nccl" if args.impl == "ours" else "gloo")
+        dist = tdist
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_ours(args, rank, world, dist)
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

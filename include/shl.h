@@ -1,0 +1,260 @@
+/*
+ * shl.h -- C ABI of the GB300 shell library (libshl_gb300.so).
+ *
+ * The library is a drop-in for the per-step force evaluation and explicit
+ * Newmark integration of the Loop-subdivision Koiter shell solver
+ * (ShellSystem::advance and everything it calls, ShellSystem.C:952-1122).
+ * A host driver keeps the mesh, the config.cfg parameters and the state file,
+ * and calls these entry points from its time loop in place of
+ * `system.advance(time_step)` (shell.C:340).
+ *
+ * Conventions
+ *  - Plain C types only.  Host arrays are owned by the caller and copied.
+ *  - Node-major vectors: x[3*nid + c], c = 0,1,2; node and face ids are the
+ *    order of the OFF file (0-based).
+ *  - Every call returns a shl_status; nothing throws or exits.  Values 1..7
+ *    equal ShellSystem::Problem (ShellSystem.h:48-49); values >= 100 are
+ *    errors of the library itself.
+ *  - A context owns its device memory and one CUDA stream; it is not
+ *    thread-safe (one host thread per context).
+ *  - All arithmetic is FP64 unless a precision mode says otherwise.
+ */
+#ifndef SHL_H_
+#define SHL_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ShellSystem::Problem (ShellSystem.h:48-49) + library errors. */
+typedef enum shl_status {
+  SHL_OK = 0,
+  SHL_NO_DISP_CHANGE = 1,
+  SHL_LARGE_DISP = 2,
+  SHL_STOP_SIM = 3,
+  SHL_TOO_MANY_CELLS = 4,
+  SHL_SMALL_TIMESTEP = 5,
+  SHL_CONTACT_PROBLEM = 6,
+  SHL_NOT_FINITE = 7,
+  SHL_ERR_ARG = 100,     /* invalid argument or unsupported option */
+  SHL_ERR_CUDA = 101,    /* a CUDA call failed; see shl_last_error() */
+  SHL_ERR_TIMEOUT = 102, /* a bounded device wait ran out */
+  SHL_ERR_OOM = 103,     /* device allocation failed */
+  SHL_ERR_CAPACITY = 104 /* a device buffer (e.g. contact pairs) is too small */
+} shl_status;
+
+/* ShellSystem::ContactType (ShellSystem.h:46). */
+enum { SHL_CONTACT_LINEAR = 0, SHL_CONTACT_SMOOTH = 1, SHL_CONTACT_NONE = 2 };
+/* ShellSystem::CoordinateSystem (ShellSystem.h:42) for pressure_base. */
+enum { SHL_CS_LOCAL = 0, SHL_CS_CARTESIAN = 1, SHL_CS_CYLINDRICAL = 2, SHL_CS_SPHERICAL = 3 };
+/* Element-force precision. */
+enum { SHL_PREC_FP64 = 0, SHL_PREC_FP32 = 1 };
+
+/* A closed triangle mesh (the OFF file after refinement/projection,
+ * shell.C:147-230).  Faces are outward oriented. */
+typedef struct shl_mesh {
+  uint32_t n_nodes;
+  uint32_t n_faces;
+  const double* xyz;      /* 3*n_nodes */
+  const uint32_t* faces;  /* 3*n_faces */
+} shl_mesh;
+
+/* The parameters of ShellSystem::set_parameters (ShellSystem.C:170-418) that
+ * act on the time step.  Names follow config.cfg. */
+typedef struct shl_params {
+  /* material (ShellSystem.C:176-186) */
+  double shell_mass_density;
+  double shell_young_modulus;   /* E1 */
+  double shell_young_modulus2;  /* E2 */
+  double shell_poisson_ratio;   /* nu12 */
+  double shell_shear_modulus;   /* G12 */
+  double bulk_modulus;
+  double memb_stiff_mult;
+  double bend_stiff_mult;
+  double thickness;
+  /* dynamics (ShellSystem.C:215-233) */
+  double damping_alpha;
+  double damping_beta;
+  double damping_gamma;
+  double pressure;        /* used when a step gets no per-step pressure table */
+  int32_t pressure_base;  /* SHL_CS_* */
+  int32_t pressure_dir;   /* 0,1,2 */
+  /* self-contact (ShellSystem.C:256-276) */
+  int32_t shell_shell_contact;  /* SHL_CONTACT_* */
+  int32_t pad0;
+  double mu_s, mu_d;
+  double self_damping;
+  double self_friction_damping;
+  double fric_stiff_mult;
+  double friction_stop_velocity;
+  double static_friction_tol;
+  double cell_size_mult;
+  double cell_margin;
+  double neighbor_margin;
+  /* time integration (ShellSystem.C:285-313) */
+  double dt;
+  double newmark_beta;
+  double newmark_gamma;
+  /* reproduce ShellSystem.C:1480, where the pressure is multiplied by a
+   * global that is never assigned (so it is always zero) */
+  int32_t compat_zero_pressure;
+  /* element-force precision, SHL_PREC_* */
+  int32_t precision;
+  /* stop after any problem, not only after those >= SHL_STOP_SIM
+   * (ShellSystem.C:289, 2952) */
+  int32_t stop_on_problem;
+  int32_t pad1;
+} shl_params;
+
+/* Scalars measured in a step (ShellSystem.C:2686-2846). */
+typedef struct shl_energies {
+  double Etens, Ebend;    /* elastic energies at the predicted state */
+  double Eself, Efric;    /* self-contact and friction energies */
+  double Ekin;            /* kinetic energy after the corrector */
+  double area, volume;    /* deformed area and enclosed volume */
+  double kGauss, kMean;   /* integrated curvatures */
+  uint32_t Nc;            /* contacts with penetration */
+  uint32_t n_pairs;       /* contact candidates in the list */
+} shl_energies;
+
+/* Summary of shl_step(). */
+typedef struct shl_step_report {
+  uint32_t steps_done;     /* steps completed (stops early on status >= SHL_STOP_SIM) */
+  int32_t worst_problem;   /* max over the steps, ShellSystem::register_problem */
+  double time;             /* simulation time after the last step */
+  double du_sum;           /* linked-cell displacement budget (ShellSystem.C:2634) */
+  uint32_t n_rebuilds;     /* candidate-list rebuilds performed */
+  uint32_t pad;
+  shl_energies last;       /* measurements of the last step */
+  /* dt-weighted sums over the steps (the MovingAverage inputs, ShellSystem.C:2830-2843) */
+  double sum_dt, sum_area, sum_volume, sum_Nc, sum_Ekin, sum_Etens, sum_Ebend,
+      sum_Eself, sum_Efric, sum_kGauss, sum_kMean;
+} shl_step_report;
+
+typedef struct shl_ctx shl_ctx;
+
+/* Library and build information ("shl_gb300 <version> sm_103a"). */
+const char* shl_version(void);
+/* Text of the last error on this thread (CUDA error string or argument check). */
+const char* shl_last_error(void);
+/* Human-readable name of a status. */
+const char* shl_status_string(shl_status s);
+
+/* Set-up: ShellSystem::set_parameters + build_cache + compute_mass_damping
+ * (ShellSystem.C:170-418, 490-681, 762-852).  Computes the subdivision basis,
+ * the reference metrics, masses, damping and the topological neighbourhood on
+ * the host and uploads everything to the current CUDA device. */
+shl_status shl_create(const shl_mesh* mesh, const shl_params* params, shl_ctx** out);
+void shl_destroy(shl_ctx* ctx);
+
+/* ShellSystem::apply_initial_conditions without a load file
+ * (ShellSystem.C:855-905): u = u0, v = a = 0, time = t0; computes the element
+ * bounding boxes, the enclosed volume, the first contact list, and
+ * a = M^-1 f at time t0 + dt with the given pressure. */
+shl_status shl_apply_initial_conditions(shl_ctx* ctx, const double* u0, double t0,
+                                        double pressure_next);
+
+/* State in and out (ShellSystem::save/load, ShellSystem.C:2956-3153).
+ * shl_set_state also sets u_pred = u. */
+shl_status shl_set_state(shl_ctx* ctx, const double* u, const double* v, const double* a);
+shl_status shl_get_state(shl_ctx* ctx, double* u, double* v, double* a);
+shl_status shl_set_time(shl_ctx* ctx, double time, uint32_t time_step);
+shl_status shl_get_time(shl_ctx* ctx, double* time, uint32_t* time_step);
+
+/* Force evaluation at a given predicted state: steps 3-8 of one advance()
+ * (ShellSystem.C:993-1008): candidate-list update if due, deformed metrics,
+ * external force (pressure at `pressure`, self-contact with friction using
+ * the current velocity), minus the internal force.  f_out gets f before the
+ * damping term (may be NULL); a_out gets M^-1 (f - C v_pred) (may be NULL).
+ * The stored u, v, a are not changed; the contact state is updated as the
+ * reference does. */
+shl_status shl_eval_forces(shl_ctx* ctx, const double* u_pred, const double* v_pred,
+                           double pressure, double* f_out, double* a_out, shl_energies* e);
+
+/* n_steps calls of ShellSystem::advance with fixed dt (ShellSystem.C:952-1122).
+ * pressure_table: pressure for each step (evaluated by the host at the step's
+ * time t + dt), or NULL to use params.pressure.  The steps run on the
+ * device without host synchronisation (captured in a CUDA graph when
+ * use_graph != 0); problems are recorded per step and the remaining steps are
+ * skipped once a problem >= SHL_STOP_SIM is registered. */
+shl_status shl_step(shl_ctx* ctx, uint32_t n_steps, const double* pressure_table,
+                    int use_graph, shl_step_report* report);
+
+/* Asynchronous stepping for drivers that overlap host work (and for timing
+ * with CUDA events on the context's stream):
+ *  shl_get_stream      the context's cudaStream_t (as void*);
+ *  shl_upload_pressure_table  copy n per-step pressures to the device and
+ *                      restart the table at its first entry;
+ *  shl_step_enqueue    enqueue n steps (graph replays) without synchronising;
+ *                      step k uses table entry k since the last upload;
+ *  shl_step_collect    wait for the stream and fill the report of every step
+ *                      enqueued since the last collect (or shl_step). */
+shl_status shl_get_stream(shl_ctx* ctx, void** stream);
+shl_status shl_upload_pressure_table(shl_ctx* ctx, const double* pressure_table, uint32_t n);
+shl_status shl_step_enqueue(shl_ctx* ctx, uint32_t n_steps);
+shl_status shl_step_collect(shl_ctx* ctx, shl_step_report* report);
+
+/* Kernel timing for the roofline report: launches one kernel of the step
+ * `reps` times at the current state on the context's stream, each launch
+ * bracketed by CUDA events, optionally after writing `flush_bytes` of a
+ * scratch buffer to evict L2; returns the mean launch time.
+ * which: 0 element kernel, 1 gather/corrector (evaluation mode),
+ * 2 contact force, 3 predictor. */
+shl_status shl_time_kernel(shl_ctx* ctx, int which, int reps, size_t flush_bytes, double* avg_ms);
+/* FP64 fused-multiply-add throughput of the current device, measured with a
+ * register-resident DFMA loop (TFLOP/s, 2 flops per DFMA). */
+shl_status shl_measure_fp64_peak(double* tflops);
+
+/* Contact candidate list, sorted by (eid1, eid2), eid1 < eid2. */
+shl_status shl_get_contact_pairs(shl_ctx* ctx, uint32_t* pairs /* 2*cap */, size_t cap,
+                                 size_t* n_pairs);
+/* Full per-pair state for checkpoints and parity checks. Any pointer may be NULL. */
+shl_status shl_get_contact_state(shl_ctx* ctx, uint32_t* pairs, uint8_t* stick,
+                                 double* spring_origin /* 3*cap */, double* d2, size_t cap,
+                                 size_t* n_pairs, double* du_sum);
+shl_status shl_set_contact_state(shl_ctx* ctx, const uint32_t* pairs, const uint8_t* stick,
+                                 const double* spring_origin, const double* d2, size_t n_pairs,
+                                 double du_sum);
+/* Force a rebuild of the candidate list at the current positions
+ * (compute_shell_shell_contact_candidates(true), ShellSystem.C:1910). */
+shl_status shl_rebuild_contacts(shl_ctx* ctx);
+
+/* Per-element kGauss/kMean/etens/ebend densities of the last force
+ * evaluation (ShellSystem.C:1299-1300, 2783-2784); any pointer may be NULL. */
+shl_status shl_get_element_fields(shl_ctx* ctx, double* kGauss, double* kMean, double* etens,
+                                  double* ebend, double* area);
+
+/* Lumped inverse masses and damping coefficients (ShellSystem.C:762-852). */
+shl_status shl_get_mass_damping(shl_ctx* ctx, double* Minv, double* C);
+
+/* ---- host helpers of the driver (no device work) ----------------------- */
+
+/* Closed icosphere: the 20-face icosahedron refined `level` times, each
+ * midpoint pushed to the unit sphere, written as OFF text with %g and read
+ * back (so ids and rounded coordinates equal those of icosasphere<level>.off).
+ * Writes up to cap_nodes nodes and cap_faces faces; returns the counts. */
+shl_status shl_icosphere(uint32_t level, double* xyz, size_t cap_nodes, uint32_t* faces,
+                         size_t cap_faces, uint32_t* n_nodes, uint32_t* n_faces);
+/* The OFF text of shl_icosphere(level) into buf (NUL terminated); *len gets
+ * the length needed (call with buf = NULL to query). */
+shl_status shl_icosphere_off(uint32_t level, char* buf, size_t cap, size_t* len);
+/* Read an OFF file (triangles only). */
+shl_status shl_read_off(const char* path, double* xyz, size_t cap_nodes, uint32_t* faces,
+                        size_t cap_faces, uint32_t* n_nodes, uint32_t* n_faces);
+
+/* Seeded imperfection u_i = amplitude * g_i * x_i/|x_i|, g_i ~ N(0,1) from
+ * Philox-4x32-10 (key = seed, counter = node id) with a Box-Muller map. */
+shl_status shl_gaussian_normal_imperfection(const double* xyz, uint32_t n_nodes, double amplitude,
+                                            uint64_t seed, double* u_out);
+
+/* Default parameters (ShellSystem constructor and set_parameters defaults). */
+void shl_params_default(shl_params* p);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SHL_H_ */

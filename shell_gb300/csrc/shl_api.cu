@@ -1,0 +1,841 @@
+// shl_api.cu -- the C ABI of include/shl.h on top of the device kernels.
+//
+// One context = one shell on the current CUDA device, with its own stream.
+// shl_step() runs n Newmark steps without host synchronisation: the steps are
+// captured once into a CUDA graph of kGraphSteps steps that is replayed; the
+// per-step pressure comes from a device table, problems and energies are
+// accumulated in the device control block and read back once at the end.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/shl.h"
+#include "shl_geom.h"
+#include "shl_internal.cuh"
+#include "shl_setup.h"
+
+using namespace shl;
+
+namespace {
+
+thread_local std::string g_err;
+constexpr uint32_t kGraphSteps = 16;
+constexpr uint32_t kTableCap = 1u << 16;
+
+#define SHL_CUDA_TRY(expr)                                                 \
+  do {                                                                     \
+    cudaError_t e_ = (expr);                                               \
+    if (e_ != cudaSuccess) {                                               \
+      g_err = std::string(#expr) + ": " + cudaGetErrorString(e_);          \
+      return e_ == cudaErrorMemoryAllocation ? SHL_ERR_OOM : SHL_ERR_CUDA; \
+    }                                                                      \
+  } while (0)
+
+}  // namespace
+
+struct shl_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  shl_params P{};
+  Setup S;
+  DevBuf b{};
+  StepConst sc{};
+  uint32_t elem_blocks = 0;
+  std::vector<void*> allocs;
+  cudaGraphExec_t graph = nullptr;
+  cudaGraphExec_t graph1 = nullptr;
+  double* h_pin = nullptr;  // pinned staging buffer, 3V doubles x 3
+  double* d_fa = nullptr;   // device f and a of shl_eval_forces, 2 x 3V doubles
+  void* d_flush = nullptr;  // L2 eviction buffer of shl_time_kernel
+  size_t flush_bytes = 0;
+};
+
+namespace {
+
+template <class T>
+shl_status dev_alloc(shl_ctx* c, T** p, size_t n) {
+  void* q = nullptr;
+  const size_t bytes = std::max<size_t>(n, 1) * sizeof(T);
+  cudaError_t e = cudaMalloc(&q, bytes);
+  if (e != cudaSuccess) {
+    g_err = "cudaMalloc(" + std::to_string(bytes) + "): " + cudaGetErrorString(e);
+    return SHL_ERR_OOM;
+  }
+  cudaMemset(q, 0, bytes);
+  c->allocs.push_back(q);
+  *p = (T*)q;
+  return SHL_OK;
+}
+
+template <class T>
+shl_status upload(shl_ctx* c, T* dst, const T* src, size_t n) {
+  SHL_CUDA_TRY(cudaMemcpyAsync(dst, src, n * sizeof(T), cudaMemcpyHostToDevice, c->stream));
+  return SHL_OK;
+}
+
+shl_status ctl_get(shl_ctx* c, Ctl& h) {
+  SHL_CUDA_TRY(cudaMemcpyAsync(&h, c->b.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, c->stream));
+  SHL_CUDA_TRY(cudaStreamSynchronize(c->stream));
+  return SHL_OK;
+}
+
+shl_status ctl_put(shl_ctx* c, const Ctl& h) {
+  SHL_CUDA_TRY(cudaMemcpyAsync(c->b.ctl, &h, sizeof(Ctl), cudaMemcpyHostToDevice, c->stream));
+  SHL_CUDA_TRY(cudaStreamSynchronize(c->stream));
+  return SHL_OK;
+}
+
+shl_status check_launch(const char* where) {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    g_err = std::string(where) + ": " + cudaGetErrorString(e);
+    return SHL_ERR_CUDA;
+  }
+  return SHL_OK;
+}
+
+#define SHL_TRY(expr)             \
+  do {                            \
+    shl_status s_ = (expr);       \
+    if (s_ != SHL_OK) return s_;  \
+  } while (0)
+
+bool validate(const shl_params& p, std::string& err) {
+  if (!(p.shell_mass_density > 0)) { err = "shell_mass_density must be > 0"; return false; }
+  if (!(p.shell_young_modulus > 0) || !(p.shell_young_modulus2 > 0)) { err = "Young's moduli must be > 0"; return false; }
+  if (!(p.shell_shear_modulus > 0)) { err = "shell_shear_modulus must be > 0"; return false; }
+  if (!(p.shell_poisson_ratio >= 0 && p.shell_poisson_ratio < 1)) { err = "shell_poisson_ratio must be in [0,1)"; return false; }
+  if (!(p.thickness > 0)) { err = "thickness must be > 0"; return false; }
+  if (!(p.dt > 0) || !(p.newmark_beta > 0)) { err = "dt and newmark_beta must be > 0"; return false; }
+  if (p.damping_alpha < 0 || p.damping_beta < 0 || p.damping_gamma < 0) { err = "damping must be >= 0"; return false; }
+  if (p.pressure_base < SHL_CS_LOCAL || p.pressure_base > SHL_CS_SPHERICAL) { err = "bad pressure_base"; return false; }
+  if (p.pressure_dir < 0 || p.pressure_dir > 2) { err = "bad pressure_dir"; return false; }
+  if (p.shell_shell_contact == SHL_CONTACT_SMOOTH) { err = "smooth (limit-surface) contact is not supported"; return false; }
+  if (p.shell_shell_contact != SHL_CONTACT_LINEAR && p.shell_shell_contact != SHL_CONTACT_NONE) { err = "bad shell_shell_contact"; return false; }
+  if (p.shell_shell_contact == SHL_CONTACT_LINEAR) {
+    if (p.mu_s < 0 || p.mu_d < 0 || p.self_damping < 0 || p.self_friction_damping < 0) { err = "contact coefficients must be >= 0"; return false; }
+    if (!(p.cell_size_mult > 0) || p.cell_margin < 0 || !(p.neighbor_margin > 0)) { err = "bad linked-cell parameters"; return false; }
+    if (!(p.friction_stop_velocity > 0)) { err = "friction_stop_velocity must be > 0"; return false; }
+  }
+  if (p.precision != SHL_PREC_FP64 && p.precision != SHL_PREC_FP32) { err = "bad precision"; return false; }
+  if (p.precision == SHL_PREC_FP32) { err = "FP32 element forces are provided by the batched ensemble API"; return false; }
+  return true;
+}
+
+// Host estimate of the first rebuild's cell grid, for buffer capacities.
+void estimate_cells(const Setup& S, const shl_params& p, uint64_t& n_cells, uint64_t& entries) {
+  std::vector<double> sizes(S.F);
+  double bmin[3] = {SHL_DBL_MAX, SHL_DBL_MAX, SHL_DBL_MAX}, bmax[3] = {-SHL_DBL_MAX, -SHL_DBL_MAX, -SHL_DBL_MAX};
+  std::vector<double> fmin(3 * (size_t)S.F), fmax(3 * (size_t)S.F);
+  for (uint32_t f = 0; f < S.F; ++f) {
+    double lo[3] = {SHL_DBL_MAX, SHL_DBL_MAX, SHL_DBL_MAX}, hi[3] = {-SHL_DBL_MAX, -SHL_DBL_MAX, -SHL_DBL_MAX};
+    for (int k = 0; k < 3; ++k)
+      for (int c = 0; c < 3; ++c) {
+        const double x = S.X[3 * (size_t)S.tri[3 * f + k] + c];
+        lo[c] = std::min(lo[c], x);
+        hi[c] = std::max(hi[c], x);
+      }
+    double d = 0;
+    for (int c = 0; c < 3; ++c) {
+      d = std::max(d, hi[c] - lo[c]);
+      bmin[c] = std::min(bmin[c], lo[c]);
+      bmax[c] = std::max(bmax[c], hi[c]);
+      fmin[3 * f + c] = lo[c];
+      fmax[3 * f + c] = hi[c];
+    }
+    sizes[f] = d;
+  }
+  const double avg = shl_fixed_order_sum(sizes.data(), S.F) / S.F;
+  double cs = p.cell_size_mult * avg;
+  const double tol = p.cell_margin * cs;
+  cs += tol;
+  const double dm = p.thickness + tol;
+  n_cells = 1;
+  uint64_t ncd[3];
+  for (int c = 0; c < 3; ++c) {
+    ncd[c] = (uint64_t)((bmax[c] - bmin[c] + dm) / cs + 1);
+    n_cells *= ncd[c];
+  }
+  entries = 0;
+  for (uint32_t f = 0; f < S.F; ++f) {
+    uint64_t e = 1;
+    for (int c = 0; c < 3; ++c) {
+      const int lo = (int)((fmin[3 * f + c] - bmin[c]) / cs);
+      const int hi = (int)((fmax[3 * f + c] - bmin[c] + dm) / cs);
+      e *= (uint64_t)(hi - lo + 1);
+    }
+    entries += e;
+  }
+}
+
+void enqueue_step(shl_ctx* c) {
+  const DevBuf& b = c->b;
+  const StepConst& sc = c->sc;
+  cudaStream_t s = c->stream;
+  launch_predict(b, sc, 0, s);
+  if (sc.contact) launch_rebuild(b, sc, s);
+  launch_elements(b, sc, c->elem_blocks, s);
+  if (sc.contact) launch_contact_force(b, sc, 0, s);
+  launch_gather_correct(b, sc, 0, true, nullptr, nullptr, s);
+  if (sc.contact) launch_rebuild(b, sc, s);
+  launch_volume_end_step(b, sc, true, s);
+}
+
+shl_status build_graph(shl_ctx* c, uint32_t steps, cudaGraphExec_t* out) {
+  cudaGraph_t g = nullptr;
+  SHL_CUDA_TRY(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+  for (uint32_t i = 0; i < steps; ++i) enqueue_step(c);
+  SHL_CUDA_TRY(cudaStreamEndCapture(c->stream, &g));
+  cudaError_t e = cudaGraphInstantiate(out, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) {
+    g_err = std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e);
+    return SHL_ERR_CUDA;
+  }
+  return SHL_OK;
+}
+
+void fill_energies(const Ctl& h, shl_energies* e) {
+  if (!e) return;
+  e->Etens = h.Etens; e->Ebend = h.Ebend; e->Eself = h.Eself; e->Efric = h.Efric; e->Ekin = h.Ekin;
+  e->area = h.area; e->volume = h.volume; e->kGauss = h.kGauss; e->kMean = h.kMean;
+  e->Nc = h.Nc; e->n_pairs = h.n_pairs;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* shl_version(void) { return "shl_gb300 0.1 sm_103a"; }
+const char* shl_last_error(void) { return g_err.c_str(); }
+
+void shl_destroy(shl_ctx* c) {
+  if (!c) return;
+  if (c->graph) cudaGraphExecDestroy(c->graph);
+  if (c->graph1) cudaGraphExecDestroy(c->graph1);
+  for (void* p : c->allocs) cudaFree(p);
+  if (c->h_pin) cudaFreeHost(c->h_pin);
+  if (c->d_flush) cudaFree(c->d_flush);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+shl_status shl_create(const shl_mesh* mesh, const shl_params* params, shl_ctx** out) {
+  if (!mesh || !params || !out) { g_err = "null argument"; return SHL_ERR_ARG; }
+  *out = nullptr;
+  std::string err;
+  if (!validate(*params, err)) { g_err = err; return SHL_ERR_ARG; }
+  shl_ctx* c = new shl_ctx;
+  c->P = *params;
+  if (!build_setup(*mesh, *params, c->S, err)) {
+    g_err = err;
+    delete c;
+    return SHL_ERR_ARG;
+  }
+  shl_status st = SHL_OK;
+  auto fail = [&](shl_status s) { shl_destroy(c); return s; };
+  if (cudaGetDevice(&c->device) != cudaSuccess || cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    g_err = "no CUDA device";
+    return fail(SHL_ERR_CUDA);
+  }
+  const Setup& S = c->S;
+  const uint32_t V = S.V, F = S.F;
+  DevBuf& b = c->b;
+  const size_t nd = 3 * (size_t)V;
+#define ALLOC(ptr, n) do { if ((st = dev_alloc(c, &(ptr), (n))) != SHL_OK) return fail(st); } while (0)
+  ALLOC(b.X, nd); ALLOC(b.u, nd); ALLOC(b.v, nd); ALLOC(b.a, nd); ALLOC(b.up, nd); ALLOC(b.vp, nd);
+  ALLOC(b.p, nd); ALLOC(b.Minv, nd); ALLOC(b.C, nd);
+  ALLOC(b.face, (size_t)FF_COUNT * F);
+  ALLOC(b.patch, 12 * (size_t)F);
+  ALLOC(b.qe, 36 * (size_t)F);
+  ALLOC(b.gather_ptr, V + 1);
+  ALLOC(b.gather_ent, S.gather_ent.size());
+  ALLOC(b.tri, 3 * (size_t)F);
+  ALLOC(b.perm, F);
+  ALLOC(b.area, F); ALLOC(b.kG, F); ALLOC(b.kM, F); ALLOC(b.etens, F); ALLOC(b.ebend, F);
+  // element launch: one block range per patch group
+  std::vector<GroupDesc> gd;
+  std::vector<double> basis;
+  uint32_t blocks = 0;
+  for (const PatchGroup& g : S.groups) {
+    GroupDesc d;
+    d.first = g.first;
+    d.count = g.count;
+    d.block_start = blocks;
+    d.n_slots = g.n_slots;
+    d.basis_off = (int32_t)basis.size();
+    basis.insert(basis.end(), g.basis.begin(), g.basis.end());
+    blocks += (g.count + kBlock - 1) / kBlock;
+    gd.push_back(d);
+  }
+  if ((int)gd.size() > kMaxGroups) { g_err = "too many patch valences"; return fail(SHL_ERR_ARG); }
+  if (blocks == 0) blocks = 1;
+  c->elem_blocks = blocks;
+  const uint32_t max_blocks = std::max({blocks, (F + kBlock - 1) / kBlock, (V + kBlock - 1) / kBlock, 4u * 152u}) + 8;
+  ALLOC(b.partial, 8 * (size_t)max_blocks);
+  ALLOC(c->d_fa, 2 * nd);
+  ALLOC(b.ctl, 1);
+  ALLOC(b.ptable, kTableCap);
+  b.ptable_cap = kTableCap;
+
+  // contact buffers
+  const bool contact = params->shell_shell_contact == SHL_CONTACT_LINEAR;
+  uint64_t n_cells0 = 0, entries0 = 0;
+  uint32_t n_cells_cap = 1, entries_cap = 1, pairs_cap = 1, csr_cap = 1;
+  if (contact) {
+    estimate_cells(S, *params, n_cells0, entries0);
+    const uint64_t want_cells = std::min<uint64_t>(S.n_cells_max, 1ull << 28);
+    n_cells_cap = (uint32_t)std::max<uint64_t>(std::min<uint64_t>(want_cells, std::max<uint64_t>(8 * n_cells0, 1u << 20)), 1);
+    if (n_cells_cap < n_cells0) n_cells_cap = (uint32_t)std::min<uint64_t>(n_cells0, 1ull << 28);
+    entries_cap = (uint32_t)std::min<uint64_t>(std::max<uint64_t>(8 * entries0, 1u << 20), 1ull << 30);
+    pairs_cap = std::max<uint32_t>(16 * F, 1u << 16);
+    csr_cap = 6 * pairs_cap;
+    ALLOC(b.close_ptr, F + 1);
+    ALLOC(b.close_list, S.close_list.size());
+    ALLOC(b.bmin, 3 * (size_t)F); ALLOC(b.bmax, 3 * (size_t)F); ALLOC(b.fsize, F);
+    ALLOC(b.cell_lo, 3 * (size_t)F); ALLOC(b.cell_hi, 3 * (size_t)F);
+    ALLOC(b.cell_count, n_cells_cap); ALLOC(b.cell_start, n_cells_cap + 1); ALLOC(b.cell_fill, n_cells_cap);
+    ALLOC(b.cell_items, entries_cap);
+    const size_t scan_cap = std::max<size_t>({(size_t)n_cells_cap, (size_t)F + 1, (size_t)V + 1});
+    ALLOC(b.scan_block, scan_cap / kScanTile + 2);
+    for (int k = 0; k < 2; ++k) {
+      ALLOC(b.pe1[k], pairs_cap); ALLOC(b.pe2[k], pairs_cap); ALLOC(b.pstick[k], pairs_cap);
+      ALLOC(b.pd2[k], pairs_cap); ALLOC(b.porig[k], 3 * (size_t)pairs_cap); ALLOC(b.pair_ptr[k], F + 1);
+    }
+    ALLOC(b.pkeep, pairs_cap);
+    ALLOC(b.new_e1, pairs_cap); ALLOC(b.new_e2, pairs_cap); ALLOC(b.new_d2, pairs_cap);
+    ALLOC(b.new_off, F); ALLOC(b.new_cnt, F);
+    ALLOC(b.seg_count, F);
+    ALLOC(b.pforce, 7 * (size_t)pairs_cap);
+    ALLOC(b.csr_count, V); ALLOC(b.csr_ptr, V + 1); ALLOC(b.csr_ent, csr_cap); ALLOC(b.csr_fill, V);
+  }
+#undef ALLOC
+
+  // uploads
+  if ((st = upload(c, b.X, S.X.data(), nd)) != SHL_OK) return fail(st);
+  if ((st = upload(c, b.p, S.X.data(), nd)) != SHL_OK) return fail(st);
+  if ((st = upload(c, b.Minv, S.Minv.data(), nd)) != SHL_OK) return fail(st);
+  if ((st = upload(c, b.C, S.C.data(), nd)) != SHL_OK) return fail(st);
+  if ((st = upload(c, b.face, S.face.data(), S.face.size())) != SHL_OK) return fail(st);
+  if ((st = upload(c, b.patch, S.patch.data(), S.patch.size())) != SHL_OK) return fail(st);
+  if ((st = upload(c, b.gather_ptr, S.gather_ptr.data(), S.gather_ptr.size())) != SHL_OK) return fail(st);
+  if ((st = upload(c, b.gather_ent, S.gather_ent.data(), S.gather_ent.size())) != SHL_OK) return fail(st);
+  if ((st = upload(c, b.tri, S.tri.data(), S.tri.size())) != SHL_OK) return fail(st);
+  if ((st = upload(c, b.perm, S.perm.data(), S.perm.size())) != SHL_OK) return fail(st);
+  if (contact) {
+    if ((st = upload(c, b.close_ptr, S.close_ptr.data(), S.close_ptr.size())) != SHL_OK) return fail(st);
+    if (!S.close_list.empty() && (st = upload(c, b.close_list, S.close_list.data(), S.close_list.size())) != SHL_OK)
+      return fail(st);
+  }
+  upload_groups(gd.data(), (int)gd.size(), basis.data(), (int)basis.size());
+
+  // step constants
+  StepConst& sc = c->sc;
+  const shl_params& p = *params;
+  sc.dt = p.dt;
+  sc.nm0 = p.newmark_beta * p.dt * p.dt;
+  sc.nm6 = (1 - p.newmark_gamma) * p.dt;
+  sc.nm7 = p.newmark_gamma * p.dt;
+  sc.nm8 = p.dt * p.dt * (0.5 - p.newmark_beta);
+  sc.thickness = p.thickness;
+  sc.K = S.K;
+  sc.D = S.D;
+  sc.qw = 0.5;
+  sc.stiff_density = S.stiff_density;
+  sc.stiff_static_friction = S.stiff_static_friction;
+  sc.d2_friction = S.d2_friction;
+  sc.mu_s = p.mu_s;
+  sc.mu_d = p.mu_d;
+  sc.self_damping = p.self_damping;
+  sc.self_friction_damping = p.self_friction_damping;
+  sc.v_stop = p.friction_stop_velocity;
+  sc.cell_size_mult = p.cell_size_mult;
+  sc.cell_margin = p.cell_margin;
+  sc.bulk_modulus = p.bulk_modulus;
+  sc.pressure_default = p.pressure;
+  sc.pressure_table = b.ptable;
+  sc.n_cells_max = S.n_cells_max;
+  sc.n_cells_cap = n_cells_cap;
+  sc.entries_cap = entries_cap;
+  sc.pairs_cap = pairs_cap;
+  sc.csr_cap = csr_cap;
+  sc.contact = contact ? 1 : 0;
+  sc.friction = (contact && (p.mu_s != 0 || p.mu_d != 0)) ? 1 : 0;
+  sc.pressure_base = p.pressure_base;
+  sc.pressure_dir = p.pressure_dir;
+  sc.compat_zero_pressure = p.compat_zero_pressure;
+  sc.stop_on_problem = p.stop_on_problem;
+  sc.V = V;
+  sc.F = F;
+
+  Ctl h;
+  std::memset(&h, 0, sizeof(h));
+  if ((st = ctl_put(c, h)) != SHL_OK) return fail(st);
+  if (cudaMallocHost(&c->h_pin, 3 * nd * sizeof(double)) != cudaSuccess) c->h_pin = nullptr;
+  if ((st = check_launch("shl_create")) != SHL_OK) return fail(st);
+  SHL_CUDA_TRY(cudaStreamSynchronize(c->stream));
+  *out = c;
+  return SHL_OK;
+}
+
+shl_status shl_set_state(shl_ctx* c, const double* u, const double* v, const double* a) {
+  if (!c) return SHL_ERR_ARG;
+  const size_t nd = 3 * (size_t)c->S.V;
+  if (u) {
+    SHL_TRY(upload(c, c->b.u, u, nd));
+    SHL_TRY(upload(c, c->b.up, u, nd));
+    launch_positions(c->b, c->sc, c->stream);
+  }
+  if (v) SHL_TRY(upload(c, c->b.v, v, nd));
+  if (a) SHL_TRY(upload(c, c->b.a, a, nd));
+  SHL_CUDA_TRY(cudaStreamSynchronize(c->stream));
+  return check_launch("shl_set_state");
+}
+
+shl_status shl_get_state(shl_ctx* c, double* u, double* v, double* a) {
+  if (!c) return SHL_ERR_ARG;
+  const size_t bytes = 3 * (size_t)c->S.V * sizeof(double);
+  if (u) SHL_CUDA_TRY(cudaMemcpyAsync(u, c->b.u, bytes, cudaMemcpyDeviceToHost, c->stream));
+  if (v) SHL_CUDA_TRY(cudaMemcpyAsync(v, c->b.v, bytes, cudaMemcpyDeviceToHost, c->stream));
+  if (a) SHL_CUDA_TRY(cudaMemcpyAsync(a, c->b.a, bytes, cudaMemcpyDeviceToHost, c->stream));
+  SHL_CUDA_TRY(cudaStreamSynchronize(c->stream));
+  return SHL_OK;
+}
+
+shl_status shl_set_time(shl_ctx* c, double t, uint32_t step) {
+  if (!c) return SHL_ERR_ARG;
+  Ctl h;
+  SHL_TRY(ctl_get(c, h));
+  h.time = t;
+  h.time_step = step;
+  return ctl_put(c, h);
+}
+
+shl_status shl_get_time(shl_ctx* c, double* t, uint32_t* step) {
+  if (!c) return SHL_ERR_ARG;
+  Ctl h;
+  SHL_TRY(ctl_get(c, h));
+  if (t) *t = h.time;
+  if (step) *step = h.time_step;
+  return SHL_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+// scalar part of a force evaluation (pressure, volume pressure, problem reset)
+shl_status begin_eval(shl_ctx* c, double pressure, bool allow_rebuild) {
+  Ctl h;
+  SHL_TRY(ctl_get(c, h));
+  h.problem = 0;
+  h.halted = 0;
+  h.error = 0;
+  h.pressure = c->P.compat_zero_pressure ? pressure * 0.0 : pressure;
+  const double red = std::max((1.0 - static_cast<int>(h.time * 5.0) * 0.01), 0.5);
+  if (h.time_step == 2) h.volume0 = h.volume;
+  h.volume_pressure = (c->P.bulk_modulus == 0 ? 0 : c->P.bulk_modulus * (h.volume0 * red / h.volume - 1));
+  if (allow_rebuild && c->sc.contact) {
+    const double tol = c->P.cell_margin * (c->P.cell_size_mult * h.avg_elem_size);
+    h.rebuild = h.du_sum >= tol ? 1u : 0u;
+  } else {
+    h.rebuild = 0;
+  }
+  return ctl_put(c, h);
+}
+
+shl_status eval_into(shl_ctx* c, double* d_f, double* d_a) {
+  const DevBuf& b = c->b;
+  if (c->sc.contact) launch_rebuild(b, c->sc, c->stream);
+  launch_elements(b, c->sc, c->elem_blocks, c->stream);
+  if (c->sc.contact) launch_contact_force(b, c->sc, 0, c->stream);
+  launch_gather_correct(b, c->sc, 0, false, d_f, d_a, c->stream);
+  return check_launch("force evaluation");
+}
+
+shl_status finish_status(shl_ctx* c, Ctl& h) {
+  SHL_TRY(ctl_get(c, h));
+  if (h.error) {
+    g_err = "device buffer capacity exceeded (contact pairs / linked cells)";
+    return (shl_status)h.error;
+  }
+  return (shl_status)h.problem;
+}
+
+}  // namespace
+
+extern "C" {
+
+shl_status shl_eval_forces(shl_ctx* c, const double* u_pred, const double* v_pred, double pressure, double* f_out,
+                           double* a_out, shl_energies* e) {
+  if (!c || !u_pred || !v_pred) return SHL_ERR_ARG;
+  const size_t nd = 3 * (size_t)c->S.V;
+  SHL_TRY(upload(c, c->b.up, u_pred, nd));
+  SHL_TRY(upload(c, c->b.vp, v_pred, nd));
+  launch_positions(c->b, c->sc, c->stream);
+  SHL_TRY(begin_eval(c, pressure, true));
+  double* d_f = c->d_fa;
+  double* d_a = c->d_fa + nd;
+  SHL_TRY(eval_into(c, d_f, d_a));
+  if (f_out) SHL_CUDA_TRY(cudaMemcpyAsync(f_out, d_f, nd * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  if (a_out) SHL_CUDA_TRY(cudaMemcpyAsync(a_out, d_a, nd * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  Ctl h;
+  const shl_status s = finish_status(c, h);
+  fill_energies(h, e);
+  return s;
+}
+
+shl_status shl_apply_initial_conditions(shl_ctx* c, const double* u0, double t0, double pressure_next) {
+  if (!c || !u0) return SHL_ERR_ARG;
+  const size_t nd = 3 * (size_t)c->S.V;
+  SHL_TRY(upload(c, c->b.u, u0, nd));
+  SHL_TRY(upload(c, c->b.up, u0, nd));
+  SHL_CUDA_TRY(cudaMemsetAsync(c->b.v, 0, nd * sizeof(double), c->stream));
+  SHL_CUDA_TRY(cudaMemsetAsync(c->b.vp, 0, nd * sizeof(double), c->stream));
+  SHL_CUDA_TRY(cudaMemsetAsync(c->b.a, 0, nd * sizeof(double), c->stream));
+  launch_positions(c->b, c->sc, c->stream);
+  Ctl h;
+  SHL_TRY(ctl_get(c, h));
+  const uint32_t step0 = h.time_step;
+  h.time = t0;
+  h.problem = 0;
+  h.halted = 0;
+  h.error = 0;
+  h.pressure = 0;
+  h.volume_pressure = 0;
+  h.rebuild = c->sc.contact ? 1u : 0u;  // compute_shell_shell_contact_candidates(true)
+  SHL_TRY(ctl_put(c, h));
+  // bounding boxes + first candidate list, then deformed metrics and volume
+  if (c->sc.contact) launch_rebuild(c->b, c->sc, c->stream);
+  launch_elements(c->b, c->sc, c->elem_blocks, c->stream);
+  launch_volume_end_step(c->b, c->sc, false, c->stream);
+  SHL_TRY(check_launch("initial conditions"));
+  SHL_TRY(ctl_get(c, h));
+  h.volume0 = h.volume;
+  // one force evaluation at t0 + dt (ShellSystem.C:892-904)
+  h.time = t0 + c->P.dt;
+  h.time_step = step0 + 1;
+  SHL_TRY(ctl_put(c, h));
+  SHL_TRY(begin_eval(c, pressure_next, false));
+  SHL_TRY(eval_into(c, nullptr, c->b.a));
+  Ctl h2;
+  const shl_status s = finish_status(c, h2);
+  h2.time = t0;
+  h2.time_step = step0;
+  SHL_TRY(ctl_put(c, h2));
+  return s;
+}
+
+namespace {
+
+shl_status reset_report(shl_ctx* c) {
+  Ctl h;
+  SHL_TRY(ctl_get(c, h));
+  h.steps_done = 0;
+  h.worst_problem = 0;
+  h.first_problem_step = 0;
+  h.halted = 0;
+  h.error = 0;
+  h.problem = 0;
+  h.n_rebuilds = 0;
+  h.sum_dt = h.sum_area = h.sum_volume = h.sum_Nc = h.sum_Ekin = h.sum_Etens = h.sum_Ebend = h.sum_Eself =
+      h.sum_Efric = h.sum_kGauss = h.sum_kMean = 0;
+  return ctl_put(c, h);
+}
+
+shl_status ensure_graphs(shl_ctx* c) {
+  if (c->graph) return SHL_OK;
+  SHL_TRY(build_graph(c, kGraphSteps, &c->graph));
+  return build_graph(c, 1, &c->graph1);
+}
+
+shl_status enqueue_steps(shl_ctx* c, uint32_t n, bool use_graph) {
+  if (use_graph) {
+    SHL_TRY(ensure_graphs(c));
+    uint32_t k = 0;
+    for (; k + kGraphSteps <= n; k += kGraphSteps) SHL_CUDA_TRY(cudaGraphLaunch(c->graph, c->stream));
+    for (; k < n; ++k) SHL_CUDA_TRY(cudaGraphLaunch(c->graph1, c->stream));
+  } else {
+    for (uint32_t k = 0; k < n; ++k) enqueue_step(c);
+  }
+  return check_launch("step");
+}
+
+shl_status upload_table(shl_ctx* c, const double* table, uint32_t n) {
+  if (n > c->b.ptable_cap) { g_err = "pressure table longer than the device table"; return SHL_ERR_CAPACITY; }
+  if (n) SHL_TRY(upload(c, c->b.ptable, table, n));
+  const uint32_t hdr[2] = {0u, n};
+  static_assert(offsetof(Ctl, table_len) == offsetof(Ctl, table_pos) + 4, "layout");
+  SHL_CUDA_TRY(cudaMemcpyAsync((char*)c->b.ctl + offsetof(Ctl, table_pos), hdr, sizeof(hdr), cudaMemcpyHostToDevice,
+                               c->stream));
+  SHL_CUDA_TRY(cudaStreamSynchronize(c->stream));
+  return SHL_OK;
+}
+
+shl_status collect(shl_ctx* c, shl_step_report* report) {
+  Ctl h;
+  SHL_TRY(ctl_get(c, h));
+  if (report) {
+    std::memset(report, 0, sizeof(*report));
+    report->steps_done = h.steps_done;
+    report->worst_problem = h.worst_problem;
+    report->time = h.time;
+    report->du_sum = h.du_sum;
+    report->n_rebuilds = h.n_rebuilds;
+    fill_energies(h, &report->last);
+    report->sum_dt = h.sum_dt; report->sum_area = h.sum_area; report->sum_volume = h.sum_volume;
+    report->sum_Nc = h.sum_Nc; report->sum_Ekin = h.sum_Ekin; report->sum_Etens = h.sum_Etens;
+    report->sum_Ebend = h.sum_Ebend; report->sum_Eself = h.sum_Eself; report->sum_Efric = h.sum_Efric;
+    report->sum_kGauss = h.sum_kGauss; report->sum_kMean = h.sum_kMean;
+  }
+  const int err = h.error;
+  const int worst = h.worst_problem;
+  SHL_TRY(reset_report(c));
+  if (err) {
+    g_err = "device buffer capacity exceeded (contact pairs / linked cells)";
+    return (shl_status)err;
+  }
+  return (shl_status)worst;
+}
+
+}  // namespace
+
+shl_status shl_step(shl_ctx* c, uint32_t n_steps, const double* pressure_table, int use_graph,
+                    shl_step_report* report) {
+  if (!c) return SHL_ERR_ARG;
+  SHL_TRY(reset_report(c));
+  std::vector<double> chunk;
+  uint32_t done = 0;
+  while (done < n_steps) {
+    const uint32_t m = std::min<uint32_t>(n_steps - done, c->b.ptable_cap);
+    chunk.resize(m);
+    for (uint32_t i = 0; i < m; ++i) chunk[i] = pressure_table ? pressure_table[done + i] : c->P.pressure;
+    SHL_TRY(upload_table(c, chunk.data(), m));
+    SHL_TRY(enqueue_steps(c, m, use_graph != 0));
+    SHL_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    done += m;
+    if (done < n_steps) {
+      Ctl hh;
+      SHL_TRY(ctl_get(c, hh));
+      if (hh.halted) break;
+    }
+  }
+  return collect(c, report);
+}
+
+shl_status shl_get_stream(shl_ctx* c, void** stream) {
+  if (!c || !stream) return SHL_ERR_ARG;
+  *stream = (void*)c->stream;
+  return SHL_OK;
+}
+
+shl_status shl_upload_pressure_table(shl_ctx* c, const double* table, uint32_t n) {
+  if (!c || (n && !table)) return SHL_ERR_ARG;
+  return upload_table(c, table, n);
+}
+
+shl_status shl_step_enqueue(shl_ctx* c, uint32_t n_steps) {
+  if (!c) return SHL_ERR_ARG;
+  return enqueue_steps(c, n_steps, true);
+}
+
+shl_status shl_step_collect(shl_ctx* c, shl_step_report* report) {
+  if (!c) return SHL_ERR_ARG;
+  return collect(c, report);
+}
+
+shl_status shl_time_kernel(shl_ctx* c, int which, int reps, size_t flush_bytes, double* avg_ms) {
+  if (!c || !avg_ms || reps <= 0 || (which != 0 && which != 1)) return SHL_ERR_ARG;
+  if (flush_bytes > c->flush_bytes) {
+    if (c->d_flush) cudaFree(c->d_flush);
+    c->d_flush = nullptr;
+    c->flush_bytes = 0;
+    SHL_CUDA_TRY(cudaMalloc(&c->d_flush, flush_bytes));
+    c->flush_bytes = flush_bytes;
+  }
+  Ctl h;
+  SHL_TRY(ctl_get(c, h));
+  const int32_t halted = h.halted;
+  h.halted = 0;
+  SHL_TRY(ctl_put(c, h));
+  cudaEvent_t e0, e1;
+  SHL_CUDA_TRY(cudaEventCreate(&e0));
+  SHL_CUDA_TRY(cudaEventCreate(&e1));
+  double total = 0.0;
+  const size_t nd = 3 * (size_t)c->S.V;
+  for (int r = 0; r < reps; ++r) {
+    if (flush_bytes) launch_flush(c->d_flush, flush_bytes, (uint32_t)r, c->stream);
+    cudaEventRecord(e0, c->stream);
+    if (which == 0)
+      launch_elements(c->b, c->sc, c->elem_blocks, c->stream);
+    else
+      launch_gather_correct(c->b, c->sc, 0, false, c->d_fa, c->d_fa + nd, c->stream);
+    cudaEventRecord(e1, c->stream);
+    SHL_CUDA_TRY(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    total += ms;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  SHL_TRY(check_launch("shl_time_kernel"));
+  SHL_TRY(ctl_get(c, h));
+  h.halted = halted;
+  SHL_TRY(ctl_put(c, h));
+  *avg_ms = total / reps;
+  return SHL_OK;
+}
+
+shl_status shl_measure_fp64_peak(double* tflops) {
+  if (!tflops) return SHL_ERR_ARG;
+  int dev = 0, sms = 0;
+  SHL_CUDA_TRY(cudaGetDevice(&dev));
+  SHL_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  cudaStream_t s;
+  SHL_CUDA_TRY(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+  double* out = nullptr;
+  SHL_CUDA_TRY(cudaMalloc(&out, 8 * 64 * 1024));
+  const int blocks = 8 * sms, iters = 1 << 14;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  launch_fp64_peak(out, blocks, iters, s);  // warm-up
+  float best = 1e30f;
+  for (int r = 0; r < 5; ++r) {
+    cudaEventRecord(e0, s);
+    launch_fp64_peak(out, blocks, iters, s);
+    cudaEventRecord(e1, s);
+    cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    best = std::min(best, ms);
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(out);
+  cudaStreamDestroy(s);
+  SHL_TRY(check_launch("shl_measure_fp64_peak"));
+  const double flops = 2.0 * 8.0 * iters * (double)blocks * 256.0;
+  *tflops = flops / (best * 1e-3) / 1e12;
+  return SHL_OK;
+}
+
+shl_status shl_get_contact_state(shl_ctx* c, uint32_t* pairs, uint8_t* stick, double* spring_origin, double* d2,
+                                 size_t cap, size_t* n_pairs, double* du_sum) {
+  if (!c) return SHL_ERR_ARG;
+  Ctl h;
+  SHL_TRY(ctl_get(c, h));
+  if (n_pairs) *n_pairs = h.n_pairs;
+  if (du_sum) *du_sum = h.du_sum;
+  if (!c->sc.contact || h.n_pairs == 0) return SHL_OK;
+  const size_t n = std::min<size_t>(cap, h.n_pairs);
+  if (pairs && n) {
+    std::vector<uint32_t> e1(n), e2(n);
+    SHL_CUDA_TRY(cudaMemcpyAsync(e1.data(), c->b.pe1[0], n * 4, cudaMemcpyDeviceToHost, c->stream));
+    SHL_CUDA_TRY(cudaMemcpyAsync(e2.data(), c->b.pe2[0], n * 4, cudaMemcpyDeviceToHost, c->stream));
+    SHL_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    for (size_t i = 0; i < n; ++i) { pairs[2 * i] = e1[i]; pairs[2 * i + 1] = e2[i]; }
+  }
+  if (stick && n) SHL_CUDA_TRY(cudaMemcpyAsync(stick, c->b.pstick[0], n, cudaMemcpyDeviceToHost, c->stream));
+  if (spring_origin && n)
+    SHL_CUDA_TRY(cudaMemcpyAsync(spring_origin, c->b.porig[0], 3 * n * 8, cudaMemcpyDeviceToHost, c->stream));
+  if (d2 && n) SHL_CUDA_TRY(cudaMemcpyAsync(d2, c->b.pd2[0], n * 8, cudaMemcpyDeviceToHost, c->stream));
+  SHL_CUDA_TRY(cudaStreamSynchronize(c->stream));
+  return SHL_OK;
+}
+
+shl_status shl_get_contact_pairs(shl_ctx* c, uint32_t* pairs, size_t cap, size_t* n_pairs) {
+  return shl_get_contact_state(c, pairs, nullptr, nullptr, nullptr, cap, n_pairs, nullptr);
+}
+
+shl_status shl_set_contact_state(shl_ctx* c, const uint32_t* pairs, const uint8_t* stick, const double* spring_origin,
+                                 const double* d2, size_t n, double du_sum) {
+  if (!c) return SHL_ERR_ARG;
+  if (!c->sc.contact) { g_err = "self-contact is off"; return SHL_ERR_ARG; }
+  if (n > c->sc.pairs_cap) { g_err = "too many pairs"; return SHL_ERR_CAPACITY; }
+  const uint32_t F = c->S.F;
+  std::vector<size_t> order(n);
+  for (size_t i = 0; i < n; ++i) {
+    order[i] = i;
+    if (pairs[2 * i] >= F || pairs[2 * i + 1] >= F || pairs[2 * i] >= pairs[2 * i + 1]) {
+      g_err = "pairs must satisfy eid1 < eid2 < n_faces";
+      return SHL_ERR_ARG;
+    }
+  }
+  std::sort(order.begin(), order.end(), [&](size_t x, size_t y) {
+    return pairs[2 * x] != pairs[2 * y] ? pairs[2 * x] < pairs[2 * y] : pairs[2 * x + 1] < pairs[2 * y + 1];
+  });
+  std::vector<uint32_t> e1(n), e2(n), ptr(F + 1, 0);
+  std::vector<uint8_t> st(n);
+  std::vector<double> org(3 * n), dd(n);
+  for (size_t k = 0; k < n; ++k) {
+    const size_t i = order[k];
+    e1[k] = pairs[2 * i];
+    e2[k] = pairs[2 * i + 1];
+    if (k > 0 && e1[k] == e1[k - 1] && e2[k] == e2[k - 1]) { g_err = "duplicate pair"; return SHL_ERR_ARG; }
+    st[k] = stick ? (stick[i] ? 1 : 0) : 0;
+    for (int q = 0; q < 3; ++q) org[3 * k + q] = spring_origin ? spring_origin[3 * i + q] : 0.0;
+    dd[k] = d2 ? d2[i] : 0.0;
+    ++ptr[e1[k] + 1];
+  }
+  for (uint32_t f = 0; f < F; ++f) ptr[f + 1] += ptr[f];
+  if (n) {
+    SHL_TRY(upload(c, c->b.pe1[0], e1.data(), n));
+    SHL_TRY(upload(c, c->b.pe2[0], e2.data(), n));
+    SHL_TRY(upload(c, c->b.pstick[0], st.data(), n));
+    SHL_TRY(upload(c, c->b.porig[0], org.data(), 3 * n));
+    SHL_TRY(upload(c, c->b.pd2[0], dd.data(), n));
+  }
+  SHL_TRY(upload(c, c->b.pair_ptr[0], ptr.data(), F + 1));
+  Ctl h;
+  SHL_TRY(ctl_get(c, h));
+  h.n_pairs = (uint32_t)n;
+  h.du_sum = du_sum;
+  h.csr_dirty = 1;
+  SHL_TRY(ctl_put(c, h));
+  launch_contact_csr(c->b, c->sc, c->stream);
+  SHL_TRY(check_launch("shl_set_contact_state"));
+  SHL_CUDA_TRY(cudaStreamSynchronize(c->stream));
+  return SHL_OK;
+}
+
+shl_status shl_rebuild_contacts(shl_ctx* c) {
+  if (!c) return SHL_ERR_ARG;
+  if (!c->sc.contact) return SHL_OK;
+  Ctl h;
+  SHL_TRY(ctl_get(c, h));
+  h.rebuild = 1;
+  h.problem = 0;
+  h.halted = 0;
+  h.error = 0;
+  SHL_TRY(ctl_put(c, h));
+  launch_rebuild(c->b, c->sc, c->stream);
+  SHL_TRY(check_launch("shl_rebuild_contacts"));
+  return finish_status(c, h);
+}
+
+shl_status shl_get_element_fields(shl_ctx* c, double* kG, double* kM, double* et, double* eb, double* area) {
+  if (!c) return SHL_ERR_ARG;
+  const size_t bytes = (size_t)c->S.F * sizeof(double);
+  if (kG) SHL_CUDA_TRY(cudaMemcpyAsync(kG, c->b.kG, bytes, cudaMemcpyDeviceToHost, c->stream));
+  if (kM) SHL_CUDA_TRY(cudaMemcpyAsync(kM, c->b.kM, bytes, cudaMemcpyDeviceToHost, c->stream));
+  if (et) SHL_CUDA_TRY(cudaMemcpyAsync(et, c->b.etens, bytes, cudaMemcpyDeviceToHost, c->stream));
+  if (eb) SHL_CUDA_TRY(cudaMemcpyAsync(eb, c->b.ebend, bytes, cudaMemcpyDeviceToHost, c->stream));
+  if (area) SHL_CUDA_TRY(cudaMemcpyAsync(area, c->b.area, bytes, cudaMemcpyDeviceToHost, c->stream));
+  SHL_CUDA_TRY(cudaStreamSynchronize(c->stream));
+  return SHL_OK;
+}
+
+shl_status shl_get_mass_damping(shl_ctx* c, double* Minv, double* C) {
+  if (!c) return SHL_ERR_ARG;
+  const size_t nd = 3 * (size_t)c->S.V;
+  if (Minv) std::memcpy(Minv, c->S.Minv.data(), nd * sizeof(double));
+  if (C) std::memcpy(C, c->S.C.data(), nd * sizeof(double));
+  return SHL_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,632 @@
+// shl_contact.cu -- linked-cell self-contact candidate list on the device.
+//
+// compute_shell_shell_contact_candidates (ShellSystem.C:1910-2135) with
+// compute_bounding_box (2544-2587), as a pipeline of kernels that all return
+// immediately unless the device flag ctl->rebuild is set (so the pipeline can
+// be captured into a CUDA graph and skipped on device):
+//
+//   k_rb_aabb      per-face AABBs, shell bounds, avg_elem_size (fixed-order
+//                  sum), cell size, d_max, cell counts; TOO_MANY_CELLS check
+//   k_rb_clear     clear the cell histogram and the per-face counters
+//   k_rb_count     cell ranges per face, cell histogram (counting sort, pass 1);
+//                  keep flags of the old list (ShellSystem.C:2016-2027)
+//   scan           cell_count -> cell_start
+//   k_rb_fill      scatter faces into their cells (counting sort, pass 2)
+//   k_rb_pairs     per face e1: faces e2 > e1 sharing a cell, emitted from the
+//                  lowest shared cell only, not topologically close, not in the
+//                  kept list, not AABB-apart by d_max, with d2 <= d2_max
+//   scan           per-face pair counts -> segment offsets
+//   k_rb_assemble  kept old pairs + new pairs of each face, merged in e2 order
+//   k_rb_copyback  scratch list -> list
+//
+// The resulting list equals, as a set, the reference's list at the same state
+// (the reference's cell-membership test is reproduced with the same rounded
+// operations); it is stored sorted by (eid1, eid2), which fixes the order the
+// per-node gather adds contact forces in.  The reference's slot order depends
+// on OpenMP scheduling and is not reproduced.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "shl_geom.h"
+#include "shl_internal.cuh"
+
+namespace shl {
+
+namespace {
+
+__device__ __forceinline__ bool rb_off(const Ctl* ctl) { return ctl->rebuild == 0 || ctl->halted != 0; }
+
+__device__ __forceinline__ bool last_block_rb(uint32_t* counter) {
+  __shared__ bool is_last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const uint32_t t = atomicAdd(counter, 1u);
+    is_last = (t == gridDim.x - 1);
+    if (is_last) *counter = 0;
+  }
+  __syncthreads();
+  return is_last;
+}
+
+__device__ __forceinline__ void set_error(Ctl* ctl, int code) {
+  atomicMax(&ctl->error, code);
+  ctl->rebuild = 0;
+}
+
+// ------------------------------------------------------------------ AABB --
+__global__ void __launch_bounds__(kBlock) k_rb_aabb(DevBuf b, StepConst sc) {
+  Ctl* ctl = b.ctl;
+  if (rb_off(ctl)) return;
+  __shared__ double sh_min[3][kBlock], sh_max[3][kBlock];
+  __shared__ double lanes[SHL_SUM_LANES];
+  const uint32_t f = blockIdx.x * blockDim.x + threadIdx.x;
+  double lo[3] = {SHL_DBL_MAX, SHL_DBL_MAX, SHL_DBL_MAX}, hi[3] = {-SHL_DBL_MAX, -SHL_DBL_MAX, -SHL_DBL_MAX};
+  if (f < sc.F) {
+    for (int k = 0; k < 3; ++k) {
+      const double* q = b.p + 3 * (size_t)b.tri[3 * (size_t)f + k];
+      for (int c = 0; c < 3; ++c) {
+        if (q[c] < lo[c]) lo[c] = q[c];
+        if (q[c] > hi[c]) hi[c] = q[c];
+      }
+    }
+    for (int c = 0; c < 3; ++c) {
+      b.bmin[3 * (size_t)f + c] = lo[c];
+      b.bmax[3 * (size_t)f + c] = hi[c];
+    }
+    // BoundingBox::max_size
+    double dmax = __dsub_rn(hi[0], lo[0]);
+    const double d1 = __dsub_rn(hi[1], lo[1]), d2 = __dsub_rn(hi[2], lo[2]);
+    if (d1 > dmax) dmax = d1;
+    if (d2 > dmax) dmax = d2;
+    b.fsize[f] = dmax;
+  }
+  for (int c = 0; c < 3; ++c) {
+    sh_min[c][threadIdx.x] = lo[c];
+    sh_max[c][threadIdx.x] = hi[c];
+  }
+  __syncthreads();
+  for (int st = blockDim.x / 2; st > 0; st >>= 1) {
+    if ((int)threadIdx.x < st)
+      for (int c = 0; c < 3; ++c) {
+        sh_min[c][threadIdx.x] = fmin(sh_min[c][threadIdx.x], sh_min[c][threadIdx.x + st]);
+        sh_max[c][threadIdx.x] = fmax(sh_max[c][threadIdx.x], sh_max[c][threadIdx.x + st]);
+      }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0)
+    for (int c = 0; c < 3; ++c) {
+      b.partial[(size_t)blockIdx.x * 8 + c] = sh_min[c][0];
+      b.partial[(size_t)blockIdx.x * 8 + 3 + c] = sh_max[c][0];
+    }
+  if (!last_block_rb(&ctl->cnt[5])) return;
+  // shell bounds (exact min/max)
+  for (int c = 0; c < 3; ++c) {
+    double mn = SHL_DBL_MAX, mx = -SHL_DBL_MAX;
+    for (uint32_t k = threadIdx.x; k < gridDim.x; k += blockDim.x) {
+      mn = fmin(mn, __ldcg(&b.partial[(size_t)k * 8 + c]));
+      mx = fmax(mx, __ldcg(&b.partial[(size_t)k * 8 + 3 + c]));
+    }
+    sh_min[c][threadIdx.x] = mn;
+    sh_max[c][threadIdx.x] = mx;
+  }
+  __syncthreads();
+  for (int st = blockDim.x / 2; st > 0; st >>= 1) {
+    if ((int)threadIdx.x < st)
+      for (int c = 0; c < 3; ++c) {
+        sh_min[c][threadIdx.x] = fmin(sh_min[c][threadIdx.x], sh_min[c][threadIdx.x + st]);
+        sh_max[c][threadIdx.x] = fmax(sh_max[c][threadIdx.x], sh_max[c][threadIdx.x + st]);
+      }
+    __syncthreads();
+  }
+  // avg_elem_size: the fixed-order sum of shl_geom.h (1024 lanes, then a tree)
+  for (uint32_t l = threadIdx.x; l < SHL_SUM_LANES; l += blockDim.x) {
+    double s = 0.0;
+    for (uint32_t i = l; i < sc.F; i += SHL_SUM_LANES) s = __dadd_rn(s, __ldcg(&b.fsize[i]));
+    lanes[l] = s;
+  }
+  __syncthreads();
+  for (uint32_t st = SHL_SUM_LANES / 2; st > 0; st >>= 1) {
+    for (uint32_t l = threadIdx.x; l < st; l += blockDim.x) lanes[l] = __dadd_rn(lanes[l], lanes[l + st]);
+    __syncthreads();
+  }
+  if (threadIdx.x != 0) return;
+  ctl->du_sum = 0.0;
+  for (int c = 0; c < 3; ++c) {
+    ctl->bmin[c] = sh_min[c][0];
+    ctl->bmax[c] = sh_max[c][0];
+  }
+  const double avg = __ddiv_rn(lanes[0], (double)sc.F);
+  ctl->avg_elem_size = avg;
+  double cell_size = __dmul_rn(sc.cell_size_mult, avg);
+  const double tolerance = __dmul_rn(sc.cell_margin, cell_size);
+  cell_size = __dadd_rn(cell_size, tolerance);
+  const double d_max = __dadd_rn(sc.thickness, tolerance);
+  ctl->cell_size = cell_size;
+  ctl->d_max = d_max;
+  ctl->d2_max = __dmul_rn(d_max, d_max);
+  uint64_t n_cells = 1;
+  for (int c = 0; c < 3; ++c) {
+    const double sz = __dsub_rn(ctl->bmax[c], ctl->bmin[c]);
+    const double q = __dadd_rn(__ddiv_rn(__dadd_rn(sz, d_max), cell_size), 1.0);
+    const int ncd = (q < 2147483647.0) ? (int)q : 2147483647;
+    ctl->ncd[c] = (uint32_t)ncd;
+    n_cells *= (uint64_t)(uint32_t)ncd;
+  }
+  if (n_cells > sc.n_cells_max) {
+    atomicMax(&ctl->problem, (int)SHL_TOO_MANY_CELLS);
+    ctl->rebuild = 0;
+    return;
+  }
+  if (n_cells > sc.n_cells_cap) {
+    set_error(ctl, SHL_ERR_CAPACITY);
+    return;
+  }
+  ctl->n_cells = (uint32_t)n_cells;
+  ctl->n_old = ctl->n_pairs;
+  ctl->n_new = 0;
+  ctl->n_rebuilds += 1;
+}
+
+// ---------------------------------------------------------------- clear --
+__global__ void k_rb_clear(DevBuf b, StepConst sc) {
+  Ctl* ctl = b.ctl;
+  if (rb_off(ctl)) return;
+  const uint32_t n_cells = ctl->n_cells;
+  const uint32_t stride = gridDim.x * blockDim.x;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_cells; i += stride) {
+    b.cell_count[i] = 0;
+    b.cell_fill[i] = 0;
+  }
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < sc.F; i += stride) b.seg_count[i] = 0;
+}
+
+// cell index range of face f on axis c (ShellSystem.C:1982-1983)
+__device__ __forceinline__ void cell_range(const DevBuf& b, const Ctl* ctl, uint32_t f, int* lo, int* hi) {
+  const double cs = ctl->cell_size, dm = ctl->d_max;
+  for (int c = 0; c < 3; ++c) {
+    lo[c] = (int)__ddiv_rn(__dsub_rn(b.bmin[3 * (size_t)f + c], ctl->bmin[c]), cs);
+    hi[c] = (int)__ddiv_rn(__dadd_rn(__dsub_rn(b.bmax[3 * (size_t)f + c], ctl->bmin[c]), dm), cs);
+  }
+}
+
+// ---------------------------------------------------------------- count --
+__global__ void __launch_bounds__(kBlock) k_rb_count(DevBuf b, StepConst sc) {
+  Ctl* ctl = b.ctl;
+  if (rb_off(ctl)) return;
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < sc.F) {
+    int lo[3], hi[3];
+    cell_range(b, ctl, t, lo, hi);
+    for (int c = 0; c < 3; ++c) {
+      b.cell_lo[3 * (size_t)t + c] = lo[c];
+      b.cell_hi[3 * (size_t)t + c] = hi[c];
+    }
+    const uint32_t ny = ctl->ncd[1], nz = ctl->ncd[2];
+    for (int cx = lo[0]; cx <= hi[0]; ++cx)
+      for (int cy = lo[1]; cy <= hi[1]; ++cy)
+        for (int cz = lo[2]; cz <= hi[2]; ++cz) {
+          const uint32_t cell = (uint32_t)cx * ny * nz + (uint32_t)cy * nz + (uint32_t)cz;
+          atomicAdd(&b.cell_count[cell], 1u);
+        }
+    return;
+  }
+  const uint32_t j = t - sc.F;
+  if (j < ctl->n_old) {
+    // ShellSystem.C:2020: drop unless sticking or still within d_max
+    const bool keep = b.pstick[0][j] != 0 || !(b.pd2[0][j] > ctl->d2_max);
+    b.pkeep[j] = keep ? 1 : 0;
+    if (keep) atomicAdd(&b.seg_count[b.pe1[0][j]], 1u);
+  }
+}
+
+// ----------------------------------------------------------------- scan --
+// Exclusive scan of in[0..n) into out[0..n) (+ out[n] = total if with_end),
+// gated by *gate; three launches, fixed grids sized by capacity.
+__global__ void __launch_bounds__(kBlock) k_scan_tiles(const uint32_t* gate, const Ctl* ctl, const uint32_t* in,
+                                                       uint32_t* out, const uint32_t* n_ptr, uint32_t n_const,
+                                                       uint32_t* tile_sums) {
+  if (*gate == 0 || ctl->halted) return;
+  const uint32_t n = n_ptr ? *n_ptr : n_const;
+  const uint32_t base = blockIdx.x * kScanTile;
+  if (base >= n) return;
+  constexpr int PER = kScanTile / kBlock;
+  uint32_t v[PER];
+  uint32_t sum = 0;
+  const uint32_t i0 = base + threadIdx.x * PER;
+#pragma unroll
+  for (int k = 0; k < PER; ++k) {
+    const uint32_t x = (i0 + k < n) ? in[i0 + k] : 0u;
+    v[k] = sum;
+    sum += x;
+  }
+  // exclusive scan of the per-thread sums over the block
+  __shared__ uint32_t wsum[kBlock / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t incl = sum;
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += y;
+  }
+  if (lane == 31) wsum[warp] = incl;
+  __syncthreads();
+  if (warp == 0) {
+    uint32_t w = (lane < kBlock / 32) ? wsum[lane] : 0u;
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += y;
+    }
+    if (lane < kBlock / 32) wsum[lane] = w;
+  }
+  __syncthreads();
+  const uint32_t excl = incl - sum + (warp > 0 ? wsum[warp - 1] : 0u);
+#pragma unroll
+  for (int k = 0; k < PER; ++k)
+    if (i0 + k < n) out[i0 + k] = v[k] + excl;
+  if (threadIdx.x == kBlock - 1) tile_sums[blockIdx.x] = excl + sum;
+}
+
+__global__ void __launch_bounds__(1024) k_scan_sums(const uint32_t* gate, Ctl* ctl, uint32_t* out,
+                                                     const uint32_t* n_ptr, uint32_t n_const, uint32_t* tile_sums,
+                                                     uint32_t* total, int with_end, uint32_t cap, int cap_error) {
+  if (*gate == 0 || ctl->halted) return;
+  const uint32_t n = n_ptr ? *n_ptr : n_const;
+  const uint32_t nt = (n + kScanTile - 1) / kScanTile;
+  const uint32_t per = (nt + blockDim.x - 1) / blockDim.x;
+  const uint32_t t0 = threadIdx.x * per;
+  uint32_t s = 0;
+  for (uint32_t k = 0; k < per; ++k)
+    if (t0 + k < nt) s += tile_sums[t0 + k];
+  __shared__ uint32_t sh[1024];
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (uint32_t o = 1; o < blockDim.x; o <<= 1) {
+    const uint32_t y = threadIdx.x >= o ? sh[threadIdx.x - o] : 0u;
+    __syncthreads();
+    sh[threadIdx.x] += y;
+    __syncthreads();
+  }
+  uint32_t run = sh[threadIdx.x] - s;
+  for (uint32_t k = 0; k < per; ++k)
+    if (t0 + k < nt) {
+      const uint32_t x = tile_sums[t0 + k];
+      tile_sums[t0 + k] = run;
+      run += x;
+    }
+  if (threadIdx.x == blockDim.x - 1) {
+    const uint32_t tot = sh[blockDim.x - 1];
+    *total = tot;
+    if (with_end) out[n] = tot;
+    if (cap_error && tot > cap) {
+      atomicMax(&ctl->error, (int)SHL_ERR_CAPACITY);
+      ctl->rebuild = 0;
+      ctl->csr_dirty = 0;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kBlock) k_scan_add(const uint32_t* gate, const Ctl* ctl, uint32_t* out,
+                                                     const uint32_t* n_ptr, uint32_t n_const,
+                                                     const uint32_t* tile_sums) {
+  if (*gate == 0 || ctl->halted) return;
+  const uint32_t n = n_ptr ? *n_ptr : n_const;
+  const uint32_t base = blockIdx.x * kScanTile;
+  if (base >= n || blockIdx.x == 0) return;
+  const uint32_t add = tile_sums[blockIdx.x];
+  for (uint32_t i = base + threadIdx.x; i < base + kScanTile && i < n; i += blockDim.x) out[i] += add;
+}
+
+void launch_scan(const uint32_t* gate, Ctl* ctl, const uint32_t* in, uint32_t* out, const uint32_t* n_ptr,
+                 uint32_t n_const, uint32_t n_cap, uint32_t* tile_sums, uint32_t* total, bool with_end,
+                 uint32_t cap, bool cap_error, cudaStream_t s) {
+  const uint32_t nt = (n_cap + kScanTile - 1) / kScanTile;
+  const uint32_t grid = nt > 0 ? nt : 1;
+  k_scan_tiles<<<grid, kBlock, 0, s>>>(gate, ctl, in, out, n_ptr, n_const, tile_sums);
+  k_scan_sums<<<1, 1024, 0, s>>>(gate, ctl, out, n_ptr, n_const, tile_sums, total, with_end ? 1 : 0, cap,
+                                 cap_error ? 1 : 0);
+  k_scan_add<<<grid, kBlock, 0, s>>>(gate, ctl, out, n_ptr, n_const, tile_sums);
+}
+
+// ----------------------------------------------------------------- fill --
+__global__ void __launch_bounds__(kBlock) k_rb_fill(DevBuf b, StepConst sc) {
+  Ctl* ctl = b.ctl;
+  if (rb_off(ctl)) return;
+  const uint32_t f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= sc.F) return;
+  int lo[3], hi[3];
+  for (int c = 0; c < 3; ++c) {
+    lo[c] = b.cell_lo[3 * (size_t)f + c];
+    hi[c] = b.cell_hi[3 * (size_t)f + c];
+  }
+  const uint32_t ny = ctl->ncd[1], nz = ctl->ncd[2];
+  for (int cx = lo[0]; cx <= hi[0]; ++cx)
+    for (int cy = lo[1]; cy <= hi[1]; ++cy)
+      for (int cz = lo[2]; cz <= hi[2]; ++cz) {
+        const uint32_t cell = (uint32_t)cx * ny * nz + (uint32_t)cy * nz + (uint32_t)cz;
+        const uint32_t pos = b.cell_start[cell] + atomicAdd(&b.cell_fill[cell], 1u);
+        b.cell_items[pos] = f;
+      }
+}
+
+__device__ __forceinline__ bool sorted_contains(const uint32_t* a, uint32_t lo, uint32_t hi, uint32_t x) {
+  while (lo < hi) {
+    const uint32_t mid = (lo + hi) >> 1;
+    const uint32_t y = a[mid];
+    if (y == x) return true;
+    if (y < x) lo = mid + 1; else hi = mid;
+  }
+  return false;
+}
+
+// index of x in a[lo..hi), or hi if absent
+__device__ __forceinline__ uint32_t sorted_find(const uint32_t* a, uint32_t lo, uint32_t hi, uint32_t x) {
+  const uint32_t end = hi;
+  while (lo < hi) {
+    const uint32_t mid = (lo + hi) >> 1;
+    const uint32_t y = a[mid];
+    if (y == x) return mid;
+    if (y < x) lo = mid + 1; else hi = mid;
+  }
+  return end;
+}
+
+// ---------------------------------------------------------------- pairs --
+__global__ void __launch_bounds__(128) k_rb_pairs(DevBuf b, StepConst sc) {
+  Ctl* ctl = b.ctl;
+  if (rb_off(ctl)) return;
+  const uint32_t e1 = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e1 >= sc.F) return;
+  int lo1[3], hi1[3];
+  for (int c = 0; c < 3; ++c) {
+    lo1[c] = b.cell_lo[3 * (size_t)e1 + c];
+    hi1[c] = b.cell_hi[3 * (size_t)e1 + c];
+  }
+  const uint32_t ny = ctl->ncd[1], nz = ctl->ncd[2];
+  const double d_max = ctl->d_max, d2_max = ctl->d2_max;
+  const uint32_t c0 = b.close_ptr[e1], c1 = b.close_ptr[e1 + 1];
+  const uint32_t o0 = b.pair_ptr[0][e1], o1 = b.pair_ptr[0][e1 + 1];
+  const double* P1[3];
+  for (int k = 0; k < 3; ++k) P1[k] = b.p + 3 * (size_t)b.tri[3 * (size_t)e1 + k];
+  double mn1[3], mx1[3];
+  for (int c = 0; c < 3; ++c) {
+    mn1[c] = b.bmin[3 * (size_t)e1 + c];
+    mx1[c] = b.bmax[3 * (size_t)e1 + c];
+  }
+  uint32_t found_e2[kMaxNewPerFace];
+  double found_d2[kMaxNewPerFace];
+  int n_found = 0;
+  bool overflow = false;
+  for (int cx = lo1[0]; cx <= hi1[0]; ++cx)
+    for (int cy = lo1[1]; cy <= hi1[1]; ++cy)
+      for (int cz = lo1[2]; cz <= hi1[2]; ++cz) {
+        const uint32_t cell = (uint32_t)cx * ny * nz + (uint32_t)cy * nz + (uint32_t)cz;
+        const uint32_t s0 = b.cell_start[cell], cnt = b.cell_count[cell];
+        for (uint32_t k = 0; k < cnt; ++k) {
+          const uint32_t e2 = b.cell_items[s0 + k];
+          if (e2 <= e1) continue;
+          // emit each pair from its lowest shared cell only
+          const int* lo2 = b.cell_lo + 3 * (size_t)e2;
+          const int lx = max(lo1[0], lo2[0]), ly = max(lo1[1], lo2[1]), lz = max(lo1[2], lo2[2]);
+          if (lx != cx || ly != cy || lz != cz) continue;
+          if (sorted_contains(b.close_list, c0, c1, e2)) continue;
+          const uint32_t at = sorted_find(b.pe2[0], o0, o1, e2);
+          if (at < o1 && b.pkeep[at]) continue;
+          bool apart = false;
+          for (int c = 0; c < 3; ++c) {
+            const double mn2 = b.bmin[3 * (size_t)e2 + c], mx2 = b.bmax[3 * (size_t)e2 + c];
+            apart = apart || mn1[c] > __dadd_rn(mx2, d_max) || mn2 > __dadd_rn(mx1[c], d_max);
+          }
+          if (apart) continue;
+          const double* P2[3];
+          for (int q = 0; q < 3; ++q) P2[q] = b.p + 3 * (size_t)b.tri[3 * (size_t)e2 + q];
+          shl_pair_geom g;
+          shl_pair_compute(P1, P2, &g);
+          if (g.d2 <= 0.0) atomicMax(&ctl->problem, (int)SHL_CONTACT_PROBLEM);
+          if (g.d2 > d2_max) continue;
+          if (n_found < kMaxNewPerFace) {
+            found_e2[n_found] = e2;
+            found_d2[n_found] = g.d2;
+            ++n_found;
+          } else {
+            overflow = true;
+          }
+        }
+      }
+  if (overflow) set_error(ctl, SHL_ERR_CAPACITY);
+  b.new_cnt[e1] = (uint32_t)n_found;
+  if (n_found == 0) return;
+  const uint32_t off = atomicAdd(&ctl->n_new, (uint32_t)n_found);
+  if (off + n_found > sc.pairs_cap) {
+    set_error(ctl, SHL_ERR_CAPACITY);
+    b.new_cnt[e1] = 0;
+    return;
+  }
+  b.new_off[e1] = off;
+  for (int k = 0; k < n_found; ++k) {
+    b.new_e1[off + k] = e1;
+    b.new_e2[off + k] = found_e2[k];
+    b.new_d2[off + k] = found_d2[k];
+  }
+  atomicAdd(&b.seg_count[e1], (uint32_t)n_found);
+}
+
+// -------------------------------------------------------------- assemble --
+__global__ void __launch_bounds__(kBlock) k_rb_assemble(DevBuf b, StepConst sc) {
+  Ctl* ctl = b.ctl;
+  if (rb_off(ctl)) return;
+  const uint32_t e1 = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e1 >= sc.F) return;
+  uint32_t dst = b.pair_ptr[1][e1];
+  const uint32_t o0 = b.pair_ptr[0][e1], o1 = b.pair_ptr[0][e1 + 1];
+  const uint32_t nn = b.new_cnt[e1];
+  uint32_t ne2[kMaxNewPerFace];
+  double nd2[kMaxNewPerFace];
+  if (nn > 0) {
+    const uint32_t off = b.new_off[e1];
+    for (uint32_t k = 0; k < nn; ++k) {
+      // insertion sort by e2
+      const uint32_t x = b.new_e2[off + k];
+      const double d = b.new_d2[off + k];
+      int q = (int)k - 1;
+      while (q >= 0 && ne2[q] > x) {
+        ne2[q + 1] = ne2[q];
+        nd2[q + 1] = nd2[q];
+        --q;
+      }
+      ne2[q + 1] = x;
+      nd2[q + 1] = d;
+    }
+  }
+  uint32_t io = o0, in = 0;
+  for (;;) {
+    while (io < o1 && !b.pkeep[io]) ++io;
+    const bool have_old = io < o1, have_new = in < nn;
+    if (!have_old && !have_new) break;
+    const bool take_old = have_old && (!have_new || b.pe2[0][io] < ne2[in]);
+    b.pe1[1][dst] = e1;
+    if (take_old) {
+      b.pe2[1][dst] = b.pe2[0][io];
+      b.pstick[1][dst] = b.pstick[0][io];
+      b.pd2[1][dst] = b.pd2[0][io];
+      for (int c = 0; c < 3; ++c) b.porig[1][3 * (size_t)dst + c] = b.porig[0][3 * (size_t)io + c];
+      ++io;
+    } else {
+      b.pe2[1][dst] = ne2[in];
+      b.pstick[1][dst] = 0;
+      b.pd2[1][dst] = nd2[in];
+      for (int c = 0; c < 3; ++c) b.porig[1][3 * (size_t)dst + c] = 0.0;
+      ++in;
+    }
+    ++dst;
+  }
+}
+
+__global__ void k_rb_copyback(DevBuf b, StepConst sc) {
+  Ctl* ctl = b.ctl;
+  if (rb_off(ctl)) return;
+  const uint32_t n = ctl->n_next;
+  const uint32_t stride = gridDim.x * blockDim.x;
+  for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += stride) {
+    b.pe1[0][j] = b.pe1[1][j];
+    b.pe2[0][j] = b.pe2[1][j];
+    b.pstick[0][j] = b.pstick[1][j];
+    b.pd2[0][j] = b.pd2[1][j];
+    for (int c = 0; c < 3; ++c) b.porig[0][3 * (size_t)j + c] = b.porig[1][3 * (size_t)j + c];
+  }
+  for (uint32_t f = blockIdx.x * blockDim.x + threadIdx.x; f <= sc.F; f += stride) b.pair_ptr[0][f] = b.pair_ptr[1][f];
+}
+
+// flag flip after the copy-back (single thread, after all blocks are done)
+__global__ void k_rb_finish(DevBuf b) {
+  Ctl* ctl = b.ctl;
+  if (rb_off(ctl)) return;
+  ctl->n_pairs = ctl->n_next;
+  ctl->rebuild = 0;
+  ctl->csr_dirty = 1;
+}
+
+// ------------------------------------------------------------ contact CSR --
+__device__ __forceinline__ bool csr_off(const Ctl* ctl) { return ctl->csr_dirty == 0 || ctl->halted != 0; }
+
+__global__ void k_csr_clear(DevBuf b, StepConst sc) {
+  if (csr_off(b.ctl)) return;
+  const uint32_t stride = gridDim.x * blockDim.x;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < sc.V; i += stride) {
+    b.csr_count[i] = 0;
+    b.csr_fill[i] = 0;
+  }
+}
+
+__global__ void k_csr_count(DevBuf b, StepConst sc) {
+  Ctl* ctl = b.ctl;
+  if (csr_off(ctl)) return;
+  const uint32_t n = ctl->n_pairs;
+  const uint32_t stride = gridDim.x * blockDim.x;
+  for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += stride) {
+    const uint32_t e[2] = {b.pe1[0][j], b.pe2[0][j]};
+    for (int r = 0; r < 6; ++r) atomicAdd(&b.csr_count[b.tri[3 * (size_t)e[r / 3] + r % 3]], 1u);
+  }
+}
+
+__global__ void k_csr_fill(DevBuf b, StepConst sc) {
+  Ctl* ctl = b.ctl;
+  if (csr_off(ctl)) return;
+  const uint32_t n = ctl->n_pairs;
+  const uint32_t stride = gridDim.x * blockDim.x;
+  for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += stride) {
+    const uint32_t e[2] = {b.pe1[0][j], b.pe2[0][j]};
+    for (int r = 0; r < 6; ++r) {
+      const uint32_t nd = b.tri[3 * (size_t)e[r / 3] + r % 3];
+      const uint32_t pos = b.csr_ptr[nd] + atomicAdd(&b.csr_fill[nd], 1u);
+      b.csr_ent[pos] = j * 8u + (uint32_t)r;
+    }
+  }
+}
+
+// sort each node's entries (deterministic order for the gather) and clear the flag
+__global__ void k_csr_sort(DevBuf b, StepConst sc) {
+  Ctl* ctl = b.ctl;
+  if (csr_off(ctl)) return;
+  const uint32_t nd = blockIdx.x * blockDim.x + threadIdx.x;
+  if (nd >= sc.V) return;
+  const uint32_t k0 = b.csr_ptr[nd], k1 = b.csr_ptr[nd + 1];
+  for (uint32_t k = k0 + 1; k < k1; ++k) {
+    const uint32_t x = b.csr_ent[k];
+    uint32_t q = k;
+    while (q > k0 && b.csr_ent[q - 1] > x) {
+      b.csr_ent[q] = b.csr_ent[q - 1];
+      --q;
+    }
+    b.csr_ent[q] = x;
+  }
+}
+
+__global__ void k_csr_finish(DevBuf b) {
+  if (csr_off(b.ctl)) return;
+  b.ctl->csr_dirty = 0;
+}
+
+inline uint32_t nblk(uint32_t n, uint32_t bs = kBlock) { return n == 0 ? 1 : (n + bs - 1) / bs; }
+
+}  // namespace
+
+void launch_contact_csr(const DevBuf& b, const StepConst& sc, cudaStream_t s) {
+  const uint32_t gV = nblk(sc.V);
+  uint32_t gP = nblk(sc.pairs_cap);
+  if (gP > 8 * 152) gP = 8 * 152;
+  k_csr_clear<<<gV, kBlock, 0, s>>>(b, sc);
+  k_csr_count<<<gP, kBlock, 0, s>>>(b, sc);
+  launch_scan(&b.ctl->csr_dirty, b.ctl, b.csr_count, b.csr_ptr, nullptr, sc.V, sc.V, b.scan_block, &b.ctl->n_csr,
+              true, sc.csr_cap, true, s);
+  k_csr_fill<<<gP, kBlock, 0, s>>>(b, sc);
+  k_csr_sort<<<gV, kBlock, 0, s>>>(b, sc);
+  k_csr_finish<<<1, 1, 0, s>>>(b);
+}
+
+void launch_rebuild(const DevBuf& b, const StepConst& sc, cudaStream_t s) {
+  const uint32_t gF = nblk(sc.F);
+  k_rb_aabb<<<gF, kBlock, 0, s>>>(b, sc);
+  {
+    uint32_t g = nblk(sc.n_cells_cap > sc.F ? sc.n_cells_cap : sc.F);
+    if (g > 16 * 152) g = 16 * 152;
+    k_rb_clear<<<g, kBlock, 0, s>>>(b, sc);
+  }
+  k_rb_count<<<nblk(sc.F + sc.pairs_cap), kBlock, 0, s>>>(b, sc);
+  launch_scan(&b.ctl->rebuild, b.ctl, b.cell_count, b.cell_start, &b.ctl->n_cells, 0, sc.n_cells_cap, b.scan_block,
+              &b.ctl->n_entries, false, sc.entries_cap, true, s);
+  k_rb_fill<<<gF, kBlock, 0, s>>>(b, sc);
+  k_rb_pairs<<<nblk(sc.F, 128), 128, 0, s>>>(b, sc);
+  launch_scan(&b.ctl->rebuild, b.ctl, b.seg_count, b.pair_ptr[1], nullptr, sc.F, sc.F, b.scan_block, &b.ctl->n_next,
+              true, sc.pairs_cap, true, s);
+  k_rb_assemble<<<gF, kBlock, 0, s>>>(b, sc);
+  {
+    uint32_t g = nblk(sc.pairs_cap > sc.F + 1 ? sc.pairs_cap : sc.F + 1);
+    if (g > 8 * 152) g = 8 * 152;
+    k_rb_copyback<<<g, kBlock, 0, s>>>(b, sc);
+  }
+  k_rb_finish<<<1, 1, 0, s>>>(b);
+  launch_contact_csr(b, sc, s);
+}
+
+}  // namespace shl

@@ -1,0 +1,166 @@
+// shl_internal.cuh -- device data layout and kernel launchers (internal).
+//
+// Layout in HBM (one context = one shell):
+//   node vectors   u, v, a, u_pred, v_pred, p, X, Minv, C : node-major xyz, 3V doubles
+//   face constants face[field * F + i], i = internal face index (regular
+//                  patches first, then irregular groups), FaceField order
+//   patch ids      patch[slot * F + i] (slot-major, coalesced per slot)
+//   element forces qe[(i * 12 + slot) * 3 + c]: the per-(face, slot) share of
+//                  f (internal minus external pressure), gathered per node
+//                  through gather_ptr/gather_ent with no atomics
+//   contact list   sorted by (eid1, eid2); per-pair state SoA; pair_ptr[F+1]
+//                  gives each eid1's segment; per-node contact CSR for the gather
+//   control block  Ctl: step scalars, problem flags, energy sums (device-resident,
+//                  so a whole multi-step sequence runs without host round trips)
+#ifndef SHL_INTERNAL_CUH_
+#define SHL_INTERNAL_CUH_
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/shl.h"
+#include "shl_setup.h"
+
+namespace shl {
+
+constexpr int kBlock = 256;          // threads per block for element / node kernels
+constexpr int kMaxGroups = 8;        // patch groups (regular + irregular valences)
+constexpr int kMaxSlots = 18;        // patch slots of the largest supported valence (12)
+constexpr int kScanTile = 2048;      // elements per block in the multi-block scan
+
+// Patch-group description for the element kernel (in __constant__ memory).
+struct GroupDesc {
+  uint32_t first;       // first internal face
+  uint32_t count;       // faces
+  uint32_t block_start; // first block of the element launch for this group
+  int32_t n_slots;
+  int32_t basis_off;    // offset into the basis table (doubles)
+};
+
+// Control block in device memory.
+struct Ctl {
+  // time stepping
+  double time;
+  double pressure;         // pressure of the current step
+  double volume_pressure;  // bulk-modulus pressure of the current step
+  double volume, volume0, area;
+  uint32_t time_step;
+  uint32_t table_pos;      // index into the per-step pressure table
+  uint32_t table_len;      // entries uploaded (the last one repeats past the end)
+  int32_t problem;         // worst problem of the current step
+  int32_t worst_problem;   // worst problem since the last report reset
+  int32_t halted;          // set at the end of a step whose problem stops the run
+  uint32_t steps_done;
+  int32_t error;           // library error (SHL_ERR_CAPACITY ...), halts the run
+  uint32_t first_problem_step;
+  // linked cells / contact
+  double du_sum;
+  double avg_elem_size;
+  double cell_size, d_max, d2_max;
+  double bmin[3], bmax[3];
+  uint32_t ncd[3];
+  uint32_t rebuild;        // rebuild requested for the next rebuild pass
+  uint32_t n_cells;
+  uint32_t n_entries;      // (cell, face) entries of the current rebuild
+  uint32_t n_pairs;        // pairs in the current list
+  uint32_t n_old;          // pairs in the previous list (during a rebuild)
+  uint32_t n_new;          // new pairs found in the current rebuild
+  uint32_t n_rebuilds;
+  uint32_t n_csr;          // contact CSR entries
+  uint32_t n_next;         // pairs in the list being assembled
+  uint32_t csr_dirty;      // the contact CSR must be rebuilt
+  // measurements of the current step
+  double Etens, Ebend, Eself, Efric, Ekin, kGauss, kMean;
+  uint32_t Nc;
+  uint32_t pad;
+  // dt-weighted sums (MovingAverage inputs)
+  double sum_dt, sum_area, sum_volume, sum_Nc, sum_Ekin, sum_Etens, sum_Ebend, sum_Eself, sum_Efric,
+      sum_kGauss, sum_kMean;
+  // last-block counters
+  uint32_t cnt[16];
+};
+
+// Step constants (captured by value in each launch).
+struct StepConst {
+  double dt;
+  double nm0, nm6, nm7, nm8;  // newmark_a[0], [6], [7], [8]
+  double thickness;
+  double K, D;
+  double qw;
+  double stiff_density, stiff_static_friction, d2_friction;
+  double mu_s, mu_d, self_damping, self_friction_damping, v_stop;
+  double cell_size_mult, cell_margin;
+  double bulk_modulus;
+  double pressure_default;
+  const double* pressure_table;  // device, or null
+  uint64_t n_cells_max;
+  uint32_t n_cells_cap, entries_cap, pairs_cap, csr_cap;
+  int32_t contact;   // 1 if self-contact is on
+  int32_t friction;  // 1 if mu_s or mu_d != 0
+  int32_t pressure_base, pressure_dir;
+  int32_t compat_zero_pressure;
+  int32_t stop_on_problem;
+  uint32_t V, F;
+};
+
+// Device buffers of one context.
+struct DevBuf {
+  double *X, *u, *v, *a, *up, *vp, *p, *Minv, *C;
+  double* face;       // FF_COUNT * F
+  int32_t* patch;     // 12 * F
+  double* qe;         // F * 12 * 3
+  uint32_t *gather_ptr, *gather_ent;
+  uint32_t* tri;      // 3F original order
+  uint32_t *perm;     // internal -> original
+  double *area, *kG, *kM, *etens, *ebend;  // original order
+  double* partial;    // per-block partial sums
+  uint32_t *close_ptr, *close_list;
+  // contact: per-face AABB (original order), size, cell ranges
+  double *bmin, *bmax, *fsize;
+  int32_t *cell_lo, *cell_hi;  // 3 per face
+  uint32_t *cell_count, *cell_start, *cell_fill, *cell_items;
+  uint32_t* scan_block;        // block sums for the scans
+  // pair lists (double buffered: cur / old), sorted by (e1, e2)
+  uint32_t *pe1[2], *pe2[2];
+  uint8_t* pstick[2];
+  double *pd2[2], *porig[2];   // porig: 3 per pair
+  uint32_t* pair_ptr[2];       // F+1
+  uint8_t* pkeep;              // keep flags of the old list
+  uint32_t *new_e1, *new_e2;   // new pairs of a rebuild
+  double* new_d2;
+  uint32_t *new_off, *new_cnt; // per face: offset and count of its new pairs
+  uint32_t* seg_count;         // per-face pair counts (F)
+  double* pforce;              // 7 per pair: f_contact(3), v1, w1, v2, w2
+  uint32_t *csr_count, *csr_ptr, *csr_ent, *csr_fill;  // per-node contact CSR
+  Ctl* ctl;
+  double* ptable;              // per-step pressure table (capacity)
+  uint32_t ptable_cap;
+};
+
+// ---- launchers (shl_kernels.cu) ----
+void launch_predict(const DevBuf& b, const StepConst& sc, int cur, cudaStream_t s);
+void launch_elements(const DevBuf& b, const StepConst& sc, uint32_t n_blocks, cudaStream_t s);
+void launch_contact_force(const DevBuf& b, const StepConst& sc, int cur, cudaStream_t s);
+void launch_gather_correct(const DevBuf& b, const StepConst& sc, int cur, bool correct, double* f_out,
+                           double* a_out, cudaStream_t s);
+void launch_volume_end_step(const DevBuf& b, const StepConst& sc, bool end_step, cudaStream_t s);
+void launch_positions(const DevBuf& b, const StepConst& sc, cudaStream_t s);
+void upload_groups(const GroupDesc* g, int n, const double* basis, int n_basis);
+void launch_fp64_peak(double* out, int blocks, int iters, cudaStream_t s);
+void launch_flush(void* buf, size_t bytes, uint32_t tag, cudaStream_t s);
+
+// ---- launchers (shl_contact.cu) ----
+// One candidate-list update (compute_shell_shell_contact_candidates,
+// ShellSystem.C:1910-2135).  Runs only when ctl->rebuild is set on the device
+// (every kernel returns at once otherwise), so it can sit in a CUDA graph.
+// The list lives in buffer 0; buffer 1 is scratch.
+void launch_rebuild(const DevBuf& b, const StepConst& sc, cudaStream_t s);
+// Rebuild the per-node contact CSR when ctl->csr_dirty is set.
+void launch_contact_csr(const DevBuf& b, const StepConst& sc, cudaStream_t s);
+constexpr int kMaxNewPerFace = 64;  // new pairs one face may add in one rebuild
+
+}  // namespace shl
+
+#endif

@@ -1,0 +1,657 @@
+// shl_kernels.cu -- FP64 kernels of one explicit Newmark step.
+//
+//   k_predict        nodes  ShellSystem.C:972-989 (predictor), 2591-2652
+//                           (check_increment), 2484-2502 (positions), and the
+//                           scalar part of prepare_next_step (924-949)
+//   k_elements       faces  1382-1464 (deformed metrics), 1125-1314 (internal
+//                           force), 1474-1585 (pressure), 2737-2788 (curvatures)
+//   k_contact_force  pairs  1792-1907 with Friction.C:4-60
+//   k_gather_correct nodes  the per-node sum of element and contact shares
+//                           (a deterministic gather, no atomics), 1006-1008
+//                           (damping, M^-1), 1046-1090 (corrector, check_increment)
+//   k_volume_end     faces  2505-2541 (enclosed volume), 2830-2843 (sums),
+//                           2901-2953 (problem handling)
+//
+// Reductions are fixed-order (warp shuffles, then the last block to finish sums
+// the per-block partials in block order), so results are bitwise reproducible
+// run to run.  The predictor, positions and the contact path use separately
+// rounded operations (no FMA) so the contact candidate list agrees bit for bit
+// with the CPU path at the same state.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "shl_geom.h"
+#include "shl_internal.cuh"
+
+namespace shl {
+
+__constant__ GroupDesc c_groups[kMaxGroups];
+__constant__ int c_n_groups;
+__constant__ double c_basis[kMaxGroups * kMaxSlots * 6];
+
+void upload_groups(const GroupDesc* g, int n, const double* basis, int n_basis) {
+  cudaMemcpyToSymbol(c_groups, g, sizeof(GroupDesc) * n);
+  cudaMemcpyToSymbol(c_n_groups, &n, sizeof(int));
+  cudaMemcpyToSymbol(c_basis, basis, sizeof(double) * n_basis);
+}
+
+// ---------------------------------------------------------------- helpers --
+
+__device__ __forceinline__ bool inactive(const Ctl* ctl) {
+  return ctl->halted != 0;
+}
+
+// fixed-order block sum; result valid in thread 0; sh needs blockDim/32 doubles
+__device__ __forceinline__ double block_sum(double x, double* sh) {
+  for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  __syncthreads();
+  if (lane == 0) sh[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    x = (lane < (int)(blockDim.x >> 5)) ? sh[lane] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+  }
+  return x;
+}
+
+__device__ __forceinline__ double block_max(double x, double* sh) {
+  for (int o = 16; o > 0; o >>= 1) x = fmax(x, __shfl_down_sync(0xffffffffu, x, o));
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  __syncthreads();
+  if (lane == 0) sh[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    x = (lane < (int)(blockDim.x >> 5)) ? sh[lane] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) x = fmax(x, __shfl_down_sync(0xffffffffu, x, o));
+  }
+  return x;
+}
+
+// true in every thread of the block that finished last; resets the counter
+__device__ __forceinline__ bool last_block(uint32_t* counter) {
+  __shared__ bool is_last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const uint32_t t = atomicAdd(counter, 1u);
+    is_last = (t == gridDim.x - 1);
+    if (is_last) *counter = 0;
+  }
+  __syncthreads();
+  return is_last;
+}
+
+// sum of partial[k * stride + b] over blocks b in fixed order (last block only)
+__device__ __forceinline__ double sum_partials(const double* partial, int k, int nb, double* sh) {
+  double s = 0.0;
+  for (int b = threadIdx.x; b < nb; b += blockDim.x) s += __ldcg(&partial[(size_t)b * 8 + k]);
+  return block_sum(s, sh);
+}
+
+__device__ __forceinline__ void register_problem(Ctl* ctl, int p) { atomicMax(&ctl->problem, p); }
+
+// tolerance of the linked-cell rebuild test, ShellSystem.C:1917-1919
+__device__ __forceinline__ double rebuild_tolerance(const StepConst& sc, const Ctl* ctl) {
+  const double cs = __dmul_rn(sc.cell_size_mult, ctl->avg_elem_size);
+  return __dmul_rn(sc.cell_margin, cs);
+}
+
+// ------------------------------------------------------------ predictor --
+// u_pred = u + dt v + a8 a ; v_pred = v + a6 a ; p = X + u_pred ; du_max
+__global__ void __launch_bounds__(kBlock) k_predict(DevBuf b, StepConst sc) {
+  Ctl* ctl = b.ctl;
+  if (inactive(ctl)) return;
+  __shared__ double sh[kBlock / 32];
+  const uint32_t n = blockIdx.x * blockDim.x + threadIdx.x;
+  double du2 = 0.0;
+  if (n < sc.V) {
+    double d[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const size_t k = 3 * (size_t)n + c;
+      const double u = b.u[k], v = b.v[k], a = b.a[k];
+      double up = __dadd_rn(__dmul_rn(sc.dt, v), u);
+      up = __dadd_rn(__dmul_rn(sc.nm8, a), up);
+      b.up[k] = up;
+      b.vp[k] = __dadd_rn(__dmul_rn(sc.nm6, a), v);
+      b.p[k] = __dadd_rn(b.X[k], up);
+      d[c] = __dsub_rn(up, u);
+    }
+    du2 = __dadd_rn(__dadd_rn(__dmul_rn(d[0], d[0]), __dmul_rn(d[1], d[1])), __dmul_rn(d[2], d[2]));
+  }
+  const double m = block_max(du2, sh);
+  if (threadIdx.x == 0) b.partial[(size_t)blockIdx.x * 8] = m;
+  if (!last_block(&ctl->cnt[0])) return;
+  double mm = 0.0;
+  for (int k = threadIdx.x; k < (int)gridDim.x; k += blockDim.x) mm = fmax(mm, __ldcg(&b.partial[(size_t)k * 8]));
+  mm = block_max(mm, sh);
+  if (threadIdx.x != 0) return;
+  // prepare_next_step: time, the step's pressure, volume pressure
+  ctl->time = __dadd_rn(ctl->time, sc.dt);
+  ctl->time_step += 1;
+  double pr = sc.pressure_default;
+  if (sc.pressure_table && ctl->table_len > 0)
+    pr = sc.pressure_table[ctl->table_pos < ctl->table_len ? ctl->table_pos : ctl->table_len - 1];
+  ctl->table_pos += 1;
+  if (sc.compat_zero_pressure) pr = pr * 0.0;
+  ctl->pressure = pr;
+  {
+    const double red = fmax(1.0 - (double)((int)(ctl->time * 5.0)) * 0.01, 0.5);
+    if (ctl->time_step == 2) ctl->volume0 = ctl->volume;
+    ctl->volume_pressure = (sc.bulk_modulus == 0.0) ? 0.0 : sc.bulk_modulus * (ctl->volume0 * red / ctl->volume - 1.0);
+  }
+  // check_increment(false)
+  const double du_max = sqrt(mm);
+  if (isfinite(du_max)) {
+    ctl->du_sum = __dadd_rn(ctl->du_sum, __dmul_rn(2.0, du_max));
+    if (sc.contact && du_max > 0.5 * sc.thickness) register_problem(ctl, SHL_LARGE_DISP);
+  } else {
+    register_problem(ctl, SHL_NOT_FINITE);
+  }
+  ctl->rebuild = (sc.contact && ctl->du_sum >= rebuild_tolerance(sc, ctl)) ? 1u : 0u;
+}
+
+// positions only (p = X + u_pred), for force evaluations at a given state
+__global__ void k_positions(DevBuf b, StepConst sc) {
+  const uint32_t n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= sc.V) return;
+  for (int c = 0; c < 3; ++c) {
+    const size_t k = 3 * (size_t)n + c;
+    b.p[k] = __dadd_rn(b.X[k], b.up[k]);
+  }
+}
+
+// ------------------------------------------------------------- elements --
+struct ElemOut {
+  double etens, ebend, kg, km, area;
+};
+
+__device__ __forceinline__ void cross3(const double* a, const double* b, double* r) {
+  r[0] = a[1] * b[2] - a[2] * b[1];
+  r[1] = a[2] * b[0] - a[0] * b[2];
+  r[2] = a[0] * b[1] - a[1] * b[0];
+}
+__device__ __forceinline__ double dot3(const double* a, const double* b) {
+  return a[0] * b[0] + a[1] * b[1] + a[2] * b[2];
+}
+
+// One face: deformed metric, stress resultants, and the per-slot force
+// share qe_s = sum_k B[s][k] Z_k (internal minus pressure), see the comments.
+template <int NP>
+__device__ __forceinline__ ElemOut element_force(uint32_t i, int np_rt, const double* __restrict__ B,
+                                                 const DevBuf& b, const StepConst& sc, double pressure,
+                                                 double vol_p) {
+  const uint32_t F = sc.F;
+  const int np = NP > 0 ? NP : np_rt;
+  // G[k] = sum_s B[s][k] u_s  (unrotated value and derivatives of u at the qp)
+  double G[6][3];
+#pragma unroll
+  for (int k = 0; k < 6; ++k) G[k][0] = G[k][1] = G[k][2] = 0.0;
+#pragma unroll
+  for (int s = 0; s < (NP > 0 ? NP : kMaxSlots); ++s) {
+    if (NP == 0 && s >= np) break;
+    const int nd = __ldg(&b.patch[(size_t)s * F + i]);
+    const double ux = __ldg(&b.up[3 * (size_t)nd]);
+    const double uy = __ldg(&b.up[3 * (size_t)nd + 1]);
+    const double uz = __ldg(&b.up[3 * (size_t)nd + 2]);
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+      const double w = B[6 * s + k];
+      G[k][0] = fma(w, ux, G[k][0]);
+      G[k][1] = fma(w, uy, G[k][1]);
+      G[k][2] = fma(w, uz, G[k][2]);
+    }
+  }
+  const double* fc = b.face;
+#define FC(fld) __ldg(&fc[(size_t)(fld) * F + i])
+  const double R00 = FC(FF_R00), R01 = FC(FF_R01), R10 = FC(FF_R10), R11 = FC(FF_R11);
+  const double JxW = FC(FF_JXW);
+  // rotation of derivatives onto the material frame (reinit_mod)
+  const double c11a = R00 * R00, c11b = R10 * R10, c11c = 2.0 * R00 * R10;
+  const double c22a = R01 * R01, c22b = R11 * R11, c22c = 2.0 * R01 * R11;
+  const double c12a = R00 * R01, c12b = R10 * R11, c12c = R01 * R10 + R00 * R11;
+  double a1[3], a2[3], v1[3], v2[3], v3[3], xq[3];
+  {
+    const double A1[3] = {FC(FF_A10), FC(FF_A11), FC(FF_A12)};
+    const double A2[3] = {FC(FF_A20), FC(FF_A21), FC(FF_A22)};
+    const double D1[3] = {FC(FF_D10), FC(FF_D11), FC(FF_D12)};
+    const double D2[3] = {FC(FF_D20), FC(FF_D21), FC(FF_D22)};
+    const double D3[3] = {FC(FF_D30), FC(FF_D31), FC(FF_D32)};
+    const double X0[3] = {FC(FF_X0), FC(FF_X1), FC(FF_X2)};
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      a1[c] = A1[c] + (R00 * G[1][c] + R10 * G[2][c]);
+      a2[c] = A2[c] + (R01 * G[1][c] + R11 * G[2][c]);
+      v1[c] = D1[c] + (c11a * G[3][c] + c11b * G[4][c] + c11c * G[5][c]);
+      v2[c] = D2[c] + (c22a * G[3][c] + c22b * G[4][c] + c22c * G[5][c]);
+      v3[c] = D3[c] + (c12a * G[3][c] + c12b * G[4][c] + c12c * G[5][c]);
+      xq[c] = X0[c] + G[0][c];
+    }
+  }
+  double a3[3];
+  cross3(a1, a2, a3);
+  const double jac = sqrt(dot3(a3, a3));
+  const double invjac = 1.0 / jac;
+  a3[0] *= invjac; a3[1] *= invjac; a3[2] *= invjac;
+  const double g0 = dot3(a1, a1), g1 = dot3(a2, a2), g2 = dot3(a1, a2);
+  const double h0 = dot3(v1, a3), h1 = dot3(v2, a3), h2 = dot3(v3, a3);
+  // strains (Voigt, shear doubled), ShellSystem.C:1190-1194
+  const double al0 = 0.5 * (g0 - FC(FF_G0)), al1 = 0.5 * (g1 - FC(FF_G1)), al2 = g2 - FC(FF_G2);
+  const double be0 = FC(FF_B0) - h0, be1 = FC(FF_B1) - h1, be2 = 2.0 * (FC(FF_B2) - h2);
+  const double H00 = FC(FF_H00), H01 = FC(FF_H01), H02 = FC(FF_H02), H11 = FC(FF_H11), H12 = FC(FF_H12),
+               H22 = FC(FF_H22);
+#undef FC
+  const double n0 = sc.K * (H00 * al0 + H01 * al1 + H02 * al2);
+  const double n1 = sc.K * (H01 * al0 + H11 * al1 + H12 * al2);
+  const double n2 = sc.K * (H02 * al0 + H12 * al1 + H22 * al2);
+  const double m0 = sc.D * (H00 * be0 + H01 * be1 + H02 * be2);
+  const double m1 = sc.D * (H01 * be0 + H11 * be1 + H12 * be2);
+  const double m2 = sc.D * (H02 * be0 + H12 * be1 + H22 * be2);
+  // sum_k m_k p_1k and sum_k m_k p_2k of eq. (A6) (ShellSystem.C:1223-1233)
+  double M[3], a2xa3[3], a3xa1[3], Mxa2[3], a1xM[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) M[c] = m0 * v1[c] + m1 * v2[c] + 2.0 * m2 * v3[c];
+  const double sm = m0 * h0 + m1 * h1 + 2.0 * m2 * h2;
+  cross3(a2, a3, a2xa3);
+  cross3(a3, a1, a3xa1);
+  cross3(M, a2, Mxa2);
+  cross3(a1, M, a1xM);
+  // pressure vector (ShellSystem.C:1509-1568)
+  double pv[3] = {0.0, 0.0, 0.0};
+  if (pressure != 0.0) {
+    switch (sc.pressure_base) {
+      case SHL_CS_LOCAL: pv[0] = a3[0]; pv[1] = a3[1]; pv[2] = a3[2]; break;
+      case SHL_CS_CARTESIAN: pv[sc.pressure_dir] = 1.0; break;
+      case SHL_CS_CYLINDRICAL:
+        if (sc.pressure_dir == 0) {
+          pv[0] = 1.0;
+        } else {
+          const double inv_r = 1.0 / sqrt(xq[1] * xq[1] + xq[2] * xq[2]);
+          if (isfinite(inv_r)) { pv[1] = inv_r * xq[1]; pv[2] = inv_r * xq[2]; }
+        }
+        break;
+      case SHL_CS_SPHERICAL: {
+        const double r = sqrt(dot3(xq, xq));
+        if (r > 0) { const double ir = 1.0 / r; pv[0] = xq[0] * ir; pv[1] = xq[1] * ir; pv[2] = xq[2] * ir; }
+        break;
+      }
+      default: break;
+    }
+    pv[0] *= pressure; pv[1] *= pressure; pv[2] *= pressure;
+  }
+  if (vol_p != 0.0) {
+    pv[0] += a3[0] * vol_p; pv[1] += a3[1] * vol_p; pv[2] += a3[2] * vol_p;
+  }
+  // Y: the qp vectors multiplying phi, phi_1, phi_2, phi_11, phi_22, phi_12;
+  // Z = the same in the unrotated derivatives
+  double Z[6][3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    const double Y1 = JxW * (n0 * a1[c] + n2 * a2[c] + invjac * (Mxa2[c] + sm * a2xa3[c]));
+    const double Y2 = JxW * (n1 * a2[c] + n2 * a1[c] + invjac * (a1xM[c] + sm * a3xa1[c]));
+    const double Y11 = -JxW * m0 * a3[c];
+    const double Y22 = -JxW * m1 * a3[c];
+    const double Y12 = -2.0 * JxW * m2 * a3[c];
+    Z[0][c] = -JxW * pv[c];
+    Z[1][c] = R00 * Y1 + R01 * Y2;
+    Z[2][c] = R10 * Y1 + R11 * Y2;
+    Z[3][c] = c11a * Y11 + c22a * Y22 + c12a * Y12;
+    Z[4][c] = c11b * Y11 + c22b * Y22 + c12b * Y12;
+    Z[5][c] = c11c * Y11 + c22c * Y22 + c12c * Y12;
+  }
+  double* qe = b.qe + (size_t)i * 36;
+#pragma unroll
+  for (int s = 0; s < (NP > 0 ? NP : kMaxSlots); ++s) {
+    if (NP == 0 && s >= np) break;
+    double q[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      double t = B[6 * s] * Z[0][c];
+#pragma unroll
+      for (int k = 1; k < 6; ++k) t = fma(B[6 * s + k], Z[k][c], t);
+      q[c] = t;
+    }
+    qe[3 * s] = q[0];
+    qe[3 * s + 1] = q[1];
+    qe[3 * s + 2] = q[2];
+  }
+  ElemOut o;
+  o.etens = 0.5 * JxW * (n0 * al0 + n1 * al1 + n2 * al2);
+  o.ebend = 0.5 * JxW * (m0 * be0 + m1 * be1 + m2 * be2);
+  o.area = sc.qw * jac;
+  const double invdet = 1.0 / (g0 * g1 - g2 * g2);
+  o.kg = o.area * invdet * (h0 * h1 - h2 * h2);
+  o.km = o.area * invdet * 0.5 * (h0 * g1 + h1 * g0 - 2.0 * h2 * g2);
+  return o;
+}
+
+__global__ void __launch_bounds__(kBlock) k_elements(DevBuf b, StepConst sc) {
+  Ctl* ctl = b.ctl;
+  if (inactive(ctl)) return;
+  __shared__ double sh[kBlock / 32];
+  int g = 0;
+  while (g + 1 < c_n_groups && blockIdx.x >= c_groups[g + 1].block_start) ++g;
+  const GroupDesc gd = c_groups[g];
+  const uint32_t li = (blockIdx.x - gd.block_start) * blockDim.x + threadIdx.x;
+  ElemOut o{0, 0, 0, 0, 0};
+  const double pressure = ctl->pressure, vol_p = ctl->volume_pressure;
+  if (li < gd.count) {
+    const uint32_t i = gd.first + li;
+    const double* B = c_basis + gd.basis_off;
+    if (gd.n_slots == 12)
+      o = element_force<12>(i, 12, B, b, sc, pressure, vol_p);
+    else if (gd.n_slots == 11)
+      o = element_force<11>(i, 11, B, b, sc, pressure, vol_p);
+    else
+      o = element_force<0>(i, gd.n_slots, B, b, sc, pressure, vol_p);
+    const uint32_t e = __ldg(&b.perm[i]);
+    b.area[e] = o.area;
+    b.kG[e] = o.kg / o.area;
+    b.kM[e] = o.km / o.area;
+    b.etens[e] = o.etens / o.area;
+    b.ebend[e] = o.ebend / o.area;
+  }
+  const double s0 = block_sum(o.etens, sh);
+  const double s1 = block_sum(o.ebend, sh);
+  const double s2 = block_sum(o.kg, sh);
+  const double s3 = block_sum(o.km, sh);
+  const double s4 = block_sum(o.area, sh);
+  if (threadIdx.x == 0) {
+    double* pp = b.partial + (size_t)blockIdx.x * 8;
+    pp[0] = s0; pp[1] = s1; pp[2] = s2; pp[3] = s3; pp[4] = s4;
+  }
+  if (!last_block(&ctl->cnt[1])) return;
+  const int nb = gridDim.x;
+  const double t0 = sum_partials(b.partial, 0, nb, sh);
+  const double t1 = sum_partials(b.partial, 1, nb, sh);
+  const double t2 = sum_partials(b.partial, 2, nb, sh);
+  const double t3 = sum_partials(b.partial, 3, nb, sh);
+  const double t4 = sum_partials(b.partial, 4, nb, sh);
+  if (threadIdx.x == 0) {
+    ctl->Etens = t0; ctl->Ebend = t1; ctl->kGauss = t2; ctl->kMean = t3; ctl->area = t4;
+  }
+}
+
+// -------------------------------------------------------- contact force --
+// One candidate pair; ShellSystem.C:1803-1900.  Rounded operation by operation.
+__global__ void __launch_bounds__(kBlock) k_contact_force(DevBuf b, StepConst sc) {
+  Ctl* ctl = b.ctl;
+  if (inactive(ctl)) return;
+  __shared__ double sh[kBlock / 32];
+  const uint32_t n_pairs = ctl->n_pairs;
+  double eself = 0.0, efric = 0.0, nc = 0.0;
+  const double h = sc.thickness;
+  for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n_pairs; j += gridDim.x * blockDim.x) {
+    const uint32_t e[2] = {b.pe1[0][j], b.pe2[0][j]};
+    const double* P1[3];
+    const double* P2[3];
+    uint32_t nid[2][3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      nid[0][k] = b.tri[3 * (size_t)e[0] + k];
+      nid[1][k] = b.tri[3 * (size_t)e[1] + k];
+      P1[k] = b.p + 3 * (size_t)nid[0][k];
+      P2[k] = b.p + 3 * (size_t)nid[1][k];
+    }
+    shl_pair_geom g;
+    shl_pair_compute(P1, P2, &g);
+    b.pd2[0][j] = g.d2;
+    if (g.d2 <= 0.0) register_problem(ctl, SHL_CONTACT_PROBLEM);
+    double* out = b.pforce + 7 * (size_t)j;
+    if (g.d2 < sc.d2_friction) {
+      const double area_min = fmin(b.area[e[0]], b.area[e[1]]);
+      const double abs_dc = SHL_SQRT(g.d2);
+      const double depth = SHL_SUB(h, abs_dc);
+      double nrm[3];
+      for (int c = 0; c < 3; ++c) nrm[c] = SHL_DIV(g.dc[c], abs_dc);
+      const double stiffness = SHL_MUL(sc.stiff_density, area_min);
+      double f_normal = 0.0, es = 0.0, ef = 0.0;
+      if (depth > 0.0) {
+        nc += 1.0;
+        f_normal = SHL_MUL(SHL_MUL(SHL_MUL(stiffness, SHL_SUB(h, abs_dc)), 0.5), SHL_ADD(1.0, SHL_DIV(h, abs_dc)));
+        const double dep = SHL_SUB(h, abs_dc);
+        es = SHL_MUL(SHL_MUL(0.5, stiffness),
+                     SHL_ADD(SHL_SUB(SHL_MUL(SHL_MUL(0.5, dep), dep), SHL_MUL(dep, h)),
+                             SHL_MUL(SHL_MUL(h, h), log(SHL_DIV(h, abs_dc)))));
+      }
+      eself += es;
+      // relative velocity at the contact points (current velocity v)
+      const double uu[2] = {SHL_SUB(SHL_SUB(1.0, g.v[0]), g.w[0]), SHL_SUB(SHL_SUB(1.0, g.v[1]), g.w[1])};
+      double vrel[3];
+      for (int c = 0; c < 3; ++c) {
+        const double s2 = SHL_ADD(SHL_ADD(SHL_MUL(uu[1], b.v[3 * (size_t)nid[1][0] + c]),
+                                          SHL_MUL(g.v[1], b.v[3 * (size_t)nid[1][1] + c])),
+                                  SHL_MUL(g.w[1], b.v[3 * (size_t)nid[1][2] + c]));
+        const double s1 = SHL_ADD(SHL_ADD(SHL_MUL(uu[0], b.v[3 * (size_t)nid[0][0] + c]),
+                                          SHL_MUL(g.v[0], b.v[3 * (size_t)nid[0][1] + c])),
+                                  SHL_MUL(g.w[0], b.v[3 * (size_t)nid[0][2] + c]));
+        vrel[c] = SHL_SUB(s2, s1);
+      }
+      const double abs_v_normal = shl_v3_dot(vrel, nrm);
+      double fcon[3] = {0.0, 0.0, 0.0};
+      if (sc.friction) {
+        double cp[3];
+        for (int c = 0; c < 3; ++c)
+          cp[c] = SHL_ADD(SHL_ADD(SHL_ADD(SHL_MUL(uu[0], P1[0][c]), SHL_MUL(g.v[0], P1[1][c])), SHL_MUL(g.w[0], P1[2][c])),
+                          SHL_MUL(0.5, g.dc[c]));
+        int stick = b.pstick[0][j];
+        double orig[3] = {b.porig[0][3 * (size_t)j], b.porig[0][3 * (size_t)j + 1], b.porig[0][3 * (size_t)j + 2]};
+        shl_friction_apply(&ef, fcon, f_normal, nrm, vrel, abs_v_normal, sc.v_stop, sc.stiff_static_friction,
+                           sc.mu_s, sc.mu_d, sc.self_friction_damping, &stick, orig, cp);
+        b.pstick[0][j] = (uint8_t)stick;
+        b.porig[0][3 * (size_t)j] = orig[0];
+        b.porig[0][3 * (size_t)j + 1] = orig[1];
+        b.porig[0][3 * (size_t)j + 2] = orig[2];
+        efric += ef;
+      }
+      f_normal = SHL_SUB(f_normal, SHL_MUL(SHL_MUL(sc.self_damping, stiffness), abs_v_normal));
+      for (int c = 0; c < 3; ++c) fcon[c] = SHL_ADD(fcon[c], SHL_MUL(f_normal, nrm[c]));
+      out[0] = fcon[0]; out[1] = fcon[1]; out[2] = fcon[2];
+      out[3] = g.v[0]; out[4] = g.w[0]; out[5] = g.v[1]; out[6] = g.w[1];
+    } else {
+      b.porig[0][3 * (size_t)j] = 0.0;
+      b.porig[0][3 * (size_t)j + 1] = 0.0;
+      b.porig[0][3 * (size_t)j + 2] = 0.0;
+      b.pstick[0][j] = 0;
+      for (int c = 0; c < 7; ++c) out[c] = 0.0;
+    }
+  }
+  const double s0 = block_sum(eself, sh);
+  const double s1 = block_sum(efric, sh);
+  const double s2 = block_sum(nc, sh);
+  if (threadIdx.x == 0) {
+    double* pp = b.partial + (size_t)blockIdx.x * 8;
+    pp[5] = s0; pp[6] = s1; pp[7] = s2;
+  }
+  if (!last_block(&ctl->cnt[2])) return;
+  const int nb = gridDim.x;
+  const double t0 = sum_partials(b.partial, 5, nb, sh);
+  const double t1 = sum_partials(b.partial, 6, nb, sh);
+  const double t2 = sum_partials(b.partial, 7, nb, sh);
+  if (threadIdx.x == 0) {
+    ctl->Eself = t0;
+    ctl->Efric = t1;
+    ctl->Nc = (uint32_t)t2;
+  }
+}
+
+// ------------------------------------------------------ gather + correct --
+__global__ void __launch_bounds__(kBlock) k_gather_correct(DevBuf b, StepConst sc, int mode, double* f_out,
+                                                           double* a_out) {
+  // mode 0: eval (write f_out / a_out), mode 1: step corrector
+  Ctl* ctl = b.ctl;
+  if (inactive(ctl)) return;
+  __shared__ double sh[kBlock / 32];
+  const uint32_t n = blockIdx.x * blockDim.x + threadIdx.x;
+  double du2 = 0.0, ekin = 0.0;
+  if (n < sc.V) {
+    double f[3] = {0.0, 0.0, 0.0};
+    if (sc.contact) {
+      const uint32_t k0 = b.csr_ptr[n], k1 = b.csr_ptr[n + 1];
+      for (uint32_t k = k0; k < k1; ++k) {
+        const uint32_t ent = b.csr_ent[k];
+        const uint32_t j = ent >> 3, role = ent & 7u;
+        const int e = role >= 3 ? 1 : 0, kk = role - 3 * e;
+        const double* pf = b.pforce + 7 * (size_t)j;
+        const double vv = pf[3 + 2 * e], ww = pf[4 + 2 * e];
+        const double bary = kk == 0 ? (1.0 - vv - ww) : (kk == 1 ? vv : ww);
+        const double pref = e == 0 ? -0.5 : 0.5;
+        f[0] += bary * (pref * pf[0]);
+        f[1] += bary * (pref * pf[1]);
+        f[2] += bary * (pref * pf[2]);
+      }
+    }
+    const uint32_t g0 = b.gather_ptr[n], g1 = b.gather_ptr[n + 1];
+    for (uint32_t k = g0; k < g1; ++k) {
+      const double* q = b.qe + 3 * (size_t)__ldg(&b.gather_ent[k]);
+      f[0] -= q[0];
+      f[1] -= q[1];
+      f[2] -= q[2];
+    }
+    double d[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const size_t k = 3 * (size_t)n + c;
+      const double vp = b.vp[k];
+      const double ap = b.Minv[k] * (f[c] - b.C[k] * vp);
+      if (mode == 0) {
+        if (f_out) f_out[k] = f[c];
+        if (a_out) a_out[k] = ap;
+      } else {
+        const double up = __dadd_rn(__dmul_rn(sc.nm0, ap), b.up[k]);
+        const double vn = __dadd_rn(__dmul_rn(sc.nm7, ap), vp);
+        d[c] = __dsub_rn(up, b.u[k]);
+        b.u[k] = up;
+        b.v[k] = vn;
+        b.a[k] = ap;
+        b.p[k] = __dadd_rn(b.X[k], up);
+        ekin += vn * vn / b.Minv[k];
+      }
+    }
+    if (mode == 1) du2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+  }
+  if (mode == 0) return;
+  const double m = block_max(du2, sh);
+  const double ek = block_sum(0.5 * ekin, sh);
+  if (threadIdx.x == 0) {
+    b.partial[(size_t)blockIdx.x * 8] = m;
+    b.partial[(size_t)blockIdx.x * 8 + 1] = ek;
+  }
+  if (!last_block(&ctl->cnt[3])) return;
+  double mm = 0.0;
+  for (int k = threadIdx.x; k < (int)gridDim.x; k += blockDim.x) mm = fmax(mm, __ldcg(&b.partial[(size_t)k * 8]));
+  mm = block_max(mm, sh);
+  const double ekt = sum_partials(b.partial, 1, gridDim.x, sh);
+  if (threadIdx.x != 0) return;
+  ctl->Ekin = ekt;
+  // check_increment(true)
+  const double du_max = sqrt(mm);
+  if (isfinite(du_max)) {
+    ctl->du_sum = __dadd_rn(ctl->du_sum, __dmul_rn(2.0, du_max));
+    if (du_max == 0.0)
+      register_problem(ctl, SHL_NO_DISP_CHANGE);
+    else if (sc.contact && du_max > 0.5 * sc.thickness)
+      register_problem(ctl, SHL_LARGE_DISP);
+  } else {
+    register_problem(ctl, SHL_NOT_FINITE);
+  }
+  if (!isfinite(ekt)) register_problem(ctl, SHL_NOT_FINITE);
+  ctl->rebuild = (sc.contact && ctl->du_sum >= rebuild_tolerance(sc, ctl)) ? 1u : 0u;
+}
+
+// ------------------------------------------------------ volume, end step --
+__global__ void __launch_bounds__(kBlock) k_volume_end(DevBuf b, StepConst sc, int end_step) {
+  Ctl* ctl = b.ctl;
+  if (inactive(ctl)) return;
+  __shared__ double sh[kBlock / 32];
+  const uint32_t f = blockIdx.x * blockDim.x + threadIdx.x;
+  double det = 0.0;
+  if (f < sc.F) {
+    const double* q0 = b.p + 3 * (size_t)b.tri[3 * (size_t)f];
+    const double* q1 = b.p + 3 * (size_t)b.tri[3 * (size_t)f + 1];
+    const double* q2 = b.p + 3 * (size_t)b.tri[3 * (size_t)f + 2];
+    det = q0[0] * (q1[1] * q2[2] - q2[1] * q1[2]) - q1[0] * (q0[1] * q2[2] - q2[1] * q0[2]) +
+          q2[0] * (q0[1] * q1[2] - q1[1] * q0[2]);
+  }
+  const double s = block_sum(det, sh);
+  if (threadIdx.x == 0) b.partial[(size_t)blockIdx.x * 8] = s;
+  if (!last_block(&ctl->cnt[4])) return;
+  const double tot = sum_partials(b.partial, 0, gridDim.x, sh);
+  if (threadIdx.x != 0) return;
+  ctl->volume = fabs(tot / 6.0) - ctl->area * 0.5 * sc.thickness;
+  if (!end_step) return;
+  const double dt = sc.dt;
+  ctl->sum_dt += dt;
+  ctl->sum_area += dt * ctl->area;
+  ctl->sum_volume += dt * ctl->volume;
+  ctl->sum_Nc += dt * (double)ctl->Nc;
+  ctl->sum_Ekin += dt * ctl->Ekin;
+  ctl->sum_Etens += dt * ctl->Etens;
+  ctl->sum_Ebend += dt * ctl->Ebend;
+  ctl->sum_Eself += dt * ctl->Eself;
+  ctl->sum_Efric += dt * ctl->Efric;
+  ctl->sum_kGauss += dt * ctl->kGauss;
+  ctl->sum_kMean += dt * ctl->kMean;
+  const int pr = ctl->problem;
+  if (pr > ctl->worst_problem) ctl->worst_problem = pr;
+  if (pr > 0 && ctl->first_problem_step == 0) ctl->first_problem_step = ctl->time_step;
+  ctl->steps_done += 1;
+  if (pr >= SHL_STOP_SIM || (sc.stop_on_problem && pr > 0) || ctl->error) ctl->halted = 1;
+  ctl->problem = 0;
+}
+
+// ------------------------------------------------------------ utilities --
+// FP64 FMA throughput probe: 8 independent register chains per thread.
+__global__ void __launch_bounds__(256) k_fp64_peak(double* out, int iters, double b, double c) {
+  double a0 = threadIdx.x * 1e-9, a1 = a0 + 1e-3, a2 = a0 + 2e-3, a3 = a0 + 3e-3;
+  double a4 = a0 + 4e-3, a5 = a0 + 5e-3, a6 = a0 + 6e-3, a7 = a0 + 7e-3;
+  for (int i = 0; i < iters; ++i) {
+    a0 = fma(a0, b, c); a1 = fma(a1, b, c); a2 = fma(a2, b, c); a3 = fma(a3, b, c);
+    a4 = fma(a4, b, c); a5 = fma(a5, b, c); a6 = fma(a6, b, c); a7 = fma(a7, b, c);
+  }
+  const double s = ((a0 + a1) + (a2 + a3)) + ((a4 + a5) + (a6 + a7));
+  if (s == 1.2345678) out[blockIdx.x] = s;  // never true; keeps the chains live
+}
+
+// write a buffer larger than L2 so that the next launch starts with a cold cache
+__global__ void k_flush(uint4* buf, size_t n16, uint32_t tag) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n16; i += (size_t)gridDim.x * blockDim.x)
+    buf[i] = make_uint4(tag, (uint32_t)i, tag, (uint32_t)(i >> 32));
+}
+
+void launch_fp64_peak(double* out, int blocks, int iters, cudaStream_t s) {
+  k_fp64_peak<<<blocks, 256, 0, s>>>(out, iters, 0.9999999, 1e-9);
+}
+void launch_flush(void* buf, size_t bytes, uint32_t tag, cudaStream_t s) {
+  k_flush<<<4 * 152, 512, 0, s>>>((uint4*)buf, bytes / 16, tag);
+}
+
+// --------------------------------------------------------------- launch --
+static inline uint32_t nblk(uint32_t n) { return (n + kBlock - 1) / kBlock; }
+
+void launch_predict(const DevBuf& b, const StepConst& sc, int, cudaStream_t s) {
+  k_predict<<<nblk(sc.V), kBlock, 0, s>>>(b, sc);
+}
+void launch_positions(const DevBuf& b, const StepConst& sc, cudaStream_t s) {
+  k_positions<<<nblk(sc.V), kBlock, 0, s>>>(b, sc);
+}
+void launch_elements(const DevBuf& b, const StepConst& sc, uint32_t n_blocks, cudaStream_t s) {
+  k_elements<<<n_blocks, kBlock, 0, s>>>(b, sc);
+}
+void launch_contact_force(const DevBuf& b, const StepConst& sc, int, cudaStream_t s) {
+  uint32_t nb = nblk(sc.pairs_cap);
+  if (nb > 4 * 152) nb = 4 * 152;
+  if (nb == 0) nb = 1;
+  k_contact_force<<<nb, kBlock, 0, s>>>(b, sc);
+}
+void launch_gather_correct(const DevBuf& b, const StepConst& sc, int, bool correct, double* f_out, double* a_out,
+                           cudaStream_t s) {
+  k_gather_correct<<<nblk(sc.V), kBlock, 0, s>>>(b, sc, correct ? 1 : 0, f_out, a_out);
+}
+void launch_volume_end_step(const DevBuf& b, const StepConst& sc, bool end_step, cudaStream_t s) {
+  k_volume_end<<<nblk(sc.F), kBlock, 0, s>>>(b, sc, end_step ? 1 : 0);
+}
+
+}  // namespace shl

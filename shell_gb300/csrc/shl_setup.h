@@ -1,0 +1,81 @@
+// shl_setup.h -- host-side set-up of the shell library (internal).
+//
+// Everything the reference computes once in ShellSystem::set_parameters /
+// build_cache / compute_mass_damping (ShellSystem.C:170-852) is computed here on
+// the host, laid out for the device kernels:
+//   * faces reordered so that the regular 12-node patches come first and the
+//     irregular (valence != 6) patches follow, grouped by valence;
+//   * patch node ids slot-major (patch[slot * n_faces + face]) for coalesced loads;
+//   * one universal table of unrotated basis values per patch type (the basis
+//     at the quadrature point (1/3,1/3) is the same for every face of a type),
+//     plus per face the 2x2 rotation R of reinit_mod (ShellSystem.C:3321-3499);
+//   * per-face reference metric and orthotropic H, structure of arrays;
+//   * lumped masses / damping, the gather CSR (node -> (face, slot) entries in
+//     ascending order) and the topological exclusion CSR (close_elems).
+#ifndef SHL_SETUP_H_
+#define SHL_SETUP_H_
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/shl.h"
+
+namespace shl {
+
+// Number of per-face FP64 constants (structure of arrays, field-major).
+enum FaceField {
+  FF_R00, FF_R01, FF_R10, FF_R11,  // rotation onto the material frame
+  FF_JXW,                          // Jacobian x weight of the first map
+  FF_X0, FF_X1, FF_X2,             // quadrature point, reference
+  FF_A10, FF_A11, FF_A12,          // a_ref.vec[0]
+  FF_A20, FF_A21, FF_A22,          // a_ref.vec[1]
+  FF_D10, FF_D11, FF_D12,          // a_ref.dvec[0]  (d2x/ds1^2)
+  FF_D20, FF_D21, FF_D22,          // a_ref.dvec[1]  (d2x/ds2^2)
+  FF_D30, FF_D31, FF_D32,          // a_ref.dvec[2]  (d2x/ds1ds2)
+  FF_G0, FF_G1, FF_G2,             // a_ref.ff1 (Voigt, no factor 2)
+  FF_B0, FF_B1, FF_B2,             // a_ref.ff2
+  FF_H00, FF_H01, FF_H02, FF_H11, FF_H12, FF_H22,  // orthotropic H incl. 1/det^2
+  FF_COUNT
+};
+
+struct PatchGroup {
+  int valence;        // valence of the first vertex (6 = regular)
+  int n_slots;        // valence + 6
+  uint32_t first;     // first internal face of the group
+  uint32_t count;     // faces in the group
+  std::vector<double> basis;  // n_slots x 6 (phi, d/dv, d/dw, d2/dv2, d2/dw2, d2/dvdw)
+};
+
+struct Setup {
+  uint32_t V = 0, F = 0;
+  std::vector<double> X;           // 3V node-major
+  std::vector<uint32_t> tri;       // 3F original order
+  std::vector<uint32_t> perm;      // internal face -> original face id
+  std::vector<uint32_t> inv_perm;  // original -> internal
+  std::vector<PatchGroup> groups;  // groups[0] = regular
+  std::vector<int32_t> patch;      // [slot * F + internal face], -1 for unused slots
+  std::vector<double> face;        // [field * F + internal face]
+  std::vector<double> Minv, C;     // 3V node-major
+  std::vector<uint32_t> gather_ptr;  // V+1
+  std::vector<uint32_t> gather_ent;  // internal_face * 12 + slot, ascending per node
+  std::vector<uint32_t> close_ptr;   // F+1 (original ids)
+  std::vector<uint32_t> close_list;  // sorted original ids
+  uint64_t n_cells_max = 0;
+  // derived constants (update_derived, ShellSystem.C:421-487)
+  double K = 0, D = 0, stiff_density = 0, stiff_static_friction = 0, d2_friction = 0;
+};
+
+// Builds everything; returns false with a message on unsupported input.
+bool build_setup(const shl_mesh& mesh, const shl_params& p, Setup& out, std::string& err);
+
+// Loop box-spline basis of a regular patch at (v, w) in this library's patch
+// order; out[6*slot + k].  Exposed for tests through the C ABI helpers.
+void regular_basis(double v, double w, double* out);
+// Basis of a patch whose first vertex has valence n at the quadrature point
+// of the middle sub-triangle; out[6*slot + k] for n + 6 slots.
+void irregular_basis(int n, double v, double w, double* out);
+
+}  // namespace shl
+
+#endif

@@ -1,0 +1,346 @@
+"""ctypes binding of the C ABI in include/shl.h (libshl_gb300.so).
+
+This is the Python side of the drop-in boundary: the structures mirror shl.h
+field by field and `Shell` mirrors the ShellSystem methods a host driver calls
+(set_parameters/build_cache -> Shell(...), apply_initial_conditions, advance,
+save/load state).  The library is loaded from the in-tree build directory; if
+it is missing the import fails loudly (there is no fallback implementation).
+"""
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libshl_gb300.so")
+
+# shl_status
+SHL_OK = 0
+PROBLEMS = {0: "NO_PROBLEM", 1: "NO_DISP_CHANGE", 2: "LARGE_DISP", 3: "STOP_SIM", 4: "TOO_MANY_CELLS",
+            5: "SMALL_TIMESTEP", 6: "CONTACT_PROBLEM", 7: "NOT_FINITE"}
+SHL_ERR_ARG, SHL_ERR_CUDA, SHL_ERR_TIMEOUT, SHL_ERR_OOM, SHL_ERR_CAPACITY = 100, 101, 102, 103, 104
+CONTACT_LINEAR, CONTACT_SMOOTH, CONTACT_NONE = 0, 1, 2
+CS_LOCAL, CS_CARTESIAN, CS_CYLINDRICAL, CS_SPHERICAL = 0, 1, 2, 3
+PREC_FP64, PREC_FP32 = 0, 1
+
+_d, _i32, _u32 = ctypes.c_double, ctypes.c_int32, ctypes.c_uint32
+
+
+class ShlMesh(ctypes.Structure):
+    _fields_ = [("n_nodes", _u32), ("n_faces", _u32), ("xyz", ctypes.c_void_p), ("faces", ctypes.c_void_p)]
+
+
+_PARAM_FIELDS = (
+    [(n, _d) for n in ("shell_mass_density", "shell_young_modulus", "shell_young_modulus2", "shell_poisson_ratio",
+                       "shell_shear_modulus", "bulk_modulus", "memb_stiff_mult", "bend_stiff_mult", "thickness",
+                       "damping_alpha", "damping_beta", "damping_gamma", "pressure")]
+    + [("pressure_base", _i32), ("pressure_dir", _i32), ("shell_shell_contact", _i32), ("pad0", _i32)]
+    + [(n, _d) for n in ("mu_s", "mu_d", "self_damping", "self_friction_damping", "fric_stiff_mult",
+                       "friction_stop_velocity", "static_friction_tol", "cell_size_mult", "cell_margin",
+                       "neighbor_margin", "dt", "newmark_beta", "newmark_gamma")]
+    + [("compat_zero_pressure", _i32), ("precision", _i32), ("stop_on_problem", _i32), ("pad1", _i32)]
+)
+
+
+class ShlParams(ctypes.Structure):
+    _fields_ = _PARAM_FIELDS
+
+    def as_dict(self):
+        return {n: getattr(self, n) for n, _ in _PARAM_FIELDS if not n.startswith("pad")}
+
+
+class ShlEnergies(ctypes.Structure):
+    _fields_ = [(n, _d) for n in ("Etens", "Ebend", "Eself", "Efric", "Ekin", "area", "volume", "kGauss", "kMean")] + [
+        ("Nc", _u32), ("n_pairs", _u32)]
+
+    def as_dict(self):
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
+class ShlStepReport(ctypes.Structure):
+    _fields_ = [("steps_done", _u32), ("worst_problem", _i32), ("time", _d), ("du_sum", _d), ("n_rebuilds", _u32),
+                ("pad", _u32), ("last", ShlEnergies)] + [
+        (n, _d) for n in ("sum_dt", "sum_area", "sum_volume", "sum_Nc", "sum_Ekin", "sum_Etens", "sum_Ebend",
+                          "sum_Eself", "sum_Efric", "sum_kGauss", "sum_kMean")]
+
+
+_lib = None
+
+
+def load():
+    """Load libshl_gb300.so (raises if it was not built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError("libshl_gb300.so is not built (run `python -m shell_gb300.build`): %s" % LIB_PATH)
+    lib = ctypes.CDLL(LIB_PATH)
+    vp, sz = ctypes.c_void_p, ctypes.c_size_t
+    sig = {
+        "shl_version": (ctypes.c_char_p, []),
+        "shl_last_error": (ctypes.c_char_p, []),
+        "shl_status_string": (ctypes.c_char_p, [_i32]),
+        "shl_create": (_i32, [ctypes.POINTER(ShlMesh), ctypes.POINTER(ShlParams), ctypes.POINTER(vp)]),
+        "shl_destroy": (None, [vp]),
+        "shl_apply_initial_conditions": (_i32, [vp, vp, _d, _d]),
+        "shl_set_state": (_i32, [vp, vp, vp, vp]),
+        "shl_get_state": (_i32, [vp, vp, vp, vp]),
+        "shl_set_time": (_i32, [vp, _d, _u32]),
+        "shl_get_time": (_i32, [vp, ctypes.POINTER(_d), ctypes.POINTER(_u32)]),
+        "shl_eval_forces": (_i32, [vp, vp, vp, _d, vp, vp, ctypes.POINTER(ShlEnergies)]),
+        "shl_step": (_i32, [vp, _u32, vp, ctypes.c_int, ctypes.POINTER(ShlStepReport)]),
+        "shl_get_contact_pairs": (_i32, [vp, vp, sz, ctypes.POINTER(sz)]),
+        "shl_get_contact_state": (_i32, [vp, vp, vp, vp, vp, sz, ctypes.POINTER(sz), ctypes.POINTER(_d)]),
+        "shl_set_contact_state": (_i32, [vp, vp, vp, vp, vp, sz, _d]),
+        "shl_rebuild_contacts": (_i32, [vp]),
+        "shl_get_element_fields": (_i32, [vp, vp, vp, vp, vp, vp]),
+        "shl_get_mass_damping": (_i32, [vp, vp, vp]),
+        "shl_icosphere": (_i32, [_u32, vp, sz, vp, sz, ctypes.POINTER(_u32), ctypes.POINTER(_u32)]),
+        "shl_icosphere_off": (_i32, [_u32, vp, sz, ctypes.POINTER(sz)]),
+        "shl_read_off": (_i32, [ctypes.c_char_p, vp, sz, vp, sz, ctypes.POINTER(_u32), ctypes.POINTER(_u32)]),
+        "shl_gaussian_normal_imperfection": (_i32, [vp, _u32, _d, ctypes.c_uint64, vp]),
+        "shl_params_default": (None, [ctypes.POINTER(ShlParams)]),
+        "shl_get_stream": (_i32, [vp, ctypes.POINTER(vp)]),
+        "shl_upload_pressure_table": (_i32, [vp, vp, _u32]),
+        "shl_step_enqueue": (_i32, [vp, _u32]),
+        "shl_step_collect": (_i32, [vp, ctypes.POINTER(ShlStepReport)]),
+        "shl_time_kernel": (_i32, [vp, ctypes.c_int, ctypes.c_int, sz, ctypes.POINTER(_d)]),
+        "shl_measure_fp64_peak": (_i32, [ctypes.POINTER(_d)]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def exported_symbols():
+    """Names declared in include/shl.h (for the export check)."""
+    return ["shl_version", "shl_last_error", "shl_status_string", "shl_create", "shl_destroy",
+            "shl_apply_initial_conditions", "shl_set_state", "shl_get_state", "shl_set_time", "shl_get_time",
+            "shl_eval_forces", "shl_step", "shl_get_contact_pairs", "shl_get_contact_state",
+            "shl_set_contact_state", "shl_rebuild_contacts", "shl_get_element_fields", "shl_get_mass_damping",
+            "shl_icosphere", "shl_icosphere_off", "shl_read_off", "shl_gaussian_normal_imperfection",
+            "shl_params_default", "shl_get_stream", "shl_upload_pressure_table", "shl_step_enqueue",
+            "shl_step_collect", "shl_time_kernel", "shl_measure_fp64_peak"]
+
+
+class ShlError(RuntimeError):
+    def __init__(self, status, where):
+        lib = load()
+        msg = lib.shl_status_string(status).decode()
+        detail = lib.shl_last_error().decode()
+        super().__init__("%s: status %d (%s) %s" % (where, status, msg, detail))
+        self.status = status
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data
+
+
+def _check(status, where, allow_problem=True):
+    if status >= 100 or (status != 0 and not allow_problem):
+        raise ShlError(status, where)
+    return status
+
+
+def default_params(**kw):
+    lib = load()
+    p = ShlParams()
+    lib.shl_params_default(ctypes.byref(p))
+    for k, v in kw.items():
+        if not hasattr(p, k):
+            raise KeyError(k)
+        setattr(p, k, v)
+    return p
+
+
+def icosphere(level):
+    """Closed icosphere mesh (node xyz (V,3) float64, faces (F,3) uint32)."""
+    lib = load()
+    nv, nf = _u32(), _u32()
+    _check(lib.shl_icosphere(level, None, 0, None, 0, ctypes.byref(nv), ctypes.byref(nf)), "shl_icosphere")
+    X = np.zeros((nv.value, 3))
+    T = np.zeros((nf.value, 3), dtype=np.uint32)
+    _check(lib.shl_icosphere(level, X.ctypes.data, nv.value, T.ctypes.data, nf.value, ctypes.byref(nv),
+                             ctypes.byref(nf)), "shl_icosphere")
+    return X, T
+
+
+def icosphere_off(level):
+    lib = load()
+    n = ctypes.c_size_t()
+    _check(lib.shl_icosphere_off(level, None, 0, ctypes.byref(n)), "shl_icosphere_off")
+    buf = ctypes.create_string_buffer(n.value + 1)
+    _check(lib.shl_icosphere_off(level, buf, n.value + 1, ctypes.byref(n)), "shl_icosphere_off")
+    return buf.value.decode()
+
+
+def read_off(path):
+    lib = load()
+    nv, nf = _u32(), _u32()
+    _check(lib.shl_read_off(path.encode(), None, 0, None, 0, ctypes.byref(nv), ctypes.byref(nf)), "shl_read_off")
+    X = np.zeros((nv.value, 3))
+    T = np.zeros((nf.value, 3), dtype=np.uint32)
+    _check(lib.shl_read_off(path.encode(), X.ctypes.data, nv.value, T.ctypes.data, nf.value, ctypes.byref(nv),
+                            ctypes.byref(nf)), "shl_read_off")
+    return X, T
+
+
+def gaussian_normal_imperfection(X, amplitude, seed):
+    lib = load()
+    X = np.ascontiguousarray(X, dtype=np.float64)
+    u = np.zeros_like(X)
+    _check(lib.shl_gaussian_normal_imperfection(X.ctypes.data, X.shape[0], amplitude, seed, u.ctypes.data),
+           "shl_gaussian_normal_imperfection")
+    return u
+
+
+def measure_fp64_peak():
+    lib = load()
+    t = _d()
+    _check(lib.shl_measure_fp64_peak(ctypes.byref(t)), "shl_measure_fp64_peak", False)
+    return t.value
+
+
+def make_mesh(X, T):
+    X = np.ascontiguousarray(X, dtype=np.float64)
+    T = np.ascontiguousarray(T, dtype=np.uint32)
+    m = ShlMesh(X.shape[0], T.shape[0], X.ctypes.data, T.ctypes.data)
+    return m, (X, T)
+
+
+class Shell:
+    """One shell on the current CUDA device (mirror of ShellSystem's step API)."""
+
+    def __init__(self, X, T, params):
+        lib = load()
+        self.lib = lib
+        self.params = params
+        m, keep = make_mesh(X, T)
+        self.X, self.T = keep
+        self.V, self.F = self.X.shape[0], self.T.shape[0]
+        h = ctypes.c_void_p()
+        _check(lib.shl_create(ctypes.byref(m), ctypes.byref(params), ctypes.byref(h)), "shl_create", False)
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.shl_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # --- ShellSystem::apply_initial_conditions
+    def apply_initial_conditions(self, u0, t0=0.0, pressure_next=None):
+        u0 = np.ascontiguousarray(u0, dtype=np.float64).reshape(-1)
+        p = self.params.pressure if pressure_next is None else pressure_next
+        return _check(self.lib.shl_apply_initial_conditions(self.h, u0.ctypes.data, t0, p),
+                      "shl_apply_initial_conditions")
+
+    def set_state(self, u=None, v=None, a=None):
+        arrs = [None if x is None else np.ascontiguousarray(x, dtype=np.float64).reshape(-1) for x in (u, v, a)]
+        return _check(self.lib.shl_set_state(self.h, *[_ptr(x) for x in arrs]), "shl_set_state", False)
+
+    def get_state(self):
+        u, v, a = (np.zeros(3 * self.V) for _ in range(3))
+        _check(self.lib.shl_get_state(self.h, u.ctypes.data, v.ctypes.data, a.ctypes.data), "shl_get_state", False)
+        return u, v, a
+
+    def set_time(self, t, step):
+        _check(self.lib.shl_set_time(self.h, t, step), "shl_set_time", False)
+
+    def get_time(self):
+        t, s = _d(), _u32()
+        _check(self.lib.shl_get_time(self.h, ctypes.byref(t), ctypes.byref(s)), "shl_get_time", False)
+        return t.value, s.value
+
+    def eval_forces(self, u_pred, v_pred, pressure):
+        u_pred = np.ascontiguousarray(u_pred, dtype=np.float64).reshape(-1)
+        v_pred = np.ascontiguousarray(v_pred, dtype=np.float64).reshape(-1)
+        f = np.zeros(3 * self.V)
+        a = np.zeros(3 * self.V)
+        e = ShlEnergies()
+        st = _check(self.lib.shl_eval_forces(self.h, u_pred.ctypes.data, v_pred.ctypes.data, pressure, f.ctypes.data,
+                                             a.ctypes.data, ctypes.byref(e)), "shl_eval_forces")
+        return f, a, e.as_dict(), st
+
+    # --- n x ShellSystem::advance
+    def step(self, n, pressure_table=None, use_graph=True):
+        r = ShlStepReport()
+        pt = None if pressure_table is None else np.ascontiguousarray(pressure_table, dtype=np.float64)
+        st = _check(self.lib.shl_step(self.h, n, _ptr(pt), 1 if use_graph else 0, ctypes.byref(r)), "shl_step")
+        return r, st
+
+    # --- asynchronous stepping (CUDA-event timing on the context stream)
+    def stream_handle(self):
+        h = ctypes.c_void_p()
+        _check(self.lib.shl_get_stream(self.h, ctypes.byref(h)), "shl_get_stream", False)
+        return h.value or 0
+
+    def upload_pressure_table(self, table):
+        t = np.ascontiguousarray(table, dtype=np.float64)
+        _check(self.lib.shl_upload_pressure_table(self.h, t.ctypes.data, t.size), "shl_upload_pressure_table", False)
+
+    def step_enqueue(self, n):
+        _check(self.lib.shl_step_enqueue(self.h, n), "shl_step_enqueue", False)
+
+    def step_collect(self):
+        r = ShlStepReport()
+        st = _check(self.lib.shl_step_collect(self.h, ctypes.byref(r)), "shl_step_collect")
+        return r, st
+
+    def time_kernel(self, which, reps=20, flush_bytes=0):
+        ms = _d()
+        _check(self.lib.shl_time_kernel(self.h, which, reps, flush_bytes, ctypes.byref(ms)), "shl_time_kernel", False)
+        return ms.value
+
+    def contact_state(self):
+        n = ctypes.c_size_t()
+        du = _d()
+        _check(self.lib.shl_get_contact_state(self.h, None, None, None, None, 0, ctypes.byref(n), ctypes.byref(du)),
+               "shl_get_contact_state", False)
+        k = n.value
+        pairs = np.zeros((k, 2), dtype=np.uint32)
+        stick = np.zeros(k, dtype=np.uint8)
+        orig = np.zeros((k, 3))
+        d2 = np.zeros(k)
+        if k:
+            _check(self.lib.shl_get_contact_state(self.h, pairs.ctypes.data, stick.ctypes.data, orig.ctypes.data,
+                                                  d2.ctypes.data, k, ctypes.byref(n), ctypes.byref(du)),
+                   "shl_get_contact_state", False)
+        return {"pairs": pairs, "stick": stick, "origin": orig, "d2": d2, "du_sum": du.value}
+
+    def set_contact_state(self, pairs, stick=None, origin=None, d2=None, du_sum=0.0):
+        pairs = np.ascontiguousarray(pairs, dtype=np.uint32).reshape(-1, 2)
+        k = pairs.shape[0]
+        stick = None if stick is None else np.ascontiguousarray(stick, dtype=np.uint8)
+        origin = None if origin is None else np.ascontiguousarray(origin, dtype=np.float64)
+        d2 = None if d2 is None else np.ascontiguousarray(d2, dtype=np.float64)
+        _check(self.lib.shl_set_contact_state(self.h, pairs.ctypes.data, _ptr(stick), _ptr(origin), _ptr(d2), k,
+                                              du_sum), "shl_set_contact_state", False)
+
+    def rebuild_contacts(self):
+        return _check(self.lib.shl_rebuild_contacts(self.h), "shl_rebuild_contacts")
+
+    def element_fields(self):
+        out = [np.zeros(self.F) for _ in range(5)]
+        _check(self.lib.shl_get_element_fields(self.h, *[o.ctypes.data for o in out]), "shl_get_element_fields",
+               False)
+        return dict(zip(("kGauss", "kMean", "etens", "ebend", "area"), out))
+
+    def mass_damping(self):
+        Minv, C = np.zeros(3 * self.V), np.zeros(3 * self.V)
+        _check(self.lib.shl_get_mass_damping(self.h, Minv.ctypes.data, C.ctypes.data), "shl_get_mass_damping", False)
+        return Minv, C
