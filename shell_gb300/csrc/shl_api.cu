@@ -45,6 +45,7 @@ struct shl_ctx {
   DevBuf b{};
   StepConst sc{};
   uint32_t elem_blocks = 0;
+  ElemGroups eg{};
   std::vector<void*> allocs;
   cudaGraphExec_t graph = nullptr;
   cudaGraphExec_t graph1 = nullptr;
@@ -178,7 +179,7 @@ void enqueue_step(shl_ctx* c) {
   cudaStream_t s = c->stream;
   launch_predict(b, sc, 0, s);
   if (sc.contact) launch_rebuild(b, sc, s);
-  launch_elements(b, sc, c->elem_blocks, s);
+  launch_elements(b, sc, c->eg, c->elem_blocks, s);
   if (sc.contact) launch_contact_force(b, sc, 0, s);
   launch_gather_correct(b, sc, 0, true, nullptr, nullptr, s);
   if (sc.contact) launch_rebuild(b, sc, s);
@@ -331,7 +332,14 @@ shl_status shl_create(const shl_mesh* mesh, const shl_params* params, shl_ctx** 
     if (!S.close_list.empty() && (st = upload(c, b.close_list, S.close_list.data(), S.close_list.size())) != SHL_OK)
       return fail(st);
   }
-  upload_groups(gd.data(), (int)gd.size(), basis.data(), (int)basis.size());
+  {
+    double* d_basis = nullptr;
+    if ((st = dev_alloc(c, &d_basis, basis.size())) != SHL_OK) return fail(st);
+    if ((st = upload(c, d_basis, basis.data(), basis.size())) != SHL_OK) return fail(st);
+    c->eg.n = (int32_t)gd.size();
+    for (size_t k = 0; k < gd.size(); ++k) c->eg.g[k] = gd[k];
+    c->eg.basis = d_basis;
+  }
 
   // step constants
   StepConst& sc = c->sc;
@@ -451,7 +459,7 @@ shl_status begin_eval(shl_ctx* c, double pressure, bool allow_rebuild) {
 shl_status eval_into(shl_ctx* c, double* d_f, double* d_a) {
   const DevBuf& b = c->b;
   if (c->sc.contact) launch_rebuild(b, c->sc, c->stream);
-  launch_elements(b, c->sc, c->elem_blocks, c->stream);
+  launch_elements(b, c->sc, c->eg, c->elem_blocks, c->stream);
   if (c->sc.contact) launch_contact_force(b, c->sc, 0, c->stream);
   launch_gather_correct(b, c->sc, 0, false, d_f, d_a, c->stream);
   return check_launch("force evaluation");
@@ -511,7 +519,7 @@ shl_status shl_apply_initial_conditions(shl_ctx* c, const double* u0, double t0,
   SHL_TRY(ctl_put(c, h));
   // bounding boxes + first candidate list, then deformed metrics and volume
   if (c->sc.contact) launch_rebuild(c->b, c->sc, c->stream);
-  launch_elements(c->b, c->sc, c->elem_blocks, c->stream);
+  launch_elements(c->b, c->sc, c->eg, c->elem_blocks, c->stream);
   launch_volume_end_step(c->b, c->sc, false, c->stream);
   SHL_TRY(check_launch("initial conditions"));
   SHL_TRY(ctl_get(c, h));
@@ -671,7 +679,7 @@ shl_status shl_time_kernel(shl_ctx* c, int which, int reps, size_t flush_bytes, 
     if (flush_bytes) launch_flush(c->d_flush, flush_bytes, (uint32_t)r, c->stream);
     cudaEventRecord(e0, c->stream);
     if (which == 0)
-      launch_elements(c->b, c->sc, c->elem_blocks, c->stream);
+      launch_elements(c->b, c->sc, c->eg, c->elem_blocks, c->stream);
     else
       launch_gather_correct(c->b, c->sc, 0, false, c->d_fa, c->d_fa + nd, c->stream);
     cudaEventRecord(e1, c->stream);

@@ -39,6 +39,14 @@ struct GroupDesc {
   int32_t basis_off;    // offset into the basis table (doubles)
 };
 
+// All patch groups of one shell, passed by value to the element kernel; the
+// basis tables live in device memory (per context).
+struct ElemGroups {
+  GroupDesc g[kMaxGroups];
+  int32_t n;
+  const double* basis;
+};
+
 // Control block in device memory.
 struct Ctl {
   // time stepping
@@ -141,13 +149,13 @@ struct DevBuf {
 
 // ---- launchers (shl_kernels.cu) ----
 void launch_predict(const DevBuf& b, const StepConst& sc, int cur, cudaStream_t s);
-void launch_elements(const DevBuf& b, const StepConst& sc, uint32_t n_blocks, cudaStream_t s);
+void launch_elements(const DevBuf& b, const StepConst& sc, const ElemGroups& eg, uint32_t n_blocks,
+                     cudaStream_t s);
 void launch_contact_force(const DevBuf& b, const StepConst& sc, int cur, cudaStream_t s);
 void launch_gather_correct(const DevBuf& b, const StepConst& sc, int cur, bool correct, double* f_out,
                            double* a_out, cudaStream_t s);
 void launch_volume_end_step(const DevBuf& b, const StepConst& sc, bool end_step, cudaStream_t s);
 void launch_positions(const DevBuf& b, const StepConst& sc, cudaStream_t s);
-void upload_groups(const GroupDesc* g, int n, const double* basis, int n_basis);
 void launch_fp64_peak(double* out, int blocks, int iters, cudaStream_t s);
 void launch_flush(void* buf, size_t bytes, uint32_t tag, cudaStream_t s);
 

@@ -26,15 +26,6 @@
 
 namespace shl {
 
-__constant__ GroupDesc c_groups[kMaxGroups];
-__constant__ int c_n_groups;
-__constant__ double c_basis[kMaxGroups * kMaxSlots * 6];
-
-void upload_groups(const GroupDesc* g, int n, const double* basis, int n_basis) {
-  cudaMemcpyToSymbol(c_groups, g, sizeof(GroupDesc) * n);
-  cudaMemcpyToSymbol(c_n_groups, &n, sizeof(int));
-  cudaMemcpyToSymbol(c_basis, basis, sizeof(double) * n_basis);
-}
 
 // ---------------------------------------------------------------- helpers --
 
@@ -327,19 +318,23 @@ __device__ __forceinline__ ElemOut element_force(uint32_t i, int np_rt, const do
   return o;
 }
 
-__global__ void __launch_bounds__(kBlock) k_elements(DevBuf b, StepConst sc) {
+__global__ void __launch_bounds__(kBlock) k_elements(DevBuf b, StepConst sc, ElemGroups eg) {
   Ctl* ctl = b.ctl;
   if (inactive(ctl)) return;
   __shared__ double sh[kBlock / 32];
+  __shared__ double sB[kMaxSlots * 6];
   int g = 0;
-  while (g + 1 < c_n_groups && blockIdx.x >= c_groups[g + 1].block_start) ++g;
-  const GroupDesc gd = c_groups[g];
+  while (g + 1 < eg.n && blockIdx.x >= eg.g[g + 1].block_start) ++g;
+  const GroupDesc gd = eg.g[g];
+  // the block's basis table (all threads of a block belong to one group)
+  for (int k = threadIdx.x; k < gd.n_slots * 6; k += blockDim.x) sB[k] = eg.basis[gd.basis_off + k];
+  __syncthreads();
   const uint32_t li = (blockIdx.x - gd.block_start) * blockDim.x + threadIdx.x;
   ElemOut o{0, 0, 0, 0, 0};
   const double pressure = ctl->pressure, vol_p = ctl->volume_pressure;
   if (li < gd.count) {
     const uint32_t i = gd.first + li;
-    const double* B = c_basis + gd.basis_off;
+    const double* B = sB;
     if (gd.n_slots == 12)
       o = element_force<12>(i, 12, B, b, sc, pressure, vol_p);
     else if (gd.n_slots == 11)
@@ -637,8 +632,9 @@ void launch_predict(const DevBuf& b, const StepConst& sc, int, cudaStream_t s) {
 void launch_positions(const DevBuf& b, const StepConst& sc, cudaStream_t s) {
   k_positions<<<nblk(sc.V), kBlock, 0, s>>>(b, sc);
 }
-void launch_elements(const DevBuf& b, const StepConst& sc, uint32_t n_blocks, cudaStream_t s) {
-  k_elements<<<n_blocks, kBlock, 0, s>>>(b, sc);
+void launch_elements(const DevBuf& b, const StepConst& sc, const ElemGroups& eg, uint32_t n_blocks,
+                     cudaStream_t s) {
+  k_elements<<<n_blocks, kBlock, 0, s>>>(b, sc, eg);
 }
 void launch_contact_force(const DevBuf& b, const StepConst& sc, int, cudaStream_t s) {
   uint32_t nb = nblk(sc.pairs_cap);

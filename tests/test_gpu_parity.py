@@ -3,7 +3,8 @@
 Tolerances: forces, accelerations and energies of one evaluation within 1e-12
 relative (2-norm of the difference over the 2-norm of the oracle vector), the
 contact candidate list bit-exact (same pairs, same FP64 squared distances),
-friction stick flags identical.  Trajectories agree to 1e-9 relative after
+friction stick flags identical, spring origins within 1e-12 relative (they
+depend on element areas computed by the fused-multiply-add element kernel).  Trajectories agree to 1e-9 relative after
 tens of steps (roundoff of the element kernel's fused multiply-adds grows
 slowly in time); run-to-run the GPU is bitwise deterministic.
 """
@@ -63,9 +64,9 @@ def test_eval_forces_no_contact(cuda_ok, meshes, level, pressure_base):
     assert rel(ag, ao) < FORCE_TOL
     for k in ("Etens", "Ebend", "area"):
         assert abs(eg[k] - eo[k]) <= FORCE_TOL * abs(eo[k]), k
-    # per-element fields
+    # per-element fields of the evaluation (curvatures belong to the step's measurement)
     fe_g, fe_o = g.element_fields(), o.element_fields()
-    for k in ("kGauss", "kMean", "etens", "ebend", "area"):
+    for k in ("etens", "ebend", "area"):
         assert rel(fe_g[k], fe_o[k]) < 1e-11, k
     g.close()
 
@@ -101,7 +102,10 @@ def test_eval_forces_contact_pairs_bitexact(cuda_ok, meshes, level):
     assert np.array_equal(cg["pairs"], co["pairs"])
     assert np.array_equal(cg["d2"].view(np.uint64), co["d2"].view(np.uint64))
     assert np.array_equal(cg["stick"], co["stick"])
-    assert np.array_equal(cg["origin"].view(np.uint64), co["origin"].view(np.uint64))
+    assert cg["stick"].sum() > 0
+    # spring origins depend on the contact stiffness, which uses the element
+    # areas of the (FMA-contracted) element kernel: equal to roundoff
+    assert rel(cg["origin"], co["origin"]) < FORCE_TOL
     assert eg["Nc"] == eo["Nc"] and eg["Nc"] > 0
     assert sg == so
     assert rel(fg, fo) < FORCE_TOL
@@ -169,6 +173,11 @@ def test_trajectory(cuda_ok, meshes, contact):
     assert abs(rg.time - ro.time) == 0.0
     for k in ("sum_Etens", "sum_Ebend", "sum_Ekin", "sum_volume", "sum_area"):
         assert abs(getattr(rg, k) - getattr(ro, k)) <= 1e-9 * abs(getattr(ro, k)), k
+    fe_g, fe_o = g.element_fields(), o.element_fields()
+    for k in ("kGauss", "kMean", "etens", "ebend", "area"):
+        assert rel(fe_g[k], fe_o[k]) < 1e-9, k
+    for k in ("kGauss", "kMean", "Etens", "Ebend", "area", "volume", "Ekin"):
+        assert abs(getattr(rg.last, k) - getattr(ro.last, k)) <= 1e-9 * abs(getattr(ro.last, k)), k
     if contact:
         assert np.array_equal(g.contact_state()["pairs"], o.contact_state()["pairs"])
 
@@ -216,3 +225,17 @@ def test_problem_not_finite(cuda_ok, meshes):
     ro, so = o.step(3)
     assert sg == so == 7
     assert rg.steps_done == ro.steps_done == 1
+
+
+def test_two_contexts_interleaved(cuda_ok, meshes):
+    """Two shells with different meshes alive at once keep their own patch
+    tables (no state shared through module globals)."""
+    rng = np.random.default_rng(11)
+    p = physics_params(contact=False)
+    shells = {lv: (L.Shell(*meshes[lv], p), O.Oracle(*meshes[lv], p, threads=2)) for lv in (3, 4)}
+    for lv in (4, 3, 4):
+        X, T = meshes[lv]
+        g, o = shells[lv]
+        u = smooth_state(X, rng)
+        z = np.zeros_like(u)
+        assert rel(g.eval_forces(u, z, -1e-4)[0], o.eval_forces(u, z, -1e-4)[0]) < FORCE_TOL
