@@ -66,7 +66,14 @@ shl_status dev_alloc(shl_ctx* c, T** p, size_t n) {
     g_err = "cudaMalloc(" + std::to_string(bytes) + "): " + cudaGetErrorString(e);
     return SHL_ERR_OOM;
   }
-  cudaMemset(q, 0, bytes);
+  // zero on the context stream: the stream is non-blocking, so a default-stream
+  // memset would not be ordered before the uploads that follow
+  e = cudaMemsetAsync(q, 0, bytes, c->stream);
+  if (e != cudaSuccess) {
+    cudaFree(q);
+    g_err = std::string("cudaMemsetAsync: ") + cudaGetErrorString(e);
+    return SHL_ERR_CUDA;
+  }
   c->allocs.push_back(q);
   *p = (T*)q;
   return SHL_OK;
