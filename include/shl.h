@@ -250,6 +250,31 @@ shl_status shl_read_off(const char* path, double* xyz, size_t cap_nodes, uint32_
 shl_status shl_gaussian_normal_imperfection(const double* xyz, uint32_t n_nodes, double amplitude,
                                             uint64_t seed, double* u_out);
 
+/* Force evaluation that allocates no device memory, for callers that cannot
+ * call cudaMalloc when they evaluate forces: code that runs inside its own
+ * CUDA stream capture (allocation is not allowed there), and hosts whose
+ * device memory all comes from an arena they own and that forbid allocation
+ * on their time-stepping path.  No counterpart in the reference.
+ *
+ * f_dev (3*n_nodes doubles, device) receives f = pressure force - internal
+ * force at the predicted displacement u_dev (3*n_nodes doubles, device), as
+ * f_out of shl_eval_forces for a shell without self-contact and with
+ * bulk_modulus = 0 (both are rejected here).  The set-up data are the
+ * context's (read only); the per-(face, slot) force shares go to a scratch
+ * array compiled into the library (a static device array of 36 doubles x
+ * 32768 faces = 9 MiB that every GPU which loads the library holds until the
+ * process exits), so shells above 32768 faces are rejected with
+ * SHL_ERR_CAPACITY.  The context's own buffers and step state are untouched.
+ *
+ * The first call on a device looks up the scratch address there (and may
+ * make the CUDA runtime load the library's device code); make that first call
+ * before any stream capture.  All calls share the one scratch array, so calls
+ * that overlap on the GPU (different streams, or different contexts on one
+ * device) race and must be ordered by the caller.  stream: a cudaStream_t, or
+ * NULL for the default stream; the call does not synchronise. */
+shl_status shl_internal_force_noalloc(shl_ctx* ctx, const double* u_dev, double pressure, double* f_dev,
+                                      void* stream);
+
 /* Default parameters (ShellSystem constructor and set_parameters defaults). */
 void shl_params_default(shl_params* p);
 

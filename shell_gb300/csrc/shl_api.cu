@@ -853,4 +853,25 @@ shl_status shl_get_mass_damping(shl_ctx* c, double* Minv, double* C) {
   return SHL_OK;
 }
 
+shl_status shl_internal_force_noalloc(shl_ctx* c, const double* u_dev, double pressure, double* f_dev,
+                                      void* stream) {
+  if (!c || !u_dev || !f_dev) { g_err = "null argument"; return SHL_ERR_ARG; }
+  if (c->sc.contact || c->P.bulk_modulus != 0.0) {
+    g_err = "shl_internal_force_noalloc: self-contact and bulk-modulus pressure are not evaluated here";
+    return SHL_ERR_ARG;
+  }
+  if (c->S.F > noalloc_max_faces()) {
+    g_err = "shl_internal_force_noalloc: " + std::to_string(c->S.F) + " faces exceed the scratch limit of " +
+            std::to_string(noalloc_max_faces()) + " faces";
+    return SHL_ERR_CAPACITY;
+  }
+  const double p = c->P.compat_zero_pressure ? pressure * 0.0 : pressure;
+  cudaError_t e = launch_force_noalloc(c->b, c->sc, c->eg, c->elem_blocks, u_dev, p, f_dev, (cudaStream_t)stream);
+  if (e != cudaSuccess) {
+    g_err = std::string("shl_internal_force_noalloc: ") + cudaGetErrorString(e);
+    return SHL_ERR_CUDA;
+  }
+  return SHL_OK;
+}
+
 }  // extern "C"

@@ -157,6 +157,10 @@ void launch_gather_correct(const DevBuf& b, const StepConst& sc, int cur, bool c
 void launch_volume_end_step(const DevBuf& b, const StepConst& sc, bool end_step, cudaStream_t s);
 void launch_positions(const DevBuf& b, const StepConst& sc, cudaStream_t s);
 void launch_fp64_peak(double* out, int blocks, int iters, cudaStream_t s);
+// allocation-free force evaluation (scratch in a static device array)
+uint32_t noalloc_max_faces();
+cudaError_t launch_force_noalloc(const DevBuf& ctx_b, const StepConst& sc, const ElemGroups& eg, uint32_t n_blocks,
+                                 const double* u, double pressure, double* f_out, cudaStream_t s);
 void launch_flush(void* buf, size_t bytes, uint32_t tag, cudaStream_t s);
 
 // ---- launchers (shl_contact.cu) ----

@@ -650,4 +650,89 @@ void launch_volume_end_step(const DevBuf& b, const StepConst& sc, bool end_step,
   k_volume_end<<<nblk(sc.F), kBlock, 0, s>>>(b, sc, end_step ? 1 : 0);
 }
 
+// ================================================================ no-alloc --
+// Force evaluation into caller-owned device memory with no device allocation:
+// the per-(face, slot) force shares go to a file-scope scratch array instead of
+// a buffer of the context.  See shl_internal_force_noalloc in include/shl.h.
+
+// Largest shell this path accepts (faces).  The scratch holds 36 doubles per
+// face: 32768 faces -> 9 MiB, resident on every GPU that loads the library.
+constexpr uint32_t kNoAllocMaxFaces = 32768;
+static __device__ __align__(256) double g_noalloc_scratch[(size_t)kNoAllocMaxFaces * 36];
+
+// Device address of the scratch array per device, looked up once per device
+// (cudaGetSymbolAddress on the host side; the array name itself is only a
+// host-side stand-in).
+static void* g_noalloc_ptr[64];
+static bool g_noalloc_ready[64];
+
+uint32_t noalloc_max_faces() { return kNoAllocMaxFaces; }
+
+cudaError_t noalloc_scratch(void** ptr) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+  if (!g_noalloc_ready[dev]) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return e;
+    g_noalloc_ptr[dev] = p;
+    g_noalloc_ready[dev] = true;
+  }
+  *ptr = g_noalloc_ptr[dev];
+  return cudaSuccess;
+}
+
+// element shares at u (caller pointer in b.up) into the scratch (b.qe);
+// touches neither the control block nor the context's buffers
+__global__ void __launch_bounds__(kBlock) k_elements_noalloc(DevBuf b, StepConst sc, ElemGroups eg,
+                                                             double pressure) {
+  __shared__ double sB[kMaxSlots * 6];
+  int g = 0;
+  while (g + 1 < eg.n && blockIdx.x >= eg.g[g + 1].block_start) ++g;
+  const GroupDesc gd = eg.g[g];
+  for (int k = threadIdx.x; k < gd.n_slots * 6; k += blockDim.x) sB[k] = eg.basis[gd.basis_off + k];
+  __syncthreads();
+  const uint32_t li = (blockIdx.x - gd.block_start) * blockDim.x + threadIdx.x;
+  if (li >= gd.count) return;
+  const uint32_t i = gd.first + li;
+  if (gd.n_slots == 12)
+    element_force<12>(i, 12, sB, b, sc, pressure, 0.0);
+  else if (gd.n_slots == 11)
+    element_force<11>(i, 11, sB, b, sc, pressure, 0.0);
+  else
+    element_force<0>(i, gd.n_slots, sB, b, sc, pressure, 0.0);
+}
+
+// f = -(sum of the node's shares), the same gather order as the step kernel
+__global__ void __launch_bounds__(kBlock) k_gather_noalloc(DevBuf b, StepConst sc, double* f_out) {
+  const uint32_t n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= sc.V) return;
+  double f[3] = {0.0, 0.0, 0.0};
+  const uint32_t g0 = b.gather_ptr[n], g1 = b.gather_ptr[n + 1];
+  for (uint32_t k = g0; k < g1; ++k) {
+    const double* q = b.qe + 3 * (size_t)__ldg(&b.gather_ent[k]);
+    f[0] -= q[0];
+    f[1] -= q[1];
+    f[2] -= q[2];
+  }
+  f_out[3 * (size_t)n] = f[0];
+  f_out[3 * (size_t)n + 1] = f[1];
+  f_out[3 * (size_t)n + 2] = f[2];
+}
+
+cudaError_t launch_force_noalloc(const DevBuf& ctx_b, const StepConst& sc, const ElemGroups& eg, uint32_t n_blocks,
+                                 const double* u, double pressure, double* f_out, cudaStream_t s) {
+  void* scratch = nullptr;
+  cudaError_t e = noalloc_scratch(&scratch);
+  if (e != cudaSuccess) return e;
+  DevBuf b = ctx_b;
+  b.up = const_cast<double*>(u);
+  b.qe = (double*)scratch;
+  k_elements_noalloc<<<n_blocks, kBlock, 0, s>>>(b, sc, eg, pressure);
+  k_gather_noalloc<<<nblk(sc.V), kBlock, 0, s>>>(b, sc, f_out);
+  return cudaGetLastError();
+}
+
 }  // namespace shl

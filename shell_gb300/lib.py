@@ -106,6 +106,7 @@ def load():
         "shl_step_collect": (_i32, [vp, ctypes.POINTER(ShlStepReport)]),
         "shl_time_kernel": (_i32, [vp, ctypes.c_int, ctypes.c_int, sz, ctypes.POINTER(_d)]),
         "shl_measure_fp64_peak": (_i32, [ctypes.POINTER(_d)]),
+        "shl_internal_force_noalloc": (_i32, [vp, vp, _d, vp, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -123,7 +124,7 @@ def exported_symbols():
             "shl_set_contact_state", "shl_rebuild_contacts", "shl_get_element_fields", "shl_get_mass_damping",
             "shl_icosphere", "shl_icosphere_off", "shl_read_off", "shl_gaussian_normal_imperfection",
             "shl_params_default", "shl_get_stream", "shl_upload_pressure_table", "shl_step_enqueue",
-            "shl_step_collect", "shl_time_kernel", "shl_measure_fp64_peak"]
+            "shl_step_collect", "shl_time_kernel", "shl_measure_fp64_peak", "shl_internal_force_noalloc"]
 
 
 class ShlError(RuntimeError):
