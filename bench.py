@@ -214,6 +214,31 @@ def run_ours(args, rank, world, dist):
         ms = float(t.item())
     value = F * K * world / (ms * 1e-3)
 
+    # the same workload with FP32 element forces (FP64 state and contact), cold L2 per step
+    fp32_value = None
+    if args.fp32:
+        p32 = L.default_params(**{k: getattr(p, k) for k, _ in L._PARAM_FIELDS if not k.startswith("pad")})
+        p32.precision = L.PREC_FP32
+        g32 = L.Shell(X, T, p32)
+        g32.apply_initial_conditions(u0, 0.0, pressure(1))
+        s32 = torch.cuda.ExternalStream(g32.stream_handle())
+        g32.upload_pressure_table(pressure(np.arange(1, 1 + W + K)))
+        g32.step_enqueue(W)
+        torch.cuda.synchronize()
+        st32 = [torch.cuda.Event(enable_timing=True) for _ in range(K)]
+        en32 = [torch.cuda.Event(enable_timing=True) for _ in range(K)]
+        with torch.cuda.stream(s32):
+            for k in range(K):
+                flush.fill_(k)
+                st32[k].record(s32)
+                g32.step_enqueue(1)
+                en32[k].record(s32)
+        torch.cuda.synchronize()
+        ms32 = sum(a.elapsed_time(b) for a, b in zip(st32, en32))
+        g32.step_collect()
+        g32.close()
+        fp32_value = F * K / (ms32 * 1e-3)
+
     # warm continuous throughput (informative): K steps back to back, one graph replay per 16 steps
     g.upload_pressure_table(pressure(np.arange(1 + W + K, 1 + W + 2 * K)))
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -269,6 +294,7 @@ def run_ours(args, rank, world, dist):
                    "faces": F, "nodes": V, "parallelism": "replicas (one shell per GPU)" if world > 1 else "single",
                    "l2": "evicted before every timed step (512 MB write)"},
         "warm_value": warm,
+        "fp32_value": fp32_value,
         "e2e": {"value": e2e, "unit": "face-steps/s", "h2d_bytes_per_step": 3 * 3 * V * 8,
                 "d2h_bytes_per_step": 3 * 3 * V * 8,
                 "how": "per step: shl_set_state from pinned host, shl_step(1), shl_get_state"},
@@ -295,6 +321,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--level", type=int, default=6)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--fp32", type=int, default=1, help="also time the FP32 element-force mode")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     world = int(os.environ.get("WORLD_SIZE", "1"))

@@ -40,6 +40,8 @@ constexpr uint32_t kTableCap = 1u << 16;
 struct shl_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
+  cudaStream_t side = nullptr;      // captures the bodies of conditional graph nodes
+  bool conditional_ok = true;       // the driver accepted conditional nodes
   shl_params P{};
   Setup S;
   DevBuf b{};
@@ -130,7 +132,6 @@ bool validate(const shl_params& p, std::string& err) {
     if (!(p.friction_stop_velocity > 0)) { err = "friction_stop_velocity must be > 0"; return false; }
   }
   if (p.precision != SHL_PREC_FP64 && p.precision != SHL_PREC_FP32) { err = "bad precision"; return false; }
-  if (p.precision == SHL_PREC_FP32) { err = "FP32 element forces are provided by the batched ensemble API"; return false; }
   return true;
 }
 
@@ -180,31 +181,79 @@ void estimate_cells(const Setup& S, const shl_params& p, uint64_t& n_cells, uint
   }
 }
 
-void enqueue_step(shl_ctx* c) {
+// A linked-cell pass inside a graph capture: an IF node whose body is the
+// rebuild pipeline, its condition set on the device from ctl->rebuild, so steps
+// without a rebuild launch one 1-thread kernel instead of the whole pipeline.
+cudaError_t capture_conditional_rebuild(shl_ctx* c) {
+  cudaStreamCaptureStatus st;
+  cudaGraph_t g = nullptr;
+  const cudaGraphNode_t* deps = nullptr;
+  const cudaGraphEdgeData* edges = nullptr;
+  size_t nd = 0;
+  cudaError_t e = cudaStreamGetCaptureInfo(c->stream, &st, nullptr, &g, &deps, &edges, &nd);
+  if (e != cudaSuccess) return e;
+  cudaGraphConditionalHandle h;
+  e = cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault);
+  if (e != cudaSuccess) return e;
+  launch_set_rebuild_cond(h, c->b.ctl, c->stream);
+  e = cudaStreamGetCaptureInfo(c->stream, &st, nullptr, &g, &deps, &edges, &nd);
+  if (e != cudaSuccess) return e;
+  cudaGraphNodeParams cp = {cudaGraphNodeTypeConditional};
+  cp.conditional.handle = h;
+  cp.conditional.type = cudaGraphCondTypeIf;
+  cp.conditional.size = 1;
+  cudaGraphNode_t node;
+  e = cudaGraphAddNode(&node, g, deps, edges, nd, &cp);
+  if (e != cudaSuccess) return e;
+  cudaGraph_t body = cp.conditional.phGraph_out[0];
+  e = cudaStreamBeginCaptureToGraph(c->side, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed);
+  if (e != cudaSuccess) return e;
+  launch_rebuild(c->b, c->sc, c->side);
+  e = cudaStreamEndCapture(c->side, &body);
+  if (e != cudaSuccess) return e;
+  return cudaStreamUpdateCaptureDependencies(c->stream, &node, nullptr, 1, cudaStreamSetCaptureDependencies);
+}
+
+cudaError_t enqueue_rebuild(shl_ctx* c, bool capturing) {
+  if (capturing && c->conditional_ok) return capture_conditional_rebuild(c);
+  launch_rebuild(c->b, c->sc, c->stream);
+  return cudaSuccess;
+}
+
+cudaError_t enqueue_step(shl_ctx* c, bool capturing = false) {
   const DevBuf& b = c->b;
   const StepConst& sc = c->sc;
   cudaStream_t s = c->stream;
+  cudaError_t e = cudaSuccess;
   launch_predict(b, sc, 0, s);
-  if (sc.contact) launch_rebuild(b, sc, s);
+  if (sc.contact && (e = enqueue_rebuild(c, capturing)) != cudaSuccess) return e;
   launch_elements(b, sc, c->eg, c->elem_blocks, s);
   if (sc.contact) launch_contact_force(b, sc, 0, s);
   launch_gather_correct(b, sc, 0, true, nullptr, nullptr, s);
-  if (sc.contact) launch_rebuild(b, sc, s);
+  if (sc.contact && (e = enqueue_rebuild(c, capturing)) != cudaSuccess) return e;
   launch_volume_end_step(b, sc, true, s);
+  return cudaSuccess;
 }
 
 shl_status build_graph(shl_ctx* c, uint32_t steps, cudaGraphExec_t* out) {
-  cudaGraph_t g = nullptr;
-  SHL_CUDA_TRY(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-  for (uint32_t i = 0; i < steps; ++i) enqueue_step(c);
-  SHL_CUDA_TRY(cudaStreamEndCapture(c->stream, &g));
-  cudaError_t e = cudaGraphInstantiate(out, g, 0);
-  cudaGraphDestroy(g);
-  if (e != cudaSuccess) {
-    g_err = std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e);
-    return SHL_ERR_CUDA;
+  for (int attempt = 0; attempt < 2; ++attempt) {
+    cudaGraph_t g = nullptr;
+    SHL_CUDA_TRY(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    cudaError_t e = cudaSuccess;
+    for (uint32_t i = 0; i < steps && e == cudaSuccess; ++i) e = enqueue_step(c, true);
+    cudaError_t e2 = cudaStreamEndCapture(c->stream, &g);
+    if (e == cudaSuccess) e = e2;
+    if (e == cudaSuccess) e = cudaGraphInstantiate(out, g, 0);
+    if (g) cudaGraphDestroy(g);
+    if (e == cudaSuccess) return SHL_OK;
+    cudaGetLastError();
+    if (!c->conditional_ok) {
+      g_err = std::string("graph capture: ") + cudaGetErrorString(e);
+      return SHL_ERR_CUDA;
+    }
+    c->conditional_ok = false;  // retry with early-exit launches instead of IF nodes
   }
-  return SHL_OK;
+  return SHL_ERR_CUDA;
 }
 
 void fill_energies(const Ctl& h, shl_energies* e) {
@@ -229,6 +278,7 @@ void shl_destroy(shl_ctx* c) {
   if (c->h_pin) cudaFreeHost(c->h_pin);
   if (c->d_flush) cudaFree(c->d_flush);
   if (c->stream) cudaStreamDestroy(c->stream);
+  if (c->side) cudaStreamDestroy(c->side);
   delete c;
 }
 
@@ -246,7 +296,8 @@ shl_status shl_create(const shl_mesh* mesh, const shl_params* params, shl_ctx** 
   }
   shl_status st = SHL_OK;
   auto fail = [&](shl_status s) { shl_destroy(c); return s; };
-  if (cudaGetDevice(&c->device) != cudaSuccess || cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+  if (cudaGetDevice(&c->device) != cudaSuccess || cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking) != cudaSuccess) {
     g_err = "no CUDA device";
     return fail(SHL_ERR_CUDA);
   }
@@ -259,7 +310,12 @@ shl_status shl_create(const shl_mesh* mesh, const shl_params* params, shl_ctx** 
   ALLOC(b.p, nd); ALLOC(b.Minv, nd); ALLOC(b.C, nd);
   ALLOC(b.face, (size_t)FF_COUNT * F);
   ALLOC(b.patch, 12 * (size_t)F);
-  ALLOC(b.qe, 36 * (size_t)F);
+  const bool fp32 = params->precision == SHL_PREC_FP32;
+  if (fp32) {
+    ALLOC(b.qe32, 36 * (size_t)F);
+    ALLOC(b.face32, (size_t)F32_COUNT * F);
+  }
+  ALLOC(b.qe, fp32 ? 1 : 36 * (size_t)F);
   ALLOC(b.gather_ptr, V + 1);
   ALLOC(b.gather_ent, S.gather_ent.size());
   ALLOC(b.tri, 3 * (size_t)F);
@@ -293,7 +349,7 @@ shl_status shl_create(const shl_mesh* mesh, const shl_params* params, shl_ctx** 
   // contact buffers
   const bool contact = params->shell_shell_contact == SHL_CONTACT_LINEAR;
   uint64_t n_cells0 = 0, entries0 = 0;
-  uint32_t n_cells_cap = 1, entries_cap = 1, pairs_cap = 1, csr_cap = 1;
+  uint32_t n_cells_cap = 1, entries_cap = 1, pairs_cap = 1, csr_cap = 1, cand_cap = 1;
   if (contact) {
     estimate_cells(S, *params, n_cells0, entries0);
     const uint64_t want_cells = std::min<uint64_t>(S.n_cells_max, 1ull << 28);
@@ -302,12 +358,14 @@ shl_status shl_create(const shl_mesh* mesh, const shl_params* params, shl_ctx** 
     entries_cap = (uint32_t)std::min<uint64_t>(std::max<uint64_t>(8 * entries0, 1u << 20), 1ull << 30);
     pairs_cap = std::max<uint32_t>(16 * F, 1u << 16);
     csr_cap = 6 * pairs_cap;
+    cand_cap = std::max<uint32_t>(32 * F, 1u << 18);
     ALLOC(b.close_ptr, F + 1);
     ALLOC(b.close_list, S.close_list.size());
     ALLOC(b.bmin, 3 * (size_t)F); ALLOC(b.bmax, 3 * (size_t)F); ALLOC(b.fsize, F);
     ALLOC(b.cell_lo, 3 * (size_t)F); ALLOC(b.cell_hi, 3 * (size_t)F);
     ALLOC(b.cell_count, n_cells_cap); ALLOC(b.cell_start, n_cells_cap + 1); ALLOC(b.cell_fill, n_cells_cap);
     ALLOC(b.cell_items, entries_cap);
+    ALLOC(b.entry_cell, entries_cap);
     const size_t scan_cap = std::max<size_t>({(size_t)n_cells_cap, (size_t)F + 1, (size_t)V + 1});
     ALLOC(b.scan_block, scan_cap / kScanTile + 2);
     for (int k = 0; k < 2; ++k) {
@@ -316,7 +374,8 @@ shl_status shl_create(const shl_mesh* mesh, const shl_params* params, shl_ctx** 
     }
     ALLOC(b.pkeep, pairs_cap);
     ALLOC(b.new_e1, pairs_cap); ALLOC(b.new_e2, pairs_cap); ALLOC(b.new_d2, pairs_cap);
-    ALLOC(b.new_off, F); ALLOC(b.new_cnt, F);
+    ALLOC(b.new_off, F + 1); ALLOC(b.new_cnt, F); ALLOC(b.new_fill, F);
+    ALLOC(b.cand_e1, cand_cap); ALLOC(b.cand_e2, cand_cap); ALLOC(b.cand_d2, cand_cap); ALLOC(b.cand_ok, cand_cap);
     ALLOC(b.seg_count, F);
     ALLOC(b.pforce, 7 * (size_t)pairs_cap);
     ALLOC(b.csr_count, V); ALLOC(b.csr_ptr, V + 1); ALLOC(b.csr_ent, csr_cap); ALLOC(b.csr_fill, V);
@@ -329,6 +388,7 @@ shl_status shl_create(const shl_mesh* mesh, const shl_params* params, shl_ctx** 
   if ((st = upload(c, b.Minv, S.Minv.data(), nd)) != SHL_OK) return fail(st);
   if ((st = upload(c, b.C, S.C.data(), nd)) != SHL_OK) return fail(st);
   if ((st = upload(c, b.face, S.face.data(), S.face.size())) != SHL_OK) return fail(st);
+  if (fp32 && (st = upload(c, b.face32, S.face32.data(), S.face32.size())) != SHL_OK) return fail(st);
   if ((st = upload(c, b.patch, S.patch.data(), S.patch.size())) != SHL_OK) return fail(st);
   if ((st = upload(c, b.gather_ptr, S.gather_ptr.data(), S.gather_ptr.size())) != SHL_OK) return fail(st);
   if ((st = upload(c, b.gather_ent, S.gather_ent.data(), S.gather_ent.size())) != SHL_OK) return fail(st);
@@ -343,9 +403,14 @@ shl_status shl_create(const shl_mesh* mesh, const shl_params* params, shl_ctx** 
     double* d_basis = nullptr;
     if ((st = dev_alloc(c, &d_basis, basis.size())) != SHL_OK) return fail(st);
     if ((st = upload(c, d_basis, basis.data(), basis.size())) != SHL_OK) return fail(st);
+    std::vector<float> basis32(basis.begin(), basis.end());
+    float* d_basis32 = nullptr;
+    if ((st = dev_alloc(c, &d_basis32, basis32.size())) != SHL_OK) return fail(st);
+    if ((st = upload(c, d_basis32, basis32.data(), basis32.size())) != SHL_OK) return fail(st);
     c->eg.n = (int32_t)gd.size();
     for (size_t k = 0; k < gd.size(); ++k) c->eg.g[k] = gd[k];
     c->eg.basis = d_basis;
+    c->eg.basis32 = d_basis32;
   }
 
   // step constants
@@ -378,12 +443,14 @@ shl_status shl_create(const shl_mesh* mesh, const shl_params* params, shl_ctx** 
   sc.entries_cap = entries_cap;
   sc.pairs_cap = pairs_cap;
   sc.csr_cap = csr_cap;
+  sc.cand_cap = cand_cap;
   sc.contact = contact ? 1 : 0;
   sc.friction = (contact && (p.mu_s != 0 || p.mu_d != 0)) ? 1 : 0;
   sc.pressure_base = p.pressure_base;
   sc.pressure_dir = p.pressure_dir;
   sc.compat_zero_pressure = p.compat_zero_pressure;
   sc.stop_on_problem = p.stop_on_problem;
+  sc.fp32 = fp32 ? 1 : 0;
   sc.V = V;
   sc.F = F;
 
@@ -856,8 +923,9 @@ shl_status shl_get_mass_damping(shl_ctx* c, double* Minv, double* C) {
 shl_status shl_internal_force_noalloc(shl_ctx* c, const double* u_dev, double pressure, double* f_dev,
                                       void* stream) {
   if (!c || !u_dev || !f_dev) { g_err = "null argument"; return SHL_ERR_ARG; }
-  if (c->sc.contact || c->P.bulk_modulus != 0.0) {
-    g_err = "shl_internal_force_noalloc: self-contact and bulk-modulus pressure are not evaluated here";
+  if (c->sc.contact || c->P.bulk_modulus != 0.0 || c->sc.fp32) {
+    g_err = "shl_internal_force_noalloc: self-contact, bulk-modulus pressure and FP32 element forces are not "
+            "evaluated here";
     return SHL_ERR_ARG;
   }
   if (c->S.F > noalloc_max_faces()) {

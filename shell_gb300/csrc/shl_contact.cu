@@ -12,9 +12,12 @@
 //                  keep flags of the old list (ShellSystem.C:2016-2027)
 //   scan           cell_count -> cell_start
 //   k_rb_fill      scatter faces into their cells (counting sort, pass 2)
-//   k_rb_pairs     per face e1: faces e2 > e1 sharing a cell, emitted from the
-//                  lowest shared cell only, not topologically close, not in the
-//                  kept list, not AABB-apart by d_max, with d2 <= d2_max
+//   k_rb_cand      per (cell, face e1) entry: faces e2 > e1 in the cell, emitted
+//                  from the lowest shared cell only, not topologically close, not
+//                  in the kept list, not AABB-apart by d_max, not certainly apart
+//                  along the line of centroids (a conservative prefilter)
+//   k_rb_narrow    per candidate: closest points, accept d2 <= d2_max
+//   scan, k_rb_scatter_new  accepted pairs grouped by eid1 (counting sort)
 //   scan           per-face pair counts -> segment offsets
 //   k_rb_assemble  kept old pairs + new pairs of each face, merged in e2 order
 //   k_rb_copyback  scratch list -> list
@@ -179,7 +182,12 @@ __global__ void k_rb_clear(DevBuf b, StepConst sc) {
     b.cell_count[i] = 0;
     b.cell_fill[i] = 0;
   }
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < sc.F; i += stride) b.seg_count[i] = 0;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < sc.F; i += stride) {
+    b.seg_count[i] = 0;
+    b.new_cnt[i] = 0;
+    b.new_fill[i] = 0;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) ctl->n_cand = 0;
 }
 
 // cell index range of face f on axis c (ShellSystem.C:1982-1983)
@@ -346,6 +354,7 @@ __global__ void __launch_bounds__(kBlock) k_rb_fill(DevBuf b, StepConst sc) {
         const uint32_t cell = (uint32_t)cx * ny * nz + (uint32_t)cy * nz + (uint32_t)cz;
         const uint32_t pos = b.cell_start[cell] + atomicAdd(&b.cell_fill[cell], 1u);
         b.cell_items[pos] = f;
+        b.entry_cell[pos] = cell;
       }
 }
 
@@ -372,83 +381,138 @@ __device__ __forceinline__ uint32_t sorted_find(const uint32_t* a, uint32_t lo, 
 }
 
 // ---------------------------------------------------------------- pairs --
-__global__ void __launch_bounds__(128) k_rb_pairs(DevBuf b, StepConst sc) {
+// Conservative separating-axis test along the line of centroids: true only
+// when the triangles are certainly farther apart than d_max, with a margin far
+// above the rounding error of the projections, so it never removes a pair
+// that the separately rounded closest-point solve would accept.
+__device__ __forceinline__ bool certainly_apart(const double* const* P1, const double* const* P2, double d_max) {
+  double d[3], S = 0.0;
+  for (int c = 0; c < 3; ++c) {
+    d[c] = (P2[0][c] + P2[1][c] + P2[2][c]) - (P1[0][c] + P1[1][c] + P1[2][c]);
+    for (int k = 0; k < 3; ++k) S = fmax(S, fmax(fabs(P1[k][c]), fabs(P2[k][c])));
+  }
+  const double L2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+  if (!(L2 > 0.0)) return false;
+  double mx1 = -SHL_DBL_MAX, mn2 = SHL_DBL_MAX;
+  for (int k = 0; k < 3; ++k) {
+    mx1 = fmax(mx1, d[0] * P1[k][0] + d[1] * P1[k][1] + d[2] * P1[k][2]);
+    mn2 = fmin(mn2, d[0] * P2[k][0] + d[1] * P2[k][1] + d[2] * P2[k][2]);
+  }
+  const double L = sqrt(L2);
+  // |rounding error of mn2 - mx1| <= 8 eps |d| (3 S); distance >= true gap / |d|
+  const double gap = (mn2 - mx1) - 8.0 * 2.220446049250313e-16 * L * 3.0 * S;
+  return gap > d_max * L * (1.0 + 1e-8);
+}
+
+// Candidate pairs of one (cell, face) entry: faces e2 > e1 in the cell, emitted
+// from the lowest shared cell only, not topologically close, not in the kept
+// list, not AABB-apart by d_max (ShellSystem.C:2047-2060), and not certainly
+// apart.  Buffered per thread, appended with one atomic per flush.
+__global__ void __launch_bounds__(kBlock) k_rb_cand(DevBuf b, StepConst sc) {
   Ctl* ctl = b.ctl;
   if (rb_off(ctl)) return;
-  const uint32_t e1 = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e1 >= sc.F) return;
-  int lo1[3], hi1[3];
-  for (int c = 0; c < 3; ++c) {
-    lo1[c] = b.cell_lo[3 * (size_t)e1 + c];
-    hi1[c] = b.cell_hi[3 * (size_t)e1 + c];
-  }
+  const uint32_t n_entries = ctl->n_entries;
+  const uint32_t stride = gridDim.x * blockDim.x;
   const uint32_t ny = ctl->ncd[1], nz = ctl->ncd[2];
-  const double d_max = ctl->d_max, d2_max = ctl->d2_max;
-  const uint32_t c0 = b.close_ptr[e1], c1 = b.close_ptr[e1 + 1];
-  const uint32_t o0 = b.pair_ptr[0][e1], o1 = b.pair_ptr[0][e1 + 1];
-  const double* P1[3];
-  for (int k = 0; k < 3; ++k) P1[k] = b.p + 3 * (size_t)b.tri[3 * (size_t)e1 + k];
-  double mn1[3], mx1[3];
-  for (int c = 0; c < 3; ++c) {
-    mn1[c] = b.bmin[3 * (size_t)e1 + c];
-    mx1[c] = b.bmax[3 * (size_t)e1 + c];
-  }
-  uint32_t found_e2[kMaxNewPerFace];
-  double found_d2[kMaxNewPerFace];
-  int n_found = 0;
-  bool overflow = false;
-  for (int cx = lo1[0]; cx <= hi1[0]; ++cx)
-    for (int cy = lo1[1]; cy <= hi1[1]; ++cy)
-      for (int cz = lo1[2]; cz <= hi1[2]; ++cz) {
-        const uint32_t cell = (uint32_t)cx * ny * nz + (uint32_t)cy * nz + (uint32_t)cz;
-        const uint32_t s0 = b.cell_start[cell], cnt = b.cell_count[cell];
-        for (uint32_t k = 0; k < cnt; ++k) {
-          const uint32_t e2 = b.cell_items[s0 + k];
-          if (e2 <= e1) continue;
-          // emit each pair from its lowest shared cell only
-          const int* lo2 = b.cell_lo + 3 * (size_t)e2;
-          const int lx = max(lo1[0], lo2[0]), ly = max(lo1[1], lo2[1]), lz = max(lo1[2], lo2[2]);
-          if (lx != cx || ly != cy || lz != cz) continue;
-          if (sorted_contains(b.close_list, c0, c1, e2)) continue;
-          const uint32_t at = sorted_find(b.pe2[0], o0, o1, e2);
-          if (at < o1 && b.pkeep[at]) continue;
-          bool apart = false;
-          for (int c = 0; c < 3; ++c) {
-            const double mn2 = b.bmin[3 * (size_t)e2 + c], mx2 = b.bmax[3 * (size_t)e2 + c];
-            apart = apart || mn1[c] > __dadd_rn(mx2, d_max) || mn2 > __dadd_rn(mx1[c], d_max);
-          }
-          if (apart) continue;
-          const double* P2[3];
-          for (int q = 0; q < 3; ++q) P2[q] = b.p + 3 * (size_t)b.tri[3 * (size_t)e2 + q];
-          shl_pair_geom g;
-          shl_pair_compute(P1, P2, &g);
-          if (g.d2 <= 0.0) atomicMax(&ctl->problem, (int)SHL_CONTACT_PROBLEM);
-          if (g.d2 > d2_max) continue;
-          if (n_found < kMaxNewPerFace) {
-            found_e2[n_found] = e2;
-            found_d2[n_found] = g.d2;
-            ++n_found;
-          } else {
-            overflow = true;
-          }
-        }
+  const double d_max = ctl->d_max;
+  constexpr int kBuf = 8;
+  uint32_t buf1[kBuf], buf2[kBuf];
+  int nb = 0;
+  auto flush = [&]() {
+    if (nb == 0) return;
+    const uint32_t off = atomicAdd(&ctl->n_cand, (uint32_t)nb);
+    if (off + nb > sc.cand_cap) {
+      set_error(ctl, SHL_ERR_CAPACITY);
+    } else {
+      for (int q = 0; q < nb; ++q) {
+        b.cand_e1[off + q] = buf1[q];
+        b.cand_e2[off + q] = buf2[q];
       }
-  if (overflow) set_error(ctl, SHL_ERR_CAPACITY);
-  b.new_cnt[e1] = (uint32_t)n_found;
-  if (n_found == 0) return;
-  const uint32_t off = atomicAdd(&ctl->n_new, (uint32_t)n_found);
-  if (off + n_found > sc.pairs_cap) {
-    set_error(ctl, SHL_ERR_CAPACITY);
-    b.new_cnt[e1] = 0;
-    return;
+    }
+    nb = 0;
+  };
+  for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n_entries; j += stride) {
+    const uint32_t cell = b.entry_cell[j];
+    const uint32_t e1 = b.cell_items[j];
+    const uint32_t cz = cell % nz, cy = (cell / nz) % ny, cx = cell / (nz * ny);
+    const int* lo1 = b.cell_lo + 3 * (size_t)e1;
+    const int l10 = lo1[0], l11 = lo1[1], l12 = lo1[2];
+    const uint32_t c0 = b.close_ptr[e1], c1 = b.close_ptr[e1 + 1];
+    const uint32_t o0 = b.pair_ptr[0][e1], o1 = b.pair_ptr[0][e1 + 1];
+    double mn1[3], mx1[3];
+    const double* P1[3];
+    for (int c = 0; c < 3; ++c) {
+      mn1[c] = b.bmin[3 * (size_t)e1 + c];
+      mx1[c] = b.bmax[3 * (size_t)e1 + c];
+      P1[c] = b.p + 3 * (size_t)b.tri[3 * (size_t)e1 + c];
+    }
+    const uint32_t s0 = b.cell_start[cell], cnt = b.cell_count[cell];
+    for (uint32_t k = 0; k < cnt; ++k) {
+      const uint32_t e2 = b.cell_items[s0 + k];
+      if (e2 <= e1) continue;
+      const int* lo2 = b.cell_lo + 3 * (size_t)e2;
+      if ((uint32_t)max(l10, lo2[0]) != cx || (uint32_t)max(l11, lo2[1]) != cy || (uint32_t)max(l12, lo2[2]) != cz)
+        continue;
+      if (sorted_contains(b.close_list, c0, c1, e2)) continue;
+      const uint32_t at = sorted_find(b.pe2[0], o0, o1, e2);
+      if (at < o1 && b.pkeep[at]) continue;
+      bool apart = false;
+      for (int c = 0; c < 3; ++c) {
+        const double mn2 = b.bmin[3 * (size_t)e2 + c], mx2 = b.bmax[3 * (size_t)e2 + c];
+        apart = apart || mn1[c] > __dadd_rn(mx2, d_max) || mn2 > __dadd_rn(mx1[c], d_max);
+      }
+      if (apart) continue;
+      const double* P2[3];
+      for (int q = 0; q < 3; ++q) P2[q] = b.p + 3 * (size_t)b.tri[3 * (size_t)e2 + q];
+      if (certainly_apart(P1, P2, d_max)) continue;
+      buf1[nb] = e1;
+      buf2[nb] = e2;
+      if (++nb == kBuf) flush();
+    }
   }
-  b.new_off[e1] = off;
-  for (int k = 0; k < n_found; ++k) {
-    b.new_e1[off + k] = e1;
-    b.new_e2[off + k] = found_e2[k];
-    b.new_d2[off + k] = found_d2[k];
+  flush();
+}
+
+// closest-point test of each candidate (rounded operation by operation)
+__global__ void __launch_bounds__(kBlock) k_rb_narrow(DevBuf b, StepConst sc) {
+  Ctl* ctl = b.ctl;
+  if (rb_off(ctl)) return;
+  const uint32_t n = min(ctl->n_cand, sc.cand_cap);
+  const double d2_max = ctl->d2_max;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const uint32_t e1 = b.cand_e1[i], e2 = b.cand_e2[i];
+    const double* P1[3];
+    const double* P2[3];
+    for (int q = 0; q < 3; ++q) {
+      P1[q] = b.p + 3 * (size_t)b.tri[3 * (size_t)e1 + q];
+      P2[q] = b.p + 3 * (size_t)b.tri[3 * (size_t)e2 + q];
+    }
+    shl_pair_geom g;
+    shl_pair_compute(P1, P2, &g);
+    if (g.d2 <= 0.0) atomicMax(&ctl->problem, (int)SHL_CONTACT_PROBLEM);
+    const bool ok = !(g.d2 > d2_max);  // ShellSystem.C:2082
+    b.cand_d2[i] = g.d2;
+    b.cand_ok[i] = ok ? 1 : 0;
+    if (ok) {
+      atomicAdd(&b.new_cnt[e1], 1u);
+      atomicAdd(&b.seg_count[e1], 1u);
+    }
   }
-  atomicAdd(&b.seg_count[e1], (uint32_t)n_found);
+}
+
+// accepted candidates grouped by eid1 (counting sort; order inside a group is
+// fixed later by the assembly)
+__global__ void __launch_bounds__(kBlock) k_rb_scatter_new(DevBuf b, StepConst sc) {
+  Ctl* ctl = b.ctl;
+  if (rb_off(ctl)) return;
+  const uint32_t n = min(ctl->n_cand, sc.cand_cap);
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    if (!b.cand_ok[i]) continue;
+    const uint32_t e1 = b.cand_e1[i];
+    const uint32_t pos = b.new_off[e1] + atomicAdd(&b.new_fill[e1], 1u);
+    b.new_e2[pos] = b.cand_e2[i];
+    b.new_d2[pos] = b.cand_d2[i];
+  }
 }
 
 // -------------------------------------------------------------- assemble --
@@ -460,23 +524,21 @@ __global__ void __launch_bounds__(kBlock) k_rb_assemble(DevBuf b, StepConst sc) 
   uint32_t dst = b.pair_ptr[1][e1];
   const uint32_t o0 = b.pair_ptr[0][e1], o1 = b.pair_ptr[0][e1 + 1];
   const uint32_t nn = b.new_cnt[e1];
-  uint32_t ne2[kMaxNewPerFace];
-  double nd2[kMaxNewPerFace];
-  if (nn > 0) {
-    const uint32_t off = b.new_off[e1];
-    for (uint32_t k = 0; k < nn; ++k) {
-      // insertion sort by e2
-      const uint32_t x = b.new_e2[off + k];
-      const double d = b.new_d2[off + k];
-      int q = (int)k - 1;
-      while (q >= 0 && ne2[q] > x) {
-        ne2[q + 1] = ne2[q];
-        nd2[q + 1] = nd2[q];
-        --q;
-      }
-      ne2[q + 1] = x;
-      nd2[q + 1] = d;
+  const uint32_t off = nn ? b.new_off[e1] : 0u;
+  uint32_t* ne2 = b.new_e2 + off;
+  double* nd2 = b.new_d2 + off;
+  // insertion sort of this face's new pairs by e2 (the segment belongs to this thread)
+  for (uint32_t k = 1; k < nn; ++k) {
+    const uint32_t x = ne2[k];
+    const double d = nd2[k];
+    uint32_t q = k;
+    while (q > 0 && ne2[q - 1] > x) {
+      ne2[q] = ne2[q - 1];
+      nd2[q] = nd2[q - 1];
+      --q;
     }
+    ne2[q] = x;
+    nd2[q] = d;
   }
   uint32_t io = o0, in = 0;
   for (;;) {
@@ -589,7 +651,16 @@ __global__ void k_csr_finish(DevBuf b) {
 
 inline uint32_t nblk(uint32_t n, uint32_t bs = kBlock) { return n == 0 ? 1 : (n + bs - 1) / bs; }
 
+// condition of the graph's IF node around a linked-cell pass
+__global__ void k_set_rebuild_cond(cudaGraphConditionalHandle h, const Ctl* ctl) {
+  cudaGraphSetConditional(h, (ctl->rebuild != 0 && ctl->halted == 0) ? 1u : 0u);
+}
+
 }  // namespace
+
+void launch_set_rebuild_cond(cudaGraphConditionalHandle h, const Ctl* ctl, cudaStream_t s) {
+  k_set_rebuild_cond<<<1, 1, 0, s>>>(h, ctl);
+}
 
 void launch_contact_csr(const DevBuf& b, const StepConst& sc, cudaStream_t s) {
   const uint32_t gV = nblk(sc.V);
@@ -616,7 +687,17 @@ void launch_rebuild(const DevBuf& b, const StepConst& sc, cudaStream_t s) {
   launch_scan(&b.ctl->rebuild, b.ctl, b.cell_count, b.cell_start, &b.ctl->n_cells, 0, sc.n_cells_cap, b.scan_block,
               &b.ctl->n_entries, false, sc.entries_cap, true, s);
   k_rb_fill<<<gF, kBlock, 0, s>>>(b, sc);
-  k_rb_pairs<<<nblk(sc.F, 128), 128, 0, s>>>(b, sc);
+  {
+    uint32_t g = nblk(sc.entries_cap);
+    if (g > 16 * 152) g = 16 * 152;
+    k_rb_cand<<<g, kBlock, 0, s>>>(b, sc);
+    uint32_t gc = nblk(sc.cand_cap);
+    if (gc > 16 * 152) gc = 16 * 152;
+    k_rb_narrow<<<gc, kBlock, 0, s>>>(b, sc);
+    launch_scan(&b.ctl->rebuild, b.ctl, b.new_cnt, b.new_off, nullptr, sc.F, sc.F, b.scan_block, &b.ctl->n_new,
+                false, sc.pairs_cap, true, s);
+    k_rb_scatter_new<<<gc, kBlock, 0, s>>>(b, sc);
+  }
   launch_scan(&b.ctl->rebuild, b.ctl, b.seg_count, b.pair_ptr[1], nullptr, sc.F, sc.F, b.scan_block, &b.ctl->n_next,
               true, sc.pairs_cap, true, s);
   k_rb_assemble<<<gF, kBlock, 0, s>>>(b, sc);

@@ -45,6 +45,7 @@ struct ElemGroups {
   GroupDesc g[kMaxGroups];
   int32_t n;
   const double* basis;
+  const float* basis32;
 };
 
 // Control block in device memory.
@@ -79,6 +80,7 @@ struct Ctl {
   uint32_t n_csr;          // contact CSR entries
   uint32_t n_next;         // pairs in the list being assembled
   uint32_t csr_dirty;      // the contact CSR must be rebuilt
+  uint32_t n_cand;         // candidates of the current rebuild
   // measurements of the current step
   double Etens, Ebend, Eself, Efric, Ekin, kGauss, kMean;
   uint32_t Nc;
@@ -104,12 +106,13 @@ struct StepConst {
   double pressure_default;
   const double* pressure_table;  // device, or null
   uint64_t n_cells_max;
-  uint32_t n_cells_cap, entries_cap, pairs_cap, csr_cap;
+  uint32_t n_cells_cap, entries_cap, pairs_cap, csr_cap, cand_cap;
   int32_t contact;   // 1 if self-contact is on
   int32_t friction;  // 1 if mu_s or mu_d != 0
   int32_t pressure_base, pressure_dir;
   int32_t compat_zero_pressure;
   int32_t stop_on_problem;
+  int32_t fp32;      // element forces in FP32 (relative-displacement form)
   uint32_t V, F;
 };
 
@@ -119,6 +122,8 @@ struct DevBuf {
   double* face;       // FF_COUNT * F
   int32_t* patch;     // 12 * F
   double* qe;         // F * 12 * 3
+  float* face32;      // F32_COUNT * F (FP32 element path)
+  float* qe32;        // F * 12 * 3 (FP32 element path)
   uint32_t *gather_ptr, *gather_ent;
   uint32_t* tri;      // 3F original order
   uint32_t *perm;     // internal -> original
@@ -138,7 +143,11 @@ struct DevBuf {
   uint8_t* pkeep;              // keep flags of the old list
   uint32_t *new_e1, *new_e2;   // new pairs of a rebuild
   double* new_d2;
-  uint32_t *new_off, *new_cnt; // per face: offset and count of its new pairs
+  uint32_t *new_off, *new_cnt, *new_fill;  // per face: offset, count, fill cursor of its new pairs
+  uint32_t* entry_cell;        // cell of each (cell, face) entry
+  uint32_t *cand_e1, *cand_e2; // candidates that passed the cheap filters
+  double* cand_d2;
+  uint8_t* cand_ok;
   uint32_t* seg_count;         // per-face pair counts (F)
   double* pforce;              // 7 per pair: f_contact(3), v1, w1, v2, w2
   uint32_t *csr_count, *csr_ptr, *csr_ent, *csr_fill;  // per-node contact CSR
@@ -169,9 +178,10 @@ void launch_flush(void* buf, size_t bytes, uint32_t tag, cudaStream_t s);
 // (every kernel returns at once otherwise), so it can sit in a CUDA graph.
 // The list lives in buffer 0; buffer 1 is scratch.
 void launch_rebuild(const DevBuf& b, const StepConst& sc, cudaStream_t s);
+// Sets an IF node's condition to (ctl->rebuild && !ctl->halted) inside a graph.
+void launch_set_rebuild_cond(cudaGraphConditionalHandle h, const Ctl* ctl, cudaStream_t s);
 // Rebuild the per-node contact CSR when ctl->csr_dirty is set.
 void launch_contact_csr(const DevBuf& b, const StepConst& sc, cudaStream_t s);
-constexpr int kMaxNewPerFace = 64;  // new pairs one face may add in one rebuild
 
 }  // namespace shl
 

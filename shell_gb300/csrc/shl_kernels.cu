@@ -318,6 +318,235 @@ __device__ __forceinline__ ElemOut element_force(uint32_t i, int np_rt, const do
   return o;
 }
 
+// FP32 element force in relative-displacement form.  Same mechanics as
+// element_force, but the strains are built from the displacement derivatives
+// and the reference geometry without subtracting nearly equal metrics:
+//   alpha_11 = A1.du1 + |du1|^2/2, alpha_22 = A2.du2 + |du2|^2/2,
+//   alpha_12 = A1.du2 + du1.A2 + du1.du2 (Voigt, shear doubled)
+//   beta_k   = -(D_k.(n - N) + d_k.n), with n - N formed from the change
+//              of a1 x a2 (no cancellation), shear doubled.
+// The per-slot shares are written in FP32.
+template <int NP>
+__device__ __forceinline__ ElemOut element_force32(uint32_t i, int np_rt, const float* __restrict__ B,
+                                                   const DevBuf& b, const StepConst& sc, float pressure,
+                                                   float vol_p) {
+  const uint32_t F = sc.F;
+  const int np = NP > 0 ? NP : np_rt;
+  float G[6][3];
+#pragma unroll
+  for (int k = 0; k < 6; ++k) G[k][0] = G[k][1] = G[k][2] = 0.f;
+#pragma unroll
+  for (int s = 0; s < (NP > 0 ? NP : kMaxSlots); ++s) {
+    if (NP == 0 && s >= np) break;
+    const int nd = __ldg(&b.patch[(size_t)s * F + i]);
+    const float ux = (float)__ldg(&b.up[3 * (size_t)nd]);
+    const float uy = (float)__ldg(&b.up[3 * (size_t)nd + 1]);
+    const float uz = (float)__ldg(&b.up[3 * (size_t)nd + 2]);
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+      const float w = B[6 * s + k];
+      G[k][0] = fmaf(w, ux, G[k][0]);
+      G[k][1] = fmaf(w, uy, G[k][1]);
+      G[k][2] = fmaf(w, uz, G[k][2]);
+    }
+  }
+  const float* fc = b.face32;
+#define FC(fld) __ldg(&fc[(size_t)(fld) * F + i])
+  const float R00 = FC(F32_R00), R01 = FC(F32_R01), R10 = FC(F32_R10), R11 = FC(F32_R11);
+  const float JxW = FC(F32_JXW);
+  const float c11a = R00 * R00, c11b = R10 * R10, c11c = 2.f * R00 * R10;
+  const float c22a = R01 * R01, c22b = R11 * R11, c22c = 2.f * R01 * R11;
+  const float c12a = R00 * R01, c12b = R10 * R11, c12c = R01 * R10 + R00 * R11;
+  float A1[3] = {FC(F32_A10), FC(F32_A11), FC(F32_A12)};
+  float A2[3] = {FC(F32_A20), FC(F32_A21), FC(F32_A22)};
+  float du1[3], du2[3], d1[3], d2[3], d3[3], xq[3];
+  {
+    const float X0[3] = {FC(F32_X0), FC(F32_X1), FC(F32_X2)};
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      du1[c] = R00 * G[1][c] + R10 * G[2][c];
+      du2[c] = R01 * G[1][c] + R11 * G[2][c];
+      d1[c] = c11a * G[3][c] + c11b * G[4][c] + c11c * G[5][c];
+      d2[c] = c22a * G[3][c] + c22b * G[4][c] + c22c * G[5][c];
+      d3[c] = c12a * G[3][c] + c12b * G[4][c] + c12c * G[5][c];
+      xq[c] = X0[c] + G[0][c];
+    }
+  }
+  auto dotf = [](const float* x, const float* y) { return x[0] * y[0] + x[1] * y[1] + x[2] * y[2]; };
+  auto crossf = [](const float* x, const float* y, float* r) {
+    r[0] = x[1] * y[2] - x[2] * y[1];
+    r[1] = x[2] * y[0] - x[0] * y[2];
+    r[2] = x[0] * y[1] - x[1] * y[0];
+  };
+  // membrane strains
+  const float al0 = dotf(A1, du1) + 0.5f * dotf(du1, du1);
+  const float al1 = dotf(A2, du2) + 0.5f * dotf(du2, du2);
+  const float al2 = dotf(A1, du2) + dotf(du1, A2) + dotf(du1, du2);
+  // deformed normal from the change of a1 x a2
+  float Dn[3], t1[3], t2[3], t3[3];
+  crossf(A1, du2, t1);
+  crossf(du1, A2, t2);
+  crossf(du1, du2, t3);
+  Dn[0] = t1[0] + t2[0] + t3[0];
+  Dn[1] = t1[1] + t2[1] + t3[1];
+  Dn[2] = t1[2] + t2[2] + t3[2];
+  const float N0[3] = {FC(F32_N0), FC(F32_N1), FC(F32_N2)};
+  const float L0 = FC(F32_L0);
+  const float dL2 = 2.f * L0 * dotf(N0, Dn) + dotf(Dn, Dn);  // |a1 x a2|^2 - L0^2
+  const float jac = sqrtf(L0 * L0 + dL2);
+  const float invjac = 1.f / jac;
+  const float s_n = -dL2 / ((L0 + jac) * jac);  // L0/jac - 1
+  float a3[3], dn[3], a1[3], a2[3], v1[3], v2[3], v3[3];
+  {
+    const float D1[3] = {FC(F32_D10), FC(F32_D11), FC(F32_D12)};
+    const float D2[3] = {FC(F32_D20), FC(F32_D21), FC(F32_D22)};
+    const float D3[3] = {FC(F32_D30), FC(F32_D31), FC(F32_D32)};
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      dn[c] = Dn[c] * invjac + N0[c] * s_n;
+      a3[c] = N0[c] + dn[c];
+      a1[c] = A1[c] + du1[c];
+      a2[c] = A2[c] + du2[c];
+      v1[c] = D1[c] + d1[c];
+      v2[c] = D2[c] + d2[c];
+      v3[c] = D3[c] + d3[c];
+    }
+    // bending strains beta_k = -(D_k.dn + d_k.a3)
+    const float be0 = -(dotf(D1, dn) + dotf(d1, a3));
+    const float be1 = -(dotf(D2, dn) + dotf(d2, a3));
+    const float be2 = -2.f * (dotf(D3, dn) + dotf(d3, a3));
+    const float H00 = FC(F32_H00), H01 = FC(F32_H01), H02 = FC(F32_H02), H11 = FC(F32_H11), H12 = FC(F32_H12),
+                H22 = FC(F32_H22);
+    const float K = (float)sc.K, Dm = (float)sc.D;
+    const float n0 = K * (H00 * al0 + H01 * al1 + H02 * al2);
+    const float n1 = K * (H01 * al0 + H11 * al1 + H12 * al2);
+    const float n2 = K * (H02 * al0 + H12 * al1 + H22 * al2);
+    const float m0 = Dm * (H00 * be0 + H01 * be1 + H02 * be2);
+    const float m1 = Dm * (H01 * be0 + H11 * be1 + H12 * be2);
+    const float m2 = Dm * (H02 * be0 + H12 * be1 + H22 * be2);
+    const float h0 = dotf(v1, a3), h1 = dotf(v2, a3), h2 = dotf(v3, a3);
+    float M[3], a2xa3[3], a3xa1[3], Mxa2[3], a1xM[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) M[c] = m0 * v1[c] + m1 * v2[c] + 2.f * m2 * v3[c];
+    const float sm = m0 * h0 + m1 * h1 + 2.f * m2 * h2;
+    crossf(a2, a3, a2xa3);
+    crossf(a3, a1, a3xa1);
+    crossf(M, a2, Mxa2);
+    crossf(a1, M, a1xM);
+    float pv[3] = {0.f, 0.f, 0.f};
+    if (pressure != 0.f) {
+      switch (sc.pressure_base) {
+        case SHL_CS_LOCAL: pv[0] = a3[0]; pv[1] = a3[1]; pv[2] = a3[2]; break;
+        case SHL_CS_CARTESIAN: pv[sc.pressure_dir] = 1.f; break;
+        case SHL_CS_CYLINDRICAL:
+          if (sc.pressure_dir == 0) {
+            pv[0] = 1.f;
+          } else {
+            const float inv_r = 1.f / sqrtf(xq[1] * xq[1] + xq[2] * xq[2]);
+            if (isfinite(inv_r)) { pv[1] = inv_r * xq[1]; pv[2] = inv_r * xq[2]; }
+          }
+          break;
+        case SHL_CS_SPHERICAL: {
+          const float r = sqrtf(dotf(xq, xq));
+          if (r > 0.f) { const float ir = 1.f / r; pv[0] = xq[0] * ir; pv[1] = xq[1] * ir; pv[2] = xq[2] * ir; }
+          break;
+        }
+        default: break;
+      }
+      pv[0] *= pressure; pv[1] *= pressure; pv[2] *= pressure;
+    }
+    if (vol_p != 0.f) {
+      pv[0] += a3[0] * vol_p; pv[1] += a3[1] * vol_p; pv[2] += a3[2] * vol_p;
+    }
+    float Z[6][3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const float Y1 = JxW * (n0 * a1[c] + n2 * a2[c] + invjac * (Mxa2[c] + sm * a2xa3[c]));
+      const float Y2 = JxW * (n1 * a2[c] + n2 * a1[c] + invjac * (a1xM[c] + sm * a3xa1[c]));
+      const float Y11 = -JxW * m0 * a3[c];
+      const float Y22 = -JxW * m1 * a3[c];
+      const float Y12 = -2.f * JxW * m2 * a3[c];
+      Z[0][c] = -JxW * pv[c];
+      Z[1][c] = R00 * Y1 + R01 * Y2;
+      Z[2][c] = R10 * Y1 + R11 * Y2;
+      Z[3][c] = c11a * Y11 + c22a * Y22 + c12a * Y12;
+      Z[4][c] = c11b * Y11 + c22b * Y22 + c12b * Y12;
+      Z[5][c] = c11c * Y11 + c22c * Y22 + c12c * Y12;
+    }
+    float* qe = b.qe32 + (size_t)i * 36;
+#pragma unroll
+    for (int s = 0; s < (NP > 0 ? NP : kMaxSlots); ++s) {
+      if (NP == 0 && s >= np) break;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        float t = B[6 * s] * Z[0][c];
+#pragma unroll
+        for (int k = 1; k < 6; ++k) t = fmaf(B[6 * s + k], Z[k][c], t);
+        qe[3 * s + c] = t;
+      }
+    }
+    ElemOut o;
+    o.etens = 0.5 * (double)JxW * ((double)n0 * al0 + (double)n1 * al1 + (double)n2 * al2);
+    o.ebend = 0.5 * (double)JxW * ((double)m0 * be0 + (double)m1 * be1 + (double)m2 * be2);
+    o.area = sc.qw * (double)jac;
+    const float g0 = FC(F32_G0) + 2.f * al0, g1 = FC(F32_G1) + 2.f * al1, g2 = FC(F32_G2) + al2;
+    const double invdet = 1.0 / ((double)g0 * g1 - (double)g2 * g2);
+    o.kg = o.area * invdet * ((double)h0 * h1 - (double)h2 * h2);
+    o.km = o.area * invdet * 0.5 * ((double)h0 * g1 + (double)h1 * g0 - 2.0 * (double)h2 * g2);
+    return o;
+  }
+#undef FC
+}
+
+__global__ void __launch_bounds__(kBlock) k_elements32(DevBuf b, StepConst sc, ElemGroups eg) {
+  Ctl* ctl = b.ctl;
+  if (inactive(ctl)) return;
+  __shared__ double sh[kBlock / 32];
+  __shared__ float sB[kMaxSlots * 6];
+  int g = 0;
+  while (g + 1 < eg.n && blockIdx.x >= eg.g[g + 1].block_start) ++g;
+  const GroupDesc gd = eg.g[g];
+  for (int k = threadIdx.x; k < gd.n_slots * 6; k += blockDim.x) sB[k] = eg.basis32[gd.basis_off + k];
+  __syncthreads();
+  const uint32_t li = (blockIdx.x - gd.block_start) * blockDim.x + threadIdx.x;
+  ElemOut o{0, 0, 0, 0, 0};
+  const float pressure = (float)ctl->pressure, vol_p = (float)ctl->volume_pressure;
+  if (li < gd.count) {
+    const uint32_t i = gd.first + li;
+    if (gd.n_slots == 12)
+      o = element_force32<12>(i, 12, sB, b, sc, pressure, vol_p);
+    else if (gd.n_slots == 11)
+      o = element_force32<11>(i, 11, sB, b, sc, pressure, vol_p);
+    else
+      o = element_force32<0>(i, gd.n_slots, sB, b, sc, pressure, vol_p);
+    const uint32_t e = __ldg(&b.perm[i]);
+    b.area[e] = o.area;
+    b.kG[e] = o.kg / o.area;
+    b.kM[e] = o.km / o.area;
+    b.etens[e] = o.etens / o.area;
+    b.ebend[e] = o.ebend / o.area;
+  }
+  const double s0 = block_sum(o.etens, sh);
+  const double s1 = block_sum(o.ebend, sh);
+  const double s2 = block_sum(o.kg, sh);
+  const double s3 = block_sum(o.km, sh);
+  const double s4 = block_sum(o.area, sh);
+  if (threadIdx.x == 0) {
+    double* pp = b.partial + (size_t)blockIdx.x * 8;
+    pp[0] = s0; pp[1] = s1; pp[2] = s2; pp[3] = s3; pp[4] = s4;
+  }
+  if (!last_block(&ctl->cnt[1])) return;
+  const int nb = gridDim.x;
+  const double t0 = sum_partials(b.partial, 0, nb, sh);
+  const double t1 = sum_partials(b.partial, 1, nb, sh);
+  const double t2 = sum_partials(b.partial, 2, nb, sh);
+  const double t3 = sum_partials(b.partial, 3, nb, sh);
+  const double t4 = sum_partials(b.partial, 4, nb, sh);
+  if (threadIdx.x == 0) {
+    ctl->Etens = t0; ctl->Ebend = t1; ctl->kGauss = t2; ctl->kMean = t3; ctl->area = t4;
+  }
+}
+
 __global__ void __launch_bounds__(kBlock) k_elements(DevBuf b, StepConst sc, ElemGroups eg) {
   Ctl* ctl = b.ctl;
   if (inactive(ctl)) return;
@@ -499,11 +728,20 @@ __global__ void __launch_bounds__(kBlock) k_gather_correct(DevBuf b, StepConst s
       }
     }
     const uint32_t g0 = b.gather_ptr[n], g1 = b.gather_ptr[n + 1];
-    for (uint32_t k = g0; k < g1; ++k) {
-      const double* q = b.qe + 3 * (size_t)__ldg(&b.gather_ent[k]);
-      f[0] -= q[0];
-      f[1] -= q[1];
-      f[2] -= q[2];
+    if (sc.fp32) {
+      for (uint32_t k = g0; k < g1; ++k) {
+        const float* q = b.qe32 + 3 * (size_t)__ldg(&b.gather_ent[k]);
+        f[0] -= (double)q[0];
+        f[1] -= (double)q[1];
+        f[2] -= (double)q[2];
+      }
+    } else {
+      for (uint32_t k = g0; k < g1; ++k) {
+        const double* q = b.qe + 3 * (size_t)__ldg(&b.gather_ent[k]);
+        f[0] -= q[0];
+        f[1] -= q[1];
+        f[2] -= q[2];
+      }
     }
     double d[3];
 #pragma unroll
@@ -634,7 +872,10 @@ void launch_positions(const DevBuf& b, const StepConst& sc, cudaStream_t s) {
 }
 void launch_elements(const DevBuf& b, const StepConst& sc, const ElemGroups& eg, uint32_t n_blocks,
                      cudaStream_t s) {
-  k_elements<<<n_blocks, kBlock, 0, s>>>(b, sc, eg);
+  if (sc.fp32)
+    k_elements32<<<n_blocks, kBlock, 0, s>>>(b, sc, eg);
+  else
+    k_elements<<<n_blocks, kBlock, 0, s>>>(b, sc, eg);
 }
 void launch_contact_force(const DevBuf& b, const StepConst& sc, int, cudaStream_t s) {
   uint32_t nb = nblk(sc.pairs_cap);

@@ -296,6 +296,7 @@ bool build_setup(const shl_mesh& mesh, const shl_params& prm, Setup& S, std::str
 
   S.patch.assign(12 * (size_t)F, -1);
   S.face.assign((size_t)FF_COUNT * F, 0.0);
+  std::vector<double> face_bal((size_t)FF_COUNT * F, 0.0);  // balanced-frame constants (FP32 path)
   S.Minv.assign(3 * (size_t)V, 0.0);
   S.C.assign(3 * (size_t)V, 0.0);
   auto Xn = [&](uint32_t n) { return V3{S.X[3 * n], S.X[3 * n + 1], S.X[3 * n + 2]}; };
@@ -345,53 +346,65 @@ bool build_setup(const shl_mesh& mesh, const shl_params& prm, Setup& S, std::str
         c1 = (g22 * t1 - g12 * t2) / det;
         c2 = (g11 * t2 - g12 * t1) / det;
       };
-      double R00, R10, R01, R11;
-      coords(k, R00, R10);  // k = R00 b1 + R10 b2
-      coords(j, R01, R11);  // j = R01 b1 + R11 b2
-      put(FF_R00, R00); put(FF_R01, R01); put(FF_R10, R10); put(FF_R11, R11);
-      put(FF_JXW, JxW);
-      put(FF_X0, xq.x); put(FF_X1, xq.y); put(FF_X2, xq.z);
-
-      // second map with the rotated derivatives
-      V3 a1{0, 0, 0}, a2{0, 0, 0}, d11{0, 0, 0}, d22{0, 0, 0}, d12{0, 0, 0};
-      for (int s = 0; s < np; ++s) {
-        const double px = B[6 * s + 1], pe = B[6 * s + 2];
-        const double pxx = B[6 * s + 3], pee = B[6 * s + 4], pxe = B[6 * s + 5];
-        const double r1 = px * R00 + pe * R10;
-        const double r2 = px * R01 + pe * R11;
-        const double r11 = pxx * R00 * R00 + pee * R10 * R10 + 2 * pxe * R00 * R10;
-        const double r22 = pxx * R01 * R01 + pee * R11 * R11 + 2 * pxe * R01 * R11;
-        const double r12 = pxx * R00 * R01 + pee * R10 * R11 + pxe * (R01 * R10 + R00 * R11);
-        const V3 x = Xn(P[s]);
-        a1 = a1 + r1 * x;
-        a2 = a2 + r2 * x;
-        d11 = d11 + r11 * x;
-        d22 = d22 + r22 * x;
-        d12 = d12 + r12 * x;
-      }
-      const V3 a3u = cross(a1, a2);
-      const V3 a3 = (1.0 / norm(a3u)) * a3u;
-      const double ff1[3] = {dot(a1, a1), dot(a2, a2), dot(a1, a2)};
-      const double ff2[3] = {dot(d11, a3), dot(d22, a3), dot(d12, a3)};
-      put(FF_A10, a1.x); put(FF_A11, a1.y); put(FF_A12, a1.z);
-      put(FF_A20, a2.x); put(FF_A21, a2.y); put(FF_A22, a2.z);
-      put(FF_D10, d11.x); put(FF_D11, d11.y); put(FF_D12, d11.z);
-      put(FF_D20, d22.x); put(FF_D21, d22.y); put(FF_D22, d22.z);
-      put(FF_D30, d12.x); put(FF_D31, d12.y); put(FF_D32, d12.z);
-      put(FF_G0, ff1[0]); put(FF_G1, ff1[1]); put(FF_G2, ff1[2]);
-      put(FF_B0, ff2[0]); put(FF_B1, ff2[1]); put(FF_B2, ff2[2]);
-      // orthotropic H, ShellSystem.C:1199-1213 (constant for constant moduli)
-      {
+      // constants of the frame (kk, jj): rotation, reference metric, H
+      auto frame_constants = [&](V3 kk, V3 jj, double* out) {
+        double R00, R10, R01, R11;
+        coords(kk, R00, R10);  // kk = R00 b1 + R10 b2
+        coords(jj, R01, R11);  // jj = R01 b1 + R11 b2
+        out[FF_R00] = R00; out[FF_R01] = R01; out[FF_R10] = R10; out[FF_R11] = R11;
+        out[FF_JXW] = JxW;
+        out[FF_X0] = xq.x; out[FF_X1] = xq.y; out[FF_X2] = xq.z;
+        // second map with the rotated derivatives
+        V3 a1{0, 0, 0}, a2{0, 0, 0}, d11{0, 0, 0}, d22{0, 0, 0}, d12{0, 0, 0};
+        for (int s = 0; s < np; ++s) {
+          const double px = B[6 * s + 1], pe = B[6 * s + 2];
+          const double pxx = B[6 * s + 3], pee = B[6 * s + 4], pxe = B[6 * s + 5];
+          const double r1 = px * R00 + pe * R10;
+          const double r2 = px * R01 + pe * R11;
+          const double r11 = pxx * R00 * R00 + pee * R10 * R10 + 2 * pxe * R00 * R10;
+          const double r22 = pxx * R01 * R01 + pee * R11 * R11 + 2 * pxe * R01 * R11;
+          const double r12 = pxx * R00 * R01 + pee * R10 * R11 + pxe * (R01 * R10 + R00 * R11);
+          const V3 x = Xn(P[s]);
+          a1 = a1 + r1 * x;
+          a2 = a2 + r2 * x;
+          d11 = d11 + r11 * x;
+          d22 = d22 + r22 * x;
+          d12 = d12 + r12 * x;
+        }
+        const V3 a3u = cross(a1, a2);
+        const V3 a3 = (1.0 / norm(a3u)) * a3u;
+        const double ff1[3] = {dot(a1, a1), dot(a2, a2), dot(a1, a2)};
+        const double ff2[3] = {dot(d11, a3), dot(d22, a3), dot(d12, a3)};
+        out[FF_A10] = a1.x; out[FF_A11] = a1.y; out[FF_A12] = a1.z;
+        out[FF_A20] = a2.x; out[FF_A21] = a2.y; out[FF_A22] = a2.z;
+        out[FF_D10] = d11.x; out[FF_D11] = d11.y; out[FF_D12] = d11.z;
+        out[FF_D20] = d22.x; out[FF_D21] = d22.y; out[FF_D22] = d22.z;
+        out[FF_D30] = d12.x; out[FF_D31] = d12.y; out[FF_D32] = d12.z;
+        out[FF_G0] = ff1[0]; out[FF_G1] = ff1[1]; out[FF_G2] = ff1[2];
+        out[FF_B0] = ff2[0]; out[FF_B1] = ff2[1]; out[FF_B2] = ff2[2];
+        // orthotropic H, ShellSystem.C:1199-1213 (constant for constant moduli)
         const double nu2 = (E1 * nu) / E2;
         const double g0 = ff1[0], g1 = ff1[1], g2 = ff1[2];
         const double id = 1 / (g0 * g1 - g2 * g2);
         const double s2 = id * id;
-        put(FF_H00, s2 * (E1 * g1 * g1));
-        put(FF_H01, s2 * (E1 * (nu * g1 * g0 + (1 - nu) * g2 * g2)));
-        put(FF_H02, s2 * (E1 * -g1 * g2));
-        put(FF_H11, s2 * (E2 * g0 * g0));
-        put(FF_H12, s2 * (E2 * -g0 * g2));
-        put(FF_H22, s2 * (G12 * ((1 - nu * nu2) * g1 * g0 + (1 - nu * nu2) * ((1 + nu) / (1 - nu)) * g2 * g2)));
+        out[FF_H00] = s2 * (E1 * g1 * g1);
+        out[FF_H01] = s2 * (E1 * (nu * g1 * g0 + (1 - nu) * g2 * g2));
+        out[FF_H02] = s2 * (E1 * -g1 * g2);
+        out[FF_H11] = s2 * (E2 * g0 * g0);
+        out[FF_H12] = s2 * (E2 * -g0 * g2);
+        out[FF_H22] = s2 * (G12 * ((1 - nu * nu2) * g1 * g0 + (1 - nu * nu2) * ((1 + nu) / (1 - nu)) * g2 * g2));
+      };
+      double cref[FF_COUNT], cbal[FF_COUNT];
+      frame_constants(k, j, cref);
+      for (int fld = 0; fld < FF_COUNT; ++fld) put(fld, cref[fld]);
+      // The scaling of reinit_mod (kfac, jfac) degenerates when b1 is nearly
+      // parallel to the meridian j (kfac -> 0 and the constants span dozens of
+      // decades).  The mechanics does not depend on the lengths of k and j, so
+      // the FP32 path uses the same directions with |k| = |j| = sqrt(|b1 x b2|).
+      {
+        const double sq = std::sqrt(nn);
+        frame_constants((sq / norm(k)) * k, (sq / norm(j)) * j, cbal);
+        for (int fld = 0; fld < FF_COUNT; ++fld) face_bal[(size_t)fld * F + i] = cbal[fld];
       }
 
       // lumped mass and damping, ShellSystem.C:795-844
@@ -414,6 +427,29 @@ bool build_setup(const shl_mesh& mesh, const shl_params& prm, Setup& S, std::str
       }
     }
   }
+  // FP32 constants of the relative-displacement element path
+  S.face32.assign((size_t)F32_COUNT * F, 0.0f);
+  for (uint32_t i = 0; i < F; ++i) {
+    auto get = [&](int fld) { return face_bal[(size_t)fld * F + i]; };
+    auto put32 = [&](int fld, double x) { S.face32[(size_t)fld * F + i] = (float)x; };
+    const int map64[][2] = {{F32_R00, FF_R00}, {F32_R01, FF_R01}, {F32_R10, FF_R10}, {F32_R11, FF_R11},
+                            {F32_JXW, FF_JXW}, {F32_X0, FF_X0}, {F32_X1, FF_X1}, {F32_X2, FF_X2},
+                            {F32_A10, FF_A10}, {F32_A11, FF_A11}, {F32_A12, FF_A12}, {F32_A20, FF_A20},
+                            {F32_A21, FF_A21}, {F32_A22, FF_A22}, {F32_D10, FF_D10}, {F32_D11, FF_D11},
+                            {F32_D12, FF_D12}, {F32_D20, FF_D20}, {F32_D21, FF_D21}, {F32_D22, FF_D22},
+                            {F32_D30, FF_D30}, {F32_D31, FF_D31}, {F32_D32, FF_D32}, {F32_G0, FF_G0},
+                            {F32_G1, FF_G1}, {F32_G2, FF_G2}, {F32_H00, FF_H00}, {F32_H01, FF_H01},
+                            {F32_H02, FF_H02}, {F32_H11, FF_H11}, {F32_H12, FF_H12}, {F32_H22, FF_H22}};
+    for (const auto& m : map64) put32(m[0], get(m[1]));
+    const V3 a1{get(FF_A10), get(FF_A11), get(FF_A12)}, a2{get(FF_A20), get(FF_A21), get(FF_A22)};
+    const V3 n = cross(a1, a2);
+    const double L = norm(n);
+    put32(F32_N0, n.x / L);
+    put32(F32_N1, n.y / L);
+    put32(F32_N2, n.z / L);
+    put32(F32_L0, L);
+  }
+
   for (double& c : S.C) c += prm.damping_gamma;
   for (double& m : S.Minv) {
     if (!(m > 0)) { err = "non-positive lumped mass"; return false; }

@@ -39,6 +39,20 @@ enum FaceField {
   FF_COUNT
 };
 
+// Per-face FP32 constants of the FP32 element path (structure of arrays).
+// The strains are formed from the displacement relative to this reference
+// geometry, so no difference of nearly equal metrics is taken.
+enum FaceField32 {
+  F32_R00, F32_R01, F32_R10, F32_R11, F32_JXW,
+  F32_X0, F32_X1, F32_X2,
+  F32_A10, F32_A11, F32_A12, F32_A20, F32_A21, F32_A22,
+  F32_D10, F32_D11, F32_D12, F32_D20, F32_D21, F32_D22, F32_D30, F32_D31, F32_D32,
+  F32_G0, F32_G1, F32_G2,          // a_ref.ff1
+  F32_N0, F32_N1, F32_N2, F32_L0,  // unit normal and |a1 x a2| of the reference
+  F32_H00, F32_H01, F32_H02, F32_H11, F32_H12, F32_H22,
+  F32_COUNT
+};
+
 struct PatchGroup {
   int valence;        // valence of the first vertex (6 = regular)
   int n_slots;        // valence + 6
@@ -56,6 +70,7 @@ struct Setup {
   std::vector<PatchGroup> groups;  // groups[0] = regular
   std::vector<int32_t> patch;      // [slot * F + internal face], -1 for unused slots
   std::vector<double> face;        // [field * F + internal face]
+  std::vector<float> face32;       // [FaceField32 * F + internal face]
   std::vector<double> Minv, C;     // 3V node-major
   std::vector<uint32_t> gather_ptr;  // V+1
   std::vector<uint32_t> gather_ent;  // internal_face * 12 + slot, ascending per node
