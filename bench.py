@@ -73,6 +73,63 @@ def pressure(step):
     return -RAMP_FACTOR * classical_pressure() * np.asarray(step, dtype=np.float64) / RAMP_STEPS
 
 
+def ensemble_workload(L, n_shells=256, seed=0):
+    """256 shells, levels uniform over 3/4/5, per-shell parameters from a seed:
+    E1/E2 log-uniform in [0.2, 5] (E1 E2 = 1), h/R log-uniform in [0.005, 0.05],
+    pressure ramp end uniform in [1.2, 3] p_cl of the shell, imperfection
+    amplitude log-uniform in [1e-4, 1e-2] R; FP32 element forces."""
+    rng = np.random.default_rng(seed)
+    meshes = {lv: L.icosphere(lv) for lv in (3, 4, 5)}
+    shells, params, scale, u0 = [], [], [], []
+    for k in range(n_shells):
+        lv = int(rng.integers(3, 6))
+        r = float(np.exp(rng.uniform(np.log(0.2), np.log(5.0))))
+        h = float(np.exp(rng.uniform(np.log(0.005), np.log(0.05))))
+        s = float(rng.uniform(1.2, 3.0))
+        amp = float(np.exp(rng.uniform(np.log(1e-4), np.log(1e-2))))
+        e1, e2 = np.sqrt(r), 1.0 / np.sqrt(r)
+        E = np.sqrt(e1 * e2)
+        nu = np.sqrt(NU12 * NU12 * e2 / e1)
+        p_cl = 2 * E * h * h / np.sqrt(3 * (1 - nu * nu))
+        X, T = meshes[lv]
+        params.append(L.default_params(shell_mass_density=RHO, shell_young_modulus=e1, shell_young_modulus2=e2,
+                                       shell_poisson_ratio=NU12, shell_shear_modulus=G12 * E, thickness=h,
+                                       damping_alpha=ALPHA, dt=DT, shell_shell_contact=L.CONTACT_NONE,
+                                       precision=L.PREC_FP32))
+        shells.append((X, T))
+        scale.append(s * p_cl)
+        u0.append(L.gaussian_normal_imperfection(X, amp, seed * 100000 + k).reshape(-1))
+    return shells, params, np.array(scale), np.concatenate(u0)
+
+
+def time_ensemble(L, torch, K, W, flush):
+    shells, params, scale, u0 = ensemble_workload(L)
+    b = L.Batch(shells, params, pressure_scale=scale)
+    ramp = lambda st: -np.asarray(st, dtype=np.float64) / RAMP_STEPS  # noqa: E731
+    b.apply_initial_conditions(u0, 0.0, ramp(1))
+    b.upload_pressure_table(ramp(np.arange(1, 1 + W + K)))
+    b.step_enqueue(W)
+    torch.cuda.synchronize()
+    stream = torch.cuda.ExternalStream(b.stream_handle())
+    st = [torch.cuda.Event(enable_timing=True) for _ in range(K)]
+    en = [torch.cuda.Event(enable_timing=True) for _ in range(K)]
+    with torch.cuda.stream(stream):
+        for k in range(K):
+            flush.fill_(k)
+            st[k].record(stream)
+            b.step_enqueue(1)
+            en[k].record(stream)
+    torch.cuda.synchronize()
+    ms = sum(a.elapsed_time(e) for a, e in zip(st, en))
+    rep, status = b.step_collect()
+    F = b.F
+    b.close()
+    levels = [int(round(np.log(len(T) / 20) / np.log(4))) for _, T in shells]
+    return {"value": F * K / (ms * 1e-3), "unit": "face-steps/s", "ms_per_step": ms / K, "shells": len(shells),
+            "faces": int(F), "levels": {str(lv): levels.count(lv) for lv in (3, 4, 5)}, "dtype": "f32 forces, f64 state",
+            "steps": K, "status": int(status)}
+
+
 def cpu_sample(X, T, p, u0, seconds=10.0, threads=None):
     """CPU oracle on the same workload: steps until about `seconds` elapsed."""
     import oracle as O
@@ -239,6 +296,8 @@ def run_ours(args, rank, world, dist):
         g32.close()
         fp32_value = F * K / (ms32 * 1e-3)
 
+    ensemble = time_ensemble(L, torch, max(20, K // 4), W, flush) if args.ensemble else None
+
     # warm continuous throughput (informative): K steps back to back, one graph replay per 16 steps
     g.upload_pressure_table(pressure(np.arange(1 + W + K, 1 + W + 2 * K)))
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -295,6 +354,7 @@ def run_ours(args, rank, world, dist):
                    "l2": "evicted before every timed step (512 MB write)"},
         "warm_value": warm,
         "fp32_value": fp32_value,
+        "ensemble": ensemble,
         "e2e": {"value": e2e, "unit": "face-steps/s", "h2d_bytes_per_step": 3 * 3 * V * 8,
                 "d2h_bytes_per_step": 3 * 3 * V * 8,
                 "how": "per step: shl_set_state from pinned host, shl_step(1), shl_get_state"},
@@ -322,6 +382,7 @@ def main():
     ap.add_argument("--level", type=int, default=6)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--fp32", type=int, default=1, help="also time the FP32 element-force mode")
+    ap.add_argument("--ensemble", type=int, default=1, help="also time the 256-shell batched ensemble")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     world = int(os.environ.get("WORLD_SIZE", "1"))

@@ -143,6 +143,20 @@ const char* shl_last_error(void);
 /* Human-readable name of a status. */
 const char* shl_status_string(shl_status s);
 
+/* A batch of independent shells advanced together (one context over the
+ * union of the meshes; no counterpart in the reference, which runs one shell
+ * per process).  Each shell has its own mesh and material/damping/thickness;
+ * dt, the Newmark parameters, the precision and the pressure basis are
+ * shared.  The pressure of shell k in a step is pressure_scale[k] times the
+ * step's value (its ramp).  Self-contact and bulk-modulus pressure are
+ * evaluated for single shells only (rejected here).  State vectors of a batch
+ * are the shells' node-major vectors concatenated; shl_batch_layout gives the
+ * node and face offsets (n_shells + 1 entries each).  Energies and the volume
+ * reported by shl_step are batch totals. */
+shl_status shl_batch_create(const shl_mesh* meshes, const shl_params* params, const double* pressure_scale,
+                            uint32_t n_shells, shl_ctx** out);
+shl_status shl_batch_layout(shl_ctx* ctx, uint32_t* n_shells, uint32_t* node_offsets, uint32_t* face_offsets);
+
 /* Set-up: ShellSystem::set_parameters + build_cache + compute_mass_damping
  * (ShellSystem.C:170-418, 490-681, 762-852).  Computes the subdivision basis,
  * the reference metrics, masses, damping and the topological neighbourhood on
@@ -204,6 +218,15 @@ shl_status shl_step_collect(shl_ctx* ctx, shl_step_report* report);
  * which: 0 element kernel, 1 gather/corrector (evaluation mode),
  * 2 contact force, 3 predictor. */
 shl_status shl_time_kernel(shl_ctx* ctx, int which, int reps, size_t flush_bytes, double* avg_ms);
+/* Per-phase timing of one step (the step is taken: the state advances):
+ * the phases of advance() are launched directly, with CUDA events between
+ * them, after evicting L2 with a write of flush_bytes (0 = no eviction).
+ * ms_out[0..6]: predictor, linked-cell pass 1, element forces, contact forces,
+ * gather + corrector, linked-cell pass 2, volume + end of step.  This is the
+ * tracing counterpart of the reference's PERFLOG_START/STOP scopes
+ * (macros.h:81-88). */
+shl_status shl_profile_step(shl_ctx* ctx, double pressure, size_t flush_bytes, double* ms_out);
+
 /* FP64 fused-multiply-add throughput of the current device, measured with a
  * register-resident DFMA loop (TFLOP/s, 2 flops per DFMA). */
 shl_status shl_measure_fp64_peak(double* tflops);

@@ -55,6 +55,7 @@ struct shl_ctx {
   double* d_fa = nullptr;   // device f and a of shl_eval_forces, 2 x 3V doubles
   void* d_flush = nullptr;  // L2 eviction buffer of shl_time_kernel
   size_t flush_bytes = 0;
+  std::vector<uint32_t> node_off, face_off;  // shell offsets (original order) of a batch
 };
 
 namespace {
@@ -282,18 +283,15 @@ void shl_destroy(shl_ctx* c) {
   delete c;
 }
 
-shl_status shl_create(const shl_mesh* mesh, const shl_params* params, shl_ctx** out) {
-  if (!mesh || !params || !out) { g_err = "null argument"; return SHL_ERR_ARG; }
-  *out = nullptr;
+}  // extern "C"
+
+namespace {
+
+// Device allocation, uploads and step constants for a context whose set-up
+// (c->S, one shell or a merged batch) is built; pscale: per original face.
+shl_status create_common(shl_ctx* c, const std::vector<double>& pscale_orig, shl_ctx** out) {
+  const shl_params* params = &c->P;
   std::string err;
-  if (!validate(*params, err)) { g_err = err; return SHL_ERR_ARG; }
-  shl_ctx* c = new shl_ctx;
-  c->P = *params;
-  if (!build_setup(*mesh, *params, c->S, err)) {
-    g_err = err;
-    delete c;
-    return SHL_ERR_ARG;
-  }
   shl_status st = SHL_OK;
   auto fail = [&](shl_status s) { shl_destroy(c); return s; };
   if (cudaGetDevice(&c->device) != cudaSuccess || cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
@@ -307,12 +305,13 @@ shl_status shl_create(const shl_mesh* mesh, const shl_params* params, shl_ctx** 
   const size_t nd = 3 * (size_t)V;
 #define ALLOC(ptr, n) do { if ((st = dev_alloc(c, &(ptr), (n))) != SHL_OK) return fail(st); } while (0)
   ALLOC(b.X, nd); ALLOC(b.u, nd); ALLOC(b.v, nd); ALLOC(b.a, nd); ALLOC(b.up, nd); ALLOC(b.vp, nd);
-  ALLOC(b.p, nd); ALLOC(b.Minv, nd); ALLOC(b.C, nd);
+  ALLOC(b.p, nd); ALLOC(b.Minv, nd); ALLOC(b.C, nd); ALLOC(b.M, nd);
   ALLOC(b.face, (size_t)FF_COUNT * F);
   ALLOC(b.patch, 12 * (size_t)F);
   const bool fp32 = params->precision == SHL_PREC_FP32;
   if (fp32) {
     ALLOC(b.qe32, 36 * (size_t)F);
+    ALLOC(b.up32, nd);
     ALLOC(b.face32, (size_t)F32_COUNT * F);
   }
   ALLOC(b.qe, fp32 ? 1 : 36 * (size_t)F);
@@ -320,6 +319,7 @@ shl_status shl_create(const shl_mesh* mesh, const shl_params* params, shl_ctx** 
   ALLOC(b.gather_ent, S.gather_ent.size());
   ALLOC(b.tri, 3 * (size_t)F);
   ALLOC(b.perm, F);
+  ALLOC(b.pscale, F);
   ALLOC(b.area, F); ALLOC(b.kG, F); ALLOC(b.kM, F); ALLOC(b.etens, F); ALLOC(b.ebend, F);
   // element launch: one block range per patch group
   std::vector<GroupDesc> gd;
@@ -366,6 +366,7 @@ shl_status shl_create(const shl_mesh* mesh, const shl_params* params, shl_ctx** 
     ALLOC(b.cell_count, n_cells_cap); ALLOC(b.cell_start, n_cells_cap + 1); ALLOC(b.cell_fill, n_cells_cap);
     ALLOC(b.cell_items, entries_cap);
     ALLOC(b.entry_cell, entries_cap);
+    ALLOC(b.p32, nd);
     const size_t scan_cap = std::max<size_t>({(size_t)n_cells_cap, (size_t)F + 1, (size_t)V + 1});
     ALLOC(b.scan_block, scan_cap / kScanTile + 2);
     for (int k = 0; k < 2; ++k) {
@@ -386,6 +387,9 @@ shl_status shl_create(const shl_mesh* mesh, const shl_params* params, shl_ctx** 
   if ((st = upload(c, b.X, S.X.data(), nd)) != SHL_OK) return fail(st);
   if ((st = upload(c, b.p, S.X.data(), nd)) != SHL_OK) return fail(st);
   if ((st = upload(c, b.Minv, S.Minv.data(), nd)) != SHL_OK) return fail(st);
+  std::vector<double> mass(nd);
+  for (size_t k = 0; k < nd; ++k) mass[k] = 1.0 / S.Minv[k];
+  if ((st = upload(c, b.M, mass.data(), nd)) != SHL_OK) return fail(st);
   if ((st = upload(c, b.C, S.C.data(), nd)) != SHL_OK) return fail(st);
   if ((st = upload(c, b.face, S.face.data(), S.face.size())) != SHL_OK) return fail(st);
   if (fp32 && (st = upload(c, b.face32, S.face32.data(), S.face32.size())) != SHL_OK) return fail(st);
@@ -394,6 +398,9 @@ shl_status shl_create(const shl_mesh* mesh, const shl_params* params, shl_ctx** 
   if ((st = upload(c, b.gather_ent, S.gather_ent.data(), S.gather_ent.size())) != SHL_OK) return fail(st);
   if ((st = upload(c, b.tri, S.tri.data(), S.tri.size())) != SHL_OK) return fail(st);
   if ((st = upload(c, b.perm, S.perm.data(), S.perm.size())) != SHL_OK) return fail(st);
+  std::vector<double> pscale(F);
+  for (uint32_t i = 0; i < F; ++i) pscale[i] = pscale_orig[S.perm[i]];
+  if ((st = upload(c, b.pscale, pscale.data(), F)) != SHL_OK) return fail(st);
   if (contact) {
     if ((st = upload(c, b.close_ptr, S.close_ptr.data(), S.close_ptr.size())) != SHL_OK) return fail(st);
     if (!S.close_list.empty() && (st = upload(c, b.close_list, S.close_list.data(), S.close_list.size())) != SHL_OK)
@@ -459,8 +466,81 @@ shl_status shl_create(const shl_mesh* mesh, const shl_params* params, shl_ctx** 
   if ((st = ctl_put(c, h)) != SHL_OK) return fail(st);
   if (cudaMallocHost(&c->h_pin, 3 * nd * sizeof(double)) != cudaSuccess) c->h_pin = nullptr;
   if ((st = check_launch("shl_create")) != SHL_OK) return fail(st);
-  SHL_CUDA_TRY(cudaStreamSynchronize(c->stream));
+  if (cudaStreamSynchronize(c->stream) != cudaSuccess) {
+    g_err = "stream synchronisation failed in shl_create";
+    return fail(SHL_ERR_CUDA);
+  }
   *out = c;
+  return SHL_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+shl_status shl_create(const shl_mesh* mesh, const shl_params* params, shl_ctx** out) {
+  if (!mesh || !params || !out) { g_err = "null argument"; return SHL_ERR_ARG; }
+  *out = nullptr;
+  std::string err;
+  if (!validate(*params, err)) { g_err = err; return SHL_ERR_ARG; }
+  shl_ctx* c = new shl_ctx;
+  c->P = *params;
+  if (!build_setup(*mesh, *params, c->S, err)) {
+    g_err = err;
+    delete c;
+    return SHL_ERR_ARG;
+  }
+  c->node_off = {0, c->S.V};
+  c->face_off = {0, c->S.F};
+  return create_common(c, std::vector<double>(c->S.F, 1.0), out);
+}
+
+shl_status shl_batch_create(const shl_mesh* meshes, const shl_params* params, const double* pressure_scale,
+                            uint32_t n_shells, shl_ctx** out) {
+  if (!meshes || !params || !out || n_shells == 0) { g_err = "null argument"; return SHL_ERR_ARG; }
+  *out = nullptr;
+  std::string err;
+  const shl_params& p0 = params[0];
+  for (uint32_t k = 0; k < n_shells; ++k) {
+    const shl_params& p = params[k];
+    if (!validate(p, err)) { g_err = "shell " + std::to_string(k) + ": " + err; return SHL_ERR_ARG; }
+    if (p.shell_shell_contact != SHL_CONTACT_NONE || p.bulk_modulus != 0.0) {
+      g_err = "batched shells: self-contact and bulk-modulus pressure are evaluated per single shell only";
+      return SHL_ERR_ARG;
+    }
+    if (p.dt != p0.dt || p.newmark_beta != p0.newmark_beta || p.newmark_gamma != p0.newmark_gamma ||
+        p.precision != p0.precision || p.pressure_base != p0.pressure_base || p.pressure_dir != p0.pressure_dir ||
+        p.compat_zero_pressure != p0.compat_zero_pressure) {
+      g_err = "batched shells must share dt, Newmark parameters, precision and pressure basis";
+      return SHL_ERR_ARG;
+    }
+  }
+  std::vector<Setup> shells(n_shells);
+  std::vector<std::string> errs(n_shells);
+  std::vector<char> ok(n_shells, 0);
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int64_t k = 0; k < (int64_t)n_shells; ++k) ok[k] = build_setup(meshes[k], params[k], shells[k], errs[k]) ? 1 : 0;
+  for (uint32_t k = 0; k < n_shells; ++k)
+    if (!ok[k]) { g_err = "shell " + std::to_string(k) + ": " + errs[k]; return SHL_ERR_ARG; }
+  shl_ctx* c = new shl_ctx;
+  c->P = p0;
+  std::vector<uint32_t> face_shell;
+  if (!merge_setups(shells, c->S, c->node_off, c->face_off, face_shell, err)) {
+    g_err = err;
+    delete c;
+    return SHL_ERR_ARG;
+  }
+  std::vector<double> pscale(c->S.F);
+  for (uint32_t f = 0; f < c->S.F; ++f) pscale[f] = pressure_scale ? pressure_scale[face_shell[f]] : 1.0;
+  return create_common(c, pscale, out);
+}
+
+shl_status shl_batch_layout(shl_ctx* c, uint32_t* n_shells, uint32_t* node_offsets, uint32_t* face_offsets) {
+  if (!c) return SHL_ERR_ARG;
+  const uint32_t n = (uint32_t)c->node_off.size() - 1;
+  if (n_shells) *n_shells = n;
+  if (node_offsets) std::copy(c->node_off.begin(), c->node_off.end(), node_offsets);
+  if (face_offsets) std::copy(c->face_off.begin(), c->face_off.end(), face_offsets);
   return SHL_OK;
 }
 
@@ -770,6 +850,47 @@ shl_status shl_time_kernel(shl_ctx* c, int which, int reps, size_t flush_bytes, 
   SHL_TRY(ctl_put(c, h));
   *avg_ms = total / reps;
   return SHL_OK;
+}
+
+shl_status shl_profile_step(shl_ctx* c, double pressure, size_t flush_bytes, double* ms_out) {
+  if (!c || !ms_out) return SHL_ERR_ARG;
+  if (flush_bytes > c->flush_bytes) {
+    if (c->d_flush) cudaFree(c->d_flush);
+    c->d_flush = nullptr;
+    c->flush_bytes = 0;
+    SHL_CUDA_TRY(cudaMalloc(&c->d_flush, flush_bytes));
+    c->flush_bytes = flush_bytes;
+  }
+  SHL_TRY(upload_table(c, &pressure, 1));
+  cudaEvent_t ev[8];
+  for (auto& e : ev) SHL_CUDA_TRY(cudaEventCreate(&e));
+  const DevBuf& b = c->b;
+  const StepConst& sc = c->sc;
+  cudaStream_t s = c->stream;
+  if (flush_bytes) launch_flush(c->d_flush, flush_bytes, 7u, s);
+  cudaEventRecord(ev[0], s);
+  launch_predict(b, sc, 0, s);
+  cudaEventRecord(ev[1], s);
+  if (sc.contact) launch_rebuild(b, sc, s);
+  cudaEventRecord(ev[2], s);
+  launch_elements(b, sc, c->eg, c->elem_blocks, s);
+  cudaEventRecord(ev[3], s);
+  if (sc.contact) launch_contact_force(b, sc, 0, s);
+  cudaEventRecord(ev[4], s);
+  launch_gather_correct(b, sc, 0, true, nullptr, nullptr, s);
+  cudaEventRecord(ev[5], s);
+  if (sc.contact) launch_rebuild(b, sc, s);
+  cudaEventRecord(ev[6], s);
+  launch_volume_end_step(b, sc, true, s);
+  cudaEventRecord(ev[7], s);
+  SHL_CUDA_TRY(cudaEventSynchronize(ev[7]));
+  for (int k = 0; k < 7; ++k) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, ev[k], ev[k + 1]);
+    ms_out[k] = ms;
+  }
+  for (auto& e : ev) cudaEventDestroy(e);
+  return check_launch("shl_profile_step");
 }
 
 shl_status shl_measure_fp64_peak(double* tflops) {

@@ -187,6 +187,7 @@ __global__ void k_rb_clear(DevBuf b, StepConst sc) {
     b.new_cnt[i] = 0;
     b.new_fill[i] = 0;
   }
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < 3 * sc.V; i += stride) b.p32[i] = (float)b.p[i];
   if (blockIdx.x == 0 && threadIdx.x == 0) ctl->n_cand = 0;
 }
 
@@ -381,27 +382,30 @@ __device__ __forceinline__ uint32_t sorted_find(const uint32_t* a, uint32_t lo, 
 }
 
 // ---------------------------------------------------------------- pairs --
-// Conservative separating-axis test along the line of centroids: true only
-// when the triangles are certainly farther apart than d_max, with a margin far
-// above the rounding error of the projections, so it never removes a pair
-// that the separately rounded closest-point solve would accept.
-__device__ __forceinline__ bool certainly_apart(const double* const* P1, const double* const* P2, double d_max) {
-  double d[3], S = 0.0;
+// Conservative separating-axis test along the line of centroids, in FP32 on
+// FP32 copies of the positions: true only when the triangles are certainly
+// farther apart than d_max.  The bound on the rounding error of the FP32
+// projections (including the rounding of the positions to FP32) is
+// 32 eps32 |d| S with S the largest coordinate magnitude, and the remaining
+// relative margin (1e-5) is far above the rounding of the FP64 closest-point
+// solve, so the test never removes a pair that the exact path would accept
+// (or that the AABB test would keep and the closest-point test accept).
+__device__ __forceinline__ bool certainly_apart32(const float* const* P1, const float* const* P2, float d_max) {
+  float d[3], S = 0.f;
   for (int c = 0; c < 3; ++c) {
     d[c] = (P2[0][c] + P2[1][c] + P2[2][c]) - (P1[0][c] + P1[1][c] + P1[2][c]);
-    for (int k = 0; k < 3; ++k) S = fmax(S, fmax(fabs(P1[k][c]), fabs(P2[k][c])));
+    for (int k = 0; k < 3; ++k) S = fmaxf(S, fmaxf(fabsf(P1[k][c]), fabsf(P2[k][c])));
   }
-  const double L2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
-  if (!(L2 > 0.0)) return false;
-  double mx1 = -SHL_DBL_MAX, mn2 = SHL_DBL_MAX;
+  const float L2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+  if (!(L2 > 0.f)) return false;
+  float mx1 = -3.0e38f, mn2 = 3.0e38f;
   for (int k = 0; k < 3; ++k) {
-    mx1 = fmax(mx1, d[0] * P1[k][0] + d[1] * P1[k][1] + d[2] * P1[k][2]);
-    mn2 = fmin(mn2, d[0] * P2[k][0] + d[1] * P2[k][1] + d[2] * P2[k][2]);
+    mx1 = fmaxf(mx1, d[0] * P1[k][0] + d[1] * P1[k][1] + d[2] * P1[k][2]);
+    mn2 = fminf(mn2, d[0] * P2[k][0] + d[1] * P2[k][1] + d[2] * P2[k][2]);
   }
-  const double L = sqrt(L2);
-  // |rounding error of mn2 - mx1| <= 8 eps |d| (3 S); distance >= true gap / |d|
-  const double gap = (mn2 - mx1) - 8.0 * 2.220446049250313e-16 * L * 3.0 * S;
-  return gap > d_max * L * (1.0 + 1e-8);
+  const float L = sqrtf(L2);
+  const float gap = (mn2 - mx1) - 32.f * 5.9604645e-8f * L * S;
+  return gap > d_max * L * (1.f + 1e-5f);
 }
 
 // Candidate pairs of one (cell, face) entry: faces e2 > e1 in the cell, emitted
@@ -415,6 +419,7 @@ __global__ void __launch_bounds__(kBlock) k_rb_cand(DevBuf b, StepConst sc) {
   const uint32_t stride = gridDim.x * blockDim.x;
   const uint32_t ny = ctl->ncd[1], nz = ctl->ncd[2];
   const double d_max = ctl->d_max;
+  const float d_max32 = (float)d_max;
   constexpr int kBuf = 8;
   uint32_t buf1[kBuf], buf2[kBuf];
   int nb = 0;
@@ -440,11 +445,11 @@ __global__ void __launch_bounds__(kBlock) k_rb_cand(DevBuf b, StepConst sc) {
     const uint32_t c0 = b.close_ptr[e1], c1 = b.close_ptr[e1 + 1];
     const uint32_t o0 = b.pair_ptr[0][e1], o1 = b.pair_ptr[0][e1 + 1];
     double mn1[3], mx1[3];
-    const double* P1[3];
+    const float* Q1[3];
     for (int c = 0; c < 3; ++c) {
       mn1[c] = b.bmin[3 * (size_t)e1 + c];
       mx1[c] = b.bmax[3 * (size_t)e1 + c];
-      P1[c] = b.p + 3 * (size_t)b.tri[3 * (size_t)e1 + c];
+      Q1[c] = b.p32 + 3 * (size_t)b.tri[3 * (size_t)e1 + c];
     }
     const uint32_t s0 = b.cell_start[cell], cnt = b.cell_count[cell];
     for (uint32_t k = 0; k < cnt; ++k) {
@@ -453,6 +458,11 @@ __global__ void __launch_bounds__(kBlock) k_rb_cand(DevBuf b, StepConst sc) {
       const int* lo2 = b.cell_lo + 3 * (size_t)e2;
       if ((uint32_t)max(l10, lo2[0]) != cx || (uint32_t)max(l11, lo2[1]) != cy || (uint32_t)max(l12, lo2[2]) != cz)
         continue;
+      {
+        const float* Q2[3];
+        for (int q = 0; q < 3; ++q) Q2[q] = b.p32 + 3 * (size_t)b.tri[3 * (size_t)e2 + q];
+        if (certainly_apart32(Q1, Q2, d_max32)) continue;
+      }
       if (sorted_contains(b.close_list, c0, c1, e2)) continue;
       const uint32_t at = sorted_find(b.pe2[0], o0, o1, e2);
       if (at < o1 && b.pkeep[at]) continue;
@@ -462,9 +472,6 @@ __global__ void __launch_bounds__(kBlock) k_rb_cand(DevBuf b, StepConst sc) {
         apart = apart || mn1[c] > __dadd_rn(mx2, d_max) || mn2 > __dadd_rn(mx1[c], d_max);
       }
       if (apart) continue;
-      const double* P2[3];
-      for (int q = 0; q < 3; ++q) P2[q] = b.p + 3 * (size_t)b.tri[3 * (size_t)e2 + q];
-      if (certainly_apart(P1, P2, d_max)) continue;
       buf1[nb] = e1;
       buf2[nb] = e2;
       if (++nb == kBuf) flush();

@@ -119,11 +119,14 @@ struct StepConst {
 // Device buffers of one context.
 struct DevBuf {
   double *X, *u, *v, *a, *up, *vp, *p, *Minv, *C;
+  double* M;          // 3V lumped masses (1 / Minv), for the kinetic energy
   double* face;       // FF_COUNT * F
+  double* pscale;     // F (internal order): factor on the step's pressure (per shell)
   int32_t* patch;     // 12 * F
   double* qe;         // F * 12 * 3
   float* face32;      // F32_COUNT * F (FP32 element path)
   float* qe32;        // F * 12 * 3 (FP32 element path)
+  float* up32;        // 3V, FP32 copy of u_pred (FP32 element path)
   uint32_t *gather_ptr, *gather_ent;
   uint32_t* tri;      // 3F original order
   uint32_t *perm;     // internal -> original
@@ -145,6 +148,7 @@ struct DevBuf {
   double* new_d2;
   uint32_t *new_off, *new_cnt, *new_fill;  // per face: offset, count, fill cursor of its new pairs
   uint32_t* entry_cell;        // cell of each (cell, face) entry
+  float* p32;                  // 3V, FP32 copy of the positions for the candidate prefilter
   uint32_t *cand_e1, *cand_e2; // candidates that passed the cheap filters
   double* cand_d2;
   uint8_t* cand_ok;

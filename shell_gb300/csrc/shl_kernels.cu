@@ -103,10 +103,19 @@ __global__ void __launch_bounds__(kBlock) k_predict(DevBuf b, StepConst sc) {
     for (int c = 0; c < 3; ++c) {
       const size_t k = 3 * (size_t)n + c;
       const double u = b.u[k], v = b.v[k], a = b.a[k];
-      double up = __dadd_rn(__dmul_rn(sc.dt, v), u);
-      up = __dadd_rn(__dmul_rn(sc.nm8, a), up);
+      double up, vp;
+      if (sc.contact) {
+        // separately rounded, as the host does: positions feed the contact list
+        up = __dadd_rn(__dmul_rn(sc.dt, v), u);
+        up = __dadd_rn(__dmul_rn(sc.nm8, a), up);
+        vp = __dadd_rn(__dmul_rn(sc.nm6, a), v);
+      } else {
+        up = fma(sc.nm8, a, fma(sc.dt, v, u));
+        vp = fma(sc.nm6, a, v);
+      }
       b.up[k] = up;
-      b.vp[k] = __dadd_rn(__dmul_rn(sc.nm6, a), v);
+      if (sc.fp32) b.up32[k] = (float)up;
+      b.vp[k] = vp;
       b.p[k] = __dadd_rn(b.X[k], up);
       d[c] = __dsub_rn(up, u);
     }
@@ -151,6 +160,7 @@ __global__ void k_positions(DevBuf b, StepConst sc) {
   for (int c = 0; c < 3; ++c) {
     const size_t k = 3 * (size_t)n + c;
     b.p[k] = __dadd_rn(b.X[k], b.up[k]);
+    if (sc.fp32) b.up32[k] = (float)b.up[k];
   }
 }
 
@@ -233,13 +243,14 @@ __device__ __forceinline__ ElemOut element_force(uint32_t i, int np_rt, const do
   const double be0 = FC(FF_B0) - h0, be1 = FC(FF_B1) - h1, be2 = 2.0 * (FC(FF_B2) - h2);
   const double H00 = FC(FF_H00), H01 = FC(FF_H01), H02 = FC(FF_H02), H11 = FC(FF_H11), H12 = FC(FF_H12),
                H22 = FC(FF_H22);
+  const double Kf = FC(FF_K), Df = FC(FF_D);
 #undef FC
-  const double n0 = sc.K * (H00 * al0 + H01 * al1 + H02 * al2);
-  const double n1 = sc.K * (H01 * al0 + H11 * al1 + H12 * al2);
-  const double n2 = sc.K * (H02 * al0 + H12 * al1 + H22 * al2);
-  const double m0 = sc.D * (H00 * be0 + H01 * be1 + H02 * be2);
-  const double m1 = sc.D * (H01 * be0 + H11 * be1 + H12 * be2);
-  const double m2 = sc.D * (H02 * be0 + H12 * be1 + H22 * be2);
+  const double n0 = Kf * (H00 * al0 + H01 * al1 + H02 * al2);
+  const double n1 = Kf * (H01 * al0 + H11 * al1 + H12 * al2);
+  const double n2 = Kf * (H02 * al0 + H12 * al1 + H22 * al2);
+  const double m0 = Df * (H00 * be0 + H01 * be1 + H02 * be2);
+  const double m1 = Df * (H01 * be0 + H11 * be1 + H12 * be2);
+  const double m2 = Df * (H02 * be0 + H12 * be1 + H22 * be2);
   // sum_k m_k p_1k and sum_k m_k p_2k of eq. (A6) (ShellSystem.C:1223-1233)
   double M[3], a2xa3[3], a3xa1[3], Mxa2[3], a1xM[3];
 #pragma unroll
@@ -339,9 +350,9 @@ __device__ __forceinline__ ElemOut element_force32(uint32_t i, int np_rt, const 
   for (int s = 0; s < (NP > 0 ? NP : kMaxSlots); ++s) {
     if (NP == 0 && s >= np) break;
     const int nd = __ldg(&b.patch[(size_t)s * F + i]);
-    const float ux = (float)__ldg(&b.up[3 * (size_t)nd]);
-    const float uy = (float)__ldg(&b.up[3 * (size_t)nd + 1]);
-    const float uz = (float)__ldg(&b.up[3 * (size_t)nd + 2]);
+    const float ux = __ldg(&b.up32[3 * (size_t)nd]);
+    const float uy = __ldg(&b.up32[3 * (size_t)nd + 1]);
+    const float uz = __ldg(&b.up32[3 * (size_t)nd + 2]);
 #pragma unroll
     for (int k = 0; k < 6; ++k) {
       const float w = B[6 * s + k];
@@ -417,7 +428,7 @@ __device__ __forceinline__ ElemOut element_force32(uint32_t i, int np_rt, const 
     const float be2 = -2.f * (dotf(D3, dn) + dotf(d3, a3));
     const float H00 = FC(F32_H00), H01 = FC(F32_H01), H02 = FC(F32_H02), H11 = FC(F32_H11), H12 = FC(F32_H12),
                 H22 = FC(F32_H22);
-    const float K = (float)sc.K, Dm = (float)sc.D;
+    const float K = FC(F32_K), Dm = FC(F32_D);
     const float n0 = K * (H00 * al0 + H01 * al1 + H02 * al2);
     const float n1 = K * (H01 * al0 + H11 * al1 + H12 * al2);
     const float n2 = K * (H02 * al0 + H12 * al1 + H22 * al2);
@@ -486,19 +497,20 @@ __device__ __forceinline__ ElemOut element_force32(uint32_t i, int np_rt, const 
       }
     }
     ElemOut o;
-    o.etens = 0.5 * (double)JxW * ((double)n0 * al0 + (double)n1 * al1 + (double)n2 * al2);
-    o.ebend = 0.5 * (double)JxW * ((double)m0 * be0 + (double)m1 * be1 + (double)m2 * be2);
-    o.area = sc.qw * (double)jac;
+    const float area = 0.5f * jac;
     const float g0 = FC(F32_G0) + 2.f * al0, g1 = FC(F32_G1) + 2.f * al1, g2 = FC(F32_G2) + al2;
-    const double invdet = 1.0 / ((double)g0 * g1 - (double)g2 * g2);
-    o.kg = o.area * invdet * ((double)h0 * h1 - (double)h2 * h2);
-    o.km = o.area * invdet * 0.5 * ((double)h0 * g1 + (double)h1 * g0 - 2.0 * (double)h2 * g2);
+    const float w_invdet = area / (g0 * g1 - g2 * g2);
+    o.etens = 0.5f * JxW * (n0 * al0 + n1 * al1 + n2 * al2);
+    o.ebend = 0.5f * JxW * (m0 * be0 + m1 * be1 + m2 * be2);
+    o.area = area;
+    o.kg = w_invdet * (h0 * h1 - h2 * h2);
+    o.km = w_invdet * 0.5f * (h0 * g1 + h1 * g0 - 2.f * h2 * g2);
     return o;
   }
 #undef FC
 }
 
-__global__ void __launch_bounds__(kBlock) k_elements32(DevBuf b, StepConst sc, ElemGroups eg) {
+__global__ void __launch_bounds__(kBlock, 2) k_elements32(DevBuf b, StepConst sc, ElemGroups eg) {
   Ctl* ctl = b.ctl;
   if (inactive(ctl)) return;
   __shared__ double sh[kBlock / 32];
@@ -510,21 +522,24 @@ __global__ void __launch_bounds__(kBlock) k_elements32(DevBuf b, StepConst sc, E
   __syncthreads();
   const uint32_t li = (blockIdx.x - gd.block_start) * blockDim.x + threadIdx.x;
   ElemOut o{0, 0, 0, 0, 0};
-  const float pressure = (float)ctl->pressure, vol_p = (float)ctl->volume_pressure;
+  const double pressure = ctl->pressure;
+  const float vol_p = (float)ctl->volume_pressure;
   if (li < gd.count) {
     const uint32_t i = gd.first + li;
+    const float pr = (float)(pressure * __ldg(&b.pscale[i]));
     if (gd.n_slots == 12)
-      o = element_force32<12>(i, 12, sB, b, sc, pressure, vol_p);
+      o = element_force32<12>(i, 12, sB, b, sc, pr, vol_p);
     else if (gd.n_slots == 11)
-      o = element_force32<11>(i, 11, sB, b, sc, pressure, vol_p);
+      o = element_force32<11>(i, 11, sB, b, sc, pr, vol_p);
     else
-      o = element_force32<0>(i, gd.n_slots, sB, b, sc, pressure, vol_p);
+      o = element_force32<0>(i, gd.n_slots, sB, b, sc, pr, vol_p);
     const uint32_t e = __ldg(&b.perm[i]);
+    const float ia = 1.f / (float)o.area;
     b.area[e] = o.area;
-    b.kG[e] = o.kg / o.area;
-    b.kM[e] = o.km / o.area;
-    b.etens[e] = o.etens / o.area;
-    b.ebend[e] = o.ebend / o.area;
+    b.kG[e] = (float)o.kg * ia;
+    b.kM[e] = (float)o.km * ia;
+    b.etens[e] = (float)o.etens * ia;
+    b.ebend[e] = (float)o.ebend * ia;
   }
   const double s0 = block_sum(o.etens, sh);
   const double s1 = block_sum(o.ebend, sh);
@@ -564,12 +579,13 @@ __global__ void __launch_bounds__(kBlock) k_elements(DevBuf b, StepConst sc, Ele
   if (li < gd.count) {
     const uint32_t i = gd.first + li;
     const double* B = sB;
+    const double pr = pressure * __ldg(&b.pscale[i]);
     if (gd.n_slots == 12)
-      o = element_force<12>(i, 12, B, b, sc, pressure, vol_p);
+      o = element_force<12>(i, 12, B, b, sc, pr, vol_p);
     else if (gd.n_slots == 11)
-      o = element_force<11>(i, 11, B, b, sc, pressure, vol_p);
+      o = element_force<11>(i, 11, B, b, sc, pr, vol_p);
     else
-      o = element_force<0>(i, gd.n_slots, B, b, sc, pressure, vol_p);
+      o = element_force<0>(i, gd.n_slots, B, b, sc, pr, vol_p);
     const uint32_t e = __ldg(&b.perm[i]);
     b.area[e] = o.area;
     b.kG[e] = o.kg / o.area;
@@ -605,6 +621,14 @@ __global__ void __launch_bounds__(kBlock) k_contact_force(DevBuf b, StepConst sc
   if (inactive(ctl)) return;
   __shared__ double sh[kBlock / 32];
   const uint32_t n_pairs = ctl->n_pairs;
+  if (n_pairs == 0) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      ctl->Eself = 0.0;
+      ctl->Efric = 0.0;
+      ctl->Nc = 0;
+    }
+    return;
+  }
   double eself = 0.0, efric = 0.0, nc = 0.0;
   const double h = sc.thickness;
   for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n_pairs; j += gridDim.x * blockDim.x) {
@@ -729,13 +753,19 @@ __global__ void __launch_bounds__(kBlock) k_gather_correct(DevBuf b, StepConst s
     }
     const uint32_t g0 = b.gather_ptr[n], g1 = b.gather_ptr[n + 1];
     if (sc.fp32) {
+      float s0 = 0.f, s1 = 0.f, s2 = 0.f;
+#pragma unroll 4
       for (uint32_t k = g0; k < g1; ++k) {
         const float* q = b.qe32 + 3 * (size_t)__ldg(&b.gather_ent[k]);
-        f[0] -= (double)q[0];
-        f[1] -= (double)q[1];
-        f[2] -= (double)q[2];
+        s0 += q[0];
+        s1 += q[1];
+        s2 += q[2];
       }
+      f[0] -= (double)s0;
+      f[1] -= (double)s1;
+      f[2] -= (double)s2;
     } else {
+#pragma unroll 4
       for (uint32_t k = g0; k < g1; ++k) {
         const double* q = b.qe + 3 * (size_t)__ldg(&b.gather_ent[k]);
         f[0] -= q[0];
@@ -753,14 +783,20 @@ __global__ void __launch_bounds__(kBlock) k_gather_correct(DevBuf b, StepConst s
         if (f_out) f_out[k] = f[c];
         if (a_out) a_out[k] = ap;
       } else {
-        const double up = __dadd_rn(__dmul_rn(sc.nm0, ap), b.up[k]);
-        const double vn = __dadd_rn(__dmul_rn(sc.nm7, ap), vp);
+        double up, vn;
+        if (sc.contact) {
+          up = __dadd_rn(__dmul_rn(sc.nm0, ap), b.up[k]);
+          vn = __dadd_rn(__dmul_rn(sc.nm7, ap), vp);
+        } else {
+          up = fma(sc.nm0, ap, b.up[k]);
+          vn = fma(sc.nm7, ap, vp);
+        }
         d[c] = __dsub_rn(up, b.u[k]);
         b.u[k] = up;
         b.v[k] = vn;
         b.a[k] = ap;
         b.p[k] = __dadd_rn(b.X[k], up);
-        ekin += vn * vn / b.Minv[k];
+        ekin += vn * vn * b.M[k];
       }
     }
     if (mode == 1) du2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
@@ -938,12 +974,13 @@ __global__ void __launch_bounds__(kBlock) k_elements_noalloc(DevBuf b, StepConst
   const uint32_t li = (blockIdx.x - gd.block_start) * blockDim.x + threadIdx.x;
   if (li >= gd.count) return;
   const uint32_t i = gd.first + li;
+  const double pr = pressure * __ldg(&b.pscale[i]);
   if (gd.n_slots == 12)
-    element_force<12>(i, 12, sB, b, sc, pressure, 0.0);
+    element_force<12>(i, 12, sB, b, sc, pr, 0.0);
   else if (gd.n_slots == 11)
-    element_force<11>(i, 11, sB, b, sc, pressure, 0.0);
+    element_force<11>(i, 11, sB, b, sc, pr, 0.0);
   else
-    element_force<0>(i, gd.n_slots, sB, b, sc, pressure, 0.0);
+    element_force<0>(i, gd.n_slots, sB, b, sc, pr, 0.0);
 }
 
 // f = -(sum of the node's shares), the same gather order as the step kernel

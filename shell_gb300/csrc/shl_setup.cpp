@@ -393,6 +393,8 @@ bool build_setup(const shl_mesh& mesh, const shl_params& prm, Setup& S, std::str
         out[FF_H11] = s2 * (E2 * g0 * g0);
         out[FF_H12] = s2 * (E2 * -g0 * g2);
         out[FF_H22] = s2 * (G12 * ((1 - nu * nu2) * g1 * g0 + (1 - nu * nu2) * ((1 + nu) / (1 - nu)) * g2 * g2));
+        out[FF_K] = S.K;
+        out[FF_D] = S.D;
       };
       double cref[FF_COUNT], cbal[FF_COUNT];
       frame_constants(k, j, cref);
@@ -439,7 +441,8 @@ bool build_setup(const shl_mesh& mesh, const shl_params& prm, Setup& S, std::str
                             {F32_D12, FF_D12}, {F32_D20, FF_D20}, {F32_D21, FF_D21}, {F32_D22, FF_D22},
                             {F32_D30, FF_D30}, {F32_D31, FF_D31}, {F32_D32, FF_D32}, {F32_G0, FF_G0},
                             {F32_G1, FF_G1}, {F32_G2, FF_G2}, {F32_H00, FF_H00}, {F32_H01, FF_H01},
-                            {F32_H02, FF_H02}, {F32_H11, FF_H11}, {F32_H12, FF_H12}, {F32_H22, FF_H22}};
+                            {F32_H02, FF_H02}, {F32_H11, FF_H11}, {F32_H12, FF_H12}, {F32_H22, FF_H22},
+                            {F32_K, FF_K}, {F32_D, FF_D}};
     for (const auto& m : map64) put32(m[0], get(m[1]));
     const V3 a1{get(FF_A10), get(FF_A11), get(FF_A12)}, a2{get(FF_A20), get(FF_A21), get(FF_A22)};
     const V3 n = cross(a1, a2);
@@ -528,6 +531,107 @@ bool build_setup(const shl_mesh& mesh, const shl_params& prm, Setup& S, std::str
     const uint64_t nc = (uint64_t)std::ceil(std::sqrt((double)F) / prm.cell_size_mult);
     S.n_cells_max = nc * nc * nc;
   }
+  return true;
+}
+
+bool merge_setups(std::vector<Setup>& shells, Setup& M, std::vector<uint32_t>& node_off,
+                  std::vector<uint32_t>& face_off, std::vector<uint32_t>& face_shell, std::string& err) {
+  const size_t n = shells.size();
+  if (n == 0) { err = "no shells"; return false; }
+  node_off.assign(n + 1, 0);
+  face_off.assign(n + 1, 0);
+  for (size_t k = 0; k < n; ++k) {
+    node_off[k + 1] = node_off[k] + shells[k].V;
+    face_off[k + 1] = face_off[k] + shells[k].F;
+  }
+  const uint32_t V = node_off[n], F = face_off[n];
+  M = Setup();
+  M.V = V;
+  M.F = F;
+  face_shell.assign(F, 0);
+  // the distinct patch types, regular first
+  std::vector<int> vals;
+  for (const Setup& S : shells)
+    for (const PatchGroup& g : S.groups)
+      if (g.count && std::find(vals.begin(), vals.end(), g.valence) == vals.end()) vals.push_back(g.valence);
+  std::sort(vals.begin(), vals.end());
+  std::stable_sort(vals.begin(), vals.end(), [](int x, int y) { return (x == 6) > (y == 6); });
+  if (vals.empty() || vals[0] != 6) vals.insert(vals.begin(), 6);
+  M.X.reserve(3 * (size_t)V);
+  M.tri.reserve(3 * (size_t)F);
+  M.Minv.reserve(3 * (size_t)V);
+  M.C.reserve(3 * (size_t)V);
+  for (size_t k = 0; k < n; ++k) {
+    const Setup& S = shells[k];
+    M.X.insert(M.X.end(), S.X.begin(), S.X.end());
+    for (uint32_t x : S.tri) M.tri.push_back(x + node_off[k]);
+    M.Minv.insert(M.Minv.end(), S.Minv.begin(), S.Minv.end());
+    M.C.insert(M.C.end(), S.C.begin(), S.C.end());
+    for (uint32_t f = 0; f < S.F; ++f) face_shell[face_off[k] + f] = (uint32_t)k;
+  }
+  // regroup: for each patch type, the faces of every shell in shell order
+  M.perm.clear();
+  std::vector<std::pair<uint32_t, uint32_t>> src;  // (shell, internal face of the shell)
+  for (int val : vals) {
+    PatchGroup g;
+    g.valence = val;
+    g.n_slots = val + 6;
+    g.first = (uint32_t)M.perm.size();
+    for (size_t k = 0; k < n; ++k) {
+      const Setup& S = shells[k];
+      for (const PatchGroup& sg : S.groups) {
+        if (sg.valence != val) continue;
+        if (g.basis.empty()) g.basis = sg.basis;
+        for (uint32_t i = sg.first; i < sg.first + sg.count; ++i) {
+          M.perm.push_back(face_off[k] + S.perm[i]);
+          src.emplace_back((uint32_t)k, i);
+        }
+      }
+    }
+    g.count = (uint32_t)M.perm.size() - g.first;
+    if (g.basis.empty()) {
+      g.basis.assign(6 * g.n_slots, 0.0);
+      if (val == 6) regular_basis(1.0 / 3.0, 1.0 / 3.0, g.basis.data());
+      else irregular_basis(val, 1.0 / 3.0, 1.0 / 3.0, g.basis.data());
+    }
+    M.groups.push_back(std::move(g));
+  }
+  if (M.perm.size() != F) { err = "face regrouping lost faces"; return false; }
+  M.inv_perm.assign(F, 0);
+  for (uint32_t i = 0; i < F; ++i) M.inv_perm[M.perm[i]] = i;
+  M.patch.assign(12 * (size_t)F, -1);
+  M.face.assign((size_t)FF_COUNT * F, 0.0);
+  M.face32.assign((size_t)F32_COUNT * F, 0.0f);
+  for (uint32_t i = 0; i < F; ++i) {
+    const uint32_t k = src[i].first, si = src[i].second;
+    const Setup& S = shells[k];
+    for (int s = 0; s < 12; ++s) {
+      const int32_t nd = S.patch[(size_t)s * S.F + si];
+      M.patch[(size_t)s * F + i] = nd < 0 ? -1 : nd + (int32_t)node_off[k];
+    }
+    for (int fld = 0; fld < FF_COUNT; ++fld) M.face[(size_t)fld * F + i] = S.face[(size_t)fld * S.F + si];
+    for (int fld = 0; fld < F32_COUNT; ++fld) M.face32[(size_t)fld * F + i] = S.face32[(size_t)fld * S.F + si];
+  }
+  // gather CSR over the merged numbering
+  M.gather_ptr.assign(V + 1, 0);
+  for (uint32_t i = 0; i < F; ++i)
+    for (int s = 0; s < 12; ++s) {
+      const int32_t nd = M.patch[(size_t)s * F + i];
+      if (nd >= 0) ++M.gather_ptr[nd + 1];
+    }
+  for (uint32_t v = 0; v < V; ++v) M.gather_ptr[v + 1] += M.gather_ptr[v];
+  M.gather_ent.assign(M.gather_ptr[V], 0);
+  {
+    std::vector<uint32_t> cur(M.gather_ptr.begin(), M.gather_ptr.end() - 1);
+    for (uint32_t i = 0; i < F; ++i)
+      for (int s = 0; s < 12; ++s) {
+        const int32_t nd = M.patch[(size_t)s * F + i];
+        if (nd >= 0) M.gather_ent[cur[nd]++] = i * 12 + s;
+      }
+  }
+  M.close_ptr.assign(F + 1, 0);
+  M.K = shells[0].K;
+  M.D = shells[0].D;
   return true;
 }
 

@@ -36,6 +36,7 @@ enum FaceField {
   FF_G0, FF_G1, FF_G2,             // a_ref.ff1 (Voigt, no factor 2)
   FF_B0, FF_B1, FF_B2,             // a_ref.ff2
   FF_H00, FF_H01, FF_H02, FF_H11, FF_H12, FF_H22,  // orthotropic H incl. 1/det^2
+  FF_K, FF_D,                      // membrane and bending stiffness of the face's shell
   FF_COUNT
 };
 
@@ -50,6 +51,7 @@ enum FaceField32 {
   F32_G0, F32_G1, F32_G2,          // a_ref.ff1
   F32_N0, F32_N1, F32_N2, F32_L0,  // unit normal and |a1 x a2| of the reference
   F32_H00, F32_H01, F32_H02, F32_H11, F32_H12, F32_H22,
+  F32_K, F32_D,
   F32_COUNT
 };
 
@@ -83,6 +85,13 @@ struct Setup {
 
 // Builds everything; returns false with a message on unsupported input.
 bool build_setup(const shl_mesh& mesh, const shl_params& p, Setup& out, std::string& err);
+
+// Concatenates the set-ups of independent shells into one (node and face
+// ids offset shell by shell, faces regrouped so that each patch group spans
+// all shells).  node_off/face_off (n+1 entries) get the original-order
+// offsets of each shell; face_shell gets the shell of every original face.
+bool merge_setups(std::vector<Setup>& shells, Setup& out, std::vector<uint32_t>& node_off,
+                  std::vector<uint32_t>& face_off, std::vector<uint32_t>& face_shell, std::string& err);
 
 // Loop box-spline basis of a regular patch at (v, w) in this library's patch
 // order; out[6*slot + k].  Exposed for tests through the C ABI helpers.

@@ -107,6 +107,9 @@ def load():
         "shl_time_kernel": (_i32, [vp, ctypes.c_int, ctypes.c_int, sz, ctypes.POINTER(_d)]),
         "shl_measure_fp64_peak": (_i32, [ctypes.POINTER(_d)]),
         "shl_internal_force_noalloc": (_i32, [vp, vp, _d, vp, vp]),
+        "shl_profile_step": (_i32, [vp, _d, sz, vp]),
+        "shl_batch_create": (_i32, [vp, vp, vp, _u32, ctypes.POINTER(vp)]),
+        "shl_batch_layout": (_i32, [vp, ctypes.POINTER(_u32), vp, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -124,7 +127,8 @@ def exported_symbols():
             "shl_set_contact_state", "shl_rebuild_contacts", "shl_get_element_fields", "shl_get_mass_damping",
             "shl_icosphere", "shl_icosphere_off", "shl_read_off", "shl_gaussian_normal_imperfection",
             "shl_params_default", "shl_get_stream", "shl_upload_pressure_table", "shl_step_enqueue",
-            "shl_step_collect", "shl_time_kernel", "shl_measure_fp64_peak", "shl_internal_force_noalloc"]
+            "shl_step_collect", "shl_time_kernel", "shl_measure_fp64_peak", "shl_internal_force_noalloc",
+            "shl_profile_step", "shl_batch_create", "shl_batch_layout"]
 
 
 class ShlError(RuntimeError):
@@ -302,6 +306,13 @@ class Shell:
         st = _check(self.lib.shl_step_collect(self.h, ctypes.byref(r)), "shl_step_collect")
         return r, st
 
+    PHASES = ("predict", "cells1", "elements", "contact", "gather_correct", "cells2", "volume_end")
+
+    def profile_step(self, pressure, flush_bytes=0):
+        out = np.zeros(7)
+        _check(self.lib.shl_profile_step(self.h, pressure, flush_bytes, out.ctypes.data), "shl_profile_step", False)
+        return dict(zip(self.PHASES, out))
+
     def time_kernel(self, which, reps=20, flush_bytes=0):
         ms = _d()
         _check(self.lib.shl_time_kernel(self.h, which, reps, flush_bytes, ctypes.byref(ms)), "shl_time_kernel", False)
@@ -345,3 +356,33 @@ class Shell:
         Minv, C = np.zeros(3 * self.V), np.zeros(3 * self.V)
         _check(self.lib.shl_get_mass_damping(self.h, Minv.ctypes.data, C.ctypes.data), "shl_get_mass_damping", False)
         return Minv, C
+
+
+class Batch(Shell):
+    """Independent shells advanced together (shl_batch_create)."""
+
+    def __init__(self, meshes, params, pressure_scale=None):
+        lib = load()
+        self.lib = lib
+        self.params = params[0]
+        n = len(meshes)
+        keep = [make_mesh(X, T) for X, T in meshes]
+        arr = (ShlMesh * n)(*[m for m, _ in keep])
+        parr = (ShlParams * n)(*params)
+        ps = None if pressure_scale is None else np.ascontiguousarray(pressure_scale, dtype=np.float64)
+        h = ctypes.c_void_p()
+        _check(lib.shl_batch_create(ctypes.cast(arr, ctypes.c_void_p), ctypes.cast(parr, ctypes.c_void_p),
+                                    _ptr(ps), n, ctypes.byref(h)), "shl_batch_create", False)
+        self.h = h
+        self.n_shells = n
+        no = np.zeros(n + 1, dtype=np.uint32)
+        fo = np.zeros(n + 1, dtype=np.uint32)
+        _check(lib.shl_batch_layout(h, None, no.ctypes.data, fo.ctypes.data), "shl_batch_layout", False)
+        self.node_off, self.face_off = no.astype(np.int64), fo.astype(np.int64)
+        self.V, self.F = int(no[-1]), int(fo[-1])
+        self.X = np.concatenate([np.asarray(X, float).reshape(-1, 3) for X, _ in meshes])
+        self.T = np.concatenate([np.asarray(T, np.int64) + no[k] for k, (_, T) in enumerate(meshes)])
+
+    def split(self, vec):
+        """Per-shell views of a concatenated node-major vector."""
+        return [vec[3 * self.node_off[k]:3 * self.node_off[k + 1]] for k in range(self.n_shells)]
