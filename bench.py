@@ -130,6 +130,57 @@ def time_ensemble(L, torch, K, W, flush):
             "steps": K, "status": int(status)}
 
 
+def fp32_accuracy(L, steps=1000, level=7):
+    """Level-7 shell, h/R = 0.005, E1/E2 = 4, pressure ramp to 3 p_cl over
+    50,000 steps, self-contact on: FP32 element forces against FP64 (the FP64
+    path equals the CPU oracle to 1e-12) -- per-vertex force error at the
+    initial state and after `steps` steps, and the displacement drift."""
+    import oracle as O
+
+    h, e1, e2, s_end, ramp_steps = 0.005, 2.0, 0.5, 3.0, 50000
+    X, T = L.icosphere(level)
+    P = X[T]
+    cell_mult = 2 * h / (P.max(axis=1) - P.min(axis=1)).max(axis=1).mean()
+    E = np.sqrt(e1 * e2)
+    nu = np.sqrt(NU12 * NU12 * e2 / e1)
+    p_cl = 2 * E * h * h / np.sqrt(3 * (1 - nu * nu))
+    common = dict(shell_mass_density=RHO, shell_young_modulus=e1, shell_young_modulus2=e2, shell_poisson_ratio=NU12,
+                  shell_shear_modulus=G12 * E, thickness=h, damping_alpha=ALPHA, dt=DT,
+                  shell_shell_contact=L.CONTACT_LINEAR, mu_s=MU, mu_d=MU, cell_size_mult=cell_mult)
+    u0 = L.gaussian_normal_imperfection(X, AMPL, SEED).reshape(-1)
+    table = -s_end * p_cl * np.arange(1, steps + 1) / ramp_steps
+    out = {}
+    runs = {}
+    for name, prec in (("fp64", L.PREC_FP64), ("fp32", L.PREC_FP32)):
+        g = L.Shell(X, T, L.default_params(precision=prec, **common))
+        g.apply_initial_conditions(u0, 0.0, table[0])
+        f0 = g.eval_forces(u0, np.zeros_like(u0), table[0])[0]
+        r, st = g.step(steps, table)
+        u, v, a = g.get_state()
+        f1 = g.eval_forces(u, v, table[-1])[0]
+        runs[name] = (f0, u, f1, st, r.steps_done)
+        g.close()
+    o = O.Oracle(X, T, L.default_params(**common), threads=os.cpu_count())
+    f0_oracle = o.eval_forces(u0, np.zeros_like(u0), table[0])[0]
+    o.close()
+
+    def node_err(f, ref):
+        d = np.linalg.norm((f - ref).reshape(-1, 3), axis=1)
+        scale = np.linalg.norm(ref.reshape(-1, 3), axis=1).max()
+        return {"max_node_rel": float(d.max() / scale), "l2_rel": float(np.linalg.norm(f - ref) / np.linalg.norm(ref))}
+
+    f0_64, u_64, f1_64, st64, n64 = runs["fp64"]
+    f0_32, u_32, f1_32, st32, n32 = runs["fp32"]
+    out["workload"] = "level-%d shell (%d faces), h/R %.3f, E1/E2 4, ramp to 3 p_cl over %d steps, %d steps" % (
+        level, len(T), h, ramp_steps, steps)
+    out["force_error_initial_vs_oracle"] = node_err(f0_32, f0_oracle)
+    out["fp64_vs_oracle_initial"] = node_err(f0_64, f0_oracle)
+    out["force_error_after"] = node_err(f1_32, f1_64)
+    out["displacement_drift"] = float(np.linalg.norm(u_32 - u_64) / np.linalg.norm(u_64 - u0))
+    out["steps_done"] = [int(n64), int(n32)]
+    return out
+
+
 def cpu_sample(X, T, p, u0, seconds=10.0, threads=None):
     """CPU oracle on the same workload: steps until about `seconds` elapsed."""
     import oracle as O
@@ -297,6 +348,7 @@ def run_ours(args, rank, world, dist):
         fp32_value = F * K / (ms32 * 1e-3)
 
     ensemble = time_ensemble(L, torch, max(20, K // 4), W, flush) if args.ensemble else None
+    accuracy = fp32_accuracy(L) if args.accuracy else None
 
     # warm continuous throughput (informative): K steps back to back, one graph replay per 16 steps
     g.upload_pressure_table(pressure(np.arange(1 + W + K, 1 + W + 2 * K)))
@@ -355,6 +407,7 @@ def run_ours(args, rank, world, dist):
         "warm_value": warm,
         "fp32_value": fp32_value,
         "ensemble": ensemble,
+        "fp32_accuracy": accuracy,
         "e2e": {"value": e2e, "unit": "face-steps/s", "h2d_bytes_per_step": 3 * 3 * V * 8,
                 "d2h_bytes_per_step": 3 * 3 * V * 8,
                 "how": "per step: shl_set_state from pinned host, shl_step(1), shl_get_state"},
@@ -383,6 +436,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--fp32", type=int, default=1, help="also time the FP32 element-force mode")
     ap.add_argument("--ensemble", type=int, default=1, help="also time the 256-shell batched ensemble")
+    ap.add_argument("--accuracy", type=int, default=1, help="also report the level-7 FP32-vs-FP64 accuracy")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     world = int(os.environ.get("WORLD_SIZE", "1"))

@@ -253,6 +253,47 @@ shl_status shl_get_element_fields(shl_ctx* ctx, double* kGauss, double* kMean, d
 /* Lumped inverse masses and damping coefficients (ShellSystem.C:762-852). */
 shl_status shl_get_mass_damping(shl_ctx* ctx, double* Minv, double* C);
 
+/* Node and face counts, and the mesh the context was made from (file order,
+ * reference positions). */
+shl_status shl_context_size(shl_ctx* ctx, uint32_t* n_nodes, uint32_t* n_faces);
+shl_status shl_context_mesh(shl_ctx* ctx, double* xyz /* 3V */, uint32_t* faces /* 3F */);
+
+/* Per-node measurement vectors of the last step (node_vectors of
+ * ShellSystem.C:126-130): kinetic energy density (Ekin_node / mean area of the
+ * incident faces, 2796-2812), cavity-contact energy density (always 0: cavity
+ * contact is not modelled), self-contact and friction energy densities
+ * (1862-1877) and nodal mass.  V values each; any pointer may be NULL. */
+shl_status shl_get_node_fields(shl_ctx* ctx, double* ekin, double* ecav, double* eself, double* efric,
+                               double* mass);
+
+/* ShellSystem::apply_initial_conditions with a load file (ShellSystem.C:855-888)
+ * after shl_set_state / shl_set_time / shl_set_contact_state: positions,
+ * bounding boxes, a forced candidate-list build that keeps the loaded pairs,
+ * deformed metrics, and volume0 = the loaded state's volume.  v and a are kept. */
+shl_status shl_apply_loaded_state(shl_ctx* ctx);
+
+/* ---- files (host code over the calls above) ---------------------------- */
+
+/* State file of shell.C:383-390 + ShellSystem::save (ShellSystem.C:2956-3032),
+ * 17 significant digits: time_step, dt, time, wall_time; per node
+ * "ux vx ax uy vy ay uz vz az sx sy sz" (s = cavity spring origin, 0 here);
+ * the number of measurement rows and the rows (14 columns each, avg_rows
+ * row-major: dt, area, vol, pcav, Nc_cav, Nc, Ekin, Etens, Ebend, Ecav, Eself,
+ * Efric, kGauss, kMean, each weighted with dt); the sticking self-contacts
+ * "eid1 eid2 ox oy oz". */
+shl_status shl_save_state_file(shl_ctx* ctx, const char* path, uint32_t time_step, double dt,
+                               double wall_time, const double* avg_rows, uint32_t n_rows);
+/* Reads such a file into the context (u, v, a, time, time_step, sticking
+ * contacts) and calls shl_apply_loaded_state.  Returns the file's time step,
+ * dt and wall time, and up to cap_rows measurement rows (SHL_ERR_CAPACITY if
+ * the file holds more); avg_rows may be NULL. */
+shl_status shl_load_state_file(shl_ctx* ctx, const char* path, uint32_t* time_step, double* dt,
+                               double* wall_time, double* avg_rows, uint32_t cap_rows, uint32_t* n_rows);
+/* ASCII VTK unstructured grid of ShellSystem::write_vtk (ShellSystem.C:3156-3320):
+ * reference positions, point data ux uy uz ecav efric ekin eself mass, cell
+ * data ebend etens kGauss kMean of the last step. */
+shl_status shl_write_vtu(shl_ctx* ctx, const char* path);
+
 /* ---- host helpers of the driver (no device work) ----------------------- */
 
 /* Closed icosphere: the 20-face icosahedron refined `level` times, each

@@ -55,6 +55,7 @@ def load():
         "oracle_get_mass_damping": (ctypes.c_int, [vp, vp, vp]),
         "oracle_get_element_fields": (ctypes.c_int, [vp, vp, vp, vp, vp, vp]),
         "oracle_get_cell_info": (ctypes.c_int, [vp, vp]),
+        "oracle_get_node_fields": (ctypes.c_int, [vp, vp, vp, vp]),
         "oracle_patch": (ctypes.c_int, [vp, u32, vp, ctypes.POINTER(u32)]),
         "oracle_basis_at": (ctypes.c_int, [vp, u32, d, d, vp]),
         "oracle_basis_cached": (ctypes.c_int, [vp, u32, vp, vp]),
@@ -180,6 +181,11 @@ class Oracle:
         out = [np.zeros(self.F) for _ in range(5)]
         self.lib.oracle_get_element_fields(self.h, *[o.ctypes.data for o in out])
         return dict(zip(("kGauss", "kMean", "etens", "ebend", "area"), out))
+
+    def node_fields(self):
+        out = [np.zeros(self.V) for _ in range(3)]
+        self.lib.oracle_get_node_fields(self.h, *[o.ctypes.data for o in out])
+        return dict(zip(("ekin", "eself", "efric"), out))
 
     def cell_info(self):
         out = np.zeros(9)

@@ -321,6 +321,8 @@ struct oracle {
   // measurement
   unsigned Nc = 0;
   Real Eself = 0, Efric = 0, Etens = 0, Ebend = 0, Ekin = 0, kGauss = 0, kMean = 0;
+  // node_vectors ekin, eself, efric (ShellSystem.C:126-130), reset every step
+  std::vector<Real> ekin_vec, eself_vec, efric_vec;
   int current_problem = 0;
 
   ~oracle() {
@@ -740,6 +742,9 @@ void oracle::reset_properties() {
   for (ElemCache& c : ec) c.kGauss = c.kMean = c.etens = c.ebend = 0;
   Nc = 0;
   Eself = Efric = Etens = Ebend = 0;
+  ekin_vec.assign(V, 0.0);
+  eself_vec.assign(V, 0.0);
+  efric_vec.assign(V, 0.0);
 }
 
 // prepare_next_step, ShellSystem.C:924-949: the only time-dependent parameter
@@ -965,6 +970,12 @@ void oracle::add_shell_shell_contact_force() {
 #pragma omp critical(oracle_assemble_vec)
       for (int e = 0; e < 2; ++e) {
         const Real vv = contact->v[e], ww = contact->w[e], u0 = 1 - vv - ww;
+        // energy densities, ShellSystem.C:1862-1877
+        const Real pre[3] = {0.5 * u0 / area_min, 0.5 * vv / area_min, 0.5 * ww / area_min};
+        for (int k = 0; k < 3; ++k) {
+          eself_vec[tri[3 * contact->eid[e] + k]] += pre[k] * Eself_contact;
+          efric_vec[tri[3 * contact->eid[e] + k]] += pre[k] * Efric_contact;
+        }
         const Real prefactor = (e == 0 ? -0.5 : 0.5);
         for (int var = 0; var < 3; ++var) {
           const Real fc = prefactor * f_contact(var);
@@ -1190,6 +1201,15 @@ void oracle::measure_properties() {
   kGauss = kG;
   kMean = kM;
   area = area_sum;
+  // mean area of the faces around each node, avg_area_node (ShellSystem.C:2462-2481)
+  std::vector<Real> node_area(V, 0.0);
+  std::vector<unsigned> node_faces(V, 0);
+  for (unsigned e = 0; e < F; ++e)
+    for (int k = 0; k < 3; ++k) {
+      node_area[tri[3 * e + k]] += ec[e].area;
+      ++node_faces[tri[3 * e + k]];
+    }
+  if (ekin_vec.size() != V) ekin_vec.assign(V, 0.0);
   Real ek = 0;
 #pragma omp parallel for reduction(+ : ek)
   for (int nid = 0; nid < (int)V; ++nid) {
@@ -1199,6 +1219,7 @@ void oracle::measure_properties() {
       e += v[d] * v[d] / Minv[d];
     }
     ek += 0.5 * e;
+    ekin_vec[nid] += 0.5 * e / (node_area[nid] / node_faces[nid]);
   }
   Ekin = ek;
   if (!std::isfinite(Ekin)) register_problem(SHL_NOT_FINITE);
@@ -1449,6 +1470,15 @@ int oracle_get_element_fields(oracle* o, double* kG, double* kM, double* et, dou
     if (et) et[e] = o->ec[e].etens;
     if (eb) eb[e] = o->ec[e].ebend;
     if (ar) ar[e] = o->ec[e].area;
+  }
+  return 0;
+}
+
+int oracle_get_node_fields(oracle* o, double* ekin, double* eself, double* efric) {
+  for (unsigned n = 0; n < o->V; ++n) {
+    if (ekin) ekin[n] = n < o->ekin_vec.size() ? o->ekin_vec[n] : 0.0;
+    if (eself) eself[n] = n < o->eself_vec.size() ? o->eself_vec[n] : 0.0;
+    if (efric) efric[n] = n < o->efric_vec.size() ? o->efric_vec[n] : 0.0;
   }
   return 0;
 }

@@ -17,7 +17,7 @@ OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libshl_gb300.so")
 
 CU_SOURCES = ["shl_kernels.cu", "shl_contact.cu", "shl_api.cu"]
-CPP_SOURCES = ["shl_setup.cpp", "shl_host.cpp"]
+CPP_SOURCES = ["shl_setup.cpp", "shl_host.cpp", "shl_io.cpp"]
 HEADERS = ["shl_geom.h", "shl_setup.h", "shl_internal.cuh", os.path.join("..", "..", "include", "shl.h")]
 
 NVCC = os.environ.get("NVCC", "nvcc")

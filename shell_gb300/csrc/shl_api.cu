@@ -37,6 +37,10 @@ constexpr uint32_t kTableCap = 1u << 16;
 
 }  // namespace
 
+namespace shl {
+void set_error(const std::string& msg) { g_err = msg; }
+}  // namespace shl
+
 struct shl_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
@@ -378,7 +382,7 @@ shl_status create_common(shl_ctx* c, const std::vector<double>& pscale_orig, shl
     ALLOC(b.new_off, F + 1); ALLOC(b.new_cnt, F); ALLOC(b.new_fill, F);
     ALLOC(b.cand_e1, cand_cap); ALLOC(b.cand_e2, cand_cap); ALLOC(b.cand_d2, cand_cap); ALLOC(b.cand_ok, cand_cap);
     ALLOC(b.seg_count, F);
-    ALLOC(b.pforce, 7 * (size_t)pairs_cap);
+    ALLOC(b.pforce, kPairOut * (size_t)pairs_cap);
     ALLOC(b.csr_count, V); ALLOC(b.csr_ptr, V + 1); ALLOC(b.csr_ent, csr_cap); ALLOC(b.csr_fill, V);
   }
 #undef ALLOC
@@ -651,6 +655,32 @@ shl_status shl_eval_forces(shl_ctx* c, const double* u_pred, const double* v_pre
   return s;
 }
 
+namespace {
+
+// the part of ShellSystem::apply_initial_conditions (ShellSystem.C:872-888)
+// shared by a new start and a loaded state: positions, bounding boxes, the
+// forced candidate-list build, deformed metrics and volume0 = volume
+shl_status initial_state(shl_ctx* c, Ctl& h) {
+  launch_positions(c->b, c->sc, c->stream);
+  SHL_TRY(ctl_get(c, h));
+  h.problem = 0;
+  h.halted = 0;
+  h.error = 0;
+  h.pressure = 0;
+  h.volume_pressure = 0;
+  h.rebuild = c->sc.contact ? 1u : 0u;  // compute_shell_shell_contact_candidates(true)
+  SHL_TRY(ctl_put(c, h));
+  if (c->sc.contact) launch_rebuild(c->b, c->sc, c->stream);
+  launch_elements(c->b, c->sc, c->eg, c->elem_blocks, c->stream);
+  launch_volume_end_step(c->b, c->sc, false, c->stream);
+  SHL_TRY(check_launch("initial conditions"));
+  SHL_TRY(ctl_get(c, h));
+  h.volume0 = h.volume;
+  return ctl_put(c, h);
+}
+
+}  // namespace
+
 shl_status shl_apply_initial_conditions(shl_ctx* c, const double* u0, double t0, double pressure_next) {
   if (!c || !u0) return SHL_ERR_ARG;
   const size_t nd = 3 * (size_t)c->S.V;
@@ -659,25 +689,12 @@ shl_status shl_apply_initial_conditions(shl_ctx* c, const double* u0, double t0,
   SHL_CUDA_TRY(cudaMemsetAsync(c->b.v, 0, nd * sizeof(double), c->stream));
   SHL_CUDA_TRY(cudaMemsetAsync(c->b.vp, 0, nd * sizeof(double), c->stream));
   SHL_CUDA_TRY(cudaMemsetAsync(c->b.a, 0, nd * sizeof(double), c->stream));
-  launch_positions(c->b, c->sc, c->stream);
   Ctl h;
   SHL_TRY(ctl_get(c, h));
   const uint32_t step0 = h.time_step;
   h.time = t0;
-  h.problem = 0;
-  h.halted = 0;
-  h.error = 0;
-  h.pressure = 0;
-  h.volume_pressure = 0;
-  h.rebuild = c->sc.contact ? 1u : 0u;  // compute_shell_shell_contact_candidates(true)
   SHL_TRY(ctl_put(c, h));
-  // bounding boxes + first candidate list, then deformed metrics and volume
-  if (c->sc.contact) launch_rebuild(c->b, c->sc, c->stream);
-  launch_elements(c->b, c->sc, c->eg, c->elem_blocks, c->stream);
-  launch_volume_end_step(c->b, c->sc, false, c->stream);
-  SHL_TRY(check_launch("initial conditions"));
-  SHL_TRY(ctl_get(c, h));
-  h.volume0 = h.volume;
+  SHL_TRY(initial_state(c, h));
   // one force evaluation at t0 + dt (ShellSystem.C:892-904)
   h.time = t0 + c->P.dt;
   h.time_step = step0 + 1;
@@ -690,6 +707,12 @@ shl_status shl_apply_initial_conditions(shl_ctx* c, const double* u0, double t0,
   h2.time_step = step0;
   SHL_TRY(ctl_put(c, h2));
   return s;
+}
+
+shl_status shl_apply_loaded_state(shl_ctx* c) {
+  if (!c) return SHL_ERR_ARG;
+  Ctl h;
+  return initial_state(c, h);
 }
 
 namespace {
@@ -1030,6 +1053,85 @@ shl_status shl_get_element_fields(shl_ctx* c, double* kG, double* kM, double* et
   if (eb) SHL_CUDA_TRY(cudaMemcpyAsync(eb, c->b.ebend, bytes, cudaMemcpyDeviceToHost, c->stream));
   if (area) SHL_CUDA_TRY(cudaMemcpyAsync(area, c->b.area, bytes, cudaMemcpyDeviceToHost, c->stream));
   SHL_CUDA_TRY(cudaStreamSynchronize(c->stream));
+  return SHL_OK;
+}
+
+shl_status shl_context_size(shl_ctx* c, uint32_t* n_nodes, uint32_t* n_faces) {
+  if (!c) return SHL_ERR_ARG;
+  if (n_nodes) *n_nodes = c->S.V;
+  if (n_faces) *n_faces = c->S.F;
+  return SHL_OK;
+}
+
+shl_status shl_context_mesh(shl_ctx* c, double* xyz, uint32_t* faces) {
+  if (!c) return SHL_ERR_ARG;
+  if (xyz) std::memcpy(xyz, c->S.X.data(), c->S.X.size() * sizeof(double));
+  if (faces) std::memcpy(faces, c->S.tri.data(), c->S.tri.size() * sizeof(uint32_t));
+  return SHL_OK;
+}
+
+shl_status shl_get_node_fields(shl_ctx* c, double* ekin, double* ecav, double* eself, double* efric,
+                               double* mass) {
+  if (!c) return SHL_ERR_ARG;
+  const uint32_t V = c->S.V, F = c->S.F;
+  const std::vector<double>& Minv = c->S.Minv;
+  if (ecav) std::fill(ecav, ecav + V, 0.0);  // cavity contact is not modelled
+  if (mass)
+    for (uint32_t n = 0; n < V; ++n) mass[n] = 1.0 / Minv[3 * (size_t)n];
+  if (!ekin && !eself && !efric) return SHL_OK;
+  std::vector<double> area(F), v(3 * (size_t)V);
+  SHL_CUDA_TRY(cudaMemcpyAsync(area.data(), c->b.area, F * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  SHL_CUDA_TRY(cudaMemcpyAsync(v.data(), c->b.v, v.size() * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  Ctl h;
+  SHL_TRY(ctl_get(c, h));
+  const std::vector<uint32_t>& T = c->S.tri;
+  if (ekin) {
+    // Ekin_node / avg_area_node (ShellSystem.C:2796-2812, 2462-2481)
+    std::vector<double> asum(V, 0.0);
+    std::vector<uint32_t> cnt(V, 0);
+    for (uint32_t e = 0; e < F; ++e)
+      for (int k = 0; k < 3; ++k) {
+        asum[T[3 * (size_t)e + k]] += area[e];
+        ++cnt[T[3 * (size_t)e + k]];
+      }
+    for (uint32_t n = 0; n < V; ++n) {
+      double en = 0.0;
+      for (int d = 0; d < 3; ++d) {
+        const size_t k = 3 * (size_t)n + d;
+        en += v[k] * v[k] / Minv[k];
+      }
+      ekin[n] = 0.5 * en / (asum[n] / cnt[n]);
+    }
+  }
+  if (!eself && !efric) return SHL_OK;
+  if (eself) std::fill(eself, eself + V, 0.0);
+  if (efric) std::fill(efric, efric + V, 0.0);
+  const uint32_t np = c->sc.contact ? h.n_pairs : 0u;
+  if (np == 0) return SHL_OK;
+  // per-pair energies spread over the six nodes with weights 0.5 (u, v, w) / area_min
+  // (ShellSystem.C:1862-1877)
+  std::vector<uint32_t> e1(np), e2(np);
+  std::vector<double> pf((size_t)kPairOut * np);
+  SHL_CUDA_TRY(cudaMemcpyAsync(e1.data(), c->b.pe1[0], np * 4, cudaMemcpyDeviceToHost, c->stream));
+  SHL_CUDA_TRY(cudaMemcpyAsync(e2.data(), c->b.pe2[0], np * 4, cudaMemcpyDeviceToHost, c->stream));
+  SHL_CUDA_TRY(cudaMemcpyAsync(pf.data(), c->b.pforce, pf.size() * 8, cudaMemcpyDeviceToHost, c->stream));
+  SHL_CUDA_TRY(cudaStreamSynchronize(c->stream));
+  for (uint32_t j = 0; j < np; ++j) {
+    const double* o = &pf[(size_t)kPairOut * j];
+    const double es = o[7], ef = o[8];
+    if (es == 0.0 && ef == 0.0) continue;
+    const uint32_t ee[2] = {e1[j], e2[j]};
+    const double area_min = std::min(area[ee[0]], area[ee[1]]);
+    for (int s = 0; s < 2; ++s) {
+      const double vv = o[3 + 2 * s], ww = o[4 + 2 * s];
+      const double w[3] = {0.5 * (1.0 - vv - ww) / area_min, 0.5 * vv / area_min, 0.5 * ww / area_min};
+      for (int k = 0; k < 3; ++k) {
+        const uint32_t n = T[3 * (size_t)ee[s] + k];
+        if (eself) eself[n] += w[k] * es;
+        if (efric) efric[n] += w[k] * ef;
+      }
+    }
+  }
   return SHL_OK;
 }
 

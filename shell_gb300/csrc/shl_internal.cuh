@@ -28,6 +28,8 @@ namespace shl {
 constexpr int kBlock = 256;          // threads per block for element / node kernels
 constexpr int kMaxGroups = 8;        // patch groups (regular + irregular valences)
 constexpr int kMaxSlots = 18;        // patch slots of the largest supported valence (12)
+// doubles per contact pair written by the contact-force kernel
+constexpr int kPairOut = 9;
 constexpr int kScanTile = 2048;      // elements per block in the multi-block scan
 
 // Patch-group description for the element kernel (in __constant__ memory).
@@ -153,7 +155,7 @@ struct DevBuf {
   double* cand_d2;
   uint8_t* cand_ok;
   uint32_t* seg_count;         // per-face pair counts (F)
-  double* pforce;              // 7 per pair: f_contact(3), v1, w1, v2, w2
+  double* pforce;              // kPairOut per pair: f_contact(3), v1, w1, v2, w2, Eself, Efric
   uint32_t *csr_count, *csr_ptr, *csr_ent, *csr_fill;  // per-node contact CSR
   Ctl* ctl;
   double* ptable;              // per-step pressure table (capacity)

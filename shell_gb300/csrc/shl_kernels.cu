@@ -647,7 +647,7 @@ __global__ void __launch_bounds__(kBlock) k_contact_force(DevBuf b, StepConst sc
     shl_pair_compute(P1, P2, &g);
     b.pd2[0][j] = g.d2;
     if (g.d2 <= 0.0) register_problem(ctl, SHL_CONTACT_PROBLEM);
-    double* out = b.pforce + 7 * (size_t)j;
+    double* out = b.pforce + kPairOut * (size_t)j;
     if (g.d2 < sc.d2_friction) {
       const double area_min = fmin(b.area[e[0]], b.area[e[1]]);
       const double abs_dc = SHL_SQRT(g.d2);
@@ -698,12 +698,13 @@ __global__ void __launch_bounds__(kBlock) k_contact_force(DevBuf b, StepConst sc
       for (int c = 0; c < 3; ++c) fcon[c] = SHL_ADD(fcon[c], SHL_MUL(f_normal, nrm[c]));
       out[0] = fcon[0]; out[1] = fcon[1]; out[2] = fcon[2];
       out[3] = g.v[0]; out[4] = g.w[0]; out[5] = g.v[1]; out[6] = g.w[1];
+      out[7] = es; out[8] = ef;
     } else {
       b.porig[0][3 * (size_t)j] = 0.0;
       b.porig[0][3 * (size_t)j + 1] = 0.0;
       b.porig[0][3 * (size_t)j + 2] = 0.0;
       b.pstick[0][j] = 0;
-      for (int c = 0; c < 7; ++c) out[c] = 0.0;
+      for (int c = 0; c < kPairOut; ++c) out[c] = 0.0;
     }
   }
   const double s0 = block_sum(eself, sh);
@@ -742,7 +743,7 @@ __global__ void __launch_bounds__(kBlock) k_gather_correct(DevBuf b, StepConst s
         const uint32_t ent = b.csr_ent[k];
         const uint32_t j = ent >> 3, role = ent & 7u;
         const int e = role >= 3 ? 1 : 0, kk = role - 3 * e;
-        const double* pf = b.pforce + 7 * (size_t)j;
+        const double* pf = b.pforce + kPairOut * (size_t)j;
         const double vv = pf[3 + 2 * e], ww = pf[4 + 2 * e];
         const double bary = kk == 0 ? (1.0 - vv - ww) : (kk == 1 ? vv : ww);
         const double pref = e == 0 ? -0.5 : 0.5;

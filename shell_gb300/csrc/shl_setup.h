@@ -100,6 +100,9 @@ void regular_basis(double v, double w, double* out);
 // of the middle sub-triangle; out[6*slot + k] for n + 6 slots.
 void irregular_basis(int n, double v, double w, double* out);
 
+// Sets the message returned by shl_last_error() on this thread.
+void set_error(const std::string& msg);
+
 }  // namespace shl
 
 #endif

@@ -110,6 +110,14 @@ def load():
         "shl_profile_step": (_i32, [vp, _d, sz, vp]),
         "shl_batch_create": (_i32, [vp, vp, vp, _u32, ctypes.POINTER(vp)]),
         "shl_batch_layout": (_i32, [vp, ctypes.POINTER(_u32), vp, vp]),
+        "shl_context_size": (_i32, [vp, ctypes.POINTER(_u32), ctypes.POINTER(_u32)]),
+        "shl_context_mesh": (_i32, [vp, vp, vp]),
+        "shl_get_node_fields": (_i32, [vp, vp, vp, vp, vp, vp]),
+        "shl_apply_loaded_state": (_i32, [vp]),
+        "shl_save_state_file": (_i32, [vp, ctypes.c_char_p, _u32, _d, _d, vp, _u32]),
+        "shl_load_state_file": (_i32, [vp, ctypes.c_char_p, ctypes.POINTER(_u32), ctypes.POINTER(_d),
+                                       ctypes.POINTER(_d), vp, _u32, ctypes.POINTER(_u32)]),
+        "shl_write_vtu": (_i32, [vp, ctypes.c_char_p]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -128,7 +136,9 @@ def exported_symbols():
             "shl_icosphere", "shl_icosphere_off", "shl_read_off", "shl_gaussian_normal_imperfection",
             "shl_params_default", "shl_get_stream", "shl_upload_pressure_table", "shl_step_enqueue",
             "shl_step_collect", "shl_time_kernel", "shl_measure_fp64_peak", "shl_internal_force_noalloc",
-            "shl_profile_step", "shl_batch_create", "shl_batch_layout"]
+            "shl_profile_step", "shl_batch_create", "shl_batch_layout", "shl_context_size", "shl_context_mesh",
+            "shl_get_node_fields", "shl_apply_loaded_state", "shl_save_state_file", "shl_load_state_file",
+            "shl_write_vtu"]
 
 
 class ShlError(RuntimeError):
@@ -356,6 +366,32 @@ class Shell:
         Minv, C = np.zeros(3 * self.V), np.zeros(3 * self.V)
         _check(self.lib.shl_get_mass_damping(self.h, Minv.ctypes.data, C.ctypes.data), "shl_get_mass_damping", False)
         return Minv, C
+
+    def node_fields(self):
+        """Per-node ekin, ecav, eself, efric densities and masses of the last step."""
+        out = [np.zeros(self.V) for _ in range(5)]
+        _check(self.lib.shl_get_node_fields(self.h, *[o.ctypes.data for o in out]), "shl_get_node_fields", False)
+        return dict(zip(("ekin", "ecav", "eself", "efric", "mass"), out))
+
+    def save_state_file(self, path, time_step, dt, wall_time=0.0, avg_rows=None):
+        """Write a state file in the layout of ShellSystem::save (see shl_save_state_file)."""
+        rows = np.zeros((0, 14)) if avg_rows is None else np.ascontiguousarray(avg_rows, dtype=np.float64)
+        _check(self.lib.shl_save_state_file(self.h, os.fsencode(path), time_step, dt, wall_time,
+                                            rows.ctypes.data if rows.size else None, rows.shape[0]),
+               "shl_save_state_file", False)
+
+    def load_state_file(self, path, max_rows=1 << 16):
+        """Load a state file; returns (time_step, dt, wall_time, avg_rows)."""
+        step, dt, wt, n = _u32(), _d(), _d(), _u32()
+        rows = np.zeros((max_rows, 14))
+        _check(self.lib.shl_load_state_file(self.h, os.fsencode(path), ctypes.byref(step), ctypes.byref(dt),
+                                            ctypes.byref(wt), rows.ctypes.data, max_rows, ctypes.byref(n)),
+               "shl_load_state_file", False)
+        return step.value, dt.value, wt.value, rows[:n.value].copy()
+
+    def write_vtu(self, path):
+        """ASCII .vtu of the current state (ShellSystem::write_vtk)."""
+        _check(self.lib.shl_write_vtu(self.h, os.fsencode(path)), "shl_write_vtu", False)
 
 
 class Batch(Shell):
