@@ -253,6 +253,10 @@ shl_status shl_get_element_fields(shl_ctx* ctx, double* kGauss, double* kMean, d
 /* Lumped inverse masses and damping coefficients (ShellSystem.C:762-852). */
 shl_status shl_get_mass_damping(shl_ctx* ctx, double* Minv, double* C);
 
+/* Measurements of the last force evaluation or step (the scalars of
+ * measure_properties, ShellSystem.C:2714-2846). */
+shl_status shl_get_energies(shl_ctx* ctx, shl_energies* e);
+
 /* Node and face counts, and the mesh the context was made from (file order,
  * reference positions). */
 shl_status shl_context_size(shl_ctx* ctx, uint32_t* n_nodes, uint32_t* n_faces);

@@ -15,10 +15,11 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libshl_gb300.so")
+RUN = os.path.join(OUT, "shl_run")  # the command-line driver (csrc/shl_run.cpp)
 
 CU_SOURCES = ["shl_kernels.cu", "shl_contact.cu", "shl_api.cu"]
 CPP_SOURCES = ["shl_setup.cpp", "shl_host.cpp", "shl_io.cpp"]
-HEADERS = ["shl_geom.h", "shl_setup.h", "shl_internal.cuh", os.path.join("..", "..", "include", "shl.h")]
+HEADERS = ["shl_geom.h", "shl_setup.h", "shl_internal.cuh", "shl_expr.h", os.path.join("..", "..", "include", "shl.h")]
 
 NVCC = os.environ.get("NVCC", "nvcc")
 CXX = os.environ.get("CXX", "g++")
@@ -69,6 +70,13 @@ def build(force=False, verbose=False):
         r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)
         if r.returncode != 0:
             raise RuntimeError("link failed:\n" + " ".join(cmd) + "\n" + r.stdout.decode(errors="replace"))
+    run_src = os.path.join(CSRC, "shl_run.cpp")
+    if force or _stale(RUN, [run_src, LIB] + headers):
+        cmd = [CXX] + [f for f in CXX_FLAGS if f != "-fPIC"] + ["-o", RUN, run_src, "-L", OUT, "-lshl_gb300",
+                                                                "-Wl,-rpath,$ORIGIN"]
+        r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)
+        if r.returncode != 0:
+            raise RuntimeError("driver build failed:\n" + " ".join(cmd) + "\n" + r.stdout.decode(errors="replace"))
     return LIB
 
 

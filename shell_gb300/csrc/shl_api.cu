@@ -1056,6 +1056,14 @@ shl_status shl_get_element_fields(shl_ctx* c, double* kG, double* kM, double* et
   return SHL_OK;
 }
 
+shl_status shl_get_energies(shl_ctx* c, shl_energies* e) {
+  if (!c || !e) return SHL_ERR_ARG;
+  Ctl h;
+  SHL_TRY(ctl_get(c, h));
+  fill_energies(h, e);
+  return SHL_OK;
+}
+
 shl_status shl_context_size(shl_ctx* c, uint32_t* n_nodes, uint32_t* n_faces) {
   if (!c) return SHL_ERR_ARG;
   if (n_nodes) *n_nodes = c->S.V;

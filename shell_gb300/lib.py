@@ -118,6 +118,7 @@ def load():
         "shl_load_state_file": (_i32, [vp, ctypes.c_char_p, ctypes.POINTER(_u32), ctypes.POINTER(_d),
                                        ctypes.POINTER(_d), vp, _u32, ctypes.POINTER(_u32)]),
         "shl_write_vtu": (_i32, [vp, ctypes.c_char_p]),
+        "shl_get_energies": (_i32, [vp, ctypes.POINTER(ShlEnergies)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -138,7 +139,7 @@ def exported_symbols():
             "shl_step_collect", "shl_time_kernel", "shl_measure_fp64_peak", "shl_internal_force_noalloc",
             "shl_profile_step", "shl_batch_create", "shl_batch_layout", "shl_context_size", "shl_context_mesh",
             "shl_get_node_fields", "shl_apply_loaded_state", "shl_save_state_file", "shl_load_state_file",
-            "shl_write_vtu"]
+            "shl_write_vtu", "shl_get_energies"]
 
 
 class ShlError(RuntimeError):
