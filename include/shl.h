@@ -253,6 +253,14 @@ shl_status shl_get_element_fields(shl_ctx* ctx, double* kGauss, double* kMean, d
 /* Lumped inverse masses and damping coefficients (ShellSystem.C:762-852). */
 shl_status shl_get_mass_damping(shl_ctx* ctx, double* Minv, double* C);
 
+/* Relative residual of the stored state, per shell (one value for a single
+ * shell, n_shells for a batch): ||f_ext - f_int||_2 / ||f_ext||_2 with
+ * f_ext the pressure force at `pressure` (times each shell's pressure scale)
+ * and f_int the internal force, at u (no damping, no inertia; self-contact
+ * forces are not included).  f2 / fext2 (may be NULL) get the squared norms.
+ * No counterpart in the reference, which has no residual stop. */
+shl_status shl_residual(shl_ctx* ctx, double pressure, double* rel, double* f2, double* fext2);
+
 /* Measurements of the last force evaluation or step (the scalars of
  * measure_properties, ShellSystem.C:2714-2846). */
 shl_status shl_get_energies(shl_ctx* ctx, shl_energies* e);
@@ -342,6 +350,35 @@ shl_status shl_gaussian_normal_imperfection(const double* xyz, uint32_t n_nodes,
  * NULL for the default stream; the call does not synchronise. */
 shl_status shl_internal_force_noalloc(shl_ctx* ctx, const double* u_dev, double pressure, double* f_dev,
                                       void* stream);
+
+/* ---- warm-start surrogate (no counterpart in the reference) ------------ */
+
+/* A multilayer perceptron dims[0] -> dims[1] -> ... -> dims[n_dims-1], GELU
+ * after every layer but the last, trained and evaluated on the GPU by the
+ * library's own BF16 tensor-core kernels (FP32 accumulation, FP32 master
+ * weights, Adam).  Weights are row-major (out x in) FP32 on the host side. */
+typedef struct shl_mlp shl_mlp;
+shl_status shl_mlp_create(const uint32_t* dims, uint32_t n_dims, uint32_t max_batch, uint64_t seed,
+                          shl_mlp** out);
+void shl_mlp_destroy(shl_mlp* mlp);
+shl_status shl_mlp_set_params(shl_mlp* mlp, uint32_t layer, const float* W, const float* b);
+shl_status shl_mlp_get_params(shl_mlp* mlp, uint32_t layer, float* W, float* b);
+/* Training set: n rows of inputs (dims[0]) and targets (dims[last]), copied to the device. */
+shl_status shl_mlp_set_dataset(shl_mlp* mlp, const float* X, const float* T, uint64_t n);
+/* iters Adam steps on shuffled mini-batches (mean squared error), learning
+ * rate decayed from lr0 to lr_final on a cosine; the loss of every
+ * curve_every-th batch goes to loss_curve (ceil(iters / curve_every) values). */
+shl_status shl_mlp_train(shl_mlp* mlp, uint32_t iters, uint32_t batch, float lr0, float lr_final, uint64_t seed,
+                         float* loss_curve, uint32_t curve_every);
+/* Outputs for n input rows (host arrays). */
+shl_status shl_mlp_predict(shl_mlp* mlp, const float* X, uint32_t n, float* Y);
+/* Loss and gradients of one batch of n <= max_batch rows (no update);
+ * dW[l] (out x in) and db[l] may be NULL. */
+shl_status shl_mlp_gradients(shl_mlp* mlp, const float* X, const float* T, uint32_t n, double* loss,
+                             float* const* dW, float* const* db);
+/* C = A . B^T with the library's BF16 GEMM: A (M x K) and B (N x K) as BF16
+ * bit patterns, K a multiple of 8; C is M x N FP32. */
+shl_status shl_gemm_bf16(const uint16_t* A, const uint16_t* B, uint32_t M, uint32_t N, uint32_t K, float* C);
 
 /* Default parameters (ShellSystem constructor and set_parameters defaults). */
 void shl_params_default(shl_params* p);

@@ -17,7 +17,7 @@ OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libshl_gb300.so")
 RUN = os.path.join(OUT, "shl_run")  # the command-line driver (csrc/shl_run.cpp)
 
-CU_SOURCES = ["shl_kernels.cu", "shl_contact.cu", "shl_api.cu"]
+CU_SOURCES = ["shl_kernels.cu", "shl_contact.cu", "shl_api.cu", "shl_mlp.cu"]
 CPP_SOURCES = ["shl_setup.cpp", "shl_host.cpp", "shl_io.cpp"]
 HEADERS = ["shl_geom.h", "shl_setup.h", "shl_internal.cuh", "shl_expr.h", os.path.join("..", "..", "include", "shl.h")]
 

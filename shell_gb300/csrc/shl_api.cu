@@ -60,6 +60,8 @@ struct shl_ctx {
   void* d_flush = nullptr;  // L2 eviction buffer of shl_time_kernel
   size_t flush_bytes = 0;
   std::vector<uint32_t> node_off, face_off;  // shell offsets (original order) of a batch
+  uint32_t* d_node_off = nullptr;            // device copy (shl_residual)
+  double* d_norms = nullptr;                 // per-shell |f|^2, |f_ext|^2
 };
 
 namespace {
@@ -464,6 +466,7 @@ shl_status create_common(shl_ctx* c, const std::vector<double>& pscale_orig, shl
   sc.fp32 = fp32 ? 1 : 0;
   sc.V = V;
   sc.F = F;
+  sc.internal_scale = 1.0;
 
   Ctl h;
   std::memset(&h, 0, sizeof(h));
@@ -1053,6 +1056,56 @@ shl_status shl_get_element_fields(shl_ctx* c, double* kG, double* kM, double* et
   if (eb) SHL_CUDA_TRY(cudaMemcpyAsync(eb, c->b.ebend, bytes, cudaMemcpyDeviceToHost, c->stream));
   if (area) SHL_CUDA_TRY(cudaMemcpyAsync(area, c->b.area, bytes, cudaMemcpyDeviceToHost, c->stream));
   SHL_CUDA_TRY(cudaStreamSynchronize(c->stream));
+  return SHL_OK;
+}
+
+shl_status shl_residual(shl_ctx* c, double pressure, double* rel, double* f2, double* fext2) {
+  if (!c) return SHL_ERR_ARG;
+  const size_t nd = 3 * (size_t)c->S.V;
+  const uint32_t ns = (uint32_t)c->node_off.size() - 1;
+  if (!c->d_node_off) {
+    SHL_TRY(dev_alloc(c, &c->d_node_off, ns + 1));
+    SHL_TRY(dev_alloc(c, &c->d_norms, 2 * (size_t)ns));
+    SHL_CUDA_TRY(cudaMemcpyAsync(c->d_node_off, c->node_off.data(), (ns + 1) * sizeof(uint32_t),
+                                 cudaMemcpyHostToDevice, c->stream));
+  }
+  const DevBuf& b = c->b;
+  SHL_CUDA_TRY(cudaMemcpyAsync(b.up, b.u, nd * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+  launch_positions(b, c->sc, c->stream);
+  Ctl h;
+  SHL_TRY(ctl_get(c, h));
+  Ctl saved = h;
+  h.halted = 0;
+  h.pressure = c->P.compat_zero_pressure ? pressure * 0.0 : pressure;
+  const double red = std::max((1.0 - static_cast<int>(h.time * 5.0) * 0.01), 0.5);
+  h.volume_pressure = (c->P.bulk_modulus == 0 ? 0 : c->P.bulk_modulus * (h.volume0 * red / h.volume - 1));
+  SHL_TRY(ctl_put(c, h));
+  // f = pressure force - internal force, then the pressure force alone (no contact, no damping)
+  StepConst sc = c->sc;
+  sc.contact = 0;
+  launch_elements(b, sc, c->eg, c->elem_blocks, c->stream);
+  launch_gather_correct(b, sc, 0, false, c->d_fa, nullptr, c->stream);
+  sc.internal_scale = 0.0;
+  launch_elements(b, sc, c->eg, c->elem_blocks, c->stream);
+  launch_gather_correct(b, sc, 0, false, c->d_fa + nd, nullptr, c->stream);
+  launch_shell_norms(c->d_fa, c->d_fa + nd, c->d_node_off, ns, c->d_norms, c->stream);
+  SHL_TRY(check_launch("shl_residual"));
+  std::vector<double> norms(2 * (size_t)ns);
+  SHL_CUDA_TRY(cudaMemcpyAsync(norms.data(), c->d_norms, norms.size() * sizeof(double), cudaMemcpyDeviceToHost,
+                               c->stream));
+  SHL_CUDA_TRY(cudaStreamSynchronize(c->stream));
+  // the step state is the stored one: restore the control block's step scalars
+  Ctl h2;
+  SHL_TRY(ctl_get(c, h2));
+  h2.halted = saved.halted;
+  h2.pressure = saved.pressure;
+  h2.volume_pressure = saved.volume_pressure;
+  SHL_TRY(ctl_put(c, h2));
+  for (uint32_t k = 0; k < ns; ++k) {
+    if (f2) f2[k] = norms[2 * k];
+    if (fext2) fext2[k] = norms[2 * k + 1];
+    if (rel) rel[k] = norms[2 * k + 1] > 0 ? std::sqrt(norms[2 * k] / norms[2 * k + 1]) : INFINITY;
+  }
   return SHL_OK;
 }
 

@@ -116,6 +116,7 @@ struct StepConst {
   int32_t stop_on_problem;
   int32_t fp32;      // element forces in FP32 (relative-displacement form)
   uint32_t V, F;
+  double internal_scale;  // 1, or 0 for the pressure-only force of a residual check
 };
 
 // Device buffers of one context.
@@ -176,6 +177,8 @@ void launch_fp64_peak(double* out, int blocks, int iters, cudaStream_t s);
 uint32_t noalloc_max_faces();
 cudaError_t launch_force_noalloc(const DevBuf& ctx_b, const StepConst& sc, const ElemGroups& eg, uint32_t n_blocks,
                                  const double* u, double pressure, double* f_out, cudaStream_t s);
+void launch_shell_norms(const double* f, const double* fext, const uint32_t* node_off, uint32_t n_shells, double* out,
+                        cudaStream_t s);
 void launch_flush(void* buf, size_t bytes, uint32_t tag, cudaStream_t s);
 
 // ---- launchers (shl_contact.cu) ----

@@ -243,7 +243,7 @@ __device__ __forceinline__ ElemOut element_force(uint32_t i, int np_rt, const do
   const double be0 = FC(FF_B0) - h0, be1 = FC(FF_B1) - h1, be2 = 2.0 * (FC(FF_B2) - h2);
   const double H00 = FC(FF_H00), H01 = FC(FF_H01), H02 = FC(FF_H02), H11 = FC(FF_H11), H12 = FC(FF_H12),
                H22 = FC(FF_H22);
-  const double Kf = FC(FF_K), Df = FC(FF_D);
+  const double Kf = FC(FF_K) * sc.internal_scale, Df = FC(FF_D) * sc.internal_scale;
 #undef FC
   const double n0 = Kf * (H00 * al0 + H01 * al1 + H02 * al2);
   const double n1 = Kf * (H01 * al0 + H11 * al1 + H12 * al2);
@@ -428,7 +428,7 @@ __device__ __forceinline__ ElemOut element_force32(uint32_t i, int np_rt, const 
     const float be2 = -2.f * (dotf(D3, dn) + dotf(d3, a3));
     const float H00 = FC(F32_H00), H01 = FC(F32_H01), H02 = FC(F32_H02), H11 = FC(F32_H11), H12 = FC(F32_H12),
                 H22 = FC(F32_H22);
-    const float K = FC(F32_K), Dm = FC(F32_D);
+    const float K = FC(F32_K) * (float)sc.internal_scale, Dm = FC(F32_D) * (float)sc.internal_scale;
     const float n0 = K * (H00 * al0 + H01 * al1 + H02 * al2);
     const float n1 = K * (H01 * al0 + H11 * al1 + H12 * al2);
     const float n2 = K * (H02 * al0 + H12 * al1 + H22 * al2);
@@ -874,6 +874,30 @@ __global__ void __launch_bounds__(kBlock) k_volume_end(DevBuf b, StepConst sc, i
 
 // ------------------------------------------------------------ utilities --
 // FP64 FMA throughput probe: 8 independent register chains per thread.
+// per shell s (nodes node_off[s] .. node_off[s+1]): sum |f|^2 and |f_ext|^2 in a
+// fixed order (one block per shell)
+__global__ void __launch_bounds__(kBlock) k_shell_norms(const double* f, const double* fext, const uint32_t* node_off,
+                                                        double* out) {
+  __shared__ double sh[kBlock / 32];
+  const uint32_t n0 = node_off[blockIdx.x], n1 = node_off[blockIdx.x + 1];
+  double a = 0.0, e = 0.0;
+  for (size_t k = 3 * (size_t)n0 + threadIdx.x; k < 3 * (size_t)n1; k += blockDim.x) {
+    a += f[k] * f[k];
+    e += fext[k] * fext[k];
+  }
+  a = block_sum(a, sh);
+  e = block_sum(e, sh);
+  if (threadIdx.x == 0) {
+    out[2 * blockIdx.x] = a;
+    out[2 * blockIdx.x + 1] = e;
+  }
+}
+
+void launch_shell_norms(const double* f, const double* fext, const uint32_t* node_off, uint32_t n_shells, double* out,
+                        cudaStream_t s) {
+  k_shell_norms<<<n_shells, kBlock, 0, s>>>(f, fext, node_off, out);
+}
+
 __global__ void __launch_bounds__(256) k_fp64_peak(double* out, int iters, double b, double c) {
   double a0 = threadIdx.x * 1e-9, a1 = a0 + 1e-3, a2 = a0 + 2e-3, a3 = a0 + 3e-3;
   double a4 = a0 + 4e-3, a5 = a0 + 5e-3, a6 = a0 + 6e-3, a7 = a0 + 7e-3;

@@ -1,0 +1,714 @@
+// shl_mlp.cu -- the warm-start surrogate: a multilayer perceptron trained and
+// evaluated on the GPU with this file's own kernels (no counterpart in the
+// reference, which always starts from the undeformed state).
+//
+// Network: x (n_in) -> [Linear -> GELU] x n_hidden -> Linear -> y (n_out).
+// Weights are kept as FP32 master copies and as BF16 copies W (out x in) and
+// W^T (in x out) for the tensor-core GEMMs; every GEMM multiplies BF16
+// operands with FP32 accumulation.  One GEMM form serves all three products
+// of a layer, C[M,N] = A[M,K] . B[N,K]^T with both operands K-contiguous:
+//   forward        Z  = H_prev . W^T        (A = H_prev,  B = W)
+//   input grad     dH = dZ . W              (A = dZ,      B = W^T)
+//   weight grad    dW = dZ^T . H_prev       (A = dZ^T,    B = H_prev^T)
+// The GEMM is a 128x128x32 block tile of eight warps, each a 64x32 warp tile
+// of mma.sync m16n8k16 BF16 products fed by ldmatrix from a two-stage
+// cp.async shared-memory pipeline.  Split-K writes FP32 partials that one
+// fixed-order kernel sums, so every result is deterministic.
+//
+// GELU is the erf form 0.5 x (1 + erf(x / sqrt 2)); the loss is the mean
+// squared error over the real (unpadded) outputs; the optimiser is Adam with
+// bias correction.  Feature dimensions are padded to multiples of 32 and the
+// batch to a multiple of 128; padded weights, inputs and targets are zero.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <random>
+#include <string>
+#include <vector>
+
+#include "../../include/shl.h"
+#include "shl_setup.h"
+
+namespace {
+
+constexpr int kBM = 128, kBN = 128, kBK = 32;
+constexpr int kLds = kBK + 8;  // padded shared row (bf16): 80 bytes, conflict-free ldmatrix
+constexpr int kGemmThreads = 256;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void* src, bool pred) {
+  const int n = pred ? 16 : 0;  // zero-fill outside the matrix
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(dst), "l"(src), "r"(n));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::); }
+
+__device__ __forceinline__ void ldmatrix_x4(uint32_t addr, uint32_t& r0, uint32_t& r1, uint32_t& r2, uint32_t& r3) {
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+               : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
+               : "r"(addr));
+}
+
+__device__ __forceinline__ void mma_bf16(float* d, const uint32_t* a, const uint32_t* b) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};\n"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+__device__ __forceinline__ float gelu(float x) { return 0.5f * x * (1.0f + erff(x * 0.70710678118654752f)); }
+__device__ __forceinline__ float gelu_grad(float x) {
+  const float cdf = 0.5f * (1.0f + erff(x * 0.70710678118654752f));
+  const float pdf = 0.39894228040143268f * expf(-0.5f * x * x);
+  return cdf + x * pdf;
+}
+
+// epilogue modes
+enum { EPI_PARTIAL = 0, EPI_BIAS = 1, EPI_BIAS_GELU = 2 };
+
+struct GemmArgs {
+  const __nv_bfloat16* A;  // M x K, row stride lda
+  const __nv_bfloat16* B;  // N x K, row stride ldb
+  int M, N, K, lda, ldb;
+  int k_per_split;         // multiple of kBK
+  int mode;
+  const float* bias;       // N (EPI_BIAS*)
+  float* C;                // M x N fp32 (ldc) ; EPI_PARTIAL: split z writes C + z*M*ldc
+  int ldc;
+  __nv_bfloat16* Cb;       // optional bf16 copy of the activation (ldc)
+};
+
+// C = A . B^T on a 128x128 block tile; blockIdx.z = split-K slice
+__global__ void __launch_bounds__(kGemmThreads) k_gemm_bf16(GemmArgs g) {
+  __shared__ __align__(16) __nv_bfloat16 sA[2][kBM * kLds];
+  __shared__ __align__(16) __nv_bfloat16 sB[2][kBN * kLds];
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int wm = warp >> 2, wn = warp & 3;  // 2 x 4 warps, warp tile 64 x 32
+  const int m0 = blockIdx.y * kBM, n0 = blockIdx.x * kBN;
+  const int k_begin = blockIdx.z * g.k_per_split;
+  const int k_end = min(g.K, k_begin + g.k_per_split);
+  const int n_tiles = (k_end - k_begin + kBK - 1) / kBK;
+
+  float acc[4][4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+#pragma unroll
+      for (int r = 0; r < 4; ++r) acc[i][j][r] = 0.f;
+
+  // each thread copies two 16-byte chunks of A and two of B per k tile
+  auto load_tile = [&](int stage, int kt) {
+    const int kb = k_begin + kt * kBK;
+#pragma unroll
+    for (int c = 0; c < 2; ++c) {
+      const int chunk = tid + c * kGemmThreads;  // 0..511
+      const int row = chunk >> 2, col = (chunk & 3) * 8;
+      const int gm = m0 + row, gk = kb + col;
+      const bool pa = gm < g.M && gk < k_end;
+      const __nv_bfloat16* srcA = g.A + (size_t)(pa ? gm : 0) * g.lda + (pa ? gk : 0);
+      cp_async16(smem_u32(&sA[stage][row * kLds + col]), srcA, pa);
+      const int gn = n0 + row;
+      const bool pb = gn < g.N && gk < k_end;
+      const __nv_bfloat16* srcB = g.B + (size_t)(pb ? gn : 0) * g.ldb + (pb ? gk : 0);
+      cp_async16(smem_u32(&sB[stage][row * kLds + col]), srcB, pb);
+    }
+    cp_async_commit();
+  };
+
+  if (n_tiles > 0) load_tile(0, 0);
+  for (int kt = 0; kt < n_tiles; ++kt) {
+    const int st = kt & 1;
+    cp_async_wait_all();
+    __syncthreads();
+    if (kt + 1 < n_tiles) load_tile(st ^ 1, kt + 1);
+#pragma unroll
+    for (int ks = 0; ks < kBK; ks += 16) {
+      uint32_t af[4][4], bfr[4][2];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        const int r = wm * 64 + i * 16 + (lane & 15);
+        const int c = ks + (lane >> 4) * 8;
+        ldmatrix_x4(smem_u32(&sA[st][r * kLds + c]), af[i][0], af[i][1], af[i][2], af[i][3]);
+      }
+#pragma unroll
+      for (int j = 0; j < 4; j += 2) {
+        // lanes 0-7: n 0-7 k 0; 8-15: n 0-7 k 8; 16-23: n 8-15 k 0; 24-31: n 8-15 k 8
+        const int r = wn * 32 + j * 8 + (lane & 7) + ((lane >> 4) << 3);
+        const int c = ks + ((lane >> 3) & 1) * 8;
+        ldmatrix_x4(smem_u32(&sB[st][r * kLds + c]), bfr[j][0], bfr[j][1], bfr[j + 1][0], bfr[j + 1][1]);
+      }
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) mma_bf16(acc[i][j], af[i], bfr[j]);
+    }
+    __syncthreads();
+  }
+
+  // epilogue: thread holds rows (lane/4, +8) and columns 2*(lane%4) + {0,1} of each 16x8 tile
+  const int gr = lane >> 2, gc = (lane & 3) * 2;
+  float* C = g.C + (g.mode == EPI_PARTIAL ? (size_t)blockIdx.z * g.M * g.ldc : 0);
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int row = m0 + wm * 64 + i * 16 + gr + h * 8;
+        if (row >= g.M) continue;
+#pragma unroll
+        for (int e = 0; e < 2; ++e) {
+          const int col = n0 + wn * 32 + j * 8 + gc + e;
+          if (col >= g.N) continue;
+          float v = acc[i][j][2 * h + e];
+          if (g.mode != EPI_PARTIAL) v += g.bias[col];
+          const size_t o = (size_t)row * g.ldc + col;
+          C[o] = v;
+          if (g.Cb) g.Cb[o] = __float2bfloat16_rn(g.mode == EPI_BIAS_GELU ? gelu(v) : v);
+        }
+      }
+}
+
+// out[m, n] = sum over splits of part[s, m, n] (fixed order), optional bf16 copy
+__global__ void k_splitk_reduce(const float* part, int splits, size_t mn, float* out, __nv_bfloat16* outb) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < mn; i += (size_t)gridDim.x * blockDim.x) {
+    float s = 0.f;
+    for (int z = 0; z < splits; ++z) s += part[(size_t)z * mn + i];
+    if (out) out[i] = s;
+    if (outb) outb[i] = __float2bfloat16_rn(s);
+  }
+}
+
+// rows of the dataset into a padded bf16 input batch and an fp32 target batch
+__global__ void k_gather_batch(const float* X, const float* T, const uint32_t* idx, int n, int in_real, int in_pad,
+                               int out_real, int out_pad, int batch_pad, __nv_bfloat16* Xb, float* Tb) {
+  const int r = blockIdx.x;
+  if (r >= batch_pad) return;
+  const bool real = r < n;
+  const size_t src = real ? idx[r] : 0;
+  for (int c = threadIdx.x; c < in_pad; c += blockDim.x)
+    Xb[(size_t)r * in_pad + c] = __float2bfloat16_rn(real && c < in_real ? X[src * in_real + c] : 0.f);
+  if (Tb)
+    for (int c = threadIdx.x; c < out_pad; c += blockDim.x)
+      Tb[(size_t)r * out_pad + c] = real && c < out_real ? T[src * out_real + c] : 0.f;
+}
+
+// loss = mean over the n x out_real block of (y - t)^2; dY = 2 (y - t) / (n out_real) as bf16;
+// per-block partial sums of the squared error
+__global__ void k_mse(const float* Y, const float* Tb, int n, int out_real, int out_pad, int batch_pad,
+                      __nv_bfloat16* dY, double* partial) {
+  __shared__ double sh[32];
+  const size_t total = (size_t)batch_pad * out_pad;
+  const float scale = 2.0f / ((float)n * (float)out_real);
+  double s = 0.0;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+    const int r = (int)(i / out_pad), c = (int)(i % out_pad);
+    float d = 0.f;
+    if (r < n && c < out_real) d = Y[i] - Tb[i];
+    s += (double)d * d;
+    dY[i] = __float2bfloat16_rn(scale * d);
+  }
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    s = threadIdx.x < (blockDim.x >> 5) ? sh[threadIdx.x] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if (threadIdx.x == 0) partial[blockIdx.x] = s;
+  }
+}
+
+// dZ = dH * gelu'(Z), padded rows and columns forced to zero; bf16 out
+__global__ void k_gelu_back(const float* dH, const float* Z, size_t mn, int cols, int n_rows, int real_cols,
+                            __nv_bfloat16* dZ) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < mn; i += (size_t)gridDim.x * blockDim.x) {
+    const int r = (int)(i / cols), c = (int)(i % cols);
+    const float v = (r < n_rows && c < real_cols) ? dH[i] * gelu_grad(Z[i]) : 0.f;
+    dZ[i] = __float2bfloat16_rn(v);
+  }
+}
+
+// out (cols x rows) = in (rows x cols)^T, bf16, 32x32 tiles
+__global__ void k_transpose(const __nv_bfloat16* in, int rows, int cols, __nv_bfloat16* out) {
+  __shared__ __nv_bfloat16 t[32][33];
+  const int bx = blockIdx.x * 32, by = blockIdx.y * 32;
+  for (int j = threadIdx.y; j < 32; j += blockDim.y) {
+    const int r = by + j, c = bx + threadIdx.x;
+    t[j][threadIdx.x] = (r < rows && c < cols) ? in[(size_t)r * cols + c] : __float2bfloat16_rn(0.f);
+  }
+  __syncthreads();
+  for (int j = threadIdx.y; j < 32; j += blockDim.y) {
+    const int c = bx + j, r = by + threadIdx.x;
+    if (c < cols && r < rows) out[(size_t)c * rows + r] = t[threadIdx.x][j];
+  }
+}
+
+// db[n] = sum over the batch rows of dZ[r, n] (fixed order)
+__global__ void k_bias_grad(const __nv_bfloat16* dZ, int rows, int cols, float* db) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= cols) return;
+  float s = 0.f;
+  for (int r = 0; r < rows; ++r) s += __bfloat162float(dZ[(size_t)r * cols + c]);
+  db[c] = s;
+}
+
+struct AdamArgs {
+  float lr, b1, b2, eps, c1, c2;  // c1 = 1/(1-b1^t), c2 = 1/(1-b2^t)
+};
+
+// Adam on the real (unpadded) block; refreshes W (out x in), W^T (in x out) bf16 copies
+__global__ void k_adam_w(float* W, float* m, float* v, const float* g, int out_real, int in_real, int out_pad,
+                         int in_pad, AdamArgs a, __nv_bfloat16* Wb, __nv_bfloat16* WTb) {
+  const size_t total = (size_t)out_pad * in_pad;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+    const int r = (int)(i / in_pad), c = (int)(i % in_pad);
+    if (r < out_real && c < in_real) {
+      const float gi = g[i];
+      const float mi = a.b1 * m[i] + (1.f - a.b1) * gi;
+      const float vi = a.b2 * v[i] + (1.f - a.b2) * gi * gi;
+      m[i] = mi;
+      v[i] = vi;
+      W[i] -= a.lr * (mi * a.c1) / (sqrtf(vi * a.c2) + a.eps);
+    }
+    const __nv_bfloat16 wb = __float2bfloat16_rn(W[i]);
+    Wb[i] = wb;
+    WTb[(size_t)c * out_pad + r] = wb;
+  }
+}
+
+__global__ void k_adam_b(float* b, float* m, float* v, const float* g, int n_real, AdamArgs a) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_real) return;
+  const float mi = a.b1 * m[i] + (1.f - a.b1) * g[i];
+  const float vi = a.b2 * v[i] + (1.f - a.b2) * g[i] * g[i];
+  m[i] = mi;
+  v[i] = vi;
+  b[i] -= a.lr * (mi * a.c1) / (sqrtf(vi * a.c2) + a.eps);
+}
+
+int pad_to(int x, int m) { return (x + m - 1) / m * m; }
+
+}  // namespace
+
+struct shl_mlp {
+  int n_layers = 0;                  // linear layers
+  std::vector<int> dim, pad;         // real and padded widths, n_layers + 1
+  int max_batch = 0, batch_pad = 0;  // rows
+  cudaStream_t stream = nullptr;
+  std::vector<void*> allocs;
+  // per layer (out x in)
+  std::vector<float*> W, b, mW, vW, mb, vb, gW, gb;
+  std::vector<__nv_bfloat16*> Wb, WTb;
+  // activations per layer boundary (batch_pad x pad[l])
+  std::vector<float*> Z;             // pre-activation of layer l output (l = 1..n)
+  std::vector<__nv_bfloat16*> H;     // bf16 activation (H[0] = input)
+  std::vector<__nv_bfloat16*> HT;    // transposes for the weight-gradient GEMM
+  float* dH = nullptr;               // fp32 input grad scratch (max width)
+  __nv_bfloat16* dZ = nullptr;       // bf16 grads (max width)
+  __nv_bfloat16* dZT = nullptr;
+  float* part = nullptr;             // split-K partials
+  size_t part_elems = 0;
+  float* Tb = nullptr;
+  double* loss_part = nullptr;
+  uint32_t* idx = nullptr;
+  float* dX = nullptr;               // dataset inputs (n x in_real)
+  float* dT = nullptr;               // dataset targets (n x out_real)
+  size_t n_data = 0;
+  int step = 0;
+};
+
+namespace {
+
+thread_local std::string g_mlp_err;
+
+#define MLP_TRY(expr)                                                            \
+  do {                                                                           \
+    cudaError_t e_ = (expr);                                                     \
+    if (e_ != cudaSuccess) {                                                     \
+      shl::set_error(std::string(#expr) + ": " + cudaGetErrorString(e_));        \
+      return e_ == cudaErrorMemoryAllocation ? SHL_ERR_OOM : SHL_ERR_CUDA;       \
+    }                                                                            \
+  } while (0)
+
+template <class T>
+shl_status mlp_alloc(shl_mlp* m, T** p, size_t n) {
+  void* q = nullptr;
+  MLP_TRY(cudaMalloc(&q, std::max<size_t>(n, 1) * sizeof(T)));
+  MLP_TRY(cudaMemsetAsync(q, 0, std::max<size_t>(n, 1) * sizeof(T), m->stream));
+  m->allocs.push_back(q);
+  *p = (T*)q;
+  return SHL_OK;
+}
+
+#define MLP_CHECK(expr)                  \
+  do {                                   \
+    shl_status s_ = (expr);              \
+    if (s_ != SHL_OK) return s_;         \
+  } while (0)
+
+// C[M,N] = A[M,K] . B[N,K]^T with the chosen epilogue.  Products without an
+// epilogue split K when the output grid alone would leave SMs idle.
+shl_status gemm(shl_mlp* m, const __nv_bfloat16* A, int lda, const __nv_bfloat16* B, int ldb, int M, int N, int K,
+                int mode, const float* bias, float* C, __nv_bfloat16* Cb) {
+  const int gx = (N + kBN - 1) / kBN, gy = (M + kBM - 1) / kBM;
+  const int k_tiles = (K + kBK - 1) / kBK;
+  int splits = 1;
+  if (mode == EPI_PARTIAL)
+    while (gx * gy * splits < 2 * 152 && k_tiles / (splits * 2) >= 8 &&
+           (size_t)(splits * 2) * M * N <= m->part_elems)
+      splits *= 2;
+  GemmArgs g{A, B, M, N, K, lda, ldb, 0, mode, bias, C, N, Cb};
+  if (splits == 1) {
+    g.k_per_split = k_tiles * kBK;
+    k_gemm_bf16<<<dim3(gx, gy, 1), kGemmThreads, 0, m->stream>>>(g);
+    return SHL_OK;
+  }
+  const int tiles_per = (k_tiles + splits - 1) / splits;
+  g.k_per_split = tiles_per * kBK;
+  splits = (k_tiles + tiles_per - 1) / tiles_per;
+  g.C = m->part;
+  g.Cb = nullptr;
+  k_gemm_bf16<<<dim3(gx, gy, splits), kGemmThreads, 0, m->stream>>>(g);
+  k_splitk_reduce<<<592, 256, 0, m->stream>>>(m->part, splits, (size_t)M * N, C, Cb);
+  return SHL_OK;
+}
+
+// forward pass of `rows` (padded) inputs already in H[0]
+shl_status forward(shl_mlp* m) {
+  const int R = m->batch_pad;
+  for (int l = 0; l < m->n_layers; ++l) {
+    const bool last = l == m->n_layers - 1;
+    MLP_CHECK(gemm(m, m->H[l], m->pad[l], m->Wb[l], m->pad[l], R, m->pad[l + 1], m->pad[l], last ? EPI_BIAS : EPI_BIAS_GELU,
+                   m->b[l], m->Z[l + 1], last ? nullptr : m->H[l + 1]));
+  }
+  return SHL_OK;
+}
+
+shl_status backward(shl_mlp* m, int n_rows) {
+  const int R = m->batch_pad;
+  // dZ of the output layer is in m->dZ (bf16, R x pad[n])
+  for (int l = m->n_layers - 1; l >= 0; --l) {
+    const int out = m->pad[l + 1], in = m->pad[l];
+    // transposes for dW = dZ^T . H_l
+    k_transpose<<<dim3((out + 31) / 32, (R + 31) / 32), dim3(32, 8), 0, m->stream>>>(m->dZ, R, out, m->dZT);
+    k_transpose<<<dim3((in + 31) / 32, (R + 31) / 32), dim3(32, 8), 0, m->stream>>>(m->H[l], R, in, m->HT[l]);
+    MLP_CHECK(gemm(m, m->dZT, R, m->HT[l], R, out, in, R, EPI_PARTIAL, nullptr, m->gW[l], nullptr));
+    k_bias_grad<<<(out + 127) / 128, 128, 0, m->stream>>>(m->dZ, R, out, m->gb[l]);
+    if (l == 0) break;
+    // dH_l = dZ . W  (B operand W^T: in x out)
+    MLP_CHECK(gemm(m, m->dZ, out, m->WTb[l], out, R, in, out, EPI_PARTIAL, nullptr, m->dH, nullptr));
+    k_gelu_back<<<592, 256, 0, m->stream>>>(m->dH, m->Z[l], (size_t)R * in, in, n_rows, m->dim[l], m->dZ);
+  }
+  return SHL_OK;
+}
+
+shl_status load_batch(shl_mlp* m, const uint32_t* idx_host, int n) {
+  MLP_TRY(cudaMemcpyAsync(m->idx, idx_host, n * sizeof(uint32_t), cudaMemcpyHostToDevice, m->stream));
+  k_gather_batch<<<m->batch_pad, 256, 0, m->stream>>>(m->dX, m->dT, m->idx, n, m->dim[0], m->pad[0],
+                                                      m->dim[m->n_layers], m->pad[m->n_layers], m->batch_pad,
+                                                      m->H[0], m->Tb);
+  return SHL_OK;
+}
+
+shl_status loss_and_grad(shl_mlp* m, int n, double* loss_out) {
+  const int L = m->n_layers;
+  k_mse<<<592, 256, 0, m->stream>>>(m->Z[L], m->Tb, n, m->dim[L], m->pad[L], m->batch_pad, m->dZ, m->loss_part);
+  if (loss_out) {
+    std::vector<double> p(592);
+    MLP_TRY(cudaMemcpyAsync(p.data(), m->loss_part, 592 * sizeof(double), cudaMemcpyDeviceToHost, m->stream));
+    MLP_TRY(cudaStreamSynchronize(m->stream));
+    double s = 0;
+    for (double x : p) s += x;
+    *loss_out = s / ((double)n * m->dim[L]);
+  }
+  return SHL_OK;
+}
+
+shl_status adam(shl_mlp* m, float lr) {
+  ++m->step;
+  AdamArgs a{lr, 0.9f, 0.999f, 1e-8f, 0.f, 0.f};
+  a.c1 = 1.f / (1.f - std::pow(a.b1, (float)m->step));
+  a.c2 = 1.f / (1.f - std::pow(a.b2, (float)m->step));
+  for (int l = 0; l < m->n_layers; ++l) {
+    k_adam_w<<<592, 256, 0, m->stream>>>(m->W[l], m->mW[l], m->vW[l], m->gW[l], m->dim[l + 1], m->dim[l],
+                                          m->pad[l + 1], m->pad[l], a, m->Wb[l], m->WTb[l]);
+    k_adam_b<<<(m->dim[l + 1] + 255) / 256, 256, 0, m->stream>>>(m->b[l], m->mb[l], m->vb[l], m->gb[l],
+                                                                 m->dim[l + 1], a);
+  }
+  return SHL_OK;
+}
+
+// refresh bf16 copies after host-set weights
+shl_status refresh_copies(shl_mlp* m) {
+  for (int l = 0; l < m->n_layers; ++l) {
+    AdamArgs a{0.f, 0.f, 0.f, 1.f, 0.f, 0.f};
+    // lr = 0: the Adam kernel only rewrites the bf16 copies (m, v unchanged since g is not read for lr 0)
+    k_adam_w<<<592, 256, 0, m->stream>>>(m->W[l], m->mW[l], m->vW[l], m->gW[l], 0, 0, m->pad[l + 1], m->pad[l], a,
+                                          m->Wb[l], m->WTb[l]);
+  }
+  return SHL_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+shl_status shl_mlp_create(const uint32_t* dims, uint32_t n_dims, uint32_t max_batch, uint64_t seed, shl_mlp** out) {
+  if (!dims || n_dims < 2 || !out || max_batch == 0) return SHL_ERR_ARG;
+  shl_mlp* m = new shl_mlp();
+  m->n_layers = (int)n_dims - 1;
+  for (uint32_t i = 0; i < n_dims; ++i) {
+    if (dims[i] == 0) {
+      delete m;
+      return SHL_ERR_ARG;
+    }
+    m->dim.push_back((int)dims[i]);
+    m->pad.push_back(pad_to((int)dims[i], 32));
+  }
+  m->max_batch = (int)max_batch;
+  m->batch_pad = pad_to((int)max_batch, kBM);
+  cudaError_t e = cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    delete m;
+    shl::set_error(std::string("cudaStreamCreate: ") + cudaGetErrorString(e));
+    return SHL_ERR_CUDA;
+  }
+  auto fail = [&](shl_status s) {
+    shl_mlp_destroy(m);
+    return s;
+  };
+  const int L = m->n_layers, R = m->batch_pad;
+  int maxw = 0;
+  for (int w : m->pad) maxw = std::max(maxw, w);
+  m->W.resize(L); m->b.resize(L); m->mW.resize(L); m->vW.resize(L); m->mb.resize(L); m->vb.resize(L);
+  m->gW.resize(L); m->gb.resize(L); m->Wb.resize(L); m->WTb.resize(L);
+  m->Z.assign(L + 1, nullptr); m->H.assign(L + 1, nullptr); m->HT.assign(L + 1, nullptr);
+  std::mt19937_64 rng(seed);
+  size_t max_wgrad = 0;
+  for (int l = 0; l < L; ++l) {
+    const size_t n = (size_t)m->pad[l + 1] * m->pad[l];
+    max_wgrad = std::max(max_wgrad, n);
+    shl_status s;
+    if ((s = mlp_alloc(m, &m->W[l], n)) || (s = mlp_alloc(m, &m->mW[l], n)) || (s = mlp_alloc(m, &m->vW[l], n)) ||
+        (s = mlp_alloc(m, &m->gW[l], n)) || (s = mlp_alloc(m, &m->Wb[l], n)) || (s = mlp_alloc(m, &m->WTb[l], n)) ||
+        (s = mlp_alloc(m, &m->b[l], m->pad[l + 1])) || (s = mlp_alloc(m, &m->mb[l], m->pad[l + 1])) ||
+        (s = mlp_alloc(m, &m->vb[l], m->pad[l + 1])) || (s = mlp_alloc(m, &m->gb[l], m->pad[l + 1])))
+      return fail(s);
+    // He-normal weights for the GELU layers, Glorot-normal for the output layer; zero bias
+    const double sd = (l < L - 1) ? std::sqrt(2.0 / m->dim[l]) : std::sqrt(2.0 / (m->dim[l] + m->dim[l + 1]));
+    std::normal_distribution<double> nd(0.0, sd);
+    std::vector<float> w(n, 0.f);
+    for (int r = 0; r < m->dim[l + 1]; ++r)
+      for (int c = 0; c < m->dim[l]; ++c) w[(size_t)r * m->pad[l] + c] = (float)nd(rng);
+    if (cudaMemcpyAsync(m->W[l], w.data(), n * sizeof(float), cudaMemcpyHostToDevice, m->stream) != cudaSuccess)
+      return fail(SHL_ERR_CUDA);
+  }
+  for (int l = 0; l <= L; ++l) {
+    shl_status s;
+    if ((s = mlp_alloc(m, &m->H[l], (size_t)R * m->pad[l])) || (s = mlp_alloc(m, &m->HT[l], (size_t)R * m->pad[l])) ||
+        (s = mlp_alloc(m, &m->Z[l], (size_t)R * m->pad[l])))
+      return fail(s);
+  }
+  m->part_elems = std::max((size_t)R * maxw, max_wgrad) * 2;
+  shl_status s;
+  if ((s = mlp_alloc(m, &m->dH, (size_t)R * maxw)) || (s = mlp_alloc(m, &m->dZ, (size_t)R * maxw)) ||
+      (s = mlp_alloc(m, &m->dZT, (size_t)R * maxw)) || (s = mlp_alloc(m, &m->part, m->part_elems)) ||
+      (s = mlp_alloc(m, &m->Tb, (size_t)R * m->pad[L])) || (s = mlp_alloc(m, &m->loss_part, 592)) ||
+      (s = mlp_alloc(m, &m->idx, (size_t)R)))
+    return fail(s);
+  if ((s = refresh_copies(m)) != SHL_OK) return fail(s);
+  if (cudaStreamSynchronize(m->stream) != cudaSuccess) return fail(SHL_ERR_CUDA);
+  *out = m;
+  return SHL_OK;
+}
+
+void shl_mlp_destroy(shl_mlp* m) {
+  if (!m) return;
+  if (m->stream) cudaStreamSynchronize(m->stream);
+  for (void* p : m->allocs) cudaFree(p);
+  if (m->stream) cudaStreamDestroy(m->stream);
+  delete m;
+}
+
+shl_status shl_mlp_set_params(shl_mlp* m, uint32_t layer, const float* W, const float* b) {
+  if (!m || (int)layer >= m->n_layers) return SHL_ERR_ARG;
+  const int l = (int)layer, out = m->dim[l + 1], in = m->dim[l];
+  if (W) {
+    std::vector<float> w((size_t)m->pad[l + 1] * m->pad[l], 0.f);
+    for (int r = 0; r < out; ++r) std::memcpy(&w[(size_t)r * m->pad[l]], W + (size_t)r * in, in * sizeof(float));
+    MLP_TRY(cudaMemcpyAsync(m->W[l], w.data(), w.size() * sizeof(float), cudaMemcpyHostToDevice, m->stream));
+  }
+  if (b) MLP_TRY(cudaMemcpyAsync(m->b[l], b, out * sizeof(float), cudaMemcpyHostToDevice, m->stream));
+  MLP_CHECK(refresh_copies(m));
+  MLP_TRY(cudaStreamSynchronize(m->stream));
+  return SHL_OK;
+}
+
+shl_status shl_mlp_get_params(shl_mlp* m, uint32_t layer, float* W, float* b) {
+  if (!m || (int)layer >= m->n_layers) return SHL_ERR_ARG;
+  const int l = (int)layer, out = m->dim[l + 1], in = m->dim[l];
+  if (W) {
+    std::vector<float> w((size_t)m->pad[l + 1] * m->pad[l]);
+    MLP_TRY(cudaMemcpyAsync(w.data(), m->W[l], w.size() * sizeof(float), cudaMemcpyDeviceToHost, m->stream));
+    MLP_TRY(cudaStreamSynchronize(m->stream));
+    for (int r = 0; r < out; ++r) std::memcpy(W + (size_t)r * in, &w[(size_t)r * m->pad[l]], in * sizeof(float));
+  }
+  if (b) {
+    MLP_TRY(cudaMemcpyAsync(b, m->b[l], out * sizeof(float), cudaMemcpyDeviceToHost, m->stream));
+    MLP_TRY(cudaStreamSynchronize(m->stream));
+  }
+  return SHL_OK;
+}
+
+shl_status shl_mlp_set_dataset(shl_mlp* m, const float* X, const float* T, uint64_t n) {
+  if (!m || !X || !T || n == 0) return SHL_ERR_ARG;
+  if (m->dX) {
+    // datasets are replaced by allocating anew (old ones stay until destroy)
+  }
+  const size_t in = (size_t)m->dim[0], out = (size_t)m->dim[m->n_layers];
+  MLP_CHECK(mlp_alloc(m, &m->dX, n * in));
+  MLP_CHECK(mlp_alloc(m, &m->dT, n * out));
+  MLP_TRY(cudaMemcpyAsync(m->dX, X, n * in * sizeof(float), cudaMemcpyHostToDevice, m->stream));
+  MLP_TRY(cudaMemcpyAsync(m->dT, T, n * out * sizeof(float), cudaMemcpyHostToDevice, m->stream));
+  MLP_TRY(cudaStreamSynchronize(m->stream));
+  m->n_data = n;
+  return SHL_OK;
+}
+
+shl_status shl_mlp_train(shl_mlp* m, uint32_t iters, uint32_t batch, float lr0, float lr_final, uint64_t seed,
+                         float* loss_curve, uint32_t curve_every) {
+  if (!m || !m->dX || batch == 0 || (int)batch > m->max_batch) return SHL_ERR_ARG;
+  std::mt19937_64 rng(seed);
+  std::vector<uint32_t> perm(m->n_data);
+  for (size_t i = 0; i < perm.size(); ++i) perm[i] = (uint32_t)i;
+  size_t pos = perm.size();
+  std::vector<uint32_t> idx(batch);
+  for (uint32_t it = 0; it < iters; ++it) {
+    for (uint32_t k = 0; k < batch; ++k) {
+      if (pos == perm.size()) {
+        std::shuffle(perm.begin(), perm.end(), rng);
+        pos = 0;
+      }
+      idx[k] = perm[pos++];
+    }
+    MLP_CHECK(load_batch(m, idx.data(), (int)batch));
+    MLP_CHECK(forward(m));
+    const bool record = loss_curve && curve_every && it % curve_every == 0;
+    double loss = 0;
+    MLP_CHECK(loss_and_grad(m, (int)batch, record ? &loss : nullptr));
+    if (record) loss_curve[it / curve_every] = (float)loss;
+    MLP_CHECK(backward(m, (int)batch));
+    // cosine decay from lr0 to lr_final
+    const float lr = lr_final + 0.5f * (lr0 - lr_final) * (1.f + std::cos(3.14159265358979f * it / std::max(1u, iters)));
+    MLP_CHECK(adam(m, lr));
+  }
+  MLP_TRY(cudaStreamSynchronize(m->stream));
+  MLP_TRY(cudaGetLastError());
+  return SHL_OK;
+}
+
+shl_status shl_mlp_predict(shl_mlp* m, const float* X, uint32_t n, float* Y) {
+  if (!m || !X || !Y) return SHL_ERR_ARG;
+  const int in = m->dim[0], L = m->n_layers, out = m->dim[L];
+  float* dXtmp = nullptr;
+  // inputs through a temporary device copy, in chunks of the maximum batch
+  MLP_TRY(cudaMallocAsync((void**)&dXtmp, (size_t)std::max<uint32_t>(n, 1) * in * sizeof(float), m->stream));
+  MLP_TRY(cudaMemcpyAsync(dXtmp, X, (size_t)n * in * sizeof(float), cudaMemcpyHostToDevice, m->stream));
+  std::vector<uint32_t> idx(m->max_batch);
+  std::vector<float> z((size_t)m->batch_pad * m->pad[L]);
+  shl_status st = SHL_OK;
+  for (uint32_t s = 0; s < n && st == SHL_OK; s += (uint32_t)m->max_batch) {
+    const int rows = (int)std::min<uint32_t>(m->max_batch, n - s);
+    for (int k = 0; k < rows; ++k) idx[k] = k;
+    if (cudaMemcpyAsync(m->idx, idx.data(), rows * sizeof(uint32_t), cudaMemcpyHostToDevice, m->stream) != cudaSuccess) {
+      st = SHL_ERR_CUDA;
+      break;
+    }
+    k_gather_batch<<<m->batch_pad, 256, 0, m->stream>>>(dXtmp + (size_t)s * in, nullptr, m->idx, rows, in, m->pad[0],
+                                                        out, m->pad[L], m->batch_pad, m->H[0], nullptr);
+    st = forward(m);
+    if (st != SHL_OK) break;
+    if (cudaMemcpyAsync(z.data(), m->Z[L], z.size() * sizeof(float), cudaMemcpyDeviceToHost, m->stream) != cudaSuccess ||
+        cudaStreamSynchronize(m->stream) != cudaSuccess) {
+      st = SHL_ERR_CUDA;
+      break;
+    }
+    for (int r = 0; r < rows; ++r)
+      std::memcpy(Y + (size_t)(s + r) * out, &z[(size_t)r * m->pad[L]], out * sizeof(float));
+  }
+  cudaFreeAsync(dXtmp, m->stream);
+  MLP_TRY(cudaStreamSynchronize(m->stream));
+  return st;
+}
+
+shl_status shl_mlp_gradients(shl_mlp* m, const float* X, const float* T, uint32_t n, double* loss, float* const* dW,
+                             float* const* db) {
+  if (!m || !X || !T || n == 0 || (int)n > m->max_batch) return SHL_ERR_ARG;
+  // the rows as a temporary dataset
+  float *x = m->dX, *t = m->dT;
+  const size_t nd = m->n_data;
+  const int in = m->dim[0], L = m->n_layers, out = m->dim[L];
+  MLP_TRY(cudaMallocAsync((void**)&m->dX, (size_t)n * in * sizeof(float), m->stream));
+  MLP_TRY(cudaMallocAsync((void**)&m->dT, (size_t)n * out * sizeof(float), m->stream));
+  MLP_TRY(cudaMemcpyAsync(m->dX, X, (size_t)n * in * sizeof(float), cudaMemcpyHostToDevice, m->stream));
+  MLP_TRY(cudaMemcpyAsync(m->dT, T, (size_t)n * out * sizeof(float), cudaMemcpyHostToDevice, m->stream));
+  std::vector<uint32_t> idx(n);
+  for (uint32_t k = 0; k < n; ++k) idx[k] = k;
+  shl_status st = load_batch(m, idx.data(), (int)n);
+  if (st == SHL_OK) st = forward(m);
+  if (st == SHL_OK) st = loss_and_grad(m, (int)n, loss);
+  if (st == SHL_OK) st = backward(m, (int)n);
+  cudaFreeAsync(m->dX, m->stream);
+  cudaFreeAsync(m->dT, m->stream);
+  m->dX = x;
+  m->dT = t;
+  m->n_data = nd;
+  if (st != SHL_OK) return st;
+  for (int l = 0; l < L; ++l) {
+    const int o = m->dim[l + 1], i = m->dim[l];
+    if (dW && dW[l]) {
+      std::vector<float> w((size_t)m->pad[l + 1] * m->pad[l]);
+      MLP_TRY(cudaMemcpyAsync(w.data(), m->gW[l], w.size() * sizeof(float), cudaMemcpyDeviceToHost, m->stream));
+      MLP_TRY(cudaStreamSynchronize(m->stream));
+      for (int r = 0; r < o; ++r) std::memcpy(dW[l] + (size_t)r * i, &w[(size_t)r * m->pad[l]], i * sizeof(float));
+    }
+    if (db && db[l]) MLP_TRY(cudaMemcpyAsync(db[l], m->gb[l], o * sizeof(float), cudaMemcpyDeviceToHost, m->stream));
+  }
+  MLP_TRY(cudaStreamSynchronize(m->stream));
+  return SHL_OK;
+}
+
+shl_status shl_gemm_bf16(const uint16_t* A, const uint16_t* B, uint32_t M, uint32_t N, uint32_t K, float* C) {
+  // C = A . B^T for host bf16 bit patterns (A: M x K, B: N x K), K a multiple of 8; a test entry point
+  if (!A || !B || !C || K % 8 != 0) return SHL_ERR_ARG;
+  shl_mlp tmp;
+  MLP_TRY(cudaStreamCreateWithFlags(&tmp.stream, cudaStreamNonBlocking));
+  __nv_bfloat16 *dA = nullptr, *dB = nullptr;
+  float* dC = nullptr;
+  tmp.part_elems = (size_t)M * N * 8;
+  shl_status st = SHL_OK;
+  if (mlp_alloc(&tmp, &dA, (size_t)M * K) || mlp_alloc(&tmp, &dB, (size_t)N * K) || mlp_alloc(&tmp, &dC, (size_t)M * N) ||
+      mlp_alloc(&tmp, &tmp.part, tmp.part_elems))
+    st = SHL_ERR_OOM;
+  if (st == SHL_OK) {
+    cudaMemcpyAsync(dA, A, (size_t)M * K * 2, cudaMemcpyHostToDevice, tmp.stream);
+    cudaMemcpyAsync(dB, B, (size_t)N * K * 2, cudaMemcpyHostToDevice, tmp.stream);
+    st = gemm(&tmp, dA, (int)K, dB, (int)K, (int)M, (int)N, (int)K, EPI_PARTIAL, nullptr, dC, nullptr);
+    cudaMemcpyAsync(C, dC, (size_t)M * N * sizeof(float), cudaMemcpyDeviceToHost, tmp.stream);
+    if (cudaStreamSynchronize(tmp.stream) != cudaSuccess || cudaGetLastError() != cudaSuccess) st = SHL_ERR_CUDA;
+  }
+  for (void* p : tmp.allocs) cudaFree(p);
+  cudaStreamDestroy(tmp.stream);
+  return st;
+}
+
+}  // extern "C"

@@ -119,6 +119,16 @@ def load():
                                        ctypes.POINTER(_d), vp, _u32, ctypes.POINTER(_u32)]),
         "shl_write_vtu": (_i32, [vp, ctypes.c_char_p]),
         "shl_get_energies": (_i32, [vp, ctypes.POINTER(ShlEnergies)]),
+        "shl_mlp_create": (_i32, [vp, _u32, _u32, ctypes.c_uint64, ctypes.POINTER(vp)]),
+        "shl_mlp_destroy": (None, [vp]),
+        "shl_mlp_set_params": (_i32, [vp, _u32, vp, vp]),
+        "shl_mlp_get_params": (_i32, [vp, _u32, vp, vp]),
+        "shl_mlp_set_dataset": (_i32, [vp, vp, vp, ctypes.c_uint64]),
+        "shl_mlp_train": (_i32, [vp, _u32, _u32, ctypes.c_float, ctypes.c_float, ctypes.c_uint64, vp, _u32]),
+        "shl_mlp_predict": (_i32, [vp, vp, _u32, vp]),
+        "shl_mlp_gradients": (_i32, [vp, vp, vp, _u32, ctypes.POINTER(_d), vp, vp]),
+        "shl_gemm_bf16": (_i32, [vp, vp, _u32, _u32, _u32, vp]),
+        "shl_residual": (_i32, [vp, _d, vp, vp, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -139,7 +149,9 @@ def exported_symbols():
             "shl_step_collect", "shl_time_kernel", "shl_measure_fp64_peak", "shl_internal_force_noalloc",
             "shl_profile_step", "shl_batch_create", "shl_batch_layout", "shl_context_size", "shl_context_mesh",
             "shl_get_node_fields", "shl_apply_loaded_state", "shl_save_state_file", "shl_load_state_file",
-            "shl_write_vtu", "shl_get_energies"]
+            "shl_write_vtu", "shl_get_energies", "shl_mlp_create", "shl_mlp_destroy", "shl_mlp_set_params",
+            "shl_mlp_get_params", "shl_mlp_set_dataset", "shl_mlp_train", "shl_mlp_predict", "shl_mlp_gradients",
+            "shl_gemm_bf16", "shl_residual"]
 
 
 class ShlError(RuntimeError):
@@ -368,6 +380,16 @@ class Shell:
         _check(self.lib.shl_get_mass_damping(self.h, Minv.ctypes.data, C.ctypes.data), "shl_get_mass_damping", False)
         return Minv, C
 
+    n_shells = 1  # a Batch sets its own count
+
+    def residual(self, pressure):
+        """Relative residual ||f_ext - f_int|| / ||f_ext|| of the stored state, per shell."""
+        n = self.n_shells
+        rel, f2, e2 = np.zeros(n), np.zeros(n), np.zeros(n)
+        _check(self.lib.shl_residual(self.h, pressure, rel.ctypes.data, f2.ctypes.data, e2.ctypes.data),
+               "shl_residual", False)
+        return rel
+
     def node_fields(self):
         """Per-node ekin, ecav, eself, efric densities and masses of the last step."""
         out = [np.zeros(self.V) for _ in range(5)]
@@ -423,3 +445,86 @@ class Batch(Shell):
     def split(self, vec):
         """Per-shell views of a concatenated node-major vector."""
         return [vec[3 * self.node_off[k]:3 * self.node_off[k + 1]] for k in range(self.n_shells)]
+
+
+def gemm_bf16(A_bits, B_bits):
+    """C = A . B^T through the library's BF16 GEMM (A, B: uint16 BF16 bit patterns)."""
+    lib = load()
+    A_bits = np.ascontiguousarray(A_bits, dtype=np.uint16)
+    B_bits = np.ascontiguousarray(B_bits, dtype=np.uint16)
+    M, K = A_bits.shape
+    N = B_bits.shape[0]
+    C = np.zeros((M, N), dtype=np.float32)
+    _check(lib.shl_gemm_bf16(A_bits.ctypes.data, B_bits.ctypes.data, M, N, K, C.ctypes.data), "shl_gemm_bf16", False)
+    return C
+
+
+class MLP:
+    """The warm-start surrogate network (shl_mlp_*): dims[0] -> ... -> dims[-1], GELU between layers."""
+
+    def __init__(self, dims, max_batch=256, seed=0):
+        self.lib = load()
+        self.dims = [int(d) for d in dims]
+        arr = (_u32 * len(self.dims))(*self.dims)
+        h = ctypes.c_void_p()
+        _check(self.lib.shl_mlp_create(arr, len(self.dims), max_batch, seed, ctypes.byref(h)), "shl_mlp_create", False)
+        self.h = h
+        self.max_batch = max_batch
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.shl_mlp_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def get_params(self):
+        out = []
+        for l in range(len(self.dims) - 1):
+            W = np.zeros((self.dims[l + 1], self.dims[l]), dtype=np.float32)
+            b = np.zeros(self.dims[l + 1], dtype=np.float32)
+            _check(self.lib.shl_mlp_get_params(self.h, l, W.ctypes.data, b.ctypes.data), "shl_mlp_get_params", False)
+            out.append((W, b))
+        return out
+
+    def set_params(self, params):
+        for l, (W, b) in enumerate(params):
+            W = np.ascontiguousarray(W, dtype=np.float32)
+            b = np.ascontiguousarray(b, dtype=np.float32)
+            _check(self.lib.shl_mlp_set_params(self.h, l, W.ctypes.data, b.ctypes.data), "shl_mlp_set_params", False)
+
+    def set_dataset(self, X, T):
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        T = np.ascontiguousarray(T, dtype=np.float32)
+        self._data = (X, T)
+        _check(self.lib.shl_mlp_set_dataset(self.h, X.ctypes.data, T.ctypes.data, X.shape[0]), "shl_mlp_set_dataset",
+               False)
+
+    def train(self, iters, batch, lr0=1e-3, lr_final=1e-5, seed=0, curve_every=100):
+        curve = np.zeros((iters + curve_every - 1) // curve_every, dtype=np.float32)
+        _check(self.lib.shl_mlp_train(self.h, iters, batch, lr0, lr_final, seed, curve.ctypes.data, curve_every),
+               "shl_mlp_train", False)
+        return curve
+
+    def predict(self, X):
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        Y = np.zeros((X.shape[0], self.dims[-1]), dtype=np.float32)
+        _check(self.lib.shl_mlp_predict(self.h, X.ctypes.data, X.shape[0], Y.ctypes.data), "shl_mlp_predict", False)
+        return Y
+
+    def gradients(self, X, T):
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        T = np.ascontiguousarray(T, dtype=np.float32)
+        L = len(self.dims) - 1
+        dW = [np.zeros((self.dims[l + 1], self.dims[l]), dtype=np.float32) for l in range(L)]
+        db = [np.zeros(self.dims[l + 1], dtype=np.float32) for l in range(L)]
+        pW = (ctypes.c_void_p * L)(*[w.ctypes.data for w in dW])
+        pb = (ctypes.c_void_p * L)(*[b.ctypes.data for b in db])
+        loss = _d()
+        _check(self.lib.shl_mlp_gradients(self.h, X.ctypes.data, T.ctypes.data, X.shape[0], ctypes.byref(loss), pW, pb),
+               "shl_mlp_gradients", False)
+        return loss.value, dW, db

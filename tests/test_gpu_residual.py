@@ -1,0 +1,61 @@
+"""Relative residual ||f_ext - f_int|| / ||f_ext|| (shl_residual), single shells
+and batches, against the CPU oracle: f from an oracle force evaluation
+without self-contact, f_ext from one with the stiffness multipliers set to 0.
+Tolerance 1e-10 relative on the residual in FP64 (norms of 1e-12-accurate
+vectors); in FP32 the residual of an equilibrium is only resolved down to the
+FP32 force error (about 1e-6 of the force scale)."""
+import numpy as np
+import pytest
+
+from shell_gb300 import lib as L
+import oracle as O
+from tests.common import classical_pressure, physics_params
+
+pytestmark = pytest.mark.gpu
+
+
+def _oracle_residual(X, T, p, u, pressure):
+    o = O.Oracle(X, T, p, threads=4)
+    o.set_state(u, np.zeros_like(u), np.zeros_like(u))
+    f = o.eval_forces(u, np.zeros_like(u), pressure)[0]
+    q = L.default_params(**{k: getattr(p, k) for k, _ in L.ShlParams._fields_})
+    q.memb_stiff_mult = 0.0
+    q.bend_stiff_mult = 0.0
+    o2 = O.Oracle(X, T, q, threads=4)
+    o2.set_state(u, np.zeros_like(u), np.zeros_like(u))
+    fe = o2.eval_forces(u, np.zeros_like(u), pressure)[0]
+    return np.linalg.norm(f) / np.linalg.norm(fe), f, fe
+
+
+def test_residual_single_matches_oracle(cuda_ok):
+    X, T = L.icosphere(3)
+    rng = np.random.default_rng(4)
+    p = physics_params(contact=False)
+    u = 1e-3 * rng.standard_normal(X.size)
+    pres = -classical_pressure()
+    g = L.Shell(X, T, p)
+    g.set_state(u, np.zeros_like(u), np.zeros_like(u))
+    r = g.residual(pres)
+    ro, _, _ = _oracle_residual(X, T, p, u, pres)
+    assert r.shape == (1,)
+    assert abs(r[0] - ro) <= 1e-10 * ro
+    # the stored state is untouched and stepping continues normally
+    u2, _, _ = g.get_state()
+    assert np.array_equal(u2, u)
+
+
+def test_residual_batch_per_shell(cuda_ok):
+    meshes = [L.icosphere(3), L.icosphere(4), L.icosphere(3)]
+    rng = np.random.default_rng(5)
+    ps = [physics_params(contact=False, thickness=h, shell_young_modulus2=e2)
+          for h, e2 in ((0.01, 0.5), (0.02, 1.0), (0.005, 2.0))]
+    scale = np.array([1.0, 0.5, 2.0])
+    b = L.Batch(meshes, ps, scale)
+    us = [1e-3 * rng.standard_normal(X.size) for X, _ in meshes]
+    u = np.concatenate(us)
+    b.set_state(u, np.zeros_like(u), np.zeros_like(u))
+    pres = -classical_pressure()
+    r = b.residual(pres)
+    for k, ((X, T), p) in enumerate(zip(meshes, ps)):
+        ro, _, _ = _oracle_residual(X, T, p, us[k], pres * scale[k])
+        assert abs(r[k] - ro) <= 1e-10 * ro, k
