@@ -258,8 +258,14 @@ shl_status shl_get_mass_damping(shl_ctx* ctx, double* Minv, double* C);
  * f_ext the pressure force at `pressure` (times each shell's pressure scale)
  * and f_int the internal force, at u (no damping, no inertia; self-contact
  * forces are not included).  f2 / fext2 (may be NULL) get the squared norms.
+ * flags: SHL_RESIDUAL_FP64 evaluates the forces in FP64 also in an FP32
+ * context; SHL_RESIDUAL_CORRECT (FP32 context, with FP64) also stores the
+ * defect f64 - f32 at this state, which the following steps add to their FP32
+ * force (mixed-precision defect correction, so relaxation converges to the
+ * FP64 equilibrium); SHL_RESIDUAL_CLEAR drops a stored defect.
  * No counterpart in the reference, which has no residual stop. */
-shl_status shl_residual(shl_ctx* ctx, double pressure, double* rel, double* f2, double* fext2);
+enum { SHL_RESIDUAL_FP64 = 1, SHL_RESIDUAL_CORRECT = 2, SHL_RESIDUAL_CLEAR = 4 };
+shl_status shl_residual(shl_ctx* ctx, double pressure, int flags, double* rel, double* f2, double* fext2);
 
 /* Measurements of the last force evaluation or step (the scalars of
  * measure_properties, ShellSystem.C:2714-2846). */

@@ -62,6 +62,8 @@ struct shl_ctx {
   std::vector<uint32_t> node_off, face_off;  // shell offsets (original order) of a batch
   uint32_t* d_node_off = nullptr;            // device copy (shl_residual)
   double* d_norms = nullptr;                 // per-shell |f|^2, |f_ext|^2
+  double* qe64 = nullptr;                    // FP64 element shares of an FP32 context (shl_residual)
+  double* f32 = nullptr;                     // FP32 force at the checked state (defect correction)
 };
 
 namespace {
@@ -1059,17 +1061,30 @@ shl_status shl_get_element_fields(shl_ctx* c, double* kG, double* kM, double* et
   return SHL_OK;
 }
 
-shl_status shl_residual(shl_ctx* c, double pressure, double* rel, double* f2, double* fext2) {
+shl_status shl_residual(shl_ctx* c, double pressure, int flags, double* rel, double* f2, double* fext2) {
   if (!c) return SHL_ERR_ARG;
   const size_t nd = 3 * (size_t)c->S.V;
   const uint32_t ns = (uint32_t)c->node_off.size() - 1;
+  const bool ctx32 = c->sc.fp32 != 0;
+  const bool fp64 = (flags & SHL_RESIDUAL_FP64) || !ctx32;
+  const bool correct = (flags & SHL_RESIDUAL_CORRECT) && ctx32 && fp64;
   if (!c->d_node_off) {
     SHL_TRY(dev_alloc(c, &c->d_node_off, ns + 1));
     SHL_TRY(dev_alloc(c, &c->d_norms, 2 * (size_t)ns));
     SHL_CUDA_TRY(cudaMemcpyAsync(c->d_node_off, c->node_off.data(), (ns + 1) * sizeof(uint32_t),
                                  cudaMemcpyHostToDevice, c->stream));
   }
-  const DevBuf& b = c->b;
+  if (fp64 && ctx32 && !c->qe64) SHL_TRY(dev_alloc(c, &c->qe64, 36 * (size_t)c->S.F));
+  if (correct && !c->b.fcorr) {
+    SHL_TRY(dev_alloc(c, &c->b.fcorr, nd));
+    SHL_TRY(dev_alloc(c, &c->f32, nd));
+    // the step graphs hold the buffer table by value: capture them again with the correction
+    if (c->graph) cudaGraphExecDestroy(c->graph);
+    if (c->graph1) cudaGraphExecDestroy(c->graph1);
+    c->graph = c->graph1 = nullptr;
+  }
+  DevBuf b = c->b;
+  b.fcorr = nullptr;
   SHL_CUDA_TRY(cudaMemcpyAsync(b.up, b.u, nd * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
   launch_positions(b, c->sc, c->stream);
   Ctl h;
@@ -1083,11 +1098,26 @@ shl_status shl_residual(shl_ctx* c, double pressure, double* rel, double* f2, do
   // f = pressure force - internal force, then the pressure force alone (no contact, no damping)
   StepConst sc = c->sc;
   sc.contact = 0;
-  launch_elements(b, sc, c->eg, c->elem_blocks, c->stream);
-  launch_gather_correct(b, sc, 0, false, c->d_fa, nullptr, c->stream);
+  DevBuf bf = b;
+  if (fp64 && ctx32) {
+    sc.fp32 = 0;
+    bf.qe = c->qe64;
+  }
+  launch_elements(bf, sc, c->eg, c->elem_blocks, c->stream);
+  launch_gather_correct(bf, sc, 0, false, c->d_fa, nullptr, c->stream);
+  if (correct) {
+    // the context's own FP32 force at the same state, and the defect the steps add to it
+    StepConst s32 = c->sc;
+    s32.contact = 0;
+    launch_elements(b, s32, c->eg, c->elem_blocks, c->stream);
+    launch_gather_correct(b, s32, 0, false, c->f32, nullptr, c->stream);
+    launch_defect(c->d_fa, c->f32, nd, c->b.fcorr, c->stream);
+  }
+  if ((flags & SHL_RESIDUAL_CLEAR) && c->b.fcorr)
+    SHL_CUDA_TRY(cudaMemsetAsync(c->b.fcorr, 0, nd * sizeof(double), c->stream));
   sc.internal_scale = 0.0;
-  launch_elements(b, sc, c->eg, c->elem_blocks, c->stream);
-  launch_gather_correct(b, sc, 0, false, c->d_fa + nd, nullptr, c->stream);
+  launch_elements(bf, sc, c->eg, c->elem_blocks, c->stream);
+  launch_gather_correct(bf, sc, 0, false, c->d_fa + nd, nullptr, c->stream);
   launch_shell_norms(c->d_fa, c->d_fa + nd, c->d_node_off, ns, c->d_norms, c->stream);
   SHL_TRY(check_launch("shl_residual"));
   std::vector<double> norms(2 * (size_t)ns);

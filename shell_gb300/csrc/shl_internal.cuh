@@ -123,6 +123,7 @@ struct StepConst {
 struct DevBuf {
   double *X, *u, *v, *a, *up, *vp, *p, *Minv, *C;
   double* M;          // 3V lumped masses (1 / Minv), for the kinetic energy
+  double* fcorr;      // 3V defect correction added to the FP32 force in a step, or null
   double* face;       // FF_COUNT * F
   double* pscale;     // F (internal order): factor on the step's pressure (per shell)
   int32_t* patch;     // 12 * F
@@ -179,6 +180,7 @@ cudaError_t launch_force_noalloc(const DevBuf& ctx_b, const StepConst& sc, const
                                  const double* u, double pressure, double* f_out, cudaStream_t s);
 void launch_shell_norms(const double* f, const double* fext, const uint32_t* node_off, uint32_t n_shells, double* out,
                         cudaStream_t s);
+void launch_defect(const double* f64, const double* f32, size_t n, double* out, cudaStream_t s);
 void launch_flush(void* buf, size_t bytes, uint32_t tag, cudaStream_t s);
 
 // ---- launchers (shl_contact.cu) ----

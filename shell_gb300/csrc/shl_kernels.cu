@@ -19,6 +19,7 @@
 // with the CPU path at the same state.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdint>
 
 #include "shl_geom.h"
@@ -774,6 +775,12 @@ __global__ void __launch_bounds__(kBlock) k_gather_correct(DevBuf b, StepConst s
         f[2] -= q[2];
       }
     }
+    if (mode == 1 && b.fcorr) {
+      // FP64 defect of the FP32 force, refreshed at each residual check (shl_residual)
+      f[0] += b.fcorr[3 * (size_t)n];
+      f[1] += b.fcorr[3 * (size_t)n + 1];
+      f[2] += b.fcorr[3 * (size_t)n + 2];
+    }
     double d[3];
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
@@ -891,6 +898,15 @@ __global__ void __launch_bounds__(kBlock) k_shell_norms(const double* f, const d
     out[2 * blockIdx.x] = a;
     out[2 * blockIdx.x + 1] = e;
   }
+}
+
+__global__ void k_defect(const double* f64, const double* f32, size_t n, double* out) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    out[i] = f64[i] - f32[i];
+}
+
+void launch_defect(const double* f64, const double* f32, size_t n, double* out, cudaStream_t s) {
+  k_defect<<<(unsigned)std::min<size_t>((n + 255) / 256, 4096), 256, 0, s>>>(f64, f32, n, out);
 }
 
 void launch_shell_norms(const double* f, const double* fext, const uint32_t* node_off, uint32_t n_shells, double* out,

@@ -65,6 +65,7 @@ class ShlStepReport(ctypes.Structure):
 
 
 _lib = None
+RESIDUAL_FP64, RESIDUAL_CORRECT, RESIDUAL_CLEAR = 1, 2, 4
 
 
 def load():
@@ -128,7 +129,7 @@ def load():
         "shl_mlp_predict": (_i32, [vp, vp, _u32, vp]),
         "shl_mlp_gradients": (_i32, [vp, vp, vp, _u32, ctypes.POINTER(_d), vp, vp]),
         "shl_gemm_bf16": (_i32, [vp, vp, _u32, _u32, _u32, vp]),
-        "shl_residual": (_i32, [vp, _d, vp, vp, vp]),
+        "shl_residual": (_i32, [vp, _d, ctypes.c_int, vp, vp, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -382,11 +383,12 @@ class Shell:
 
     n_shells = 1  # a Batch sets its own count
 
-    def residual(self, pressure):
-        """Relative residual ||f_ext - f_int|| / ||f_ext|| of the stored state, per shell."""
+    def residual(self, pressure, flags=0):
+        """Relative residual ||f_ext - f_int|| / ||f_ext|| of the stored state, per shell
+        (flags: RESIDUAL_FP64, RESIDUAL_CORRECT, RESIDUAL_CLEAR)."""
         n = self.n_shells
         rel, f2, e2 = np.zeros(n), np.zeros(n), np.zeros(n)
-        _check(self.lib.shl_residual(self.h, pressure, rel.ctypes.data, f2.ctypes.data, e2.ctypes.data),
+        _check(self.lib.shl_residual(self.h, pressure, flags, rel.ctypes.data, f2.ctypes.data, e2.ctypes.data),
                "shl_residual", False)
         return rel
 

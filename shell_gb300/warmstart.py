@@ -28,8 +28,8 @@ from . import lib as L
 LEVEL = 5
 DIMS = [8, 512, 512, 512, 512, 3 * 10242]
 IMPERFECTION = 0.3        # amplitude of the imperfection in units of h
-DAMPING = 2.0             # mass-proportional damping of the relaxation
-DT = 1e-3                 # relaxation time step
+DAMPING = 1.5             # mass-proportional damping of the relaxation
+DT = 2e-3                 # relaxation time step
 CHECK_EVERY = 50          # steps between residual checks
 
 
@@ -87,17 +87,21 @@ def build_batch(pr, precision=L.PREC_FP32, level=LEVEL, dt=DT, damping=DAMPING):
     return L.Batch(meshes, params, np.array(scale)), np.asarray(pr["h"], float)
 
 
-def relax(batch, u_start, tol=1e-6, check_every=CHECK_EVERY, max_steps=40000, active_until_all=True):
+def relax(batch, u_start, tol=1e-6, check_every=CHECK_EVERY, max_steps=40000, correct=True):
     """Explicit relaxation under the constant pressure (table value -1 times
-    each shell's scale) from u_start (v = 0).  Returns a dict with the steps
-    at which each shell's residual first fell below tol (-1 if never), the
-    final residuals, the displacement at convergence and the wall time."""
+    each shell's scale) from u_start (v = 0).  The residual is evaluated with
+    FP64 forces; in an FP32 batch each check also refreshes the FP64 defect
+    that the FP32 steps add (correct=True), without which FP32 relaxation
+    stalls at the FP32 force error.  Returns a dict with the steps at which
+    each shell's residual first fell below tol (-1 if never), the final
+    residuals, the displacement at convergence and the wall time."""
     n = batch.n_shells
+    flags = L.RESIDUAL_FP64 | (L.RESIDUAL_CORRECT if correct else L.RESIDUAL_CLEAR)
     t0 = time.perf_counter()
     batch.apply_initial_conditions(u_start, 0.0, -1.0)
     conv_step = np.full(n, -1, dtype=np.int64)
     u_conv = [None] * n
-    rel = batch.residual(-1.0)
+    rel = batch.residual(-1.0, flags)
     steps = 0
     table = np.full(check_every, -1.0)
     hist = [rel.copy()]
@@ -110,7 +114,7 @@ def relax(batch, u_start, tol=1e-6, check_every=CHECK_EVERY, max_steps=40000, ac
     while steps < max_steps and np.any(conv_step < 0):
         _, status = batch.step(check_every, table)
         steps += check_every
-        rel = batch.residual(-1.0)
+        rel = batch.residual(-1.0, flags)
         hist.append(rel.copy())
         new = np.nonzero((rel < tol) & (conv_step < 0))[0]
         if len(new):
@@ -136,7 +140,7 @@ def standardizer(F):
     return mu.astype(np.float32), sd.astype(np.float32)
 
 
-def generate(problems, batch_size=512, precision=L.PREC_FP32, tol=1e-6, max_steps=40000, log=None):
+def generate(problems, batch_size=512, precision=L.PREC_FP32, tol=1e-6, max_steps=40000, log=None, level=LEVEL):
     """Equilibria of the problems by plain relaxation from zero, in batches.
     Returns (u_eq as n x 3V float64, conv_step, final residual, stats)."""
     n = len(problems["h"])
@@ -145,7 +149,7 @@ def generate(problems, batch_size=512, precision=L.PREC_FP32, tol=1e-6, max_step
     for s in range(0, n, batch_size):
         idx = np.arange(s, min(n, s + batch_size))
         t0 = time.perf_counter()
-        b, _ = build_batch(subset(problems, idx), precision=precision)
+        b, _ = build_batch(subset(problems, idx), precision=precision, level=level)
         stats["setup_s"] += time.perf_counter() - t0
         r = relax(b, np.zeros(3 * b.V), tol=tol, max_steps=max_steps)
         stats["wall_s"] += r["wall_s"]
@@ -159,12 +163,13 @@ def generate(problems, batch_size=512, precision=L.PREC_FP32, tol=1e-6, max_step
     return np.array(U), np.concatenate(steps), np.concatenate(rels), stats
 
 
-def train_surrogate(F_train, U_train, h_train, iters=4000, batch=256, seed=0, lr0=1e-3, lr_final=1e-5):
+def train_surrogate(F_train, U_train, h_train, iters=4000, batch=256, seed=0, lr0=1e-3, lr_final=1e-5, hidden=None):
     """Trains the network on standardised inputs and targets u / h; returns (net, scaler, loss curve)."""
     mu, sd = standardizer(F_train)
     Xn = (F_train - mu) / sd
     Tn = (U_train / h_train[:, None]).astype(np.float32)
-    net = L.MLP(DIMS, max_batch=batch, seed=seed)
+    dims = DIMS if hidden is None else [DIMS[0]] + list(hidden) + [U_train.shape[1]]
+    net = L.MLP(dims, max_batch=batch, seed=seed)
     net.set_dataset(Xn, Tn)
     curve = net.train(iters, batch, lr0=lr0, lr_final=lr_final, seed=seed, curve_every=max(1, iters // 50))
     return net, (mu, sd), curve
@@ -177,7 +182,7 @@ def predict(net, scaler, F, h):
 
 
 def experiment(n_train=3584, n_test=512, seed=0, batch_size=512, train_iters=4000, tol=1e-6, max_steps=40000,
-               fp64_check=True, log=print):
+               fp64_check=True, log=print, level=LEVEL, hidden=None, train_batch=256):
     """The whole warm-start study: equilibria of n_train + n_test seeded
     problems by plain FP32 relaxation, the network trained on the first
     n_train, then the n_test held-out problems relaxed from zero and from the
@@ -188,20 +193,21 @@ def experiment(n_train=3584, n_test=512, seed=0, batch_size=512, train_iters=400
     pr = sample_problems(n_train + n_test, seed)
     F = features(pr)
     t0 = time.perf_counter()
-    U, steps, rels, st = generate(subset(pr, np.arange(n_train)), batch_size, tol=tol, max_steps=max_steps, log=log)
+    U, steps, rels, st = generate(subset(pr, np.arange(n_train)), batch_size, tol=tol, max_steps=max_steps, log=log,
+                                  level=level)
     ok = steps >= 0
     out["generation"] = {"problems": n_train, "converged": int(ok.sum()), "wall_s": st["wall_s"],
                          "setup_s": st["setup_s"], "face_steps_per_s": st["face_steps"] / st["wall_s"],
                          "median_steps": float(np.median(steps[ok])) if ok.any() else None}
     t1 = time.perf_counter()
-    net, scaler, curve = train_surrogate(F[:n_train][ok], U[ok], pr["h"][:n_train][ok], iters=train_iters, seed=seed)
+    net, scaler, curve = train_surrogate(F[:n_train][ok], U[ok], pr["h"][:n_train][ok], iters=train_iters, seed=seed,
+                                         hidden=hidden, batch=train_batch)
     out["training"] = {"samples": int(ok.sum()), "iters": train_iters, "wall_s": time.perf_counter() - t1,
                        "loss_first": float(curve[0]), "loss_last": float(curve[-1])}
     test = subset(pr, np.arange(n_train, n_train + n_test))
     Ft, ht = F[n_train:], test["h"]
     # plain start
-    b, _ = build_batch(test)
-    V1 = b.V // n_test
+    b, _ = build_batch(test, level=level)
     plain = relax(b, np.zeros(3 * b.V), tol=tol, max_steps=max_steps)
     F_faces = b.F
     b.close()
@@ -209,7 +215,7 @@ def experiment(n_train=3584, n_test=512, seed=0, batch_size=512, train_iters=400
     tp = time.perf_counter()
     U_pred = predict(net, scaler, Ft, ht)
     pred_s = time.perf_counter() - tp
-    b, _ = build_batch(test)
+    b, _ = build_batch(test, level=level)
     warm = relax(b, U_pred.reshape(-1), tol=tol, max_steps=max_steps)
     b.close()
     # fallback: shells whose warm start did not converge restart from zero (the plain result)
@@ -228,7 +234,7 @@ def experiment(n_train=3584, n_test=512, seed=0, batch_size=512, train_iters=400
                                                           for k in range(n_test)])),
     }
     if fp64_check:
-        b, _ = build_batch(test, precision=L.PREC_FP64)
+        b, _ = build_batch(test, precision=L.PREC_FP64, level=level)
         ref = relax(b, np.zeros(3 * b.V), tol=tol, max_steps=max_steps)
         b.close()
         okr = ref["conv_step"] >= 0

@@ -59,3 +59,41 @@ def test_residual_batch_per_shell(cuda_ok):
     for k, ((X, T), p) in enumerate(zip(meshes, ps)):
         ro, _, _ = _oracle_residual(X, T, p, us[k], pres * scale[k])
         assert abs(r[k] - ro) <= 1e-10 * ro, k
+
+
+def test_residual_fp64_in_fp32_context_and_defect_correction(cuda_ok):
+    """An FP32 batch evaluates its residual with FP64 forces on request (the
+    same value as an FP64 batch at the same state); with the defect correction
+    its relaxation reaches the FP64 residual tolerance and the FP64
+    equilibrium, which plain FP32 relaxation cannot."""
+    meshes = [L.icosphere(3), L.icosphere(3)]
+    ps32 = [physics_params(contact=False, damping_alpha=1.5, dt=2e-3, precision=L.PREC_FP32, thickness=h)
+            for h in (0.01, 0.02)]
+    ps64 = [physics_params(contact=False, damping_alpha=1.5, dt=2e-3, thickness=h) for h in (0.01, 0.02)]
+    scale = np.array([0.5 * classical_pressure(h=0.01), 0.5 * classical_pressure(h=0.02)])
+    rng = np.random.default_rng(6)
+    u = 1e-3 * rng.standard_normal(2 * meshes[0][0].size)
+    b32, b64 = L.Batch(meshes, ps32, scale), L.Batch(meshes, ps64, scale)
+    for b in (b32, b64):
+        b.set_state(u, np.zeros_like(u), np.zeros_like(u))
+    r64 = b64.residual(-1.0)
+    r32_64 = b32.residual(-1.0, L.RESIDUAL_FP64)
+    assert np.allclose(r32_64, r64, rtol=1e-13, atol=0)
+    r32 = b32.residual(-1.0)
+    assert np.all(np.abs(r32 - r64) <= 1e-3 * r64)
+
+    def relax(b, flags, n_checks=120, every=100):
+        b.apply_initial_conditions(np.zeros_like(u), 0.0, -1.0)
+        r = b.residual(-1.0, flags)
+        for _ in range(n_checks):
+            if np.all(r < 1e-6):
+                break
+            b.step(every, np.full(every, -1.0))
+            r = b.residual(-1.0, flags)
+        return r, b.get_state()[0]
+
+    r_ref, u_ref = relax(b64, 0)
+    assert np.all(r_ref < 1e-6)
+    r_c, u_c = relax(b32, L.RESIDUAL_FP64 | L.RESIDUAL_CORRECT)
+    assert np.all(r_c < 1e-6)
+    assert np.abs(u_c - u_ref).max() < 1e-4 * np.abs(u_ref).max()
