@@ -349,6 +349,10 @@ def run_ours(args, rank, world, dist):
 
     ensemble = time_ensemble(L, torch, max(20, K // 4), W, flush) if args.ensemble else None
     accuracy = fp32_accuracy(L) if args.accuracy else None
+    warmstart = None
+    if args.warmstart:
+        from shell_gb300 import warmstart as WS
+        warmstart = WS.experiment(n_train=args.ws_train, n_test=args.ws_test, log=lambda m: print(m, file=sys.stderr))
 
     # warm continuous throughput (informative): K steps back to back, one graph replay per 16 steps
     g.upload_pressure_table(pressure(np.arange(1 + W + K, 1 + W + 2 * K)))
@@ -408,6 +412,7 @@ def run_ours(args, rank, world, dist):
         "fp32_value": fp32_value,
         "ensemble": ensemble,
         "fp32_accuracy": accuracy,
+        "warmstart": warmstart,
         "e2e": {"value": e2e, "unit": "face-steps/s", "h2d_bytes_per_step": 3 * 3 * V * 8,
                 "d2h_bytes_per_step": 3 * 3 * V * 8,
                 "how": "per step: shl_set_state from pinned host, shl_step(1), shl_get_state"},
@@ -437,6 +442,10 @@ def main():
     ap.add_argument("--fp32", type=int, default=1, help="also time the FP32 element-force mode")
     ap.add_argument("--ensemble", type=int, default=1, help="also time the 256-shell batched ensemble")
     ap.add_argument("--accuracy", type=int, default=1, help="also report the level-7 FP32-vs-FP64 accuracy")
+    ap.add_argument("--warmstart", type=int, default=0,
+                    help="also run the learned warm-start study (level-5 shells; minutes of GPU time)")
+    ap.add_argument("--ws-train", type=int, default=3584)
+    ap.add_argument("--ws-test", type=int, default=512)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     world = int(os.environ.get("WORLD_SIZE", "1"))

@@ -107,6 +107,15 @@ typedef struct shl_params {
    * (ShellSystem.C:289, 2952) */
   int32_t stop_on_problem;
   int32_t pad1;
+  /* adaptive time stepping (ShellSystem.C:291-313, 1010-1044, 1104-1117):
+   * every adapt_dt_every-th step estimates the local error and retries the
+   * step with a smaller dt when it is too large; 0 = fixed dt */
+  uint32_t adapt_dt_every;
+  int32_t pad2;
+  double dt_min;            /* 0 = machine epsilon */
+  double dt_max;            /* 0 = unbounded */
+  double rel_loc_err_min;
+  double rel_loc_err_max;
 } shl_params;
 
 /* Scalars measured in a step (ShellSystem.C:2686-2846). */
@@ -127,11 +136,13 @@ typedef struct shl_step_report {
   double time;             /* simulation time after the last step */
   double du_sum;           /* linked-cell displacement budget (ShellSystem.C:2634) */
   uint32_t n_rebuilds;     /* candidate-list rebuilds performed */
-  uint32_t pad;
+  uint32_t rejections;     /* repeated attempts (adaptive dt, ShellSystem.C:1104-1117) */
   shl_energies last;       /* measurements of the last step */
   /* dt-weighted sums over the steps (the MovingAverage inputs, ShellSystem.C:2830-2843) */
   double sum_dt, sum_area, sum_volume, sum_Nc, sum_Ekin, sum_Etens, sum_Ebend,
       sum_Eself, sum_Efric, sum_kGauss, sum_kMean;
+  uint32_t stopped;        /* the stopping criterion became true (shl_set_stop_function) */
+  uint32_t pad;
 } shl_step_report;
 
 typedef struct shl_ctx shl_ctx;
@@ -188,7 +199,9 @@ shl_status shl_get_time(shl_ctx* ctx, double* time, uint32_t* time_step);
 shl_status shl_eval_forces(shl_ctx* ctx, const double* u_pred, const double* v_pred,
                            double pressure, double* f_out, double* a_out, shl_energies* e);
 
-/* n_steps calls of ShellSystem::advance with fixed dt (ShellSystem.C:952-1122).
+/* n_steps calls of ShellSystem::advance (ShellSystem.C:952-1122); with
+ * adapt_dt_every > 0 each call may repeat its step with a smaller dt, and the
+ * table entry of a step is used for all of its attempts.
  * pressure_table: pressure for each step (evaluated by the host at the step's
  * time t + dt), or NULL to use params.pressure.  The steps run on the
  * device without host synchronisation (captured in a CUDA graph when
@@ -257,7 +270,10 @@ shl_status shl_get_mass_damping(shl_ctx* ctx, double* Minv, double* C);
  * shell, n_shells for a batch): ||f_ext - f_int||_2 / ||f_ext||_2 with
  * f_ext the pressure force at `pressure` (times each shell's pressure scale)
  * and f_int the internal force, at u (no damping, no inertia; self-contact
- * forces are not included).  f2 / fext2 (may be NULL) get the squared norms.
+ * forces are not included), each vector without its rigid-translation part
+ * (the resultant spread by nodal mass): the discrete pressure load of a
+ * closed shell has a small resultant that moves a free shell at constant
+ * speed instead of deforming it.  f2 / fext2 (may be NULL) get the squared norms.
  * flags: SHL_RESIDUAL_FP64 evaluates the forces in FP64 also in an FP32
  * context; SHL_RESIDUAL_CORRECT (FP32 context, with FP64) also stores the
  * defect f64 - f32 at this state, which the following steps add to their FP32
@@ -266,6 +282,23 @@ shl_status shl_get_mass_damping(shl_ctx* ctx, double* Minv, double* C);
  * No counterpart in the reference, which has no residual stop. */
 enum { SHL_RESIDUAL_FP64 = 1, SHL_RESIDUAL_CORRECT = 2, SHL_RESIDUAL_CLEAR = 4 };
 shl_status shl_residual(shl_ctx* ctx, double pressure, int flags, double* rel, double* f2, double* fext2);
+
+/* The pressure as a config expression of t (the muparser language of the
+ * config file: operators, functions, pi; d reads 0): compiled on the host and
+ * evaluated by the device at each step's time t + dt, in place of the
+ * per-step table (ShellSystem.C:934-936).  NULL or "" returns to the table.
+ * shl_eval_pressure_function evaluates the compiled program at n times (a
+ * check of the device evaluation). */
+shl_status shl_set_pressure_function(shl_ctx* ctx, const char* expr);
+shl_status shl_eval_pressure_function(shl_ctx* ctx, const double* t, uint32_t n, double* out);
+
+/* The current time step (adaptive dt: the next attempt's) and the repeated
+ * attempts since the last report. */
+shl_status shl_get_dt(shl_ctx* ctx, double* dt, uint32_t* rejections);
+/* Stopping criterion as a config expression of t (shell.C:314-318), tested on
+ * the device after every step; shl_step returns early with report->stopped
+ * set once it is nonzero.  NULL or "" removes it. */
+shl_status shl_set_stop_function(shl_ctx* ctx, const char* expr);
 
 /* Measurements of the last force evaluation or step (the scalars of
  * measure_properties, ShellSystem.C:2714-2846). */

@@ -56,6 +56,9 @@ def load():
         "oracle_get_element_fields": (ctypes.c_int, [vp, vp, vp, vp, vp, vp]),
         "oracle_get_cell_info": (ctypes.c_int, [vp, vp]),
         "oracle_get_node_fields": (ctypes.c_int, [vp, vp, vp, vp]),
+        "oracle_set_pressure_function": (ctypes.c_int, [vp, ctypes.c_char_p]),
+        "oracle_get_dt": (d, [vp]),
+        "oracle_get_rejections": (ctypes.c_uint64, [vp]),
         "oracle_patch": (ctypes.c_int, [vp, u32, vp, ctypes.POINTER(u32)]),
         "oracle_basis_at": (ctypes.c_int, [vp, u32, d, d, vp]),
         "oracle_basis_cached": (ctypes.c_int, [vp, u32, vp, vp]),
@@ -181,6 +184,16 @@ class Oracle:
         out = [np.zeros(self.F) for _ in range(5)]
         self.lib.oracle_get_element_fields(self.h, *[o.ctypes.data for o in out])
         return dict(zip(("kGauss", "kMean", "etens", "ebend", "area"), out))
+
+    def set_pressure_function(self, expr):
+        if self.lib.oracle_set_pressure_function(self.h, None if expr is None else expr.encode()) != 0:
+            raise RuntimeError(self.lib.oracle_error().decode())
+
+    def dt(self):
+        return self.lib.oracle_get_dt(self.h)
+
+    def rejections(self):
+        return int(self.lib.oracle_get_rejections(self.h))
 
     def node_fields(self):
         out = [np.zeros(self.V) for _ in range(3)]

@@ -44,6 +44,11 @@ int oracle_set_contact_state(oracle* o, const uint32_t* pairs, const uint8_t* st
                              const double* origin, const double* d2, size_t n, double du_sum);
 int oracle_rebuild_contacts(oracle* o);
 int oracle_get_mass_damping(oracle* o, double* Minv, double* C);
+/* Pressure as a config expression of t (evaluated each attempt); NULL or "" = table. */
+int oracle_set_pressure_function(oracle* o, const char* expr);
+/* Current time step size (adaptive dt) and the number of repeated steps so far. */
+double oracle_get_dt(oracle* o);
+uint64_t oracle_get_rejections(oracle* o);
 /* node_vectors ekin, eself, efric of the last step (ShellSystem.C:126-130). */
 int oracle_get_node_fields(oracle* o, double* ekin, double* eself, double* efric);
 int oracle_get_element_fields(oracle* o, double* kGauss, double* kMean, double* etens,

@@ -57,6 +57,7 @@
 #include <omp.h>
 #endif
 
+#include "../shell_gb300/csrc/shl_expr.h"
 #include "../shell_gb300/csrc/shl_geom.h"
 
 namespace {
@@ -344,6 +345,13 @@ struct oracle {
   void compute_mass_damping();
   void build_topological_neighborhood();
   void set_newmark_parameters(Real new_dt);
+  template <class PressureAt>
+  bool advance(const PressureAt& p_at);
+  Real dt_step = 0;       // dt of the last accepted step
+  bool accepted = false;  // the last advance() accepted a step
+  uint64_t rejections = 0;
+  shl::expr::Expression pfun;  // pressure as an expression of t, when set
+  bool has_pfun = false;
 
   /* ------------------------------ step ---------------------------------- */
   void compute_position();
@@ -381,7 +389,6 @@ struct oracle {
     const Point& p2 = p[tri[3 * c.eid[0] + 2]];
     return (1 - c.v[0] - c.w[0]) * p0 + c.v[0] * p1 + c.w[0] * p2 + 0.5 * c.dc;
   }
-  bool advance();
 };
 
 bool oracle::build_patch(unsigned eid, std::vector<unsigned>& patch, int& N) {
@@ -652,9 +659,13 @@ void oracle::build_topological_neighborhood() {
   }
 }
 
-// ShellSystem::set_newmark_parameters, ShellSystem.C:744-759 (no dt bounds: fixed dt)
+// ShellSystem::set_newmark_parameters, ShellSystem.C:744-759, with the bounds of
+// ShellSystem.C:306-310 (dt_min at least the machine epsilon, dt_max 0 = none)
 void oracle::set_newmark_parameters(Real new_dt) {
-  dt = new_dt;
+  const Real dt_min = std::max(P.dt_min, std::numeric_limits<Real>::epsilon());
+  const Real dt_max = P.dt_max <= 0 ? std::numeric_limits<Real>::max() : P.dt_max;
+  dt = std::max(new_dt, dt_min);
+  dt = std::min(dt, dt_max);
   const Real beta = P.newmark_beta, gamma = P.newmark_gamma;
   newmark_a[0] = beta * dt * dt;
   newmark_a[1] = gamma / (beta * dt);
@@ -1226,40 +1237,86 @@ void oracle::measure_properties() {
   compute_enclosed_volume();
 }
 
-// one fixed-dt advance(), ShellSystem.C:952-1122
-bool oracle::advance() {
-  // predictor (972-989)
-  for (unsigned i = 0; i < 3 * V; ++i) {
-    u_pred[i] = u[i];
-    u_pred[i] = dt * v[i] + u_pred[i];
-    u_pred[i] = newmark_a[8] * a[i] + u_pred[i];
+// advance(), ShellSystem.C:952-1122: predictor, forces, and with adaptive dt
+// the local-error estimate (1010-1044) that repeats the step with a smaller dt
+// (1104-1117).  p_at(time) gives the pressure of an attempt at its time.
+// Returns true when the run must stop; dt_step is the dt of the accepted step.
+template <class PressureAt>
+bool oracle::advance(const PressureAt& p_at) {
+  const bool adapt_now = P.adapt_dt_every && time_step % P.adapt_dt_every == 0;
+  const Real target = std::sqrt(P.rel_loc_err_min * P.rel_loc_err_max);
+  accepted = false;
+  while (true) {
+    prepare_next_step(p_at(time + dt));
+    // predictor (972-989)
+    for (unsigned i = 0; i < 3 * V; ++i) {
+      u_pred[i] = u[i];
+      u_pred[i] = dt * v[i] + u_pred[i];
+      u_pred[i] = newmark_a[8] * a[i] + u_pred[i];
+    }
+    check_increment(false);
+    compute_position();
+    for (unsigned i = 0; i < 3 * V; ++i) {
+      v_pred[i] = v[i];
+      v_pred[i] = newmark_a[6] * a[i] + v_pred[i];
+    }
+    compute_shell_shell_contact_candidates(false);
+    compute_deformed_metrics();
+    compute_external_force();
+    subtract_internal_force();
+    for (unsigned i = 0; i < 3 * V; ++i) {
+      a_pred[i] = C[i] * v_pred[i];
+      f[i] -= a_pred[i];
+      a_pred[i] = Minv[i] * f[i];
+    }
+    Real new_dt = dt;
+    if (adapt_now) {
+      // Zienkiewicz-Xie local error with the thickness as reference length (1010-1044)
+      Real norm_a = 0, vmax = 0;
+      for (unsigned i = 0; i < 3 * V; ++i) {
+        norm_a = std::max(norm_a, std::fabs(a_pred[i] - a[i]));
+        vmax = std::max(vmax, std::fabs(v_pred[i]));
+      }
+      Real rel_loc_err = target;
+      if (std::isfinite(norm_a))
+        rel_loc_err = newmark_a[9] * norm_a / P.thickness;
+      else
+        register_problem(SHL_NOT_FINITE);
+      if (rel_loc_err == 0)
+        new_dt = 2 * dt;
+      else if (rel_loc_err > P.rel_loc_err_max || rel_loc_err < P.rel_loc_err_min)
+        new_dt = dt * std::pow(target / rel_loc_err, 1. / 3);
+      if (P.shell_shell_contact != SHL_CONTACT_NONE) {
+        const unsigned contact_resolution = 10;
+        if (new_dt * vmax * contact_resolution * 2 > P.thickness) new_dt = P.thickness / (2 * contact_resolution * vmax);
+      }
+    }
+    if (new_dt >= dt) {
+      // accept (1046-1101)
+      for (unsigned i = 0; i < 3 * V; ++i) u_pred[i] = newmark_a[0] * a_pred[i] + u_pred[i];
+      check_increment(true);
+      compute_position();
+      u.swap(u_pred);
+      for (unsigned i = 0; i < 3 * V; ++i) v_pred[i] = newmark_a[7] * a_pred[i] + v_pred[i];
+      v.swap(v_pred);
+      a.swap(a_pred);
+      compute_shell_shell_contact_candidates(false);
+      measure_properties();
+      dt_step = dt;
+      accepted = true;
+      set_newmark_parameters(new_dt);
+      break;
+    }
+    // repeat the step (1104-1117)
+    time -= dt;
+    set_newmark_parameters(new_dt);
+    ++rejections;
+    if (dt <= std::numeric_limits<Real>::epsilon()) {
+      register_problem(SHL_SMALL_TIMESTEP);
+      break;
+    }
   }
-  check_increment(false);
-  compute_position();
-  for (unsigned i = 0; i < 3 * V; ++i) {
-    v_pred[i] = v[i];
-    v_pred[i] = newmark_a[6] * a[i] + v_pred[i];
-  }
-  compute_shell_shell_contact_candidates(false);
-  compute_deformed_metrics();
-  compute_external_force();
-  subtract_internal_force();
-  for (unsigned i = 0; i < 3 * V; ++i) {
-    a_pred[i] = C[i] * v_pred[i];
-    f[i] -= a_pred[i];
-    a_pred[i] = Minv[i] * f[i];
-  }
-  // accept (1046-1101)
-  for (unsigned i = 0; i < 3 * V; ++i) u_pred[i] = newmark_a[0] * a_pred[i] + u_pred[i];
-  check_increment(true);
-  compute_position();
-  u.swap(u_pred);
-  for (unsigned i = 0; i < 3 * V; ++i) v_pred[i] = newmark_a[7] * a_pred[i] + v_pred[i];
-  v.swap(v_pred);
-  a.swap(a_pred);
-  compute_shell_shell_contact_candidates(false);
-  measure_properties();
-  return current_problem >= SHL_STOP_SIM;
+  return current_problem >= SHL_STOP_SIM || (P.stop_on_problem && current_problem > 0);
 }
 
 /* ------------------------------ C interface ------------------------------ */
@@ -1379,28 +1436,37 @@ int oracle_step(oracle* o, uint32_t n_steps, const double* pressure_table, shl_s
   std::memset(&rep, 0, sizeof(rep));
   int worst = 0;
   uint32_t done = 0;
+  const uint64_t rej0 = o->rejections;
   for (uint32_t s = 0; s < n_steps; ++s) {
     o->current_problem = 0;
     ++o->time_step;
-    o->prepare_next_step(pressure_table ? pressure_table[s] : o->P.pressure);
-    const bool stop = o->advance();
-    ++done;
+    // the pressure of an attempt: the expression at its time, else the step's table entry
+    const double p_tab = pressure_table ? pressure_table[s] : o->P.pressure;
+    const bool stop = o->advance([&](double t) {
+      return o->has_pfun ? o->pfun.eval({{"t", t}, {"d", 0.0}}) : p_tab;
+    });
     worst = std::max(worst, o->current_problem);
-    const Real dt = o->dt;
-    rep.sum_dt += dt;
-    rep.sum_area += dt * o->area;
-    rep.sum_volume += dt * o->volume;
-    rep.sum_Nc += dt * o->Nc;
-    rep.sum_Ekin += dt * o->Ekin;
-    rep.sum_Etens += dt * o->Etens;
-    rep.sum_Ebend += dt * o->Ebend;
-    rep.sum_Eself += dt * o->Eself;
-    rep.sum_Efric += dt * o->Efric;
-    rep.sum_kGauss += dt * o->kGauss;
-    rep.sum_kMean += dt * o->kMean;
+    if (o->accepted) {
+      ++done;
+      const Real dt = o->dt_step;
+      rep.sum_dt += dt;
+      rep.sum_area += dt * o->area;
+      rep.sum_volume += dt * o->volume;
+      rep.sum_Nc += dt * o->Nc;
+      rep.sum_Ekin += dt * o->Ekin;
+      rep.sum_Etens += dt * o->Etens;
+      rep.sum_Ebend += dt * o->Ebend;
+      rep.sum_Eself += dt * o->Eself;
+      rep.sum_Efric += dt * o->Efric;
+      rep.sum_kGauss += dt * o->kGauss;
+      rep.sum_kMean += dt * o->kMean;
+    } else {
+      --o->time_step;
+    }
     if (stop) break;
   }
   rep.steps_done = done;
+  rep.rejections = (uint32_t)(o->rejections - rej0);
   rep.worst_problem = worst;
   rep.time = o->time;
   rep.du_sum = o->du_sum;
@@ -1408,6 +1474,24 @@ int oracle_step(oracle* o, uint32_t n_steps, const double* pressure_table, shl_s
   if (r) *r = rep;
   return worst;
 }
+
+int oracle_set_pressure_function(oracle* o, const char* expr) {
+  if (!expr || !*expr) {
+    o->has_pfun = false;
+    return 0;
+  }
+  try {
+    o->pfun = shl::expr::Expression(expr);
+  } catch (const std::exception& e) {
+    g_err = e.what();
+    return -1;
+  }
+  o->has_pfun = true;
+  return 0;
+}
+
+double oracle_get_dt(oracle* o) { return o->dt; }
+uint64_t oracle_get_rejections(oracle* o) { return o->rejections; }
 
 size_t oracle_get_contact_state(oracle* o, uint32_t* pairs, uint8_t* stick, double* origin, double* d2,
                                 size_t cap, double* du_sum) {

@@ -63,6 +63,8 @@ struct shl_ctx {
   uint32_t* d_node_off = nullptr;            // device copy (shl_residual)
   double* d_norms = nullptr;                 // per-shell |f|^2, |f_ext|^2
   double* qe64 = nullptr;                    // FP64 element shares of an FP32 context (shl_residual)
+  shl::expr::Op* d_pfun = nullptr;           // compiled pressure expression (device)
+  shl::expr::Op* d_sfun = nullptr;           // compiled stopping criterion (device)
   double* f32 = nullptr;                     // FP32 force at the checked state (defect correction)
 };
 
@@ -141,6 +143,18 @@ bool validate(const shl_params& p, std::string& err) {
     if (!(p.friction_stop_velocity > 0)) { err = "friction_stop_velocity must be > 0"; return false; }
   }
   if (p.precision != SHL_PREC_FP64 && p.precision != SHL_PREC_FP32) { err = "bad precision"; return false; }
+  if (p.adapt_dt_every > 0) {
+    // ShellSystem.C:300-313
+    if (!(p.rel_loc_err_min >= 0) || !(p.rel_loc_err_max > p.rel_loc_err_min)) {
+      err = "adaptive dt needs 0 <= rel_loc_err_min < rel_loc_err_max";
+      return false;
+    }
+    if (p.newmark_beta == 1.0 / 6) { err = "adaptive dt: no error estimate for newmark_beta = 1/6"; return false; }
+    if (p.dt_min < 0 || p.dt_max < 0 || (p.dt_min > p.dt) || (p.dt_max > 0 && p.dt_max < p.dt)) {
+      err = "adaptive dt needs dt_min <= dt <= dt_max";
+      return false;
+    }
+  }
   return true;
 }
 
@@ -238,7 +252,13 @@ cudaError_t enqueue_step(shl_ctx* c, bool capturing = false) {
   if (sc.contact && (e = enqueue_rebuild(c, capturing)) != cudaSuccess) return e;
   launch_elements(b, sc, c->eg, c->elem_blocks, s);
   if (sc.contact) launch_contact_force(b, sc, 0, s);
-  launch_gather_correct(b, sc, 0, true, nullptr, nullptr, s);
+  if (sc.adapt_every) {
+    // one attempt: estimate, then correct only if accepted (ShellSystem.C:1010-1117)
+    launch_gather_correct(b, sc, 2, false, nullptr, nullptr, s);
+    launch_correct_adapt(b, sc, s);
+  } else {
+    launch_gather_correct(b, sc, 0, true, nullptr, nullptr, s);
+  }
   if (sc.contact && (e = enqueue_rebuild(c, capturing)) != cudaSuccess) return e;
   launch_volume_end_step(b, sc, true, s);
   return cudaSuccess;
@@ -263,6 +283,21 @@ shl_status build_graph(shl_ctx* c, uint32_t steps, cudaGraphExec_t* out) {
     c->conditional_ok = false;  // retry with early-exit launches instead of IF nodes
   }
   return SHL_ERR_CUDA;
+}
+
+// newmark_a of dt (ShellSystem.C:744-759) into the control block
+void set_newmark_host(Ctl& h, double dt, double beta, double gamma) {
+  h.dt_cur = dt;
+  h.nm[0] = beta * dt * dt;
+  h.nm[1] = gamma / (beta * dt);
+  h.nm[2] = 1 / (beta * dt);
+  h.nm[3] = 1 / (2 * beta) - 1;
+  h.nm[4] = gamma / beta - 1;
+  h.nm[5] = dt * (gamma / (2 * beta) - 1);
+  h.nm[6] = (1 - gamma) * dt;
+  h.nm[7] = gamma * dt;
+  h.nm[8] = dt * dt * (0.5 - beta);
+  h.nm[9] = dt * dt * std::fabs(beta - 1. / 6);
 }
 
 void fill_energies(const Ctl& h, shl_energies* e) {
@@ -314,6 +349,7 @@ shl_status create_common(shl_ctx* c, const std::vector<double>& pscale_orig, shl
 #define ALLOC(ptr, n) do { if ((st = dev_alloc(c, &(ptr), (n))) != SHL_OK) return fail(st); } while (0)
   ALLOC(b.X, nd); ALLOC(b.u, nd); ALLOC(b.v, nd); ALLOC(b.a, nd); ALLOC(b.up, nd); ALLOC(b.vp, nd);
   ALLOC(b.p, nd); ALLOC(b.Minv, nd); ALLOC(b.C, nd); ALLOC(b.M, nd);
+  if (params->adapt_dt_every) ALLOC(b.ap, nd);
   ALLOC(b.face, (size_t)FF_COUNT * F);
   ALLOC(b.patch, 12 * (size_t)F);
   const bool fp32 = params->precision == SHL_PREC_FP32;
@@ -469,9 +505,19 @@ shl_status create_common(shl_ctx* c, const std::vector<double>& pscale_orig, shl
   sc.V = V;
   sc.F = F;
   sc.internal_scale = 1.0;
+  sc.adapt_every = p.adapt_dt_every;
+  sc.beta = p.newmark_beta;
+  sc.gamma = p.newmark_gamma;
+  sc.err_min = p.rel_loc_err_min;
+  sc.err_max = p.rel_loc_err_max;
+  sc.err_target = std::sqrt(p.rel_loc_err_min * p.rel_loc_err_max);
+  sc.dt_min_eff = std::max(p.dt_min, 2.220446049250313e-16);
+  sc.dt_max_eff = p.dt_max <= 0 ? SHL_DBL_MAX : p.dt_max;
 
   Ctl h;
   std::memset(&h, 0, sizeof(h));
+  set_newmark_host(h, p.dt, p.newmark_beta, p.newmark_gamma);
+  h.steps_target = ~0u;
   if ((st = ctl_put(c, h)) != SHL_OK) return fail(st);
   if (cudaMallocHost(&c->h_pin, 3 * nd * sizeof(double)) != cudaSuccess) c->h_pin = nullptr;
   if ((st = check_launch("shl_create")) != SHL_OK) return fail(st);
@@ -732,6 +778,9 @@ shl_status reset_report(shl_ctx* c) {
   h.error = 0;
   h.problem = 0;
   h.n_rebuilds = 0;
+  h.rejections = 0;
+  h.paused = 0;
+  h.steps_target = ~0u;
   h.sum_dt = h.sum_area = h.sum_volume = h.sum_Nc = h.sum_Ekin = h.sum_Etens = h.sum_Ebend = h.sum_Eself =
       h.sum_Efric = h.sum_kGauss = h.sum_kMean = 0;
   return ctl_put(c, h);
@@ -776,6 +825,8 @@ shl_status collect(shl_ctx* c, shl_step_report* report) {
     report->time = h.time;
     report->du_sum = h.du_sum;
     report->n_rebuilds = h.n_rebuilds;
+    report->rejections = h.rejections;
+    report->stopped = (h.paused & 2u) ? 1u : 0u;
     fill_energies(h, &report->last);
     report->sum_dt = h.sum_dt; report->sum_area = h.sum_area; report->sum_volume = h.sum_volume;
     report->sum_Nc = h.sum_Nc; report->sum_Ekin = h.sum_Ekin; report->sum_Etens = h.sum_Etens;
@@ -800,21 +851,74 @@ shl_status shl_step(shl_ctx* c, uint32_t n_steps, const double* pressure_table, 
   SHL_TRY(reset_report(c));
   std::vector<double> chunk;
   uint32_t done = 0;
-  while (done < n_steps) {
+  bool stop = false;
+  while (done < n_steps && !stop) {
     const uint32_t m = std::min<uint32_t>(n_steps - done, c->b.ptable_cap);
     chunk.resize(m);
     for (uint32_t i = 0; i < m; ++i) chunk[i] = pressure_table ? pressure_table[done + i] : c->P.pressure;
     SHL_TRY(upload_table(c, chunk.data(), m));
-    SHL_TRY(enqueue_steps(c, m, use_graph != 0));
-    SHL_CUDA_TRY(cudaStreamSynchronize(c->stream));
-    done += m;
-    if (done < n_steps) {
-      Ctl hh;
+    Ctl hh;
+    SHL_TRY(ctl_get(c, hh));
+    const uint32_t target = hh.steps_done + m;
+    hh.steps_target = target;
+    hh.paused = 0;
+    SHL_TRY(ctl_put(c, hh));
+    // one slot per attempt: with adaptive dt, repeated attempts leave steps to top up
+    uint32_t attempts = m;
+    for (int round = 0;; ++round) {
+      SHL_TRY(enqueue_steps(c, attempts, use_graph != 0));
+      SHL_CUDA_TRY(cudaStreamSynchronize(c->stream));
       SHL_TRY(ctl_get(c, hh));
-      if (hh.halted) break;
+      if (hh.halted || (hh.paused & 2u) || hh.steps_done >= target) break;
+      if (round >= 100000) {
+        g_err = "shl_step: steps were repeated without end (adaptive dt)";
+        return SHL_ERR_TIMEOUT;
+      }
+      attempts = target - hh.steps_done;
     }
+    done += m;
+    if (hh.halted) break;
+    if (hh.paused & 2u) stop = true;
   }
   return collect(c, report);
+}
+
+shl_status shl_get_dt(shl_ctx* c, double* dt, uint32_t* rejections) {
+  if (!c) return SHL_ERR_ARG;
+  Ctl h;
+  SHL_TRY(ctl_get(c, h));
+  if (dt) *dt = c->sc.adapt_every ? h.dt_cur : c->P.dt;
+  if (rejections) *rejections = h.rejections;
+  return SHL_OK;
+}
+
+shl_status shl_set_stop_function(shl_ctx* c, const char* expr) {
+  if (!c) return SHL_ERR_ARG;
+  if (!expr || !*expr) {
+    c->sc.sfun = nullptr;
+    c->sc.sfun_len = 0;
+  } else {
+    std::vector<shl::expr::Op> prog;
+    try {
+      shl::expr::Expression e(expr);
+      if (e.size() != 1) throw std::runtime_error("one expression expected");
+      if (e.uses("x") || e.uses("y") || e.uses("z")) throw std::runtime_error("the criterion may depend on t and d only");
+      prog = e.compile();
+    } catch (const std::exception& ex) {
+      g_err = ex.what();
+      return SHL_ERR_ARG;
+    }
+    if (!c->d_sfun) SHL_TRY(dev_alloc(c, &c->d_sfun, shl::expr::kMaxProgram));
+    SHL_CUDA_TRY(cudaMemcpyAsync(c->d_sfun, prog.data(), prog.size() * sizeof(shl::expr::Op), cudaMemcpyHostToDevice,
+                                 c->stream));
+    SHL_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    c->sc.sfun = c->d_sfun;
+    c->sc.sfun_len = (int32_t)prog.size();
+  }
+  if (c->graph) cudaGraphExecDestroy(c->graph);
+  if (c->graph1) cudaGraphExecDestroy(c->graph1);
+  c->graph = c->graph1 = nullptr;
+  return SHL_OK;
 }
 
 shl_status shl_get_stream(shl_ctx* c, void** stream) {
@@ -1118,7 +1222,7 @@ shl_status shl_residual(shl_ctx* c, double pressure, int flags, double* rel, dou
   sc.internal_scale = 0.0;
   launch_elements(bf, sc, c->eg, c->elem_blocks, c->stream);
   launch_gather_correct(bf, sc, 0, false, c->d_fa + nd, nullptr, c->stream);
-  launch_shell_norms(c->d_fa, c->d_fa + nd, c->d_node_off, ns, c->d_norms, c->stream);
+  launch_shell_norms(c->d_fa, c->d_fa + nd, c->b.M, c->d_node_off, ns, c->d_norms, c->stream);
   SHL_TRY(check_launch("shl_residual"));
   std::vector<double> norms(2 * (size_t)ns);
   SHL_CUDA_TRY(cudaMemcpyAsync(norms.data(), c->d_norms, norms.size() * sizeof(double), cudaMemcpyDeviceToHost,
@@ -1137,6 +1241,53 @@ shl_status shl_residual(shl_ctx* c, double pressure, int flags, double* rel, dou
     if (rel) rel[k] = norms[2 * k + 1] > 0 ? std::sqrt(norms[2 * k] / norms[2 * k + 1]) : INFINITY;
   }
   return SHL_OK;
+}
+
+shl_status shl_set_pressure_function(shl_ctx* c, const char* expr) {
+  if (!c) return SHL_ERR_ARG;
+  if (!expr || !*expr) {
+    c->sc.pfun = nullptr;
+    c->sc.pfun_len = 0;
+  } else {
+    std::vector<shl::expr::Op> prog;
+    try {
+      shl::expr::Expression e(expr);
+      if (e.size() != 1) throw std::runtime_error("one expression expected");
+      if (e.uses("x") || e.uses("y") || e.uses("z")) throw std::runtime_error("the pressure may depend on t and d only");
+      prog = e.compile();
+    } catch (const std::exception& ex) {
+      g_err = ex.what();
+      return SHL_ERR_ARG;
+    }
+    if (!c->d_pfun) SHL_TRY(dev_alloc(c, &c->d_pfun, shl::expr::kMaxProgram));
+    SHL_CUDA_TRY(cudaMemcpyAsync(c->d_pfun, prog.data(), prog.size() * sizeof(shl::expr::Op), cudaMemcpyHostToDevice,
+                                 c->stream));
+    SHL_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    c->sc.pfun = c->d_pfun;
+    c->sc.pfun_len = (int32_t)prog.size();
+  }
+  // the step graphs hold the step constants by value
+  if (c->graph) cudaGraphExecDestroy(c->graph);
+  if (c->graph1) cudaGraphExecDestroy(c->graph1);
+  c->graph = c->graph1 = nullptr;
+  return SHL_OK;
+}
+
+shl_status shl_eval_pressure_function(shl_ctx* c, const double* t, uint32_t n, double* out) {
+  if (!c || (n && (!t || !out))) return SHL_ERR_ARG;
+  if (c->sc.pfun_len == 0) {
+    g_err = "no pressure function set";
+    return SHL_ERR_ARG;
+  }
+  if (n == 0) return SHL_OK;
+  double* d = nullptr;
+  SHL_CUDA_TRY(cudaMallocAsync((void**)&d, 2 * (size_t)n * sizeof(double), c->stream));
+  SHL_CUDA_TRY(cudaMemcpyAsync(d, t, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  launch_eval_program(c->sc.pfun, c->sc.pfun_len, d, (int)n, d + n, c->stream);
+  SHL_CUDA_TRY(cudaMemcpyAsync(out, d + n, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  SHL_CUDA_TRY(cudaFreeAsync(d, c->stream));
+  SHL_CUDA_TRY(cudaStreamSynchronize(c->stream));
+  return check_launch("shl_eval_pressure_function");
 }
 
 shl_status shl_get_energies(shl_ctx* c, shl_energies* e) {

@@ -18,6 +18,7 @@
 #include <cctype>
 #include <cmath>
 #include <cstdlib>
+#include <cstring>
 #include <map>
 #include <memory>
 #include <stdexcept>
@@ -26,6 +27,24 @@
 
 namespace shl {
 namespace expr {
+
+// A flat program for a stack machine (compiled from an Expression), so that
+// the device can evaluate a parameter at its own time (one thread).
+enum OpCode : int32_t {
+  OP_CONST, OP_VAR, OP_NEG, OP_ADD, OP_SUB, OP_MUL, OP_DIV, OP_POW, OP_LT, OP_GT, OP_LE, OP_GE, OP_EQ, OP_NE,
+  OP_AND, OP_OR, OP_FUN1, OP_MIN, OP_MAX, OP_SUM, OP_AVG, OP_JZ, OP_JMP
+};
+enum Fun1 : int32_t {
+  F_SIN, F_COS, F_TAN, F_ASIN, F_ACOS, F_ATAN, F_SINH, F_COSH, F_TANH, F_ASINH, F_ACOSH, F_ATANH, F_EXP, F_LOG,
+  F_LOG2, F_LOG10, F_SQRT, F_SIGN, F_RINT, F_ABS
+};
+struct Op {
+  int32_t code;
+  int32_t arg;   // variable index (t, d, x, y, z), function id, argument count, or jump target
+  double value;  // constant
+};
+constexpr int kMaxProgram = 256;
+constexpr int kMaxStack = 32;
 
 struct Node {
   enum Kind { NUM, VAR, NEG, BIN, FUN, IF } kind = NUM;
@@ -65,6 +84,16 @@ class Expression {
     return eval(roots_.at(component).get(), vars);
   }
   const std::string& text() const { return text_; }
+
+  // program of one component; throws if it exceeds kMaxProgram ops or kMaxStack depth
+  std::vector<Op> compile(size_t component = 0) const {
+    std::vector<Op> prog;
+    int depth = 0, max_depth = 0;
+    emit(roots_.at(component).get(), prog, depth, max_depth);
+    if ((int)prog.size() > kMaxProgram || max_depth > kMaxStack)
+      throw std::runtime_error("expression \"" + text_ + "\" is too long for the device");
+    return prog;
+  }
 
  private:
   std::string text_;
@@ -234,6 +263,71 @@ class Expression {
       return;
     }
     fail("unknown function '" + n.name + "'");
+  }
+  static void push(std::vector<Op>& p, int32_t code, int32_t arg, double value, int& depth, int& max_depth,
+                   int pops, int pushes) {
+    p.push_back(Op{code, arg, value});
+    depth += pushes - pops;
+    if (depth > max_depth) max_depth = depth;
+  }
+  void emit(const Node* n, std::vector<Op>& p, int& depth, int& max_depth) const {
+    switch (n->kind) {
+      case Node::NUM: push(p, OP_CONST, 0, n->value, depth, max_depth, 0, 1); return;
+      case Node::VAR: {
+        const char* names = "tdxyz";
+        const int idx = (int)(std::strchr(names, n->name[0]) - names);
+        push(p, OP_VAR, idx, 0, depth, max_depth, 0, 1);
+        return;
+      }
+      case Node::NEG:
+        emit(n->args[0].get(), p, depth, max_depth);
+        push(p, OP_NEG, 0, 0, depth, max_depth, 1, 1);
+        return;
+      case Node::IF: {
+        emit(n->args[0].get(), p, depth, max_depth);
+        const size_t jz = p.size();
+        push(p, OP_JZ, 0, 0, depth, max_depth, 1, 0);
+        emit(n->args[1].get(), p, depth, max_depth);
+        const size_t jmp = p.size();
+        push(p, OP_JMP, 0, 0, depth, max_depth, 0, 0);
+        depth -= 1;  // only one branch's value stays on the stack
+        p[jz].arg = (int32_t)p.size();
+        emit(n->args[2].get(), p, depth, max_depth);
+        p[jmp].arg = (int32_t)p.size();
+        return;
+      }
+      case Node::BIN: {
+        emit(n->args[0].get(), p, depth, max_depth);
+        emit(n->args[1].get(), p, depth, max_depth);
+        static const char* ops[] = {"+", "-", "*", "/", "^", "<", ">", "<=", ">=", "==", "!=", "&&", "||"};
+        static const int32_t codes[] = {OP_ADD, OP_SUB, OP_MUL, OP_DIV, OP_POW, OP_LT, OP_GT,
+                                        OP_LE,  OP_GE,  OP_EQ,  OP_NE,  OP_AND, OP_OR};
+        for (int k = 0; k < 13; ++k)
+          if (n->name == ops[k]) {
+            push(p, codes[k], 0, 0, depth, max_depth, 2, 1);
+            return;
+          }
+        return;
+      }
+      case Node::FUN: {
+        for (const auto& a : n->args) emit(a.get(), p, depth, max_depth);
+        static const char* f1[] = {"sin",   "cos",   "tan", "asin", "acos", "atan", "sinh",  "cosh", "tanh", "asinh",
+                                   "acosh", "atanh", "exp", "log",  "log2", "log10", "sqrt", "sign", "rint", "abs"};
+        for (int k = 0; k < 20; ++k)
+          if (n->name == f1[k]) {
+            push(p, OP_FUN1, k, 0, depth, max_depth, 1, 1);
+            return;
+          }
+        if (n->name == "ln") {
+          push(p, OP_FUN1, F_LOG, 0, depth, max_depth, 1, 1);
+          return;
+        }
+        const int cnt = (int)n->args.size();
+        const int32_t code = n->name == "min" ? OP_MIN : n->name == "max" ? OP_MAX : n->name == "sum" ? OP_SUM : OP_AVG;
+        push(p, code, cnt, 0, depth, max_depth, cnt, 1);
+        return;
+      }
+    }
   }
   static void collect(const Node* n, std::vector<std::string>& out) {
     if (n->kind == Node::VAR) {

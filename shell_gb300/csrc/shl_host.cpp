@@ -219,6 +219,11 @@ void shl_params_default(shl_params* p) {
   p->newmark_beta = 0.25;
   p->newmark_gamma = 0.5;
   p->precision = SHL_PREC_FP64;
+  p->adapt_dt_every = 0;
+  p->dt_min = 0.0;
+  p->dt_max = 0.0;
+  p->rel_loc_err_min = 5e-5;
+  p->rel_loc_err_max = 5e-4;
 }
 
 const char* shl_status_string(shl_status s) {

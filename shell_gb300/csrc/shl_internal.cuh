@@ -17,6 +17,8 @@
 
 #include <cuda_runtime.h>
 #include <cstdint>
+
+#include "shl_expr.h"
 #include <string>
 #include <vector>
 
@@ -87,6 +89,14 @@ struct Ctl {
   double Etens, Ebend, Eself, Efric, Ekin, kGauss, kMean;
   uint32_t Nc;
   uint32_t pad;
+  // adaptive time stepping (ShellSystem.C:1010-1044, 1104-1117)
+  double dt_cur;            // time step of the next attempt
+  double nm[10];            // newmark_a of dt_cur (ShellSystem.C:744-759)
+  double new_dt;            // proposal of the current attempt
+  uint32_t accept;          // the current attempt is accepted
+  uint32_t rejections;      // repeated attempts since the last report reset
+  uint32_t steps_target;    // pause once steps_done reaches it
+  uint32_t paused;          // 1: steps_target reached, 2: stopping criterion true
   // dt-weighted sums (MovingAverage inputs)
   double sum_dt, sum_area, sum_volume, sum_Nc, sum_Ekin, sum_Etens, sum_Ebend, sum_Eself, sum_Efric,
       sum_kGauss, sum_kMean;
@@ -117,12 +127,23 @@ struct StepConst {
   int32_t fp32;      // element forces in FP32 (relative-displacement form)
   uint32_t V, F;
   double internal_scale;  // 1, or 0 for the pressure-only force of a residual check
+  const shl::expr::Op* pfun;  // pressure as a compiled expression of t (device), or null: use the table
+  int32_t pfun_len;
+  int32_t sfun_len;
+  const shl::expr::Op* sfun;  // stopping criterion as a compiled expression of t, or null
+  // adaptive time stepping: 0 = fixed dt
+  uint32_t adapt_every;
+  int32_t pad_adapt;
+  double beta, gamma;
+  double err_min, err_max, err_target;
+  double dt_min_eff, dt_max_eff;
 };
 
 // Device buffers of one context.
 struct DevBuf {
   double *X, *u, *v, *a, *up, *vp, *p, *Minv, *C;
   double* M;          // 3V lumped masses (1 / Minv), for the kinetic energy
+  double* ap;         // 3V predicted acceleration of an adaptive attempt (adaptive dt only)
   double* fcorr;      // 3V defect correction added to the FP32 force in a step, or null
   double* face;       // FF_COUNT * F
   double* pscale;     // F (internal order): factor on the step's pressure (per shell)
@@ -178,9 +199,11 @@ void launch_fp64_peak(double* out, int blocks, int iters, cudaStream_t s);
 uint32_t noalloc_max_faces();
 cudaError_t launch_force_noalloc(const DevBuf& ctx_b, const StepConst& sc, const ElemGroups& eg, uint32_t n_blocks,
                                  const double* u, double pressure, double* f_out, cudaStream_t s);
-void launch_shell_norms(const double* f, const double* fext, const uint32_t* node_off, uint32_t n_shells, double* out,
-                        cudaStream_t s);
+void launch_shell_norms(const double* f, const double* fext, const double* mass, const uint32_t* node_off,
+                        uint32_t n_shells, double* out, cudaStream_t s);
 void launch_defect(const double* f64, const double* f32, size_t n, double* out, cudaStream_t s);
+void launch_eval_program(const void* prog, int n, const double* t, int m, double* out, cudaStream_t s);
+void launch_correct_adapt(const DevBuf& b, const StepConst& sc, cudaStream_t s);
 void launch_flush(void* buf, size_t bytes, uint32_t tag, cudaStream_t s);
 
 // ---- launchers (shl_contact.cu) ----

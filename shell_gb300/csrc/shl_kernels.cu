@@ -31,7 +31,26 @@ namespace shl {
 // ---------------------------------------------------------------- helpers --
 
 __device__ __forceinline__ bool inactive(const Ctl* ctl) {
-  return ctl->halted != 0;
+  return ctl->halted != 0 || ctl->paused != 0;
+}
+
+// ShellSystem::set_newmark_parameters (ShellSystem.C:744-759) with the bounds
+// of ShellSystem.C:306-310, into the control block (adaptive dt)
+__device__ void set_newmark(Ctl* ctl, const StepConst& sc, double new_dt) {
+  double dt = fmax(new_dt, sc.dt_min_eff);
+  dt = fmin(dt, sc.dt_max_eff);
+  const double beta = sc.beta, gamma = sc.gamma;
+  ctl->dt_cur = dt;
+  ctl->nm[0] = beta * dt * dt;
+  ctl->nm[1] = gamma / (beta * dt);
+  ctl->nm[2] = 1 / (beta * dt);
+  ctl->nm[3] = 1 / (2 * beta) - 1;
+  ctl->nm[4] = gamma / beta - 1;
+  ctl->nm[5] = dt * (gamma / (2 * beta) - 1);
+  ctl->nm[6] = (1 - gamma) * dt;
+  ctl->nm[7] = gamma * dt;
+  ctl->nm[8] = dt * dt * (0.5 - beta);
+  ctl->nm[9] = dt * dt * fabs(beta - 1. / 6);
 }
 
 // fixed-order block sum; result valid in thread 0; sh needs blockDim/32 doubles
@@ -90,6 +109,107 @@ __device__ __forceinline__ double rebuild_tolerance(const StepConst& sc, const C
   return __dmul_rn(sc.cell_margin, cs);
 }
 
+// ------------------------------------------------ config expressions --
+// Stack-machine evaluation of a program compiled by shl_expr.h, one thread;
+// bounded by the program length (at most shl::expr::kMaxProgram ops, each
+// jump forward) and stack depth (checked when compiling).
+__device__ double eval_program(const shl::expr::Op* prog, int n, double t, double d) {
+  using namespace shl::expr;
+  double st[kMaxStack];
+  int sp = 0;
+  const double vars[5] = {t, d, 0.0, 0.0, 0.0};
+  for (int pc = 0; pc < n && pc < kMaxProgram;) {
+    const Op op = prog[pc++];
+    switch (op.code) {
+      case OP_CONST: st[sp++] = op.value; break;
+      case OP_VAR: st[sp++] = vars[op.arg]; break;
+      case OP_NEG: st[sp - 1] = -st[sp - 1]; break;
+      case OP_JZ: {
+        const double c = st[--sp];
+        if (c == 0.0) pc = op.arg;
+        break;
+      }
+      case OP_JMP: pc = op.arg; break;
+      case OP_FUN1: {
+        const double x = st[sp - 1];
+        double r = 0.0;
+        switch (op.arg) {
+          case F_SIN: r = sin(x); break;
+          case F_COS: r = cos(x); break;
+          case F_TAN: r = tan(x); break;
+          case F_ASIN: r = asin(x); break;
+          case F_ACOS: r = acos(x); break;
+          case F_ATAN: r = atan(x); break;
+          case F_SINH: r = sinh(x); break;
+          case F_COSH: r = cosh(x); break;
+          case F_TANH: r = tanh(x); break;
+          case F_ASINH: r = asinh(x); break;
+          case F_ACOSH: r = acosh(x); break;
+          case F_ATANH: r = atanh(x); break;
+          case F_EXP: r = exp(x); break;
+          case F_LOG: r = log(x); break;
+          case F_LOG2: r = log2(x); break;
+          case F_LOG10: r = log10(x); break;
+          case F_SQRT: r = sqrt(x); break;
+          case F_SIGN: r = (double)((x > 0.0) - (x < 0.0)); break;
+          case F_RINT: r = rint(x); break;
+          case F_ABS: r = fabs(x); break;
+        }
+        st[sp - 1] = r;
+        break;
+      }
+      case OP_MIN:
+      case OP_MAX:
+      case OP_SUM:
+      case OP_AVG: {
+        const int k = op.arg;
+        double r = st[sp - k];
+        if (op.code == OP_SUM || op.code == OP_AVG) r = 0.0;
+        for (int i = sp - k; i < sp; ++i) {
+          const double x = st[i];
+          if (op.code == OP_MIN) r = x < r ? x : r;
+          else if (op.code == OP_MAX) r = x > r ? x : r;
+          else r += x;
+        }
+        if (op.code == OP_AVG) r /= (double)k;
+        sp -= k;
+        st[sp++] = r;
+        break;
+      }
+      default: {
+        const double b = st[--sp], a = st[sp - 1];
+        double r = 0.0;
+        switch (op.code) {
+          case OP_ADD: r = a + b; break;
+          case OP_SUB: r = a - b; break;
+          case OP_MUL: r = a * b; break;
+          case OP_DIV: r = a / b; break;
+          case OP_POW: r = pow(a, b); break;
+          case OP_LT: r = a < b; break;
+          case OP_GT: r = a > b; break;
+          case OP_LE: r = a <= b; break;
+          case OP_GE: r = a >= b; break;
+          case OP_EQ: r = a == b; break;
+          case OP_NE: r = a != b; break;
+          case OP_AND: r = (a != 0.0 && b != 0.0); break;
+          case OP_OR: r = (a != 0.0 || b != 0.0); break;
+        }
+        st[sp - 1] = r;
+      }
+    }
+  }
+  return sp > 0 ? st[sp - 1] : 0.0;
+}
+
+__global__ void k_eval_program(const shl::expr::Op* prog, int n, const double* t, int m, double* out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < m) out[i] = eval_program(prog, n, t[i], 0.0);
+}
+
+void launch_eval_program(const void* prog, int n, const double* t, int m, double* out, cudaStream_t s) {
+  k_eval_program<<<(m + 127) / 128, 128, 0, s>>>((const shl::expr::Op*)prog, n, t, m, out);
+}
+
 // ------------------------------------------------------------ predictor --
 // u_pred = u + dt v + a8 a ; v_pred = v + a6 a ; p = X + u_pred ; du_max
 __global__ void __launch_bounds__(kBlock) k_predict(DevBuf b, StepConst sc) {
@@ -97,6 +217,8 @@ __global__ void __launch_bounds__(kBlock) k_predict(DevBuf b, StepConst sc) {
   if (inactive(ctl)) return;
   __shared__ double sh[kBlock / 32];
   const uint32_t n = blockIdx.x * blockDim.x + threadIdx.x;
+  const double dt = sc.adapt_every ? ctl->dt_cur : sc.dt;
+  const double nm8 = sc.adapt_every ? ctl->nm[8] : sc.nm8, nm6 = sc.adapt_every ? ctl->nm[6] : sc.nm6;
   double du2 = 0.0;
   if (n < sc.V) {
     double d[3];
@@ -107,12 +229,12 @@ __global__ void __launch_bounds__(kBlock) k_predict(DevBuf b, StepConst sc) {
       double up, vp;
       if (sc.contact) {
         // separately rounded, as the host does: positions feed the contact list
-        up = __dadd_rn(__dmul_rn(sc.dt, v), u);
-        up = __dadd_rn(__dmul_rn(sc.nm8, a), up);
-        vp = __dadd_rn(__dmul_rn(sc.nm6, a), v);
+        up = __dadd_rn(__dmul_rn(dt, v), u);
+        up = __dadd_rn(__dmul_rn(nm8, a), up);
+        vp = __dadd_rn(__dmul_rn(nm6, a), v);
       } else {
-        up = fma(sc.nm8, a, fma(sc.dt, v, u));
-        vp = fma(sc.nm6, a, v);
+        up = fma(nm8, a, fma(dt, v, u));
+        vp = fma(nm6, a, v);
       }
       b.up[k] = up;
       if (sc.fp32) b.up32[k] = (float)up;
@@ -130,10 +252,12 @@ __global__ void __launch_bounds__(kBlock) k_predict(DevBuf b, StepConst sc) {
   mm = block_max(mm, sh);
   if (threadIdx.x != 0) return;
   // prepare_next_step: time, the step's pressure, volume pressure
-  ctl->time = __dadd_rn(ctl->time, sc.dt);
+  ctl->time = __dadd_rn(ctl->time, dt);
   ctl->time_step += 1;
   double pr = sc.pressure_default;
-  if (sc.pressure_table && ctl->table_len > 0)
+  if (sc.pfun_len > 0)
+    pr = eval_program(sc.pfun, sc.pfun_len, ctl->time, 0.0);
+  else if (sc.pressure_table && ctl->table_len > 0)
     pr = sc.pressure_table[ctl->table_pos < ctl->table_len ? ctl->table_pos : ctl->table_len - 1];
   ctl->table_pos += 1;
   if (sc.compat_zero_pressure) pr = pr * 0.0;
@@ -775,7 +899,7 @@ __global__ void __launch_bounds__(kBlock) k_gather_correct(DevBuf b, StepConst s
         f[2] -= q[2];
       }
     }
-    if (mode == 1 && b.fcorr) {
+    if (mode >= 1 && b.fcorr) {
       // FP64 defect of the FP32 force, refreshed at each residual check (shl_residual)
       f[0] += b.fcorr[3 * (size_t)n];
       f[1] += b.fcorr[3 * (size_t)n + 1];
@@ -787,6 +911,13 @@ __global__ void __launch_bounds__(kBlock) k_gather_correct(DevBuf b, StepConst s
       const size_t k = 3 * (size_t)n + c;
       const double vp = b.vp[k];
       const double ap = b.Minv[k] * (f[c] - b.C[k] * vp);
+      if (mode == 2) {
+        // adaptive attempt: keep a_pred; local-error and velocity norms (ShellSystem.C:1017-1040)
+        b.ap[k] = ap;
+        du2 = fmax(du2, fabs(ap - b.a[k]));
+        ekin = fmax(ekin, fabs(vp));
+        continue;
+      }
       if (mode == 0) {
         if (f_out) f_out[k] = f[c];
         if (a_out) a_out[k] = ap;
@@ -810,6 +941,53 @@ __global__ void __launch_bounds__(kBlock) k_gather_correct(DevBuf b, StepConst s
     if (mode == 1) du2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
   }
   if (mode == 0) return;
+  if (mode == 2) {
+    const double na = block_max(du2, sh);
+    const double vm = block_max(ekin, sh);
+    if (threadIdx.x == 0) {
+      b.partial[(size_t)blockIdx.x * 8] = na;
+      b.partial[(size_t)blockIdx.x * 8 + 1] = vm;
+    }
+    if (!last_block(&ctl->cnt[3])) return;
+    double m0 = 0.0, m1 = 0.0;
+    for (int k = threadIdx.x; k < (int)gridDim.x; k += blockDim.x) {
+      m0 = fmax(m0, __ldcg(&b.partial[(size_t)k * 8]));
+      m1 = fmax(m1, __ldcg(&b.partial[(size_t)k * 8 + 1]));
+    }
+    const double norm_a = block_max(m0, sh);
+    const double vmax = block_max(m1, sh);
+    if (threadIdx.x != 0) return;
+    const double dt = ctl->dt_cur;
+    double new_dt = dt;
+    if (ctl->time_step % sc.adapt_every == 0) {
+      double rel_loc_err = sc.err_target;
+      if (isfinite(norm_a))
+        rel_loc_err = ctl->nm[9] * norm_a / sc.thickness;
+      else
+        register_problem(ctl, SHL_NOT_FINITE);
+      if (rel_loc_err == 0.0)
+        new_dt = 2 * dt;
+      else if (rel_loc_err > sc.err_max || rel_loc_err < sc.err_min)
+        new_dt = dt * pow(sc.err_target / rel_loc_err, 1. / 3);
+      if (sc.contact) {
+        // resolve the contact depth with at least 10 steps
+        if (__dmul_rn(__dmul_rn(__dmul_rn(new_dt, vmax), 10.0), 2.0) > sc.thickness)
+          new_dt = sc.thickness / (2.0 * 10.0 * vmax);
+      }
+    }
+    ctl->new_dt = new_dt;
+    ctl->accept = new_dt >= dt ? 1u : 0u;
+    if (!ctl->accept) {
+      // repeat the step with the smaller dt (ShellSystem.C:1104-1117)
+      ctl->time = ctl->time - dt;
+      ctl->time_step -= 1;
+      if (ctl->table_pos > 0) ctl->table_pos -= 1;
+      ctl->rejections += 1;
+      set_newmark(ctl, sc, new_dt);
+      if (ctl->dt_cur <= 2.220446049250313e-16) register_problem(ctl, SHL_SMALL_TIMESTEP);
+    }
+    return;
+  }
   const double m = block_max(du2, sh);
   const double ek = block_sum(0.5 * ekin, sh);
   if (threadIdx.x == 0) {
@@ -838,10 +1016,83 @@ __global__ void __launch_bounds__(kBlock) k_gather_correct(DevBuf b, StepConst s
   ctl->rebuild = (sc.contact && ctl->du_sum >= rebuild_tolerance(sc, ctl)) ? 1u : 0u;
 }
 
+// corrector of an accepted adaptive attempt (ShellSystem.C:1046-1101): u, v, a
+// from the stored a_pred; check_increment(true); contact-list flag
+__global__ void __launch_bounds__(kBlock) k_correct_adapt(DevBuf b, StepConst sc) {
+  Ctl* ctl = b.ctl;
+  if (inactive(ctl) || !ctl->accept) return;
+  __shared__ double sh[kBlock / 32];
+  const uint32_t n = blockIdx.x * blockDim.x + threadIdx.x;
+  const double nm0 = ctl->nm[0], nm7 = ctl->nm[7];
+  double du2 = 0.0, ekin = 0.0;
+  if (n < sc.V) {
+    double d[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const size_t k = 3 * (size_t)n + c;
+      const double ap = b.ap[k], vp = b.vp[k];
+      double up, vn;
+      if (sc.contact) {
+        up = __dadd_rn(__dmul_rn(nm0, ap), b.up[k]);
+        vn = __dadd_rn(__dmul_rn(nm7, ap), vp);
+      } else {
+        up = fma(nm0, ap, b.up[k]);
+        vn = fma(nm7, ap, vp);
+      }
+      d[c] = __dsub_rn(up, b.u[k]);
+      b.u[k] = up;
+      b.v[k] = vn;
+      b.a[k] = ap;
+      b.p[k] = __dadd_rn(b.X[k], up);
+      ekin += vn * vn * b.M[k];
+    }
+    du2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+  }
+  const double m = block_max(du2, sh);
+  const double ek = block_sum(0.5 * ekin, sh);
+  if (threadIdx.x == 0) {
+    b.partial[(size_t)blockIdx.x * 8] = m;
+    b.partial[(size_t)blockIdx.x * 8 + 1] = ek;
+  }
+  if (!last_block(&ctl->cnt[6])) return;
+  double mm = 0.0;
+  for (int k = threadIdx.x; k < (int)gridDim.x; k += blockDim.x) mm = fmax(mm, __ldcg(&b.partial[(size_t)k * 8]));
+  mm = block_max(mm, sh);
+  const double ekt = sum_partials(b.partial, 1, gridDim.x, sh);
+  if (threadIdx.x != 0) return;
+  ctl->Ekin = ekt;
+  const double du_max = sqrt(mm);
+  if (isfinite(du_max)) {
+    ctl->du_sum = __dadd_rn(ctl->du_sum, __dmul_rn(2.0, du_max));
+    if (du_max == 0.0)
+      register_problem(ctl, SHL_NO_DISP_CHANGE);
+    else if (sc.contact && du_max > 0.5 * sc.thickness)
+      register_problem(ctl, SHL_LARGE_DISP);
+  } else {
+    register_problem(ctl, SHL_NOT_FINITE);
+  }
+  if (!isfinite(ekt)) register_problem(ctl, SHL_NOT_FINITE);
+  ctl->rebuild = (sc.contact && ctl->du_sum >= rebuild_tolerance(sc, ctl)) ? 1u : 0u;
+}
+
 // ------------------------------------------------------ volume, end step --
 __global__ void __launch_bounds__(kBlock) k_volume_end(DevBuf b, StepConst sc, int end_step) {
   Ctl* ctl = b.ctl;
   if (inactive(ctl)) return;
+  if (end_step && sc.adapt_every && !ctl->accept) {
+    // a repeated attempt ends no step; only a step size below the machine
+    // precision (SHL_SMALL_TIMESTEP) ends the run (ShellSystem.C:1110-1117)
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      const int pr = ctl->problem;
+      if (pr >= SHL_STOP_SIM) {
+        if (pr > ctl->worst_problem) ctl->worst_problem = pr;
+        if (ctl->first_problem_step == 0) ctl->first_problem_step = ctl->time_step + 1;
+        ctl->halted = 1;
+        ctl->problem = 0;
+      }
+    }
+    return;
+  }
   __shared__ double sh[kBlock / 32];
   const uint32_t f = blockIdx.x * blockDim.x + threadIdx.x;
   double det = 0.0;
@@ -859,7 +1110,7 @@ __global__ void __launch_bounds__(kBlock) k_volume_end(DevBuf b, StepConst sc, i
   if (threadIdx.x != 0) return;
   ctl->volume = fabs(tot / 6.0) - ctl->area * 0.5 * sc.thickness;
   if (!end_step) return;
-  const double dt = sc.dt;
+  const double dt = sc.adapt_every ? ctl->dt_cur : sc.dt;
   ctl->sum_dt += dt;
   ctl->sum_area += dt * ctl->area;
   ctl->sum_volume += dt * ctl->volume;
@@ -877,20 +1128,48 @@ __global__ void __launch_bounds__(kBlock) k_volume_end(DevBuf b, StepConst sc, i
   ctl->steps_done += 1;
   if (pr >= SHL_STOP_SIM || (sc.stop_on_problem && pr > 0) || ctl->error) ctl->halted = 1;
   ctl->problem = 0;
+  // the next step's dt, after the measurement used this one (ShellSystem.C:1096-1098)
+  if (sc.adapt_every) set_newmark(ctl, sc, ctl->new_dt);
+  if (ctl->steps_done >= ctl->steps_target) ctl->paused |= 1u;
+  // stopping criterion, tested before the next step (shell.C:314-318)
+  if (sc.sfun_len > 0 && eval_program(sc.sfun, sc.sfun_len, ctl->time, 0.0) != 0.0) ctl->paused |= 2u;
 }
 
 // ------------------------------------------------------------ utilities --
-// FP64 FMA throughput probe: 8 independent register chains per thread.
-// per shell s (nodes node_off[s] .. node_off[s+1]): sum |f|^2 and |f_ext|^2 in a
-// fixed order (one block per shell)
-__global__ void __launch_bounds__(kBlock) k_shell_norms(const double* f, const double* fext, const uint32_t* node_off,
-                                                        double* out) {
+// per shell s (nodes node_off[s] .. node_off[s+1]), one block per shell, fixed
+// order: |f - m F/M|^2 and |f_ext - m F_ext/M|^2, where F is the resultant of f
+// over the shell and m, M the nodal and total mass -- the residual without its
+// rigid-translation part.  (A closed shell under uniform pressure carries a
+// resultant of the order of the quadrature error, which a free shell answers
+// with a steady drift, not with deformation.)
+__global__ void __launch_bounds__(kBlock) k_shell_norms(const double* f, const double* fext, const double* mass,
+                                                        const uint32_t* node_off, double* out) {
   __shared__ double sh[kBlock / 32];
+  __shared__ double res[7];
   const uint32_t n0 = node_off[blockIdx.x], n1 = node_off[blockIdx.x + 1];
+  double s[7] = {0, 0, 0, 0, 0, 0, 0};  // F (3), F_ext (3), M
+  for (uint32_t n = n0 + threadIdx.x; n < n1; n += blockDim.x) {
+    for (int c = 0; c < 3; ++c) {
+      s[c] += f[3 * (size_t)n + c];
+      s[3 + c] += fext[3 * (size_t)n + c];
+    }
+    s[6] += mass[3 * (size_t)n];
+  }
+  for (int k = 0; k < 7; ++k) {
+    const double t = block_sum(s[k], sh);
+    if (threadIdx.x == 0) res[k] = t;
+  }
+  __syncthreads();
+  const double inv_m = 1.0 / res[6];
   double a = 0.0, e = 0.0;
-  for (size_t k = 3 * (size_t)n0 + threadIdx.x; k < 3 * (size_t)n1; k += blockDim.x) {
-    a += f[k] * f[k];
-    e += fext[k] * fext[k];
+  for (uint32_t n = n0 + threadIdx.x; n < n1; n += blockDim.x) {
+    const double w = mass[3 * (size_t)n] * inv_m;
+    for (int c = 0; c < 3; ++c) {
+      const double x = f[3 * (size_t)n + c] - w * res[c];
+      const double y = fext[3 * (size_t)n + c] - w * res[3 + c];
+      a += x * x;
+      e += y * y;
+    }
   }
   a = block_sum(a, sh);
   e = block_sum(e, sh);
@@ -898,6 +1177,11 @@ __global__ void __launch_bounds__(kBlock) k_shell_norms(const double* f, const d
     out[2 * blockIdx.x] = a;
     out[2 * blockIdx.x + 1] = e;
   }
+}
+
+void launch_shell_norms(const double* f, const double* fext, const double* mass, const uint32_t* node_off,
+                        uint32_t n_shells, double* out, cudaStream_t s) {
+  k_shell_norms<<<n_shells, kBlock, 0, s>>>(f, fext, mass, node_off, out);
 }
 
 __global__ void k_defect(const double* f64, const double* f32, size_t n, double* out) {
@@ -909,11 +1193,8 @@ void launch_defect(const double* f64, const double* f32, size_t n, double* out, 
   k_defect<<<(unsigned)std::min<size_t>((n + 255) / 256, 4096), 256, 0, s>>>(f64, f32, n, out);
 }
 
-void launch_shell_norms(const double* f, const double* fext, const uint32_t* node_off, uint32_t n_shells, double* out,
-                        cudaStream_t s) {
-  k_shell_norms<<<n_shells, kBlock, 0, s>>>(f, fext, node_off, out);
-}
 
+// FP64 FMA throughput probe: 8 independent register chains per thread.
 __global__ void __launch_bounds__(256) k_fp64_peak(double* out, int iters, double b, double c) {
   double a0 = threadIdx.x * 1e-9, a1 = a0 + 1e-3, a2 = a0 + 2e-3, a3 = a0 + 3e-3;
   double a4 = a0 + 4e-3, a5 = a0 + 5e-3, a6 = a0 + 6e-3, a7 = a0 + 7e-3;
@@ -960,10 +1241,15 @@ void launch_contact_force(const DevBuf& b, const StepConst& sc, int, cudaStream_
   if (nb == 0) nb = 1;
   k_contact_force<<<nb, kBlock, 0, s>>>(b, sc);
 }
-void launch_gather_correct(const DevBuf& b, const StepConst& sc, int, bool correct, double* f_out, double* a_out,
+// mode 2: an adaptive attempt (a_pred and the error estimate); else correct ? step corrector : evaluation
+void launch_gather_correct(const DevBuf& b, const StepConst& sc, int mode, bool correct, double* f_out, double* a_out,
                            cudaStream_t s) {
-  k_gather_correct<<<nblk(sc.V), kBlock, 0, s>>>(b, sc, correct ? 1 : 0, f_out, a_out);
+  k_gather_correct<<<nblk(sc.V), kBlock, 0, s>>>(b, sc, mode == 2 ? 2 : (correct ? 1 : 0), f_out, a_out);
 }
+void launch_correct_adapt(const DevBuf& b, const StepConst& sc, cudaStream_t s) {
+  k_correct_adapt<<<(sc.V + kBlock - 1) / kBlock, kBlock, 0, s>>>(b, sc);
+}
+
 void launch_volume_end_step(const DevBuf& b, const StepConst& sc, bool end_step, cudaStream_t s) {
   k_volume_end<<<nblk(sc.F), kBlock, 0, s>>>(b, sc, end_step ? 1 : 0);
 }

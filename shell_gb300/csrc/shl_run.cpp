@@ -481,10 +481,11 @@ int run(int argc, char** argv) {
   Function stop = function(cfg, "stopping_criterion", "0");
   P.stop_on_problem = cfg.boolean("stop_on_problem", false) ? 1 : 0;
   const unsigned adapt_dt_every = cfg.uint("adapt_dt_every", 0);
-  cfg.real("dt_min", 0);
-  cfg.real("dt_max", 0);
-  cfg.real("rel_loc_err_max", 5e-4);
-  cfg.real("rel_loc_err_min", 5e-5);
+  P.adapt_dt_every = adapt_dt_every;
+  P.dt_min = cfg.real("dt_min", 0);
+  P.dt_max = cfg.real("dt_max", 0);
+  P.rel_loc_err_max = cfg.real("rel_loc_err_max", 5e-4);
+  P.rel_loc_err_min = cfg.real("rel_loc_err_min", 5e-5);
   const unsigned random_seed = cfg.uint("random_seed", (unsigned)std::time(nullptr));
   const double distortion = cfg.real("distortion", 0);
   // parameters of this library only (no warning when absent)
@@ -498,7 +499,6 @@ int run(int argc, char** argv) {
   };
   need(P.shell_shell_contact != SHL_CONTACT_SMOOTH, "shell_shell_contact = smooth");
   need(!cavity_contact, "shell_cavity_contact = true (cavity contact)");
-  need(adapt_dt_every == 0, "adapt_dt_every > 0 (adaptive time stepping)");
   need(damping_rotation == 0 && perturbation_rate == 0 && gravity == 0 && !stand_still,
        "damping_rotation, perturbation_rate, gravity or stand_still");
   need(growth1 == 1 && growth2 == 1 && mgr == 0 && cgr == 0, "growth");
@@ -627,6 +627,17 @@ int run(int argc, char** argv) {
       avg.load_rows(rows, nr);
       check(shl_get_time(ctx, &time, nullptr), "shl_get_time");
       loaded = true;
+      if (adapt_dt_every > 0 && dt_loaded != P.dt) {
+        // with adaptive dt the saved step size is resumed (ShellSystem.C:3064-3067)
+        shl_destroy(ctx);
+        guard.c = nullptr;
+        P.dt = dt_loaded;
+        st = shl_create(&mesh, &P, &ctx);
+        if (st != SHL_OK) throw Error(std::string("ERROR: shl_create: ") + shl_last_error());
+        guard.c = ctx;
+        check(shl_load_state_file(ctx, load_filename.c_str(), &time_step, &dt_loaded, &wall_time, nullptr, 0, &nr),
+              "shl_load_state_file");
+      }
     }
   }
   if (!loaded) {
@@ -637,6 +648,12 @@ int run(int argc, char** argv) {
     check(shl_set_time(ctx, 0.0, 0), "shl_set_time");
     check(shl_apply_initial_conditions(ctx, u0.data(), 0.0, eval_at(pressure_fn, P.dt)),
           "shl_apply_initial_conditions");
+  }
+  if (adapt_dt_every > 0) {
+    // the step times are not known in advance: the device evaluates the
+    // pressure at each attempt's time and tests the stopping criterion after each step
+    check(shl_set_pressure_function(ctx, pressure_fn.e.text().c_str()), "shl_set_pressure_function");
+    if (!stop.e.is_constant()) check(shl_set_stop_function(ctx, stop.e.text().c_str()), "shl_set_stop_function");
   }
   std::cout.precision(std::numeric_limits<double>::digits10 + 2);
   if (data_time > 0) print_header();
@@ -679,17 +696,32 @@ int run(int argc, char** argv) {
       stop_now = true;
     }
     if (!stop_now) {
-      while (table.size() < kMaxChunk) {
-        if (!table.empty() && eval_at(stop, t) != 0) break;  // the next iteration stops before stepping
-        t += P.dt;
-        table.push_back(eval_at(pressure_fn, t));
-        const uint32_t step_no = time_step + (uint32_t)table.size();
-        if (data_time > 0 && (unsigned)(t / data_time) > last_data) break;
-        if (vtk_time > 0 && (unsigned)(t / vtk_time) > last_vtk) break;
-        if (time_steps && step_no >= time_steps) break;
-      }
       shl_step_report rep{};
-      check(shl_step(ctx, (uint32_t)table.size(), table.data(), 1, &rep), "shl_step");
+      if (adapt_dt_every > 0) {
+        // steps of unknown size: run half the steps the current dt needs to the next
+        // output time, so the step that crosses it is found one step at a time
+        double dt_now = P.dt;
+        check(shl_get_dt(ctx, &dt_now, nullptr), "shl_get_dt");
+        double next_t = INFINITY;
+        if (data_time > 0) next_t = std::min(next_t, (last_data + 1) * data_time);
+        if (vtk_time > 0) next_t = std::min(next_t, (last_vtk + 1) * vtk_time);
+        double k = std::isfinite(next_t) ? std::floor((next_t - time) / dt_now / 2) : (double)kMaxChunk;
+        uint32_t n = (uint32_t)std::max(1.0, std::min(k, (double)kMaxChunk));
+        if (time_steps) n = std::min<uint32_t>(n, time_steps - time_step);
+        check(shl_step(ctx, n, nullptr, 1, &rep), "shl_step");
+        if (rep.stopped) exit_code = SUCCESS;
+      } else {
+        while (table.size() < kMaxChunk) {
+          if (!table.empty() && eval_at(stop, t) != 0) break;  // the next iteration stops before stepping
+          t += P.dt;
+          table.push_back(eval_at(pressure_fn, t));
+          const uint32_t step_no = time_step + (uint32_t)table.size();
+          if (data_time > 0 && (unsigned)(t / data_time) > last_data) break;
+          if (vtk_time > 0 && (unsigned)(t / vtk_time) > last_vtk) break;
+          if (time_steps && step_no >= time_steps) break;
+        }
+        check(shl_step(ctx, (uint32_t)table.size(), table.data(), 1, &rep), "shl_step");
+      }
       time_step += rep.steps_done;
       time = rep.time;
       avg.add_report(rep);
@@ -718,7 +750,9 @@ int run(int argc, char** argv) {
       char name[64];
       std::snprintf(name, sizeof(name), "shell_state%010u.dat", time_step);
       const std::vector<double> rows = avg.rows();
-      check(shl_save_state_file(ctx, (data_dir + "/" + name).c_str(), time_step, P.dt, wall_time + elapsed(),
+      double dt_save = P.dt;
+      check(shl_get_dt(ctx, &dt_save, nullptr), "shl_get_dt");
+      check(shl_save_state_file(ctx, (data_dir + "/" + name).c_str(), time_step, dt_save, wall_time + elapsed(),
                                 rows.empty() ? nullptr : rows.data(), (uint32_t)(rows.size() / 14)),
             "shl_save_state_file");
       const std::string latest = data_dir + "/shell_state_latest.dat";

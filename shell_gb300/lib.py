@@ -39,6 +39,8 @@ _PARAM_FIELDS = (
                        "friction_stop_velocity", "static_friction_tol", "cell_size_mult", "cell_margin",
                        "neighbor_margin", "dt", "newmark_beta", "newmark_gamma")]
     + [("compat_zero_pressure", _i32), ("precision", _i32), ("stop_on_problem", _i32), ("pad1", _i32)]
+    + [("adapt_dt_every", _u32), ("pad2", _i32)]
+    + [(n, _d) for n in ("dt_min", "dt_max", "rel_loc_err_min", "rel_loc_err_max")]
 )
 
 
@@ -59,9 +61,9 @@ class ShlEnergies(ctypes.Structure):
 
 class ShlStepReport(ctypes.Structure):
     _fields_ = [("steps_done", _u32), ("worst_problem", _i32), ("time", _d), ("du_sum", _d), ("n_rebuilds", _u32),
-                ("pad", _u32), ("last", ShlEnergies)] + [
+                ("rejections", _u32), ("last", ShlEnergies)] + [
         (n, _d) for n in ("sum_dt", "sum_area", "sum_volume", "sum_Nc", "sum_Ekin", "sum_Etens", "sum_Ebend",
-                          "sum_Eself", "sum_Efric", "sum_kGauss", "sum_kMean")]
+                          "sum_Eself", "sum_Efric", "sum_kGauss", "sum_kMean")] + [("stopped", _u32), ("pad", _u32)]
 
 
 _lib = None
@@ -130,6 +132,10 @@ def load():
         "shl_mlp_gradients": (_i32, [vp, vp, vp, _u32, ctypes.POINTER(_d), vp, vp]),
         "shl_gemm_bf16": (_i32, [vp, vp, _u32, _u32, _u32, vp]),
         "shl_residual": (_i32, [vp, _d, ctypes.c_int, vp, vp, vp]),
+        "shl_set_pressure_function": (_i32, [vp, ctypes.c_char_p]),
+        "shl_get_dt": (_i32, [vp, ctypes.POINTER(_d), ctypes.POINTER(_u32)]),
+        "shl_set_stop_function": (_i32, [vp, ctypes.c_char_p]),
+        "shl_eval_pressure_function": (_i32, [vp, vp, _u32, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -152,7 +158,8 @@ def exported_symbols():
             "shl_get_node_fields", "shl_apply_loaded_state", "shl_save_state_file", "shl_load_state_file",
             "shl_write_vtu", "shl_get_energies", "shl_mlp_create", "shl_mlp_destroy", "shl_mlp_set_params",
             "shl_mlp_get_params", "shl_mlp_set_dataset", "shl_mlp_train", "shl_mlp_predict", "shl_mlp_gradients",
-            "shl_gemm_bf16", "shl_residual"]
+            "shl_gemm_bf16", "shl_residual", "shl_set_pressure_function", "shl_eval_pressure_function",
+            "shl_get_dt", "shl_set_stop_function"]
 
 
 class ShlError(RuntimeError):
@@ -382,6 +389,29 @@ class Shell:
         return Minv, C
 
     n_shells = 1  # a Batch sets its own count
+
+    def set_pressure_function(self, expr):
+        """Pressure as an expression of t evaluated on the device each step (None: use the table)."""
+        _check(self.lib.shl_set_pressure_function(self.h, None if expr is None else expr.encode()),
+               "shl_set_pressure_function", False)
+
+    def set_stop_function(self, expr):
+        """Stopping criterion (expression of t) tested on the device after every step (None: none)."""
+        _check(self.lib.shl_set_stop_function(self.h, None if expr is None else expr.encode()),
+               "shl_set_stop_function", False)
+
+    def dt(self):
+        """(current dt, repeated attempts since the last report)."""
+        d, r = _d(), _u32()
+        _check(self.lib.shl_get_dt(self.h, ctypes.byref(d), ctypes.byref(r)), "shl_get_dt", False)
+        return d.value, r.value
+
+    def eval_pressure_function(self, t):
+        t = np.ascontiguousarray(t, dtype=np.float64)
+        out = np.zeros_like(t)
+        _check(self.lib.shl_eval_pressure_function(self.h, t.ctypes.data, t.size, out.ctypes.data),
+               "shl_eval_pressure_function", False)
+        return out
 
     def residual(self, pressure, flags=0):
         """Relative residual ||f_ext - f_int|| / ||f_ext|| of the stored state, per shell

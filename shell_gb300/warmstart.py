@@ -28,9 +28,9 @@ from . import lib as L
 LEVEL = 5
 DIMS = [8, 512, 512, 512, 512, 3 * 10242]
 IMPERFECTION = 0.3        # amplitude of the imperfection in units of h
-DAMPING = 1.5             # mass-proportional damping of the relaxation
-DT = 2e-3                 # relaxation time step
-CHECK_EVERY = 50          # steps between residual checks
+DAMPING = 1.0             # mass-proportional damping of the relaxation
+DT = 4e-3                 # relaxation time step
+CHECK_EVERY = 100         # steps between residual checks
 
 
 def harmonics(X):
@@ -40,7 +40,7 @@ def harmonics(X):
     return np.stack([(3 * z * z - 1) / 2, np.sqrt(3.0) * x * z, x * (5 * z * z - 1) / 2], 1), n
 
 
-def sample_problems(n, seed, s_range=(0.3, 0.9)):
+def sample_problems(n, seed, s_range=(0.15, 0.5)):
     """n problems from a seed (material, thickness, pressure, imperfection)."""
     rng = np.random.default_rng(seed)
     return {
@@ -135,12 +135,18 @@ def relax(batch, u_start, tol=1e-6, check_every=CHECK_EVERY, max_steps=40000, co
             "history": np.array(hist)}
 
 
+def drop_drift(u):
+    """A displacement field without its mean translation (the drift of a free shell)."""
+    x = np.asarray(u, np.float64).reshape(-1, 3)
+    return (x - x.mean(0)).reshape(-1)
+
+
 def standardizer(F):
     mu, sd = F.mean(0), F.std(0) + 1e-12
     return mu.astype(np.float32), sd.astype(np.float32)
 
 
-def generate(problems, batch_size=512, precision=L.PREC_FP32, tol=1e-6, max_steps=40000, log=None, level=LEVEL):
+def generate(problems, batch_size=512, precision=L.PREC_FP32, tol=5e-5, max_steps=10000, log=None, level=LEVEL):
     """Equilibria of the problems by plain relaxation from zero, in batches.
     Returns (u_eq as n x 3V float64, conv_step, final residual, stats)."""
     n = len(problems["h"])
@@ -164,10 +170,10 @@ def generate(problems, batch_size=512, precision=L.PREC_FP32, tol=1e-6, max_step
 
 
 def train_surrogate(F_train, U_train, h_train, iters=4000, batch=256, seed=0, lr0=1e-3, lr_final=1e-5, hidden=None):
-    """Trains the network on standardised inputs and targets u / h; returns (net, scaler, loss curve)."""
+    """Trains the network on standardised inputs and targets u / h (drift removed); returns (net, scaler, curve)."""
     mu, sd = standardizer(F_train)
     Xn = (F_train - mu) / sd
-    Tn = (U_train / h_train[:, None]).astype(np.float32)
+    Tn = (np.array([drop_drift(u) for u in U_train]) / h_train[:, None]).astype(np.float32)
     dims = DIMS if hidden is None else [DIMS[0]] + list(hidden) + [U_train.shape[1]]
     net = L.MLP(dims, max_batch=batch, seed=seed)
     net.set_dataset(Xn, Tn)
@@ -181,72 +187,110 @@ def predict(net, scaler, F, h):
     return Y * np.asarray(h)[:, None]
 
 
-def experiment(n_train=3584, n_test=512, seed=0, batch_size=512, train_iters=4000, tol=1e-6, max_steps=40000,
-               fp64_check=True, log=print, level=LEVEL, hidden=None, train_batch=256):
-    """The whole warm-start study: equilibria of n_train + n_test seeded
-    problems by plain FP32 relaxation, the network trained on the first
-    n_train, then the n_test held-out problems relaxed from zero and from the
-    prediction (FP32 forces), with the plain start as fallback; optionally the
-    held-out problems relaxed in FP64 from zero as the accuracy reference and
-    for the FP64 face-steps/s.  Returns a JSON-able summary."""
-    out = {}
-    pr = sample_problems(n_train + n_test, seed)
+def solve(pr, U_start, level, precision, tol, max_steps, polish_tol=None, polish_max=None):
+    """Relaxation of a batch of problems from U_start (n x 3V).  With
+    polish_tol, a second FP64 phase continues from the first phase's state
+    (restarted at rest) down to polish_tol.  Returns per-shell steps to the
+    final tolerance (-1: not reached), the final displacements, wall time and
+    face-steps of each phase."""
+    n = len(pr["h"])
+    b, _ = build_batch(pr, precision=precision, level=level)
+    F = b.F
+    r = relax(b, np.asarray(U_start, np.float64).reshape(-1), tol=tol, max_steps=max_steps)
+    b.close()
+    out = {"steps": r["conv_step"].copy(), "u": r["u"], "wall_s": r["wall_s"], "phases": [
+        {"precision": "fp32" if precision == L.PREC_FP32 else "fp64", "steps": r["steps"], "wall_s": r["wall_s"],
+         "face_steps_per_s": F * r["steps"] / r["wall_s"], "reached": int((r["conv_step"] >= 0).sum())}]}
+    if polish_tol is None:
+        return out
+    b, _ = build_batch(pr, precision=L.PREC_FP64, level=level)
+    r2 = relax(b, np.concatenate(r["u"]), tol=polish_tol, max_steps=polish_max)
+    b.close()
+    ok = (r["conv_step"] >= 0) & (r2["conv_step"] >= 0)
+    out["steps"] = np.where(ok, r["conv_step"] + r2["conv_step"], -1)
+    out["u"] = r2["u"]
+    out["wall_s"] += r2["wall_s"]
+    out["phases"].append({"precision": "fp64", "steps": r2["steps"], "wall_s": r2["wall_s"],
+                          "face_steps_per_s": F * r2["steps"] / r2["wall_s"], "reached": int(ok.sum())})
+    return out
+
+
+def _stats(steps, mask):
+    s = steps[mask]
+    return {"median_steps": float(np.median(s)) if len(s) else None, "mean_steps": float(np.mean(s)) if len(s) else None}
+
+
+def experiment(n_train=2048, n_test=256, seed=0, batch_size=512, train_iters=4000, gen_tol=5e-5, gen_max=10000,
+               tol=1e-6, max_steps=15000, log=print, level=LEVEL, hidden=None, train_batch=256, s_range=(0.15, 0.5),
+               mixed=True):
+    """The warm-start study.  Equilibria of n_train seeded problems by plain
+    FP32 relaxation (FP64 defect correction) to gen_tol train the network;
+    n_test held-out problems are then solved to the FP64 residual tol from
+    zero (plain) and from the prediction (warm): in FP64, and (mixed=True) as
+    FP32 relaxation to gen_tol followed by an FP64 polish.  Shells whose warm
+    start does not converge fall back to the plain start (counted).  Returns
+    a JSON-able summary."""
+    t_all = time.perf_counter()
+    out = {"level": level, "problems": {"train": n_train, "test": n_test, "seed": seed, "pressure_over_p_cl": s_range},
+           "relaxation": {"dt": DT, "damping_alpha": DAMPING, "check_every": CHECK_EVERY, "tol": tol,
+                          "fp32_tol": gen_tol}}
+    pr = sample_problems(n_train + n_test, seed, s_range)
     F = features(pr)
-    t0 = time.perf_counter()
-    U, steps, rels, st = generate(subset(pr, np.arange(n_train)), batch_size, tol=tol, max_steps=max_steps, log=log,
+    U, steps, rels, st = generate(subset(pr, np.arange(n_train)), batch_size, tol=gen_tol, max_steps=gen_max, log=log,
                                   level=level)
     ok = steps >= 0
-    out["generation"] = {"problems": n_train, "converged": int(ok.sum()), "wall_s": st["wall_s"],
-                         "setup_s": st["setup_s"], "face_steps_per_s": st["face_steps"] / st["wall_s"],
-                         "median_steps": float(np.median(steps[ok])) if ok.any() else None}
+    out["generation"] = {"converged": int(ok.sum()), "wall_s": st["wall_s"], "setup_s": st["setup_s"],
+                         "fp32_face_steps_per_s": st["face_steps"] / st["wall_s"],
+                         **_stats(steps, ok)}
     t1 = time.perf_counter()
     net, scaler, curve = train_surrogate(F[:n_train][ok], U[ok], pr["h"][:n_train][ok], iters=train_iters, seed=seed,
                                          hidden=hidden, batch=train_batch)
-    out["training"] = {"samples": int(ok.sum()), "iters": train_iters, "wall_s": time.perf_counter() - t1,
-                       "loss_first": float(curve[0]), "loss_last": float(curve[-1])}
+    out["training"] = {"samples": int(ok.sum()), "iters": train_iters, "batch": train_batch,
+                       "wall_s": time.perf_counter() - t1, "loss_first": float(curve[0]), "loss_last": float(curve[-1])}
     test = subset(pr, np.arange(n_train, n_train + n_test))
     Ft, ht = F[n_train:], test["h"]
-    # plain start
-    b, _ = build_batch(test, level=level)
-    plain = relax(b, np.zeros(3 * b.V), tol=tol, max_steps=max_steps)
-    F_faces = b.F
-    b.close()
-    # warm start from the prediction
     tp = time.perf_counter()
     U_pred = predict(net, scaler, Ft, ht)
     pred_s = time.perf_counter() - tp
-    b, _ = build_batch(test, level=level)
-    warm = relax(b, U_pred.reshape(-1), tol=tol, max_steps=max_steps)
-    b.close()
-    # fallback: shells whose warm start did not converge restart from zero (the plain result)
-    fb = warm["conv_step"] < 0
-    warm_steps = np.where(fb, max_steps + np.maximum(plain["conv_step"], 0), warm["conv_step"])
-    both = (plain["conv_step"] >= 0)
-    out["test"] = {
-        "problems": n_test, "faces_per_batch": int(F_faces), "prediction_s": pred_s,
-        "plain": {"converged": int(both.sum()), "median_steps": float(np.median(plain["conv_step"][both])),
-                  "mean_steps": float(np.mean(plain["conv_step"][both])), "wall_s_all": plain["wall_s"],
-                  "steps_all": plain["steps"]},
-        "warm": {"converged": int((~fb).sum()), "fallbacks": int(fb.sum()),
-                 "median_steps": float(np.median(warm_steps[both])), "mean_steps": float(np.mean(warm_steps[both])),
-                 "wall_s_all": warm["wall_s"] + pred_s, "steps_all": warm["steps"]},
-        "prediction_error_vs_plain_eq": float(np.median([np.abs(U_pred[k] - plain["u"][k]).max() / ht[k]
-                                                          for k in range(n_test)])),
-    }
-    if fp64_check:
-        b, _ = build_batch(test, precision=L.PREC_FP64, level=level)
-        ref = relax(b, np.zeros(3 * b.V), tol=tol, max_steps=max_steps)
-        b.close()
-        okr = ref["conv_step"] >= 0
-        d_plain = np.array([np.abs(plain["u"][k] - ref["u"][k]).max() for k in range(n_test)])
-        d_warm = np.array([np.abs(warm["u"][k] - ref["u"][k]).max() for k in range(n_test)])
-        out["fp64_reference"] = {
-            "converged": int(okr.sum()), "wall_s_all": ref["wall_s"], "steps_all": ref["steps"],
-            "face_steps_per_s": F_faces * ref["steps"] / ref["wall_s"],
-            "fp32_face_steps_per_s": F_faces * plain["steps"] / plain["wall_s"],
-            "plain_fp32_within_1e-4": float(np.mean(d_plain[okr] < 1e-4)),
-            "warm_fp32_within_1e-4": float(np.mean(d_warm[okr] < 1e-4)),
-            "max_dev_plain": float(d_plain[okr].max()) if okr.any() else None,
+    V3 = U_pred.shape[1]
+    res = {}
+    variants = [("fp64", dict(precision=L.PREC_FP64, tol=tol, max_steps=max_steps))]
+    if mixed:
+        variants.append(("fp32+fp64", dict(precision=L.PREC_FP32, tol=gen_tol, max_steps=gen_max, polish_tol=tol,
+                                           polish_max=max_steps)))
+    for name, kw in variants:
+        plain = solve(test, np.zeros((n_test, V3)), level, **kw)
+        warm = solve(test, U_pred, level, **kw)
+        base = plain["steps"] >= 0
+        fb = warm["steps"] < 0
+        warm_steps = np.where(fb, np.where(base, plain["steps"] + max_steps, -1), warm["steps"])
+        dev = np.array([np.abs(drop_drift(warm["u"][k]) - drop_drift(plain["u"][k])).max() for k in range(n_test)])
+        res[name] = {
+            "plain": {"converged": int(base.sum()), **_stats(plain["steps"], base), "wall_s": plain["wall_s"],
+                      "phases": plain["phases"]},
+            "warm": {"converged": int((~fb).sum()), "fallbacks": int((fb & base).sum()),
+                     **_stats(warm_steps, base), "wall_s": warm["wall_s"] + pred_s, "phases": warm["phases"]},
+            "warm_vs_plain_equilibrium_within_1e-4": float(np.mean(dev[base & ~fb] < 1e-4)) if (base & ~fb).any()
+            else None,
+            "max_dev": float(dev[base & ~fb].max()) if (base & ~fb).any() else None,
         }
-    out["total_wall_s"] = time.perf_counter() - t0
+        res[name]["u_plain"] = plain["u"]
+        if name == "fp64":
+            err = np.array([np.abs(drop_drift(U_pred[k]) - drop_drift(plain["u"][k])).max() / ht[k]
+                            for k in range(n_test)])
+            res[name]["prediction_error_over_h"] = {"median": float(np.median(err[base])) if base.any() else None,
+                                                    "max": float(err[base].max()) if base.any() else None}
+        if log:
+            log("%s: plain median %s, warm median %s" % (name, res[name]["plain"]["median_steps"],
+                                                         res[name]["warm"]["median_steps"]))
+    if mixed:
+        ref = res["fp64"].pop("u_plain")
+        mix = res["fp32+fp64"].pop("u_plain")
+        dev = np.array([np.abs(drop_drift(mix[k]) - drop_drift(ref[k])).max() for k in range(n_test)])
+        res["fp32+fp64"]["plain_vs_fp64_plain_within_1e-4"] = float(np.mean(dev < 1e-4))
+    else:
+        res["fp64"].pop("u_plain")
+    out["test"] = res
+    out["prediction_wall_s"] = pred_s
+    out["total_wall_s"] = time.perf_counter() - t_all
     return out

@@ -95,7 +95,7 @@ def test_mesh_transforms(driver, tmp_path):
     assert d["nodes"] == 2562 and d["faces"] == 5120
 
 
-@pytest.mark.parametrize("bad", ["shell_cavity_contact = true", "adapt_dt_every = 1", "shell_shell_contact = smooth",
+@pytest.mark.parametrize("bad", ["shell_cavity_contact = true", "shell_shell_contact = smooth",
                                  "thickness = 0.01*(1+t)", "gravity = 9.81", "pressure = 2*", "extra_order = 1"])
 def test_unsupported_options_fail(driver, tmp_path, bad):
     c, m = _write(tmp_path, BASE_CFG + bad + "\n")
@@ -174,4 +174,30 @@ def test_run_resume_and_match_binding(driver, cuda_ok, tmp_path):
     step, dt, _, rows = g3.load_state_file(os.path.join(d2, "shell_state0000000060.dat"))
     assert step == 60 and dt == 1e-4
     for x, y in zip(g.get_state(), g3.get_state()):
+        assert np.array_equal(x, y)
+
+
+@pytest.mark.gpu
+def test_run_adaptive_dt_matches_binding(driver, cuda_ok, tmp_path):
+    cfg = BASE_CFG + "adapt_dt_every = 1\ndt = 2e-2\nrel_loc_err_min = 5e-5\nrel_loc_err_max = 5e-4\n" \
+                     "pressure = -1e-3*min(1, t/0.5)\ndata_time = 0.05\nvtk_time = 0\nstate_time = 0\ntime_steps = 30\n"
+    c, m = _write(tmp_path, cfg)
+    d1 = str(tmp_path / "d1")
+    rc, out = _run(driver, "-c", c, "-m", m, "-d", d1)
+    assert rc == 0, out
+    X, T = L.icosphere(3)
+    p = L.default_params(shell_mass_density=1.0, shell_young_modulus=1.0, shell_young_modulus2=0.5,
+                         shell_poisson_ratio=0.3, shell_shear_modulus=0.35, thickness=0.01, damping_alpha=0.05,
+                         dt=2e-2, shell_shell_contact=L.CONTACT_NONE, adapt_dt_every=1, rel_loc_err_min=5e-5,
+                         rel_loc_err_max=5e-4)
+    rng = Drand48(7)
+    u0 = np.array([0.1 * (2 * rng() - 1) * 0.01 for _ in range(3 * X.shape[0])])
+    g = L.Shell(X, T, p)
+    g.set_pressure_function("-1e-3*min(1, t/0.5)")
+    g.apply_initial_conditions(u0, 0.0, -1e-3 * min(1, 2e-2 / 0.5))
+    g.step(30, None)
+    g2 = L.Shell(X, T, p)
+    step, dt, _, _ = g2.load_state_file(os.path.join(d1, "shell_state0000000030.dat"))
+    assert step == 30 and dt == g.dt()[0]
+    for x, y in zip(g.get_state(), g2.get_state()):
         assert np.array_equal(x, y)

@@ -1,6 +1,7 @@
 """Relative residual ||f_ext - f_int|| / ||f_ext|| (shl_residual), single shells
 and batches, against the CPU oracle: f from an oracle force evaluation
-without self-contact, f_ext from one with the stiffness multipliers set to 0.
+without self-contact, f_ext from one with the stiffness multipliers set to 0,
+both without their rigid-translation part (resultant spread by nodal mass).
 Tolerance 1e-10 relative on the residual in FP64 (norms of 1e-12-accurate
 vectors); in FP32 the residual of an equilibrium is only resolved down to the
 FP32 force error (about 1e-6 of the force scale)."""
@@ -24,6 +25,13 @@ def _oracle_residual(X, T, p, u, pressure):
     o2 = O.Oracle(X, T, q, threads=4)
     o2.set_state(u, np.zeros_like(u), np.zeros_like(u))
     fe = o2.eval_forces(u, np.zeros_like(u), pressure)[0]
+    m = 1.0 / o.mass_damping()[0].reshape(-1, 3)[:, :1]
+
+    def drop_translation(x):  # the resultant spread over the nodes by mass
+        x = x.reshape(-1, 3)
+        return (x - m * (x.sum(0) / m.sum())).reshape(-1)
+
+    f, fe = drop_translation(f), drop_translation(fe)
     return np.linalg.norm(f) / np.linalg.norm(fe), f, fe
 
 
@@ -67,10 +75,10 @@ def test_residual_fp64_in_fp32_context_and_defect_correction(cuda_ok):
     its relaxation reaches the FP64 residual tolerance and the FP64
     equilibrium, which plain FP32 relaxation cannot."""
     meshes = [L.icosphere(3), L.icosphere(3)]
-    ps32 = [physics_params(contact=False, damping_alpha=1.5, dt=2e-3, precision=L.PREC_FP32, thickness=h)
+    ps32 = [physics_params(contact=False, damping_alpha=1.5, dt=4e-3, precision=L.PREC_FP32, thickness=h)
             for h in (0.01, 0.02)]
-    ps64 = [physics_params(contact=False, damping_alpha=1.5, dt=2e-3, thickness=h) for h in (0.01, 0.02)]
-    scale = np.array([0.5 * classical_pressure(h=0.01), 0.5 * classical_pressure(h=0.02)])
+    ps64 = [physics_params(contact=False, damping_alpha=1.5, dt=4e-3, thickness=h) for h in (0.01, 0.02)]
+    scale = np.array([0.2 * classical_pressure(h=0.01), 0.2 * classical_pressure(h=0.02)])
     rng = np.random.default_rng(6)
     u = 1e-3 * rng.standard_normal(2 * meshes[0][0].size)
     b32, b64 = L.Batch(meshes, ps32, scale), L.Batch(meshes, ps64, scale)

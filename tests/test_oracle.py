@@ -330,3 +330,28 @@ def test_oracle_step_conserves_free_flight(mesh3):
     u, v, a = o.get_state()
     assert np.allclose(u, 10 * p.dt * v0, rtol=1e-12, atol=1e-18)
     assert np.allclose(v, v0, rtol=1e-12)
+
+
+def test_oracle_adaptive_dt_grows_and_rejects():
+    """Adaptive time stepping (ShellSystem.C:1010-1044, 1104-1117): a too-small
+    dt grows by (target/err)^(1/3) until the error estimate is inside the band;
+    a too-large one is rejected and retried smaller; the accepted steps' dt sum
+    to the simulated time."""
+    import numpy as np
+    from shell_gb300 import lib as L
+    from tests.common import classical_pressure, physics_params
+    X, T = L.icosphere(3)
+    u0 = L.gaussian_normal_imperfection(X, 1e-3, 0).reshape(-1)
+    final = []
+    for dt0 in (1e-6, 5e-2):
+        p = physics_params(contact=False, dt=dt0, adapt_dt_every=1, rel_loc_err_min=5e-5, rel_loc_err_max=5e-4)
+        o = O.Oracle(X, T, p, threads=4)
+        o.apply_initial_conditions(u0, 0.0, -classical_pressure())
+        rep, st = o.step(30, np.full(30, -classical_pressure()))
+        assert rep.steps_done == 30 and st < 3
+        assert abs(rep.sum_dt - o.get_time()[0]) <= 1e-15 * o.get_time()[0]
+        final.append((o.dt(), o.rejections()))
+    (dt_a, rej_a), (dt_b, rej_b) = final
+    assert dt_a > 100 * 1e-6          # grew from a too-small step
+    assert rej_b >= 1                 # a too-large first step was repeated
+    assert 0.5 < dt_a / dt_b < 2.0    # both settle where the error estimate is inside the band
