@@ -116,7 +116,19 @@ typedef struct shl_params {
   double dt_max;            /* 0 = unbounded */
   double rel_loc_err_min;
   double rel_loc_err_max;
+  /* cavity contact (ShellSystem.C:1600-1723): the shell is kept inside a box,
+   * a cylinder (axis x) or an ellipsoid of semi-axes Rx, Ry, Rz, with linear
+   * penalty contact, normal damping and Coulomb friction per node */
+  int32_t shell_cavity_contact;
+  int32_t cavity;         /* SHL_CAVITY_* */
+  double Rx, Ry, Rz;      /* constant semi-axes; see shl_set_cavity_functions */
+  double mu_s_cavity, mu_d_cavity;
+  double cavity_damping;
+  double cavity_friction_damping;
 } shl_params;
+
+/* ShellSystem::CavityType (ShellSystem.h:44). */
+enum { SHL_CAVITY_BOX = 0, SHL_CAVITY_CYLINDER = 1, SHL_CAVITY_ELLIPSOID = 2 };
 
 /* Scalars measured in a step (ShellSystem.C:2686-2846). */
 typedef struct shl_energies {
@@ -127,6 +139,10 @@ typedef struct shl_energies {
   double kGauss, kMean;   /* integrated curvatures */
   uint32_t Nc;            /* contacts with penetration */
   uint32_t n_pairs;       /* contact candidates in the list */
+  double Ecav;            /* cavity contact energy */
+  double cavity_force;    /* sum of the cavity normal forces */
+  uint32_t Nc_cav;        /* nodes penetrating the cavity */
+  uint32_t pad;
 } shl_energies;
 
 /* Summary of shl_step(). */
@@ -143,6 +159,8 @@ typedef struct shl_step_report {
       sum_Eself, sum_Efric, sum_kGauss, sum_kMean;
   uint32_t stopped;        /* the stopping criterion became true (shl_set_stop_function) */
   uint32_t pad;
+  /* dt-weighted sums of the cavity measurements (pcav = force / cavity surface) */
+  double sum_pcav, sum_Nc_cav, sum_Ecav;
 } shl_step_report;
 
 typedef struct shl_ctx shl_ctx;
@@ -292,6 +310,17 @@ shl_status shl_residual(shl_ctx* ctx, double pressure, int flags, double* rel, d
 shl_status shl_set_pressure_function(shl_ctx* ctx, const char* expr);
 shl_status shl_eval_pressure_function(shl_ctx* ctx, const double* t, uint32_t n, double* out);
 
+/* Cavity semi-axes as config expressions of t (Rx, Ry, Rz of config.cfg),
+ * evaluated by the device at each step's time (ShellSystem.C:194-196,
+ * 421-470); NULL or "" keeps the constant of the parameters. */
+shl_status shl_set_cavity_functions(shl_ctx* ctx, const char* rx, const char* ry, const char* rz);
+
+/* Static-friction spring origins of the cavity contacts, 3 per node (the
+ * NodeCache::spring_origin of save/load, ShellSystem.C:2976-2980, 3073-3076);
+ * zeros without cavity contact. */
+shl_status shl_get_cavity_origins(shl_ctx* ctx, double* origins);
+shl_status shl_set_cavity_origins(shl_ctx* ctx, const double* origins);
+
 /* The current time step (adaptive dt: the next attempt's) and the repeated
  * attempts since the last report. */
 shl_status shl_get_dt(shl_ctx* ctx, double* dt, uint32_t* rejections);
@@ -311,9 +340,8 @@ shl_status shl_context_mesh(shl_ctx* ctx, double* xyz /* 3V */, uint32_t* faces 
 
 /* Per-node measurement vectors of the last step (node_vectors of
  * ShellSystem.C:126-130): kinetic energy density (Ekin_node / mean area of the
- * incident faces, 2796-2812), cavity-contact energy density (always 0: cavity
- * contact is not modelled), self-contact and friction energy densities
- * (1862-1877) and nodal mass.  V values each; any pointer may be NULL. */
+ * incident faces, 2796-2812), cavity-contact energy density (1630), self-contact
+ * and friction energy densities (1699, 1862-1877) and nodal mass.  V values each; any pointer may be NULL. */
 shl_status shl_get_node_fields(shl_ctx* ctx, double* ekin, double* ecav, double* eself, double* efric,
                                double* mass);
 

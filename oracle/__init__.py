@@ -58,6 +58,8 @@ def load():
         "oracle_get_node_fields": (ctypes.c_int, [vp, vp, vp, vp]),
         "oracle_set_pressure_function": (ctypes.c_int, [vp, ctypes.c_char_p]),
         "oracle_get_dt": (d, [vp]),
+        "oracle_set_cavity_functions": (ctypes.c_int, [vp, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p]),
+        "oracle_get_cavity": (ctypes.c_int, [vp, vp, vp, vp]),
         "oracle_get_rejections": (ctypes.c_uint64, [vp]),
         "oracle_patch": (ctypes.c_int, [vp, u32, vp, ctypes.POINTER(u32)]),
         "oracle_basis_at": (ctypes.c_int, [vp, u32, d, d, vp]),
@@ -191,6 +193,16 @@ class Oracle:
 
     def dt(self):
         return self.lib.oracle_get_dt(self.h)
+
+    def set_cavity_functions(self, rx=None, ry=None, rz=None):
+        enc = lambda e: None if e is None else e.encode()  # noqa: E731
+        if self.lib.oracle_set_cavity_functions(self.h, enc(rx), enc(ry), enc(rz)) != 0:
+            raise RuntimeError(self.lib.oracle_error().decode())
+
+    def cavity(self):
+        o, e, t = np.zeros(3 * self.V), np.zeros(self.V), np.zeros(3)
+        self.lib.oracle_get_cavity(self.h, o.ctypes.data, e.ctypes.data, t.ctypes.data)
+        return {"origins": o, "ecav": e, "Ecav": t[0], "cavity_force": t[1], "Nc_cav": int(t[2])}
 
     def rejections(self):
         return int(self.lib.oracle_get_rejections(self.h))

@@ -46,6 +46,10 @@ int oracle_rebuild_contacts(oracle* o);
 int oracle_get_mass_damping(oracle* o, double* Minv, double* C);
 /* Pressure as a config expression of t (evaluated each attempt); NULL or "" = table. */
 int oracle_set_pressure_function(oracle* o, const char* expr);
+/* Cavity semi-axes as expressions of t (NULL/"" = the constants of the parameters). */
+int oracle_set_cavity_functions(oracle* o, const char* rx, const char* ry, const char* rz);
+/* Cavity spring origins (3V), cavity energy densities (V) and (Ecav, cavity force, Nc_cav). */
+int oracle_get_cavity(oracle* o, double* origins, double* ecav, double* out3);
 /* Current time step size (adaptive dt) and the number of repeated steps so far. */
 double oracle_get_dt(oracle* o);
 uint64_t oracle_get_rejections(oracle* o);

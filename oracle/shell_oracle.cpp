@@ -323,7 +323,16 @@ struct oracle {
   unsigned Nc = 0;
   Real Eself = 0, Efric = 0, Etens = 0, Ebend = 0, Ekin = 0, kGauss = 0, kMean = 0;
   // node_vectors ekin, eself, efric (ShellSystem.C:126-130), reset every step
-  std::vector<Real> ekin_vec, eself_vec, efric_vec;
+  std::vector<Real> ekin_vec, eself_vec, efric_vec, ecav_vec;
+  // cavity contact (ShellSystem.C:1600-1723): spring origins per node, measurements
+  std::vector<Point> cav_origin;
+  std::vector<std::vector<unsigned>> vertex_faces;  // faces of which each node is a vertex
+  unsigned Nc_cav = 0;
+  Real Ecav = 0, cavity_force = 0;
+  Real cav_R[3] = {0, 0, 0};
+  shl::expr::Expression rfun[3];
+  bool has_rfun[3] = {false, false, false};
+  void add_cavity_force();
   int current_problem = 0;
 
   ~oracle() {
@@ -713,6 +722,10 @@ bool oracle::build(const shl_mesh* m, const shl_params* prm) {
     const uint64_t nc = (uint64_t)std::ceil(std::sqrt((double)F) / P.cell_size_mult);
     n_cells_max = nc * nc * nc;
   }
+  vertex_faces.assign(V, {});
+  for (unsigned e = 0; e < F; ++e)
+    for (int q = 0; q < 3; ++q) vertex_faces[tri[3 * e + q]].push_back(e);
+  cav_origin.assign(V, Point());
   set_newmark_parameters(P.dt);
   update_derived();
 
@@ -753,6 +766,9 @@ void oracle::reset_properties() {
   for (ElemCache& c : ec) c.kGauss = c.kMean = c.etens = c.ebend = 0;
   Nc = 0;
   Eself = Efric = Etens = Ebend = 0;
+  Nc_cav = 0;
+  Ecav = cavity_force = 0;
+  ecav_vec.assign(V, 0.0);
   ekin_vec.assign(V, 0.0);
   eself_vec.assign(V, 0.0);
   efric_vec.assign(V, 0.0);
@@ -923,7 +939,102 @@ void oracle::compute_external_force() {
       }
     }
   }
+  if (P.shell_cavity_contact) add_cavity_force();
   if (P.shell_shell_contact != SHL_CONTACT_NONE) add_shell_shell_contact_force();
+}
+
+// interaction with the cavity, ShellSystem.C:1600-1723, with update_derived's
+// cavity quantities (421-436) at the current semi-axes
+void oracle::add_cavity_force() {
+  for (int c = 0; c < 3; ++c)
+    cav_R[c] = has_rfun[c] ? rfun[c].eval({{"t", time}, {"d", 0.0}}) : (c == 0 ? P.Rx : c == 1 ? P.Ry : P.Rz);
+  const Real h_half = 0.5 * P.thickness;
+  const Real Rx_eff = cav_R[0] - h_half, Ry_eff = cav_R[1] - h_half, Rz_eff = cav_R[2] - h_half;
+  const Real avg_R_eff = (Rx_eff + Ry_eff + Rz_eff) / 3;
+  const Real inv_R2_eff[3] = {1 / (Rx_eff * Rx_eff), 1 / (Ry_eff * Ry_eff), 1 / (Rz_eff * Rz_eff)};
+  const Real one_plus_delta_friction = std::pow(1 - P.static_friction_tol * P.thickness / avg_R_eff, 2);
+  const bool cavity_friction = P.mu_s_cavity != 0 || P.mu_d_cavity != 0;
+  unsigned Nc_cav_sum = 0;
+  Real Efric_sum = 0, Ecav_sum = 0, cavity_force_sum = 0;
+  if (cav_origin.size() != V) cav_origin.assign(V, Point());
+#pragma omp parallel for reduction(+ : Nc_cav_sum, Efric_sum, Ecav_sum, cavity_force_sum)
+  for (int nid = 0; nid < (int)V; ++nid) {
+    const Point& pp = p[nid];
+    Real x_red = pp(0) / Rx_eff, y_red = pp(1) / Ry_eff, z_red = pp(2) / Rz_eff;
+    x_red = x_red * x_red;
+    y_red = y_red * y_red;
+    z_red = z_red * z_red;
+    Real one_plus_delta;  // cavity_isoparameter, ShellSystem.h:336-362
+    if (P.cavity == SHL_CAVITY_BOX)
+      one_plus_delta = std::max(x_red, std::max(y_red, z_red));
+    else if (P.cavity == SHL_CAVITY_CYLINDER)
+      one_plus_delta = std::max(x_red, y_red + z_red);
+    else
+      one_plus_delta = x_red + y_red + z_red;
+    if (one_plus_delta > one_plus_delta_friction) {
+      const Real depth = avg_R_eff * (std::sqrt(one_plus_delta) - 1);
+      Real area_node = 0;  // avg_area_node, ShellSystem.C:2462-2481
+      for (unsigned e : vertex_faces[nid]) area_node += ec[e].area;
+      area_node /= vertex_faces[nid].size();
+      const Real stiffness = stiff_density * area_node;
+      Real f_normal = 0;
+      if (depth > 0) {
+        ++Nc_cav_sum;
+        const Real Ecav_node = 0.5 * stiffness * depth * depth;
+        Ecav_sum += Ecav_node;
+        ecav_vec[nid] += Ecav_node / area_node;
+        f_normal = stiffness * depth;
+        cavity_force_sum += f_normal;
+      }
+      Point n;
+      const Real xr = pp(0) * pp(0) * inv_R2_eff[0], yr = pp(1) * pp(1) * inv_R2_eff[1],
+                 zr = pp(2) * pp(2) * inv_R2_eff[2];
+      auto sgn = [](Real x) { return (Real)((x > 0) - (x < 0)); };
+      if (P.cavity == SHL_CAVITY_BOX) {
+        if (xr > yr && xr > zr)
+          n(0) = sgn(pp(0));
+        else if (yr > zr)
+          n(1) = sgn(pp(1));
+        else
+          n(2) = sgn(pp(2));
+      } else if (P.cavity == SHL_CAVITY_CYLINDER) {
+        if (xr > yr + zr) {
+          n(0) = sgn(pp(0));
+        } else {
+          n(1) = pp(1) * inv_R2_eff[1];
+          n(2) = pp(2) * inv_R2_eff[2];
+        }
+      } else {
+        n(0) = pp(0) * inv_R2_eff[0];
+        n(1) = pp(1) * inv_R2_eff[1];
+        n(2) = pp(2) * inv_R2_eff[2];
+      }
+      n = n * (1 / n.size());
+      const Point vel(v[dof(nid, 0)], v[dof(nid, 1)], v[dof(nid, 2)]);
+      const Real abs_v_normal = vel * n;
+      Point f_contact;
+      if (cavity_friction) {
+        Real Efric_node = 0;
+        int stick = cav_origin[nid].size_sq() != 0 ? 1 : 0;
+        shl_friction_apply(&Efric_node, f_contact.x, f_normal, n.x, vel.x, abs_v_normal, P.friction_stop_velocity,
+                           stiff_static_friction, P.mu_s_cavity, P.mu_d_cavity, P.cavity_friction_damping, &stick,
+                           cav_origin[nid].x, pp.x);
+        Efric_sum += Efric_node;
+        efric_vec[nid] += Efric_node / area_node;
+      }
+      f_normal += P.cavity_damping * stiffness * abs_v_normal;
+      f_contact -= f_normal * n;
+      f[dof(nid, 0)] += f_contact(0);
+      f[dof(nid, 1)] += f_contact(1);
+      f[dof(nid, 2)] += f_contact(2);
+    } else {
+      cav_origin[nid].zero();
+    }
+  }
+  Nc_cav += Nc_cav_sum;
+  Efric += Efric_sum;
+  Ecav += Ecav_sum;
+  cavity_force += cavity_force_sum;
 }
 
 void oracle::add_shell_shell_contact_force() {
@@ -1402,7 +1513,7 @@ static void fill_energies(const oracle* o, shl_energies* e) {
   if (!e) return;
   e->Etens = o->Etens; e->Ebend = o->Ebend; e->Eself = o->Eself; e->Efric = o->Efric;
   e->Ekin = o->Ekin; e->area = o->area; e->volume = o->volume;
-  e->kGauss = o->kGauss; e->kMean = o->kMean; e->Nc = o->Nc;
+  e->kGauss = o->kGauss; e->kMean = o->kMean; e->Nc = o->Nc; e->Ecav = o->Ecav; e->cavity_force = o->cavity_force; e->Nc_cav = o->Nc_cav;
   unsigned n = 0;
   for (const Contact* c : o->candidates) n += c != nullptr;
   e->n_pairs = n;
@@ -1429,6 +1540,19 @@ int oracle_eval_forces(oracle* o, const double* u_pred, const double* v_pred, do
   o->area = area;
   fill_energies(o, e);
   return o->current_problem;
+}
+
+// cavity surface, ShellSystem.C:441-468
+static Real cavity_surface(const Real* R, int type) {
+  const Real Rx = R[0], Ry = R[1], Rz = R[2];
+  const Real pi = 3.141592653589793238;
+  if (type == SHL_CAVITY_BOX) return 8 * (Rx * Ry + Rx * Rz + Ry * Rz);
+  if (type == SHL_CAVITY_CYLINDER) {
+    const Real lambda = (Ry - Rz) / (Ry + Rz);
+    const Real lambda32 = 3 * lambda * lambda;
+    return 2 * pi * ((Ry + Rz) * (1 + lambda32 / (10 + std::sqrt(4 - lambda32))) + Ry * Rz);
+  }
+  return 4 * pi * std::pow((std::pow(Rx * Ry, 1.6) + std::pow(Rx * Rz, 1.6) + std::pow(Ry * Rz, 1.6)) / 3, 0.625);
 }
 
 int oracle_step(oracle* o, uint32_t n_steps, const double* pressure_table, shl_step_report* r) {
@@ -1460,6 +1584,11 @@ int oracle_step(oracle* o, uint32_t n_steps, const double* pressure_table, shl_s
       rep.sum_Efric += dt * o->Efric;
       rep.sum_kGauss += dt * o->kGauss;
       rep.sum_kMean += dt * o->kMean;
+      if (o->P.shell_cavity_contact) {
+        rep.sum_pcav += dt * o->cavity_force / cavity_surface(o->cav_R, o->P.cavity);
+        rep.sum_Nc_cav += dt * o->Nc_cav;
+        rep.sum_Ecav += dt * o->Ecav;
+      }
     } else {
       --o->time_step;
     }
@@ -1487,6 +1616,35 @@ int oracle_set_pressure_function(oracle* o, const char* expr) {
     return -1;
   }
   o->has_pfun = true;
+  return 0;
+}
+
+int oracle_set_cavity_functions(oracle* o, const char* rx, const char* ry, const char* rz) {
+  const char* ex[3] = {rx, ry, rz};
+  for (int k = 0; k < 3; ++k) {
+    o->has_rfun[k] = ex[k] && *ex[k];
+    if (!o->has_rfun[k]) continue;
+    try {
+      o->rfun[k] = shl::expr::Expression(ex[k]);
+    } catch (const std::exception& e) {
+      g_err = e.what();
+      return -1;
+    }
+  }
+  return 0;
+}
+
+int oracle_get_cavity(oracle* o, double* origins, double* ecav, double* out3) {
+  for (unsigned n = 0; n < o->V; ++n) {
+    if (origins)
+      for (int c = 0; c < 3; ++c) origins[3 * n + c] = n < o->cav_origin.size() ? o->cav_origin[n](c) : 0.0;
+    if (ecav) ecav[n] = n < o->ecav_vec.size() ? o->ecav_vec[n] : 0.0;
+  }
+  if (out3) {
+    out3[0] = o->Ecav;
+    out3[1] = o->cavity_force;
+    out3[2] = o->Nc_cav;
+  }
   return 0;
 }
 

@@ -65,6 +65,8 @@ struct shl_ctx {
   double* qe64 = nullptr;                    // FP64 element shares of an FP32 context (shl_residual)
   shl::expr::Op* d_pfun = nullptr;           // compiled pressure expression (device)
   shl::expr::Op* d_sfun = nullptr;           // compiled stopping criterion (device)
+  shl::expr::Op* d_rfun = nullptr;           // compiled cavity semi-axes (device), 3 programs
+  std::string rfun_text[3];                  // the same, for evaluations started by the host
   double* f32 = nullptr;                     // FP32 force at the checked state (defect correction)
 };
 
@@ -143,6 +145,20 @@ bool validate(const shl_params& p, std::string& err) {
     if (!(p.friction_stop_velocity > 0)) { err = "friction_stop_velocity must be > 0"; return false; }
   }
   if (p.precision != SHL_PREC_FP64 && p.precision != SHL_PREC_FP32) { err = "bad precision"; return false; }
+  if (p.shell_cavity_contact) {
+    // ShellSystem.C:373-380
+    if (p.cavity < SHL_CAVITY_BOX || p.cavity > SHL_CAVITY_ELLIPSOID) { err = "bad cavity"; return false; }
+    if (p.mu_s_cavity < 0 || p.mu_d_cavity < 0 || p.cavity_damping < 0 || p.cavity_friction_damping < 0 ||
+        p.static_friction_tol < 0) {
+      err = "cavity coefficients must be >= 0";
+      return false;
+    }
+    if (!(p.Rx > 0.5 * p.thickness && p.Ry > 0.5 * p.thickness && p.Rz > 0.5 * p.thickness)) {
+      err = "cavity semi-axes must exceed half the thickness";
+      return false;
+    }
+    if (!(p.friction_stop_velocity > 0)) { err = "friction_stop_velocity must be > 0"; return false; }
+  }
   if (p.adapt_dt_every > 0) {
     // ShellSystem.C:300-313
     if (!(p.rel_loc_err_min >= 0) || !(p.rel_loc_err_max > p.rel_loc_err_min)) {
@@ -285,6 +301,15 @@ shl_status build_graph(shl_ctx* c, uint32_t steps, cudaGraphExec_t* out) {
   return SHL_ERR_CUDA;
 }
 
+// cavity semi-axes at time t as the device computes them (functions or constants)
+void cavity_axes_host(const shl_ctx* c, double t, double* R) {
+  const double R0[3] = {c->P.Rx, c->P.Ry, c->P.Rz};
+  for (int k = 0; k < 3; ++k) {
+    R[k] = R0[k];
+    if (!c->rfun_text[k].empty()) R[k] = shl::expr::Expression(c->rfun_text[k]).eval({{"t", t}, {"d", 0.0}});
+  }
+}
+
 // newmark_a of dt (ShellSystem.C:744-759) into the control block
 void set_newmark_host(Ctl& h, double dt, double beta, double gamma) {
   h.dt_cur = dt;
@@ -305,6 +330,7 @@ void fill_energies(const Ctl& h, shl_energies* e) {
   e->Etens = h.Etens; e->Ebend = h.Ebend; e->Eself = h.Eself; e->Efric = h.Efric; e->Ekin = h.Ekin;
   e->area = h.area; e->volume = h.volume; e->kGauss = h.kGauss; e->kMean = h.kMean;
   e->Nc = h.Nc; e->n_pairs = h.n_pairs;
+  e->Ecav = h.Ecav; e->cavity_force = h.cavity_force; e->Nc_cav = h.Nc_cav;
 }
 
 }  // namespace
@@ -350,6 +376,11 @@ shl_status create_common(shl_ctx* c, const std::vector<double>& pscale_orig, shl
   ALLOC(b.X, nd); ALLOC(b.u, nd); ALLOC(b.v, nd); ALLOC(b.a, nd); ALLOC(b.up, nd); ALLOC(b.vp, nd);
   ALLOC(b.p, nd); ALLOC(b.Minv, nd); ALLOC(b.C, nd); ALLOC(b.M, nd);
   if (params->adapt_dt_every) ALLOC(b.ap, nd);
+  if (params->shell_cavity_contact) {
+    ALLOC(b.cav_origin, nd);
+    ALLOC(b.cav_ecav, V);
+    ALLOC(b.cav_efric, V);
+  }
   ALLOC(b.face, (size_t)FF_COUNT * F);
   ALLOC(b.patch, 12 * (size_t)F);
   const bool fp32 = params->precision == SHL_PREC_FP32;
@@ -513,11 +544,25 @@ shl_status create_common(shl_ctx* c, const std::vector<double>& pscale_orig, shl
   sc.err_target = std::sqrt(p.rel_loc_err_min * p.rel_loc_err_max);
   sc.dt_min_eff = std::max(p.dt_min, 2.220446049250313e-16);
   sc.dt_max_eff = p.dt_max <= 0 ? SHL_DBL_MAX : p.dt_max;
+  sc.cavity_contact = p.shell_cavity_contact ? 1 : 0;
+  sc.cavity_type = p.cavity;
+  sc.cavity_friction = (p.shell_cavity_contact && (p.mu_s_cavity != 0 || p.mu_d_cavity != 0)) ? 1 : 0;
+  sc.cav_R[0] = p.Rx;
+  sc.cav_R[1] = p.Ry;
+  sc.cav_R[2] = p.Rz;
+  sc.mu_s_cav = p.mu_s_cavity;
+  sc.mu_d_cav = p.mu_d_cavity;
+  sc.cav_damping = p.cavity_damping;
+  sc.cav_fric_damping = p.cavity_friction_damping;
+  sc.static_friction_tol = p.static_friction_tol;
 
   Ctl h;
   std::memset(&h, 0, sizeof(h));
   set_newmark_host(h, p.dt, p.newmark_beta, p.newmark_gamma);
   h.steps_target = ~0u;
+  h.cav_R[0] = p.Rx;
+  h.cav_R[1] = p.Ry;
+  h.cav_R[2] = p.Rz;
   if ((st = ctl_put(c, h)) != SHL_OK) return fail(st);
   if (cudaMallocHost(&c->h_pin, 3 * nd * sizeof(double)) != cudaSuccess) c->h_pin = nullptr;
   if ((st = check_launch("shl_create")) != SHL_OK) return fail(st);
@@ -656,6 +701,7 @@ shl_status begin_eval(shl_ctx* c, double pressure, bool allow_rebuild) {
   const double red = std::max((1.0 - static_cast<int>(h.time * 5.0) * 0.01), 0.5);
   if (h.time_step == 2) h.volume0 = h.volume;
   h.volume_pressure = (c->P.bulk_modulus == 0 ? 0 : c->P.bulk_modulus * (h.volume0 * red / h.volume - 1));
+  cavity_axes_host(c, h.time, h.cav_R);
   if (allow_rebuild && c->sc.contact) {
     const double tol = c->P.cell_margin * (c->P.cell_size_mult * h.avg_elem_size);
     h.rebuild = h.du_sum >= tol ? 1u : 0u;
@@ -780,6 +826,7 @@ shl_status reset_report(shl_ctx* c) {
   h.n_rebuilds = 0;
   h.rejections = 0;
   h.paused = 0;
+  h.sum_pcav = h.sum_Nc_cav = h.sum_Ecav = 0;
   h.steps_target = ~0u;
   h.sum_dt = h.sum_area = h.sum_volume = h.sum_Nc = h.sum_Ekin = h.sum_Etens = h.sum_Ebend = h.sum_Eself =
       h.sum_Efric = h.sum_kGauss = h.sum_kMean = 0;
@@ -826,6 +873,7 @@ shl_status collect(shl_ctx* c, shl_step_report* report) {
     report->du_sum = h.du_sum;
     report->n_rebuilds = h.n_rebuilds;
     report->rejections = h.rejections;
+    report->sum_pcav = h.sum_pcav; report->sum_Nc_cav = h.sum_Nc_cav; report->sum_Ecav = h.sum_Ecav;
     report->stopped = (h.paused & 2u) ? 1u : 0u;
     fill_energies(h, &report->last);
     report->sum_dt = h.sum_dt; report->sum_area = h.sum_area; report->sum_volume = h.sum_volume;
@@ -881,6 +929,62 @@ shl_status shl_step(shl_ctx* c, uint32_t n_steps, const double* pressure_table, 
     if (hh.paused & 2u) stop = true;
   }
   return collect(c, report);
+}
+
+shl_status shl_set_cavity_functions(shl_ctx* c, const char* rx, const char* ry, const char* rz) {
+  if (!c) return SHL_ERR_ARG;
+  if (!c->sc.cavity_contact) {
+    g_err = "cavity contact is off";
+    return SHL_ERR_ARG;
+  }
+  const char* ex[3] = {rx, ry, rz};
+  std::vector<shl::expr::Op> prog[3];
+  for (int k = 0; k < 3; ++k) {
+    if (!ex[k] || !*ex[k]) continue;
+    try {
+      shl::expr::Expression e(ex[k]);
+      if (e.size() != 1) throw std::runtime_error("one expression expected");
+      if (e.uses("x") || e.uses("y") || e.uses("z")) throw std::runtime_error("semi-axes may depend on t and d only");
+      prog[k] = e.compile();
+    } catch (const std::exception& x) {
+      g_err = x.what();
+      return SHL_ERR_ARG;
+    }
+  }
+  if (!c->d_rfun) SHL_TRY(dev_alloc(c, &c->d_rfun, 3 * (size_t)shl::expr::kMaxProgram));
+  for (int k = 0; k < 3; ++k) {
+    c->rfun_text[k] = prog[k].empty() ? std::string() : std::string(ex[k]);
+    c->sc.rfun[k] = prog[k].empty() ? nullptr : c->d_rfun + k * shl::expr::kMaxProgram;
+    c->sc.rfun_len[k] = (int32_t)prog[k].size();
+    if (!prog[k].empty())
+      SHL_CUDA_TRY(cudaMemcpyAsync(c->d_rfun + k * shl::expr::kMaxProgram, prog[k].data(),
+                                   prog[k].size() * sizeof(shl::expr::Op), cudaMemcpyHostToDevice, c->stream));
+  }
+  SHL_CUDA_TRY(cudaStreamSynchronize(c->stream));
+  if (c->graph) cudaGraphExecDestroy(c->graph);
+  if (c->graph1) cudaGraphExecDestroy(c->graph1);
+  c->graph = c->graph1 = nullptr;
+  return SHL_OK;
+}
+
+shl_status shl_get_cavity_origins(shl_ctx* c, double* origins) {
+  if (!c || !origins) return SHL_ERR_ARG;
+  const size_t nd = 3 * (size_t)c->S.V;
+  if (!c->b.cav_origin) {
+    std::fill(origins, origins + nd, 0.0);
+    return SHL_OK;
+  }
+  SHL_CUDA_TRY(cudaMemcpyAsync(origins, c->b.cav_origin, nd * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  SHL_CUDA_TRY(cudaStreamSynchronize(c->stream));
+  return SHL_OK;
+}
+
+shl_status shl_set_cavity_origins(shl_ctx* c, const double* origins) {
+  if (!c || !origins) return SHL_ERR_ARG;
+  if (!c->b.cav_origin) return SHL_OK;  // nothing to keep without cavity contact
+  SHL_TRY(upload(c, c->b.cav_origin, origins, 3 * (size_t)c->S.V));
+  SHL_CUDA_TRY(cudaStreamSynchronize(c->stream));
+  return SHL_OK;
 }
 
 shl_status shl_get_dt(shl_ctx* c, double* dt, uint32_t* rejections) {
@@ -1202,6 +1306,7 @@ shl_status shl_residual(shl_ctx* c, double pressure, int flags, double* rel, dou
   // f = pressure force - internal force, then the pressure force alone (no contact, no damping)
   StepConst sc = c->sc;
   sc.contact = 0;
+  sc.cavity_contact = 0;
   DevBuf bf = b;
   if (fp64 && ctx32) {
     sc.fp32 = 0;
@@ -1213,6 +1318,7 @@ shl_status shl_residual(shl_ctx* c, double pressure, int flags, double* rel, dou
     // the context's own FP32 force at the same state, and the defect the steps add to it
     StepConst s32 = c->sc;
     s32.contact = 0;
+    s32.cavity_contact = 0;
     launch_elements(b, s32, c->eg, c->elem_blocks, c->stream);
     launch_gather_correct(b, s32, 0, false, c->f32, nullptr, c->stream);
     launch_defect(c->d_fa, c->f32, nd, c->b.fcorr, c->stream);
@@ -1317,7 +1423,14 @@ shl_status shl_get_node_fields(shl_ctx* c, double* ekin, double* ecav, double* e
   if (!c) return SHL_ERR_ARG;
   const uint32_t V = c->S.V, F = c->S.F;
   const std::vector<double>& Minv = c->S.Minv;
-  if (ecav) std::fill(ecav, ecav + V, 0.0);  // cavity contact is not modelled
+  if (ecav) {
+    if (c->b.cav_ecav) {
+      SHL_CUDA_TRY(cudaMemcpyAsync(ecav, c->b.cav_ecav, V * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+      SHL_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    } else {
+      std::fill(ecav, ecav + V, 0.0);
+    }
+  }
   if (mass)
     for (uint32_t n = 0; n < V; ++n) mass[n] = 1.0 / Minv[3 * (size_t)n];
   if (!ekin && !eself && !efric) return SHL_OK;
@@ -1347,7 +1460,14 @@ shl_status shl_get_node_fields(shl_ctx* c, double* ekin, double* ecav, double* e
   }
   if (!eself && !efric) return SHL_OK;
   if (eself) std::fill(eself, eself + V, 0.0);
-  if (efric) std::fill(efric, efric + V, 0.0);
+  if (efric) {
+    if (c->b.cav_efric) {
+      SHL_CUDA_TRY(cudaMemcpyAsync(efric, c->b.cav_efric, V * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+      SHL_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    } else {
+      std::fill(efric, efric + V, 0.0);
+    }
+  }
   const uint32_t np = c->sc.contact ? h.n_pairs : 0u;
   if (np == 0) return SHL_OK;
   // per-pair energies spread over the six nodes with weights 0.5 (u, v, w) / area_min

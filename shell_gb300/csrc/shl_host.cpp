@@ -224,6 +224,11 @@ void shl_params_default(shl_params* p) {
   p->dt_max = 0.0;
   p->rel_loc_err_min = 5e-5;
   p->rel_loc_err_max = 5e-4;
+  p->shell_cavity_contact = 0;
+  p->cavity = SHL_CAVITY_ELLIPSOID;
+  p->Rx = p->Ry = p->Rz = 0.1005;
+  p->mu_s_cavity = p->mu_d_cavity = 0.0;
+  p->cavity_damping = p->cavity_friction_damping = 0.0;
 }
 
 const char* shl_status_string(shl_status s) {

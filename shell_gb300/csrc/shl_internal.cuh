@@ -97,6 +97,12 @@ struct Ctl {
   uint32_t rejections;      // repeated attempts since the last report reset
   uint32_t steps_target;    // pause once steps_done reaches it
   uint32_t paused;          // 1: steps_target reached, 2: stopping criterion true
+  // cavity contact (ShellSystem.C:1600-1723)
+  double cav_R[3];          // semi-axes of the current step
+  double Ecav, cavity_force;
+  uint32_t Nc_cav;
+  uint32_t pad_cav;
+  double sum_pcav, sum_Nc_cav, sum_Ecav;
   // dt-weighted sums (MovingAverage inputs)
   double sum_dt, sum_area, sum_volume, sum_Nc, sum_Ekin, sum_Etens, sum_Ebend, sum_Eself, sum_Efric,
       sum_kGauss, sum_kMean;
@@ -137,6 +143,13 @@ struct StepConst {
   double beta, gamma;
   double err_min, err_max, err_target;
   double dt_min_eff, dt_max_eff;
+  // cavity contact
+  int32_t cavity_contact, cavity_type, cavity_friction, pad_cav;
+  double cav_R[3];
+  double mu_s_cav, mu_d_cav, cav_damping, cav_fric_damping, static_friction_tol;
+  const shl::expr::Op* rfun[3];  // semi-axes as compiled expressions of t, or null: cav_R
+  int32_t rfun_len[3];
+  int32_t pad_rfun;
 };
 
 // Device buffers of one context.
@@ -144,6 +157,9 @@ struct DevBuf {
   double *X, *u, *v, *a, *up, *vp, *p, *Minv, *C;
   double* M;          // 3V lumped masses (1 / Minv), for the kinetic energy
   double* ap;         // 3V predicted acceleration of an adaptive attempt (adaptive dt only)
+  double* cav_origin; // 3V static-friction spring origins of the cavity contacts (cavity contact only)
+  double* cav_ecav;   // V cavity-contact energy density of the last step
+  double* cav_efric;  // V cavity-friction energy density of the last step
   double* fcorr;      // 3V defect correction added to the FP32 force in a step, or null
   double* face;       // FF_COUNT * F
   double* pscale;     // F (internal order): factor on the step's pressure (per shell)

@@ -54,9 +54,10 @@ shl_status shl_save_state_file(shl_ctx* ctx, const char* path, uint32_t time_ste
   uint32_t nv = 0;
   s = shl_context_size(ctx, &nv, nullptr);
   if (s != SHL_OK) return s;
-  std::vector<double> u(3 * (size_t)nv), v(3 * (size_t)nv), a(3 * (size_t)nv);
+  std::vector<double> u(3 * (size_t)nv), v(3 * (size_t)nv), a(3 * (size_t)nv), so(3 * (size_t)nv);
   s = shl_get_state(ctx, u.data(), v.data(), a.data());
   if (s != SHL_OK) return s;
+  if ((s = shl_get_cavity_origins(ctx, so.data())) != SHL_OK) return s;
   std::ofstream f(path);
   if (!f) {
     set_error(std::string("cannot write ") + path);
@@ -66,7 +67,7 @@ shl_status shl_save_state_file(shl_ctx* ctx, const char* path, uint32_t time_ste
   f << time_step << "\n" << dt << "\n" << t << "\n" << wall_time << "\n";
   for (uint32_t n = 0; n < nv; ++n) {
     for (int c = 0; c < 3; ++c) f << u[3 * n + c] << "\t" << v[3 * n + c] << "\t" << a[3 * n + c] << "\t";
-    f << 0.0 << "\t" << 0.0 << "\t" << 0.0 << "\n";  // cavity spring origin (cavity contact off)
+    f << so[3 * n] << "\t" << so[3 * n + 1] << "\t" << so[3 * n + 2] << "\n";  // cavity spring origin
   }
   f << n_rows << "\n";
   for (uint32_t r = 0; r < n_rows; ++r) {
@@ -95,11 +96,10 @@ shl_status shl_load_state_file(shl_ctx* ctx, const char* path, uint32_t* time_st
   f >> step >> dtl >> t >> wt;
   shl_status s = shl_context_size(ctx, &nv, nullptr);
   if (s != SHL_OK) return s;
-  std::vector<double> u(3 * (size_t)nv), v(3 * (size_t)nv), a(3 * (size_t)nv);
+  std::vector<double> u(3 * (size_t)nv), v(3 * (size_t)nv), a(3 * (size_t)nv), so(3 * (size_t)nv);
   for (uint32_t n = 0; n < nv; ++n) {
     for (int c = 0; c < 3; ++c) f >> u[3 * n + c] >> v[3 * n + c] >> a[3 * n + c];
-    double so[3];
-    f >> so[0] >> so[1] >> so[2];
+    f >> so[3 * n] >> so[3 * n + 1] >> so[3 * n + 2];
   }
   uint32_t rows = 0;
   f >> rows;
@@ -125,6 +125,7 @@ shl_status shl_load_state_file(shl_ctx* ctx, const char* path, uint32_t* time_st
   }
   if ((s = shl_set_state(ctx, u.data(), v.data(), a.data())) != SHL_OK) return s;
   if ((s = shl_set_time(ctx, t, step)) != SHL_OK) return s;
+  if ((s = shl_set_cavity_origins(ctx, so.data())) != SHL_OK) return s;
   if (nc) {
     if ((s = shl_set_contact_state(ctx, pairs.data(), stick.data(), origin.data(), d2.data(), nc, 0.0)) != SHL_OK)
       return s;

@@ -109,6 +109,39 @@ __device__ __forceinline__ double rebuild_tolerance(const StepConst& sc, const C
   return __dmul_rn(sc.cell_margin, cs);
 }
 
+// ---------------------------------------------------------------- cavity --
+// effective semi-axes and friction scope (update_derived, ShellSystem.C:421-436)
+struct CavityGeom {
+  double R_eff[3], inv_R2[3], avg_R_eff, opd_friction;
+};
+
+__device__ __forceinline__ CavityGeom cavity_geom(const double* R, const StepConst& sc) {
+  CavityGeom g;
+  const double h_half = 0.5 * sc.thickness;
+  for (int c = 0; c < 3; ++c) {
+    g.R_eff[c] = R[c] - h_half;
+    g.inv_R2[c] = 1 / (g.R_eff[c] * g.R_eff[c]);
+  }
+  g.avg_R_eff = (g.R_eff[0] + g.R_eff[1] + g.R_eff[2]) / 3;
+  const double q = 1 - sc.static_friction_tol * sc.thickness / g.avg_R_eff;
+  g.opd_friction = q * q;
+  return g;
+}
+
+// cavity surface (Knud Thomsen's approximation for the ellipsoid, an ellipse
+// circumference approximation for the cylinder), ShellSystem.C:441-468
+__device__ double cavity_surface(const double* R, int type) {
+  const double Rx = R[0], Ry = R[1], Rz = R[2];
+  if (type == SHL_CAVITY_BOX) return 8 * (Rx * Ry + Rx * Rz + Ry * Rz);
+  if (type == SHL_CAVITY_CYLINDER) {
+    const double lambda = (Ry - Rz) / (Ry + Rz);
+    const double lambda32 = 3 * lambda * lambda;
+    return 2 * 3.141592653589793238 * ((Ry + Rz) * (1 + lambda32 / (10 + sqrt(4 - lambda32))) + Ry * Rz);
+  }
+  return 4 * 3.141592653589793238 *
+         pow((pow(Rx * Ry, 1.6) + pow(Rx * Rz, 1.6) + pow(Ry * Rz, 1.6)) / 3, 0.625);
+}
+
 // ------------------------------------------------ config expressions --
 // Stack-machine evaluation of a program compiled by shl_expr.h, one thread;
 // bounded by the program length (at most shl::expr::kMaxProgram ops, each
@@ -262,6 +295,9 @@ __global__ void __launch_bounds__(kBlock) k_predict(DevBuf b, StepConst sc) {
   ctl->table_pos += 1;
   if (sc.compat_zero_pressure) pr = pr * 0.0;
   ctl->pressure = pr;
+  if (sc.cavity_contact)
+    for (int c = 0; c < 3; ++c)
+      ctl->cav_R[c] = sc.rfun_len[c] > 0 ? eval_program(sc.rfun[c], sc.rfun_len[c], ctl->time, 0.0) : sc.cav_R[c];
   {
     const double red = fmax(1.0 - (double)((int)(ctl->time * 5.0)) * 0.01, 0.5);
     if (ctl->time_step == 2) ctl->volume0 = ctl->volume;
@@ -852,6 +888,21 @@ __global__ void __launch_bounds__(kBlock) k_contact_force(DevBuf b, StepConst sc
 }
 
 // ------------------------------------------------------ gather + correct --
+// last block of the gather: the step's cavity totals (fixed order over blocks)
+__device__ void cavity_totals(const DevBuf& b, const StepConst& sc, Ctl* ctl, double* sh) {
+  const double nc = sum_partials(b.partial, 2, gridDim.x, sh);
+  const double e = sum_partials(b.partial, 3, gridDim.x, sh);
+  const double ef = sum_partials(b.partial, 4, gridDim.x, sh);
+  const double fn = sum_partials(b.partial, 5, gridDim.x, sh);
+  if (threadIdx.x == 0) {
+    ctl->Nc_cav = (uint32_t)nc;
+    ctl->Ecav = e;
+    ctl->cavity_force = fn;
+    ctl->Efric = (sc.contact ? ctl->Efric : 0.0) + ef;
+  }
+  __syncthreads();
+}
+
 __global__ void __launch_bounds__(kBlock) k_gather_correct(DevBuf b, StepConst sc, int mode, double* f_out,
                                                            double* a_out) {
   // mode 0: eval (write f_out / a_out), mode 1: step corrector
@@ -860,6 +911,7 @@ __global__ void __launch_bounds__(kBlock) k_gather_correct(DevBuf b, StepConst s
   __shared__ double sh[kBlock / 32];
   const uint32_t n = blockIdx.x * blockDim.x + threadIdx.x;
   double du2 = 0.0, ekin = 0.0;
+  double c_nc = 0.0, c_e = 0.0, c_ef = 0.0, c_fn = 0.0;  // cavity: contacts, energy, friction energy, force
   if (n < sc.V) {
     double f[3] = {0.0, 0.0, 0.0};
     if (sc.contact) {
@@ -897,6 +949,91 @@ __global__ void __launch_bounds__(kBlock) k_gather_correct(DevBuf b, StepConst s
         f[0] -= q[0];
         f[1] -= q[1];
         f[2] -= q[2];
+      }
+    }
+    if (sc.cavity_contact) {
+      // interaction with the cavity (ShellSystem.C:1600-1723)
+      const CavityGeom cg = cavity_geom(ctl->cav_R, sc);
+      const size_t k3 = 3 * (size_t)n;
+      const double p[3] = {b.p[k3], b.p[k3 + 1], b.p[k3 + 2]};
+      const double xr = (p[0] / cg.R_eff[0]) * (p[0] / cg.R_eff[0]);
+      const double yr = (p[1] / cg.R_eff[1]) * (p[1] / cg.R_eff[1]);
+      const double zr = (p[2] / cg.R_eff[2]) * (p[2] / cg.R_eff[2]);
+      double opd;  // cavity_isoparameter, ShellSystem.h:336-362
+      if (sc.cavity_type == SHL_CAVITY_BOX)
+        opd = fmax(xr, fmax(yr, zr));
+      else if (sc.cavity_type == SHL_CAVITY_CYLINDER)
+        opd = fmax(xr, yr + zr);
+      else
+        opd = xr + yr + zr;
+      double ecav_d = 0.0, efric_d = 0.0;
+      if (opd > cg.opd_friction) {
+        const double depth = cg.avg_R_eff * (sqrt(opd) - 1);
+        // avg_area_node (ShellSystem.C:2462-2481): the faces of which the node is a vertex
+        double area_sum = 0.0;
+        uint32_t n_faces = 0;
+        for (uint32_t k = g0; k < g1; ++k) {
+          const uint32_t ent = __ldg(&b.gather_ent[k]);
+          if (ent % 12u < 3u) {
+            area_sum += b.area[__ldg(&b.perm[ent / 12u])];
+            ++n_faces;
+          }
+        }
+        const double area_node = area_sum / n_faces;
+        const double stiffness = sc.stiff_density * area_node;
+        double f_normal = 0.0;
+        if (depth > 0) {
+          c_nc += 1.0;
+          const double e_node = 0.5 * stiffness * depth * depth;
+          c_e += e_node;
+          ecav_d = e_node / area_node;
+          f_normal = stiffness * depth;
+          c_fn += f_normal;
+        }
+        double nv[3] = {0.0, 0.0, 0.0};
+        if (sc.cavity_type == SHL_CAVITY_BOX) {
+          const int c = (xr > yr && xr > zr) ? 0 : (yr > zr ? 1 : 2);
+          nv[c] = (double)((p[c] > 0) - (p[c] < 0));
+        } else if (sc.cavity_type == SHL_CAVITY_CYLINDER) {
+          if (xr > yr + zr) {
+            nv[0] = (double)((p[0] > 0) - (p[0] < 0));
+          } else {
+            nv[1] = p[1] * cg.inv_R2[1];
+            nv[2] = p[2] * cg.inv_R2[2];
+          }
+        } else {
+          for (int c = 0; c < 3; ++c) nv[c] = p[c] * cg.inv_R2[c];
+        }
+        const double inv_len = 1 / sqrt(nv[0] * nv[0] + nv[1] * nv[1] + nv[2] * nv[2]);
+        for (int c = 0; c < 3; ++c) nv[c] *= inv_len;
+        const double vel[3] = {b.v[k3], b.v[k3 + 1], b.v[k3 + 2]};
+        const double abs_v_normal = vel[0] * nv[0] + vel[1] * nv[1] + vel[2] * nv[2];
+        double fc[3] = {0.0, 0.0, 0.0};
+        if (sc.cavity_friction) {
+          double* so = b.cav_origin + k3;
+          double orig[3] = {so[0], so[1], so[2]};
+          int stick = (orig[0] * orig[0] + orig[1] * orig[1] + orig[2] * orig[2]) != 0.0;
+          double ef = 0.0;
+          shl_friction_apply(&ef, fc, f_normal, nv, vel, abs_v_normal, sc.v_stop, sc.stiff_static_friction,
+                             sc.mu_s_cav, sc.mu_d_cav, sc.cav_fric_damping, &stick, orig, p);
+          so[0] = orig[0];
+          so[1] = orig[1];
+          so[2] = orig[2];
+          c_ef += ef;
+          efric_d = ef / area_node;
+        }
+        f_normal += sc.cav_damping * stiffness * abs_v_normal;
+        for (int c = 0; c < 3; ++c) {
+          fc[c] -= f_normal * nv[c];
+          f[c] += fc[c];
+        }
+      } else if (sc.cavity_friction) {
+        // the spring is dropped only beyond the friction scope
+        b.cav_origin[k3] = b.cav_origin[k3 + 1] = b.cav_origin[k3 + 2] = 0.0;
+      }
+      if (mode >= 1) {
+        b.cav_ecav[n] = ecav_d;
+        b.cav_efric[n] = efric_d;
       }
     }
     if (mode >= 1 && b.fcorr) {
@@ -941,6 +1078,14 @@ __global__ void __launch_bounds__(kBlock) k_gather_correct(DevBuf b, StepConst s
     if (mode == 1) du2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
   }
   if (mode == 0) return;
+  if (sc.cavity_contact) {
+    const double r0 = block_sum(c_nc, sh), r1 = block_sum(c_e, sh), r2 = block_sum(c_ef, sh),
+                 r3 = block_sum(c_fn, sh);
+    if (threadIdx.x == 0) {
+      double* pp = b.partial + (size_t)blockIdx.x * 8;
+      pp[2] = r0; pp[3] = r1; pp[4] = r2; pp[5] = r3;
+    }
+  }
   if (mode == 2) {
     const double na = block_max(du2, sh);
     const double vm = block_max(ekin, sh);
@@ -949,6 +1094,7 @@ __global__ void __launch_bounds__(kBlock) k_gather_correct(DevBuf b, StepConst s
       b.partial[(size_t)blockIdx.x * 8 + 1] = vm;
     }
     if (!last_block(&ctl->cnt[3])) return;
+    if (sc.cavity_contact) cavity_totals(b, sc, ctl, sh);
     double m0 = 0.0, m1 = 0.0;
     for (int k = threadIdx.x; k < (int)gridDim.x; k += blockDim.x) {
       m0 = fmax(m0, __ldcg(&b.partial[(size_t)k * 8]));
@@ -969,7 +1115,7 @@ __global__ void __launch_bounds__(kBlock) k_gather_correct(DevBuf b, StepConst s
         new_dt = 2 * dt;
       else if (rel_loc_err > sc.err_max || rel_loc_err < sc.err_min)
         new_dt = dt * pow(sc.err_target / rel_loc_err, 1. / 3);
-      if (sc.contact) {
+      if (sc.contact || sc.cavity_contact) {
         // resolve the contact depth with at least 10 steps
         if (__dmul_rn(__dmul_rn(__dmul_rn(new_dt, vmax), 10.0), 2.0) > sc.thickness)
           new_dt = sc.thickness / (2.0 * 10.0 * vmax);
@@ -995,6 +1141,7 @@ __global__ void __launch_bounds__(kBlock) k_gather_correct(DevBuf b, StepConst s
     b.partial[(size_t)blockIdx.x * 8 + 1] = ek;
   }
   if (!last_block(&ctl->cnt[3])) return;
+  if (sc.cavity_contact) cavity_totals(b, sc, ctl, sh);
   double mm = 0.0;
   for (int k = threadIdx.x; k < (int)gridDim.x; k += blockDim.x) mm = fmax(mm, __ldcg(&b.partial[(size_t)k * 8]));
   mm = block_max(mm, sh);
@@ -1122,6 +1269,11 @@ __global__ void __launch_bounds__(kBlock) k_volume_end(DevBuf b, StepConst sc, i
   ctl->sum_Efric += dt * ctl->Efric;
   ctl->sum_kGauss += dt * ctl->kGauss;
   ctl->sum_kMean += dt * ctl->kMean;
+  if (sc.cavity_contact) {
+    ctl->sum_pcav += dt * ctl->cavity_force / cavity_surface(ctl->cav_R, sc.cavity_type);
+    ctl->sum_Nc_cav += dt * (double)ctl->Nc_cav;
+    ctl->sum_Ecav += dt * ctl->Ecav;
+  }
   const int pr = ctl->problem;
   if (pr > ctl->worst_problem) ctl->worst_problem = pr;
   if (pr > 0 && ctl->first_problem_step == 0) ctl->first_problem_step = ctl->time_step;

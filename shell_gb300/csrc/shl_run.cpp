@@ -259,14 +259,15 @@ struct Averages {
   double s[14] = {0};
   void add_report(const shl_step_report& r) {
     n += r.steps_done;
-    const double v[14] = {r.sum_dt, r.sum_area, r.sum_volume, 0, 0, r.sum_Nc, r.sum_Ekin, r.sum_Etens,
-                          r.sum_Ebend, 0, r.sum_Eself, r.sum_Efric, r.sum_kGauss, r.sum_kMean};
+    const double v[14] = {r.sum_dt,    r.sum_area,  r.sum_volume, r.sum_pcav,  r.sum_Nc_cav, r.sum_Nc,     r.sum_Ekin,
+                          r.sum_Etens, r.sum_Ebend, r.sum_Ecav,   r.sum_Eself, r.sum_Efric,  r.sum_kGauss, r.sum_kMean};
     for (int k = 0; k < 14; ++k) s[k] += v[k];
   }
-  void add_sample(double dt, const shl_energies& e, double Ekin) {
+  void add_sample(double dt, const shl_energies& e, double Ekin, double pcav) {
     n += 1;
-    const double v[14] = {dt, dt * e.area, dt * e.volume, 0, 0, dt * e.Nc, dt * Ekin, dt * e.Etens,
-                          dt * e.Ebend, 0, dt * e.Eself, dt * e.Efric, dt * e.kGauss, dt * e.kMean};
+    const double v[14] = {dt,         dt * e.area,  dt * e.volume, dt * pcav,   dt * e.Nc_cav, dt * e.Nc,
+                          dt * Ekin,  dt * e.Etens, dt * e.Ebend,  dt * e.Ecav, dt * e.Eself,  dt * e.Efric,
+                          dt * e.kGauss, dt * e.kMean};
     for (int k = 0; k < 14; ++k) s[k] += v[k];
   }
   // n rows of the mean sample: keeps both the sums and the count in a state file
@@ -290,12 +291,29 @@ void print_header() {
             << std::string(60 + 72 + 95, '-') << std::endl;
 }
 
-void print_properties(Averages& avg, uint32_t time_step, double time, double secs_running) {
+// cavity surface and volume, ShellSystem.C:441-468 (box; cylinder with axis x; ellipsoid)
+void cavity_size(int type, const double* R, double* surface, double* volume) {
+  const double Rx = R[0], Ry = R[1], Rz = R[2], pi = 3.141592653589793238;
+  if (type == SHL_CAVITY_BOX) {
+    *surface = 8 * (Rx * Ry + Rx * Rz + Ry * Rz);
+    *volume = 8 * Rx * Ry * Rz;
+  } else if (type == SHL_CAVITY_CYLINDER) {
+    const double lambda = (Ry - Rz) / (Ry + Rz);
+    const double lambda32 = 3 * lambda * lambda;
+    *surface = 2 * pi * ((Ry + Rz) * (1 + lambda32 / (10 + std::sqrt(4 - lambda32))) + Ry * Rz);
+    *volume = 2 * pi * Rx * Ry * Rz;
+  } else {
+    *surface = 4 * pi * std::pow((std::pow(Rx * Ry, 1.6) + std::pow(Rx * Rz, 1.6) + std::pow(Ry * Rz, 1.6)) / 3, 0.625);
+    *volume = 4. / 3 * pi * Rx * Ry * Rz;
+  }
+}
+
+// density: the packing density of the last measurement (area h / cavity volume), 0 without cavity
+void print_properties(Averages& avg, uint32_t time_step, double time, double secs_running, double density) {
   if (avg.n == 0) return;
   const double adt = avg.s[0] / avg.n;
   if (secs_running < 1) secs_running = std::floor(secs_running * 1e7) * 1e-7;
   auto a = [&](int k) { return (avg.s[k] / avg.n) / adt; };
-  const double density = 0.0;  // packing density: cavity contact is not modelled
   char line[512];
   std::snprintf(line, sizeof(line),
                 "%12s %10d %11.6g %11.6g %9.8g %11.6g %11.6g %11.6g %11.6g %11.6g %11.6g %11.6g %11.6g %11.6g "
@@ -423,10 +441,13 @@ int run(int argc, char** argv) {
   P.memb_stiff_mult = F_("memb_stiff_mult", "1");
   P.bend_stiff_mult = F_("bend_stiff_mult", "1");
   P.thickness = F_("thickness", "1e-3");
-  cfg.upper("cavity", "ELLIPSOID");
-  F_("Rx", "0.1005");
-  F_("Ry", "0.1005");
-  F_("Rz", "0.1005");
+  const std::string cav = cfg.upper("cavity", "ELLIPSOID");
+  P.cavity = cav == "BOX" ? SHL_CAVITY_BOX : cav == "CYLINDER" ? SHL_CAVITY_CYLINDER
+             : cav == "ELLIPSOID" ? SHL_CAVITY_ELLIPSOID : -1;
+  if (P.cavity < 0) throw Error("ERROR: unknown cavity " + cav);
+  P.Rx = F_("Rx", "0.1005");
+  P.Ry = F_("Ry", "0.1005");
+  P.Rz = F_("Rz", "0.1005");
   cfg.upper("shell_boundary", "FREE");  // no boundary on a closed mesh
   cfg.uint("bc_coords", 7);
   cfg.uint("bc_every", 0);
@@ -461,14 +482,15 @@ int run(int argc, char** argv) {
                                                              : ssc == "SMOOTH" ? SHL_CONTACT_SMOOTH : -1;
   if (P.shell_shell_contact < 0) throw Error("ERROR: unknown shell_shell_contact " + ssc);
   const bool cavity_contact = cfg.boolean("shell_cavity_contact", false);
+  P.shell_cavity_contact = cavity_contact ? 1 : 0;
   P.mu_s = F_("mu_s", "0");
   P.mu_d = F_("mu_d", "0");
-  F_("mu_s_cavity", "0");
-  F_("mu_d_cavity", "0");
+  P.mu_s_cavity = F_("mu_s_cavity", "0");
+  P.mu_d_cavity = F_("mu_d_cavity", "0");
   P.self_damping = F_("self_damping", "0");
-  F_("cavity_damping", "0");
+  P.cavity_damping = F_("cavity_damping", "0");
   P.self_friction_damping = F_("self_friction_damping", "0");
-  F_("cavity_friction_damping", "0");
+  P.cavity_friction_damping = F_("cavity_friction_damping", "0");
   P.fric_stiff_mult = F_("fric_stiff_mult", "1");
   P.friction_stop_velocity = cfg.real("friction_stop_velocity", P.friction_stop_velocity);
   P.static_friction_tol = cfg.real("static_friction_tol", P.static_friction_tol);
@@ -498,14 +520,14 @@ int run(int argc, char** argv) {
     if (!ok) throw Error("ERROR: " + what + " is not supported by this library");
   };
   need(P.shell_shell_contact != SHL_CONTACT_SMOOTH, "shell_shell_contact = smooth");
-  need(!cavity_contact, "shell_cavity_contact = true (cavity contact)");
   need(damping_rotation == 0 && perturbation_rate == 0 && gravity == 0 && !stand_still,
        "damping_rotation, perturbation_rate, gravity or stand_still");
   need(growth1 == 1 && growth2 == 1 && mgr == 0 && cgr == 0, "growth");
   for (const Function& f : fn) {
     if (f.name == "pressure" || f.name == "Rx" || f.name == "Ry" || f.name == "Rz" || f.name == "bc_stiff_mult" ||
-        f.name == "bc_criterion" || f.name.find("cavity") != std::string::npos)
+        f.name == "bc_criterion")
       continue;
+    if (!cavity_contact && f.name.find("cavity") != std::string::npos) continue;
     need(f.e.is_constant(), "a time-dependent " + f.name);
   }
   need(!stop.e.uses("x") && !stop.e.uses("y") && !stop.e.uses("z"), "a stopping criterion of x, y, z");
@@ -649,6 +671,27 @@ int run(int argc, char** argv) {
     check(shl_apply_initial_conditions(ctx, u0.data(), 0.0, eval_at(pressure_fn, P.dt)),
           "shl_apply_initial_conditions");
   }
+  auto fn_named = [&](const char* name) -> const Function& {
+    return *std::find_if(fn.begin(), fn.end(), [&](const Function& f) { return f.name == name; });
+  };
+  // cavity semi-axes and packing density at time t (update_derived, measure_properties)
+  auto cavity_R = [&](double t, double* R) {
+    const char* names[3] = {"Rx", "Ry", "Rz"};
+    for (int k = 0; k < 3; ++k) R[k] = eval_at(fn_named(names[k]), t);
+  };
+  auto density_at = [&](double t, double area) {
+    if (!cavity_contact) return 0.0;
+    double R[3], surface, volume;
+    cavity_R(t, R);
+    cavity_size(P.cavity, R, &surface, &volume);
+    return area * P.thickness / volume;
+  };
+  if (cavity_contact) {
+    const Function &rx = fn_named("Rx"), &ry = fn_named("Ry"), &rz = fn_named("Rz");
+    if (!rx.e.is_constant() || !ry.e.is_constant() || !rz.e.is_constant())
+      check(shl_set_cavity_functions(ctx, rx.e.text().c_str(), ry.e.text().c_str(), rz.e.text().c_str()),
+            "shl_set_cavity_functions");
+  }
   if (adapt_dt_every > 0) {
     // the step times are not known in advance: the device evaluates the
     // pressure at each attempt's time and tests the stopping criterion after each step
@@ -662,8 +705,15 @@ int run(int argc, char** argv) {
     if (data_time > 0) {
       shl_energies e{};
       check(shl_get_energies(ctx, &e), "shl_get_energies");
-      avg.add_sample(P.dt, e, 0.0);
-      print_properties(avg, time_step, time, wall_time + elapsed());
+      double pcav = 0.0;
+      if (cavity_contact) {
+        double R[3], surface, volume;
+        cavity_R(time + P.dt, R);  // the initial force evaluation's time (ShellSystem.C:892-904)
+        cavity_size(P.cavity, R, &surface, &volume);
+        pcav = e.cavity_force / surface;
+      }
+      avg.add_sample(P.dt, e, 0.0, pcav);
+      print_properties(avg, time_step, time, wall_time + elapsed(), density_at(time + P.dt, e.area));
     }
     if (vtk_time > 0) {
       std::snprintf(path, sizeof(path), "%s/shell%010u.vtu", data_dir.c_str(), time_step);
@@ -733,7 +783,7 @@ int run(int argc, char** argv) {
       const unsigned dc = data_time > 0 ? (unsigned)(time / data_time) : 0;
       if (dc > last_data) {
         last_data = dc;
-        print_properties(avg, time_step, time, wall_time + elapsed());
+        print_properties(avg, time_step, time, wall_time + elapsed(), density_at(time, rep.last.area));
       }
       const unsigned vc = vtk_time > 0 ? (unsigned)(time / vtk_time) : 0;
       if (vc > last_vtk) {

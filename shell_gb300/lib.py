@@ -22,6 +22,7 @@ SHL_ERR_ARG, SHL_ERR_CUDA, SHL_ERR_TIMEOUT, SHL_ERR_OOM, SHL_ERR_CAPACITY = 100,
 CONTACT_LINEAR, CONTACT_SMOOTH, CONTACT_NONE = 0, 1, 2
 CS_LOCAL, CS_CARTESIAN, CS_CYLINDRICAL, CS_SPHERICAL = 0, 1, 2, 3
 PREC_FP64, PREC_FP32 = 0, 1
+CAVITY_BOX, CAVITY_CYLINDER, CAVITY_ELLIPSOID = 0, 1, 2
 
 _d, _i32, _u32 = ctypes.c_double, ctypes.c_int32, ctypes.c_uint32
 
@@ -41,6 +42,8 @@ _PARAM_FIELDS = (
     + [("compat_zero_pressure", _i32), ("precision", _i32), ("stop_on_problem", _i32), ("pad1", _i32)]
     + [("adapt_dt_every", _u32), ("pad2", _i32)]
     + [(n, _d) for n in ("dt_min", "dt_max", "rel_loc_err_min", "rel_loc_err_max")]
+    + [("shell_cavity_contact", _i32), ("cavity", _i32)]
+    + [(n, _d) for n in ("Rx", "Ry", "Rz", "mu_s_cavity", "mu_d_cavity", "cavity_damping", "cavity_friction_damping")]
 )
 
 
@@ -53,7 +56,7 @@ class ShlParams(ctypes.Structure):
 
 class ShlEnergies(ctypes.Structure):
     _fields_ = [(n, _d) for n in ("Etens", "Ebend", "Eself", "Efric", "Ekin", "area", "volume", "kGauss", "kMean")] + [
-        ("Nc", _u32), ("n_pairs", _u32)]
+        ("Nc", _u32), ("n_pairs", _u32), ("Ecav", _d), ("cavity_force", _d), ("Nc_cav", _u32), ("pad", _u32)]
 
     def as_dict(self):
         return {n: getattr(self, n) for n, _ in self._fields_}
@@ -63,7 +66,8 @@ class ShlStepReport(ctypes.Structure):
     _fields_ = [("steps_done", _u32), ("worst_problem", _i32), ("time", _d), ("du_sum", _d), ("n_rebuilds", _u32),
                 ("rejections", _u32), ("last", ShlEnergies)] + [
         (n, _d) for n in ("sum_dt", "sum_area", "sum_volume", "sum_Nc", "sum_Ekin", "sum_Etens", "sum_Ebend",
-                          "sum_Eself", "sum_Efric", "sum_kGauss", "sum_kMean")] + [("stopped", _u32), ("pad", _u32)]
+                          "sum_Eself", "sum_Efric", "sum_kGauss", "sum_kMean")] + [("stopped", _u32), ("pad", _u32)] + [
+        (n, _d) for n in ("sum_pcav", "sum_Nc_cav", "sum_Ecav")]
 
 
 _lib = None
@@ -135,6 +139,9 @@ def load():
         "shl_set_pressure_function": (_i32, [vp, ctypes.c_char_p]),
         "shl_get_dt": (_i32, [vp, ctypes.POINTER(_d), ctypes.POINTER(_u32)]),
         "shl_set_stop_function": (_i32, [vp, ctypes.c_char_p]),
+        "shl_set_cavity_functions": (_i32, [vp, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p]),
+        "shl_get_cavity_origins": (_i32, [vp, vp]),
+        "shl_set_cavity_origins": (_i32, [vp, vp]),
         "shl_eval_pressure_function": (_i32, [vp, vp, _u32, vp]),
     }
     for name, (res, args) in sig.items():
@@ -159,7 +166,8 @@ def exported_symbols():
             "shl_write_vtu", "shl_get_energies", "shl_mlp_create", "shl_mlp_destroy", "shl_mlp_set_params",
             "shl_mlp_get_params", "shl_mlp_set_dataset", "shl_mlp_train", "shl_mlp_predict", "shl_mlp_gradients",
             "shl_gemm_bf16", "shl_residual", "shl_set_pressure_function", "shl_eval_pressure_function",
-            "shl_get_dt", "shl_set_stop_function"]
+            "shl_get_dt", "shl_set_stop_function", "shl_set_cavity_functions", "shl_get_cavity_origins",
+            "shl_set_cavity_origins"]
 
 
 class ShlError(RuntimeError):
@@ -399,6 +407,17 @@ class Shell:
         """Stopping criterion (expression of t) tested on the device after every step (None: none)."""
         _check(self.lib.shl_set_stop_function(self.h, None if expr is None else expr.encode()),
                "shl_set_stop_function", False)
+
+    def set_cavity_functions(self, rx=None, ry=None, rz=None):
+        """Cavity semi-axes as expressions of t (None keeps the constant)."""
+        enc = lambda e: None if e is None else e.encode()  # noqa: E731
+        _check(self.lib.shl_set_cavity_functions(self.h, enc(rx), enc(ry), enc(rz)), "shl_set_cavity_functions",
+               False)
+
+    def cavity_origins(self):
+        o = np.zeros(3 * self.V)
+        _check(self.lib.shl_get_cavity_origins(self.h, o.ctypes.data), "shl_get_cavity_origins", False)
+        return o
 
     def dt(self):
         """(current dt, repeated attempts since the last report)."""
