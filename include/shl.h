@@ -281,6 +281,12 @@ shl_status shl_rebuild_contacts(shl_ctx* ctx);
 shl_status shl_get_element_fields(shl_ctx* ctx, double* kGauss, double* kMean, double* etens,
                                   double* ebend, double* area);
 
+/* Scale the damping coefficients of the following steps by `factor` (relative
+ * to those of the parameters; 1 restores them).  No counterpart in the
+ * reference; used by relaxation schemes that smooth a starting field with
+ * heavy damping before relaxing it. */
+shl_status shl_scale_damping(shl_ctx* ctx, double factor);
+
 /* Lumped inverse masses and damping coefficients (ShellSystem.C:762-852). */
 shl_status shl_get_mass_damping(shl_ctx* ctx, double* Minv, double* C);
 

@@ -375,6 +375,8 @@ shl_status create_common(shl_ctx* c, const std::vector<double>& pscale_orig, shl
 #define ALLOC(ptr, n) do { if ((st = dev_alloc(c, &(ptr), (n))) != SHL_OK) return fail(st); } while (0)
   ALLOC(b.X, nd); ALLOC(b.u, nd); ALLOC(b.v, nd); ALLOC(b.a, nd); ALLOC(b.up, nd); ALLOC(b.vp, nd);
   ALLOC(b.p, nd); ALLOC(b.Minv, nd); ALLOC(b.C, nd); ALLOC(b.M, nd);
+  ALLOC(b.uph, nd);
+  ALLOC(b.upl, nd);
   if (params->adapt_dt_every) ALLOC(b.ap, nd);
   if (params->shell_cavity_contact) {
     ALLOC(b.cav_origin, nd);
@@ -1494,6 +1496,16 @@ shl_status shl_get_node_fields(shl_ctx* c, double* ekin, double* ecav, double* e
       }
     }
   }
+  return SHL_OK;
+}
+
+shl_status shl_scale_damping(shl_ctx* c, double factor) {
+  if (!c || !(factor >= 0)) return SHL_ERR_ARG;
+  const size_t nd = 3 * (size_t)c->S.V;
+  std::vector<double> C(nd);
+  for (size_t i = 0; i < nd; ++i) C[i] = factor * c->S.C[i];
+  SHL_TRY(upload(c, c->b.C, C.data(), nd));
+  SHL_CUDA_TRY(cudaStreamSynchronize(c->stream));
   return SHL_OK;
 }
 

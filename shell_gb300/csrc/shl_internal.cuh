@@ -168,6 +168,7 @@ struct DevBuf {
   float* face32;      // F32_COUNT * F (FP32 element path)
   float* qe32;        // F * 12 * 3 (FP32 element path)
   float* up32;        // 3V, FP32 copy of u_pred (FP32 element path)
+  float *uph, *upl;   // 3V, u_pred as a float pair hi + lo (the FP64 path's contractions)
   uint32_t *gather_ptr, *gather_ent;
   uint32_t* tri;      // 3F original order
   uint32_t *perm;     // internal -> original

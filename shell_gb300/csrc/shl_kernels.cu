@@ -109,6 +109,34 @@ __device__ __forceinline__ double rebuild_tolerance(const StepConst& sc, const C
   return __dmul_rn(sc.cell_margin, cs);
 }
 
+// ---- float-pair ("double-float") arithmetic for the FP64 path's two
+// basis contractions.  GB300 issues 64 FP32 FMAs per FP64 FMA, so a product
+// sum carried as an unevaluated pair hi + lo of floats (about 48 significant
+// bits: TwoProd by FMA, TwoSum by Knuth, with the lo parts accumulated; the
+// intrinsics keep the compiler from fusing the error terms) is several times
+// cheaper than the same sum in FP64, and its error (~2^-48 of the summands)
+// stays far below the path's 1e-12 budget: the contractions produce the
+// displacement derivatives and the per-slot force shares, and the
+// cancellation-prone steps (metric differences, the nodal gather) stay FP64.
+__device__ __forceinline__ void df_madd(float& ah, float& al, float bh, float bl, float xh, float xl) {
+  const float p = __fmul_rn(bh, xh);
+  float e = __fmaf_rn(bh, xh, -p);
+  e = __fmaf_rn(bh, xl, e);
+  e = __fmaf_rn(bl, xh, e);
+  const float s = __fadd_rn(ah, p);
+  const float bb = __fsub_rn(s, ah);
+  const float err = __fadd_rn(__fsub_rn(ah, __fsub_rn(s, bb)), __fsub_rn(p, bb));
+  al = __fadd_rn(al, __fadd_rn(e, err));
+  ah = s;
+}
+
+__device__ __forceinline__ void df_split(double x, float& h, float& l) {
+  h = __double2float_rn(x);
+  l = __double2float_rn(x - (double)h);
+}
+
+__device__ __forceinline__ double df_value(float h, float l) { return (double)h + (double)l; }
+
 // ---------------------------------------------------------------- cavity --
 // effective semi-axes and friction scope (update_derived, ShellSystem.C:421-436)
 struct CavityGeom {
@@ -270,7 +298,10 @@ __global__ void __launch_bounds__(kBlock) k_predict(DevBuf b, StepConst sc) {
         vp = fma(nm6, a, v);
       }
       b.up[k] = up;
-      if (sc.fp32) b.up32[k] = (float)up;
+      if (sc.fp32)
+        b.up32[k] = (float)up;
+      else
+        df_split(up, b.uph[k], b.upl[k]);
       b.vp[k] = vp;
       b.p[k] = __dadd_rn(b.X[k], up);
       d[c] = __dsub_rn(up, u);
@@ -322,6 +353,7 @@ __global__ void k_positions(DevBuf b, StepConst sc) {
     const size_t k = 3 * (size_t)n + c;
     b.p[k] = __dadd_rn(b.X[k], b.up[k]);
     if (sc.fp32) b.up32[k] = (float)b.up[k];
+    df_split(b.up[k], b.uph[k], b.upl[k]);
   }
 }
 
@@ -341,7 +373,7 @@ __device__ __forceinline__ double dot3(const double* a, const double* b) {
 
 // One face: deformed metric, stress resultants, and the per-slot force
 // share qe_s = sum_k B[s][k] Z_k (internal minus pressure), see the comments.
-template <int NP>
+template <int NP, bool DF = false>
 __device__ __forceinline__ ElemOut element_force(uint32_t i, int np_rt, const double* __restrict__ B,
                                                  const DevBuf& b, const StepConst& sc, double pressure,
                                                  double vol_p) {
@@ -349,21 +381,53 @@ __device__ __forceinline__ ElemOut element_force(uint32_t i, int np_rt, const do
   const int np = NP > 0 ? NP : np_rt;
   // G[k] = sum_s B[s][k] u_s  (unrotated value and derivatives of u at the qp)
   double G[6][3];
+  if (DF) {
+    // B as float pairs in shared memory right after the FP64 table (Bh, then Bl)
+    const float* Bh = reinterpret_cast<const float*>(B + kMaxSlots * 6);
+    const float* Bl = Bh + kMaxSlots * 6;
+    float gh[6][3], gl[6][3];
 #pragma unroll
-  for (int k = 0; k < 6; ++k) G[k][0] = G[k][1] = G[k][2] = 0.0;
+    for (int k = 0; k < 6; ++k)
 #pragma unroll
-  for (int s = 0; s < (NP > 0 ? NP : kMaxSlots); ++s) {
-    if (NP == 0 && s >= np) break;
-    const int nd = __ldg(&b.patch[(size_t)s * F + i]);
-    const double ux = __ldg(&b.up[3 * (size_t)nd]);
-    const double uy = __ldg(&b.up[3 * (size_t)nd + 1]);
-    const double uz = __ldg(&b.up[3 * (size_t)nd + 2]);
+      for (int c = 0; c < 3; ++c) gh[k][c] = gl[k][c] = 0.f;
 #pragma unroll
-    for (int k = 0; k < 6; ++k) {
-      const double w = B[6 * s + k];
-      G[k][0] = fma(w, ux, G[k][0]);
-      G[k][1] = fma(w, uy, G[k][1]);
-      G[k][2] = fma(w, uz, G[k][2]);
+    for (int s = 0; s < (NP > 0 ? NP : kMaxSlots); ++s) {
+      if (NP == 0 && s >= np) break;
+      const int nd = __ldg(&b.patch[(size_t)s * F + i]);
+      float uh[3], ul[3];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        uh[c] = __ldg(&b.uph[3 * (size_t)nd + c]);
+        ul[c] = __ldg(&b.upl[3 * (size_t)nd + c]);
+      }
+#pragma unroll
+      for (int k = 0; k < 6; ++k) {
+        const float wh = Bh[6 * s + k], wl = Bl[6 * s + k];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) df_madd(gh[k][c], gl[k][c], wh, wl, uh[c], ul[c]);
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < 6; ++k)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) G[k][c] = df_value(gh[k][c], gl[k][c]);
+  } else {
+#pragma unroll
+    for (int k = 0; k < 6; ++k) G[k][0] = G[k][1] = G[k][2] = 0.0;
+#pragma unroll
+    for (int s = 0; s < (NP > 0 ? NP : kMaxSlots); ++s) {
+      if (NP == 0 && s >= np) break;
+      const int nd = __ldg(&b.patch[(size_t)s * F + i]);
+      const double ux = __ldg(&b.up[3 * (size_t)nd]);
+      const double uy = __ldg(&b.up[3 * (size_t)nd + 1]);
+      const double uz = __ldg(&b.up[3 * (size_t)nd + 2]);
+#pragma unroll
+      for (int k = 0; k < 6; ++k) {
+        const double w = B[6 * s + k];
+        G[k][0] = fma(w, ux, G[k][0]);
+        G[k][1] = fma(w, uy, G[k][1]);
+        G[k][2] = fma(w, uz, G[k][2]);
+      }
     }
   }
   const double* fc = b.face;
@@ -465,20 +529,41 @@ __device__ __forceinline__ ElemOut element_force(uint32_t i, int np_rt, const do
     Z[5][c] = c11c * Y11 + c22c * Y22 + c12c * Y12;
   }
   double* qe = b.qe + (size_t)i * 36;
+  if (DF) {
+    const float* Bh = reinterpret_cast<const float*>(B + kMaxSlots * 6);
+    const float* Bl = Bh + kMaxSlots * 6;
+    float zh[6][3], zl[6][3];
 #pragma unroll
-  for (int s = 0; s < (NP > 0 ? NP : kMaxSlots); ++s) {
-    if (NP == 0 && s >= np) break;
-    double q[3];
+    for (int k = 0; k < 6; ++k)
 #pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      double t = B[6 * s] * Z[0][c];
+      for (int c = 0; c < 3; ++c) df_split(Z[k][c], zh[k][c], zl[k][c]);
 #pragma unroll
-      for (int k = 1; k < 6; ++k) t = fma(B[6 * s + k], Z[k][c], t);
-      q[c] = t;
+    for (int s = 0; s < (NP > 0 ? NP : kMaxSlots); ++s) {
+      if (NP == 0 && s >= np) break;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        float th = 0.f, tl = 0.f;
+#pragma unroll
+        for (int k = 0; k < 6; ++k) df_madd(th, tl, Bh[6 * s + k], Bl[6 * s + k], zh[k][c], zl[k][c]);
+        qe[3 * s + c] = df_value(th, tl);
+      }
     }
-    qe[3 * s] = q[0];
-    qe[3 * s + 1] = q[1];
-    qe[3 * s + 2] = q[2];
+  } else {
+#pragma unroll
+    for (int s = 0; s < (NP > 0 ? NP : kMaxSlots); ++s) {
+      if (NP == 0 && s >= np) break;
+      double q[3];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        double t = B[6 * s] * Z[0][c];
+#pragma unroll
+        for (int k = 1; k < 6; ++k) t = fma(B[6 * s + k], Z[k][c], t);
+        q[c] = t;
+      }
+      qe[3 * s] = q[0];
+      qe[3 * s + 1] = q[1];
+      qe[3 * s + 2] = q[2];
+    }
   }
   ElemOut o;
   o.etens = 0.5 * JxW * (n0 * al0 + n1 * al1 + n2 * al2);
@@ -727,12 +812,19 @@ __global__ void __launch_bounds__(kBlock) k_elements(DevBuf b, StepConst sc, Ele
   Ctl* ctl = b.ctl;
   if (inactive(ctl)) return;
   __shared__ double sh[kBlock / 32];
-  __shared__ double sB[kMaxSlots * 6];
+  // FP64 basis table followed by its float pairs (hi, lo): kMaxSlots * 6 doubles + 2 x kMaxSlots * 6 floats
+  __shared__ double sB[kMaxSlots * 6 * 2];
   int g = 0;
   while (g + 1 < eg.n && blockIdx.x >= eg.g[g + 1].block_start) ++g;
   const GroupDesc gd = eg.g[g];
   // the block's basis table (all threads of a block belong to one group)
-  for (int k = threadIdx.x; k < gd.n_slots * 6; k += blockDim.x) sB[k] = eg.basis[gd.basis_off + k];
+  float* sBh = reinterpret_cast<float*>(sB + kMaxSlots * 6);
+  float* sBl = sBh + kMaxSlots * 6;
+  for (int k = threadIdx.x; k < gd.n_slots * 6; k += blockDim.x) {
+    const double w = eg.basis[gd.basis_off + k];
+    sB[k] = w;
+    df_split(w, sBh[k], sBl[k]);
+  }
   __syncthreads();
   const uint32_t li = (blockIdx.x - gd.block_start) * blockDim.x + threadIdx.x;
   ElemOut o{0, 0, 0, 0, 0};
@@ -742,11 +834,11 @@ __global__ void __launch_bounds__(kBlock) k_elements(DevBuf b, StepConst sc, Ele
     const double* B = sB;
     const double pr = pressure * __ldg(&b.pscale[i]);
     if (gd.n_slots == 12)
-      o = element_force<12>(i, 12, B, b, sc, pr, vol_p);
+      o = element_force<12, true>(i, 12, B, b, sc, pr, vol_p);
     else if (gd.n_slots == 11)
-      o = element_force<11>(i, 11, B, b, sc, pr, vol_p);
+      o = element_force<11, true>(i, 11, B, b, sc, pr, vol_p);
     else
-      o = element_force<0>(i, gd.n_slots, B, b, sc, pr, vol_p);
+      o = element_force<0, true>(i, gd.n_slots, B, b, sc, pr, vol_p);
     const uint32_t e = __ldg(&b.perm[i]);
     b.area[e] = o.area;
     b.kG[e] = o.kg / o.area;
@@ -991,11 +1083,13 @@ __global__ void __launch_bounds__(kBlock) k_gather_correct(DevBuf b, StepConst s
           c_fn += f_normal;
         }
         double nv[3] = {0.0, 0.0, 0.0};
+        // the normal's case split uses p^2 / R_eff^2 (ShellSystem.C:1638-1660)
+        const double xn = p[0] * p[0] * cg.inv_R2[0], yn = p[1] * p[1] * cg.inv_R2[1], zn = p[2] * p[2] * cg.inv_R2[2];
         if (sc.cavity_type == SHL_CAVITY_BOX) {
-          const int c = (xr > yr && xr > zr) ? 0 : (yr > zr ? 1 : 2);
+          const int c = (xn > yn && xn > zn) ? 0 : (yn > zn ? 1 : 2);
           nv[c] = (double)((p[c] > 0) - (p[c] < 0));
         } else if (sc.cavity_type == SHL_CAVITY_CYLINDER) {
-          if (xr > yr + zr) {
+          if (xn > yn + zn) {
             nv[0] = (double)((p[0] > 0) - (p[0] < 0));
           } else {
             nv[1] = p[1] * cg.inv_R2[1];

@@ -142,6 +142,7 @@ def load():
         "shl_set_cavity_functions": (_i32, [vp, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p]),
         "shl_get_cavity_origins": (_i32, [vp, vp]),
         "shl_set_cavity_origins": (_i32, [vp, vp]),
+        "shl_scale_damping": (_i32, [vp, _d]),
         "shl_eval_pressure_function": (_i32, [vp, vp, _u32, vp]),
     }
     for name, (res, args) in sig.items():
@@ -167,7 +168,7 @@ def exported_symbols():
             "shl_mlp_get_params", "shl_mlp_set_dataset", "shl_mlp_train", "shl_mlp_predict", "shl_mlp_gradients",
             "shl_gemm_bf16", "shl_residual", "shl_set_pressure_function", "shl_eval_pressure_function",
             "shl_get_dt", "shl_set_stop_function", "shl_set_cavity_functions", "shl_get_cavity_origins",
-            "shl_set_cavity_origins"]
+            "shl_set_cavity_origins", "shl_scale_damping"]
 
 
 class ShlError(RuntimeError):
@@ -413,6 +414,9 @@ class Shell:
         enc = lambda e: None if e is None else e.encode()  # noqa: E731
         _check(self.lib.shl_set_cavity_functions(self.h, enc(rx), enc(ry), enc(rz)), "shl_set_cavity_functions",
                False)
+
+    def scale_damping(self, factor):
+        _check(self.lib.shl_scale_damping(self.h, factor), "shl_scale_damping", False)
 
     def cavity_origins(self):
         o = np.zeros(3 * self.V)
