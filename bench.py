@@ -385,6 +385,7 @@ def run_ours(args, rank, world, dist):
 
     # roofline of the element kernel (live, cold L2)
     elem_ms = g.time_kernel(0, reps=20, flush_bytes=FLUSH_BYTES)
+    elem_variant = g.element_variant()[1]
     fp64_peak = L.measure_fp64_peak()
     g.close()
     bytes_elem = F * ELEM_BYTES_PER_FACE + V * ELEM_BYTES_PER_NODE
@@ -417,7 +418,7 @@ def run_ours(args, rank, world, dist):
                 "d2h_bytes_per_step": 3 * 3 * V * 8,
                 "how": "per step: shl_set_state from pinned host, shl_step(1), shl_get_state"},
         "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm, "unit": "GB/s",
-                     "frac": achieved_gbs / hbm, "traffic": None, "kernel": "k_elements",
+                     "frac": achieved_gbs / hbm, "traffic": None, "kernel": "k_elements", "variant": elem_variant,
                      "kernel_ms": elem_ms, "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)",
                      "fp64": {"achieved_tflops": achieved_tf, "peak_tflops": fp64_peak,
                               "frac": achieved_tf / fp64_peak,

@@ -51,7 +51,11 @@ struct shl_ctx {
   DevBuf b{};
   StepConst sc{};
   uint32_t elem_blocks = 0;
-  ElemGroups eg{};
+  ElemGroups eg{};                 // 256-thread block ranges (the no-allocation path)
+  ElemGroups eg_bs[3]{};           // block ranges for 64, 128, 256 threads per block
+  uint32_t blocks_bs[3]{};
+  int var64 = 0, var32 = kFirstFp32Variant;  // chosen element-kernel variants
+  float variant_ms[kNumElemVariants]{};      // tuning times (0: not timed)
   std::vector<void*> allocs;
   cudaGraphExec_t graph = nullptr;
   cudaGraphExec_t graph1 = nullptr;
@@ -69,6 +73,22 @@ struct shl_ctx {
   std::string rfun_text[3];                  // the same, for evaluations started by the host
   double* f32 = nullptr;                     // FP32 force at the checked state (defect correction)
 };
+
+namespace {
+
+int bs_index(int block) { return block == 64 ? 0 : block == 128 ? 1 : 2; }
+
+// the element launch of the context's current variant for the given step constants
+ElemLaunch elem_launch(const shl_ctx* c, const StepConst& sc) {
+  ElemLaunch el;
+  el.variant = sc.fp32 ? c->var32 : c->var64;
+  const int k = bs_index(kElemVariants[el.variant].block);
+  el.blocks = c->blocks_bs[k];
+  el.eg = c->eg_bs[k];
+  return el;
+}
+
+}  // namespace
 
 namespace {
 
@@ -266,7 +286,7 @@ cudaError_t enqueue_step(shl_ctx* c, bool capturing = false) {
   cudaError_t e = cudaSuccess;
   launch_predict(b, sc, 0, s);
   if (sc.contact && (e = enqueue_rebuild(c, capturing)) != cudaSuccess) return e;
-  launch_elements(b, sc, c->eg, c->elem_blocks, s);
+  launch_elements(b, sc, elem_launch(c, sc), s);
   if (sc.contact) launch_contact_force(b, sc, 0, s);
   if (sc.adapt_every) {
     // one attempt: estimate, then correct only if accepted (ShellSystem.C:1010-1117)
@@ -358,6 +378,52 @@ namespace {
 
 // Device allocation, uploads and step constants for a context whose set-up
 // (c->S, one shell or a merged batch) is built; pscale: per original face.
+// The FP64 path's arithmetic: 0 = both basis contractions in FP64, 1 = the
+// displacement contraction as float pairs (measured 24-26 % faster at levels 6
+// and 7 than 0; also pairing the force contraction costs more in conversions
+// than it saves).  Fixed for all contexts, so that results do not depend on
+// which launch shape a context picks (the per-face arithmetic of a variant
+// does not depend on its shape).
+constexpr int kFp64Pairs = 1;
+
+// Element-kernel autotuning: time every launch shape of the context's path on
+// its own mesh (one warm-up and three timed launches each, CUDA events on the
+// context stream) and keep the fastest.
+shl_status tune_elements(shl_ctx* c) {
+  cudaEvent_t e0, e1;
+  SHL_CUDA_TRY(cudaEventCreate(&e0));
+  SHL_CUDA_TRY(cudaEventCreate(&e1));
+  const bool fp32 = c->sc.fp32 != 0;
+  float best = 0.f;
+  int best_v = -1;
+  for (int v = 0; v < kNumElemVariants; ++v) {
+    const bool v32 = v >= kFirstFp32Variant;
+    if (v32 != fp32 || (!v32 && kElemVariants[v].pairs != kFp64Pairs)) continue;
+    if (fp32) c->var32 = v; else c->var64 = v;
+    const ElemLaunch el = elem_launch(c, c->sc);
+    launch_elements(c->b, c->sc, el, c->stream);
+    float total = 0.f;
+    for (int r = 0; r < 3; ++r) {
+      cudaEventRecord(e0, c->stream);
+      launch_elements(c->b, c->sc, el, c->stream);
+      cudaEventRecord(e1, c->stream);
+      SHL_CUDA_TRY(cudaEventSynchronize(e1));
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      total += ms;
+    }
+    c->variant_ms[v] = total / 3;
+    if (best_v < 0 || c->variant_ms[v] < best) {
+      best = c->variant_ms[v];
+      best_v = v;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (fp32) c->var32 = best_v; else c->var64 = best_v;
+  return check_launch("element tuning");
+}
+
 shl_status create_common(shl_ctx* c, const std::vector<double>& pscale_orig, shl_ctx** out) {
   const shl_params* params = &c->P;
   std::string err;
@@ -416,6 +482,18 @@ shl_status create_common(shl_ctx* c, const std::vector<double>& pscale_orig, shl
   if ((int)gd.size() > kMaxGroups) { g_err = "too many patch valences"; return fail(SHL_ERR_ARG); }
   if (blocks == 0) blocks = 1;
   c->elem_blocks = blocks;
+  // block ranges of the other launch shapes
+  const int bs_list[3] = {64, 128, 256};
+  std::vector<GroupDesc> gd_bs[3];
+  for (int k = 0; k < 3; ++k) {
+    uint32_t nb = 0;
+    for (GroupDesc d : gd) {
+      d.block_start = nb;
+      nb += (d.count + bs_list[k] - 1) / bs_list[k];
+      gd_bs[k].push_back(d);
+    }
+    c->blocks_bs[k] = nb ? nb : 1;
+  }
   const uint32_t max_blocks = std::max({blocks, (F + kBlock - 1) / kBlock, (V + kBlock - 1) / kBlock, 4u * 152u}) + 8;
   ALLOC(b.partial, 8 * (size_t)max_blocks);
   ALLOC(c->d_fa, 2 * nd);
@@ -495,6 +573,10 @@ shl_status create_common(shl_ctx* c, const std::vector<double>& pscale_orig, shl
     for (size_t k = 0; k < gd.size(); ++k) c->eg.g[k] = gd[k];
     c->eg.basis = d_basis;
     c->eg.basis32 = d_basis32;
+    for (int k = 0; k < 3; ++k) {
+      c->eg_bs[k] = c->eg;
+      for (size_t q = 0; q < gd_bs[k].size(); ++q) c->eg_bs[k].g[q] = gd_bs[k][q];
+    }
   }
 
   // step constants
@@ -572,6 +654,7 @@ shl_status create_common(shl_ctx* c, const std::vector<double>& pscale_orig, shl
     g_err = "stream synchronisation failed in shl_create";
     return fail(SHL_ERR_CUDA);
   }
+  if ((st = tune_elements(c)) != SHL_OK) return fail(st);
   *out = c;
   return SHL_OK;
 }
@@ -716,7 +799,7 @@ shl_status begin_eval(shl_ctx* c, double pressure, bool allow_rebuild) {
 shl_status eval_into(shl_ctx* c, double* d_f, double* d_a) {
   const DevBuf& b = c->b;
   if (c->sc.contact) launch_rebuild(b, c->sc, c->stream);
-  launch_elements(b, c->sc, c->eg, c->elem_blocks, c->stream);
+  launch_elements(b, c->sc, elem_launch(c, c->sc), c->stream);
   if (c->sc.contact) launch_contact_force(b, c->sc, 0, c->stream);
   launch_gather_correct(b, c->sc, 0, false, d_f, d_a, c->stream);
   return check_launch("force evaluation");
@@ -770,7 +853,7 @@ shl_status initial_state(shl_ctx* c, Ctl& h) {
   h.rebuild = c->sc.contact ? 1u : 0u;  // compute_shell_shell_contact_candidates(true)
   SHL_TRY(ctl_put(c, h));
   if (c->sc.contact) launch_rebuild(c->b, c->sc, c->stream);
-  launch_elements(c->b, c->sc, c->eg, c->elem_blocks, c->stream);
+  launch_elements(c->b, c->sc, elem_launch(c, c->sc), c->stream);
   launch_volume_end_step(c->b, c->sc, false, c->stream);
   SHL_TRY(check_launch("initial conditions"));
   SHL_TRY(ctl_get(c, h));
@@ -1071,7 +1154,7 @@ shl_status shl_time_kernel(shl_ctx* c, int which, int reps, size_t flush_bytes, 
     if (flush_bytes) launch_flush(c->d_flush, flush_bytes, (uint32_t)r, c->stream);
     cudaEventRecord(e0, c->stream);
     if (which == 0)
-      launch_elements(c->b, c->sc, c->eg, c->elem_blocks, c->stream);
+      launch_elements(c->b, c->sc, elem_launch(c, c->sc), c->stream);
     else
       launch_gather_correct(c->b, c->sc, 0, false, c->d_fa, c->d_fa + nd, c->stream);
     cudaEventRecord(e1, c->stream);
@@ -1111,7 +1194,7 @@ shl_status shl_profile_step(shl_ctx* c, double pressure, size_t flush_bytes, dou
   cudaEventRecord(ev[1], s);
   if (sc.contact) launch_rebuild(b, sc, s);
   cudaEventRecord(ev[2], s);
-  launch_elements(b, sc, c->eg, c->elem_blocks, s);
+  launch_elements(b, sc, elem_launch(c, sc), s);
   cudaEventRecord(ev[3], s);
   if (sc.contact) launch_contact_force(b, sc, 0, s);
   cudaEventRecord(ev[4], s);
@@ -1314,21 +1397,21 @@ shl_status shl_residual(shl_ctx* c, double pressure, int flags, double* rel, dou
     sc.fp32 = 0;
     bf.qe = c->qe64;
   }
-  launch_elements(bf, sc, c->eg, c->elem_blocks, c->stream);
+  launch_elements(bf, sc, elem_launch(c, sc), c->stream);
   launch_gather_correct(bf, sc, 0, false, c->d_fa, nullptr, c->stream);
   if (correct) {
     // the context's own FP32 force at the same state, and the defect the steps add to it
     StepConst s32 = c->sc;
     s32.contact = 0;
     s32.cavity_contact = 0;
-    launch_elements(b, s32, c->eg, c->elem_blocks, c->stream);
+    launch_elements(b, s32, elem_launch(c, s32), c->stream);
     launch_gather_correct(b, s32, 0, false, c->f32, nullptr, c->stream);
     launch_defect(c->d_fa, c->f32, nd, c->b.fcorr, c->stream);
   }
   if ((flags & SHL_RESIDUAL_CLEAR) && c->b.fcorr)
     SHL_CUDA_TRY(cudaMemsetAsync(c->b.fcorr, 0, nd * sizeof(double), c->stream));
   sc.internal_scale = 0.0;
-  launch_elements(bf, sc, c->eg, c->elem_blocks, c->stream);
+  launch_elements(bf, sc, elem_launch(c, sc), c->stream);
   launch_gather_correct(bf, sc, 0, false, c->d_fa + nd, nullptr, c->stream);
   launch_shell_norms(c->d_fa, c->d_fa + nd, c->b.M, c->d_node_off, ns, c->d_norms, c->stream);
   SHL_TRY(check_launch("shl_residual"));
@@ -1496,6 +1579,32 @@ shl_status shl_get_node_fields(shl_ctx* c, double* ekin, double* ecav, double* e
       }
     }
   }
+  return SHL_OK;
+}
+
+shl_status shl_set_element_variant(shl_ctx* c, int variant) {
+  if (!c) return SHL_ERR_ARG;
+  if (variant < 0) return tune_elements(c);
+  if (variant >= kNumElemVariants || (variant >= kFirstFp32Variant) != (c->sc.fp32 != 0)) {
+    g_err = "element variant does not exist for this precision";
+    return SHL_ERR_ARG;
+  }
+  if (c->sc.fp32) c->var32 = variant; else c->var64 = variant;
+  if (c->graph) cudaGraphExecDestroy(c->graph);
+  if (c->graph1) cudaGraphExecDestroy(c->graph1);
+  c->graph = c->graph1 = nullptr;
+  return SHL_OK;
+}
+
+shl_status shl_get_element_variant(shl_ctx* c, int* variant, char* name, size_t cap, float* tuned_ms) {
+  if (!c) return SHL_ERR_ARG;
+  const int v = c->sc.fp32 ? c->var32 : c->var64;
+  if (variant) *variant = v;
+  if (name && cap) {
+    std::strncpy(name, kElemVariants[v].name, cap - 1);
+    name[cap - 1] = 0;
+  }
+  if (tuned_ms) std::memcpy(tuned_ms, c->variant_ms, sizeof(c->variant_ms));
   return SHL_OK;
 }
 

@@ -52,6 +52,25 @@ struct ElemGroups {
   const float* basis32;
 };
 
+// An element-kernel variant: threads per block, arithmetic (0 FP64, 1 the
+// displacement contraction as float pairs, 2 both contractions as float
+// pairs; FP32-path variants use 0) and a name for reports.
+struct ElemVariant {
+  int block;
+  int pairs;
+  const char* name;
+};
+constexpr int kNumElemVariants = 9;
+constexpr int kFirstFp32Variant = 6;
+extern const ElemVariant kElemVariants[kNumElemVariants];
+
+// The element launch of a context: variant, grid and patch-group block ranges for its block size.
+struct ElemLaunch {
+  int variant;
+  uint32_t blocks;
+  ElemGroups eg;
+};
+
 // Control block in device memory.
 struct Ctl {
   // time stepping
@@ -204,8 +223,7 @@ struct DevBuf {
 
 // ---- launchers (shl_kernels.cu) ----
 void launch_predict(const DevBuf& b, const StepConst& sc, int cur, cudaStream_t s);
-void launch_elements(const DevBuf& b, const StepConst& sc, const ElemGroups& eg, uint32_t n_blocks,
-                     cudaStream_t s);
+void launch_elements(const DevBuf& b, const StepConst& sc, const ElemLaunch& el, cudaStream_t s);
 void launch_contact_force(const DevBuf& b, const StepConst& sc, int cur, cudaStream_t s);
 void launch_gather_correct(const DevBuf& b, const StepConst& sc, int cur, bool correct, double* f_out,
                            double* a_out, cudaStream_t s);

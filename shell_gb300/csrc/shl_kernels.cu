@@ -373,7 +373,7 @@ __device__ __forceinline__ double dot3(const double* a, const double* b) {
 
 // One face: deformed metric, stress resultants, and the per-slot force
 // share qe_s = sum_k B[s][k] Z_k (internal minus pressure), see the comments.
-template <int NP, bool DF = false>
+template <int NP, bool DFG = false, bool DFQ = false>
 __device__ __forceinline__ ElemOut element_force(uint32_t i, int np_rt, const double* __restrict__ B,
                                                  const DevBuf& b, const StepConst& sc, double pressure,
                                                  double vol_p) {
@@ -381,7 +381,7 @@ __device__ __forceinline__ ElemOut element_force(uint32_t i, int np_rt, const do
   const int np = NP > 0 ? NP : np_rt;
   // G[k] = sum_s B[s][k] u_s  (unrotated value and derivatives of u at the qp)
   double G[6][3];
-  if (DF) {
+  if (DFG) {
     // B as float pairs in shared memory right after the FP64 table (Bh, then Bl)
     const float* Bh = reinterpret_cast<const float*>(B + kMaxSlots * 6);
     const float* Bl = Bh + kMaxSlots * 6;
@@ -529,7 +529,7 @@ __device__ __forceinline__ ElemOut element_force(uint32_t i, int np_rt, const do
     Z[5][c] = c11c * Y11 + c22c * Y22 + c12c * Y12;
   }
   double* qe = b.qe + (size_t)i * 36;
-  if (DF) {
+  if (DFQ) {
     const float* Bh = reinterpret_cast<const float*>(B + kMaxSlots * 6);
     const float* Bl = Bh + kMaxSlots * 6;
     float zh[6][3], zl[6][3];
@@ -756,10 +756,16 @@ __device__ __forceinline__ ElemOut element_force32(uint32_t i, int np_rt, const 
 #undef FC
 }
 
-__global__ void __launch_bounds__(kBlock, 2) k_elements32(DevBuf b, StepConst sc, ElemGroups eg) {
+// Element kernels are compiled in several launch shapes (threads per block,
+// blocks per SM, hence registers per thread) -- and for the FP64 path with the
+// two basis contractions in FP64 or as float pairs; set-up times them on the
+// context's own mesh and keeps the fastest (shl_api.cu, tune_elements).  The
+// per-face arithmetic of one path does not depend on the launch shape.  The
+// totals of the per-face measurements are summed by k_elem_totals.
+template <int BS, int MINB>
+__global__ void __launch_bounds__(BS, MINB) k_elements32(DevBuf b, StepConst sc, ElemGroups eg) {
   Ctl* ctl = b.ctl;
   if (inactive(ctl)) return;
-  __shared__ double sh[kBlock / 32];
   __shared__ float sB[kMaxSlots * 6];
   int g = 0;
   while (g + 1 < eg.n && blockIdx.x >= eg.g[g + 1].block_start) ++g;
@@ -767,51 +773,31 @@ __global__ void __launch_bounds__(kBlock, 2) k_elements32(DevBuf b, StepConst sc
   for (int k = threadIdx.x; k < gd.n_slots * 6; k += blockDim.x) sB[k] = eg.basis32[gd.basis_off + k];
   __syncthreads();
   const uint32_t li = (blockIdx.x - gd.block_start) * blockDim.x + threadIdx.x;
-  ElemOut o{0, 0, 0, 0, 0};
+  if (li >= gd.count) return;
   const double pressure = ctl->pressure;
   const float vol_p = (float)ctl->volume_pressure;
-  if (li < gd.count) {
-    const uint32_t i = gd.first + li;
-    const float pr = (float)(pressure * __ldg(&b.pscale[i]));
-    if (gd.n_slots == 12)
-      o = element_force32<12>(i, 12, sB, b, sc, pr, vol_p);
-    else if (gd.n_slots == 11)
-      o = element_force32<11>(i, 11, sB, b, sc, pr, vol_p);
-    else
-      o = element_force32<0>(i, gd.n_slots, sB, b, sc, pr, vol_p);
-    const uint32_t e = __ldg(&b.perm[i]);
-    const float ia = 1.f / (float)o.area;
-    b.area[e] = o.area;
-    b.kG[e] = (float)o.kg * ia;
-    b.kM[e] = (float)o.km * ia;
-    b.etens[e] = (float)o.etens * ia;
-    b.ebend[e] = (float)o.ebend * ia;
-  }
-  const double s0 = block_sum(o.etens, sh);
-  const double s1 = block_sum(o.ebend, sh);
-  const double s2 = block_sum(o.kg, sh);
-  const double s3 = block_sum(o.km, sh);
-  const double s4 = block_sum(o.area, sh);
-  if (threadIdx.x == 0) {
-    double* pp = b.partial + (size_t)blockIdx.x * 8;
-    pp[0] = s0; pp[1] = s1; pp[2] = s2; pp[3] = s3; pp[4] = s4;
-  }
-  if (!last_block(&ctl->cnt[1])) return;
-  const int nb = gridDim.x;
-  const double t0 = sum_partials(b.partial, 0, nb, sh);
-  const double t1 = sum_partials(b.partial, 1, nb, sh);
-  const double t2 = sum_partials(b.partial, 2, nb, sh);
-  const double t3 = sum_partials(b.partial, 3, nb, sh);
-  const double t4 = sum_partials(b.partial, 4, nb, sh);
-  if (threadIdx.x == 0) {
-    ctl->Etens = t0; ctl->Ebend = t1; ctl->kGauss = t2; ctl->kMean = t3; ctl->area = t4;
-  }
+  const uint32_t i = gd.first + li;
+  const float pr = (float)(pressure * __ldg(&b.pscale[i]));
+  ElemOut o;
+  if (gd.n_slots == 12)
+    o = element_force32<12>(i, 12, sB, b, sc, pr, vol_p);
+  else if (gd.n_slots == 11)
+    o = element_force32<11>(i, 11, sB, b, sc, pr, vol_p);
+  else
+    o = element_force32<0>(i, gd.n_slots, sB, b, sc, pr, vol_p);
+  const uint32_t e = __ldg(&b.perm[i]);
+  const float ia = 1.f / (float)o.area;
+  b.area[e] = o.area;
+  b.kG[e] = (float)o.kg * ia;
+  b.kM[e] = (float)o.km * ia;
+  b.etens[e] = (float)o.etens * ia;
+  b.ebend[e] = (float)o.ebend * ia;
 }
 
-__global__ void __launch_bounds__(kBlock) k_elements(DevBuf b, StepConst sc, ElemGroups eg) {
+template <int BS, int MINB, bool DFG, bool DFQ>
+__global__ void __launch_bounds__(BS, MINB) k_elements(DevBuf b, StepConst sc, ElemGroups eg) {
   Ctl* ctl = b.ctl;
   if (inactive(ctl)) return;
-  __shared__ double sh[kBlock / 32];
   // FP64 basis table followed by its float pairs (hi, lo): kMaxSlots * 6 doubles + 2 x kMaxSlots * 6 floats
   __shared__ double sB[kMaxSlots * 6 * 2];
   int g = 0;
@@ -827,30 +813,43 @@ __global__ void __launch_bounds__(kBlock) k_elements(DevBuf b, StepConst sc, Ele
   }
   __syncthreads();
   const uint32_t li = (blockIdx.x - gd.block_start) * blockDim.x + threadIdx.x;
-  ElemOut o{0, 0, 0, 0, 0};
+  if (li >= gd.count) return;
   const double pressure = ctl->pressure, vol_p = ctl->volume_pressure;
-  if (li < gd.count) {
-    const uint32_t i = gd.first + li;
-    const double* B = sB;
-    const double pr = pressure * __ldg(&b.pscale[i]);
-    if (gd.n_slots == 12)
-      o = element_force<12, true>(i, 12, B, b, sc, pr, vol_p);
-    else if (gd.n_slots == 11)
-      o = element_force<11, true>(i, 11, B, b, sc, pr, vol_p);
-    else
-      o = element_force<0, true>(i, gd.n_slots, B, b, sc, pr, vol_p);
-    const uint32_t e = __ldg(&b.perm[i]);
-    b.area[e] = o.area;
-    b.kG[e] = o.kg / o.area;
-    b.kM[e] = o.km / o.area;
-    b.etens[e] = o.etens / o.area;
-    b.ebend[e] = o.ebend / o.area;
+  const uint32_t i = gd.first + li;
+  const double* B = sB;
+  const double pr = pressure * __ldg(&b.pscale[i]);
+  ElemOut o;
+  if (gd.n_slots == 12)
+    o = element_force<12, DFG, DFQ>(i, 12, B, b, sc, pr, vol_p);
+  else if (gd.n_slots == 11)
+    o = element_force<11, DFG, DFQ>(i, 11, B, b, sc, pr, vol_p);
+  else
+    o = element_force<0, DFG, DFQ>(i, gd.n_slots, B, b, sc, pr, vol_p);
+  const uint32_t e = __ldg(&b.perm[i]);
+  b.area[e] = o.area;
+  b.kG[e] = o.kg / o.area;
+  b.kM[e] = o.km / o.area;
+  b.etens[e] = o.etens / o.area;
+  b.ebend[e] = o.ebend / o.area;
+}
+
+// totals of the per-face measurements (original face order, fixed-order sums):
+// E_tens, E_bend, kGauss, kMean and the area (ShellSystem.C:1285-1300, 2760-2786)
+__global__ void __launch_bounds__(kBlock) k_elem_totals(DevBuf b, StepConst sc) {
+  Ctl* ctl = b.ctl;
+  if (inactive(ctl)) return;
+  __shared__ double sh[kBlock / 32];
+  const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
+  double et = 0.0, eb = 0.0, kg = 0.0, km = 0.0, ar = 0.0;
+  if (e < sc.F) {
+    ar = b.area[e];
+    et = b.etens[e] * ar;
+    eb = b.ebend[e] * ar;
+    kg = b.kG[e] * ar;
+    km = b.kM[e] * ar;
   }
-  const double s0 = block_sum(o.etens, sh);
-  const double s1 = block_sum(o.ebend, sh);
-  const double s2 = block_sum(o.kg, sh);
-  const double s3 = block_sum(o.km, sh);
-  const double s4 = block_sum(o.area, sh);
+  const double s0 = block_sum(et, sh), s1 = block_sum(eb, sh), s2 = block_sum(kg, sh), s3 = block_sum(km, sh),
+               s4 = block_sum(ar, sh);
   if (threadIdx.x == 0) {
     double* pp = b.partial + (size_t)blockIdx.x * 8;
     pp[0] = s0; pp[1] = s1; pp[2] = s2; pp[3] = s3; pp[4] = s4;
@@ -1474,12 +1473,27 @@ void launch_predict(const DevBuf& b, const StepConst& sc, int, cudaStream_t s) {
 void launch_positions(const DevBuf& b, const StepConst& sc, cudaStream_t s) {
   k_positions<<<nblk(sc.V), kBlock, 0, s>>>(b, sc);
 }
-void launch_elements(const DevBuf& b, const StepConst& sc, const ElemGroups& eg, uint32_t n_blocks,
-                     cudaStream_t s) {
-  if (sc.fp32)
-    k_elements32<<<n_blocks, kBlock, 0, s>>>(b, sc, eg);
-  else
-    k_elements<<<n_blocks, kBlock, 0, s>>>(b, sc, eg);
+// launch shapes and arithmetic of the element kernels (see k_elements)
+const ElemVariant kElemVariants[kNumElemVariants] = {
+    {256, 0, "fp64 256x1"},        {256, 1, "fp64 256x1 pair-G"}, {128, 1, "fp64 128x3 pair-G"},
+    {64, 1, "fp64 64x5 pair-G"},   {64, 1, "fp64 64x6 pair-G"},   {64, 0, "fp64 64x5"},
+    {256, 0, "fp32 256x2"},        {128, 0, "fp32 128x4"},        {64, 0, "fp32 64x8"}};
+
+void launch_elements(const DevBuf& b, const StepConst& sc, const ElemLaunch& el, cudaStream_t s) {
+  const uint32_t nb = el.blocks;
+  const ElemGroups& eg = el.eg;
+  switch (el.variant) {
+    case 0: k_elements<256, 1, false, false><<<nb, 256, 0, s>>>(b, sc, eg); break;
+    case 1: k_elements<256, 1, true, false><<<nb, 256, 0, s>>>(b, sc, eg); break;
+    case 2: k_elements<128, 3, true, false><<<nb, 128, 0, s>>>(b, sc, eg); break;
+    case 3: k_elements<64, 5, true, false><<<nb, 64, 0, s>>>(b, sc, eg); break;
+    case 4: k_elements<64, 6, true, false><<<nb, 64, 0, s>>>(b, sc, eg); break;
+    case 5: k_elements<64, 5, false, false><<<nb, 64, 0, s>>>(b, sc, eg); break;
+    case 6: k_elements32<256, 2><<<nb, 256, 0, s>>>(b, sc, eg); break;
+    case 7: k_elements32<128, 4><<<nb, 128, 0, s>>>(b, sc, eg); break;
+    default: k_elements32<64, 8><<<nb, 64, 0, s>>>(b, sc, eg); break;
+  }
+  k_elem_totals<<<nblk(sc.F), kBlock, 0, s>>>(b, sc);
 }
 void launch_contact_force(const DevBuf& b, const StepConst& sc, int, cudaStream_t s) {
   uint32_t nb = nblk(sc.pairs_cap);

@@ -143,6 +143,8 @@ def load():
         "shl_get_cavity_origins": (_i32, [vp, vp]),
         "shl_set_cavity_origins": (_i32, [vp, vp]),
         "shl_scale_damping": (_i32, [vp, _d]),
+        "shl_set_element_variant": (_i32, [vp, ctypes.c_int]),
+        "shl_get_element_variant": (_i32, [vp, ctypes.POINTER(ctypes.c_int), ctypes.c_char_p, sz, vp]),
         "shl_eval_pressure_function": (_i32, [vp, vp, _u32, vp]),
     }
     for name, (res, args) in sig.items():
@@ -168,7 +170,7 @@ def exported_symbols():
             "shl_mlp_get_params", "shl_mlp_set_dataset", "shl_mlp_train", "shl_mlp_predict", "shl_mlp_gradients",
             "shl_gemm_bf16", "shl_residual", "shl_set_pressure_function", "shl_eval_pressure_function",
             "shl_get_dt", "shl_set_stop_function", "shl_set_cavity_functions", "shl_get_cavity_origins",
-            "shl_set_cavity_origins", "shl_scale_damping"]
+            "shl_set_cavity_origins", "shl_scale_damping", "shl_set_element_variant", "shl_get_element_variant"]
 
 
 class ShlError(RuntimeError):
@@ -414,6 +416,18 @@ class Shell:
         enc = lambda e: None if e is None else e.encode()  # noqa: E731
         _check(self.lib.shl_set_cavity_functions(self.h, enc(rx), enc(ry), enc(rz)), "shl_set_cavity_functions",
                False)
+
+    def set_element_variant(self, v):
+        _check(self.lib.shl_set_element_variant(self.h, v), "shl_set_element_variant", False)
+
+    def element_variant(self):
+        """(variant id, name, tuning times in ms of all variants)."""
+        v = ctypes.c_int()
+        name = ctypes.create_string_buffer(64)
+        ms = np.zeros(9, dtype=np.float32)
+        _check(self.lib.shl_get_element_variant(self.h, ctypes.byref(v), name, 64, ms.ctypes.data),
+               "shl_get_element_variant", False)
+        return v.value, name.value.decode(), ms
 
     def scale_damping(self, factor):
         _check(self.lib.shl_scale_damping(self.h, factor), "shl_scale_damping", False)

@@ -14,7 +14,7 @@ def test_warm_start_needs_fewer_steps(cuda_ok):
                       gen_max=15000, tol=1e-6, max_steps=15000, log=None, level=3, hidden=[256, 256],
                       train_batch=128, mixed=False)
     plain, warm = r["test"]["fp64"]["plain"], r["test"]["fp64"]["warm"]
-    assert r["generation"]["converged"] >= 0.7 * 448, r
-    assert plain["converged"] >= 0.7 * 64, r
+    assert r["generation"]["converged"] >= 0.6 * 448, r
+    assert plain["converged"] >= 0.6 * 64, r
     assert warm["fallbacks"] <= 0.1 * 64, r
     assert warm["median_steps"] < plain["median_steps"], r
