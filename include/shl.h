@@ -46,7 +46,11 @@ typedef enum shl_status {
   SHL_ERR_CAPACITY = 104 /* a device buffer (e.g. contact pairs) is too small */
 } shl_status;
 
-/* ShellSystem::ContactType (ShellSystem.h:46). */
+/* ShellSystem::ContactType (ShellSystem.h:46).  LINEAR: closest points of the
+ * flat triangles (ShellShellContact.C); SMOOTH: closest points of the Loop
+ * limit surfaces of the two faces, searched from the pair's previous solution
+ * (SmoothShellShellContact.C); both distribute the contact force linearly over
+ * the faces' nodes (ShellSystem.C:1862-1890). */
 enum { SHL_CONTACT_LINEAR = 0, SHL_CONTACT_SMOOTH = 1, SHL_CONTACT_NONE = 2 };
 /* ShellSystem::CoordinateSystem (ShellSystem.h:42) for pressure_base. */
 enum { SHL_CS_LOCAL = 0, SHL_CS_CARTESIAN = 1, SHL_CS_CYLINDRICAL = 2, SHL_CS_SPHERICAL = 3 };
@@ -272,6 +276,14 @@ shl_status shl_get_contact_state(shl_ctx* ctx, uint32_t* pairs, uint8_t* stick,
 shl_status shl_set_contact_state(shl_ctx* ctx, const uint32_t* pairs, const uint8_t* stick,
                                  const double* spring_origin, const double* d2, size_t n_pairs,
                                  double du_sum);
+/* SMOOTH contact: per pair (same order as shl_get_contact_state) the limit
+ * surfaces' closest-point coordinates (v1, w1, v2, w2) in each face's patch
+ * frame (the face's irregular vertex first), which the next step's search starts
+ * from (SmoothShellShellContact::v, w, SmoothShellShellContact.C:9-14, 38-44).
+ * shl_set_contact_state resets them to 1/3; shl_set_contact_coords sets them
+ * (n_pairs must equal the current pair count). */
+shl_status shl_get_contact_coords(shl_ctx* ctx, double* x /* 4*cap */, size_t cap, size_t* n_pairs);
+shl_status shl_set_contact_coords(shl_ctx* ctx, const double* x, size_t n_pairs);
 /* Force a rebuild of the candidate list at the current positions
  * (compute_shell_shell_contact_candidates(true), ShellSystem.C:1910). */
 shl_status shl_rebuild_contacts(shl_ctx* ctx);

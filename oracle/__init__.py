@@ -62,6 +62,12 @@ def load():
         "oracle_get_cavity": (ctypes.c_int, [vp, vp, vp, vp]),
         "oracle_get_rejections": (ctypes.c_uint64, [vp]),
         "oracle_patch": (ctypes.c_int, [vp, u32, vp, ctypes.POINTER(u32)]),
+        "oracle_get_contact_coords": (sz, [vp, vp, sz]),
+        "oracle_set_contact_coords": (ctypes.c_int, [vp, vp, sz]),
+        "oracle_limit_eval": (ctypes.c_int, [vp, u32, d, d, vp]),
+        "oracle_limit_basis": (ctypes.c_int, [vp, u32, d, d, vp]),
+        "oracle_smooth_closest": (ctypes.c_int, [vp, u32, u32, vp, ctypes.POINTER(d), vp]),
+        "oracle_subdiv_table": (sz, [ctypes.c_int, vp, sz]),
         "oracle_basis_at": (ctypes.c_int, [vp, u32, d, d, vp]),
         "oracle_basis_cached": (ctypes.c_int, [vp, u32, vp, vp]),
         "oracle_elem_metric": (ctypes.c_int, [vp, u32, ctypes.c_int, vp]),
@@ -218,10 +224,46 @@ class Oracle:
         return {"avg_elem_size": out[0], "cell_size": out[1], "d_max": out[2], "bmin": out[3:6], "bmax": out[6:9]}
 
     def patch(self, eid):
-        nodes = np.zeros(12, dtype=np.uint32)
+        nodes = np.zeros(18, dtype=np.uint32)
         n = ctypes.c_uint32()
         self.lib.oracle_patch(self.h, eid, nodes.ctypes.data, ctypes.byref(n))
         return nodes[:n.value].copy()
+
+    def contact_coords(self):
+        k = self.lib.oracle_get_contact_coords(self.h, None, 0)
+        x = np.zeros((k, 4))
+        if k:
+            self.lib.oracle_get_contact_coords(self.h, x.ctypes.data, k)
+        return x
+
+    def set_contact_coords(self, x):
+        x = np.ascontiguousarray(x, dtype=np.float64).reshape(-1, 4)
+        if self.lib.oracle_set_contact_coords(self.h, x.ctypes.data, x.shape[0]) != 0:
+            raise RuntimeError(self.lib.oracle_error().decode())
+
+    def limit_eval(self, eid, v, w):
+        """SMOOTH: point and first / second derivatives of the limit surface, (6, 3)."""
+        out = np.zeros(18)
+        if self.lib.oracle_limit_eval(self.h, eid, v, w, out.ctypes.data) != 0:
+            raise RuntimeError(self.lib.oracle_error().decode())
+        return out.reshape(6, 3)
+
+    def limit_basis(self, eid, v, w):
+        """SMOOTH: limit-surface weights of the patch nodes at (v, w), (N + 6, 6)."""
+        n = len(self.patch(eid))
+        out = np.zeros(6 * n)
+        if self.lib.oracle_limit_basis(self.h, eid, v, w, out.ctypes.data) != 0:
+            raise RuntimeError(self.lib.oracle_error().decode())
+        return out.reshape(n, 6)
+
+    def smooth_closest(self, e1, e2, x0=(1 / 3, 1 / 3, 1 / 3, 1 / 3)):
+        x = np.array(x0, dtype=np.float64)
+        d2 = ctypes.c_double()
+        dc = np.zeros(3)
+        it = self.lib.oracle_smooth_closest(self.h, e1, e2, x.ctypes.data, ctypes.byref(d2), dc.ctypes.data)
+        if it < 0:
+            raise RuntimeError(self.lib.oracle_error().decode())
+        return x, d2.value, dc, it
 
     def basis_at(self, eid, v, w):
         n = len(self.patch(eid))
@@ -285,6 +327,15 @@ def friction_apply(f_normal, n, v, abs_v_normal, v_stop, k, mu_s, mu_d, damping,
                               abs_v_normal, v_stop, k, mu_s, mu_d, damping, ctypes.byref(st), so.ctypes.data,
                               arr[2].ctypes.data)
     return E.value, fc, st.value, so
+
+
+def subdiv_table(N):
+    """Subdivision table of valence N: (34, 3, 12, N + 6)."""
+    lib = load()
+    n = lib.oracle_subdiv_table(N, None, 0)
+    out = np.zeros(n)
+    lib.oracle_subdiv_table(N, out.ctypes.data, n)
+    return out.reshape(34, 3, 12, N + 6)
 
 
 def fixed_order_sum(x):

@@ -63,6 +63,20 @@ int oracle_get_cell_info(oracle* o, double* out /* 9 */);
 /* ---- known-answer helpers ---- */
 /* patch node ids of element eid in the oracle's patch order (up to 12) */
 int oracle_patch(oracle* o, uint32_t eid, uint32_t* nodes, uint32_t* n);
+/* SMOOTH contact: the minimiser's start / end point (v1, w1, v2, w2) in each
+ * face's patch frame, per pair in (eid1, eid2) order */
+size_t oracle_get_contact_coords(oracle* o, double* x, size_t cap);
+int oracle_set_contact_coords(oracle* o, const double* x, size_t n);
+/* SMOOTH: limit surface of face eid at patch-frame (v, w) at the current
+ * positions: out[3*k + c], k = point, d/dv, d/dw, d2/dv2, d2/dw2, d2/dvdw */
+int oracle_limit_eval(oracle* o, uint32_t eid, double v, double w, double* out);
+/* SMOOTH: the same as weights of the patch nodes, out[6*j + k] */
+int oracle_limit_basis(oracle* o, uint32_t eid, double v, double w, double* out);
+/* SMOOTH: closest points of the limit patches of e1 and e2 from start x[4];
+ * returns the iterations, x the minimiser, d2 and dc = p2 - p1 */
+int oracle_smooth_closest(oracle* o, uint32_t e1, uint32_t e2, double* x, double* d2, double* dc);
+/* subdivision table of valence N (shl_subdiv.h layout); returns its length */
+size_t oracle_subdiv_table(int N, double* out, size_t cap);
 /* unrotated basis of element eid at element parameters (v, w):
  * out[6*i + k], k = phi, d/dv, d/dw, d2/dv2, d2/dw2, d2/dvdw, in patch order.
  * Regular patches: any (v, w); irregular patches: the middle triangle of the

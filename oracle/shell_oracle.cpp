@@ -58,6 +58,8 @@
 #endif
 
 #include "../shell_gb300/csrc/shl_expr.h"
+#include "../shell_gb300/csrc/shl_smooth.h"
+#include "../shell_gb300/csrc/shl_subdiv.h"
 #include "../shell_gb300/csrc/shl_geom.h"
 
 namespace {
@@ -283,6 +285,10 @@ struct Contact {  // Contact.h:14-19, ShellShellContact.h:17-20
   bool stick = false;
   Point dc, spring_origin;
   Real v[2] = {0, 0}, w[2] = {0, 0};
+  // SMOOTH: the minimiser's (v1, w1, v2, w2) in each face's patch frame (irregular
+  // vertex first), kept from step to step; 1/3 for a new pair
+  // (SmoothShellShellContact.C:9-14)
+  Real x[4] = {1.0 / 3, 1.0 / 3, 1.0 / 3, 1.0 / 3};
 };
 
 }  // namespace
@@ -316,6 +322,7 @@ struct oracle {
   Real du_sum = 0, avg_elem_size = 0;
   Real bounds_min[3], bounds_max[3];
   Real last_cell_size = 0, last_d_max = 0;
+  std::vector<std::vector<double>> subdiv_tab = std::vector<std::vector<double>>(13);  // SMOOTH: by valence
   uint64_t n_cells_max = 0;
   std::vector<Contact*> candidates;
 
@@ -379,7 +386,45 @@ struct oracle {
     const std::vector<unsigned>& ce = ec[e1].close_elems;
     return std::binary_search(ce.begin(), ce.end(), e2);
   }
+  // limit patch of face e at the current positions (SubdivEvaluation.C:14-77)
+  void limit_patch(unsigned e, shl_limit_patch& lp) const {
+    const std::vector<unsigned>& pt = ec[e].patch;
+    lp.N = (int)pt.size() - 6;
+    for (size_t j = 0; j < pt.size(); ++j) lp.P[j] = p[pt[j]].x;
+    lp.tab = lp.N == 6 ? nullptr : subdiv_tab[lp.N].data();
+  }
+  // position of the patch's first vertex in the face's node list
+  int patch_rotation(unsigned e) const {
+    for (int k = 0; k < 3; ++k)
+      if (tri[3 * e + k] == ec[e].patch[0]) return k;
+    return 0;
+  }
+  // SmoothShellShellContact::compute (SmoothShellShellContact.C:16-60); the
+  // minimiser's coordinates are handed to the force distribution in the face's
+  // own node order (u, v, w of tri[0..2])
+  void smooth_compute(Contact& c) const {
+    shl_limit_patch A, B;
+    limit_patch(c.eid[0], A);
+    limit_patch(c.eid[1], B);
+    double d2, dc[3];
+    shl_smooth_closest(&A, &B, c.x, &d2, dc);
+    c.d2 = d2;
+    c.dc = Point(dc[0], dc[1], dc[2]);
+    for (int e = 0; e < 2; ++e) {
+      const int r = patch_rotation(c.eid[e]);
+      double lam[3];
+      lam[r] = 1 - c.x[2 * e] - c.x[2 * e + 1];
+      lam[(r + 1) % 3] = c.x[2 * e];
+      lam[(r + 2) % 3] = c.x[2 * e + 1];
+      c.v[e] = lam[1];
+      c.w[e] = lam[2];
+    }
+  }
   void pair_compute(Contact& c, bool on_mesh) const {
+    if (!on_mesh && P.shell_shell_contact == SHL_CONTACT_SMOOTH) {
+      smooth_compute(c);
+      return;
+    }
     const double* p1[3];
     const double* p2[3];
     for (int n = 0; n < 3; ++n) {
@@ -694,10 +739,6 @@ bool oracle::build(const shl_mesh* m, const shl_params* prm) {
     return false;
   }
   P = *prm;
-  if (P.shell_shell_contact == SHL_CONTACT_SMOOTH) {
-    g_err = "smooth contact is not restated";
-    return false;
-  }
   V = m->n_nodes;
   F = m->n_faces;
   X.resize(V);
@@ -735,6 +776,14 @@ bool oracle::build(const shl_mesh* m, const shl_params* prm) {
     ok = build_patch(e, ec[e].patch, N);
   }
   if (!ok) return false;
+  if (P.shell_shell_contact == SHL_CONTACT_SMOOTH)
+    for (unsigned e = 0; e < F; ++e) {
+      const int N = (int)ec[e].patch.size() - 6;
+      if (N != 6 && subdiv_tab[N].empty() && !shl_subdiv::build_table(N, subdiv_tab[N])) {
+        g_err = "subdivision table of valence " + std::to_string(N);
+        return false;
+      }
+    }
 #pragma omp parallel for
   for (int e = 0; e < (int)F; ++e) reinit_mod_and_reference(e);
 
@@ -1208,7 +1257,9 @@ void oracle::compute_shell_shell_contact_candidates(bool force) {
   cell_size = P.cell_size_mult * avg_elem_size;
   tolerance = P.cell_margin * cell_size;
   cell_size += tolerance;
-  const Real d_max = P.thickness + tolerance;
+  Real d_max = P.thickness + tolerance;
+  // SMOOTH: the limit surfaces may be closer than the facets (ShellSystem.C:1940-1944)
+  if (P.shell_shell_contact == SHL_CONTACT_SMOOTH) d_max += avg_elem_size;
   const Real d2_max = d_max * d_max;
   last_cell_size = cell_size;
   last_d_max = d_max;
@@ -1691,6 +1742,75 @@ int oracle_set_contact_state(oracle* o, const uint32_t* pairs, const uint8_t* st
   }
   o->du_sum = du_sum;
   return 0;
+}
+
+static std::vector<Contact*> sorted_contacts(oracle* o) {
+  std::vector<Contact*> cs;
+  for (Contact* c : o->candidates)
+    if (c) cs.push_back(c);
+  std::sort(cs.begin(), cs.end(), [](const Contact* x, const Contact* y) {
+    return x->eid[0] != y->eid[0] ? x->eid[0] < y->eid[0] : x->eid[1] < y->eid[1];
+  });
+  return cs;
+}
+
+size_t oracle_get_contact_coords(oracle* o, double* x, size_t cap) {
+  const std::vector<Contact*> cs = sorted_contacts(o);
+  for (size_t i = 0; i < cs.size() && i < cap; ++i)
+    for (int k = 0; k < 4; ++k) x[4 * i + k] = cs[i]->x[k];
+  return cs.size();
+}
+
+int oracle_set_contact_coords(oracle* o, const double* x, size_t n) {
+  const std::vector<Contact*> cs = sorted_contacts(o);
+  if (n != cs.size()) { g_err = "contact count mismatch"; return -1; }
+  for (size_t i = 0; i < n; ++i)
+    for (int k = 0; k < 4; ++k) cs[i]->x[k] = x[4 * i + k];
+  return 0;
+}
+
+int oracle_limit_eval(oracle* o, uint32_t eid, double v, double w, double* out) {
+  if (eid >= o->F || o->P.shell_shell_contact != SHL_CONTACT_SMOOTH) { g_err = "limit evaluation needs SMOOTH"; return -1; }
+  shl_limit_patch lp;
+  o->limit_patch(eid, lp);
+  double r[6][3];
+  shl_limit_eval(&lp, v, w, 2, r);
+  for (int k = 0; k < 6; ++k)
+    for (int c = 0; c < 3; ++c) out[3 * k + c] = r[k][c];
+  return 0;
+}
+
+int oracle_limit_basis(oracle* o, uint32_t eid, double v, double w, double* out) {
+  if (eid >= o->F || o->P.shell_shell_contact != SHL_CONTACT_SMOOTH) { g_err = "limit evaluation needs SMOOTH"; return -1; }
+  shl_limit_patch lp;
+  o->limit_patch(eid, lp);
+  const int np = lp.N + 6;
+  std::vector<double> E(3 * (size_t)np, 0.0);
+  for (int j = 0; j < np; ++j) lp.P[j] = &E[3 * j];
+  for (int j0 = 0; j0 < np; j0 += 3) {
+    std::fill(E.begin(), E.end(), 0.0);
+    for (int c = 0; c < 3 && j0 + c < np; ++c) E[3 * (j0 + c) + c] = 1.0;
+    double r[6][3];
+    shl_limit_eval(&lp, v, w, 2, r);
+    for (int c = 0; c < 3 && j0 + c < np; ++c)
+      for (int k = 0; k < 6; ++k) out[6 * (j0 + c) + k] = r[k][c];
+  }
+  return 0;
+}
+
+int oracle_smooth_closest(oracle* o, uint32_t e1, uint32_t e2, double* x, double* d2, double* dc) {
+  if (e1 >= o->F || e2 >= o->F || o->P.shell_shell_contact != SHL_CONTACT_SMOOTH) { g_err = "needs SMOOTH"; return -1; }
+  shl_limit_patch A, B;
+  o->limit_patch(e1, A);
+  o->limit_patch(e2, B);
+  return shl_smooth_closest(&A, &B, x, d2, dc);
+}
+
+size_t oracle_subdiv_table(int N, double* out, size_t cap) {
+  std::vector<double> tab;
+  if (N < 3 || N > 12 || N == 6 || !shl_subdiv::build_table(N, tab)) return 0;
+  for (size_t i = 0; i < tab.size() && i < cap; ++i) out[i] = tab[i];
+  return tab.size();
 }
 
 int oracle_rebuild_contacts(oracle* o) {

@@ -16,6 +16,7 @@
 #include "../../include/shl.h"
 #include "shl_geom.h"
 #include "shl_internal.cuh"
+#include "shl_subdiv.h"
 #include "shl_setup.h"
 
 using namespace shl;
@@ -157,9 +158,12 @@ bool validate(const shl_params& p, std::string& err) {
   if (p.damping_alpha < 0 || p.damping_beta < 0 || p.damping_gamma < 0) { err = "damping must be >= 0"; return false; }
   if (p.pressure_base < SHL_CS_LOCAL || p.pressure_base > SHL_CS_SPHERICAL) { err = "bad pressure_base"; return false; }
   if (p.pressure_dir < 0 || p.pressure_dir > 2) { err = "bad pressure_dir"; return false; }
-  if (p.shell_shell_contact == SHL_CONTACT_SMOOTH) { err = "smooth (limit-surface) contact is not supported"; return false; }
-  if (p.shell_shell_contact != SHL_CONTACT_LINEAR && p.shell_shell_contact != SHL_CONTACT_NONE) { err = "bad shell_shell_contact"; return false; }
-  if (p.shell_shell_contact == SHL_CONTACT_LINEAR) {
+  if (p.shell_shell_contact != SHL_CONTACT_LINEAR && p.shell_shell_contact != SHL_CONTACT_SMOOTH &&
+      p.shell_shell_contact != SHL_CONTACT_NONE) {
+    err = "bad shell_shell_contact";
+    return false;
+  }
+  if (p.shell_shell_contact != SHL_CONTACT_NONE) {
     if (p.mu_s < 0 || p.mu_d < 0 || p.self_damping < 0 || p.self_friction_damping < 0) { err = "contact coefficients must be >= 0"; return false; }
     if (!(p.cell_size_mult > 0) || p.cell_margin < 0 || !(p.neighbor_margin > 0)) { err = "bad linked-cell parameters"; return false; }
     if (!(p.friction_stop_velocity > 0)) { err = "friction_stop_velocity must be > 0"; return false; }
@@ -450,16 +454,20 @@ shl_status create_common(shl_ctx* c, const std::vector<double>& pscale_orig, shl
     ALLOC(b.cav_efric, V);
   }
   ALLOC(b.face, (size_t)FF_COUNT * F);
-  ALLOC(b.patch, 12 * (size_t)F);
+  ALLOC(b.patch, (size_t)S.patch_rows * F);
   const bool fp32 = params->precision == SHL_PREC_FP32;
   if (fp32) {
-    ALLOC(b.qe32, 36 * (size_t)F);
+    ALLOC(b.qe32, 3 * (size_t)S.n_slots_total);
     ALLOC(b.up32, nd);
     ALLOC(b.face32, (size_t)F32_COUNT * F);
   }
-  ALLOC(b.qe, fp32 ? 1 : 36 * (size_t)F);
+  ALLOC(b.qe, fp32 ? 1 : 3 * (size_t)S.n_slots_total);
   ALLOC(b.gather_ptr, V + 1);
   ALLOC(b.gather_ent, S.gather_ent.size());
+  if (params->shell_cavity_contact) {
+    ALLOC(b.node_face_ptr, V + 1);
+    ALLOC(b.node_face, S.node_face.size());
+  }
   ALLOC(b.tri, 3 * (size_t)F);
   ALLOC(b.perm, F);
   ALLOC(b.pscale, F);
@@ -474,6 +482,7 @@ shl_status create_common(shl_ctx* c, const std::vector<double>& pscale_orig, shl
     d.count = g.count;
     d.block_start = blocks;
     d.n_slots = g.n_slots;
+    d.slot_base = g.slot_base;
     d.basis_off = (int32_t)basis.size();
     basis.insert(basis.end(), g.basis.begin(), g.basis.end());
     blocks += (g.count + kBlock - 1) / kBlock;
@@ -502,7 +511,8 @@ shl_status create_common(shl_ctx* c, const std::vector<double>& pscale_orig, shl
   b.ptable_cap = kTableCap;
 
   // contact buffers
-  const bool contact = params->shell_shell_contact == SHL_CONTACT_LINEAR;
+  const bool contact = params->shell_shell_contact != SHL_CONTACT_NONE;
+  const bool smooth = params->shell_shell_contact == SHL_CONTACT_SMOOTH;
   uint64_t n_cells0 = 0, entries0 = 0;
   uint32_t n_cells_cap = 1, entries_cap = 1, pairs_cap = 1, csr_cap = 1, cand_cap = 1;
   if (contact) {
@@ -535,6 +545,11 @@ shl_status create_common(shl_ctx* c, const std::vector<double>& pscale_orig, shl
     ALLOC(b.seg_count, F);
     ALLOC(b.pforce, kPairOut * (size_t)pairs_cap);
     ALLOC(b.csr_count, V); ALLOC(b.csr_ptr, V + 1); ALLOC(b.csr_ent, csr_cap); ALLOC(b.csr_fill, V);
+    if (smooth) {
+      ALLOC(b.pvw[0], 4 * (size_t)pairs_cap); ALLOC(b.pvw[1], 4 * (size_t)pairs_cap);
+      ALLOC(b.new_x, 4 * (size_t)pairs_cap); ALLOC(b.cand_x, 4 * (size_t)cand_cap);
+      ALLOC(b.inv_perm, F); ALLOC(b.fsm, F);
+    }
   }
 #undef ALLOC
 
@@ -551,11 +566,44 @@ shl_status create_common(shl_ctx* c, const std::vector<double>& pscale_orig, shl
   if ((st = upload(c, b.patch, S.patch.data(), S.patch.size())) != SHL_OK) return fail(st);
   if ((st = upload(c, b.gather_ptr, S.gather_ptr.data(), S.gather_ptr.size())) != SHL_OK) return fail(st);
   if ((st = upload(c, b.gather_ent, S.gather_ent.data(), S.gather_ent.size())) != SHL_OK) return fail(st);
+  if (params->shell_cavity_contact) {
+    if ((st = upload(c, b.node_face_ptr, S.node_face_ptr.data(), S.node_face_ptr.size())) != SHL_OK) return fail(st);
+    if ((st = upload(c, b.node_face, S.node_face.data(), S.node_face.size())) != SHL_OK) return fail(st);
+  }
   if ((st = upload(c, b.tri, S.tri.data(), S.tri.size())) != SHL_OK) return fail(st);
   if ((st = upload(c, b.perm, S.perm.data(), S.perm.size())) != SHL_OK) return fail(st);
   std::vector<double> pscale(F);
   for (uint32_t i = 0; i < F; ++i) pscale[i] = pscale_orig[S.perm[i]];
   if ((st = upload(c, b.pscale, pscale.data(), F)) != SHL_OK) return fail(st);
+  int32_t stab_off[13];
+  for (int k = 0; k < 13; ++k) stab_off[k] = -1;
+  if (smooth) {
+    // per original face: valence of the patch's first vertex | (its position in the face) << 8
+    std::vector<int32_t> fsm(F);
+    std::vector<int> vals;
+    for (const PatchGroup& g : S.groups)
+      for (uint32_t i = g.first; i < g.first + g.count; ++i) {
+        const uint32_t e = S.perm[i];
+        int r = 0;
+        for (int k = 0; k < 3; ++k)
+          if ((int32_t)S.tri[3 * (size_t)e + k] == S.patch[i]) r = k;
+        fsm[e] = g.valence | (r << 8);
+        if (g.valence != 6 && std::find(vals.begin(), vals.end(), g.valence) == vals.end()) vals.push_back(g.valence);
+      }
+    std::vector<double> tabs;
+    for (int N : vals) {
+      std::vector<double> t;
+      if (!shl_subdiv::build_table(N, t)) { g_err = "subdivision table of valence " + std::to_string(N); return fail(SHL_ERR_ARG); }
+      stab_off[N] = (int32_t)tabs.size();
+      tabs.insert(tabs.end(), t.begin(), t.end());
+    }
+    if (!tabs.empty()) {
+      if ((st = dev_alloc(c, &b.stab, tabs.size())) != SHL_OK) return fail(st);
+      if ((st = upload(c, b.stab, tabs.data(), tabs.size())) != SHL_OK) return fail(st);
+    }
+    if ((st = upload(c, b.fsm, fsm.data(), F)) != SHL_OK) return fail(st);
+    if ((st = upload(c, b.inv_perm, S.inv_perm.data(), F)) != SHL_OK) return fail(st);
+  }
   if (contact) {
     if ((st = upload(c, b.close_ptr, S.close_ptr.data(), S.close_ptr.size())) != SHL_OK) return fail(st);
     if (!S.close_list.empty() && (st = upload(c, b.close_list, S.close_list.data(), S.close_list.size())) != SHL_OK)
@@ -611,6 +659,8 @@ shl_status create_common(shl_ctx* c, const std::vector<double>& pscale_orig, shl
   sc.csr_cap = csr_cap;
   sc.cand_cap = cand_cap;
   sc.contact = contact ? 1 : 0;
+  sc.smooth = smooth ? 1 : 0;
+  for (int k = 0; k < 13; ++k) sc.stab_off[k] = stab_off[k];
   sc.friction = (contact && (p.mu_s != 0 || p.mu_d != 0)) ? 1 : 0;
   sc.pressure_base = p.pressure_base;
   sc.pressure_dir = p.pressure_dir;
@@ -1276,6 +1326,31 @@ shl_status shl_get_contact_pairs(shl_ctx* c, uint32_t* pairs, size_t cap, size_t
   return shl_get_contact_state(c, pairs, nullptr, nullptr, nullptr, cap, n_pairs, nullptr);
 }
 
+shl_status shl_get_contact_coords(shl_ctx* c, double* x, size_t cap, size_t* n_pairs) {
+  if (!c) return SHL_ERR_ARG;
+  Ctl h;
+  SHL_TRY(ctl_get(c, h));
+  if (n_pairs) *n_pairs = h.n_pairs;
+  if (!c->sc.smooth) { g_err = "closest-point coordinates are kept for SMOOTH contact only"; return SHL_ERR_ARG; }
+  const size_t n = std::min<size_t>(cap, h.n_pairs);
+  if (x && n) {
+    SHL_CUDA_TRY(cudaMemcpyAsync(x, c->b.pvw[0], 4 * n * 8, cudaMemcpyDeviceToHost, c->stream));
+    SHL_CUDA_TRY(cudaStreamSynchronize(c->stream));
+  }
+  return SHL_OK;
+}
+
+shl_status shl_set_contact_coords(shl_ctx* c, const double* x, size_t n) {
+  if (!c || (n && !x)) return SHL_ERR_ARG;
+  if (!c->sc.smooth) { g_err = "closest-point coordinates are kept for SMOOTH contact only"; return SHL_ERR_ARG; }
+  Ctl h;
+  SHL_TRY(ctl_get(c, h));
+  if (n != h.n_pairs) { g_err = "coordinate count differs from the pair count"; return SHL_ERR_ARG; }
+  if (n) SHL_TRY(upload(c, c->b.pvw[0], x, 4 * n));
+  SHL_CUDA_TRY(cudaStreamSynchronize(c->stream));
+  return SHL_OK;
+}
+
 shl_status shl_set_contact_state(shl_ctx* c, const uint32_t* pairs, const uint8_t* stick, const double* spring_origin,
                                  const double* d2, size_t n, double du_sum) {
   if (!c) return SHL_ERR_ARG;
@@ -1313,6 +1388,10 @@ shl_status shl_set_contact_state(shl_ctx* c, const uint32_t* pairs, const uint8_
     SHL_TRY(upload(c, c->b.pstick[0], st.data(), n));
     SHL_TRY(upload(c, c->b.porig[0], org.data(), 3 * n));
     SHL_TRY(upload(c, c->b.pd2[0], dd.data(), n));
+    if (c->sc.smooth) {  // loaded pairs restart their closest-point search at 1/3
+      std::vector<double> x(4 * n, 1.0 / 3.0);
+      SHL_TRY(upload(c, c->b.pvw[0], x.data(), 4 * n));
+    }
   }
   SHL_TRY(upload(c, c->b.pair_ptr[0], ptr.data(), F + 1));
   Ctl h;
@@ -1367,7 +1446,7 @@ shl_status shl_residual(shl_ctx* c, double pressure, int flags, double* rel, dou
     SHL_CUDA_TRY(cudaMemcpyAsync(c->d_node_off, c->node_off.data(), (ns + 1) * sizeof(uint32_t),
                                  cudaMemcpyHostToDevice, c->stream));
   }
-  if (fp64 && ctx32 && !c->qe64) SHL_TRY(dev_alloc(c, &c->qe64, 36 * (size_t)c->S.F));
+  if (fp64 && ctx32 && !c->qe64) SHL_TRY(dev_alloc(c, &c->qe64, 3 * (size_t)c->S.n_slots_total));
   if (correct && !c->b.fcorr) {
     SHL_TRY(dev_alloc(c, &c->b.fcorr, nd));
     SHL_TRY(dev_alloc(c, &c->f32, nd));
@@ -1634,9 +1713,9 @@ shl_status shl_internal_force_noalloc(shl_ctx* c, const double* u_dev, double pr
             "evaluated here";
     return SHL_ERR_ARG;
   }
-  if (c->S.F > noalloc_max_faces()) {
+  if (c->S.n_slots_total > 12 * noalloc_max_faces()) {
     g_err = "shl_internal_force_noalloc: " + std::to_string(c->S.F) + " faces exceed the scratch limit of " +
-            std::to_string(noalloc_max_faces()) + " faces";
+            std::to_string(noalloc_max_faces()) + " regular faces";
     return SHL_ERR_CAPACITY;
   }
   const double p = c->P.compat_zero_pressure ? pressure * 0.0 : pressure;

@@ -145,7 +145,9 @@ __global__ void __launch_bounds__(kBlock) k_rb_aabb(DevBuf b, StepConst sc) {
   double cell_size = __dmul_rn(sc.cell_size_mult, avg);
   const double tolerance = __dmul_rn(sc.cell_margin, cell_size);
   cell_size = __dadd_rn(cell_size, tolerance);
-  const double d_max = __dadd_rn(sc.thickness, tolerance);
+  double d_max = __dadd_rn(sc.thickness, tolerance);
+  // SMOOTH: the limit surfaces may be closer than the facets (ShellSystem.C:1940-1944)
+  if (sc.smooth) d_max = __dadd_rn(d_max, avg);
   ctl->cell_size = cell_size;
   ctl->d_max = d_max;
   ctl->d2_max = __dmul_rn(d_max, d_max);
@@ -458,7 +460,7 @@ __global__ void __launch_bounds__(kBlock) k_rb_cand(DevBuf b, StepConst sc) {
       const int* lo2 = b.cell_lo + 3 * (size_t)e2;
       if ((uint32_t)max(l10, lo2[0]) != cx || (uint32_t)max(l11, lo2[1]) != cy || (uint32_t)max(l12, lo2[2]) != cz)
         continue;
-      {
+      if (!sc.smooth) {  // a facet bound; SMOOTH distances are between limit surfaces
         const float* Q2[3];
         for (int q = 0; q < 3; ++q) Q2[q] = b.p32 + 3 * (size_t)b.tri[3 * (size_t)e2 + q];
         if (certainly_apart32(Q1, Q2, d_max32)) continue;
@@ -481,6 +483,7 @@ __global__ void __launch_bounds__(kBlock) k_rb_cand(DevBuf b, StepConst sc) {
 }
 
 // closest-point test of each candidate (rounded operation by operation)
+template <bool SMOOTH>
 __global__ void __launch_bounds__(kBlock) k_rb_narrow(DevBuf b, StepConst sc) {
   Ctl* ctl = b.ctl;
   if (rb_off(ctl)) return;
@@ -495,7 +498,13 @@ __global__ void __launch_bounds__(kBlock) k_rb_narrow(DevBuf b, StepConst sc) {
       P2[q] = b.p + 3 * (size_t)b.tri[3 * (size_t)e2 + q];
     }
     shl_pair_geom g;
-    shl_pair_compute(P1, P2, &g);
+    if (SMOOTH) {  // a new SmoothShellShellContact starts at (1/3, 1/3) (SmoothShellShellContact.C:9-14)
+      double x[4] = {1.0 / 3.0, 1.0 / 3.0, 1.0 / 3.0, 1.0 / 3.0};
+      smooth_pair(b, sc, e1, e2, x, &g);
+      for (int k = 0; k < 4; ++k) b.cand_x[4 * (size_t)i + k] = x[k];
+    } else {
+      shl_pair_compute(P1, P2, &g);
+    }
     if (g.d2 <= 0.0) atomicMax(&ctl->problem, (int)SHL_CONTACT_PROBLEM);
     const bool ok = !(g.d2 > d2_max);  // ShellSystem.C:2082
     b.cand_d2[i] = g.d2;
@@ -519,6 +528,8 @@ __global__ void __launch_bounds__(kBlock) k_rb_scatter_new(DevBuf b, StepConst s
     const uint32_t pos = b.new_off[e1] + atomicAdd(&b.new_fill[e1], 1u);
     b.new_e2[pos] = b.cand_e2[i];
     b.new_d2[pos] = b.cand_d2[i];
+    if (sc.smooth)
+      for (int k = 0; k < 4; ++k) b.new_x[4 * (size_t)pos + k] = b.cand_x[4 * (size_t)i + k];
   }
 }
 
@@ -534,18 +545,26 @@ __global__ void __launch_bounds__(kBlock) k_rb_assemble(DevBuf b, StepConst sc) 
   const uint32_t off = nn ? b.new_off[e1] : 0u;
   uint32_t* ne2 = b.new_e2 + off;
   double* nd2 = b.new_d2 + off;
+  double* nx = sc.smooth ? b.new_x + 4 * (size_t)off : nullptr;
   // insertion sort of this face's new pairs by e2 (the segment belongs to this thread)
   for (uint32_t k = 1; k < nn; ++k) {
     const uint32_t x = ne2[k];
     const double d = nd2[k];
+    double xs[4];
+    if (nx)
+      for (int c = 0; c < 4; ++c) xs[c] = nx[4 * k + c];
     uint32_t q = k;
     while (q > 0 && ne2[q - 1] > x) {
       ne2[q] = ne2[q - 1];
       nd2[q] = nd2[q - 1];
+      if (nx)
+        for (int c = 0; c < 4; ++c) nx[4 * q + c] = nx[4 * (q - 1) + c];
       --q;
     }
     ne2[q] = x;
     nd2[q] = d;
+    if (nx)
+      for (int c = 0; c < 4; ++c) nx[4 * q + c] = xs[c];
   }
   uint32_t io = o0, in = 0;
   for (;;) {
@@ -559,12 +578,16 @@ __global__ void __launch_bounds__(kBlock) k_rb_assemble(DevBuf b, StepConst sc) 
       b.pstick[1][dst] = b.pstick[0][io];
       b.pd2[1][dst] = b.pd2[0][io];
       for (int c = 0; c < 3; ++c) b.porig[1][3 * (size_t)dst + c] = b.porig[0][3 * (size_t)io + c];
+      if (nx)
+        for (int c = 0; c < 4; ++c) b.pvw[1][4 * (size_t)dst + c] = b.pvw[0][4 * (size_t)io + c];
       ++io;
     } else {
       b.pe2[1][dst] = ne2[in];
       b.pstick[1][dst] = 0;
       b.pd2[1][dst] = nd2[in];
       for (int c = 0; c < 3; ++c) b.porig[1][3 * (size_t)dst + c] = 0.0;
+      if (nx)
+        for (int c = 0; c < 4; ++c) b.pvw[1][4 * (size_t)dst + c] = nx[4 * in + c];
       ++in;
     }
     ++dst;
@@ -582,6 +605,8 @@ __global__ void k_rb_copyback(DevBuf b, StepConst sc) {
     b.pstick[0][j] = b.pstick[1][j];
     b.pd2[0][j] = b.pd2[1][j];
     for (int c = 0; c < 3; ++c) b.porig[0][3 * (size_t)j + c] = b.porig[1][3 * (size_t)j + c];
+    if (sc.smooth)
+      for (int c = 0; c < 4; ++c) b.pvw[0][4 * (size_t)j + c] = b.pvw[1][4 * (size_t)j + c];
   }
   for (uint32_t f = blockIdx.x * blockDim.x + threadIdx.x; f <= sc.F; f += stride) b.pair_ptr[0][f] = b.pair_ptr[1][f];
 }
@@ -700,7 +725,10 @@ void launch_rebuild(const DevBuf& b, const StepConst& sc, cudaStream_t s) {
     k_rb_cand<<<g, kBlock, 0, s>>>(b, sc);
     uint32_t gc = nblk(sc.cand_cap);
     if (gc > 16 * 152) gc = 16 * 152;
-    k_rb_narrow<<<gc, kBlock, 0, s>>>(b, sc);
+    if (sc.smooth)
+      k_rb_narrow<true><<<gc, kBlock, 0, s>>>(b, sc);
+    else
+      k_rb_narrow<false><<<gc, kBlock, 0, s>>>(b, sc);
     launch_scan(&b.ctl->rebuild, b.ctl, b.new_cnt, b.new_off, nullptr, sc.F, sc.F, b.scan_block, &b.ctl->n_new,
                 false, sc.pairs_cap, true, s);
     k_rb_scatter_new<<<gc, kBlock, 0, s>>>(b, sc);

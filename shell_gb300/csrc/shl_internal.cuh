@@ -19,6 +19,8 @@
 #include <cstdint>
 
 #include "shl_expr.h"
+#include "shl_geom.h"
+#include "shl_smooth.h"
 #include <string>
 #include <vector>
 
@@ -41,6 +43,8 @@ struct GroupDesc {
   uint32_t block_start; // first block of the element launch for this group
   int32_t n_slots;
   int32_t basis_off;    // offset into the basis table (doubles)
+  uint32_t slot_base;   // first element-force slot: face i owns slot_base + (i - first) * n_slots + [0, n_slots)
+  uint32_t pad;
 };
 
 // All patch groups of one shell, passed by value to the element kernel; the
@@ -144,7 +148,9 @@ struct StepConst {
   const double* pressure_table;  // device, or null
   uint64_t n_cells_max;
   uint32_t n_cells_cap, entries_cap, pairs_cap, csr_cap, cand_cap;
-  int32_t contact;   // 1 if self-contact is on
+  int32_t contact;   // 1 if self-contact is on (LINEAR or SMOOTH)
+  int32_t smooth;    // 1 for SMOOTH (limit-surface) self-contact
+  int32_t stab_off[13];  // SMOOTH: offset of the subdivision table of valence N in DevBuf::stab, or -1
   int32_t friction;  // 1 if mu_s or mu_d != 0
   int32_t pressure_base, pressure_dir;
   int32_t compat_zero_pressure;
@@ -182,13 +188,14 @@ struct DevBuf {
   double* fcorr;      // 3V defect correction added to the FP32 force in a step, or null
   double* face;       // FF_COUNT * F
   double* pscale;     // F (internal order): factor on the step's pressure (per shell)
-  int32_t* patch;     // 12 * F
-  double* qe;         // F * 12 * 3
+  int32_t* patch;     // patch_rows * F, slot-major
+  double* qe;         // 3 per element-force slot (GroupDesc::slot_base)
   float* face32;      // F32_COUNT * F (FP32 element path)
-  float* qe32;        // F * 12 * 3 (FP32 element path)
+  float* qe32;        // 3 per element-force slot (FP32 element path)
   float* up32;        // 3V, FP32 copy of u_pred (FP32 element path)
   float *uph, *upl;   // 3V, u_pred as a float pair hi + lo (the FP64 path's contractions)
   uint32_t *gather_ptr, *gather_ent;
+  uint32_t *node_face_ptr, *node_face;  // V+1 / faces of each node (original ids; cavity contact only)
   uint32_t* tri;      // 3F original order
   uint32_t *perm;     // internal -> original
   double *area, *kG, *kM, *etens, *ebend;  // original order
@@ -215,11 +222,50 @@ struct DevBuf {
   uint8_t* cand_ok;
   uint32_t* seg_count;         // per-face pair counts (F)
   double* pforce;              // kPairOut per pair: f_contact(3), v1, w1, v2, w2, Eself, Efric
+  // SMOOTH contact
+  double* pvw[2];              // 4 per pair: the closest-point search's (v1, w1, v2, w2), patch frames
+  double* new_x;               // 4 per new pair of a rebuild
+  double* cand_x;              // 4 per candidate
+  uint32_t* inv_perm;          // original -> internal face
+  int32_t* fsm;                // per original face: valence | (position of the patch's first vertex) << 8
+  double* stab;                // subdivision tables of the valences present
   uint32_t *csr_count, *csr_ptr, *csr_ent, *csr_fill;  // per-node contact CSR
   Ctl* ctl;
   double* ptable;              // per-step pressure table (capacity)
   uint32_t ptable_cap;
 };
+
+#ifdef __CUDACC__
+// Limit patch of original face e at the current positions b.p (SMOOTH contact).
+__device__ __forceinline__ void smooth_patch(const DevBuf& b, const StepConst& sc, uint32_t e, shl_limit_patch& lp) {
+  const uint32_t i = b.inv_perm[e];
+  const int N = b.fsm[e] & 0xff;
+  lp.N = N;
+  for (int j = 0; j < N + 6; ++j) lp.P[j] = b.p + 3 * (size_t)b.patch[(size_t)j * sc.F + i];
+  lp.tab = N == 6 ? nullptr : b.stab + sc.stab_off[N];
+}
+
+// Closest points of the limit patches of a pair from the start x[4] (patch
+// frames); fills the pair geometry with the coordinates in each face's own node
+// order (the force distribution's u, v, w of tri[0..2]).
+__device__ __forceinline__ void smooth_pair(const DevBuf& b, const StepConst& sc, uint32_t e1, uint32_t e2,
+                                            double* x, shl_pair_geom* g) {
+  shl_limit_patch A, B;
+  smooth_patch(b, sc, e1, A);
+  smooth_patch(b, sc, e2, B);
+  shl_smooth_closest(&A, &B, x, &g->d2, g->dc);
+  const uint32_t e[2] = {e1, e2};
+  for (int t = 0; t < 2; ++t) {
+    const int r = b.fsm[e[t]] >> 8;
+    double lam[3];
+    lam[r] = SHL_SUB(SHL_SUB(1.0, x[2 * t]), x[2 * t + 1]);
+    lam[(r + 1) % 3] = x[2 * t];
+    lam[(r + 2) % 3] = x[2 * t + 1];
+    g->v[t] = lam[1];
+    g->w[t] = lam[2];
+  }
+}
+#endif
 
 // ---- launchers (shl_kernels.cu) ----
 void launch_predict(const DevBuf& b, const StepConst& sc, int cur, cudaStream_t s);

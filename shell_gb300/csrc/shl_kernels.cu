@@ -374,7 +374,7 @@ __device__ __forceinline__ double dot3(const double* a, const double* b) {
 // One face: deformed metric, stress resultants, and the per-slot force
 // share qe_s = sum_k B[s][k] Z_k (internal minus pressure), see the comments.
 template <int NP, bool DFG = false, bool DFQ = false>
-__device__ __forceinline__ ElemOut element_force(uint32_t i, int np_rt, const double* __restrict__ B,
+__device__ __forceinline__ ElemOut element_force(uint32_t i, int np_rt, uint32_t slot0, const double* __restrict__ B,
                                                  const DevBuf& b, const StepConst& sc, double pressure,
                                                  double vol_p) {
   const uint32_t F = sc.F;
@@ -528,7 +528,7 @@ __device__ __forceinline__ ElemOut element_force(uint32_t i, int np_rt, const do
     Z[4][c] = c11b * Y11 + c22b * Y22 + c12b * Y12;
     Z[5][c] = c11c * Y11 + c22c * Y22 + c12c * Y12;
   }
-  double* qe = b.qe + (size_t)i * 36;
+  double* qe = b.qe + 3 * (size_t)slot0;
   if (DFQ) {
     const float* Bh = reinterpret_cast<const float*>(B + kMaxSlots * 6);
     const float* Bl = Bh + kMaxSlots * 6;
@@ -584,7 +584,7 @@ __device__ __forceinline__ ElemOut element_force(uint32_t i, int np_rt, const do
 //              of a1 x a2 (no cancellation), shear doubled.
 // The per-slot shares are written in FP32.
 template <int NP>
-__device__ __forceinline__ ElemOut element_force32(uint32_t i, int np_rt, const float* __restrict__ B,
+__device__ __forceinline__ ElemOut element_force32(uint32_t i, int np_rt, uint32_t slot0, const float* __restrict__ B,
                                                    const DevBuf& b, const StepConst& sc, float pressure,
                                                    float vol_p) {
   const uint32_t F = sc.F;
@@ -730,7 +730,7 @@ __device__ __forceinline__ ElemOut element_force32(uint32_t i, int np_rt, const 
       Z[4][c] = c11b * Y11 + c22b * Y22 + c12b * Y12;
       Z[5][c] = c11c * Y11 + c22c * Y22 + c12c * Y12;
     }
-    float* qe = b.qe32 + (size_t)i * 36;
+    float* qe = b.qe32 + 3 * (size_t)slot0;
 #pragma unroll
     for (int s = 0; s < (NP > 0 ? NP : kMaxSlots); ++s) {
       if (NP == 0 && s >= np) break;
@@ -777,14 +777,15 @@ __global__ void __launch_bounds__(BS, MINB) k_elements32(DevBuf b, StepConst sc,
   const double pressure = ctl->pressure;
   const float vol_p = (float)ctl->volume_pressure;
   const uint32_t i = gd.first + li;
+  const uint32_t slot0 = gd.slot_base + li * (uint32_t)gd.n_slots;
   const float pr = (float)(pressure * __ldg(&b.pscale[i]));
   ElemOut o;
   if (gd.n_slots == 12)
-    o = element_force32<12>(i, 12, sB, b, sc, pr, vol_p);
+    o = element_force32<12>(i, 12, slot0, sB, b, sc, pr, vol_p);
   else if (gd.n_slots == 11)
-    o = element_force32<11>(i, 11, sB, b, sc, pr, vol_p);
+    o = element_force32<11>(i, 11, slot0, sB, b, sc, pr, vol_p);
   else
-    o = element_force32<0>(i, gd.n_slots, sB, b, sc, pr, vol_p);
+    o = element_force32<0>(i, gd.n_slots, slot0, sB, b, sc, pr, vol_p);
   const uint32_t e = __ldg(&b.perm[i]);
   const float ia = 1.f / (float)o.area;
   b.area[e] = o.area;
@@ -816,15 +817,16 @@ __global__ void __launch_bounds__(BS, MINB) k_elements(DevBuf b, StepConst sc, E
   if (li >= gd.count) return;
   const double pressure = ctl->pressure, vol_p = ctl->volume_pressure;
   const uint32_t i = gd.first + li;
+  const uint32_t slot0 = gd.slot_base + li * (uint32_t)gd.n_slots;
   const double* B = sB;
   const double pr = pressure * __ldg(&b.pscale[i]);
   ElemOut o;
   if (gd.n_slots == 12)
-    o = element_force<12, DFG, DFQ>(i, 12, B, b, sc, pr, vol_p);
+    o = element_force<12, DFG, DFQ>(i, 12, slot0, B, b, sc, pr, vol_p);
   else if (gd.n_slots == 11)
-    o = element_force<11, DFG, DFQ>(i, 11, B, b, sc, pr, vol_p);
+    o = element_force<11, DFG, DFQ>(i, 11, slot0, B, b, sc, pr, vol_p);
   else
-    o = element_force<0, DFG, DFQ>(i, gd.n_slots, B, b, sc, pr, vol_p);
+    o = element_force<0, DFG, DFQ>(i, gd.n_slots, slot0, B, b, sc, pr, vol_p);
   const uint32_t e = __ldg(&b.perm[i]);
   b.area[e] = o.area;
   b.kG[e] = o.kg / o.area;
@@ -868,6 +870,7 @@ __global__ void __launch_bounds__(kBlock) k_elem_totals(DevBuf b, StepConst sc) 
 
 // -------------------------------------------------------- contact force --
 // One candidate pair; ShellSystem.C:1803-1900.  Rounded operation by operation.
+template <bool SMOOTH>
 __global__ void __launch_bounds__(kBlock) k_contact_force(DevBuf b, StepConst sc) {
   Ctl* ctl = b.ctl;
   if (inactive(ctl)) return;
@@ -896,7 +899,14 @@ __global__ void __launch_bounds__(kBlock) k_contact_force(DevBuf b, StepConst sc
       P2[k] = b.p + 3 * (size_t)nid[1][k];
     }
     shl_pair_geom g;
-    shl_pair_compute(P1, P2, &g);
+    if (SMOOTH) {  // SmoothShellShellContact::compute from the pair's previous solution
+      double x[4];
+      for (int k = 0; k < 4; ++k) x[k] = b.pvw[0][4 * (size_t)j + k];
+      smooth_pair(b, sc, e[0], e[1], x, &g);
+      for (int k = 0; k < 4; ++k) b.pvw[0][4 * (size_t)j + k] = x[k];
+    } else {
+      shl_pair_compute(P1, P2, &g);
+    }
     b.pd2[0][j] = g.d2;
     if (g.d2 <= 0.0) register_problem(ctl, SHL_CONTACT_PROBLEM);
     double* out = b.pforce + kPairOut * (size_t)j;
@@ -1063,12 +1073,9 @@ __global__ void __launch_bounds__(kBlock) k_gather_correct(DevBuf b, StepConst s
         // avg_area_node (ShellSystem.C:2462-2481): the faces of which the node is a vertex
         double area_sum = 0.0;
         uint32_t n_faces = 0;
-        for (uint32_t k = g0; k < g1; ++k) {
-          const uint32_t ent = __ldg(&b.gather_ent[k]);
-          if (ent % 12u < 3u) {
-            area_sum += b.area[__ldg(&b.perm[ent / 12u])];
-            ++n_faces;
-          }
+        for (uint32_t k = __ldg(&b.node_face_ptr[n]); k < __ldg(&b.node_face_ptr[n + 1]); ++k) {
+          area_sum += b.area[__ldg(&b.node_face[k])];
+          ++n_faces;
         }
         const double area_node = area_sum / n_faces;
         const double stiffness = sc.stiff_density * area_node;
@@ -1499,7 +1506,10 @@ void launch_contact_force(const DevBuf& b, const StepConst& sc, int, cudaStream_
   uint32_t nb = nblk(sc.pairs_cap);
   if (nb > 4 * 152) nb = 4 * 152;
   if (nb == 0) nb = 1;
-  k_contact_force<<<nb, kBlock, 0, s>>>(b, sc);
+  if (sc.smooth)
+    k_contact_force<true><<<nb, kBlock, 0, s>>>(b, sc);
+  else
+    k_contact_force<false><<<nb, kBlock, 0, s>>>(b, sc);
 }
 // mode 2: an adaptive attempt (a_pred and the error estimate); else correct ? step corrector : evaluation
 void launch_gather_correct(const DevBuf& b, const StepConst& sc, int mode, bool correct, double* f_out, double* a_out,
@@ -1561,13 +1571,14 @@ __global__ void __launch_bounds__(kBlock) k_elements_noalloc(DevBuf b, StepConst
   const uint32_t li = (blockIdx.x - gd.block_start) * blockDim.x + threadIdx.x;
   if (li >= gd.count) return;
   const uint32_t i = gd.first + li;
+  const uint32_t slot0 = gd.slot_base + li * (uint32_t)gd.n_slots;
   const double pr = pressure * __ldg(&b.pscale[i]);
   if (gd.n_slots == 12)
-    element_force<12>(i, 12, sB, b, sc, pr, 0.0);
+    element_force<12>(i, 12, slot0, sB, b, sc, pr, 0.0);
   else if (gd.n_slots == 11)
-    element_force<11>(i, 11, sB, b, sc, pr, 0.0);
+    element_force<11>(i, 11, slot0, sB, b, sc, pr, 0.0);
   else
-    element_force<0>(i, gd.n_slots, sB, b, sc, pr, 0.0);
+    element_force<0>(i, gd.n_slots, slot0, sB, b, sc, pr, 0.0);
 }
 
 // f = -(sum of the node's shares), the same gather order as the step kernel

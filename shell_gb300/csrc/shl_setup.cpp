@@ -176,6 +176,54 @@ void irregular_basis(int n, double v, double w, double* out) {
   }
 }
 
+namespace {
+
+// Element-force slot layout: group after group, n_slots slots per face.
+void layout_slots(Setup& S) {
+  uint32_t base = 0, rows = 12;
+  for (PatchGroup& g : S.groups) {
+    g.slot_base = base;
+    base += g.count * (uint32_t)g.n_slots;
+    if ((uint32_t)g.n_slots > rows) rows = (uint32_t)g.n_slots;
+  }
+  S.n_slots_total = base;
+  S.patch_rows = rows;
+}
+
+// Gather CSR (node -> element-force slots, ascending) and the node -> face
+// CSR (faces of which a node is a vertex, ascending internal order).
+void build_node_lists(Setup& S) {
+  const uint32_t V = S.V, F = S.F;
+  S.gather_ptr.assign(V + 1, 0);
+  S.node_face_ptr.assign(V + 1, 0);
+  for (const PatchGroup& g : S.groups)
+    for (uint32_t i = g.first; i < g.first + g.count; ++i)
+      for (int s = 0; s < g.n_slots; ++s) {
+        const int32_t nd = S.patch[(size_t)s * F + i];
+        if (nd < 0) continue;
+        ++S.gather_ptr[nd + 1];
+        if (s < 3) ++S.node_face_ptr[nd + 1];
+      }
+  for (uint32_t nd = 0; nd < V; ++nd) {
+    S.gather_ptr[nd + 1] += S.gather_ptr[nd];
+    S.node_face_ptr[nd + 1] += S.node_face_ptr[nd];
+  }
+  S.gather_ent.assign(S.gather_ptr[V], 0);
+  S.node_face.assign(S.node_face_ptr[V], 0);
+  std::vector<uint32_t> cur(S.gather_ptr.begin(), S.gather_ptr.end() - 1);
+  std::vector<uint32_t> cur_f(S.node_face_ptr.begin(), S.node_face_ptr.end() - 1);
+  for (const PatchGroup& g : S.groups)
+    for (uint32_t i = g.first; i < g.first + g.count; ++i)
+      for (int s = 0; s < g.n_slots; ++s) {
+        const int32_t nd = S.patch[(size_t)s * F + i];
+        if (nd < 0) continue;
+        S.gather_ent[cur[nd]++] = g.slot_base + (i - g.first) * (uint32_t)g.n_slots + (uint32_t)s;
+        if (s < 3) S.node_face[cur_f[nd]++] = S.perm[i];
+      }
+}
+
+}  // namespace
+
 bool build_setup(const shl_mesh& mesh, const shl_params& prm, Setup& S, std::string& err) {
   const uint32_t V = mesh.n_nodes, F = mesh.n_faces;
   if (V < 4 || F < 4 || !mesh.xyz || !mesh.faces) { err = "empty mesh"; return false; }
@@ -281,6 +329,7 @@ bool build_setup(const shl_mesh& mesh, const shl_params& prm, Setup& S, std::str
   }
   S.inv_perm.assign(F, 0);
   for (uint32_t i = 0; i < F; ++i) S.inv_perm[S.perm[i]] = i;
+  layout_slots(S);
 
   // derived constants, ShellSystem.C:472-486
   {
@@ -294,7 +343,7 @@ bool build_setup(const shl_mesh& mesh, const shl_params& prm, Setup& S, std::str
     S.d2_friction = std::pow((1 + prm.static_friction_tol) * prm.thickness, 2);
   }
 
-  S.patch.assign(12 * (size_t)F, -1);
+  S.patch.assign((size_t)S.patch_rows * F, -1);
   S.face.assign((size_t)FF_COUNT * F, 0.0);
   std::vector<double> face_bal((size_t)FF_COUNT * F, 0.0);  // balanced-frame constants (FP32 path)
   S.Minv.assign(3 * (size_t)V, 0.0);
@@ -459,23 +508,7 @@ bool build_setup(const shl_mesh& mesh, const shl_params& prm, Setup& S, std::str
     m = 1 / m;
   }
 
-  // gather CSR: node -> entries (internal face * 12 + slot), ascending
-  S.gather_ptr.assign(V + 1, 0);
-  for (uint32_t i = 0; i < F; ++i)
-    for (int s = 0; s < 12; ++s) {
-      const int32_t nd = S.patch[(size_t)s * F + i];
-      if (nd >= 0) ++S.gather_ptr[nd + 1];
-    }
-  for (uint32_t nd = 0; nd < V; ++nd) S.gather_ptr[nd + 1] += S.gather_ptr[nd];
-  S.gather_ent.assign(S.gather_ptr[V], 0);
-  {
-    std::vector<uint32_t> cur(S.gather_ptr.begin(), S.gather_ptr.end() - 1);
-    for (uint32_t i = 0; i < F; ++i)
-      for (int s = 0; s < 12; ++s) {
-        const int32_t nd = S.patch[(size_t)s * F + i];
-        if (nd >= 0) S.gather_ent[cur[nd]++] = i * 12 + s;
-      }
-  }
+  build_node_lists(S);
 
   // topological exclusion set, ShellSystem.C:657-741 (original face ids)
   S.close_ptr.assign(F + 1, 0);
@@ -599,36 +632,21 @@ bool merge_setups(std::vector<Setup>& shells, Setup& M, std::vector<uint32_t>& n
   if (M.perm.size() != F) { err = "face regrouping lost faces"; return false; }
   M.inv_perm.assign(F, 0);
   for (uint32_t i = 0; i < F; ++i) M.inv_perm[M.perm[i]] = i;
-  M.patch.assign(12 * (size_t)F, -1);
+  layout_slots(M);
+  M.patch.assign((size_t)M.patch_rows * F, -1);
   M.face.assign((size_t)FF_COUNT * F, 0.0);
   M.face32.assign((size_t)F32_COUNT * F, 0.0f);
   for (uint32_t i = 0; i < F; ++i) {
     const uint32_t k = src[i].first, si = src[i].second;
     const Setup& S = shells[k];
-    for (int s = 0; s < 12; ++s) {
+    for (uint32_t s = 0; s < S.patch_rows; ++s) {
       const int32_t nd = S.patch[(size_t)s * S.F + si];
       M.patch[(size_t)s * F + i] = nd < 0 ? -1 : nd + (int32_t)node_off[k];
     }
     for (int fld = 0; fld < FF_COUNT; ++fld) M.face[(size_t)fld * F + i] = S.face[(size_t)fld * S.F + si];
     for (int fld = 0; fld < F32_COUNT; ++fld) M.face32[(size_t)fld * F + i] = S.face32[(size_t)fld * S.F + si];
   }
-  // gather CSR over the merged numbering
-  M.gather_ptr.assign(V + 1, 0);
-  for (uint32_t i = 0; i < F; ++i)
-    for (int s = 0; s < 12; ++s) {
-      const int32_t nd = M.patch[(size_t)s * F + i];
-      if (nd >= 0) ++M.gather_ptr[nd + 1];
-    }
-  for (uint32_t v = 0; v < V; ++v) M.gather_ptr[v + 1] += M.gather_ptr[v];
-  M.gather_ent.assign(M.gather_ptr[V], 0);
-  {
-    std::vector<uint32_t> cur(M.gather_ptr.begin(), M.gather_ptr.end() - 1);
-    for (uint32_t i = 0; i < F; ++i)
-      for (int s = 0; s < 12; ++s) {
-        const int32_t nd = M.patch[(size_t)s * F + i];
-        if (nd >= 0) M.gather_ent[cur[nd]++] = i * 12 + s;
-      }
-  }
+  build_node_lists(M);
   M.close_ptr.assign(F + 1, 0);
   M.K = shells[0].K;
   M.D = shells[0].D;

@@ -60,6 +60,8 @@ struct PatchGroup {
   int n_slots;        // valence + 6
   uint32_t first;     // first internal face of the group
   uint32_t count;     // faces in the group
+  uint32_t slot_base; // first element-force slot of the group: face i of the group owns
+                      // slots slot_base + (i - first) * n_slots + [0, n_slots)
   std::vector<double> basis;  // n_slots x 6 (phi, d/dv, d/dw, d2/dv2, d2/dw2, d2/dvdw)
 };
 
@@ -70,12 +72,16 @@ struct Setup {
   std::vector<uint32_t> perm;      // internal face -> original face id
   std::vector<uint32_t> inv_perm;  // original -> internal
   std::vector<PatchGroup> groups;  // groups[0] = regular
+  uint32_t patch_rows = 12;        // slot rows of `patch` (the largest n_slots, at least 12)
+  uint32_t n_slots_total = 0;      // element-force slots of all faces (sum of n_slots)
   std::vector<int32_t> patch;      // [slot * F + internal face], -1 for unused slots
   std::vector<double> face;        // [field * F + internal face]
   std::vector<float> face32;       // [FaceField32 * F + internal face]
   std::vector<double> Minv, C;     // 3V node-major
   std::vector<uint32_t> gather_ptr;  // V+1
-  std::vector<uint32_t> gather_ent;  // internal_face * 12 + slot, ascending per node
+  std::vector<uint32_t> gather_ent;  // element-force slot (PatchGroup::slot_base), ascending per node
+  std::vector<uint32_t> node_face_ptr;  // V+1: faces of which each node is a vertex
+  std::vector<uint32_t> node_face;      // original face ids, ascending internal order
   std::vector<uint32_t> close_ptr;   // F+1 (original ids)
   std::vector<uint32_t> close_list;  // sorted original ids
   uint64_t n_cells_max = 0;

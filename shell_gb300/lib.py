@@ -100,6 +100,8 @@ def load():
         "shl_get_contact_state": (_i32, [vp, vp, vp, vp, vp, sz, ctypes.POINTER(sz), ctypes.POINTER(_d)]),
         "shl_set_contact_state": (_i32, [vp, vp, vp, vp, vp, sz, _d]),
         "shl_rebuild_contacts": (_i32, [vp]),
+        "shl_get_contact_coords": (_i32, [vp, vp, sz, ctypes.POINTER(sz)]),
+        "shl_set_contact_coords": (_i32, [vp, vp, sz]),
         "shl_get_element_fields": (_i32, [vp, vp, vp, vp, vp, vp]),
         "shl_get_mass_damping": (_i32, [vp, vp, vp]),
         "shl_icosphere": (_i32, [_u32, vp, sz, vp, sz, ctypes.POINTER(_u32), ctypes.POINTER(_u32)]),
@@ -170,7 +172,8 @@ def exported_symbols():
             "shl_mlp_get_params", "shl_mlp_set_dataset", "shl_mlp_train", "shl_mlp_predict", "shl_mlp_gradients",
             "shl_gemm_bf16", "shl_residual", "shl_set_pressure_function", "shl_eval_pressure_function",
             "shl_get_dt", "shl_set_stop_function", "shl_set_cavity_functions", "shl_get_cavity_origins",
-            "shl_set_cavity_origins", "shl_scale_damping", "shl_set_element_variant", "shl_get_element_variant"]
+            "shl_set_cavity_origins", "shl_scale_damping", "shl_set_element_variant", "shl_get_element_variant",
+            "shl_get_contact_coords", "shl_set_contact_coords"]
 
 
 class ShlError(RuntimeError):
@@ -384,6 +387,20 @@ class Shell:
         d2 = None if d2 is None else np.ascontiguousarray(d2, dtype=np.float64)
         _check(self.lib.shl_set_contact_state(self.h, pairs.ctypes.data, _ptr(stick), _ptr(origin), _ptr(d2), k,
                                               du_sum), "shl_set_contact_state", False)
+
+    def contact_coords(self):
+        """SMOOTH contact: (n_pairs, 4) closest-point coordinates (v1, w1, v2, w2), patch frames."""
+        n = ctypes.c_size_t()
+        _check(self.lib.shl_get_contact_coords(self.h, None, 0, ctypes.byref(n)), "shl_get_contact_coords", False)
+        x = np.zeros((n.value, 4))
+        if n.value:
+            _check(self.lib.shl_get_contact_coords(self.h, x.ctypes.data, n.value, ctypes.byref(n)),
+                   "shl_get_contact_coords", False)
+        return x
+
+    def set_contact_coords(self, x):
+        x = np.ascontiguousarray(x, dtype=np.float64).reshape(-1, 4)
+        _check(self.lib.shl_set_contact_coords(self.h, x.ctypes.data, x.shape[0]), "shl_set_contact_coords", False)
 
     def rebuild_contacts(self):
         return _check(self.lib.shl_rebuild_contacts(self.h), "shl_rebuild_contacts")

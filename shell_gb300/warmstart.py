@@ -341,3 +341,38 @@ def experiment(n_train=2048, n_test=256, seed=0, batch_size=512, train_iters=400
     out["prediction_wall_s"] = pred_s
     out["total_wall_s"] = time.perf_counter() - t_all
     return out
+
+
+def _jsonable(o):
+    if isinstance(o, dict):
+        return {str(k): _jsonable(v) for k, v in o.items()}
+    if isinstance(o, (list, tuple)):
+        return [_jsonable(v) for v in o]
+    if isinstance(o, np.generic):
+        return o.item()
+    return o
+
+
+def main(argv=None):
+    """python -m shell_gb300.warmstart --train N --test M --out study.json"""
+    import argparse
+    import json
+    ap = argparse.ArgumentParser(description="learned warm start study (level-5 shells)")
+    ap.add_argument("--train", type=int, default=3584)
+    ap.add_argument("--test", type=int, default=256)
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--train-iters", type=int, default=6000)
+    ap.add_argument("--max-steps", type=int, default=15000)
+    ap.add_argument("--out", default="warmstart_study.json")
+    a = ap.parse_args(argv)
+    t0 = time.perf_counter()
+    r = experiment(n_train=a.train, n_test=a.test, seed=a.seed, batch_size=512, train_iters=a.train_iters,
+                   max_steps=a.max_steps, log=lambda m: print("[%.0f s] %s" % (time.perf_counter() - t0, m),
+                                                              flush=True))
+    with open(a.out, "w") as f:
+        json.dump(_jsonable(r), f, indent=1)
+    print(json.dumps(_jsonable(r)))
+
+
+if __name__ == "__main__":
+    main()

@@ -40,3 +40,53 @@ def folded_state(X, rng, amplitude=0.05):
     u[:, 2] = -amplitude * np.clip(z, 0, None) ** 2
     u += 1e-4 * rng.standard_normal(X.shape)
     return u.reshape(-1)
+
+
+def midpoint_refine(X, T, project=True):
+    """Each triangle split into four at its edge midpoints (new nodes projected
+    onto the unit sphere when `project`)."""
+    X = [tuple(x) for x in np.asarray(X, float)]
+    cache = {}
+
+    def mid(a, b):
+        k = (min(a, b), max(a, b))
+        if k not in cache:
+            m = (np.asarray(X[a]) + np.asarray(X[b])) / 2
+            if project:
+                m = m / np.linalg.norm(m)
+            cache[k] = len(X)
+            X.append(tuple(m))
+        return cache[k]
+
+    out = []
+    for a, b, c in np.asarray(T, int):
+        ab, bc, ca = mid(a, b), mid(b, c), mid(c, a)
+        out += [(a, ab, ca), (b, bc, ab), (c, ca, bc), (ab, bc, ca)]
+    return np.array(X), np.array(out, dtype=np.uint32)
+
+
+def flipped_sphere(level=1):
+    """An icosphere of level 2 with one edge flipped (two vertices of valence
+    7, two more of valence 5), refined `level` times: patches of valence 5, 6
+    and 7 (13 patch nodes)."""
+    X, T = L.icosphere(2)
+    T = np.array(T, dtype=np.int64)
+    val = np.bincount(T.ravel())
+    faces_of = {}
+    for f, t in enumerate(T):
+        for k in range(3):
+            faces_of[(int(t[k]), int(t[(k + 1) % 3]))] = f
+    for f, t in enumerate(T):
+        for k in range(3):
+            p, q = int(t[k]), int(t[(k + 1) % 3])
+            r = int(t[(k + 2) % 3])
+            g = faces_of[(q, p)]
+            s = [int(x) for x in T[g] if x != p and x != q][0]
+            if val[p] == val[q] == val[r] == val[s] == 6:
+                # (p, q, r) and (q, p, s) -> (r, s, q) and (s, r, p)
+                T[f] = (r, s, q)
+                T[g] = (s, r, p)
+                for _ in range(level):
+                    X, T = midpoint_refine(X, T)
+                return np.ascontiguousarray(X, dtype=np.float64), np.ascontiguousarray(T, dtype=np.uint32)
+    raise AssertionError("no flippable edge")

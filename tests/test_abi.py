@@ -78,5 +78,5 @@ def test_create_rejects_bad_params(built):
     p = L.default_params()  # shear modulus 0: the reference asserts > 0
     assert lib.shl_create(ctypes.byref(m), ctypes.byref(p), ctypes.byref(h)) == L.SHL_ERR_ARG
     assert b"shear" in lib.shl_last_error()
-    p = L.default_params(shell_shear_modulus=1.0, shell_shell_contact=L.CONTACT_SMOOTH)
+    p = L.default_params(shell_shear_modulus=1.0, shell_shell_contact=7)
     assert lib.shl_create(ctypes.byref(m), ctypes.byref(p), ctypes.byref(h)) == L.SHL_ERR_ARG

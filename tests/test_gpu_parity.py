@@ -13,7 +13,7 @@ import pytest
 
 from shell_gb300 import lib as L
 import oracle as O
-from tests.common import cell_size_mult_for, classical_pressure, physics_params
+from tests.common import cell_size_mult_for, classical_pressure, flipped_sphere, physics_params
 
 pytestmark = pytest.mark.gpu
 
@@ -68,6 +68,28 @@ def test_eval_forces_no_contact(cuda_ok, meshes, level, pressure_base):
     fe_g, fe_o = g.element_fields(), o.element_fields()
     for k in ("etens", "ebend", "area"):
         assert rel(fe_g[k], fe_o[k]) < 1e-11, k
+    g.close()
+
+
+@pytest.mark.parametrize("precision", [L.PREC_FP64, L.PREC_FP32])
+def test_eval_forces_valence_5_6_7(cuda_ok, precision):
+    """A mesh with valence-7 vertices (13-node patches, more than the 12 slots
+    of a regular patch): forces and energies against the oracle."""
+    X, T = flipped_sphere(1)
+    rng = np.random.default_rng(11)
+    p = physics_params(contact=False, precision=precision)
+    g = L.Shell(X, T, p)
+    o = O.Oracle(X, T, physics_params(contact=False), threads=4)
+    u = smooth_state(X, rng)
+    v = 1e-3 * rng.standard_normal(u.shape)
+    pres = -classical_pressure()
+    fg, ag, eg, _ = g.eval_forces(u, v, pres)
+    fo, ao, eo, _ = o.eval_forces(u, v, pres)
+    tol = FORCE_TOL if precision == L.PREC_FP64 else 1e-4  # FP32: relative to the strain size
+    assert rel(fg, fo) < tol
+    assert rel(ag, ao) < tol
+    for k in ("Etens", "Ebend", "area"):
+        assert abs(eg[k] - eo[k]) <= tol * abs(eo[k]), k
     g.close()
 
 
