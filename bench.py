@@ -35,8 +35,9 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-E1, E2, NU12, G12, H, RHO, ALPHA, DT = 1.0, 0.5, 0.3, 0.35, 0.01, 1.0, 0.05, 1e-4
-RAMP_STEPS, RAMP_FACTOR, AMPL, SEED, MU = 20000, 2.0, 1e-3, 0, 0.3
+from shell_gb300.workloads import (ALPHA, AMPL, DT, G12, MU, NU12, RAMP_STEPS, RHO, SEED,  # noqa: E402
+                                   classical_pressure, pressure, squashed_state, workload)
+
 FLUSH_BYTES = 512 << 20
 # library kernels per step with self-contact: predictor, two rebuild-condition kernels (the IF nodes'
 # conditions), element kernel + totals, contact force, gather/corrector, volume/end of step; plus
@@ -50,28 +51,6 @@ ELEM_BYTES_PER_NODE = 24
 # FP64 flops of one regular face in the element kernel (count of the
 # arithmetic in element_force<12>, fused multiply-add = 2)
 ELEM_FLOPS_PER_FACE = 1372
-
-
-def classical_pressure():
-    E = np.sqrt(E1 * E2)
-    nu = np.sqrt(NU12 * NU12 * E2 / E1)
-    return 2 * E * H * H / np.sqrt(3 * (1 - nu * nu))
-
-
-def workload(L, level):
-    X, T = L.icosphere(level)
-    P = X[T]
-    cell_mult = 2 * H / (P.max(axis=1) - P.min(axis=1)).max(axis=1).mean()
-    p = L.default_params(shell_mass_density=RHO, shell_young_modulus=E1, shell_young_modulus2=E2,
-                         shell_poisson_ratio=NU12, shell_shear_modulus=G12, thickness=H, damping_alpha=ALPHA, dt=DT,
-                         shell_shell_contact=L.CONTACT_LINEAR, mu_s=MU, mu_d=MU, cell_size_mult=cell_mult)
-    u0 = L.gaussian_normal_imperfection(X, AMPL, SEED).reshape(-1)
-    return X, T, p, u0
-
-
-def pressure(step):
-    """p(t) at the end of step `step` (1-based): -s p_cl t / T."""
-    return -RAMP_FACTOR * classical_pressure() * np.asarray(step, dtype=np.float64) / RAMP_STEPS
 
 
 def ensemble_workload(L, n_shells=256, seed=0):
@@ -129,6 +108,49 @@ def time_ensemble(L, torch, K, W, flush):
     return {"value": F * K / (ms * 1e-3), "unit": "face-steps/s", "ms_per_step": ms / K, "shells": len(shells),
             "faces": int(F), "levels": {str(lv): levels.count(lv) for lv in (3, 4, 5)}, "dtype": "f32 forces, f64 state",
             "steps": K, "status": int(status)}
+
+
+def time_contact_modes(L, torch, K, W, flush, level):
+    """Self-contact at a contact-heavy state: the level-`level` shell of the
+    main workload squashed to a double layer (every face has candidates on the
+    other layer), zero pressure, with the LINEAR (flat triangles) and SMOOTH
+    (Loop limit surfaces) narrow phases: K timed steps each (L2 evicted before
+    every step) after W warm-up steps, and the first candidate-list build."""
+    X, T, _, _ = workload(L, level)
+    u = squashed_state(X)
+    z = np.zeros_like(u)
+    F = len(T)
+    out = {"workload": "level-%d shell squashed to a double layer (gap 2 x 0.0042 |z|), zero pressure, steps "
+                       "%d-%d" % (level, W + 1, W + K), "faces": F}
+    for name, mode in (("linear", L.CONTACT_LINEAR), ("smooth", L.CONTACT_SMOOTH)):
+        _, _, p, _ = workload(L, level, contact=mode)
+        g = L.Shell(X, T, p)
+        g.set_state(u, z, z)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        g.rebuild_contacts()
+        build_s = time.perf_counter() - t0
+        g.upload_pressure_table(np.zeros(W + K))
+        g.step_enqueue(W)
+        torch.cuda.synchronize()
+        g.step_collect()
+        stream = torch.cuda.ExternalStream(g.stream_handle())
+        st = [torch.cuda.Event(enable_timing=True) for _ in range(K)]
+        en = [torch.cuda.Event(enable_timing=True) for _ in range(K)]
+        with torch.cuda.stream(stream):
+            for k in range(K):
+                flush.fill_(k)
+                st[k].record(stream)
+                g.step_enqueue(1)
+                en[k].record(stream)
+        torch.cuda.synchronize()
+        ms = sum(a.elapsed_time(e) for a, e in zip(st, en))
+        rep, status = g.step_collect()
+        out[name] = {"value": F * K / (ms * 1e-3), "unit": "face-steps/s", "ms_per_step": ms / K,
+                     "n_pairs": int(rep.last.n_pairs), "Nc": int(rep.last.Nc), "n_rebuilds": int(rep.n_rebuilds),
+                     "first_build_s": build_s, "status": int(status)}
+        g.close()
+    return out
 
 
 def fp32_accuracy(L, steps=1000, level=7):
@@ -350,6 +372,7 @@ def run_ours(args, rank, world, dist):
         fp32_value = F * K / (ms32 * 1e-3)
 
     ensemble = time_ensemble(L, torch, max(20, K // 4), W, flush) if args.ensemble else None
+    contact_modes = time_contact_modes(L, torch, 10, 2, flush, args.level) if args.contact_modes else None
     accuracy = fp32_accuracy(L) if args.accuracy else None
     warmstart = None
     if args.warmstart:
@@ -414,6 +437,7 @@ def run_ours(args, rank, world, dist):
         "warm_value": warm,
         "fp32_value": fp32_value,
         "ensemble": ensemble,
+        "contact_modes": contact_modes,
         "fp32_accuracy": accuracy,
         "warmstart": warmstart,
         "e2e": {"value": e2e, "unit": "face-steps/s", "h2d_bytes_per_step": 3 * 3 * V * 8,
@@ -445,6 +469,8 @@ def main():
     ap.add_argument("--fp32", type=int, default=1, help="also time the FP32 element-force mode")
     ap.add_argument("--ensemble", type=int, default=1, help="also time the 256-shell batched ensemble")
     ap.add_argument("--accuracy", type=int, default=1, help="also report the level-7 FP32-vs-FP64 accuracy")
+    ap.add_argument("--contact-modes", type=int, default=1,
+                    help="also time LINEAR and SMOOTH self-contact at a squashed (contact-heavy) state")
     ap.add_argument("--warmstart", type=int, default=0,
                     help="also run the learned warm-start study (level-5 shells; minutes of GPU time)")
     ap.add_argument("--ws-train", type=int, default=3584)

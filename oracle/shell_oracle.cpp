@@ -1298,7 +1298,13 @@ void oracle::compute_shell_shell_contact_candidates(bool force) {
       first_empty = std::min(first_empty, i);
     }
   }
-  for (unsigned eid1 = 0; eid1 < F; ++eid1) {
+  // candidates of each eid1 in discovery order (the searches are independent per
+  // eid1; the reference runs this loop with OpenMP too), then added to the list
+  // in eid1 order exactly as the serial loop would
+  std::vector<std::vector<Contact*>> found(F);
+#pragma omp parallel for schedule(dynamic, 8)
+  for (int e1i = 0; e1i < (int)F; ++e1i) {
+    const unsigned eid1 = (unsigned)e1i;
     const std::vector<unsigned>& cells = elem_to_cell_map[eid1];
     for (unsigned cidx = 0; cidx < cells.size(); ++cidx) {
       const std::vector<unsigned>& elems_in_cell = cell_to_elem_map[cells[cidx]];
@@ -1318,23 +1324,30 @@ void oracle::compute_shell_shell_contact_candidates(bool force) {
         cand->eid[0] = eid1;
         cand->eid[1] = eid2;
         pair_compute(*cand, false);
-        if (cand->d2 <= 0) register_problem(SHL_CONTACT_PROBLEM);
+        if (cand->d2 <= 0) {
+#pragma omp critical(oracle_problem)
+          register_problem(SHL_CONTACT_PROBLEM);
+        }
         if (cand->d2 > d2_max) {
           delete cand;
           continue;
         }
-        if (first_empty == candidates.size()) {
-          ++first_empty;
-          candidates.push_back(cand);
-        } else {
-          candidates[first_empty] = cand;
-          auto it = std::find(candidates.begin() + first_empty + 1, candidates.end(), (Contact*)nullptr);
-          first_empty = (unsigned)(it - candidates.begin());
-        }
+        found[eid1].push_back(cand);
         ec[eid1].in_contact_with.push_back(eid2);
       }
     }
   }
+  for (unsigned eid1 = 0; eid1 < F; ++eid1)
+    for (Contact* cand : found[eid1]) {
+      if (first_empty == candidates.size()) {
+        ++first_empty;
+        candidates.push_back(cand);
+      } else {
+        candidates[first_empty] = cand;
+        auto it = std::find(candidates.begin() + first_empty + 1, candidates.end(), (Contact*)nullptr);
+        first_empty = (unsigned)(it - candidates.begin());
+      }
+    }
 }
 
 void oracle::compute_enclosed_volume() {

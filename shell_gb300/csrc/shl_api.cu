@@ -521,9 +521,11 @@ shl_status create_common(shl_ctx* c, const std::vector<double>& pscale_orig, shl
     n_cells_cap = (uint32_t)std::max<uint64_t>(std::min<uint64_t>(want_cells, std::max<uint64_t>(8 * n_cells0, 1u << 20)), 1);
     if (n_cells_cap < n_cells0) n_cells_cap = (uint32_t)std::min<uint64_t>(n_cells0, 1ull << 28);
     entries_cap = (uint32_t)std::min<uint64_t>(std::max<uint64_t>(8 * entries0, 1u << 20), 1ull << 30);
-    pairs_cap = std::max<uint32_t>(16 * F, 1u << 16);
-    csr_cap = 6 * pairs_cap;
-    cand_cap = std::max<uint32_t>(32 * F, 1u << 18);
+    // SMOOTH reaches farther (d_max + the mean element size): four times the room
+    const uint32_t room = smooth ? 4u : 1u;
+    pairs_cap = (uint32_t)std::min<uint64_t>(std::max<uint64_t>((uint64_t)16 * room * F, 1u << 16), 1u << 28);  // csr entries hold j * 8 + role
+    csr_cap = (uint32_t)std::min<uint64_t>((uint64_t)6 * pairs_cap, 0xFFFFFFF0u);
+    cand_cap = (uint32_t)std::min<uint64_t>(std::max<uint64_t>((uint64_t)32 * room * F, 1u << 18), 1u << 30);
     ALLOC(b.close_ptr, F + 1);
     ALLOC(b.close_list, S.close_list.size());
     ALLOC(b.bmin, 3 * (size_t)F); ALLOC(b.bmax, 3 * (size_t)F); ALLOC(b.fsize, F);

@@ -519,7 +519,6 @@ int run(int argc, char** argv) {
   auto need = [](bool ok, const std::string& what) {
     if (!ok) throw Error("ERROR: " + what + " is not supported by this library");
   };
-  need(P.shell_shell_contact != SHL_CONTACT_SMOOTH, "shell_shell_contact = smooth");
   need(damping_rotation == 0 && perturbation_rate == 0 && gravity == 0 && !stand_still,
        "damping_rotation, perturbation_rate, gravity or stand_still");
   need(growth1 == 1 && growth2 == 1 && mgr == 0 && cgr == 0, "growth");

@@ -1,0 +1,56 @@
+"""Steps of the benchmark workload with every kernel launched on its own, for
+kernel profilers (the CUDA graphs of shl_step hold conditional nodes, whose
+kernels profilers cannot replay one by one).
+
+python -m shell_gb300.profile [--level 6] [--warmup 3] [--steps 5] [--squashed] [--contact linear|smooth|none]
+    [--phases]
+
+--squashed starts from the double-layer state of the contact-mode benchmark
+instead of the imperfect sphere; --phases also prints shl_profile_step's
+per-phase event times (predictor, linked cells, elements, contact, gather,
+volume) of one more step.
+"""
+import argparse
+import time
+
+import numpy as np
+
+from . import lib as L
+from .workloads import pressure, squashed_state, workload
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
+    ap.add_argument("--level", type=int, default=6)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--squashed", action="store_true")
+    ap.add_argument("--contact", default="linear", choices=["linear", "smooth", "none"])
+    ap.add_argument("--phases", action="store_true")
+    a = ap.parse_args(argv)
+    mode = {"linear": L.CONTACT_LINEAR, "smooth": L.CONTACT_SMOOTH, "none": L.CONTACT_NONE}[a.contact]
+    X, T, p, u0 = workload(L, a.level, contact=mode)
+    g = L.Shell(X, T, p)
+    if a.squashed:
+        u = squashed_state(X)
+        z = np.zeros_like(u)
+        g.set_state(u, z, z)
+        g.rebuild_contacts()
+        table = np.zeros(a.warmup + a.steps + 1)
+    else:
+        g.apply_initial_conditions(u0, 0.0, pressure(1))
+        table = pressure(np.arange(1, a.warmup + a.steps + 2))
+    g.step(a.warmup, table[:a.warmup], use_graph=False)
+    t0 = time.perf_counter()
+    r, st = g.step(a.steps, table[a.warmup:a.warmup + a.steps], use_graph=False)
+    wall = time.perf_counter() - t0
+    print("faces %d, %d steps in %.3f s (kernels launched one by one), status %d, pairs %d, rebuilds %d"
+          % (len(T), a.steps, wall, st, r.last.n_pairs, r.n_rebuilds))
+    if a.phases:
+        ms = g.profile_step(table[-1])
+        print("  ".join("%s %.4f ms" % (n, m) for n, m in ms.items()))
+    g.close()
+
+
+if __name__ == "__main__":
+    main()

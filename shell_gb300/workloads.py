@@ -1,0 +1,47 @@
+"""Synthetic workloads of the benchmark and the profiling runs (no datasets:
+generated icospheres and seeded perturbations).
+
+The single-shell configuration: an icosphere of the given level, orthotropic
+Koiter shell E1 = 1, E2 = 0.5, nu12 = 0.3, G12 = 0.35, h/R = 0.01, density 1,
+Rayleigh damping 0.05, dt = 1e-4, a seeded Gaussian normal imperfection of
+amplitude 1e-3 R, self-contact with Coulomb friction mu = 0.3 and linked cells
+of 2h, and an external pressure ramped from 0 to 2 p_cl over 20,000 steps.
+"""
+import numpy as np
+
+E1, E2, NU12, G12, H, RHO, ALPHA, DT = 1.0, 0.5, 0.3, 0.35, 0.01, 1.0, 0.05, 1e-4
+RAMP_STEPS, RAMP_FACTOR, AMPL, SEED, MU = 20000, 2.0, 1e-3, 0, 0.3
+
+
+def classical_pressure():
+    """p_cl = 2 E_eff (h/R)^2 / sqrt(3 (1 - nu_eff^2)), E_eff = sqrt(E1 E2), nu_eff = sqrt(nu12 nu21)."""
+    E = np.sqrt(E1 * E2)
+    nu = np.sqrt(NU12 * NU12 * E2 / E1)
+    return 2 * E * H * H / np.sqrt(3 * (1 - nu * nu))
+
+
+def workload(L, level, contact=None):
+    """Mesh, parameters and initial displacement of the single-shell workload."""
+    X, T = L.icosphere(level)
+    P = X[T]
+    cell_mult = 2 * H / (P.max(axis=1) - P.min(axis=1)).max(axis=1).mean()
+    p = L.default_params(shell_mass_density=RHO, shell_young_modulus=E1, shell_young_modulus2=E2,
+                         shell_poisson_ratio=NU12, shell_shear_modulus=G12, thickness=H, damping_alpha=ALPHA, dt=DT,
+                         shell_shell_contact=L.CONTACT_LINEAR if contact is None else contact, mu_s=MU, mu_d=MU,
+                         cell_size_mult=cell_mult)
+    u0 = L.gaussian_normal_imperfection(X, AMPL, SEED).reshape(-1)
+    return X, T, p, u0
+
+
+def pressure(step):
+    """p(t) at the end of step `step` (1-based): -s p_cl t / T."""
+    return -RAMP_FACTOR * classical_pressure() * np.asarray(step, dtype=np.float64) / RAMP_STEPS
+
+
+def squashed_state(X, s=0.0042, seed=0):
+    """The sphere flattened to a double layer (gap about 2 s |z|) with 2e-5
+    seeded noise: every face has contact candidates on the other layer."""
+    rng = np.random.default_rng(seed)
+    u = np.zeros_like(X)
+    u[:, 2] = (s - 1.0) * X[:, 2]
+    return (u + 2e-5 * rng.standard_normal(X.shape)).reshape(-1)

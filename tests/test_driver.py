@@ -95,7 +95,12 @@ def test_mesh_transforms(driver, tmp_path):
     assert d["nodes"] == 2562 and d["faces"] == 5120
 
 
-@pytest.mark.parametrize("bad", ["growth1 = 1.1", "shell_shell_contact = smooth",
+def test_smooth_contact_accepted(driver, tmp_path):
+    d, _ = _dry(driver, tmp_path, BASE_CFG + "shell_shell_contact = smooth\n")
+    assert d["shell_shell_contact"] == L.CONTACT_SMOOTH
+
+
+@pytest.mark.parametrize("bad", ["growth1 = 1.1", "shell_shell_contact = curved",
                                  "thickness = 0.01*(1+t)", "gravity = 9.81", "pressure = 2*", "extra_order = 1"])
 def test_unsupported_options_fail(driver, tmp_path, bad):
     c, m = _write(tmp_path, BASE_CFG + bad + "\n")
