@@ -55,7 +55,7 @@ struct shl_ctx {
   ElemGroups eg{};                 // 256-thread block ranges (the no-allocation path)
   ElemGroups eg_bs[3]{};           // block ranges for 64, 128, 256 threads per block
   uint32_t blocks_bs[3]{};
-  int var64 = 0, var32 = kFirstFp32Variant;  // chosen element-kernel variants
+  int var64 = -1, var32 = kFirstFp32Variant;  // chosen element-kernel variants (-1: not set yet)
   float variant_ms[kNumElemVariants]{};      // tuning times (0: not timed)
   std::vector<void*> allocs;
   cudaGraphExec_t graph = nullptr;
@@ -199,7 +199,11 @@ bool validate(const shl_params& p, std::string& err) {
 }
 
 // Host estimate of the first rebuild's cell grid, for buffer capacities.
-void estimate_cells(const Setup& S, const shl_params& p, uint64_t& n_cells, uint64_t& entries) {
+// Linked-cell sizes at the reference configuration, and the pairs per face of a
+// double layer in contact everywhere (pi (d_max + 2 avg)^2 / mean face area):
+// the largest list a folded shell can need.
+void estimate_cells(const Setup& S, const shl_params& p, uint64_t& n_cells, uint64_t& entries,
+                    double& pairs_per_face) {
   std::vector<double> sizes(S.F);
   double bmin[3] = {SHL_DBL_MAX, SHL_DBL_MAX, SHL_DBL_MAX}, bmax[3] = {-SHL_DBL_MAX, -SHL_DBL_MAX, -SHL_DBL_MAX};
   std::vector<double> fmin(3 * (size_t)S.F), fmax(3 * (size_t)S.F);
@@ -225,7 +229,21 @@ void estimate_cells(const Setup& S, const shl_params& p, uint64_t& n_cells, uint
   double cs = p.cell_size_mult * avg;
   const double tol = p.cell_margin * cs;
   cs += tol;
-  const double dm = p.thickness + tol;
+  double dm = p.thickness + tol;
+  if (p.shell_shell_contact == SHL_CONTACT_SMOOTH) dm += avg;
+  double area = 0;
+  for (uint32_t f = 0; f < S.F; ++f) {
+    double e1[3], e2[3];
+    for (int c = 0; c < 3; ++c) {
+      e1[c] = S.X[3 * (size_t)S.tri[3 * f + 1] + c] - S.X[3 * (size_t)S.tri[3 * f] + c];
+      e2[c] = S.X[3 * (size_t)S.tri[3 * f + 2] + c] - S.X[3 * (size_t)S.tri[3 * f] + c];
+    }
+    const double nx = e1[1] * e2[2] - e1[2] * e2[1], ny = e1[2] * e2[0] - e1[0] * e2[2],
+                 nz = e1[0] * e2[1] - e1[1] * e2[0];
+    area += 0.5 * std::sqrt(nx * nx + ny * ny + nz * nz);
+  }
+  const double af = area / S.F;
+  pairs_per_face = af > 0 ? M_PI * (dm + 2 * avg) * (dm + 2 * avg) / af : 16.0;
   n_cells = 1;
   uint64_t ncd[3];
   for (int c = 0; c < 3; ++c) {
@@ -384,11 +402,22 @@ namespace {
 // (c->S, one shell or a merged batch) is built; pscale: per original face.
 // The FP64 path's arithmetic: 0 = both basis contractions in FP64, 1 = the
 // displacement contraction as float pairs (measured 24-26 % faster at levels 6
-// and 7 than 0; also pairing the force contraction costs more in conversions
-// than it saves).  Fixed for all contexts, so that results do not depend on
-// which launch shape a context picks (the per-face arithmetic of a variant
-// does not depend on its shape).
+// and 7 than 0), 3 = also the force contraction, whose shares stay float pairs
+// until the gather adds them in FP64 (no conversion back in the element
+// kernel).  Fixed for all contexts, so that results do not depend on which
+// launch shape a context picks (the per-face arithmetic of a variant does not
+// depend on its shape).
 constexpr int kFp64Pairs = 1;
+
+// first FP64 variant of the fixed arithmetic (the FP64 launch of FP32 contexts)
+int default_var64() {
+  for (int v = 0; v < kFirstFp32Variant; ++v)
+    if (kElemVariants[v].pairs == kFp64Pairs) return v;
+  return 0;
+}
+
+// step constants that follow the chosen FP64 variant (the share format)
+void apply_variant(shl_ctx* c) { c->sc.qe_pairs = (kElemVariants[c->var64].pairs & 2) ? 1 : 0; }
 
 // Element-kernel autotuning: time every launch shape of the context's path on
 // its own mesh (one warm-up and three timed launches each, CUDA events on the
@@ -425,6 +454,7 @@ shl_status tune_elements(shl_ctx* c) {
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (fp32) c->var32 = best_v; else c->var64 = best_v;
+  apply_variant(c);
   return check_launch("element tuning");
 }
 
@@ -516,16 +546,20 @@ shl_status create_common(shl_ctx* c, const std::vector<double>& pscale_orig, shl
   uint64_t n_cells0 = 0, entries0 = 0;
   uint32_t n_cells_cap = 1, entries_cap = 1, pairs_cap = 1, csr_cap = 1, cand_cap = 1;
   if (contact) {
-    estimate_cells(S, *params, n_cells0, entries0);
+    double ppf = 16.0;
+    estimate_cells(S, *params, n_cells0, entries0, ppf);
     const uint64_t want_cells = std::min<uint64_t>(S.n_cells_max, 1ull << 28);
     n_cells_cap = (uint32_t)std::max<uint64_t>(std::min<uint64_t>(want_cells, std::max<uint64_t>(8 * n_cells0, 1u << 20)), 1);
     if (n_cells_cap < n_cells0) n_cells_cap = (uint32_t)std::min<uint64_t>(n_cells0, 1ull << 28);
     entries_cap = (uint32_t)std::min<uint64_t>(std::max<uint64_t>(8 * entries0, 1u << 20), 1ull << 30);
-    // SMOOTH reaches farther (d_max + the mean element size): four times the room
-    const uint32_t room = smooth ? 4u : 1u;
-    pairs_cap = (uint32_t)std::min<uint64_t>(std::max<uint64_t>((uint64_t)16 * room * F, 1u << 16), 1u << 28);  // csr entries hold j * 8 + role
+    // room for a shell folded onto itself everywhere (1.5 x the double-layer estimate);
+    // csr entries hold pair * 8 + role, so at most 2^28 pairs
+    const double per_face = std::max(16.0, 1.5 * ppf);
+    pairs_cap = (uint32_t)std::min<double>(std::max<double>(per_face * F, 65536.0), (double)(1u << 28));
     csr_cap = (uint32_t)std::min<uint64_t>((uint64_t)6 * pairs_cap, 0xFFFFFFF0u);
-    cand_cap = (uint32_t)std::min<uint64_t>(std::max<uint64_t>((uint64_t)32 * room * F, 1u << 18), 1u << 30);
+    // candidates before the distance test (SMOOTH skips the facet prefilter)
+    cand_cap = (uint32_t)std::min<uint64_t>(std::max<uint64_t>((uint64_t)(smooth ? 3 : 2) * pairs_cap, 1u << 18),
+                                            1u << 30);
     ALLOC(b.close_ptr, F + 1);
     ALLOC(b.close_list, S.close_list.size());
     ALLOC(b.bmin, 3 * (size_t)F); ALLOC(b.bmax, 3 * (size_t)F); ALLOC(b.fsize, F);
@@ -662,6 +696,8 @@ shl_status create_common(shl_ctx* c, const std::vector<double>& pscale_orig, shl
   sc.cand_cap = cand_cap;
   sc.contact = contact ? 1 : 0;
   sc.smooth = smooth ? 1 : 0;
+  c->var64 = default_var64();
+  apply_variant(c);
   for (int k = 0; k < 13; ++k) sc.stab_off[k] = stab_off[k];
   sc.friction = (contact && (p.mu_s != 0 || p.mu_d != 0)) ? 1 : 0;
   sc.pressure_base = p.pressure_base;
@@ -1671,6 +1707,7 @@ shl_status shl_set_element_variant(shl_ctx* c, int variant) {
     return SHL_ERR_ARG;
   }
   if (c->sc.fp32) c->var32 = variant; else c->var64 = variant;
+  apply_variant(c);
   if (c->graph) cudaGraphExecDestroy(c->graph);
   if (c->graph1) cudaGraphExecDestroy(c->graph1);
   c->graph = c->graph1 = nullptr;

@@ -203,10 +203,8 @@ __device__ __forceinline__ void cell_range(const DevBuf& b, const Ctl* ctl, uint
 }
 
 // ---------------------------------------------------------------- count --
-__global__ void __launch_bounds__(kBlock) k_rb_count(DevBuf b, StepConst sc) {
-  Ctl* ctl = b.ctl;
-  if (rb_off(ctl)) return;
-  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+// one face t < F (cell ranges, histogram) or one old pair j = t - F (keep flag)
+__device__ __forceinline__ void rb_count_one(const DevBuf& b, const StepConst& sc, const Ctl* ctl, uint32_t t) {
   if (t < sc.F) {
     int lo[3], hi[3];
     cell_range(b, ctl, t, lo, hi);
@@ -230,6 +228,14 @@ __global__ void __launch_bounds__(kBlock) k_rb_count(DevBuf b, StepConst sc) {
     b.pkeep[j] = keep ? 1 : 0;
     if (keep) atomicAdd(&b.seg_count[b.pe1[0][j]], 1u);
   }
+}
+
+__global__ void __launch_bounds__(kBlock) k_rb_count(DevBuf b, StepConst sc) {
+  Ctl* ctl = b.ctl;
+  if (rb_off(ctl)) return;
+  const uint32_t n_all = sc.F + ctl->n_old;
+  for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n_all; t += gridDim.x * blockDim.x)
+    rb_count_one(b, sc, ctl, t);
 }
 
 // ----------------------------------------------------------------- scan --
@@ -715,7 +721,11 @@ void launch_rebuild(const DevBuf& b, const StepConst& sc, cudaStream_t s) {
     if (g > 16 * 152) g = 16 * 152;
     k_rb_clear<<<g, kBlock, 0, s>>>(b, sc);
   }
-  k_rb_count<<<nblk(sc.F + sc.pairs_cap), kBlock, 0, s>>>(b, sc);
+  {
+    uint32_t g = nblk(sc.F + sc.pairs_cap);
+    if (g > 16 * 152) g = 16 * 152;
+    k_rb_count<<<g, kBlock, 0, s>>>(b, sc);
+  }
   launch_scan(&b.ctl->rebuild, b.ctl, b.cell_count, b.cell_start, &b.ctl->n_cells, 0, sc.n_cells_cap, b.scan_block,
               &b.ctl->n_entries, false, sc.entries_cap, true, s);
   k_rb_fill<<<gF, kBlock, 0, s>>>(b, sc);

@@ -22,6 +22,7 @@ SHL_ERR_ARG, SHL_ERR_CUDA, SHL_ERR_TIMEOUT, SHL_ERR_OOM, SHL_ERR_CAPACITY = 100,
 CONTACT_LINEAR, CONTACT_SMOOTH, CONTACT_NONE = 0, 1, 2
 CS_LOCAL, CS_CARTESIAN, CS_CYLINDRICAL, CS_SPHERICAL = 0, 1, 2, 3
 PREC_FP64, PREC_FP32 = 0, 1
+ELEMENT_VARIANTS = 14  # SHL_ELEMENT_VARIANTS
 CAVITY_BOX, CAVITY_CYLINDER, CAVITY_ELLIPSOID = 0, 1, 2
 
 _d, _i32, _u32 = ctypes.c_double, ctypes.c_int32, ctypes.c_uint32
@@ -441,7 +442,7 @@ class Shell:
         """(variant id, name, tuning times in ms of all variants)."""
         v = ctypes.c_int()
         name = ctypes.create_string_buffer(64)
-        ms = np.zeros(9, dtype=np.float32)
+        ms = np.zeros(ELEMENT_VARIANTS, dtype=np.float32)
         _check(self.lib.shl_get_element_variant(self.h, ctypes.byref(v), name, 64, ms.ctypes.data),
                "shl_get_element_variant", False)
         return v.value, name.value.decode(), ms
