@@ -92,6 +92,7 @@ struct Point {
   void zero() { x[0] = x[1] = x[2] = 0; }
 };
 inline Point operator*(Real s, const Point& p) { return p * s; }
+static_assert(sizeof(Point) == 3 * sizeof(Real), "positions are read as packed xyz");
 
 struct Tensor {  // 3x3, row major
   Real a[3][3];
@@ -390,7 +391,9 @@ struct oracle {
   void limit_patch(unsigned e, shl_limit_patch& lp) const {
     const std::vector<unsigned>& pt = ec[e].patch;
     lp.N = (int)pt.size() - 6;
-    for (size_t j = 0; j < pt.size(); ++j) lp.P[j] = p[pt[j]].x;
+    lp.base = p[0].x;  // Point is three packed doubles
+    lp.ids = pt.data();
+    lp.stride = 1;
     lp.tab = lp.N == 6 ? nullptr : subdiv_tab[lp.N].data();
   }
   // position of the patch's first vertex in the face's node list
@@ -1799,7 +1802,11 @@ int oracle_limit_basis(oracle* o, uint32_t eid, double v, double w, double* out)
   o->limit_patch(eid, lp);
   const int np = lp.N + 6;
   std::vector<double> E(3 * (size_t)np, 0.0);
-  for (int j = 0; j < np; ++j) lp.P[j] = &E[3 * j];
+  std::vector<uint32_t> ids(np);
+  for (int j = 0; j < np; ++j) ids[j] = (uint32_t)j;
+  lp.base = E.data();
+  lp.ids = ids.data();
+  lp.stride = 1;
   for (int j0 = 0; j0 < np; j0 += 3) {
     std::fill(E.begin(), E.end(), 0.0);
     for (int c = 0; c < 3 && j0 + c < np; ++c) E[3 * (j0 + c) + c] = 1.0;

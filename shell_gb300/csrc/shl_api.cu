@@ -402,11 +402,13 @@ namespace {
 // (c->S, one shell or a merged batch) is built; pscale: per original face.
 // The FP64 path's arithmetic: 0 = both basis contractions in FP64, 1 = the
 // displacement contraction as float pairs (measured 24-26 % faster at levels 6
-// and 7 than 0), 3 = also the force contraction, whose shares stay float pairs
-// until the gather adds them in FP64 (no conversion back in the element
-// kernel).  Fixed for all contexts, so that results do not depend on which
-// launch shape a context picks (the per-face arithmetic of a variant does not
-// depend on its shape).
+// and 7 than 0).  Pairing the force contraction as well is slower: converted
+// back in the element kernel it costs more than it saves, and left as pairs
+// for the gather to add in FP64 it doubles the gather's time (the float to
+// double conversions), more than the 6 % it saves in the element kernel at
+// level 7 (measured).  Fixed for all contexts, so that results do not depend
+// on which launch shape a context picks (the per-face arithmetic of a variant
+// does not depend on its shape).
 constexpr int kFp64Pairs = 1;
 
 // first FP64 variant of the fixed arithmetic (the FP64 launch of FP32 contexts)
@@ -416,8 +418,6 @@ int default_var64() {
   return 0;
 }
 
-// step constants that follow the chosen FP64 variant (the share format)
-void apply_variant(shl_ctx* c) { c->sc.qe_pairs = (kElemVariants[c->var64].pairs & 2) ? 1 : 0; }
 
 // Element-kernel autotuning: time every launch shape of the context's path on
 // its own mesh (one warm-up and three timed launches each, CUDA events on the
@@ -454,7 +454,6 @@ shl_status tune_elements(shl_ctx* c) {
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (fp32) c->var32 = best_v; else c->var64 = best_v;
-  apply_variant(c);
   return check_launch("element tuning");
 }
 
@@ -697,7 +696,6 @@ shl_status create_common(shl_ctx* c, const std::vector<double>& pscale_orig, shl
   sc.contact = contact ? 1 : 0;
   sc.smooth = smooth ? 1 : 0;
   c->var64 = default_var64();
-  apply_variant(c);
   for (int k = 0; k < 13; ++k) sc.stab_off[k] = stab_off[k];
   sc.friction = (contact && (p.mu_s != 0 || p.mu_d != 0)) ? 1 : 0;
   sc.pressure_base = p.pressure_base;
@@ -1707,7 +1705,6 @@ shl_status shl_set_element_variant(shl_ctx* c, int variant) {
     return SHL_ERR_ARG;
   }
   if (c->sc.fp32) c->var32 = variant; else c->var64 = variant;
-  apply_variant(c);
   if (c->graph) cudaGraphExecDestroy(c->graph);
   if (c->graph1) cudaGraphExecDestroy(c->graph1);
   c->graph = c->graph1 = nullptr;

@@ -57,16 +57,15 @@ struct ElemGroups {
 };
 
 // An element-kernel variant: threads per block, arithmetic (0 FP64, 1 the
-// displacement contraction as float pairs, 3 also the force contraction, its
-// shares stored as float pairs and added in FP64 by the gather; FP32-path
-// variants use 0) and a name for reports.
+// displacement contraction as float pairs; FP32-path variants use 0) and a
+// name for reports.
 struct ElemVariant {
   int block;
   int pairs;
   const char* name;
 };
 constexpr int kNumElemVariants = SHL_ELEMENT_VARIANTS;
-constexpr int kFirstFp32Variant = 11;
+constexpr int kFirstFp32Variant = 6;
 extern const ElemVariant kElemVariants[kNumElemVariants];
 
 // The element launch of a context: variant, grid and patch-group block ranges for its block size.
@@ -151,7 +150,6 @@ struct StepConst {
   uint32_t n_cells_cap, entries_cap, pairs_cap, csr_cap, cand_cap;
   int32_t contact;   // 1 if self-contact is on (LINEAR or SMOOTH)
   int32_t smooth;    // 1 for SMOOTH (limit-surface) self-contact
-  int32_t qe_pairs;  // FP64 element shares stored as float pairs (hi, lo) by the element kernel variant
   int32_t stab_off[13];  // SMOOTH: offset of the subdivision table of valence N in DevBuf::stab, or -1
   int32_t friction;  // 1 if mu_s or mu_d != 0
   int32_t pressure_base, pressure_dir;
@@ -243,7 +241,9 @@ __device__ __forceinline__ void smooth_patch(const DevBuf& b, const StepConst& s
   const uint32_t i = b.inv_perm[e];
   const int N = b.fsm[e] & 0xff;
   lp.N = N;
-  for (int j = 0; j < N + 6; ++j) lp.P[j] = b.p + 3 * (size_t)b.patch[(size_t)j * sc.F + i];
+  lp.base = b.p;
+  lp.ids = reinterpret_cast<const uint32_t*>(b.patch) + i;
+  lp.stride = sc.F;
   lp.tab = N == 6 ? nullptr : b.stab + sc.stab_off[N];
 }
 

@@ -540,8 +540,6 @@ __device__ __forceinline__ ElemOut element_force(uint32_t i, int np_rt, uint32_t
   }
   double* qe = b.qe + 3 * (size_t)slot0;
   if (DFQ) {
-    // the shares stay float pairs (hi, lo) in the same 8 bytes; the gather adds them in FP64
-    float2* qp = reinterpret_cast<float2*>(qe);
     const float* Bh = reinterpret_cast<const float*>(B + kMaxSlots * 6);
     const float* Bl = Bh + kMaxSlots * 6;
     float zh[6][3], zl[6][3];
@@ -557,7 +555,7 @@ __device__ __forceinline__ ElemOut element_force(uint32_t i, int np_rt, uint32_t
         float th = 0.f, tl = 0.f;
 #pragma unroll
         for (int k = 0; k < 6; ++k) df_madd(th, tl, Bh[6 * s + k], Bl[6 * s + k], zh[k][c], zl[k][c]);
-        qp[3 * s + c] = make_float2(th, tl);
+        qe[3 * s + c] = df_value(th, tl);
       }
     }
   } else {
@@ -1048,15 +1046,6 @@ __global__ void __launch_bounds__(kBlock) k_gather_correct(DevBuf b, StepConst s
       f[0] -= (double)s0;
       f[1] -= (double)s1;
       f[2] -= (double)s2;
-    } else if (sc.qe_pairs) {
-#pragma unroll 4
-      for (uint32_t k = g0; k < g1; ++k) {
-        const float2* q = reinterpret_cast<const float2*>(b.qe) + 3 * (size_t)__ldg(&b.gather_ent[k]);
-        const float2 q0 = q[0], q1 = q[1], q2 = q[2];
-        f[0] -= df_value(q0.x, q0.y);
-        f[1] -= df_value(q1.x, q1.y);
-        f[2] -= df_value(q2.x, q2.y);
-      }
     } else {
 #pragma unroll 4
       for (uint32_t k = g0; k < g1; ++k) {
@@ -1498,8 +1487,6 @@ void launch_positions(const DevBuf& b, const StepConst& sc, cudaStream_t s) {
 const ElemVariant kElemVariants[kNumElemVariants] = {
     {256, 0, "fp64 256x1"},        {256, 1, "fp64 256x1 pair-G"}, {128, 1, "fp64 128x3 pair-G"},
     {64, 1, "fp64 64x5 pair-G"},   {64, 1, "fp64 64x6 pair-G"},   {64, 0, "fp64 64x5"},
-    {64, 1, "fp64 64x8 pair-G"},   {256, 3, "fp64 256x1 pair-GQ"}, {128, 3, "fp64 128x3 pair-GQ"},
-    {64, 3, "fp64 64x6 pair-GQ"},  {64, 3, "fp64 64x8 pair-GQ"},
     {256, 0, "fp32 256x2"},        {128, 0, "fp32 128x4"},        {64, 0, "fp32 64x8"}};
 
 void launch_elements(const DevBuf& b, const StepConst& sc, const ElemLaunch& el, cudaStream_t s) {
@@ -1512,13 +1499,8 @@ void launch_elements(const DevBuf& b, const StepConst& sc, const ElemLaunch& el,
     case 3: k_elements<64, 5, true, false><<<nb, 64, 0, s>>>(b, sc, eg); break;
     case 4: k_elements<64, 6, true, false><<<nb, 64, 0, s>>>(b, sc, eg); break;
     case 5: k_elements<64, 5, false, false><<<nb, 64, 0, s>>>(b, sc, eg); break;
-    case 6: k_elements<64, 8, true, false><<<nb, 64, 0, s>>>(b, sc, eg); break;
-    case 7: k_elements<256, 1, true, true><<<nb, 256, 0, s>>>(b, sc, eg); break;
-    case 8: k_elements<128, 3, true, true><<<nb, 128, 0, s>>>(b, sc, eg); break;
-    case 9: k_elements<64, 6, true, true><<<nb, 64, 0, s>>>(b, sc, eg); break;
-    case 10: k_elements<64, 8, true, true><<<nb, 64, 0, s>>>(b, sc, eg); break;
-    case 11: k_elements32<256, 2><<<nb, 256, 0, s>>>(b, sc, eg); break;
-    case 12: k_elements32<128, 4><<<nb, 128, 0, s>>>(b, sc, eg); break;
+    case 6: k_elements32<256, 2><<<nb, 256, 0, s>>>(b, sc, eg); break;
+    case 7: k_elements32<128, 4><<<nb, 128, 0, s>>>(b, sc, eg); break;
     default: k_elements32<64, 8><<<nb, 64, 0, s>>>(b, sc, eg); break;
   }
   k_elem_totals<<<nblk(sc.F), kBlock, 0, s>>>(b, sc);

@@ -39,10 +39,13 @@
  *    can no longer decrease f, or after SHL_SMOOTH_MAX_IT iterations.
  *
  * Every floating-point operation is rounded on its own (SHL_MUL / SHL_ADD of
- * shl_geom.h); frexp / ldexp are exact, so host and device agree bit for bit.
+ * shl_geom.h) or is an explicit fused multiply-add (fma, IEEE on both sides);
+ * frexp / ldexp are exact, so host and device agree bit for bit.
  */
 #ifndef SHL_SMOOTH_H_
 #define SHL_SMOOTH_H_
+
+#include <stdint.h>
 
 #include "shl_geom.h"
 
@@ -103,41 +106,6 @@ static const signed char kShlStamSlot_h[12] = SHL_STAM_SLOT;
 #define SHL_STAMSLOT kShlStamSlot_h
 #endif
 
-/* The 12 box splines at (v, w): B[0] values, B[1] d/dv, B[2] d/dw and, for
- * order 2, B[3] d2/dv2, B[4] d2/dw2, B[5] d2/dvdw. */
-SHL_HD void shl_box_eval(double v, double w, int order, double B[6][12])
-{
-  double vp[5], wp[5];
-  vp[0] = 1.0;
-  wp[0] = 1.0;
-  for (int i = 1; i < 5; ++i) {
-    vp[i] = SHL_MUL(vp[i - 1], v);
-    wp[i] = SHL_MUL(wp[i - 1], w);
-  }
-  const int nq = order >= 2 ? 6 : (order >= 1 ? 3 : 1);
-  for (int s = 0; s < 12; ++s) {
-    double acc[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
-    for (int m = 0; m < 15; ++m) {
-      const int c = SHL_BOXC[s][m];
-      if (c == 0) continue;
-      const int p = SHL_BOXP[m], q = SHL_BOXQ[m];
-      const double cd = (double)c;
-      acc[0] = SHL_ADD(acc[0], SHL_MUL(cd, SHL_MUL(vp[p], wp[q])));
-      if (nq > 1) {
-        if (p >= 1) acc[1] = SHL_ADD(acc[1], SHL_MUL((double)(c * p), SHL_MUL(vp[p - 1], wp[q])));
-        if (q >= 1) acc[2] = SHL_ADD(acc[2], SHL_MUL((double)(c * q), SHL_MUL(vp[p], wp[q - 1])));
-      }
-      if (nq > 3) {
-        if (p >= 2) acc[3] = SHL_ADD(acc[3], SHL_MUL((double)(c * p * (p - 1)), SHL_MUL(vp[p - 2], wp[q])));
-        if (q >= 2) acc[4] = SHL_ADD(acc[4], SHL_MUL((double)(c * q * (q - 1)), SHL_MUL(vp[p], wp[q - 2])));
-        if (p >= 1 && q >= 1)
-          acc[5] = SHL_ADD(acc[5], SHL_MUL((double)(c * p * q), SHL_MUL(vp[p - 1], wp[q - 1])));
-      }
-    }
-    for (int k = 0; k < nq; ++k) B[k][s] = SHL_DIV(acc[k], 12.0);
-  }
-}
-
 /* rescale_irregular_coords (SubdivEvaluation.C:168-187): returns n and scales
  * (v, w) by 2^(n-1) so that v + w lies in (1/2, 1].  n = floor(1 - log2(v+w))
  * is computed exactly from the binary exponent. */
@@ -160,31 +128,32 @@ SHL_HD int shl_rescale_irregular(double* v, double* w)
 }
 
 /* A face's limit patch: its node positions in this library's patch order
- * (a, b, c, the remaining ring of a, d, b_far0, b_far1, c_far0, c_far1), the
- * valence N of its first vertex, and for N != 6 the subdivision table of
- * valence N (shl_subdiv.h layout: [level n-1][child k][Stam node s][slot]). */
+ * (a, b, c, the remaining ring of a, d, b_far0, b_far1, c_far0, c_far1) as
+ * base + 3 * ids[j * stride], the valence N of its first vertex, and for
+ * N != 6 the subdivision table of valence N (shl_subdiv.h layout: [level n-1]
+ * [child k][Stam node s][slot]). */
 typedef struct {
-  const double* P[SHL_SMOOTH_MAX_SLOTS];
+  const double* base;
+  const uint32_t* ids;
+  uint32_t stride;
   int N;
   const double* tab;
 } shl_limit_patch;
 
+#define SHL_FMA(a, b, c) fma((a), (b), (c))
+
 /* Limit surface of a patch at (v, w): out[0] the point, out[1] d/dv, out[2]
- * d/dw (order >= 1), out[3] d2/dv2, out[4] d2/dw2, out[5] d2/dvdw (order 2). */
+ * d/dw (order >= 1), out[3] d2/dv2, out[4] d2/dw2, out[5] d2/dvdw (order 2).
+ * The twelve control points of the regular (sub-)patch are formed one at a
+ * time and contracted with the box splines as they are evaluated (12 times
+ * the splines, scaled by 1/12 at the end), in fused multiply-adds; fma is
+ * IEEE on host and device, so both round alike. */
 SHL_HD void shl_limit_eval(const shl_limit_patch* pt, double v, double w, int order, double out[6][3])
 {
-  double Q[12][3];
   double j1 = 1.0;
-  if (pt->N == 6) {
-    for (int s = 0; s < 12; ++s) {
-      const double* x = pt->P[SHL_STAMSLOT[s]];
-      Q[s][0] = x[0];
-      Q[s][1] = x[1];
-      Q[s][2] = x[2];
-    }
-  } else {
-    const int n = shl_rescale_irregular(&v, &w);
-    int k;
+  int n = 0, k = 0;
+  if (pt->N != 6) {
+    n = shl_rescale_irregular(&v, &w);
     if (v > 0.5) {
       k = 0;
       v = SHL_SUB(SHL_MUL(2.0, v), 1.0);
@@ -201,33 +170,65 @@ SHL_HD void shl_limit_eval(const shl_limit_patch* pt, double v, double w, int or
       w = SHL_SUB(1.0, SHL_MUL(2.0, w));
       j1 = -ldexp(1.0, n);
     }
-    const int np = pt->N + 6;
-    const double* T = pt->tab + (size_t)((n - 1) * 3 + k) * 12 * (size_t)np;
-    for (int s = 0; s < 12; ++s) {
-      double q0 = 0.0, q1 = 0.0, q2 = 0.0;
+  }
+  const int np = pt->N + 6;
+  const double* T = pt->N == 6 ? 0 : pt->tab + (size_t)((n - 1) * 3 + k) * 12 * (size_t)np;
+  double vp[5], wp[5];
+  vp[0] = 1.0;
+  wp[0] = 1.0;
+  for (int i = 1; i < 5; ++i) {
+    vp[i] = SHL_MUL(vp[i - 1], v);
+    wp[i] = SHL_MUL(wp[i - 1], w);
+  }
+  const int nq = order >= 2 ? 6 : (order >= 1 ? 3 : 1);
+  double acc[6][3];
+  for (int q = 0; q < 6; ++q) acc[q][0] = acc[q][1] = acc[q][2] = 0.0;
+  for (int s = 0; s < 12; ++s) {
+    /* control point s */
+    double Q0, Q1, Q2;
+    if (T == 0) {
+      const double* x = pt->base + 3 * (size_t)pt->ids[(size_t)SHL_STAMSLOT[s] * pt->stride];
+      Q0 = x[0];
+      Q1 = x[1];
+      Q2 = x[2];
+    } else {
+      Q0 = Q1 = Q2 = 0.0;
       for (int j = 0; j < np; ++j) {
         const double t = T[s * np + j];
         if (t == 0.0) continue;
-        const double* x = pt->P[j];
-        q0 = SHL_ADD(q0, SHL_MUL(t, x[0]));
-        q1 = SHL_ADD(q1, SHL_MUL(t, x[1]));
-        q2 = SHL_ADD(q2, SHL_MUL(t, x[2]));
+        const double* x = pt->base + 3 * (size_t)pt->ids[(size_t)j * pt->stride];
+        Q0 = SHL_FMA(t, x[0], Q0);
+        Q1 = SHL_FMA(t, x[1], Q1);
+        Q2 = SHL_FMA(t, x[2], Q2);
       }
-      Q[s][0] = q0;
-      Q[s][1] = q1;
-      Q[s][2] = q2;
+    }
+    /* box spline s and its derivatives, times 12 */
+    double bs[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    for (int m = 0; m < 15; ++m) {
+      const int c = SHL_BOXC[s][m];
+      if (c == 0) continue;
+      const int p = SHL_BOXP[m], q = SHL_BOXQ[m];
+      bs[0] = SHL_FMA((double)c, SHL_MUL(vp[p], wp[q]), bs[0]);
+      if (nq > 1) {
+        if (p >= 1) bs[1] = SHL_FMA((double)(c * p), SHL_MUL(vp[p - 1], wp[q]), bs[1]);
+        if (q >= 1) bs[2] = SHL_FMA((double)(c * q), SHL_MUL(vp[p], wp[q - 1]), bs[2]);
+      }
+      if (nq > 3) {
+        if (p >= 2) bs[3] = SHL_FMA((double)(c * p * (p - 1)), SHL_MUL(vp[p - 2], wp[q]), bs[3]);
+        if (q >= 2) bs[4] = SHL_FMA((double)(c * q * (q - 1)), SHL_MUL(vp[p], wp[q - 2]), bs[4]);
+        if (p >= 1 && q >= 1) bs[5] = SHL_FMA((double)(c * p * q), SHL_MUL(vp[p - 1], wp[q - 1]), bs[5]);
+      }
+    }
+    for (int q = 0; q < nq; ++q) {
+      acc[q][0] = SHL_FMA(bs[q], Q0, acc[q][0]);
+      acc[q][1] = SHL_FMA(bs[q], Q1, acc[q][1]);
+      acc[q][2] = SHL_FMA(bs[q], Q2, acc[q][2]);
     }
   }
-  double B[6][12];
-  shl_box_eval(v, w, order, B);
-  const int nq = order >= 2 ? 6 : (order >= 1 ? 3 : 1);
-  for (int k = 0; k < nq; ++k) {
-    const double sc = k == 0 ? 1.0 : (k < 3 ? j1 : SHL_MUL(j1, j1));
-    for (int c = 0; c < 3; ++c) {
-      double acc = 0.0;
-      for (int s = 0; s < 12; ++s) acc = SHL_ADD(acc, SHL_MUL(B[k][s], Q[s][c]));
-      out[k][c] = SHL_MUL(acc, sc);
-    }
+  const double twelfth = 1.0 / 12.0;
+  for (int q = 0; q < nq; ++q) {
+    const double sc = q == 0 ? twelfth : (q < 3 ? SHL_MUL(j1, twelfth) : SHL_MUL(SHL_MUL(j1, j1), twelfth));
+    for (int c = 0; c < 3; ++c) out[q][c] = SHL_MUL(acc[q][c], sc);
   }
 }
 
