@@ -35,8 +35,11 @@
  *    line search then starts at the boundary: f is not convex there), the
  *    working set from the first-order multipliers of the active constraints,
  *    an Armijo backtracking line search capped by find_max_alpha.  It stops
- *    when a step no longer changes x by more than 1e-14, when the line search
- *    can no longer decrease f, or after SHL_SMOOTH_MAX_IT iterations.
+ *    when the Newton step is below 1e-12 (x in units of the triangle), after
+ *    a full Newton step (convex model) shorter than 1e-6 (quadratic
+ *    convergence: the next would be of order 1e-12), when a step no longer
+ *    changes x by more than 1e-14, when the line search can no longer decrease
+ *    f, or after SHL_SMOOTH_MAX_IT iterations.
  *
  * Every floating-point operation is rounded on its own (SHL_MUL / SHL_ADD of
  * shl_geom.h) or is an explicit fused multiply-add (fma, IEEE on both sides);
@@ -59,6 +62,9 @@
 #define SHL_SMOOTH_MAX_IT 40
 #define SHL_SMOOTH_CONSTRAINT_TOL (100 * 2.220446049250313e-16)
 #define SHL_SMOOTH_STEP_TOL 1e-14
+#define SHL_SMOOTH_NEWTON_TOL 1e-12
+#define SHL_SMOOTH_QUAD_TOL 1e-6
+#define SHL_SMOOTH_MAX_HALVINGS 30
 
 /* Stam's box splines (J. Stam, "Evaluation of Loop subdivision surfaces",
  * SIGGRAPH'98 course notes) expanded into monomials of (v, w) with
@@ -506,7 +512,9 @@ SHL_HD int shl_smooth_closest(const shl_limit_patch* A, const shl_limit_patch* B
       dn = fmax(dn, fabs(d[i]));
       gd = SHL_ADD(gd, SHL_MUL(g[i], d[i]));
     }
-    if (!(dn > 0.0) || !(gd < 0.0)) break;
+    /* converged: a Newton step this short moves the closest points by less
+     * than 1e-12 of the element size (the distance error is its square) */
+    if (!(dn > SHL_SMOOTH_NEWTON_TOL) || !(gd < 0.0)) break;
     const double amax = shl_smooth_max_alpha(x, d);
     /* a Newton step where f is convex on the free subspace; otherwise the step
      * to the boundary first (along a direction of negative curvature f keeps
@@ -515,7 +523,7 @@ SHL_HD int shl_smooth_closest(const shl_limit_patch* A, const shl_limit_patch* B
     if (!(alpha > 0.0)) break;
     bool accepted = false;
     double xt[4], q1[3], q2[3], ft = 0.0;
-    for (int ls = 0; ls < 40; ++ls) {
+    for (int ls = 0; ls < SHL_SMOOTH_MAX_HALVINGS; ++ls) {
       for (int i = 0; i < 4; ++i) xt[i] = SHL_ADD(x[i], SHL_MUL(alpha, d[i]));
       shl_smooth_apply_constraints(xt);
       ft = shl_smooth_f(A, B, xt, q1, q2);
@@ -531,7 +539,10 @@ SHL_HD int shl_smooth_closest(const shl_limit_patch* A, const shl_limit_patch* B
       step = fmax(step, fabs(SHL_SUB(xt[i], x[i])));
       x[i] = xt[i];
     }
-    if (step <= SHL_SMOOTH_STEP_TOL) {
+    /* done after a vanishing step, or after a full Newton step of a convex
+     * model that was already short: the next one would be of its square */
+    const int full_newton = !shifted && alpha == 1.0;
+    if (step <= SHL_SMOOTH_STEP_TOL || (full_newton && step <= SHL_SMOOTH_QUAD_TOL)) {
       f = ft;
       for (int c = 0; c < 3; ++c) {
         p1[c] = q1[c];
