@@ -32,10 +32,13 @@
  *    the reference's sources; it is restated here as an active-set projected
  *    Newton method: exact Hessian of f from the limit surface's second
  *    derivatives, shifted to positive definite on the free subspace (the
- *    line search then starts at the boundary: f is not convex there), the
+ *    line search then starts at the boundary, f being not convex there, and
+ *    goes on from a step of length 0.05 if that is rejected), the
  *    working set from the first-order multipliers of the active constraints,
  *    an Armijo backtracking line search capped by find_max_alpha.  It stops
- *    when the Newton step is below 1e-12 (x in units of the triangle), after
+ *    when the gradient projected on the free directions of the working set
+ *    is below 1e-9 of the gradient (first-order optimality), when the
+ *    decrease the Newton step promises is below 1e-15 of f, after
  *    a full Newton step (convex model) shorter than 1e-6 (quadratic
  *    convergence: the next would be of order 1e-12), when a step no longer
  *    changes x by more than 1e-14, when the line search can no longer decrease
@@ -62,8 +65,9 @@
 #define SHL_SMOOTH_MAX_IT 40
 #define SHL_SMOOTH_CONSTRAINT_TOL (100 * 2.220446049250313e-16)
 #define SHL_SMOOTH_STEP_TOL 1e-14
-#define SHL_SMOOTH_NEWTON_TOL 1e-12
+#define SHL_SMOOTH_DECREMENT_TOL 1e-15
 #define SHL_SMOOTH_QUAD_TOL 1e-6
+#define SHL_SMOOTH_KKT_TOL 1e-9
 #define SHL_SMOOTH_MAX_HALVINGS 30
 
 /* Stam's box splines (J. Stam, "Evaluation of Loop subdivision surfaces",
@@ -417,15 +421,25 @@ SHL_HD int shl_smooth_direction(const double* g, double H[4][4], const unsigned*
       HZ[a][i] = t;
     }
   }
-  double dmax = 0.0;
   for (int a = 0; a < m; ++a)
     for (int b = 0; b < m; ++b) {
       double s = 0.0;
       for (int i = 0; i < 4; ++i) s = SHL_ADD(s, SHL_MUL(Z[a][i], HZ[b][i]));
       Hr[a][b] = s;
-      if (a == b) dmax = fmax(dmax, fabs(s));
     }
-  if (!(dmax > 0.0)) dmax = 1.0;
+  /* Jacobi scaling: the free directions can differ in scale by many orders
+   * (the limit surface's parametric derivatives grow like 2^n next to an
+   * irregular vertex), so the system is solved for the unit-diagonal matrix
+   * S Hr S, S = diag(|Hr_aa|^-1/2), and the shift mu is relative to 1 */
+  double S[4];
+  for (int a = 0; a < m; ++a) {
+    const double h = fabs(Hr[a][a]);
+    S[a] = h > 0.0 ? SHL_DIV(1.0, SHL_SQRT(h)) : 1.0;
+  }
+  for (int a = 0; a < m; ++a) {
+    gr[a] = SHL_MUL(S[a], gr[a]);
+    for (int b = 0; b < m; ++b) Hr[a][b] = SHL_MUL(SHL_MUL(S[a], Hr[a][b]), S[b]);
+  }
   double mu = 0.0, L[4][4], y[4];
   for (int attempt = 0; attempt < 24; ++attempt) {
     bool ok = true;
@@ -435,7 +449,7 @@ SHL_HD int shl_smooth_direction(const double* g, double H[4][4], const unsigned*
         if (a == b) s = SHL_ADD(s, mu);
         for (int k = 0; k < b; ++k) s = SHL_SUB(s, SHL_MUL(L[a][k], L[b][k]));
         if (a == b) {
-          if (!(s > SHL_MUL(1e-14, dmax))) { ok = false; break; }
+          if (!(s > 1e-14)) { ok = false; break; }
           L[a][a] = SHL_SQRT(s);
         } else {
           L[a][b] = SHL_DIV(s, L[b][b]);
@@ -454,18 +468,18 @@ SHL_HD int shl_smooth_direction(const double* g, double H[4][4], const unsigned*
       }
       for (int i = 0; i < 4; ++i) {
         double s = 0.0;
-        for (int a = 0; a < m; ++a) s = SHL_ADD(s, SHL_MUL(Z[a][i], y[a]));
+        for (int a = 0; a < m; ++a) s = SHL_ADD(s, SHL_MUL(Z[a][i], SHL_MUL(S[a], y[a])));
         d[i] = s;
       }
       return mu > 0.0 ? 1 : 0;
     }
-    mu = mu == 0.0 ? SHL_MUL(1e-10, dmax) : SHL_MUL(mu, 10.0);
+    mu = mu == 0.0 ? 1e-10 : SHL_MUL(mu, 10.0);
   }
-  /* not reached for finite input: projected steepest descent */
+  /* not reached for finite input: scaled projected steepest descent */
   for (int i = 0; i < 4; ++i) {
     double s = 0.0;
-    for (int a = 0; a < m; ++a) s = SHL_ADD(s, SHL_MUL(Z[a][i], -gr[a]));
-    d[i] = SHL_DIV(s, dmax);
+    for (int a = 0; a < m; ++a) s = SHL_ADD(s, SHL_MUL(Z[a][i], SHL_MUL(S[a], -gr[a])));
+    d[i] = s;
   }
   return 1;
 }
@@ -486,6 +500,21 @@ SHL_HD int shl_smooth_closest(const shl_limit_patch* A, const shl_limit_patch* B
     for (int t = 0; t < 2; ++t) {
       act[t] = ((bm >> (2 * t)) & 1u) | (((bm >> (2 * t + 1)) & 1u) << 1) | (((bm >> (4 + t)) & 1u) << 2);
       work[t] = shl_smooth_working(act[t], g[2 * t], g[2 * t + 1]);
+    }
+    /* first-order optimality on the working set (the KKT conditions of the
+     * constrained minimum, the multipliers' signs being the working set's
+     * condition): the projected gradient vanishes to 1e-9 of the gradient */
+    {
+      double pg = 0.0, gn = 0.0;
+      for (int t = 0; t < 2; ++t) {
+        const double gv = g[2 * t], gw = g[2 * t + 1];
+        gn = fmax(gn, fmax(fabs(gv), fabs(gw)));
+        if (work[t] == 0u) pg = fmax(pg, fmax(fabs(gv), fabs(gw)));
+        else if (work[t] == 1u) pg = fmax(pg, fabs(gw));
+        else if (work[t] == 2u) pg = fmax(pg, fabs(gv));
+        else if (work[t] == 4u) pg = fmax(pg, SHL_MUL(0.5, fabs(SHL_SUB(gv, gw))));
+      }
+      if (pg <= SHL_MUL(SHL_SMOOTH_KKT_TOL, gn)) break;
     }
     double d[4];
     int shifted = 0;
@@ -512,9 +541,12 @@ SHL_HD int shl_smooth_closest(const shl_limit_patch* A, const shl_limit_patch* B
       dn = fmax(dn, fabs(d[i]));
       gd = SHL_ADD(gd, SHL_MUL(g[i], d[i]));
     }
-    /* converged: a Newton step this short moves the closest points by less
-     * than 1e-12 of the element size (the distance error is its square) */
-    if (!(dn > SHL_SMOOTH_NEWTON_TOL) || !(gd < 0.0)) break;
+#ifdef SHL_SMOOTH_TRACE
+    SHL_SMOOTH_TRACE(it, x, f, g, d, work);
+#endif
+    /* converged: the model decrease along the step (-g.d, the Newton
+     * decrement) is below 1e-15 of f, the precision of f itself */
+    if (!(dn > 0.0) || !(gd < 0.0) || -gd <= SHL_MUL(SHL_SMOOTH_DECREMENT_TOL, f)) break;
     const double amax = shl_smooth_max_alpha(x, d);
     /* a Newton step where f is convex on the free subspace; otherwise the step
      * to the boundary first (along a direction of negative curvature f keeps
@@ -531,7 +563,10 @@ SHL_HD int shl_smooth_closest(const shl_limit_patch* A, const shl_limit_patch* B
         accepted = true;
         break;
       }
-      alpha = SHL_MUL(alpha, 0.5);
+      /* after a rejected step to the boundary along a direction of negative
+       * curvature, go on from a step of length 0.05 (triangle units) */
+      const double a_half = SHL_MUL(alpha, 0.5);
+      alpha = (ls == 0 && shifted) ? fmin(a_half, SHL_DIV(0.05, dn)) : a_half;
     }
     if (!accepted) break;
     double step = 0.0;
