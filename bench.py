@@ -18,7 +18,9 @@ face-steps per second.  Reported:
              and the state is copied back;
   roofline   the element-force kernel timed live (events, cold L2) against
              its algorithmic bytes and FP64 flops;
-  cpu_baseline  the CPU oracle on this host's cores on a bounded sample.
+  cpu_baseline  the CPU oracle on this host's cores on a bounded sample;
+  contact_modes  LINEAR and SMOOTH self-contact at a squashed, contact-heavy
+             state of the same shell (10 steps each).
 
 python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--level L]
 """
@@ -40,9 +42,9 @@ from shell_gb300.workloads import (ALPHA, AMPL, DT, G12, MU, NU12, RAMP_STEPS, R
 
 FLUSH_BYTES = 512 << 20
 # library kernels per step with self-contact: predictor, two rebuild-condition kernels (the IF nodes'
-# conditions), element kernel + totals, contact force, gather/corrector, volume/end of step; plus
-# the 27 kernels of each candidate-list rebuild that runs (10 pipeline + 3 x 3 scan + 8 contact CSR)
-LAUNCHES_PER_STEP_CONTACT = 8
+# conditions), element kernel, contact force, gather/corrector, volume/measurement totals/end of step;
+# plus the 27 kernels of each candidate-list rebuild that runs (10 pipeline + 3 x 3 scan + 8 contact CSR)
+LAUNCHES_PER_STEP_CONTACT = 7
 LAUNCHES_PER_REBUILD = 27
 # element kernel: per-face FP64 constants, patch ids, force shares, element
 # fields, face permutation (bytes); per-node predicted displacement (bytes)

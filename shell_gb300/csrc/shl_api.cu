@@ -308,7 +308,7 @@ cudaError_t enqueue_step(shl_ctx* c, bool capturing = false) {
   cudaError_t e = cudaSuccess;
   launch_predict(b, sc, 0, s);
   if (sc.contact && (e = enqueue_rebuild(c, capturing)) != cudaSuccess) return e;
-  launch_elements(b, sc, elem_launch(c, sc), s);
+  launch_elements(b, sc, elem_launch(c, sc), s, false);  // totals in k_volume_end
   if (sc.contact) launch_contact_force(b, sc, 0, s);
   if (sc.adapt_every) {
     // one attempt: estimate, then correct only if accepted (ShellSystem.C:1010-1117)
@@ -939,7 +939,7 @@ shl_status initial_state(shl_ctx* c, Ctl& h) {
   h.rebuild = c->sc.contact ? 1u : 0u;  // compute_shell_shell_contact_candidates(true)
   SHL_TRY(ctl_put(c, h));
   if (c->sc.contact) launch_rebuild(c->b, c->sc, c->stream);
-  launch_elements(c->b, c->sc, elem_launch(c, c->sc), c->stream);
+  launch_elements(c->b, c->sc, elem_launch(c, c->sc), c->stream, false);
   launch_volume_end_step(c->b, c->sc, false, c->stream);
   SHL_TRY(check_launch("initial conditions"));
   SHL_TRY(ctl_get(c, h));
@@ -1280,7 +1280,7 @@ shl_status shl_profile_step(shl_ctx* c, double pressure, size_t flush_bytes, dou
   cudaEventRecord(ev[1], s);
   if (sc.contact) launch_rebuild(b, sc, s);
   cudaEventRecord(ev[2], s);
-  launch_elements(b, sc, elem_launch(c, sc), s);
+  launch_elements(b, sc, elem_launch(c, sc), s, false);
   cudaEventRecord(ev[3], s);
   if (sc.contact) launch_contact_force(b, sc, 0, s);
   cudaEventRecord(ev[4], s);

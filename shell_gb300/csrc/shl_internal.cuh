@@ -271,7 +271,9 @@ __device__ __forceinline__ void smooth_pair(const DevBuf& b, const StepConst& sc
 
 // ---- launchers (shl_kernels.cu) ----
 void launch_predict(const DevBuf& b, const StepConst& sc, int cur, cudaStream_t s);
-void launch_elements(const DevBuf& b, const StepConst& sc, const ElemLaunch& el, cudaStream_t s);
+// totals: also the fixed-order sums of the per-face measurements (k_elem_totals);
+// k_volume_end forms them too, so launches followed by it pass false
+void launch_elements(const DevBuf& b, const StepConst& sc, const ElemLaunch& el, cudaStream_t s, bool totals = true);
 void launch_contact_force(const DevBuf& b, const StepConst& sc, int cur, cudaStream_t s);
 void launch_gather_correct(const DevBuf& b, const StepConst& sc, int cur, bool correct, double* f_out,
                            double* a_out, cudaStream_t s);

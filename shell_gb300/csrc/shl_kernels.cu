@@ -94,6 +94,49 @@ __device__ __forceinline__ bool last_block(uint32_t* counter) {
   return is_last;
 }
 
+// N block sums at once (the same order per sum as block_sum); the result is in thread 0
+template <int N>
+__device__ __forceinline__ void block_sum_n(double* x, double (*sh)[kBlock / 32]) {
+#pragma unroll
+  for (int k = 0; k < N; ++k)
+    for (int o = 16; o > 0; o >>= 1) x[k] += __shfl_down_sync(0xffffffffu, x[k], o);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  __syncthreads();
+  if (lane == 0)
+#pragma unroll
+    for (int k = 0; k < N; ++k) sh[k][warp] = x[k];
+  __syncthreads();
+  if (warp == 0)
+#pragma unroll
+    for (int k = 0; k < N; ++k) {
+      x[k] = (lane < (int)(blockDim.x >> 5)) ? sh[k][lane] : 0.0;
+      for (int o = 16; o > 0; o >>= 1) x[k] += __shfl_down_sync(0xffffffffu, x[k], o);
+    }
+}
+
+// fields 0..N-1 of the per-block partials summed over the blocks in fixed order
+// (the same order per field as sum_partials; last block only, result in thread 0)
+template <int N>
+__device__ __forceinline__ void sum_partials_n(const double* partial, int nb, double (*sh)[kBlock / 32],
+                                               double* out) {
+#pragma unroll
+  for (int k = 0; k < N; ++k) out[k] = 0.0;
+  for (int b = threadIdx.x; b < nb; b += blockDim.x)
+#pragma unroll
+    for (int k = 0; k < N; ++k) out[k] += __ldcg(&partial[(size_t)b * 8 + k]);
+  block_sum_n<N>(out, sh);
+}
+
+// per-face measurement densities times area (E_tens, E_bend, kGauss, kMean) and the area
+__device__ __forceinline__ void face_totals(const DevBuf& b, uint32_t e, double* v) {
+  const double ar = b.area[e];
+  v[0] = b.etens[e] * ar;
+  v[1] = b.ebend[e] * ar;
+  v[2] = b.kG[e] * ar;
+  v[3] = b.kM[e] * ar;
+  v[4] = ar;
+}
+
 // sum of partial[k * stride + b] over blocks b in fixed order (last block only)
 __device__ __forceinline__ double sum_partials(const double* partial, int k, int nb, double* sh) {
   double s = 0.0;
@@ -843,31 +886,20 @@ __global__ void __launch_bounds__(BS, MINB) k_elements(DevBuf b, StepConst sc, E
 __global__ void __launch_bounds__(kBlock) k_elem_totals(DevBuf b, StepConst sc) {
   Ctl* ctl = b.ctl;
   if (inactive(ctl)) return;
-  __shared__ double sh[kBlock / 32];
+  __shared__ double sh[5][kBlock / 32];
   const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
-  double et = 0.0, eb = 0.0, kg = 0.0, km = 0.0, ar = 0.0;
-  if (e < sc.F) {
-    ar = b.area[e];
-    et = b.etens[e] * ar;
-    eb = b.ebend[e] * ar;
-    kg = b.kG[e] * ar;
-    km = b.kM[e] * ar;
-  }
-  const double s0 = block_sum(et, sh), s1 = block_sum(eb, sh), s2 = block_sum(kg, sh), s3 = block_sum(km, sh),
-               s4 = block_sum(ar, sh);
+  double v[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+  if (e < sc.F) face_totals(b, e, v);
+  block_sum_n<5>(v, sh);
   if (threadIdx.x == 0) {
     double* pp = b.partial + (size_t)blockIdx.x * 8;
-    pp[0] = s0; pp[1] = s1; pp[2] = s2; pp[3] = s3; pp[4] = s4;
+    for (int k = 0; k < 5; ++k) pp[k] = v[k];
   }
   if (!last_block(&ctl->cnt[1])) return;
-  const int nb = gridDim.x;
-  const double t0 = sum_partials(b.partial, 0, nb, sh);
-  const double t1 = sum_partials(b.partial, 1, nb, sh);
-  const double t2 = sum_partials(b.partial, 2, nb, sh);
-  const double t3 = sum_partials(b.partial, 3, nb, sh);
-  const double t4 = sum_partials(b.partial, 4, nb, sh);
+  double t[5];
+  sum_partials_n<5>(b.partial, gridDim.x, sh, t);
   if (threadIdx.x == 0) {
-    ctl->Etens = t0; ctl->Ebend = t1; ctl->kGauss = t2; ctl->kMean = t3; ctl->area = t4;
+    ctl->Etens = t[0]; ctl->Ebend = t[1]; ctl->kGauss = t[2]; ctl->kMean = t[3]; ctl->area = t[4];
   }
 }
 
@@ -1343,22 +1375,30 @@ __global__ void __launch_bounds__(kBlock) k_volume_end(DevBuf b, StepConst sc, i
     }
     return;
   }
-  __shared__ double sh[kBlock / 32];
+  // the element kernel's per-face measurement totals (as k_elem_totals forms
+  // them, bit for bit) and the enclosed volume, in one pass over the faces
+  __shared__ double sh[6][kBlock / 32];
   const uint32_t f = blockIdx.x * blockDim.x + threadIdx.x;
-  double det = 0.0;
+  double v[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
   if (f < sc.F) {
+    face_totals(b, f, v);
     const double* q0 = b.p + 3 * (size_t)b.tri[3 * (size_t)f];
     const double* q1 = b.p + 3 * (size_t)b.tri[3 * (size_t)f + 1];
     const double* q2 = b.p + 3 * (size_t)b.tri[3 * (size_t)f + 2];
-    det = q0[0] * (q1[1] * q2[2] - q2[1] * q1[2]) - q1[0] * (q0[1] * q2[2] - q2[1] * q0[2]) +
-          q2[0] * (q0[1] * q1[2] - q1[1] * q0[2]);
+    v[5] = q0[0] * (q1[1] * q2[2] - q2[1] * q1[2]) - q1[0] * (q0[1] * q2[2] - q2[1] * q0[2]) +
+           q2[0] * (q0[1] * q1[2] - q1[1] * q0[2]);
   }
-  const double s = block_sum(det, sh);
-  if (threadIdx.x == 0) b.partial[(size_t)blockIdx.x * 8] = s;
+  block_sum_n<6>(v, sh);
+  if (threadIdx.x == 0) {
+    double* pp = b.partial + (size_t)blockIdx.x * 8;
+    for (int k = 0; k < 6; ++k) pp[k] = v[k];
+  }
   if (!last_block(&ctl->cnt[4])) return;
-  const double tot = sum_partials(b.partial, 0, gridDim.x, sh);
+  double t[6];
+  sum_partials_n<6>(b.partial, gridDim.x, sh, t);
   if (threadIdx.x != 0) return;
-  ctl->volume = fabs(tot / 6.0) - ctl->area * 0.5 * sc.thickness;
+  ctl->Etens = t[0]; ctl->Ebend = t[1]; ctl->kGauss = t[2]; ctl->kMean = t[3]; ctl->area = t[4];
+  ctl->volume = fabs(t[5] / 6.0) - ctl->area * 0.5 * sc.thickness;
   if (!end_step) return;
   const double dt = sc.adapt_every ? ctl->dt_cur : sc.dt;
   ctl->sum_dt += dt;
@@ -1489,7 +1529,7 @@ const ElemVariant kElemVariants[kNumElemVariants] = {
     {64, 1, "fp64 64x5 pair-G"},   {64, 1, "fp64 64x6 pair-G"},   {64, 0, "fp64 64x5"},
     {256, 0, "fp32 256x2"},        {128, 0, "fp32 128x4"},        {64, 0, "fp32 64x8"}};
 
-void launch_elements(const DevBuf& b, const StepConst& sc, const ElemLaunch& el, cudaStream_t s) {
+void launch_elements(const DevBuf& b, const StepConst& sc, const ElemLaunch& el, cudaStream_t s, bool totals) {
   const uint32_t nb = el.blocks;
   const ElemGroups& eg = el.eg;
   switch (el.variant) {
@@ -1503,7 +1543,7 @@ void launch_elements(const DevBuf& b, const StepConst& sc, const ElemLaunch& el,
     case 7: k_elements32<128, 4><<<nb, 128, 0, s>>>(b, sc, eg); break;
     default: k_elements32<64, 8><<<nb, 64, 0, s>>>(b, sc, eg); break;
   }
-  k_elem_totals<<<nblk(sc.F), kBlock, 0, s>>>(b, sc);
+  if (totals) k_elem_totals<<<nblk(sc.F), kBlock, 0, s>>>(b, sc);
 }
 void launch_contact_force(const DevBuf& b, const StepConst& sc, int, cudaStream_t s) {
   uint32_t nb = nblk(sc.pairs_cap);
