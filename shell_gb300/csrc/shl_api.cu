@@ -532,10 +532,7 @@ shl_status create_common(shl_ctx* c, const std::vector<double>& pscale_orig, shl
     }
     c->blocks_bs[k] = nb ? nb : 1;
   }
-  // per-block partial sums: the largest grid of any reducing kernel (predictor: 64-thread
-  // blocks over nodes, gather: kGatherLanes lanes per node, face sums: kTotalsBlock)
-  const uint32_t max_blocks = std::max({blocks, (F + kBlock - 1) / kBlock, (F + kTotalsBlock - 1) / kTotalsBlock,
-                                        (kGatherLanes * V + kBlock - 1) / kBlock, (V + 63) / 64, 4u * 152u}) + 8;
+  const uint32_t max_blocks = std::max({blocks, (F + kBlock - 1) / kBlock, (V + kBlock - 1) / kBlock, 4u * 152u}) + 8;
   ALLOC(b.partial, 8 * (size_t)max_blocks);
   ALLOC(c->d_fa, 2 * nd);
   ALLOC(b.ctl, 1);

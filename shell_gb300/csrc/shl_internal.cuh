@@ -30,8 +30,6 @@
 namespace shl {
 
 constexpr int kBlock = 256;          // threads per block for element / node kernels
-constexpr int kGatherLanes = 4;      // lanes per node in the gather (k_gather_correct)
-constexpr int kTotalsBlock = 128;    // threads per block of the fixed-order face sums (k_elem_totals, k_volume_end)
 constexpr int kMaxGroups = 8;        // patch groups (regular + irregular valences)
 constexpr int kMaxSlots = 18;        // patch slots of the largest supported valence (12)
 // doubles per contact pair written by the contact-force kernel

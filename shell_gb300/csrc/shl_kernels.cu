@@ -1045,20 +1045,14 @@ __global__ void __launch_bounds__(kBlock) k_gather_correct(DevBuf b, StepConst s
   Ctl* ctl = b.ctl;
   if (inactive(ctl)) return;
   __shared__ double sh[kBlock / 32];
-  // kGatherLanes consecutive lanes per node: each adds every kGatherLanes-th
-  // contact and element share of the node, then the lanes' sums are combined in
-  // a fixed tree order (deterministic), and the node's first lane goes on alone
-  const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
-  const uint32_t n = tid / kGatherLanes;
-  const uint32_t lane = tid % kGatherLanes;
-  const bool node_ok = n < sc.V;
+  const uint32_t n = blockIdx.x * blockDim.x + threadIdx.x;
   double du2 = 0.0, ekin = 0.0;
   double c_nc = 0.0, c_e = 0.0, c_ef = 0.0, c_fn = 0.0;  // cavity: contacts, energy, friction energy, force
-  double cs[3] = {0.0, 0.0, 0.0}, es[3] = {0.0, 0.0, 0.0};  // this lane's contact and element sums
-  if (node_ok) {
+  if (n < sc.V) {
+    double f[3] = {0.0, 0.0, 0.0};
     if (sc.contact) {
       const uint32_t k0 = b.csr_ptr[n], k1 = b.csr_ptr[n + 1];
-      for (uint32_t k = k0 + lane; k < k1; k += kGatherLanes) {
+      for (uint32_t k = k0; k < k1; ++k) {
         const uint32_t ent = b.csr_ent[k];
         const uint32_t j = ent >> 3, role = ent & 7u;
         const int e = role >= 3 ? 1 : 0, kk = role - 3 * e;
@@ -1066,45 +1060,33 @@ __global__ void __launch_bounds__(kBlock) k_gather_correct(DevBuf b, StepConst s
         const double vv = pf[3 + 2 * e], ww = pf[4 + 2 * e];
         const double bary = kk == 0 ? (1.0 - vv - ww) : (kk == 1 ? vv : ww);
         const double pref = e == 0 ? -0.5 : 0.5;
-        cs[0] += bary * (pref * pf[0]);
-        cs[1] += bary * (pref * pf[1]);
-        cs[2] += bary * (pref * pf[2]);
+        f[0] += bary * (pref * pf[0]);
+        f[1] += bary * (pref * pf[1]);
+        f[2] += bary * (pref * pf[2]);
       }
     }
     const uint32_t g0 = b.gather_ptr[n], g1 = b.gather_ptr[n + 1];
     if (sc.fp32) {
       float s0 = 0.f, s1 = 0.f, s2 = 0.f;
-#pragma unroll 2
-      for (uint32_t k = g0 + lane; k < g1; k += kGatherLanes) {
+#pragma unroll 4
+      for (uint32_t k = g0; k < g1; ++k) {
         const float* q = b.qe32 + 3 * (size_t)__ldg(&b.gather_ent[k]);
         s0 += q[0];
         s1 += q[1];
         s2 += q[2];
       }
-      es[0] = (double)s0;
-      es[1] = (double)s1;
-      es[2] = (double)s2;
+      f[0] -= (double)s0;
+      f[1] -= (double)s1;
+      f[2] -= (double)s2;
     } else {
-#pragma unroll 2
-      for (uint32_t k = g0 + lane; k < g1; k += kGatherLanes) {
+#pragma unroll 4
+      for (uint32_t k = g0; k < g1; ++k) {
         const double* q = b.qe + 3 * (size_t)__ldg(&b.gather_ent[k]);
-        es[0] += q[0];
-        es[1] += q[1];
-        es[2] += q[2];
+        f[0] -= q[0];
+        f[1] -= q[1];
+        f[2] -= q[2];
       }
     }
-  }
-  // (l0 + l1) + (l2 + l3): every lane ends with the same sums
-#pragma unroll
-  for (int c = 0; c < 3; ++c)
-#pragma unroll
-    for (int o = 1; o < kGatherLanes; o <<= 1) {
-      const double a0 = __shfl_xor_sync(0xffffffffu, cs[c], o), a1 = __shfl_xor_sync(0xffffffffu, es[c], o);
-      cs[c] = (lane & o) ? a0 + cs[c] : cs[c] + a0;
-      es[c] = (lane & o) ? a1 + es[c] : es[c] + a1;
-    }
-  if (node_ok && lane == 0) {
-    double f[3] = {cs[0] - es[0], cs[1] - es[1], cs[2] - es[2]};
     if (sc.cavity_contact) {
       // interaction with the cavity (ShellSystem.C:1600-1723)
       const CavityGeom cg = cavity_geom(ctl->cav_R, sc);
@@ -1533,11 +1515,10 @@ void launch_flush(void* buf, size_t bytes, uint32_t tag, cudaStream_t s) {
 }
 
 // --------------------------------------------------------------- launch --
-static inline uint32_t nblk(uint32_t n, uint32_t bs = kBlock) { return n == 0 ? 1 : (n + bs - 1) / bs; }
+static inline uint32_t nblk(uint32_t n) { return (n + kBlock - 1) / kBlock; }
 
 void launch_predict(const DevBuf& b, const StepConst& sc, int, cudaStream_t s) {
-  // small blocks: the FP64 pipe bounds each SM, so the finer split balances the SMs
-  k_predict<<<nblk(sc.V, 64), 64, 0, s>>>(b, sc);
+  k_predict<<<nblk(sc.V), kBlock, 0, s>>>(b, sc);
 }
 void launch_positions(const DevBuf& b, const StepConst& sc, cudaStream_t s) {
   k_positions<<<nblk(sc.V), kBlock, 0, s>>>(b, sc);
@@ -1562,7 +1543,7 @@ void launch_elements(const DevBuf& b, const StepConst& sc, const ElemLaunch& el,
     case 7: k_elements32<128, 4><<<nb, 128, 0, s>>>(b, sc, eg); break;
     default: k_elements32<64, 8><<<nb, 64, 0, s>>>(b, sc, eg); break;
   }
-  if (totals) k_elem_totals<<<nblk(sc.F, kTotalsBlock), kTotalsBlock, 0, s>>>(b, sc);
+  if (totals) k_elem_totals<<<nblk(sc.F), kBlock, 0, s>>>(b, sc);
 }
 void launch_contact_force(const DevBuf& b, const StepConst& sc, int, cudaStream_t s) {
   uint32_t nb = nblk(sc.pairs_cap);
@@ -1576,15 +1557,14 @@ void launch_contact_force(const DevBuf& b, const StepConst& sc, int, cudaStream_
 // mode 2: an adaptive attempt (a_pred and the error estimate); else correct ? step corrector : evaluation
 void launch_gather_correct(const DevBuf& b, const StepConst& sc, int mode, bool correct, double* f_out, double* a_out,
                            cudaStream_t s) {
-  k_gather_correct<<<nblk(kGatherLanes * sc.V), kBlock, 0, s>>>(b, sc, mode == 2 ? 2 : (correct ? 1 : 0), f_out,
-                                                                a_out);
+  k_gather_correct<<<nblk(sc.V), kBlock, 0, s>>>(b, sc, mode == 2 ? 2 : (correct ? 1 : 0), f_out, a_out);
 }
 void launch_correct_adapt(const DevBuf& b, const StepConst& sc, cudaStream_t s) {
   k_correct_adapt<<<(sc.V + kBlock - 1) / kBlock, kBlock, 0, s>>>(b, sc);
 }
 
 void launch_volume_end_step(const DevBuf& b, const StepConst& sc, bool end_step, cudaStream_t s) {
-  k_volume_end<<<nblk(sc.F, kTotalsBlock), kTotalsBlock, 0, s>>>(b, sc, end_step ? 1 : 0);
+  k_volume_end<<<nblk(sc.F), kBlock, 0, s>>>(b, sc, end_step ? 1 : 0);
 }
 
 // ================================================================ no-alloc --
