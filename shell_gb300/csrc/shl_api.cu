@@ -492,7 +492,7 @@ shl_status create_common(shl_ctx* c, const std::vector<double>& pscale_orig, shl
   }
   ALLOC(b.qe, fp32 ? 1 : 3 * (size_t)S.n_slots_total);
   ALLOC(b.gather_ptr, V + 1);
-  ALLOC(b.gather_ent, S.gather_ent.size());
+  ALLOC(b.slot_pos, S.slot_pos.size());
   if (params->shell_cavity_contact) {
     ALLOC(b.node_face_ptr, V + 1);
     ALLOC(b.node_face, S.node_face.size());
@@ -600,7 +600,7 @@ shl_status create_common(shl_ctx* c, const std::vector<double>& pscale_orig, shl
   if (fp32 && (st = upload(c, b.face32, S.face32.data(), S.face32.size())) != SHL_OK) return fail(st);
   if ((st = upload(c, b.patch, S.patch.data(), S.patch.size())) != SHL_OK) return fail(st);
   if ((st = upload(c, b.gather_ptr, S.gather_ptr.data(), S.gather_ptr.size())) != SHL_OK) return fail(st);
-  if ((st = upload(c, b.gather_ent, S.gather_ent.data(), S.gather_ent.size())) != SHL_OK) return fail(st);
+  if ((st = upload(c, b.slot_pos, S.slot_pos.data(), S.slot_pos.size())) != SHL_OK) return fail(st);
   if (params->shell_cavity_contact) {
     if ((st = upload(c, b.node_face_ptr, S.node_face_ptr.data(), S.node_face_ptr.size())) != SHL_OK) return fail(st);
     if ((st = upload(c, b.node_face, S.node_face.data(), S.node_face.size())) != SHL_OK) return fail(st);

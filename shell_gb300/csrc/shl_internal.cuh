@@ -189,12 +189,15 @@ struct DevBuf {
   double* face;       // FF_COUNT * F
   double* pscale;     // F (internal order): factor on the step's pressure (per shell)
   int32_t* patch;     // patch_rows * F, slot-major
-  double* qe;         // 3 per element-force slot (GroupDesc::slot_base)
+  double* qe;         // 3 per element-force slot, in gather order (slot_pos)
   float* face32;      // F32_COUNT * F (FP32 element path)
-  float* qe32;        // 3 per element-force slot (FP32 element path)
+  float* qe32;        // 3 per element-force slot, in gather order (FP32 element path)
   float* up32;        // 3V, FP32 copy of u_pred (FP32 element path)
   float *uph, *upl;   // 3V, u_pred as a float pair hi + lo (the FP64 path's contractions)
-  uint32_t *gather_ptr, *gather_ent;
+  // element force shares are stored in gather order (node by node, ascending
+  // element-force slot): slot_pos maps a (face, slot) to its place, and node n's
+  // shares are qe[gather_ptr[n] .. gather_ptr[n + 1])
+  uint32_t *gather_ptr, *slot_pos;
   uint32_t *node_face_ptr, *node_face;  // V+1 / faces of each node (original ids; cavity contact only)
   uint32_t* tri;      // 3F original order
   uint32_t *perm;     // internal -> original

@@ -581,7 +581,8 @@ __device__ __forceinline__ ElemOut element_force(uint32_t i, int np_rt, uint32_t
     o.kg = o.area * invdet * (h0 * h1 - h2 * h2);
     o.km = o.area * invdet * 0.5 * (h0 * g1 + h1 * g0 - 2.0 * h2 * g2);
   }
-  double* qe = b.qe + 3 * (size_t)slot0;
+  // shares go to their places in gather order (scattered writes, contiguous reads in the gather)
+  const uint32_t* spos = b.slot_pos + slot0;
   if (DFQ) {
     const float* Bh = reinterpret_cast<const float*>(B + kMaxSlots * 6);
     const float* Bl = Bh + kMaxSlots * 6;
@@ -598,7 +599,7 @@ __device__ __forceinline__ ElemOut element_force(uint32_t i, int np_rt, uint32_t
         float th = 0.f, tl = 0.f;
 #pragma unroll
         for (int k = 0; k < 6; ++k) df_madd(th, tl, Bh[6 * s + k], Bl[6 * s + k], zh[k][c], zl[k][c]);
-        qe[3 * s + c] = df_value(th, tl);
+        b.qe[3 * (size_t)__ldg(&spos[s]) + c] = df_value(th, tl);
       }
     }
   } else {
@@ -613,9 +614,10 @@ __device__ __forceinline__ ElemOut element_force(uint32_t i, int np_rt, uint32_t
         for (int k = 1; k < 6; ++k) t = fma(B[6 * s + k], Z[k][c], t);
         q[c] = t;
       }
-      qe[3 * s] = q[0];
-      qe[3 * s + 1] = q[1];
-      qe[3 * s + 2] = q[2];
+      double* qe = b.qe + 3 * (size_t)__ldg(&spos[s]);
+      qe[0] = q[0];
+      qe[1] = q[1];
+      qe[2] = q[2];
     }
   }
   return o;
@@ -776,7 +778,7 @@ __device__ __forceinline__ ElemOut element_force32(uint32_t i, int np_rt, uint32
       Z[4][c] = c11b * Y11 + c22b * Y22 + c12b * Y12;
       Z[5][c] = c11c * Y11 + c22c * Y22 + c12c * Y12;
     }
-    float* qe = b.qe32 + 3 * (size_t)slot0;
+    const uint32_t* spos = b.slot_pos + slot0;
 #pragma unroll
     for (int s = 0; s < (NP > 0 ? NP : kMaxSlots); ++s) {
       if (NP == 0 && s >= np) break;
@@ -785,7 +787,7 @@ __device__ __forceinline__ ElemOut element_force32(uint32_t i, int np_rt, uint32
         float t = B[6 * s] * Z[0][c];
 #pragma unroll
         for (int k = 1; k < 6; ++k) t = fmaf(B[6 * s + k], Z[k][c], t);
-        qe[3 * s + c] = t;
+        b.qe32[3 * (size_t)__ldg(&spos[s]) + c] = t;
       }
     }
     ElemOut o;
@@ -1070,7 +1072,7 @@ __global__ void __launch_bounds__(kBlock) k_gather_correct(DevBuf b, StepConst s
       float s0 = 0.f, s1 = 0.f, s2 = 0.f;
 #pragma unroll 4
       for (uint32_t k = g0; k < g1; ++k) {
-        const float* q = b.qe32 + 3 * (size_t)__ldg(&b.gather_ent[k]);
+        const float* q = b.qe32 + 3 * (size_t)k;
         s0 += q[0];
         s1 += q[1];
         s2 += q[2];
@@ -1081,7 +1083,7 @@ __global__ void __launch_bounds__(kBlock) k_gather_correct(DevBuf b, StepConst s
     } else {
 #pragma unroll 4
       for (uint32_t k = g0; k < g1; ++k) {
-        const double* q = b.qe + 3 * (size_t)__ldg(&b.gather_ent[k]);
+        const double* q = b.qe + 3 * (size_t)k;
         f[0] -= q[0];
         f[1] -= q[1];
         f[2] -= q[2];
@@ -1631,7 +1633,7 @@ __global__ void __launch_bounds__(kBlock) k_gather_noalloc(DevBuf b, StepConst s
   double f[3] = {0.0, 0.0, 0.0};
   const uint32_t g0 = b.gather_ptr[n], g1 = b.gather_ptr[n + 1];
   for (uint32_t k = g0; k < g1; ++k) {
-    const double* q = b.qe + 3 * (size_t)__ldg(&b.gather_ent[k]);
+    const double* q = b.qe + 3 * (size_t)k;
     f[0] -= q[0];
     f[1] -= q[1];
     f[2] -= q[2];

@@ -220,6 +220,8 @@ void build_node_lists(Setup& S) {
         S.gather_ent[cur[nd]++] = g.slot_base + (i - g.first) * (uint32_t)g.n_slots + (uint32_t)s;
         if (s < 3) S.node_face[cur_f[nd]++] = S.perm[i];
       }
+  S.slot_pos.assign(S.n_slots_total, 0);
+  for (uint32_t k = 0; k < (uint32_t)S.gather_ent.size(); ++k) S.slot_pos[S.gather_ent[k]] = k;
 }
 
 }  // namespace

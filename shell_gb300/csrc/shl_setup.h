@@ -80,6 +80,7 @@ struct Setup {
   std::vector<double> Minv, C;     // 3V node-major
   std::vector<uint32_t> gather_ptr;  // V+1
   std::vector<uint32_t> gather_ent;  // element-force slot (PatchGroup::slot_base), ascending per node
+  std::vector<uint32_t> slot_pos;    // per element-force slot: its position k in gather_ent (the inverse)
   std::vector<uint32_t> node_face_ptr;  // V+1: faces of which each node is a vertex
   std::vector<uint32_t> node_face;      // original face ids, ascending internal order
   std::vector<uint32_t> close_ptr;   // F+1 (original ids)
