@@ -883,73 +883,6 @@ __global__ void __launch_bounds__(BS, MINB) k_elements(DevBuf b, StepConst sc, E
   b.ebend[e] = o.ebend / o.area;
 }
 
-// The same per-face arithmetic on a resident grid (a few blocks per SM): each
-// warp fetches chunks of kElemChunk faces of one patch group from a device
-// counter until all are done, so the SMs finish together instead of in
-// block-sized waves.  The last warp to finish resets the counters.
-template <int BS, int MINB, bool DFG>
-__global__ void __launch_bounds__(BS, MINB) k_elements_dyn(DevBuf b, StepConst sc, ElemGroups eg) {
-  Ctl* ctl = b.ctl;
-  if (inactive(ctl)) return;
-  // every group's basis table, each followed by its float pairs (as k_elements stages one)
-  __shared__ double sB[kMaxGroups][kMaxSlots * 6 * 2];
-  for (int g = 0; g < eg.n; ++g) {
-    float* sBh = reinterpret_cast<float*>(sB[g] + kMaxSlots * 6);
-    float* sBl = sBh + kMaxSlots * 6;
-    for (int k = threadIdx.x; k < eg.g[g].n_slots * 6; k += blockDim.x) {
-      const double w = eg.basis[eg.g[g].basis_off + k];
-      sB[g][k] = w;
-      df_split(w, sBh[k], sBl[k]);
-    }
-  }
-  __syncthreads();
-  uint32_t n_chunks = 0;
-  for (int g = 0; g < eg.n; ++g) n_chunks += (eg.g[g].count + kElemChunk - 1) / kElemChunk;
-  const int lane = threadIdx.x & 31;
-  const double pressure = ctl->pressure, vol_p = ctl->volume_pressure;
-  for (;;) {
-    uint32_t c = 0;
-    if (lane == 0) c = atomicAdd(&ctl->cnt[8], 1u);
-    c = __shfl_sync(0xffffffffu, c, 0);
-    if (c >= n_chunks) break;
-    int g = 0;
-    uint32_t c0 = 0;
-    for (;;) {
-      const uint32_t nc = (eg.g[g].count + kElemChunk - 1) / kElemChunk;
-      if (c < c0 + nc || g + 1 >= eg.n) break;
-      c0 += nc;
-      ++g;
-    }
-    const GroupDesc gd = eg.g[g];
-    const uint32_t li = (c - c0) * kElemChunk + (uint32_t)lane;
-    if (li >= gd.count) continue;
-    const uint32_t i = gd.first + li;
-    const uint32_t slot0 = gd.slot_base + li * (uint32_t)gd.n_slots;
-    const double pr = pressure * __ldg(&b.pscale[i]);
-    const double* B = sB[g];
-    ElemOut o;
-    if (gd.n_slots == 12)
-      o = element_force<12, DFG, false>(i, 12, slot0, B, b, sc, pr, vol_p);
-    else if (gd.n_slots == 11)
-      o = element_force<11, DFG, false>(i, 11, slot0, B, b, sc, pr, vol_p);
-    else
-      o = element_force<0, DFG, false>(i, gd.n_slots, slot0, B, b, sc, pr, vol_p);
-    const uint32_t e = __ldg(&b.perm[i]);
-    b.area[e] = o.area;
-    b.kG[e] = o.kg / o.area;
-    b.kM[e] = o.km / o.area;
-    b.etens[e] = o.etens / o.area;
-    b.ebend[e] = o.ebend / o.area;
-  }
-  if (lane == 0) {
-    const uint32_t warps = gridDim.x * (BS / 32);
-    if (atomicAdd(&ctl->cnt[9], 1u) == warps - 1) {
-      ctl->cnt[8] = 0;
-      ctl->cnt[9] = 0;
-    }
-  }
-}
-
 // totals of the per-face measurements (original face order, fixed-order sums):
 // E_tens, E_bend, kGauss, kMean and the area (ShellSystem.C:1285-1300, 2760-2786)
 __global__ void __launch_bounds__(kBlock) k_elem_totals(DevBuf b, StepConst sc) {
@@ -1596,7 +1529,6 @@ void launch_positions(const DevBuf& b, const StepConst& sc, cudaStream_t s) {
 const ElemVariant kElemVariants[kNumElemVariants] = {
     {256, 0, "fp64 256x1"},        {256, 1, "fp64 256x1 pair-G"}, {128, 1, "fp64 128x3 pair-G"},
     {64, 1, "fp64 64x5 pair-G"},   {64, 1, "fp64 64x6 pair-G"},   {64, 0, "fp64 64x5"},
-    {64, 1, "fp64 64x6 pair-G dyn", 6}, {128, 1, "fp64 128x3 pair-G dyn", 3},
     {256, 0, "fp32 256x2"},        {128, 0, "fp32 128x4"},        {64, 0, "fp32 64x8"}};
 
 void launch_elements(const DevBuf& b, const StepConst& sc, const ElemLaunch& el, cudaStream_t s, bool totals) {
@@ -1609,10 +1541,8 @@ void launch_elements(const DevBuf& b, const StepConst& sc, const ElemLaunch& el,
     case 3: k_elements<64, 5, true, false><<<nb, 64, 0, s>>>(b, sc, eg); break;
     case 4: k_elements<64, 6, true, false><<<nb, 64, 0, s>>>(b, sc, eg); break;
     case 5: k_elements<64, 5, false, false><<<nb, 64, 0, s>>>(b, sc, eg); break;
-    case 6: k_elements_dyn<64, 6, true><<<nb, 64, 0, s>>>(b, sc, eg); break;
-    case 7: k_elements_dyn<128, 3, true><<<nb, 128, 0, s>>>(b, sc, eg); break;
-    case 8: k_elements32<256, 2><<<nb, 256, 0, s>>>(b, sc, eg); break;
-    case 9: k_elements32<128, 4><<<nb, 128, 0, s>>>(b, sc, eg); break;
+    case 6: k_elements32<256, 2><<<nb, 256, 0, s>>>(b, sc, eg); break;
+    case 7: k_elements32<128, 4><<<nb, 128, 0, s>>>(b, sc, eg); break;
     default: k_elements32<64, 8><<<nb, 64, 0, s>>>(b, sc, eg); break;
   }
   if (totals) k_elem_totals<<<nblk(sc.F), kBlock, 0, s>>>(b, sc);
