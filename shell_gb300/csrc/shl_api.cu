@@ -489,6 +489,8 @@ shl_status create_common(shl_ctx* c, const std::vector<double>& pscale_orig, shl
     ALLOC(b.qe32, 3 * (size_t)S.n_slots_total);
     ALLOC(b.up32, nd);
     ALLOC(b.face32, (size_t)F32_COUNT * F);
+  } else {
+    ALLOC(b.face_df, (size_t)2 * F32_COUNT * F);
   }
   ALLOC(b.qe, fp32 ? 1 : 3 * (size_t)S.n_slots_total);
   ALLOC(b.gather_ptr, V + 1);
@@ -598,6 +600,7 @@ shl_status create_common(shl_ctx* c, const std::vector<double>& pscale_orig, shl
   if ((st = upload(c, b.C, S.C.data(), nd)) != SHL_OK) return fail(st);
   if ((st = upload(c, b.face, S.face.data(), S.face.size())) != SHL_OK) return fail(st);
   if (fp32 && (st = upload(c, b.face32, S.face32.data(), S.face32.size())) != SHL_OK) return fail(st);
+  if (!fp32 && (st = upload(c, b.face_df, S.face_df.data(), S.face_df.size())) != SHL_OK) return fail(st);
   if ((st = upload(c, b.patch, S.patch.data(), S.patch.size())) != SHL_OK) return fail(st);
   if ((st = upload(c, b.gather_ptr, S.gather_ptr.data(), S.gather_ptr.size())) != SHL_OK) return fail(st);
   if ((st = upload(c, b.slot_pos, S.slot_pos.data(), S.slot_pos.size())) != SHL_OK) return fail(st);

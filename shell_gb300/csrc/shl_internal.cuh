@@ -57,15 +57,15 @@ struct ElemGroups {
 };
 
 // An element-kernel variant: threads per block, arithmetic (0 FP64, 1 the
-// displacement contraction as float pairs; FP32-path variants use 0) and a
-// name for reports.
+// displacement contraction as float pairs, 2 double-float throughout;
+// FP32-path variants use 0) and a name for reports.
 struct ElemVariant {
   int block;
   int pairs;
   const char* name;
 };
 constexpr int kNumElemVariants = SHL_ELEMENT_VARIANTS;
-constexpr int kFirstFp32Variant = 6;
+constexpr int kFirstFp32Variant = 9;
 extern const ElemVariant kElemVariants[kNumElemVariants];
 
 // The element launch of a context: variant, grid and patch-group block ranges for its block size.
@@ -191,6 +191,7 @@ struct DevBuf {
   int32_t* patch;     // patch_rows * F, slot-major
   double* qe;         // 3 per element-force slot, in gather order (slot_pos)
   float* face32;      // F32_COUNT * F (FP32 element path)
+  float* face_df;     // 2 * F32_COUNT * F: the same constants as float pairs (double-float FP64 path)
   float* qe32;        // 3 per element-force slot, in gather order (FP32 element path)
   float* up32;        // 3V, FP32 copy of u_pred (FP32 element path)
   float *uph, *upl;   // 3V, u_pred as a float pair hi + lo (the FP64 path's contractions)

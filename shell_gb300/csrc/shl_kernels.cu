@@ -24,6 +24,7 @@
 
 #include "shl_geom.h"
 #include "shl_internal.cuh"
+#include "shl_df.cuh"
 
 namespace shl {
 
@@ -810,6 +811,246 @@ __device__ __forceinline__ ElemOut element_force32(uint32_t i, int np_rt, uint32
 // context's own mesh and keeps the fastest (shl_api.cu, tune_elements).  The
 // per-face arithmetic of one path does not depend on the launch shape.  The
 // totals of the per-face measurements are summed by k_elem_totals.
+// FP64-class element force in double-float arithmetic on the FP32 pipe: the
+// relative-displacement formulation of element_force32 with every quantity a
+// float pair (about 48 significant bits), the constants from face_df (the
+// same balanced-frame values as face32, kept to 48 bits), the displacement
+// derivatives from the hi/lo copy of u_pred.  No step subtracts nearly equal
+// quantities, so the forces carry a relative error of a few 1e-14 -- the
+// class of the FP64 path -- at FP32 instruction rates.  Shares are written as
+// FP64; the measurements are returned as FP64.
+template <int NP>
+__device__ __forceinline__ ElemOut element_force_df(uint32_t i, int np_rt, uint32_t slot0,
+                                                    const double* __restrict__ B, const DevBuf& b,
+                                                    const StepConst& sc, double pressure_d, double vol_p_d) {
+  const uint32_t F = sc.F;
+  const int np = NP > 0 ? NP : np_rt;
+  const float* Bh = reinterpret_cast<const float*>(B + kMaxSlots * 6);
+  const float* Bl = Bh + kMaxSlots * 6;
+  df2 G[6][3];
+  {
+    float gh[6][3], gl[6][3];
+#pragma unroll
+    for (int k = 0; k < 6; ++k)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) gh[k][c] = gl[k][c] = 0.f;
+#pragma unroll
+    for (int s = 0; s < (NP > 0 ? NP : kMaxSlots); ++s) {
+      if (NP == 0 && s >= np) break;
+      const int nd = __ldg(&b.patch[(size_t)s * F + i]);
+      float uh[3], ul[3];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        uh[c] = __ldg(&b.uph[3 * (size_t)nd + c]);
+        ul[c] = __ldg(&b.upl[3 * (size_t)nd + c]);
+      }
+#pragma unroll
+      for (int k = 0; k < 6; ++k) {
+        const float wh = Bh[6 * s + k], wl = Bl[6 * s + k];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) df_madd(gh[k][c], gl[k][c], wh, wl, uh[c], ul[c]);
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < 6; ++k)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) df_quick_two_sum(gh[k][c], gl[k][c], G[k][c].h, G[k][c].l);
+  }
+  const float* fd = b.face_df;
+  auto FC = [&](int fld) -> df2 {
+    return {__ldg(&fd[(size_t)fld * F + i]), __ldg(&fd[(size_t)(F32_COUNT + fld) * F + i])};
+  };
+  const df2 R00 = FC(F32_R00), R01 = FC(F32_R01), R10 = FC(F32_R10), R11 = FC(F32_R11);
+  const df2 JxW = FC(F32_JXW);
+  const df2 c11a = R00 * R00, c11b = R10 * R10, c11c = 2.f * (R00 * R10);
+  const df2 c22a = R01 * R01, c22b = R11 * R11, c22c = 2.f * (R01 * R11);
+  const df2 c12a = R00 * R01, c12b = R10 * R11, c12c = R01 * R10 + R00 * R11;
+  df2 A1[3] = {FC(F32_A10), FC(F32_A11), FC(F32_A12)};
+  df2 A2[3] = {FC(F32_A20), FC(F32_A21), FC(F32_A22)};
+  df2 du1[3], du2[3], d1[3], d2[3], d3[3], xq[3];
+  {
+    const df2 X0[3] = {FC(F32_X0), FC(F32_X1), FC(F32_X2)};
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      du1[c] = R00 * G[1][c] + R10 * G[2][c];
+      du2[c] = R01 * G[1][c] + R11 * G[2][c];
+      d1[c] = c11a * G[3][c] + c11b * G[4][c] + c11c * G[5][c];
+      d2[c] = c22a * G[3][c] + c22b * G[4][c] + c22c * G[5][c];
+      d3[c] = c12a * G[3][c] + c12b * G[4][c] + c12c * G[5][c];
+      xq[c] = X0[c] + G[0][c];
+    }
+  }
+  // membrane strains (Voigt, shear doubled), without metric differences
+  const df2 al0 = dot3df(A1, du1) + 0.5f * dot3df(du1, du1);
+  const df2 al1 = dot3df(A2, du2) + 0.5f * dot3df(du2, du2);
+  const df2 al2 = dot3df(A1, du2) + dot3df(du1, A2) + dot3df(du1, du2);
+  // deformed normal from the change of a1 x a2
+  df2 Dn[3], t1[3], t2[3], t3[3];
+  cross3df(A1, du2, t1);
+  cross3df(du1, A2, t2);
+  cross3df(du1, du2, t3);
+#pragma unroll
+  for (int c = 0; c < 3; ++c) Dn[c] = t1[c] + t2[c] + t3[c];
+  const df2 N0[3] = {FC(F32_N0), FC(F32_N1), FC(F32_N2)};
+  const df2 L0 = FC(F32_L0);
+  const df2 dL2 = 2.f * (L0 * dot3df(N0, Dn)) + dot3df(Dn, Dn);  // |a1 x a2|^2 - L0^2
+  const df2 jac = df_sqrt(L0 * L0 + dL2);
+  const df2 invjac = df_recip(jac);
+  const df2 s_n = -(dL2 * df_recip((L0 + jac) * jac));  // L0/jac - 1
+  df2 a3[3], dn[3], a1[3], a2[3], v1[3], v2[3], v3[3];
+  const df2 D1[3] = {FC(F32_D10), FC(F32_D11), FC(F32_D12)};
+  const df2 D2[3] = {FC(F32_D20), FC(F32_D21), FC(F32_D22)};
+  const df2 D3[3] = {FC(F32_D30), FC(F32_D31), FC(F32_D32)};
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    dn[c] = Dn[c] * invjac + N0[c] * s_n;
+    a3[c] = N0[c] + dn[c];
+    a1[c] = A1[c] + du1[c];
+    a2[c] = A2[c] + du2[c];
+    v1[c] = D1[c] + d1[c];
+    v2[c] = D2[c] + d2[c];
+    v3[c] = D3[c] + d3[c];
+  }
+  // bending strains beta_k = -(D_k.dn + d_k.a3), shear doubled
+  const df2 be0 = -(dot3df(D1, dn) + dot3df(d1, a3));
+  const df2 be1 = -(dot3df(D2, dn) + dot3df(d2, a3));
+  const df2 be2 = -2.f * (dot3df(D3, dn) + dot3df(d3, a3));
+  const df2 H00 = FC(F32_H00), H01 = FC(F32_H01), H02 = FC(F32_H02), H11 = FC(F32_H11), H12 = FC(F32_H12),
+            H22 = FC(F32_H22);
+  const float scale = (float)sc.internal_scale;  // 1, or 0 for the pressure-only force
+  const df2 K = scale * FC(F32_K), Dm = scale * FC(F32_D);
+  const df2 n0 = K * (H00 * al0 + H01 * al1 + H02 * al2);
+  const df2 n1 = K * (H01 * al0 + H11 * al1 + H12 * al2);
+  const df2 n2 = K * (H02 * al0 + H12 * al1 + H22 * al2);
+  const df2 m0 = Dm * (H00 * be0 + H01 * be1 + H02 * be2);
+  const df2 m1 = Dm * (H01 * be0 + H11 * be1 + H12 * be2);
+  const df2 m2 = Dm * (H02 * be0 + H12 * be1 + H22 * be2);
+  const df2 h0 = dot3df(v1, a3), h1 = dot3df(v2, a3), h2 = dot3df(v3, a3);
+  df2 M[3], a2xa3[3], a3xa1[3], Mxa2[3], a1xM[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) M[c] = m0 * v1[c] + m1 * v2[c] + 2.f * (m2 * v3[c]);
+  const df2 sm = m0 * h0 + m1 * h1 + 2.f * (m2 * h2);
+  cross3df(a2, a3, a2xa3);
+  cross3df(a3, a1, a3xa1);
+  cross3df(M, a2, Mxa2);
+  cross3df(a1, M, a1xM);
+  df2 pv[3] = {dfv(0.f), dfv(0.f), dfv(0.f)};
+  if (pressure_d != 0.0) {
+    const df2 pressure = df_from_double(pressure_d);
+    switch (sc.pressure_base) {
+      case SHL_CS_LOCAL: pv[0] = a3[0]; pv[1] = a3[1]; pv[2] = a3[2]; break;
+      case SHL_CS_CARTESIAN: pv[sc.pressure_dir] = dfv(1.f); break;
+      case SHL_CS_CYLINDRICAL:
+        if (sc.pressure_dir == 0) {
+          pv[0] = dfv(1.f);
+        } else {
+          const df2 r2 = xq[1] * xq[1] + xq[2] * xq[2];
+          if (r2.h > 0.f) {
+            const df2 inv_r = df_recip(df_sqrt(r2));
+            pv[1] = inv_r * xq[1];
+            pv[2] = inv_r * xq[2];
+          }
+        }
+        break;
+      case SHL_CS_SPHERICAL: {
+        const df2 r2 = dot3df(xq, xq);
+        if (r2.h > 0.f) {
+          const df2 ir = df_recip(df_sqrt(r2));
+          pv[0] = xq[0] * ir; pv[1] = xq[1] * ir; pv[2] = xq[2] * ir;
+        }
+        break;
+      }
+      default: break;
+    }
+    pv[0] = pv[0] * pressure; pv[1] = pv[1] * pressure; pv[2] = pv[2] * pressure;
+  }
+  if (vol_p_d != 0.0) {
+    const df2 vol_p = df_from_double(vol_p_d);
+    pv[0] += a3[0] * vol_p; pv[1] += a3[1] * vol_p; pv[2] += a3[2] * vol_p;
+  }
+  df2 Z[6][3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    const df2 Y1 = JxW * (n0 * a1[c] + n2 * a2[c] + invjac * (Mxa2[c] + sm * a2xa3[c]));
+    const df2 Y2 = JxW * (n1 * a2[c] + n2 * a1[c] + invjac * (a1xM[c] + sm * a3xa1[c]));
+    const df2 Y11 = -(JxW * m0 * a3[c]);
+    const df2 Y22 = -(JxW * m1 * a3[c]);
+    const df2 Y12 = -2.f * (JxW * m2 * a3[c]);
+    Z[0][c] = -(JxW * pv[c]);
+    Z[1][c] = R00 * Y1 + R01 * Y2;
+    Z[2][c] = R10 * Y1 + R11 * Y2;
+    Z[3][c] = c11a * Y11 + c22a * Y22 + c12a * Y12;
+    Z[4][c] = c11b * Y11 + c22b * Y22 + c12b * Y12;
+    Z[5][c] = c11c * Y11 + c22c * Y22 + c12c * Y12;
+  }
+  ElemOut o;
+  {
+    const df2 area = 0.5f * jac;
+    const df2 g0 = FC(F32_G0) + 2.f * al0, g1 = FC(F32_G1) + 2.f * al1, g2 = FC(F32_G2) + al2;
+    const df2 w_invdet = area * df_recip(g0 * g1 - g2 * g2);
+    o.etens = df_to_double(0.5f * (JxW * (n0 * al0 + n1 * al1 + n2 * al2)));
+    o.ebend = df_to_double(0.5f * (JxW * (m0 * be0 + m1 * be1 + m2 * be2)));
+    o.area = df_to_double(area);
+    o.kg = df_to_double(w_invdet * (h0 * h1 - h2 * h2));
+    o.km = df_to_double(w_invdet * (0.5f * (h0 * g1 + h1 * g0 - 2.f * (h2 * g2))));
+  }
+  const uint32_t* spos = b.slot_pos + slot0;
+#pragma unroll
+  for (int s = 0; s < (NP > 0 ? NP : kMaxSlots); ++s) {
+    if (NP == 0 && s >= np) break;
+    const df2 Bs[6] = {{Bh[6 * s], Bl[6 * s]},         {Bh[6 * s + 1], Bl[6 * s + 1]},
+                       {Bh[6 * s + 2], Bl[6 * s + 2]}, {Bh[6 * s + 3], Bl[6 * s + 3]},
+                       {Bh[6 * s + 4], Bl[6 * s + 4]}, {Bh[6 * s + 5], Bl[6 * s + 5]}};
+    double* qe = b.qe + 3 * (size_t)__ldg(&spos[s]);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      df2 t = Bs[0] * Z[0][c];
+#pragma unroll
+      for (int k = 1; k < 6; ++k) t += Bs[k] * Z[k][c];
+      qe[c] = df_to_double(t);
+    }
+  }
+  return o;
+}
+
+// the element kernel of the double-float path (block shapes as k_elements)
+template <int BS, int MINB>
+__global__ void __launch_bounds__(BS, MINB) k_elements_df(DevBuf b, StepConst sc, ElemGroups eg) {
+  Ctl* ctl = b.ctl;
+  if (inactive(ctl)) return;
+  __shared__ double sB[kMaxSlots * 6 * 2];
+  int g = 0;
+  while (g + 1 < eg.n && blockIdx.x >= eg.g[g + 1].block_start) ++g;
+  const GroupDesc gd = eg.g[g];
+  float* sBh = reinterpret_cast<float*>(sB + kMaxSlots * 6);
+  float* sBl = sBh + kMaxSlots * 6;
+  for (int k = threadIdx.x; k < gd.n_slots * 6; k += blockDim.x) {
+    const double w = eg.basis[gd.basis_off + k];
+    sB[k] = w;
+    df_split(w, sBh[k], sBl[k]);
+  }
+  __syncthreads();
+  const uint32_t li = (blockIdx.x - gd.block_start) * blockDim.x + threadIdx.x;
+  if (li >= gd.count) return;
+  const double pressure = ctl->pressure, vol_p = ctl->volume_pressure;
+  const uint32_t i = gd.first + li;
+  const uint32_t slot0 = gd.slot_base + li * (uint32_t)gd.n_slots;
+  const double pr = pressure * __ldg(&b.pscale[i]);
+  ElemOut o;
+  if (gd.n_slots == 12)
+    o = element_force_df<12>(i, 12, slot0, sB, b, sc, pr, vol_p);
+  else if (gd.n_slots == 11)
+    o = element_force_df<11>(i, 11, slot0, sB, b, sc, pr, vol_p);
+  else
+    o = element_force_df<0>(i, gd.n_slots, slot0, sB, b, sc, pr, vol_p);
+  const uint32_t e = __ldg(&b.perm[i]);
+  b.area[e] = o.area;
+  b.kG[e] = o.kg / o.area;
+  b.kM[e] = o.km / o.area;
+  b.etens[e] = o.etens / o.area;
+  b.ebend[e] = o.ebend / o.area;
+}
+
 template <int BS, int MINB>
 __global__ void __launch_bounds__(BS, MINB) k_elements32(DevBuf b, StepConst sc, ElemGroups eg) {
   Ctl* ctl = b.ctl;
@@ -1529,6 +1770,7 @@ void launch_positions(const DevBuf& b, const StepConst& sc, cudaStream_t s) {
 const ElemVariant kElemVariants[kNumElemVariants] = {
     {256, 0, "fp64 256x1"},        {256, 1, "fp64 256x1 pair-G"}, {128, 1, "fp64 128x3 pair-G"},
     {64, 1, "fp64 64x5 pair-G"},   {64, 1, "fp64 64x6 pair-G"},   {64, 0, "fp64 64x5"},
+    {256, 2, "fp64 256x1 df"},     {128, 2, "fp64 128x3 df"},     {64, 2, "fp64 64x6 df"},
     {256, 0, "fp32 256x2"},        {128, 0, "fp32 128x4"},        {64, 0, "fp32 64x8"}};
 
 void launch_elements(const DevBuf& b, const StepConst& sc, const ElemLaunch& el, cudaStream_t s, bool totals) {
@@ -1541,8 +1783,11 @@ void launch_elements(const DevBuf& b, const StepConst& sc, const ElemLaunch& el,
     case 3: k_elements<64, 5, true, false><<<nb, 64, 0, s>>>(b, sc, eg); break;
     case 4: k_elements<64, 6, true, false><<<nb, 64, 0, s>>>(b, sc, eg); break;
     case 5: k_elements<64, 5, false, false><<<nb, 64, 0, s>>>(b, sc, eg); break;
-    case 6: k_elements32<256, 2><<<nb, 256, 0, s>>>(b, sc, eg); break;
-    case 7: k_elements32<128, 4><<<nb, 128, 0, s>>>(b, sc, eg); break;
+    case 6: k_elements_df<256, 1><<<nb, 256, 0, s>>>(b, sc, eg); break;
+    case 7: k_elements_df<128, 3><<<nb, 128, 0, s>>>(b, sc, eg); break;
+    case 8: k_elements_df<64, 6><<<nb, 64, 0, s>>>(b, sc, eg); break;
+    case 9: k_elements32<256, 2><<<nb, 256, 0, s>>>(b, sc, eg); break;
+    case 10: k_elements32<128, 4><<<nb, 128, 0, s>>>(b, sc, eg); break;
     default: k_elements32<64, 8><<<nb, 64, 0, s>>>(b, sc, eg); break;
   }
   if (totals) k_elem_totals<<<nblk(sc.F), kBlock, 0, s>>>(b, sc);

@@ -482,9 +482,15 @@ bool build_setup(const shl_mesh& mesh, const shl_params& prm, Setup& S, std::str
   }
   // FP32 constants of the relative-displacement element path
   S.face32.assign((size_t)F32_COUNT * F, 0.0f);
+  S.face_df.assign((size_t)2 * F32_COUNT * F, 0.0f);
   for (uint32_t i = 0; i < F; ++i) {
     auto get = [&](int fld) { return face_bal[(size_t)fld * F + i]; };
-    auto put32 = [&](int fld, double x) { S.face32[(size_t)fld * F + i] = (float)x; };
+    auto put32 = [&](int fld, double x) {
+      const float h = (float)x;
+      S.face32[(size_t)fld * F + i] = h;
+      S.face_df[(size_t)fld * F + i] = h;
+      S.face_df[(size_t)(F32_COUNT + fld) * F + i] = (float)(x - (double)h);
+    };
     const int map64[][2] = {{F32_R00, FF_R00}, {F32_R01, FF_R01}, {F32_R10, FF_R10}, {F32_R11, FF_R11},
                             {F32_JXW, FF_JXW}, {F32_X0, FF_X0}, {F32_X1, FF_X1}, {F32_X2, FF_X2},
                             {F32_A10, FF_A10}, {F32_A11, FF_A11}, {F32_A12, FF_A12}, {F32_A20, FF_A20},
@@ -638,6 +644,7 @@ bool merge_setups(std::vector<Setup>& shells, Setup& M, std::vector<uint32_t>& n
   M.patch.assign((size_t)M.patch_rows * F, -1);
   M.face.assign((size_t)FF_COUNT * F, 0.0);
   M.face32.assign((size_t)F32_COUNT * F, 0.0f);
+  M.face_df.assign((size_t)2 * F32_COUNT * F, 0.0f);
   for (uint32_t i = 0; i < F; ++i) {
     const uint32_t k = src[i].first, si = src[i].second;
     const Setup& S = shells[k];
@@ -647,6 +654,7 @@ bool merge_setups(std::vector<Setup>& shells, Setup& M, std::vector<uint32_t>& n
     }
     for (int fld = 0; fld < FF_COUNT; ++fld) M.face[(size_t)fld * F + i] = S.face[(size_t)fld * S.F + si];
     for (int fld = 0; fld < F32_COUNT; ++fld) M.face32[(size_t)fld * F + i] = S.face32[(size_t)fld * S.F + si];
+    for (int fld = 0; fld < 2 * F32_COUNT; ++fld) M.face_df[(size_t)fld * F + i] = S.face_df[(size_t)fld * S.F + si];
   }
   build_node_lists(M);
   M.close_ptr.assign(F + 1, 0);

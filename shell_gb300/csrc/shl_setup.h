@@ -77,6 +77,7 @@ struct Setup {
   std::vector<int32_t> patch;      // [slot * F + internal face], -1 for unused slots
   std::vector<double> face;        // [field * F + internal face]
   std::vector<float> face32;       // [FaceField32 * F + internal face]
+  std::vector<float> face_df;      // the same constants as float pairs: hi [fld * F + i], lo [(F32_COUNT + fld) * F + i]
   std::vector<double> Minv, C;     // 3V node-major
   std::vector<uint32_t> gather_ptr;  // V+1
   std::vector<uint32_t> gather_ent;  // element-force slot (PatchGroup::slot_base), ascending per node
