@@ -834,9 +834,9 @@ __device__ __forceinline__ ElemOut element_force_df(uint32_t i, int np_rt, uint3
     for (int k = 0; k < 6; ++k)
 #pragma unroll
       for (int c = 0; c < 3; ++c) gh[k][c] = gl[k][c] = 0.f;
-#pragma unroll
-    for (int s = 0; s < (NP > 0 ? NP : kMaxSlots); ++s) {
-      if (NP == 0 && s >= np) break;
+    // slots in a rolled loop: the unrolled double-float code would not fit the instruction cache
+#pragma unroll 1
+    for (int s = 0; s < np; ++s) {
       const int nd = __ldg(&b.patch[(size_t)s * F + i]);
       float uh[3], ul[3];
 #pragma unroll
@@ -995,9 +995,8 @@ __device__ __forceinline__ ElemOut element_force_df(uint32_t i, int np_rt, uint3
     o.km = df_to_double(w_invdet * (0.5f * (h0 * g1 + h1 * g0 - 2.f * (h2 * g2))));
   }
   const uint32_t* spos = b.slot_pos + slot0;
-#pragma unroll
-  for (int s = 0; s < (NP > 0 ? NP : kMaxSlots); ++s) {
-    if (NP == 0 && s >= np) break;
+#pragma unroll 1
+  for (int s = 0; s < np; ++s) {
     const df2 Bs[6] = {{Bh[6 * s], Bl[6 * s]},         {Bh[6 * s + 1], Bl[6 * s + 1]},
                        {Bh[6 * s + 2], Bl[6 * s + 2]}, {Bh[6 * s + 3], Bl[6 * s + 3]},
                        {Bh[6 * s + 4], Bl[6 * s + 4]}, {Bh[6 * s + 5], Bl[6 * s + 5]}};

@@ -3,7 +3,7 @@ kernel profilers (the CUDA graphs of shl_step hold conditional nodes, whose
 kernels profilers cannot replay one by one).
 
 python -m shell_gb300.profile [--level 6] [--warmup 3] [--steps 5] [--squashed] [--contact linear|smooth|none]
-    [--phases]
+    [--phases] [--variant V]
 
 --squashed starts from the double-layer state of the contact-mode benchmark
 instead of the imperfect sphere; --phases also prints shl_profile_step's
@@ -27,10 +27,13 @@ def main(argv=None):
     ap.add_argument("--squashed", action="store_true")
     ap.add_argument("--contact", default="linear", choices=["linear", "smooth", "none"])
     ap.add_argument("--phases", action="store_true")
+    ap.add_argument("--variant", type=int, default=-1, help="element-kernel variant (-1: the autotuned one)")
     a = ap.parse_args(argv)
     mode = {"linear": L.CONTACT_LINEAR, "smooth": L.CONTACT_SMOOTH, "none": L.CONTACT_NONE}[a.contact]
     X, T, p, u0 = workload(L, a.level, contact=mode)
     g = L.Shell(X, T, p)
+    if a.variant >= 0:
+        g.set_element_variant(a.variant)
     if a.squashed:
         u = squashed_state(X)
         z = np.zeros_like(u)
