@@ -411,6 +411,9 @@ namespace {
 // does not depend on its shape).
 constexpr int kFp64Pairs = 1;
 
+// step constants that follow the FP64 variant: its share format
+void apply_variant(shl_ctx* c) { c->sc.qe_df = kElemVariants[c->var64].pairs == 2 ? 1 : 0; }
+
 // first FP64 variant of the fixed arithmetic (the FP64 launch of FP32 contexts)
 int default_var64() {
   for (int v = 0; v < kFirstFp32Variant; ++v)
@@ -454,6 +457,7 @@ shl_status tune_elements(shl_ctx* c) {
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (fp32) c->var32 = best_v; else c->var64 = best_v;
+  apply_variant(c);
   return check_launch("element tuning");
 }
 
@@ -699,6 +703,7 @@ shl_status create_common(shl_ctx* c, const std::vector<double>& pscale_orig, shl
   sc.contact = contact ? 1 : 0;
   sc.smooth = smooth ? 1 : 0;
   c->var64 = default_var64();
+  apply_variant(c);
   for (int k = 0; k < 13; ++k) sc.stab_off[k] = stab_off[k];
   sc.friction = (contact && (p.mu_s != 0 || p.mu_d != 0)) ? 1 : 0;
   sc.pressure_base = p.pressure_base;
@@ -1708,6 +1713,7 @@ shl_status shl_set_element_variant(shl_ctx* c, int variant) {
     return SHL_ERR_ARG;
   }
   if (c->sc.fp32) c->var32 = variant; else c->var64 = variant;
+  apply_variant(c);
   if (c->graph) cudaGraphExecDestroy(c->graph);
   if (c->graph1) cudaGraphExecDestroy(c->graph1);
   c->graph = c->graph1 = nullptr;

@@ -150,6 +150,7 @@ struct StepConst {
   uint32_t n_cells_cap, entries_cap, pairs_cap, csr_cap, cand_cap;
   int32_t contact;   // 1 if self-contact is on (LINEAR or SMOOTH)
   int32_t smooth;    // 1 for SMOOTH (limit-surface) self-contact
+  int32_t qe_df;     // element shares are double-float pairs (the FP64 variants of arithmetic 2)
   int32_t stab_off[13];  // SMOOTH: offset of the subdivision table of valence N in DevBuf::stab, or -1
   int32_t friction;  // 1 if mu_s or mu_d != 0
   int32_t pressure_base, pressure_dir;

@@ -1000,13 +1000,14 @@ __device__ __forceinline__ ElemOut element_force_df(uint32_t i, int np_rt, uint3
     const df2 Bs[6] = {{Bh[6 * s], Bl[6 * s]},         {Bh[6 * s + 1], Bl[6 * s + 1]},
                        {Bh[6 * s + 2], Bl[6 * s + 2]}, {Bh[6 * s + 3], Bl[6 * s + 3]},
                        {Bh[6 * s + 4], Bl[6 * s + 4]}, {Bh[6 * s + 5], Bl[6 * s + 5]}};
-    double* qe = b.qe + 3 * (size_t)__ldg(&spos[s]);
+    // the share stays a float pair in its 8 bytes; the gather adds the pairs and converts once per node
+    float2* qe = reinterpret_cast<float2*>(b.qe) + 3 * (size_t)__ldg(&spos[s]);
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
       df2 t = Bs[0] * Z[0][c];
 #pragma unroll
       for (int k = 1; k < 6; ++k) t += Bs[k] * Z[k][c];
-      qe[c] = df_to_double(t);
+      qe[c] = make_float2(t.h, t.l);
     }
   }
   return o;
@@ -1320,6 +1321,20 @@ __global__ void __launch_bounds__(kBlock) k_gather_correct(DevBuf b, StepConst s
       f[0] -= (double)s0;
       f[1] -= (double)s1;
       f[2] -= (double)s2;
+    } else if (sc.qe_df) {
+      // double-float shares: added as pairs on the FP32 pipe, converted once
+      const float2* q2 = reinterpret_cast<const float2*>(b.qe);
+      df2 s0 = dfv(0.f), s1 = dfv(0.f), s2 = dfv(0.f);
+#pragma unroll 4
+      for (uint32_t k = g0; k < g1; ++k) {
+        const float2 x = q2[3 * (size_t)k], y = q2[3 * (size_t)k + 1], z = q2[3 * (size_t)k + 2];
+        s0 += df2{x.x, x.y};
+        s1 += df2{y.x, y.y};
+        s2 += df2{z.x, z.y};
+      }
+      f[0] -= df_to_double(s0);
+      f[1] -= df_to_double(s1);
+      f[2] -= df_to_double(s2);
     } else {
 #pragma unroll 4
       for (uint32_t k = g0; k < g1; ++k) {
