@@ -401,15 +401,14 @@ namespace {
 // Device allocation, uploads and step constants for a context whose set-up
 // (c->S, one shell or a merged batch) is built; pscale: per original face.
 // The FP64 path's arithmetic: 0 = both basis contractions in FP64, 1 = the
-// displacement contraction as float pairs (measured 24-26 % faster at levels 6
-// and 7 than 0).  Pairing the force contraction as well is slower: converted
-// back in the element kernel it costs more than it saves, and left as pairs
-// for the gather to add in FP64 it doubles the gather's time (the float to
-// double conversions), more than the 6 % it saves in the element kernel at
-// level 7 (measured).  Fixed for all contexts, so that results do not depend
-// on which launch shape a context picks (the per-face arithmetic of a variant
-// does not depend on its shape).
-constexpr int kFp64Pairs = 1;
+// displacement contraction as float pairs (24-26 % faster than 0 at levels 6
+// and 7), 2 = double-float throughout: the relative-displacement formulation
+// in float pairs on the FP32 pipe, shares kept as pairs and added in
+// double-float by the gather (element kernel 14 % faster than 1 at level 6,
+// 34 % at level 7; forces within 1e-14 of FP64).  Fixed for all contexts, so
+// that results do not depend on which launch shape a context picks (the
+// per-face arithmetic of a variant does not depend on its shape).
+constexpr int kFp64Pairs = 2;
 
 // step constants that follow the FP64 variant: its share format
 void apply_variant(shl_ctx* c) { c->sc.qe_df = kElemVariants[c->var64].pairs == 2 ? 1 : 0; }
@@ -1491,6 +1490,10 @@ shl_status shl_residual(shl_ctx* c, double pressure, int flags, double* rel, dou
                                  cudaMemcpyHostToDevice, c->stream));
   }
   if (fp64 && ctx32 && !c->qe64) SHL_TRY(dev_alloc(c, &c->qe64, 3 * (size_t)c->S.n_slots_total));
+  if (fp64 && ctx32 && !c->b.face_df) {  // the double-float FP64 path's constants
+    SHL_TRY(dev_alloc(c, &c->b.face_df, c->S.face_df.size()));
+    SHL_TRY(upload(c, c->b.face_df, c->S.face_df.data(), c->S.face_df.size()));
+  }
   if (correct && !c->b.fcorr) {
     SHL_TRY(dev_alloc(c, &c->b.fcorr, nd));
     SHL_TRY(dev_alloc(c, &c->f32, nd));
