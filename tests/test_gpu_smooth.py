@@ -121,7 +121,7 @@ def test_smooth_trajectory(cuda_ok, meshes, name):
     cg, co = g.contact_state(), o.contact_state()
     assert np.array_equal(cg["pairs"], co["pairs"])
     assert np.array_equal(cg["stick"], co["stick"])
-    assert np.abs(g.contact_coords() - o.contact_coords()).max() < 1e-6
+    assert np.abs(g.contact_coords() - o.contact_coords()).max() < 1e-5  # search steps stop at 1e-6
     assert abs(rg.sum_Eself - ro.sum_Eself) <= 1e-9 * abs(ro.sum_Eself)
     g.close()
 
