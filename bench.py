@@ -46,10 +46,9 @@ FLUSH_BYTES = 512 << 20
 # plus the 27 kernels of each candidate-list rebuild that runs (10 pipeline + 3 x 3 scan + 8 contact CSR)
 LAUNCHES_PER_STEP_CONTACT = 7
 LAUNCHES_PER_REBUILD = 27
-# element kernel (double-float FP64 path): per-face constants as float pairs
-# (38 x 8), patch ids, force shares (36 pairs), element fields, face
-# permutation (bytes); per-node predicted displacement as float pairs (bytes)
-ELEM_BYTES_PER_FACE = 38 * 8 + 12 * 4 + 36 * 8 + 5 * 8 + 4
+# element kernel: per-face FP64 constants, patch ids, force shares, element
+# fields, face permutation (bytes); per-node predicted displacement (bytes)
+ELEM_BYTES_PER_FACE = 35 * 8 + 12 * 4 + 36 * 8 + 5 * 8 + 4
 ELEM_BYTES_PER_NODE = 24
 # FP64 flops of one regular face in the element kernel (count of the
 # arithmetic in element_force<12>, fused multiply-add = 2)

@@ -56,7 +56,6 @@ struct shl_ctx {
   ElemGroups eg_bs[3]{};           // block ranges for 64, 128, 256 threads per block
   uint32_t blocks_bs[3]{};
   int var64 = -1, var32 = kFirstFp32Variant;  // chosen element-kernel variants (-1: not set yet)
-  int sm_count = 1;                          // SMs of the context's device (resident grids)
   float variant_ms[kNumElemVariants]{};      // tuning times (0: not timed)
   std::vector<void*> allocs;
   cudaGraphExec_t graph = nullptr;
@@ -84,9 +83,8 @@ int bs_index(int block) { return block == 64 ? 0 : block == 128 ? 1 : 2; }
 ElemLaunch elem_launch(const shl_ctx* c, const StepConst& sc) {
   ElemLaunch el;
   el.variant = sc.fp32 ? c->var32 : c->var64;
-  const ElemVariant& v = kElemVariants[el.variant];
-  const int k = bs_index(v.block);
-  el.blocks = v.dyn_blocks_per_sm ? (uint32_t)(c->sm_count * v.dyn_blocks_per_sm) : c->blocks_bs[k];
+  const int k = bs_index(kElemVariants[el.variant].block);
+  el.blocks = c->blocks_bs[k];
   el.eg = c->eg_bs[k];
   return el;
 }
@@ -472,9 +470,6 @@ shl_status create_common(shl_ctx* c, const std::vector<double>& pscale_orig, shl
     g_err = "no CUDA device";
     return fail(SHL_ERR_CUDA);
   }
-  if (cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, c->device) != cudaSuccess ||
-      c->sm_count < 1)
-    c->sm_count = 1;
   const Setup& S = c->S;
   const uint32_t V = S.V, F = S.F;
   DevBuf& b = c->b;

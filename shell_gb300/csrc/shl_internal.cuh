@@ -63,12 +63,9 @@ struct ElemVariant {
   int block;
   int pairs;
   const char* name;
-  int dyn_blocks_per_sm;  // 0: one face per thread, a block per 'block' faces; else a resident grid of
-                          // this many blocks per SM whose warps fetch 32-face chunks (k_elements_df_dyn)
 };
-constexpr int kElemChunk = 32;  // faces per chunk of the dynamically scheduled element kernel
 constexpr int kNumElemVariants = SHL_ELEMENT_VARIANTS;
-constexpr int kFirstFp32Variant = 11;
+constexpr int kFirstFp32Variant = 9;
 extern const ElemVariant kElemVariants[kNumElemVariants];
 
 // The element launch of a context: variant, grid and patch-group block ranges for its block size.
@@ -133,8 +130,7 @@ struct Ctl {
   double sum_dt, sum_area, sum_volume, sum_Nc, sum_Ekin, sum_Etens, sum_Ebend, sum_Eself, sum_Efric,
       sum_kGauss, sum_kMean;
   // last-block counters
-  uint32_t cnt[16];        // last-block counters of the reducing kernels; cnt[8] / cnt[9]: next chunk /
-                           // finished warps of the dynamically scheduled element kernel
+  uint32_t cnt[16];
 };
 
 // Step constants (captured by value in each launch).

@@ -1051,74 +1051,6 @@ __global__ void __launch_bounds__(BS, MINB) k_elements_df(DevBuf b, StepConst sc
   b.ebend[e] = o.ebend / o.area;
 }
 
-// The double-float element kernel on a resident grid (a few blocks per SM):
-// each warp fetches chunks of kElemChunk faces of one patch group from a
-// device counter until all are done, so the SMs stay busy to the end instead
-// of finishing in block-sized waves.  The last warp to finish resets the
-// counters.  Per-face arithmetic as k_elements_df.
-template <int BS, int MINB>
-__global__ void __launch_bounds__(BS, MINB) k_elements_df_dyn(DevBuf b, StepConst sc, ElemGroups eg) {
-  Ctl* ctl = b.ctl;
-  if (inactive(ctl)) return;
-  // every group's basis table, each followed by its float pairs (as k_elements_df stages one)
-  __shared__ double sB[kMaxGroups][kMaxSlots * 6 * 2];
-  for (int g = 0; g < eg.n; ++g) {
-    float* sBh = reinterpret_cast<float*>(sB[g] + kMaxSlots * 6);
-    float* sBl = sBh + kMaxSlots * 6;
-    for (int k = threadIdx.x; k < eg.g[g].n_slots * 6; k += blockDim.x) {
-      const double w = eg.basis[eg.g[g].basis_off + k];
-      sB[g][k] = w;
-      df_split(w, sBh[k], sBl[k]);
-    }
-  }
-  __syncthreads();
-  uint32_t n_chunks = 0;
-  for (int g = 0; g < eg.n; ++g) n_chunks += (eg.g[g].count + kElemChunk - 1) / kElemChunk;
-  const int lane = threadIdx.x & 31;
-  const double pressure = ctl->pressure, vol_p = ctl->volume_pressure;
-  for (;;) {
-    uint32_t c = 0;
-    if (lane == 0) c = atomicAdd(&ctl->cnt[8], 1u);
-    c = __shfl_sync(0xffffffffu, c, 0);
-    if (c >= n_chunks) break;
-    int g = 0;
-    uint32_t c0 = 0;
-    for (;;) {
-      const uint32_t nc = (eg.g[g].count + kElemChunk - 1) / kElemChunk;
-      if (c < c0 + nc || g + 1 >= eg.n) break;
-      c0 += nc;
-      ++g;
-    }
-    const GroupDesc gd = eg.g[g];
-    const uint32_t li = (c - c0) * kElemChunk + (uint32_t)lane;
-    if (li >= gd.count) continue;
-    const uint32_t i = gd.first + li;
-    const uint32_t slot0 = gd.slot_base + li * (uint32_t)gd.n_slots;
-    const double pr = pressure * __ldg(&b.pscale[i]);
-    const double* B = sB[g];
-    ElemOut o;
-    if (gd.n_slots == 12)
-      o = element_force_df<12>(i, 12, slot0, B, b, sc, pr, vol_p);
-    else if (gd.n_slots == 11)
-      o = element_force_df<11>(i, 11, slot0, B, b, sc, pr, vol_p);
-    else
-      o = element_force_df<0>(i, gd.n_slots, slot0, B, b, sc, pr, vol_p);
-    const uint32_t e = __ldg(&b.perm[i]);
-    b.area[e] = o.area;
-    b.kG[e] = o.kg / o.area;
-    b.kM[e] = o.km / o.area;
-    b.etens[e] = o.etens / o.area;
-    b.ebend[e] = o.ebend / o.area;
-  }
-  if (lane == 0) {
-    const uint32_t warps = gridDim.x * (BS / 32);
-    if (atomicAdd(&ctl->cnt[9], 1u) == warps - 1) {
-      ctl->cnt[8] = 0;
-      ctl->cnt[9] = 0;
-    }
-  }
-}
-
 template <int BS, int MINB>
 __global__ void __launch_bounds__(BS, MINB) k_elements32(DevBuf b, StepConst sc, ElemGroups eg) {
   Ctl* ctl = b.ctl;
@@ -1853,7 +1785,6 @@ const ElemVariant kElemVariants[kNumElemVariants] = {
     {256, 0, "fp64 256x1"},        {256, 1, "fp64 256x1 pair-G"}, {128, 1, "fp64 128x3 pair-G"},
     {64, 1, "fp64 64x5 pair-G"},   {64, 1, "fp64 64x6 pair-G"},   {64, 0, "fp64 64x5"},
     {256, 2, "fp64 256x1 df"},     {128, 2, "fp64 128x3 df"},     {64, 2, "fp64 64x6 df"},
-    {64, 2, "fp64 64x6 df dyn", 6}, {128, 2, "fp64 128x3 df dyn", 3},
     {256, 0, "fp32 256x2"},        {128, 0, "fp32 128x4"},        {64, 0, "fp32 64x8"}};
 
 void launch_elements(const DevBuf& b, const StepConst& sc, const ElemLaunch& el, cudaStream_t s, bool totals) {
@@ -1869,10 +1800,8 @@ void launch_elements(const DevBuf& b, const StepConst& sc, const ElemLaunch& el,
     case 6: k_elements_df<256, 1><<<nb, 256, 0, s>>>(b, sc, eg); break;
     case 7: k_elements_df<128, 3><<<nb, 128, 0, s>>>(b, sc, eg); break;
     case 8: k_elements_df<64, 6><<<nb, 64, 0, s>>>(b, sc, eg); break;
-    case 9: k_elements_df_dyn<64, 6><<<nb, 64, 0, s>>>(b, sc, eg); break;
-    case 10: k_elements_df_dyn<128, 3><<<nb, 128, 0, s>>>(b, sc, eg); break;
-    case 11: k_elements32<256, 2><<<nb, 256, 0, s>>>(b, sc, eg); break;
-    case 12: k_elements32<128, 4><<<nb, 128, 0, s>>>(b, sc, eg); break;
+    case 9: k_elements32<256, 2><<<nb, 256, 0, s>>>(b, sc, eg); break;
+    case 10: k_elements32<128, 4><<<nb, 128, 0, s>>>(b, sc, eg); break;
     default: k_elements32<64, 8><<<nb, 64, 0, s>>>(b, sc, eg); break;
   }
   if (totals) k_elem_totals<<<nblk(sc.F), kBlock, 0, s>>>(b, sc);
