@@ -827,18 +827,6 @@ __device__ __forceinline__ ElemOut element_force_df(uint32_t i, int np_rt, uint3
   const int np = NP > 0 ? NP : np_rt;
   const float* Bh = reinterpret_cast<const float*>(B + kMaxSlots * 6);
   const float* Bl = Bh + kMaxSlots * 6;
-  {
-    // The face constants come from DRAM when the step starts with a cold L2, and
-    // they are used along a long dependency chain: the warp asks for all of its
-    // rows (one 128-byte line per constant for 32 consecutive faces) up front.
-    const int lane = threadIdx.x & 31;
-    const uint32_t i0 = i - (uint32_t)lane;
-    for (int r = lane; r < 2 * F32_COUNT; r += 32)
-      asm volatile("prefetch.global.L2 [%0];" ::"l"(b.face_df + (size_t)r * F + i0));
-    // and the share places it writes at the end (np slots per face, consecutive)
-    const uint32_t s0 = slot0 - (uint32_t)lane * (uint32_t)np;
-    if (lane < np) asm volatile("prefetch.global.L2 [%0];" ::"l"(b.slot_pos + s0 + 32 * (size_t)lane));
-  }
   df2 G[6][3];
   {
     float gh[6][3], gl[6][3];
