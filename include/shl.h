@@ -296,12 +296,12 @@ shl_status shl_get_element_fields(shl_ctx* ctx, double* kGauss, double* kMean, d
 /* Element-kernel variants (launch shape; for FP64, the arithmetic of the two
  * basis contractions): shl_create times the shapes of the context's path on
  * its mesh and keeps the fastest (autotuning).  shl_set_element_variant forces
- * one (0-8 FP64, 9-11 FP32; 0 and 5 keep the displacement contraction in
- * FP64, 6-8 compute in double-float) or, with -1, tunes again; shl_get_element_variant
+ * one (0-9 FP64, 10-12 FP32; 0 and 5 keep the displacement contraction in
+ * FP64, 6-9 compute in double-float) or, with -1, tunes again; shl_get_element_variant
  * returns the choice, its name and the tuning times of all
  * SHL_ELEMENT_VARIANTS (ms, 0 = not timed; tuned_ms holds that many floats).
  * No counterpart in the reference. */
-enum { SHL_ELEMENT_VARIANTS = 12 };
+enum { SHL_ELEMENT_VARIANTS = 13 };
 shl_status shl_set_element_variant(shl_ctx* ctx, int variant);
 shl_status shl_get_element_variant(shl_ctx* ctx, int* variant, char* name, size_t cap, float* tuned_ms);
 

@@ -65,7 +65,7 @@ struct ElemVariant {
   const char* name;
 };
 constexpr int kNumElemVariants = SHL_ELEMENT_VARIANTS;
-constexpr int kFirstFp32Variant = 9;
+constexpr int kFirstFp32Variant = 10;
 extern const ElemVariant kElemVariants[kNumElemVariants];
 
 // The element launch of a context: variant, grid and patch-group block ranges for its block size.

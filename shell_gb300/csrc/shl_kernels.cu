@@ -1785,6 +1785,7 @@ const ElemVariant kElemVariants[kNumElemVariants] = {
     {256, 0, "fp64 256x1"},        {256, 1, "fp64 256x1 pair-G"}, {128, 1, "fp64 128x3 pair-G"},
     {64, 1, "fp64 64x5 pair-G"},   {64, 1, "fp64 64x6 pair-G"},   {64, 0, "fp64 64x5"},
     {256, 2, "fp64 256x1 df"},     {128, 2, "fp64 128x3 df"},     {64, 2, "fp64 64x6 df"},
+    {64, 2, "fp64 64x8 df"},
     {256, 0, "fp32 256x2"},        {128, 0, "fp32 128x4"},        {64, 0, "fp32 64x8"}};
 
 void launch_elements(const DevBuf& b, const StepConst& sc, const ElemLaunch& el, cudaStream_t s, bool totals) {
@@ -1800,8 +1801,9 @@ void launch_elements(const DevBuf& b, const StepConst& sc, const ElemLaunch& el,
     case 6: k_elements_df<256, 1><<<nb, 256, 0, s>>>(b, sc, eg); break;
     case 7: k_elements_df<128, 3><<<nb, 128, 0, s>>>(b, sc, eg); break;
     case 8: k_elements_df<64, 6><<<nb, 64, 0, s>>>(b, sc, eg); break;
-    case 9: k_elements32<256, 2><<<nb, 256, 0, s>>>(b, sc, eg); break;
-    case 10: k_elements32<128, 4><<<nb, 128, 0, s>>>(b, sc, eg); break;
+    case 9: k_elements_df<64, 8><<<nb, 64, 0, s>>>(b, sc, eg); break;
+    case 10: k_elements32<256, 2><<<nb, 256, 0, s>>>(b, sc, eg); break;
+    case 11: k_elements32<128, 4><<<nb, 128, 0, s>>>(b, sc, eg); break;
     default: k_elements32<64, 8><<<nb, 64, 0, s>>>(b, sc, eg); break;
   }
   if (totals) k_elem_totals<<<nblk(sc.F), kBlock, 0, s>>>(b, sc);

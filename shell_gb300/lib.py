@@ -22,7 +22,7 @@ SHL_ERR_ARG, SHL_ERR_CUDA, SHL_ERR_TIMEOUT, SHL_ERR_OOM, SHL_ERR_CAPACITY = 100,
 CONTACT_LINEAR, CONTACT_SMOOTH, CONTACT_NONE = 0, 1, 2
 CS_LOCAL, CS_CARTESIAN, CS_CYLINDRICAL, CS_SPHERICAL = 0, 1, 2, 3
 PREC_FP64, PREC_FP32 = 0, 1
-ELEMENT_VARIANTS = 12  # SHL_ELEMENT_VARIANTS
+ELEMENT_VARIANTS = 13  # SHL_ELEMENT_VARIANTS
 CAVITY_BOX, CAVITY_CYLINDER, CAVITY_ELLIPSOID = 0, 1, 2
 
 _d, _i32, _u32 = ctypes.c_double, ctypes.c_int32, ctypes.c_uint32
