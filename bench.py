@@ -46,13 +46,18 @@ FLUSH_BYTES = 512 << 20
 # plus the 27 kernels of each candidate-list rebuild that runs (10 pipeline + 3 x 3 scan + 8 contact CSR)
 LAUNCHES_PER_STEP_CONTACT = 7
 LAUNCHES_PER_REBUILD = 27
-# element kernel: per-face FP64 constants, patch ids, force shares, element
-# fields, face permutation (bytes); per-node predicted displacement (bytes)
-ELEM_BYTES_PER_FACE = 35 * 8 + 12 * 4 + 36 * 8 + 5 * 8 + 4
+# element kernel (double-float FP64 path): per-face constants as float pairs
+# (38 fields x 8 B), patch ids, force shares (float pairs), element fields,
+# face permutation (bytes); per-node predicted displacement (bytes)
+ELEM_BYTES_PER_FACE = 38 * 8 + 12 * 4 + 36 * 8 + 5 * 8 + 4
 ELEM_BYTES_PER_NODE = 24
 # FP64 flops of one regular face in the element kernel (count of the
 # arithmetic in element_force<12>, fused multiply-add = 2)
 ELEM_FLOPS_PER_FACE = 1372
+# DRAM bytes (read + write) of one element-kernel launch on the level-6 shell,
+# from one ncu --set full capture with caches flushed (38.2 MB read, 3.4 MB
+# written; the force shares mostly stay in the 129 MB L2)
+ELEM_TRAFFIC_LEVEL6 = 41.6e6
 
 
 def ensemble_workload(L, n_shells=256, seed=0):
@@ -446,10 +451,15 @@ def run_ours(args, rank, world, dist):
                 "d2h_bytes_per_step": 3 * 3 * V * 8,
                 "how": "per step: shl_set_state from pinned host, shl_step(1), shl_get_state"},
         "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm, "unit": "GB/s",
-                     "frac": achieved_gbs / hbm, "traffic": None, "kernel": "k_elements", "variant": elem_variant,
+                     "frac": achieved_gbs / hbm,
+                     "traffic": ELEM_TRAFFIC_LEVEL6 if args.level == 6 else None,
+                     "traffic_note": "bytes per launch, ncu capture of the level-6 element kernel",
+                     "kernel": "k_elements", "variant": elem_variant,
                      "kernel_ms": elem_ms, "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)",
                      "fp64": {"achieved_tflops": achieved_tf, "peak_tflops": fp64_peak,
                               "frac": achieved_tf / fp64_peak,
+                              "flops": "FP64-equivalent flops of the element arithmetic (executed as float "
+                                       "pairs on the FP32 pipe by the double-float variants)",
                               "peak_source": "DFMA register loop measured in this run"}},
         "cpu_baseline": cpu,
         "clocks": clk.summary(),
