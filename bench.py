@@ -410,8 +410,7 @@ def run_ours(args, rank, world, dist):
     for k in range(Ke):
         g.set_state(nu_, nv_, na_)
         g.step(1, pt[k:k + 1])
-        uu, vv, aa = g.get_state()
-        nu_[:], nv_[:], na_[:] = uu, vv, aa
+        g.get_state(out=(nu_, nv_, na_))
     e2e_s = time.perf_counter() - t0
     e2e = F * Ke * world / e2e_s
 

@@ -61,6 +61,8 @@ struct shl_ctx {
   cudaGraphExec_t graph = nullptr;
   cudaGraphExec_t graph1 = nullptr;
   double* h_pin = nullptr;  // pinned staging buffer, 3V doubles x 3
+  Ctl* h_ctl = nullptr;     // pinned copy of the device control block
+  double* h_table = nullptr;  // pinned staging of the pressure table (kTableCap doubles)
   double* d_fa = nullptr;   // device f and a of shl_eval_forces, 2 x 3V doubles
   void* d_flush = nullptr;  // L2 eviction buffer of shl_time_kernel
   size_t flush_bytes = 0;
@@ -121,14 +123,22 @@ shl_status upload(shl_ctx* c, T* dst, const T* src, size_t n) {
   return SHL_OK;
 }
 
+// the control block travels through a pinned host copy (one DMA, no staging)
 shl_status ctl_get(shl_ctx* c, Ctl& h) {
-  SHL_CUDA_TRY(cudaMemcpyAsync(&h, c->b.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, c->stream));
+  Ctl* dst = c->h_ctl ? c->h_ctl : &h;
+  SHL_CUDA_TRY(cudaMemcpyAsync(dst, c->b.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, c->stream));
   SHL_CUDA_TRY(cudaStreamSynchronize(c->stream));
+  if (dst != &h) std::memcpy(&h, dst, sizeof(Ctl));
   return SHL_OK;
 }
 
 shl_status ctl_put(shl_ctx* c, const Ctl& h) {
-  SHL_CUDA_TRY(cudaMemcpyAsync(c->b.ctl, &h, sizeof(Ctl), cudaMemcpyHostToDevice, c->stream));
+  const Ctl* src = &h;
+  if (c->h_ctl) {
+    std::memcpy(c->h_ctl, &h, sizeof(Ctl));
+    src = c->h_ctl;
+  }
+  SHL_CUDA_TRY(cudaMemcpyAsync(c->b.ctl, src, sizeof(Ctl), cudaMemcpyHostToDevice, c->stream));
   SHL_CUDA_TRY(cudaStreamSynchronize(c->stream));
   return SHL_OK;
 }
@@ -388,6 +398,8 @@ void shl_destroy(shl_ctx* c) {
   if (c->graph1) cudaGraphExecDestroy(c->graph1);
   for (void* p : c->allocs) cudaFree(p);
   if (c->h_pin) cudaFreeHost(c->h_pin);
+  if (c->h_ctl) cudaFreeHost(c->h_ctl);
+  if (c->h_table) cudaFreeHost(c->h_table);
   if (c->d_flush) cudaFree(c->d_flush);
   if (c->stream) cudaStreamDestroy(c->stream);
   if (c->side) cudaStreamDestroy(c->side);
@@ -470,6 +482,10 @@ shl_status create_common(shl_ctx* c, const std::vector<double>& pscale_orig, shl
     g_err = "no CUDA device";
     return fail(SHL_ERR_CUDA);
   }
+  if (cudaError_t e = init_element_kernels(); e != cudaSuccess) {
+    g_err = std::string("element kernel attributes: ") + cudaGetErrorString(e);
+    return fail(SHL_ERR_CUDA);
+  }
   const Setup& S = c->S;
   const uint32_t V = S.V, F = S.F;
   DevBuf& b = c->b;
@@ -477,8 +493,7 @@ shl_status create_common(shl_ctx* c, const std::vector<double>& pscale_orig, shl
 #define ALLOC(ptr, n) do { if ((st = dev_alloc(c, &(ptr), (n))) != SHL_OK) return fail(st); } while (0)
   ALLOC(b.X, nd); ALLOC(b.u, nd); ALLOC(b.v, nd); ALLOC(b.a, nd); ALLOC(b.up, nd); ALLOC(b.vp, nd);
   ALLOC(b.p, nd); ALLOC(b.Minv, nd); ALLOC(b.C, nd); ALLOC(b.M, nd);
-  ALLOC(b.uph, nd);
-  ALLOC(b.upl, nd);
+  ALLOC(b.upk, 2 * (size_t)S.V);
   if (params->adapt_dt_every) ALLOC(b.ap, nd);
   if (params->shell_cavity_contact) {
     ALLOC(b.cav_origin, nd);
@@ -740,6 +755,8 @@ shl_status create_common(shl_ctx* c, const std::vector<double>& pscale_orig, shl
   h.cav_R[0] = p.Rx;
   h.cav_R[1] = p.Ry;
   h.cav_R[2] = p.Rz;
+  if (cudaMallocHost(&c->h_ctl, sizeof(Ctl)) != cudaSuccess) c->h_ctl = nullptr;
+  if (cudaMallocHost(&c->h_table, kTableCap * sizeof(double)) != cudaSuccess) c->h_table = nullptr;
   if ((st = ctl_put(c, h)) != SHL_OK) return fail(st);
   if (cudaMallocHost(&c->h_pin, 3 * nd * sizeof(double)) != cudaSuccess) c->h_pin = nullptr;
   if ((st = check_launch("shl_create")) != SHL_OK) return fail(st);
@@ -992,23 +1009,10 @@ shl_status shl_apply_loaded_state(shl_ctx* c) {
 
 namespace {
 
+// clears the run report on the device, ordered on the context stream (no host round trip)
 shl_status reset_report(shl_ctx* c) {
-  Ctl h;
-  SHL_TRY(ctl_get(c, h));
-  h.steps_done = 0;
-  h.worst_problem = 0;
-  h.first_problem_step = 0;
-  h.halted = 0;
-  h.error = 0;
-  h.problem = 0;
-  h.n_rebuilds = 0;
-  h.rejections = 0;
-  h.paused = 0;
-  h.sum_pcav = h.sum_Nc_cav = h.sum_Ecav = 0;
-  h.steps_target = ~0u;
-  h.sum_dt = h.sum_area = h.sum_volume = h.sum_Nc = h.sum_Ekin = h.sum_Etens = h.sum_Ebend = h.sum_Eself =
-      h.sum_Efric = h.sum_kGauss = h.sum_kMean = 0;
-  return ctl_put(c, h);
+  launch_ctl_begin(c->b.ctl, 0, kCtlReset, c->stream);
+  return check_launch("reset_report");
 }
 
 shl_status ensure_graphs(shl_ctx* c) {
@@ -1029,20 +1033,33 @@ shl_status enqueue_steps(shl_ctx* c, uint32_t n, bool use_graph) {
   return check_launch("step");
 }
 
-shl_status upload_table(shl_ctx* c, const double* table, uint32_t n) {
+// Uploads n pressures and rewinds the device table to them; `flags` adds further
+// control-block updates (kCtlReset, kCtlArm) to the same launch.  With the pinned
+// staging buffer the copy is asynchronous: callers synchronise the stream before
+// the buffer is written again (shl_step does at the end of every chunk).
+shl_status upload_table(shl_ctx* c, const double* table, uint32_t n, uint32_t flags = 0, bool sync = true) {
   if (n > c->b.ptable_cap) { g_err = "pressure table longer than the device table"; return SHL_ERR_CAPACITY; }
-  if (n) SHL_TRY(upload(c, c->b.ptable, table, n));
-  const uint32_t hdr[2] = {0u, n};
-  static_assert(offsetof(Ctl, table_len) == offsetof(Ctl, table_pos) + 4, "layout");
-  SHL_CUDA_TRY(cudaMemcpyAsync((char*)c->b.ctl + offsetof(Ctl, table_pos), hdr, sizeof(hdr), cudaMemcpyHostToDevice,
-                               c->stream));
-  SHL_CUDA_TRY(cudaStreamSynchronize(c->stream));
+  if (n) {
+    const double* src = table;
+    if (c->h_table && table != c->h_table) {
+      std::memcpy(c->h_table, table, n * sizeof(double));
+      src = c->h_table;
+    }
+    SHL_TRY(upload(c, c->b.ptable, src, n));
+  }
+  launch_ctl_begin(c->b.ctl, n, kCtlTable | flags, c->stream);
+  SHL_TRY(check_launch("upload_table"));
+  if (sync) SHL_CUDA_TRY(cudaStreamSynchronize(c->stream));
   return SHL_OK;
 }
 
-shl_status collect(shl_ctx* c, shl_step_report* report) {
+// `fresh`: the caller has just read the control block into `h` (no launch since)
+shl_status collect(shl_ctx* c, shl_step_report* report, const Ctl* fresh = nullptr) {
   Ctl h;
-  SHL_TRY(ctl_get(c, h));
+  if (fresh)
+    h = *fresh;
+  else
+    SHL_TRY(ctl_get(c, h));
   if (report) {
     std::memset(report, 0, sizeof(*report));
     report->steps_done = h.steps_done;
@@ -1074,27 +1091,26 @@ shl_status collect(shl_ctx* c, shl_step_report* report) {
 shl_status shl_step(shl_ctx* c, uint32_t n_steps, const double* pressure_table, int use_graph,
                     shl_step_report* report) {
   if (!c) return SHL_ERR_ARG;
-  SHL_TRY(reset_report(c));
   std::vector<double> chunk;
-  uint32_t done = 0;
+  uint32_t done = 0, steps_before = 0;
   bool stop = false;
+  Ctl hh;
   while (done < n_steps && !stop) {
     const uint32_t m = std::min<uint32_t>(n_steps - done, c->b.ptable_cap);
-    chunk.resize(m);
-    for (uint32_t i = 0; i < m; ++i) chunk[i] = pressure_table ? pressure_table[done + i] : c->P.pressure;
-    SHL_TRY(upload_table(c, chunk.data(), m));
-    Ctl hh;
-    SHL_TRY(ctl_get(c, hh));
-    const uint32_t target = hh.steps_done + m;
-    hh.steps_target = target;
-    hh.paused = 0;
-    SHL_TRY(ctl_put(c, hh));
+    double* t = c->h_table;
+    if (!t) {
+      chunk.resize(m);
+      t = chunk.data();
+    }
+    for (uint32_t i = 0; i < m; ++i) t[i] = pressure_table ? pressure_table[done + i] : c->P.pressure;
+    // one launch rewinds the table, arms the pause target (and clears the report before the first chunk)
+    SHL_TRY(upload_table(c, t, m, kCtlArm | (done == 0 ? kCtlReset : 0u), false));
+    const uint32_t target = steps_before + m;
     // one slot per attempt: with adaptive dt, repeated attempts leave steps to top up
     uint32_t attempts = m;
     for (int round = 0;; ++round) {
       SHL_TRY(enqueue_steps(c, attempts, use_graph != 0));
-      SHL_CUDA_TRY(cudaStreamSynchronize(c->stream));
-      SHL_TRY(ctl_get(c, hh));
+      SHL_TRY(ctl_get(c, hh));  // copy + stream synchronisation
       if (hh.halted || (hh.paused & 2u) || hh.steps_done >= target) break;
       if (round >= 100000) {
         g_err = "shl_step: steps were repeated without end (adaptive dt)";
@@ -1103,10 +1119,12 @@ shl_status shl_step(shl_ctx* c, uint32_t n_steps, const double* pressure_table, 
       attempts = target - hh.steps_done;
     }
     done += m;
+    steps_before = hh.steps_done;
     if (hh.halted) break;
     if (hh.paused & 2u) stop = true;
   }
-  return collect(c, report);
+  if (n_steps == 0) SHL_TRY(reset_report(c));
+  return collect(c, report, n_steps ? &hh : nullptr);
 }
 
 shl_status shl_set_cavity_functions(shl_ctx* c, const char* rx, const char* ry, const char* rz) {

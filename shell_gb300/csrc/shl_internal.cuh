@@ -195,7 +195,7 @@ struct DevBuf {
   float* face_df;     // 2 * F32_COUNT * F: the same constants as float pairs (double-float FP64 path)
   float* qe32;        // 3 per element-force slot, in gather order (FP32 element path)
   float* up32;        // 3V, FP32 copy of u_pred (FP32 element path)
-  float *uph, *upl;   // 3V, u_pred as a float pair hi + lo (the FP64 path's contractions)
+  float4* upk;        // 2V, u_pred as float pairs: [2n] = hi (x, y, z, 0), [2n + 1] = lo (the FP64 path's contractions)
   // element force shares are stored in gather order (node by node, ascending
   // element-force slot): slot_pos maps a (face, slot) to its place, and node n's
   // shares are qe[gather_ptr[n] .. gather_ptr[n + 1])
@@ -284,6 +284,9 @@ void launch_gather_correct(const DevBuf& b, const StepConst& sc, int cur, bool c
                            double* a_out, cudaStream_t s);
 void launch_volume_end_step(const DevBuf& b, const StepConst& sc, bool end_step, cudaStream_t s);
 void launch_positions(const DevBuf& b, const StepConst& sc, cudaStream_t s);
+cudaError_t init_element_kernels();
+enum : uint32_t { kCtlReset = 1u, kCtlTable = 2u, kCtlArm = 4u };
+void launch_ctl_begin(Ctl* ctl, uint32_t n, uint32_t flags, cudaStream_t s);
 void launch_fp64_peak(double* out, int blocks, int iters, cudaStream_t s);
 // allocation-free force evaluation (scratch in a static device array)
 uint32_t noalloc_max_faces();

@@ -181,6 +181,19 @@ __device__ __forceinline__ void df_split(double x, float& h, float& l) {
 
 __device__ __forceinline__ double df_value(float h, float l) { return (double)h + (double)l; }
 
+// 16-byte asynchronous global -> shared copy (LDGSTS; both addresses 16-byte
+// aligned) and the wait for all of this thread's copies
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const uint32_t d = (uint32_t)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
+// dynamic shared memory of the double-float element kernels: the displacements
+// (hi and lo float4) of up to 12 patch slots per thread
+constexpr int kDfStageSlots = 12;
+constexpr size_t df_stage_bytes(int block) { return (size_t)kDfStageSlots * 2 * sizeof(float4) * block; }
+
 // ---------------------------------------------------------------- cavity --
 // effective semi-axes and friction scope (update_derived, ShellSystem.C:421-436)
 struct CavityGeom {
@@ -327,6 +340,7 @@ __global__ void __launch_bounds__(kBlock) k_predict(DevBuf b, StepConst sc) {
   double du2 = 0.0;
   if (n < sc.V) {
     double d[3];
+    float uh[3], ul[3];
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
       const size_t k = 3 * (size_t)n + c;
@@ -345,10 +359,14 @@ __global__ void __launch_bounds__(kBlock) k_predict(DevBuf b, StepConst sc) {
       if (sc.fp32)
         b.up32[k] = (float)up;
       else
-        df_split(up, b.uph[k], b.upl[k]);
+        df_split(up, uh[c], ul[c]);
       b.vp[k] = vp;
       b.p[k] = __dadd_rn(b.X[k], up);
       d[c] = __dsub_rn(up, u);
+    }
+    if (!sc.fp32) {
+      b.upk[2 * (size_t)n] = make_float4(uh[0], uh[1], uh[2], 0.f);
+      b.upk[2 * (size_t)n + 1] = make_float4(ul[0], ul[1], ul[2], 0.f);
     }
     du2 = __dadd_rn(__dadd_rn(__dmul_rn(d[0], d[0]), __dmul_rn(d[1], d[1])), __dmul_rn(d[2], d[2]));
   }
@@ -393,12 +411,15 @@ __global__ void __launch_bounds__(kBlock) k_predict(DevBuf b, StepConst sc) {
 __global__ void k_positions(DevBuf b, StepConst sc) {
   const uint32_t n = blockIdx.x * blockDim.x + threadIdx.x;
   if (n >= sc.V) return;
+  float uh[3], ul[3];
   for (int c = 0; c < 3; ++c) {
     const size_t k = 3 * (size_t)n + c;
     b.p[k] = __dadd_rn(b.X[k], b.up[k]);
     if (sc.fp32) b.up32[k] = (float)b.up[k];
-    df_split(b.up[k], b.uph[k], b.upl[k]);
+    df_split(b.up[k], uh[c], ul[c]);
   }
+  b.upk[2 * (size_t)n] = make_float4(uh[0], uh[1], uh[2], 0.f);
+  b.upk[2 * (size_t)n + 1] = make_float4(ul[0], ul[1], ul[2], 0.f);
 }
 
 // ------------------------------------------------------------- elements --
@@ -438,12 +459,8 @@ __device__ __forceinline__ ElemOut element_force(uint32_t i, int np_rt, uint32_t
     for (int s = 0; s < (NP > 0 ? NP : kMaxSlots); ++s) {
       if (NP == 0 && s >= np) break;
       const int nd = __ldg(&b.patch[(size_t)s * F + i]);
-      float uh[3], ul[3];
-#pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        uh[c] = __ldg(&b.uph[3 * (size_t)nd + c]);
-        ul[c] = __ldg(&b.upl[3 * (size_t)nd + c]);
-      }
+      const float4 h4 = __ldg(&b.upk[2 * (size_t)nd]), l4 = __ldg(&b.upk[2 * (size_t)nd + 1]);
+      const float uh[3] = {h4.x, h4.y, h4.z}, ul[3] = {l4.x, l4.y, l4.z};
 #pragma unroll
       for (int k = 0; k < 6; ++k) {
         const float wh = Bh[6 * s + k], wl = Bl[6 * s + k];
@@ -822,11 +839,27 @@ __device__ __forceinline__ ElemOut element_force32(uint32_t i, int np_rt, uint32
 template <int NP>
 __device__ __forceinline__ ElemOut element_force_df(uint32_t i, int np_rt, uint32_t slot0,
                                                     const double* __restrict__ B, const DevBuf& b,
-                                                    const StepConst& sc, double pressure_d, double vol_p_d) {
+                                                    const StepConst& sc, double pressure_d, double vol_p_d,
+                                                    float4* __restrict__ su) {
   const uint32_t F = sc.F;
   const int np = NP > 0 ? NP : np_rt;
   const float* Bh = reinterpret_cast<const float*>(B + kMaxSlots * 6);
   const float* Bl = Bh + kMaxSlots * 6;
+  const uint32_t t = threadIdx.x, bs = blockDim.x;
+  if (NP > 0) {
+    // all patch ids, then all node displacements copied asynchronously into this
+    // thread's shared-memory column ([2 s + hi/lo][thread], 16 B each): one
+    // memory latency for the whole patch instead of one per slot of the loop below
+    int nd[NP > 0 ? NP : 1];
+#pragma unroll
+    for (int s = 0; s < NP; ++s) nd[s] = __ldg(&b.patch[(size_t)s * F + i]);
+#pragma unroll
+    for (int s = 0; s < NP; ++s) {
+      cp_async16(&su[(2 * s) * bs + t], &b.upk[2 * (size_t)nd[s]]);
+      cp_async16(&su[(2 * s + 1) * bs + t], &b.upk[2 * (size_t)nd[s] + 1]);
+    }
+    cp_async_wait_all();
+  }
   df2 G[6][3];
   {
     float gh[6][3], gl[6][3];
@@ -837,13 +870,16 @@ __device__ __forceinline__ ElemOut element_force_df(uint32_t i, int np_rt, uint3
     // slots in a rolled loop: the unrolled double-float code would not fit the instruction cache
 #pragma unroll 1
     for (int s = 0; s < np; ++s) {
-      const int nd = __ldg(&b.patch[(size_t)s * F + i]);
-      float uh[3], ul[3];
-#pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        uh[c] = __ldg(&b.uph[3 * (size_t)nd + c]);
-        ul[c] = __ldg(&b.upl[3 * (size_t)nd + c]);
+      float4 h4, l4;
+      if (NP > 0) {
+        h4 = su[(2 * s) * bs + t];
+        l4 = su[(2 * s + 1) * bs + t];
+      } else {
+        const int nd = __ldg(&b.patch[(size_t)s * F + i]);
+        h4 = __ldg(&b.upk[2 * (size_t)nd]);
+        l4 = __ldg(&b.upk[2 * (size_t)nd + 1]);
       }
+      const float uh[3] = {h4.x, h4.y, h4.z}, ul[3] = {l4.x, l4.y, l4.z};
 #pragma unroll
       for (int k = 0; k < 6; ++k) {
         const float wh = Bh[6 * s + k], wl = Bl[6 * s + k];
@@ -1019,6 +1055,7 @@ __global__ void __launch_bounds__(BS, MINB) k_elements_df(DevBuf b, StepConst sc
   Ctl* ctl = b.ctl;
   if (inactive(ctl)) return;
   __shared__ double sB[kMaxSlots * 6 * 2];
+  extern __shared__ float4 su[];  // kDfStageSlots x 2 x BS: the patch displacements of the block's faces
   int g = 0;
   while (g + 1 < eg.n && blockIdx.x >= eg.g[g + 1].block_start) ++g;
   const GroupDesc gd = eg.g[g];
@@ -1038,11 +1075,11 @@ __global__ void __launch_bounds__(BS, MINB) k_elements_df(DevBuf b, StepConst sc
   const double pr = pressure * __ldg(&b.pscale[i]);
   ElemOut o;
   if (gd.n_slots == 12)
-    o = element_force_df<12>(i, 12, slot0, sB, b, sc, pr, vol_p);
+    o = element_force_df<12>(i, 12, slot0, sB, b, sc, pr, vol_p, su);
   else if (gd.n_slots == 11)
-    o = element_force_df<11>(i, 11, slot0, sB, b, sc, pr, vol_p);
+    o = element_force_df<11>(i, 11, slot0, sB, b, sc, pr, vol_p, su);
   else
-    o = element_force_df<0>(i, gd.n_slots, slot0, sB, b, sc, pr, vol_p);
+    o = element_force_df<0>(i, gd.n_slots, slot0, sB, b, sc, pr, vol_p, su);
   const uint32_t e = __ldg(&b.perm[i]);
   b.area[e] = o.area;
   b.kG[e] = o.kg / o.area;
@@ -1780,6 +1817,39 @@ void launch_predict(const DevBuf& b, const StepConst& sc, int, cudaStream_t s) {
 void launch_positions(const DevBuf& b, const StepConst& sc, cudaStream_t s) {
   k_positions<<<nblk(sc.V), kBlock, 0, s>>>(b, sc);
 }
+
+// Control-block updates that the host would otherwise make by a read-modify-write
+// round trip: kCtlReset clears the run report (worst problem, counters, sums),
+// kCtlTable rewinds the pressure table to n entries, kCtlArm sets the pause
+// target n steps past the steps done.
+__global__ void k_ctl_begin(Ctl* ctl, uint32_t n, uint32_t flags) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  Ctl& h = *ctl;
+  if (flags & kCtlReset) {
+    h.steps_done = 0;
+    h.worst_problem = 0;
+    h.first_problem_step = 0;
+    h.halted = 0;
+    h.error = 0;
+    h.problem = 0;
+    h.n_rebuilds = 0;
+    h.rejections = 0;
+    h.paused = 0;
+    h.sum_pcav = h.sum_Nc_cav = h.sum_Ecav = 0;
+    h.steps_target = ~0u;
+    h.sum_dt = h.sum_area = h.sum_volume = h.sum_Nc = h.sum_Ekin = h.sum_Etens = h.sum_Ebend = h.sum_Eself =
+        h.sum_Efric = h.sum_kGauss = h.sum_kMean = 0;
+  }
+  if (flags & kCtlTable) {
+    h.table_pos = 0;
+    h.table_len = n;
+  }
+  if (flags & kCtlArm) {
+    h.steps_target = h.steps_done + n;
+    h.paused = 0;
+  }
+}
+void launch_ctl_begin(Ctl* ctl, uint32_t n, uint32_t flags, cudaStream_t s) { k_ctl_begin<<<1, 32, 0, s>>>(ctl, n, flags); }
 // launch shapes and arithmetic of the element kernels (see k_elements)
 const ElemVariant kElemVariants[kNumElemVariants] = {
     {256, 0, "fp64 256x1"},        {256, 1, "fp64 256x1 pair-G"}, {128, 1, "fp64 128x3 pair-G"},
@@ -1787,6 +1857,23 @@ const ElemVariant kElemVariants[kNumElemVariants] = {
     {256, 2, "fp64 256x1 df"},     {128, 2, "fp64 128x3 df"},     {64, 2, "fp64 64x6 df"},
     {64, 2, "fp64 64x8 df"},
     {256, 0, "fp32 256x2"},        {128, 0, "fp32 128x4"},        {64, 0, "fp32 64x8"}};
+
+// the double-float kernels take more than the default 48 KB of shared memory
+// (staging plus the basis table); called once per device before their first launch
+cudaError_t init_element_kernels() {
+  cudaError_t e = cudaSuccess;
+  auto set = [&](const void* f, int block) {
+    if (e != cudaSuccess) return;
+    e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)df_stage_bytes(block));
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(f, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
+  };
+  set((const void*)k_elements_df<256, 1>, 256);
+  set((const void*)k_elements_df<128, 3>, 128);
+  set((const void*)k_elements_df<64, 6>, 64);
+  set((const void*)k_elements_df<64, 8>, 64);
+  return e;
+}
 
 void launch_elements(const DevBuf& b, const StepConst& sc, const ElemLaunch& el, cudaStream_t s, bool totals) {
   const uint32_t nb = el.blocks;
@@ -1798,10 +1885,10 @@ void launch_elements(const DevBuf& b, const StepConst& sc, const ElemLaunch& el,
     case 3: k_elements<64, 5, true, false><<<nb, 64, 0, s>>>(b, sc, eg); break;
     case 4: k_elements<64, 6, true, false><<<nb, 64, 0, s>>>(b, sc, eg); break;
     case 5: k_elements<64, 5, false, false><<<nb, 64, 0, s>>>(b, sc, eg); break;
-    case 6: k_elements_df<256, 1><<<nb, 256, 0, s>>>(b, sc, eg); break;
-    case 7: k_elements_df<128, 3><<<nb, 128, 0, s>>>(b, sc, eg); break;
-    case 8: k_elements_df<64, 6><<<nb, 64, 0, s>>>(b, sc, eg); break;
-    case 9: k_elements_df<64, 8><<<nb, 64, 0, s>>>(b, sc, eg); break;
+    case 6: k_elements_df<256, 1><<<nb, 256, df_stage_bytes(256), s>>>(b, sc, eg); break;
+    case 7: k_elements_df<128, 3><<<nb, 128, df_stage_bytes(128), s>>>(b, sc, eg); break;
+    case 8: k_elements_df<64, 6><<<nb, 64, df_stage_bytes(64), s>>>(b, sc, eg); break;
+    case 9: k_elements_df<64, 8><<<nb, 64, df_stage_bytes(64), s>>>(b, sc, eg); break;
     case 10: k_elements32<256, 2><<<nb, 256, 0, s>>>(b, sc, eg); break;
     case 11: k_elements32<128, 4><<<nb, 128, 0, s>>>(b, sc, eg); break;
     default: k_elements32<64, 8><<<nb, 64, 0, s>>>(b, sc, eg); break;

@@ -304,8 +304,16 @@ class Shell:
         arrs = [None if x is None else np.ascontiguousarray(x, dtype=np.float64).reshape(-1) for x in (u, v, a)]
         return _check(self.lib.shl_set_state(self.h, *[_ptr(x) for x in arrs]), "shl_set_state", False)
 
-    def get_state(self):
-        u, v, a = (np.zeros(3 * self.V) for _ in range(3))
+    def get_state(self, out=None):
+        """Returns (u, v, a); with out=(u, v, a) (contiguous float64 arrays of 3 V values, e.g. views of
+        pinned host buffers) the state is copied into them."""
+        if out is None:
+            u, v, a = (np.zeros(3 * self.V) for _ in range(3))
+        else:
+            u, v, a = out
+            for x in out:
+                if x.dtype != np.float64 or x.size != 3 * self.V or not x.flags.c_contiguous:
+                    raise ValueError("get_state: out arrays must be contiguous float64 of %d values" % (3 * self.V))
         _check(self.lib.shl_get_state(self.h, u.ctypes.data, v.ctypes.data, a.ctypes.data), "shl_get_state", False)
         return u, v, a
 
