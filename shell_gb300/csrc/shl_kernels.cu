@@ -187,6 +187,10 @@ __device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
   const uint32_t d = (uint32_t)__cvta_generic_to_shared(smem);
   asm volatile("cp.async.ca.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(gmem) : "memory");
 }
+__device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
+  const uint32_t d = (uint32_t)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(gmem) : "memory");
+}
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
 // dynamic shared memory of the double-float element kernels: the displacements
@@ -835,7 +839,8 @@ __device__ __forceinline__ ElemOut element_force32(uint32_t i, int np_rt, uint32
 // derivatives from the hi/lo copy of u_pred.  No step subtracts nearly equal
 // quantities, so the forces carry a relative error of a few 1e-14 -- the
 // class of the FP64 path -- at FP32 instruction rates.  Shares are written as
-// FP64; the measurements are returned as FP64.
+// float pairs; the measurements are returned as FP64, E_tens, E_bend, kGauss
+// and kMean already divided by the area.
 template <int NP>
 __device__ __forceinline__ ElemOut element_force_df(uint32_t i, int np_rt, uint32_t slot0,
                                                     const double* __restrict__ B, const DevBuf& b,
@@ -893,7 +898,20 @@ __device__ __forceinline__ ElemOut element_force_df(uint32_t i, int np_rt, uint3
       for (int c = 0; c < 3; ++c) df_quick_two_sum(gh[k][c], gl[k][c], G[k][c].h, G[k][c].l);
   }
   const float* fd = b.face_df;
+  // constant row r (hi rows 0..37, lo rows 38..75) in component r % 4 of this
+  // thread's float4 entry r / 4 -- the entries that held its displacements
+  static_assert(2 * F32_COUNT <= 4 * 2 * kDfStageSlots, "face constants exceed the staging column");
+  float* sf = reinterpret_cast<float*>(su);
+  auto srow = [&](int r) -> float* { return &sf[4 * ((r >> 2) * bs + t) + (r & 3)]; };
+  if (NP > 0) {
+    // the displacements are consumed: the same entries now take the face's
+    // constants, all 76 rows in flight at once
+#pragma unroll
+    for (int r = 0; r < 2 * F32_COUNT; ++r) cp_async4(srow(r), &fd[(size_t)r * F + i]);
+    cp_async_wait_all();
+  }
   auto FC = [&](int fld) -> df2 {
+    if (NP > 0) return {*srow(fld), *srow(F32_COUNT + fld)};
     return {__ldg(&fd[(size_t)fld * F + i]), __ldg(&fd[(size_t)(F32_COUNT + fld) * F + i])};
   };
   const df2 R00 = FC(F32_R00), R01 = FC(F32_R01), R10 = FC(F32_R10), R11 = FC(F32_R11);
@@ -1021,14 +1039,17 @@ __device__ __forceinline__ ElemOut element_force_df(uint32_t i, int np_rt, uint3
   }
   ElemOut o;
   {
+    // per unit area, as stored (the area cancels from the curvatures): double-float
+    // quotients instead of four FP64 divisions per face on GB300's narrow FP64 pipe
     const df2 area = 0.5f * jac;
+    const df2 inv_area = df_recip(area);
     const df2 g0 = FC(F32_G0) + 2.f * al0, g1 = FC(F32_G1) + 2.f * al1, g2 = FC(F32_G2) + al2;
-    const df2 w_invdet = area * df_recip(g0 * g1 - g2 * g2);
-    o.etens = df_to_double(0.5f * (JxW * (n0 * al0 + n1 * al1 + n2 * al2)));
-    o.ebend = df_to_double(0.5f * (JxW * (m0 * be0 + m1 * be1 + m2 * be2)));
+    const df2 invdet = df_recip(g0 * g1 - g2 * g2);
+    o.etens = df_to_double((0.5f * (JxW * (n0 * al0 + n1 * al1 + n2 * al2))) * inv_area);
+    o.ebend = df_to_double((0.5f * (JxW * (m0 * be0 + m1 * be1 + m2 * be2))) * inv_area);
     o.area = df_to_double(area);
-    o.kg = df_to_double(w_invdet * (h0 * h1 - h2 * h2));
-    o.km = df_to_double(w_invdet * (0.5f * (h0 * g1 + h1 * g0 - 2.f * (h2 * g2))));
+    o.kg = df_to_double(invdet * (h0 * h1 - h2 * h2));
+    o.km = df_to_double(invdet * (0.5f * (h0 * g1 + h1 * g0 - 2.f * (h2 * g2))));
   }
   const uint32_t* spos = b.slot_pos + slot0;
 #pragma unroll 1
@@ -1081,11 +1102,11 @@ __global__ void __launch_bounds__(BS, MINB) k_elements_df(DevBuf b, StepConst sc
   else
     o = element_force_df<0>(i, gd.n_slots, slot0, sB, b, sc, pr, vol_p, su);
   const uint32_t e = __ldg(&b.perm[i]);
-  b.area[e] = o.area;
-  b.kG[e] = o.kg / o.area;
-  b.kM[e] = o.km / o.area;
-  b.etens[e] = o.etens / o.area;
-  b.ebend[e] = o.ebend / o.area;
+  b.area[e] = o.area;  // the other fields come per unit area
+  b.kG[e] = o.kg;
+  b.kM[e] = o.km;
+  b.etens[e] = o.etens;
+  b.ebend[e] = o.ebend;
 }
 
 template <int BS, int MINB>
