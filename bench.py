@@ -41,10 +41,11 @@ from shell_gb300.workloads import (ALPHA, AMPL, DT, G12, MU, NU12, RAMP_STEPS, R
                                    classical_pressure, pressure, squashed_state, workload)
 
 FLUSH_BYTES = 512 << 20
-# library kernels per step with self-contact: predictor, two rebuild-condition kernels (the IF nodes'
-# conditions), element kernel, contact force, gather/corrector, volume/measurement totals/end of step;
-# plus the 27 kernels of each candidate-list rebuild that runs (10 pipeline + 3 x 3 scan + 8 contact CSR)
-LAUNCHES_PER_STEP_CONTACT = 7
+# library kernels per step with self-contact: predictor, element kernel, contact force,
+# gather/corrector, volume/measurement totals/end of step (predictor and corrector set the
+# conditions of the two rebuild IF nodes themselves); plus the 27 kernels of each
+# candidate-list rebuild that runs (10 pipeline + 3 x 3 scan + 8 contact CSR)
+LAUNCHES_PER_STEP_CONTACT = 5
 LAUNCHES_PER_REBUILD = 27
 # element kernel (double-float FP64 path): per-face constants as float pairs
 # (38 fields x 8 B), patch ids, force shares (float pairs), element fields,

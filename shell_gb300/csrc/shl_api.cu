@@ -273,9 +273,10 @@ void estimate_cells(const Setup& S, const shl_params& p, uint64_t& n_cells, uint
 }
 
 // A linked-cell pass inside a graph capture: an IF node whose body is the
-// rebuild pipeline, its condition set on the device from ctl->rebuild, so steps
-// without a rebuild launch one 1-thread kernel instead of the whole pipeline.
-cudaError_t capture_conditional_rebuild(shl_ctx* c) {
+// rebuild pipeline.  Its condition handle is created first and handed to the
+// kernel that decides the rebuild (predictor, corrector), whose last block sets
+// it from ctl->rebuild, so steps without a rebuild launch no extra kernel.
+cudaError_t rebuild_cond_create(shl_ctx* c, RebuildCond* rc) {
   cudaStreamCaptureStatus st;
   cudaGraph_t g = nullptr;
   const cudaGraphNode_t* deps = nullptr;
@@ -283,14 +284,22 @@ cudaError_t capture_conditional_rebuild(shl_ctx* c) {
   size_t nd = 0;
   cudaError_t e = cudaStreamGetCaptureInfo(c->stream, &st, nullptr, &g, &deps, &edges, &nd);
   if (e != cudaSuccess) return e;
-  cudaGraphConditionalHandle h;
-  e = cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault);
+  e = cudaGraphConditionalHandleCreate(&rc->h, g, 0, cudaGraphCondAssignDefault);
   if (e != cudaSuccess) return e;
-  launch_set_rebuild_cond(h, c->b.ctl, c->stream);
-  e = cudaStreamGetCaptureInfo(c->stream, &st, nullptr, &g, &deps, &edges, &nd);
+  rc->has = 1;
+  return cudaSuccess;
+}
+
+cudaError_t rebuild_if_node(shl_ctx* c, const RebuildCond& rc) {
+  cudaStreamCaptureStatus st;
+  cudaGraph_t g = nullptr;
+  const cudaGraphNode_t* deps = nullptr;
+  const cudaGraphEdgeData* edges = nullptr;
+  size_t nd = 0;
+  cudaError_t e = cudaStreamGetCaptureInfo(c->stream, &st, nullptr, &g, &deps, &edges, &nd);
   if (e != cudaSuccess) return e;
   cudaGraphNodeParams cp = {cudaGraphNodeTypeConditional};
-  cp.conditional.handle = h;
+  cp.conditional.handle = rc.h;
   cp.conditional.type = cudaGraphCondTypeIf;
   cp.conditional.size = 1;
   cudaGraphNode_t node;
@@ -305,8 +314,11 @@ cudaError_t capture_conditional_rebuild(shl_ctx* c) {
   return cudaStreamUpdateCaptureDependencies(c->stream, &node, nullptr, 1, cudaStreamSetCaptureDependencies);
 }
 
-cudaError_t enqueue_rebuild(shl_ctx* c, bool capturing) {
-  if (capturing && c->conditional_ok) return capture_conditional_rebuild(c);
+// the linked-cell pass after the kernel that decided it: an IF node in a graph
+// with conditional nodes, else the pipeline itself (its kernels return at once
+// when no rebuild is due)
+cudaError_t enqueue_rebuild(shl_ctx* c, const RebuildCond& rc) {
+  if (rc.has) return rebuild_if_node(c, rc);
   launch_rebuild(c->b, c->sc, c->stream);
   return cudaSuccess;
 }
@@ -316,18 +328,22 @@ cudaError_t enqueue_step(shl_ctx* c, bool capturing = false) {
   const StepConst& sc = c->sc;
   cudaStream_t s = c->stream;
   cudaError_t e = cudaSuccess;
-  launch_predict(b, sc, 0, s);
-  if (sc.contact && (e = enqueue_rebuild(c, capturing)) != cudaSuccess) return e;
+  const bool cond = capturing && c->conditional_ok && sc.contact;
+  RebuildCond r1{0, 0}, r2{0, 0};
+  if (cond && (e = rebuild_cond_create(c, &r1)) != cudaSuccess) return e;
+  launch_predict(b, sc, r1, s);
+  if (sc.contact && (e = enqueue_rebuild(c, r1)) != cudaSuccess) return e;
   launch_elements(b, sc, elem_launch(c, sc), s, false);  // totals in k_volume_end
   if (sc.contact) launch_contact_force(b, sc, 0, s);
+  if (cond && (e = rebuild_cond_create(c, &r2)) != cudaSuccess) return e;
   if (sc.adapt_every) {
     // one attempt: estimate, then correct only if accepted (ShellSystem.C:1010-1117)
     launch_gather_correct(b, sc, 2, false, nullptr, nullptr, s);
-    launch_correct_adapt(b, sc, s);
+    launch_correct_adapt(b, sc, s, r2);
   } else {
-    launch_gather_correct(b, sc, 0, true, nullptr, nullptr, s);
+    launch_gather_correct(b, sc, 0, true, nullptr, nullptr, s, r2);
   }
-  if (sc.contact && (e = enqueue_rebuild(c, capturing)) != cudaSuccess) return e;
+  if (sc.contact && (e = enqueue_rebuild(c, r2)) != cudaSuccess) return e;
   launch_volume_end_step(b, sc, true, s);
   return cudaSuccess;
 }
@@ -1301,7 +1317,7 @@ shl_status shl_profile_step(shl_ctx* c, double pressure, size_t flush_bytes, dou
   cudaStream_t s = c->stream;
   if (flush_bytes) launch_flush(c->d_flush, flush_bytes, 7u, s);
   cudaEventRecord(ev[0], s);
-  launch_predict(b, sc, 0, s);
+  launch_predict(b, sc, RebuildCond{0, 0}, s);
   cudaEventRecord(ev[1], s);
   if (sc.contact) launch_rebuild(b, sc, s);
   cudaEventRecord(ev[2], s);

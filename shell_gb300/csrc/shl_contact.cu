@@ -689,16 +689,7 @@ __global__ void k_csr_finish(DevBuf b) {
 
 inline uint32_t nblk(uint32_t n, uint32_t bs = kBlock) { return n == 0 ? 1 : (n + bs - 1) / bs; }
 
-// condition of the graph's IF node around a linked-cell pass
-__global__ void k_set_rebuild_cond(cudaGraphConditionalHandle h, const Ctl* ctl) {
-  cudaGraphSetConditional(h, (ctl->rebuild != 0 && ctl->halted == 0) ? 1u : 0u);
-}
-
 }  // namespace
-
-void launch_set_rebuild_cond(cudaGraphConditionalHandle h, const Ctl* ctl, cudaStream_t s) {
-  k_set_rebuild_cond<<<1, 1, 0, s>>>(h, ctl);
-}
 
 void launch_contact_csr(const DevBuf& b, const StepConst& sc, cudaStream_t s) {
   const uint32_t gV = nblk(sc.V);

@@ -275,13 +275,20 @@ __device__ __forceinline__ void smooth_pair(const DevBuf& b, const StepConst& sc
 #endif
 
 // ---- launchers (shl_kernels.cu) ----
-void launch_predict(const DevBuf& b, const StepConst& sc, int cur, cudaStream_t s);
+// The condition of a graph IF node around a linked-cell pass, set to
+// (ctl->rebuild && !ctl->halted) by the last block of the kernel that decides
+// the rebuild (has = 0: launched outside a graph, or no IF node follows).
+struct RebuildCond {
+  cudaGraphConditionalHandle h;
+  int has;
+};
+void launch_predict(const DevBuf& b, const StepConst& sc, RebuildCond rc, cudaStream_t s);
 // totals: also the fixed-order sums of the per-face measurements (k_elem_totals);
 // k_volume_end forms them too, so launches followed by it pass false
 void launch_elements(const DevBuf& b, const StepConst& sc, const ElemLaunch& el, cudaStream_t s, bool totals = true);
 void launch_contact_force(const DevBuf& b, const StepConst& sc, int cur, cudaStream_t s);
 void launch_gather_correct(const DevBuf& b, const StepConst& sc, int cur, bool correct, double* f_out,
-                           double* a_out, cudaStream_t s);
+                           double* a_out, cudaStream_t s, RebuildCond rc = {0, 0});
 void launch_volume_end_step(const DevBuf& b, const StepConst& sc, bool end_step, cudaStream_t s);
 void launch_positions(const DevBuf& b, const StepConst& sc, cudaStream_t s);
 cudaError_t init_element_kernels();
@@ -296,7 +303,7 @@ void launch_shell_norms(const double* f, const double* fext, const double* mass,
                         uint32_t n_shells, double* out, cudaStream_t s);
 void launch_defect(const double* f64, const double* f32, size_t n, double* out, cudaStream_t s);
 void launch_eval_program(const void* prog, int n, const double* t, int m, double* out, cudaStream_t s);
-void launch_correct_adapt(const DevBuf& b, const StepConst& sc, cudaStream_t s);
+void launch_correct_adapt(const DevBuf& b, const StepConst& sc, cudaStream_t s, RebuildCond rc = {0, 0});
 void launch_flush(void* buf, size_t bytes, uint32_t tag, cudaStream_t s);
 
 // ---- launchers (shl_contact.cu) ----
@@ -305,8 +312,6 @@ void launch_flush(void* buf, size_t bytes, uint32_t tag, cudaStream_t s);
 // (every kernel returns at once otherwise), so it can sit in a CUDA graph.
 // The list lives in buffer 0; buffer 1 is scratch.
 void launch_rebuild(const DevBuf& b, const StepConst& sc, cudaStream_t s);
-// Sets an IF node's condition to (ctl->rebuild && !ctl->halted) inside a graph.
-void launch_set_rebuild_cond(cudaGraphConditionalHandle h, const Ctl* ctl, cudaStream_t s);
 // Rebuild the per-node contact CSR when ctl->csr_dirty is set.
 void launch_contact_csr(const DevBuf& b, const StepConst& sc, cudaStream_t s);
 

@@ -35,6 +35,11 @@ __device__ __forceinline__ bool inactive(const Ctl* ctl) {
   return ctl->halted != 0 || ctl->paused != 0;
 }
 
+// the rebuild IF node's condition (one thread, after ctl->rebuild is final)
+__device__ __forceinline__ void set_rebuild_cond(const RebuildCond& rc, const Ctl* ctl) {
+  if (rc.has) cudaGraphSetConditional(rc.h, (ctl->rebuild != 0 && ctl->halted == 0) ? 1u : 0u);
+}
+
 // ShellSystem::set_newmark_parameters (ShellSystem.C:744-759) with the bounds
 // of ShellSystem.C:306-310, into the control block (adaptive dt)
 __device__ void set_newmark(Ctl* ctl, const StepConst& sc, double new_dt) {
@@ -334,9 +339,12 @@ void launch_eval_program(const void* prog, int n, const double* t, int m, double
 
 // ------------------------------------------------------------ predictor --
 // u_pred = u + dt v + a8 a ; v_pred = v + a6 a ; p = X + u_pred ; du_max
-__global__ void __launch_bounds__(kBlock) k_predict(DevBuf b, StepConst sc) {
+__global__ void __launch_bounds__(kBlock) k_predict(DevBuf b, StepConst sc, RebuildCond rc) {
   Ctl* ctl = b.ctl;
-  if (inactive(ctl)) return;
+  if (inactive(ctl)) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) set_rebuild_cond(rc, ctl);
+    return;
+  }
   __shared__ double sh[kBlock / 32];
   const uint32_t n = blockIdx.x * blockDim.x + threadIdx.x;
   const double dt = sc.adapt_every ? ctl->dt_cur : sc.dt;
@@ -409,6 +417,7 @@ __global__ void __launch_bounds__(kBlock) k_predict(DevBuf b, StepConst sc) {
     register_problem(ctl, SHL_NOT_FINITE);
   }
   ctl->rebuild = (sc.contact && ctl->du_sum >= rebuild_tolerance(sc, ctl)) ? 1u : 0u;
+  set_rebuild_cond(rc, ctl);
 }
 
 // positions only (p = X + u_pred), for force evaluations at a given state
@@ -1341,10 +1350,13 @@ __device__ void cavity_totals(const DevBuf& b, const StepConst& sc, Ctl* ctl, do
 }
 
 __global__ void __launch_bounds__(kBlock) k_gather_correct(DevBuf b, StepConst sc, int mode, double* f_out,
-                                                           double* a_out) {
+                                                           double* a_out, RebuildCond rc) {
   // mode 0: eval (write f_out / a_out), mode 1: step corrector
   Ctl* ctl = b.ctl;
-  if (inactive(ctl)) return;
+  if (inactive(ctl)) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) set_rebuild_cond(rc, ctl);
+    return;
+  }
   __shared__ double sh[kBlock / 32];
   const uint32_t n = blockIdx.x * blockDim.x + threadIdx.x;
   double du2 = 0.0, ekin = 0.0;
@@ -1611,13 +1623,17 @@ __global__ void __launch_bounds__(kBlock) k_gather_correct(DevBuf b, StepConst s
   }
   if (!isfinite(ekt)) register_problem(ctl, SHL_NOT_FINITE);
   ctl->rebuild = (sc.contact && ctl->du_sum >= rebuild_tolerance(sc, ctl)) ? 1u : 0u;
+  set_rebuild_cond(rc, ctl);
 }
 
 // corrector of an accepted adaptive attempt (ShellSystem.C:1046-1101): u, v, a
 // from the stored a_pred; check_increment(true); contact-list flag
-__global__ void __launch_bounds__(kBlock) k_correct_adapt(DevBuf b, StepConst sc) {
+__global__ void __launch_bounds__(kBlock) k_correct_adapt(DevBuf b, StepConst sc, RebuildCond rc) {
   Ctl* ctl = b.ctl;
-  if (inactive(ctl) || !ctl->accept) return;
+  if (inactive(ctl) || !ctl->accept) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) set_rebuild_cond(rc, ctl);
+    return;
+  }
   __shared__ double sh[kBlock / 32];
   const uint32_t n = blockIdx.x * blockDim.x + threadIdx.x;
   const double nm0 = ctl->nm[0], nm7 = ctl->nm[7];
@@ -1670,6 +1686,7 @@ __global__ void __launch_bounds__(kBlock) k_correct_adapt(DevBuf b, StepConst sc
   }
   if (!isfinite(ekt)) register_problem(ctl, SHL_NOT_FINITE);
   ctl->rebuild = (sc.contact && ctl->du_sum >= rebuild_tolerance(sc, ctl)) ? 1u : 0u;
+  set_rebuild_cond(rc, ctl);
 }
 
 // ------------------------------------------------------ volume, end step --
@@ -1832,8 +1849,8 @@ void launch_flush(void* buf, size_t bytes, uint32_t tag, cudaStream_t s) {
 // --------------------------------------------------------------- launch --
 static inline uint32_t nblk(uint32_t n) { return (n + kBlock - 1) / kBlock; }
 
-void launch_predict(const DevBuf& b, const StepConst& sc, int, cudaStream_t s) {
-  k_predict<<<nblk(sc.V), kBlock, 0, s>>>(b, sc);
+void launch_predict(const DevBuf& b, const StepConst& sc, RebuildCond rc, cudaStream_t s) {
+  k_predict<<<nblk(sc.V), kBlock, 0, s>>>(b, sc, rc);
 }
 void launch_positions(const DevBuf& b, const StepConst& sc, cudaStream_t s) {
   k_positions<<<nblk(sc.V), kBlock, 0, s>>>(b, sc);
@@ -1927,11 +1944,11 @@ void launch_contact_force(const DevBuf& b, const StepConst& sc, int, cudaStream_
 }
 // mode 2: an adaptive attempt (a_pred and the error estimate); else correct ? step corrector : evaluation
 void launch_gather_correct(const DevBuf& b, const StepConst& sc, int mode, bool correct, double* f_out, double* a_out,
-                           cudaStream_t s) {
-  k_gather_correct<<<nblk(sc.V), kBlock, 0, s>>>(b, sc, mode == 2 ? 2 : (correct ? 1 : 0), f_out, a_out);
+                           cudaStream_t s, RebuildCond rc) {
+  k_gather_correct<<<nblk(sc.V), kBlock, 0, s>>>(b, sc, mode == 2 ? 2 : (correct ? 1 : 0), f_out, a_out, rc);
 }
-void launch_correct_adapt(const DevBuf& b, const StepConst& sc, cudaStream_t s) {
-  k_correct_adapt<<<(sc.V + kBlock - 1) / kBlock, kBlock, 0, s>>>(b, sc);
+void launch_correct_adapt(const DevBuf& b, const StepConst& sc, cudaStream_t s, RebuildCond rc) {
+  k_correct_adapt<<<(sc.V + kBlock - 1) / kBlock, kBlock, 0, s>>>(b, sc, rc);
 }
 
 void launch_volume_end_step(const DevBuf& b, const StepConst& sc, bool end_step, cudaStream_t s) {
