@@ -60,6 +60,10 @@ struct shl_ctx {
   std::vector<void*> allocs;
   cudaGraphExec_t graph = nullptr;
   cudaGraphExec_t graph1 = nullptr;
+  // The graphs run fused steps (fixed dt): each corrector also predicts the next
+  // step.  pred_valid: the device holds that prediction for the current state
+  // (set by graph steps, cleared by every entry point that may change the state)
+  bool pred_valid = false;
   double* h_pin = nullptr;  // pinned staging buffer, 3V doubles x 3
   Ctl* h_ctl = nullptr;     // pinned copy of the device control block
   double* h_table = nullptr;  // pinned staging of the pressure table (kTableCap doubles)
@@ -290,7 +294,7 @@ cudaError_t rebuild_cond_create(shl_ctx* c, RebuildCond* rc) {
   return cudaSuccess;
 }
 
-cudaError_t rebuild_if_node(shl_ctx* c, const RebuildCond& rc) {
+cudaError_t rebuild_if_node(shl_ctx* c, const RebuildCond& rc, const DevBuf& b) {
   cudaStreamCaptureStatus st;
   cudaGraph_t g = nullptr;
   const cudaGraphNode_t* deps = nullptr;
@@ -308,7 +312,7 @@ cudaError_t rebuild_if_node(shl_ctx* c, const RebuildCond& rc) {
   cudaGraph_t body = cp.conditional.phGraph_out[0];
   e = cudaStreamBeginCaptureToGraph(c->side, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed);
   if (e != cudaSuccess) return e;
-  launch_rebuild(c->b, c->sc, c->side);
+  launch_rebuild(b, c->sc, c->side);
   e = cudaStreamEndCapture(c->side, &body);
   if (e != cudaSuccess) return e;
   return cudaStreamUpdateCaptureDependencies(c->stream, &node, nullptr, 1, cudaStreamSetCaptureDependencies);
@@ -316,34 +320,45 @@ cudaError_t rebuild_if_node(shl_ctx* c, const RebuildCond& rc) {
 
 // the linked-cell pass after the kernel that decided it: an IF node in a graph
 // with conditional nodes, else the pipeline itself (its kernels return at once
-// when no rebuild is due)
-cudaError_t enqueue_rebuild(shl_ctx* c, const RebuildCond& rc) {
-  if (rc.has) return rebuild_if_node(c, rc);
-  launch_rebuild(c->b, c->sc, c->stream);
+// when no rebuild is due); b.p = the positions it works on
+cudaError_t enqueue_rebuild(shl_ctx* c, const RebuildCond& rc, const DevBuf& b) {
+  if (rc.has) return rebuild_if_node(c, rc, b);
+  launch_rebuild(b, c->sc, c->stream);
   return cudaSuccess;
 }
 
-cudaError_t enqueue_step(shl_ctx* c, bool capturing = false) {
+bool fused_steps(const shl_ctx* c) { return c->sc.adapt_every == 0; }
+
+// One step.  fused (graphs, fixed dt): the step opens with k_begin_step, its
+// nodes having been predicted by the previous corrector (or k_predict with
+// nodes_only), reads the predicted positions from b.pn and predicts the next
+// step in its corrector; otherwise the predictor opens the step.
+cudaError_t enqueue_step(shl_ctx* c, bool capturing = false, bool fused = false) {
   const DevBuf& b = c->b;
   const StepConst& sc = c->sc;
   cudaStream_t s = c->stream;
   cudaError_t e = cudaSuccess;
   const bool cond = capturing && c->conditional_ok && sc.contact;
+  DevBuf bp = b;  // the step's predicted positions
+  if (fused) bp.p = b.pn;
   RebuildCond r1{0, 0}, r2{0, 0};
   if (cond && (e = rebuild_cond_create(c, &r1)) != cudaSuccess) return e;
-  launch_predict(b, sc, r1, s);
-  if (sc.contact && (e = enqueue_rebuild(c, r1)) != cudaSuccess) return e;
+  if (fused)
+    launch_begin_step(b, sc, r1, s);
+  else
+    launch_predict(b, sc, r1, s);
+  if (sc.contact && (e = enqueue_rebuild(c, r1, bp)) != cudaSuccess) return e;
   launch_elements(b, sc, elem_launch(c, sc), s, false);  // totals in k_volume_end
-  if (sc.contact) launch_contact_force(b, sc, 0, s);
+  if (sc.contact) launch_contact_force(bp, sc, 0, s);
   if (cond && (e = rebuild_cond_create(c, &r2)) != cudaSuccess) return e;
   if (sc.adapt_every) {
     // one attempt: estimate, then correct only if accepted (ShellSystem.C:1010-1117)
     launch_gather_correct(b, sc, 2, false, nullptr, nullptr, s);
     launch_correct_adapt(b, sc, s, r2);
   } else {
-    launch_gather_correct(b, sc, 0, true, nullptr, nullptr, s, r2);
+    launch_gather_correct(b, sc, fused ? 3 : 0, true, nullptr, nullptr, s, r2);
   }
-  if (sc.contact && (e = enqueue_rebuild(c, r2)) != cudaSuccess) return e;
+  if (sc.contact && (e = enqueue_rebuild(c, r2, b)) != cudaSuccess) return e;
   launch_volume_end_step(b, sc, true, s);
   return cudaSuccess;
 }
@@ -353,7 +368,7 @@ shl_status build_graph(shl_ctx* c, uint32_t steps, cudaGraphExec_t* out) {
     cudaGraph_t g = nullptr;
     SHL_CUDA_TRY(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
     cudaError_t e = cudaSuccess;
-    for (uint32_t i = 0; i < steps && e == cudaSuccess; ++i) e = enqueue_step(c, true);
+    for (uint32_t i = 0; i < steps && e == cudaSuccess; ++i) e = enqueue_step(c, true, fused_steps(c));
     cudaError_t e2 = cudaStreamEndCapture(c->stream, &g);
     if (e == cudaSuccess) e = e2;
     if (e == cudaSuccess) e = cudaGraphInstantiate(out, g, 0);
@@ -508,7 +523,7 @@ shl_status create_common(shl_ctx* c, const std::vector<double>& pscale_orig, shl
   const size_t nd = 3 * (size_t)V;
 #define ALLOC(ptr, n) do { if ((st = dev_alloc(c, &(ptr), (n))) != SHL_OK) return fail(st); } while (0)
   ALLOC(b.X, nd); ALLOC(b.u, nd); ALLOC(b.v, nd); ALLOC(b.a, nd); ALLOC(b.up, nd); ALLOC(b.vp, nd);
-  ALLOC(b.p, nd); ALLOC(b.Minv, nd); ALLOC(b.C, nd); ALLOC(b.M, nd);
+  ALLOC(b.p, nd); ALLOC(b.Minv, nd); ALLOC(b.C, nd); ALLOC(b.M, nd); ALLOC(b.pn, nd);
   ALLOC(b.upk, 2 * (size_t)S.V);
   if (params->adapt_dt_every) ALLOC(b.ap, nd);
   if (params->shell_cavity_contact) {
@@ -857,6 +872,7 @@ shl_status shl_batch_layout(shl_ctx* c, uint32_t* n_shells, uint32_t* node_offse
 
 shl_status shl_set_state(shl_ctx* c, const double* u, const double* v, const double* a) {
   if (!c) return SHL_ERR_ARG;
+  c->pred_valid = false;  // may change what the step prediction was made from
   const size_t nd = 3 * (size_t)c->S.V;
   if (u) {
     SHL_TRY(upload(c, c->b.u, u, nd));
@@ -881,6 +897,7 @@ shl_status shl_get_state(shl_ctx* c, double* u, double* v, double* a) {
 
 shl_status shl_set_time(shl_ctx* c, double t, uint32_t step) {
   if (!c) return SHL_ERR_ARG;
+  c->pred_valid = false;  // may change what the step prediction was made from
   Ctl h;
   SHL_TRY(ctl_get(c, h));
   h.time = t;
@@ -947,6 +964,7 @@ extern "C" {
 shl_status shl_eval_forces(shl_ctx* c, const double* u_pred, const double* v_pred, double pressure, double* f_out,
                            double* a_out, shl_energies* e) {
   if (!c || !u_pred || !v_pred) return SHL_ERR_ARG;
+  c->pred_valid = false;  // may change what the step prediction was made from
   const size_t nd = 3 * (size_t)c->S.V;
   SHL_TRY(upload(c, c->b.up, u_pred, nd));
   SHL_TRY(upload(c, c->b.vp, v_pred, nd));
@@ -991,6 +1009,7 @@ shl_status initial_state(shl_ctx* c, Ctl& h) {
 
 shl_status shl_apply_initial_conditions(shl_ctx* c, const double* u0, double t0, double pressure_next) {
   if (!c || !u0) return SHL_ERR_ARG;
+  c->pred_valid = false;  // may change what the step prediction was made from
   const size_t nd = 3 * (size_t)c->S.V;
   SHL_TRY(upload(c, c->b.u, u0, nd));
   SHL_TRY(upload(c, c->b.up, u0, nd));
@@ -1019,6 +1038,7 @@ shl_status shl_apply_initial_conditions(shl_ctx* c, const double* u0, double t0,
 
 shl_status shl_apply_loaded_state(shl_ctx* c) {
   if (!c) return SHL_ERR_ARG;
+  c->pred_valid = false;  // may change what the step prediction was made from
   Ctl h;
   return initial_state(c, h);
 }
@@ -1038,13 +1058,21 @@ shl_status ensure_graphs(shl_ctx* c) {
 }
 
 shl_status enqueue_steps(shl_ctx* c, uint32_t n, bool use_graph) {
+  if (n == 0) return SHL_OK;
   if (use_graph) {
     SHL_TRY(ensure_graphs(c));
+    if (fused_steps(c) && !c->pred_valid) {
+      DevBuf bp = c->b;
+      bp.p = c->b.pn;
+      launch_predict(bp, c->sc, RebuildCond{0, 0}, c->stream, true);
+    }
     uint32_t k = 0;
     for (; k + kGraphSteps <= n; k += kGraphSteps) SHL_CUDA_TRY(cudaGraphLaunch(c->graph, c->stream));
     for (; k < n; ++k) SHL_CUDA_TRY(cudaGraphLaunch(c->graph1, c->stream));
+    c->pred_valid = fused_steps(c);
   } else {
     for (uint32_t k = 0; k < n; ++k) enqueue_step(c);
+    c->pred_valid = false;
   }
   return check_launch("step");
 }
@@ -1094,6 +1122,7 @@ shl_status collect(shl_ctx* c, shl_step_report* report, const Ctl* fresh = nullp
   }
   const int err = h.error;
   const int worst = h.worst_problem;
+  if (h.halted || h.error) c->pred_valid = false;  // the run stopped inside a step
   SHL_TRY(reset_report(c));
   if (err) {
     g_err = "device buffer capacity exceeded (contact pairs / linked cells)";
@@ -1193,6 +1222,7 @@ shl_status shl_get_cavity_origins(shl_ctx* c, double* origins) {
 
 shl_status shl_set_cavity_origins(shl_ctx* c, const double* origins) {
   if (!c || !origins) return SHL_ERR_ARG;
+  c->pred_valid = false;  // may change what the step prediction was made from
   if (!c->b.cav_origin) return SHL_OK;  // nothing to keep without cavity contact
   SHL_TRY(upload(c, c->b.cav_origin, origins, 3 * (size_t)c->S.V));
   SHL_CUDA_TRY(cudaStreamSynchronize(c->stream));
@@ -1302,6 +1332,7 @@ shl_status shl_time_kernel(shl_ctx* c, int which, int reps, size_t flush_bytes, 
 
 shl_status shl_profile_step(shl_ctx* c, double pressure, size_t flush_bytes, double* ms_out) {
   if (!c || !ms_out) return SHL_ERR_ARG;
+  c->pred_valid = false;  // may change what the step prediction was made from
   if (flush_bytes > c->flush_bytes) {
     if (c->d_flush) cudaFree(c->d_flush);
     c->d_flush = nullptr;
@@ -1419,6 +1450,7 @@ shl_status shl_get_contact_coords(shl_ctx* c, double* x, size_t cap, size_t* n_p
 
 shl_status shl_set_contact_coords(shl_ctx* c, const double* x, size_t n) {
   if (!c || (n && !x)) return SHL_ERR_ARG;
+  c->pred_valid = false;  // may change what the step prediction was made from
   if (!c->sc.smooth) { g_err = "closest-point coordinates are kept for SMOOTH contact only"; return SHL_ERR_ARG; }
   Ctl h;
   SHL_TRY(ctl_get(c, h));
@@ -1431,6 +1463,7 @@ shl_status shl_set_contact_coords(shl_ctx* c, const double* x, size_t n) {
 shl_status shl_set_contact_state(shl_ctx* c, const uint32_t* pairs, const uint8_t* stick, const double* spring_origin,
                                  const double* d2, size_t n, double du_sum) {
   if (!c) return SHL_ERR_ARG;
+  c->pred_valid = false;  // may change what the step prediction was made from
   if (!c->sc.contact) { g_err = "self-contact is off"; return SHL_ERR_ARG; }
   if (n > c->sc.pairs_cap) { g_err = "too many pairs"; return SHL_ERR_CAPACITY; }
   const uint32_t F = c->S.F;
@@ -1485,6 +1518,7 @@ shl_status shl_set_contact_state(shl_ctx* c, const uint32_t* pairs, const uint8_
 
 shl_status shl_rebuild_contacts(shl_ctx* c) {
   if (!c) return SHL_ERR_ARG;
+  c->pred_valid = false;  // may change what the step prediction was made from
   if (!c->sc.contact) return SHL_OK;
   Ctl h;
   SHL_TRY(ctl_get(c, h));
@@ -1512,6 +1546,7 @@ shl_status shl_get_element_fields(shl_ctx* c, double* kG, double* kM, double* et
 
 shl_status shl_residual(shl_ctx* c, double pressure, int flags, double* rel, double* f2, double* fext2) {
   if (!c) return SHL_ERR_ARG;
+  c->pred_valid = false;  // may change what the step prediction was made from
   const size_t nd = 3 * (size_t)c->S.V;
   const uint32_t ns = (uint32_t)c->node_off.size() - 1;
   const bool ctx32 = c->sc.fp32 != 0;
@@ -1771,6 +1806,7 @@ shl_status shl_get_element_variant(shl_ctx* c, int* variant, char* name, size_t 
 
 shl_status shl_scale_damping(shl_ctx* c, double factor) {
   if (!c || !(factor >= 0)) return SHL_ERR_ARG;
+  c->pred_valid = false;  // may change what the step prediction was made from
   const size_t nd = 3 * (size_t)c->S.V;
   std::vector<double> C(nd);
   for (size_t i = 0; i < nd; ++i) C[i] = factor * c->S.C[i];
@@ -1790,6 +1826,7 @@ shl_status shl_get_mass_damping(shl_ctx* c, double* Minv, double* C) {
 shl_status shl_internal_force_noalloc(shl_ctx* c, const double* u_dev, double pressure, double* f_dev,
                                       void* stream) {
   if (!c || !u_dev || !f_dev) { g_err = "null argument"; return SHL_ERR_ARG; }
+  c->pred_valid = false;  // may change what the step prediction was made from
   if (c->sc.contact || c->P.bulk_modulus != 0.0 || c->sc.fp32) {
     g_err = "shl_internal_force_noalloc: self-contact, bulk-modulus pressure and FP32 element forces are not "
             "evaluated here";

@@ -93,6 +93,7 @@ struct Ctl {
   uint32_t first_problem_step;
   // linked cells / contact
   double du_sum;
+  double du2_pred;         // largest |u_pred - u|^2 of the prediction made ahead (fused steps)
   double avg_elem_size;
   double cell_size, d_max, d2_max;
   double bmin[3], bmax[3];
@@ -182,6 +183,7 @@ struct StepConst {
 struct DevBuf {
   double *X, *u, *v, *a, *up, *vp, *p, *Minv, *C;
   double* M;          // 3V lumped masses (1 / Minv), for the kinetic energy
+  double* pn;         // 3V predicted positions of fused steps (written by the previous step's corrector)
   double* ap;         // 3V predicted acceleration of an adaptive attempt (adaptive dt only)
   double* cav_origin; // 3V static-friction spring origins of the cavity contacts (cavity contact only)
   double* cav_ecav;   // V cavity-contact energy density of the last step
@@ -282,12 +284,18 @@ struct RebuildCond {
   cudaGraphConditionalHandle h;
   int has;
 };
-void launch_predict(const DevBuf& b, const StepConst& sc, RebuildCond rc, cudaStream_t s);
+// nodes_only: the predicted state and its largest |du|^2 (ctl->du2_pred) without
+// the step's scalar start, which k_begin_step then makes (fused steps)
+void launch_predict(const DevBuf& b, const StepConst& sc, RebuildCond rc, cudaStream_t s, bool nodes_only = false);
+void launch_begin_step(const DevBuf& b, const StepConst& sc, RebuildCond rc, cudaStream_t s);
 // totals: also the fixed-order sums of the per-face measurements (k_elem_totals);
 // k_volume_end forms them too, so launches followed by it pass false
 void launch_elements(const DevBuf& b, const StepConst& sc, const ElemLaunch& el, cudaStream_t s, bool totals = true);
 void launch_contact_force(const DevBuf& b, const StepConst& sc, int cur, cudaStream_t s);
-void launch_gather_correct(const DevBuf& b, const StepConst& sc, int cur, bool correct, double* f_out,
+// mode 2: adaptive attempt; mode 3: corrector fused with the next step's prediction
+// (reads the step's predicted positions from b.pn and writes the next ones there);
+// otherwise correct ? corrector : evaluation
+void launch_gather_correct(const DevBuf& b, const StepConst& sc, int mode, bool correct, double* f_out,
                            double* a_out, cudaStream_t s, RebuildCond rc = {0, 0});
 void launch_volume_end_step(const DevBuf& b, const StepConst& sc, bool end_step, cudaStream_t s);
 void launch_positions(const DevBuf& b, const StepConst& sc, cudaStream_t s);

@@ -338,58 +338,48 @@ void launch_eval_program(const void* prog, int n, const double* t, int m, double
 }
 
 // ------------------------------------------------------------ predictor --
-// u_pred = u + dt v + a8 a ; v_pred = v + a6 a ; p = X + u_pred ; du_max
-__global__ void __launch_bounds__(kBlock) k_predict(DevBuf b, StepConst sc, RebuildCond rc) {
-  Ctl* ctl = b.ctl;
-  if (inactive(ctl)) {
-    if (blockIdx.x == 0 && threadIdx.x == 0) set_rebuild_cond(rc, ctl);
-    return;
-  }
-  __shared__ double sh[kBlock / 32];
-  const uint32_t n = blockIdx.x * blockDim.x + threadIdx.x;
-  const double dt = sc.adapt_every ? ctl->dt_cur : sc.dt;
-  const double nm8 = sc.adapt_every ? ctl->nm[8] : sc.nm8, nm6 = sc.adapt_every ? ctl->nm[6] : sc.nm6;
-  double du2 = 0.0;
-  if (n < sc.V) {
-    double d[3];
-    float uh[3], ul[3];
+// One node's prediction (ShellSystem.C:972-989): u_pred = u + dt v + a8 a,
+// v_pred = v + a6 a, positions X + u_pred into `pos`, the FP32 or float-pair
+// copy of u_pred; returns |u_pred - u|^2.  Shared by k_predict and the fused
+// corrector of k_gather_correct, so both give the same bits.
+__device__ __forceinline__ double predict_node(const DevBuf& b, const StepConst& sc, uint32_t n, const double* u,
+                                               const double* v, const double* a, double dt, double nm8, double nm6,
+                                               double* pos) {
+  double d[3];
+  float uh[3], ul[3];
 #pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      const size_t k = 3 * (size_t)n + c;
-      const double u = b.u[k], v = b.v[k], a = b.a[k];
-      double up, vp;
-      if (sc.contact) {
-        // separately rounded, as the host does: positions feed the contact list
-        up = __dadd_rn(__dmul_rn(dt, v), u);
-        up = __dadd_rn(__dmul_rn(nm8, a), up);
-        vp = __dadd_rn(__dmul_rn(nm6, a), v);
-      } else {
-        up = fma(nm8, a, fma(dt, v, u));
-        vp = fma(nm6, a, v);
-      }
-      b.up[k] = up;
-      if (sc.fp32)
-        b.up32[k] = (float)up;
-      else
-        df_split(up, uh[c], ul[c]);
-      b.vp[k] = vp;
-      b.p[k] = __dadd_rn(b.X[k], up);
-      d[c] = __dsub_rn(up, u);
+  for (int c = 0; c < 3; ++c) {
+    const size_t k = 3 * (size_t)n + c;
+    double up, vp;
+    if (sc.contact) {
+      // separately rounded, as the host does: positions feed the contact list
+      up = __dadd_rn(__dmul_rn(dt, v[c]), u[c]);
+      up = __dadd_rn(__dmul_rn(nm8, a[c]), up);
+      vp = __dadd_rn(__dmul_rn(nm6, a[c]), v[c]);
+    } else {
+      up = fma(nm8, a[c], fma(dt, v[c], u[c]));
+      vp = fma(nm6, a[c], v[c]);
     }
-    if (!sc.fp32) {
-      b.upk[2 * (size_t)n] = make_float4(uh[0], uh[1], uh[2], 0.f);
-      b.upk[2 * (size_t)n + 1] = make_float4(ul[0], ul[1], ul[2], 0.f);
-    }
-    du2 = __dadd_rn(__dadd_rn(__dmul_rn(d[0], d[0]), __dmul_rn(d[1], d[1])), __dmul_rn(d[2], d[2]));
+    b.up[k] = up;
+    if (sc.fp32)
+      b.up32[k] = (float)up;
+    else
+      df_split(up, uh[c], ul[c]);
+    b.vp[k] = vp;
+    pos[k] = __dadd_rn(b.X[k], up);
+    d[c] = __dsub_rn(up, u[c]);
   }
-  const double m = block_max(du2, sh);
-  if (threadIdx.x == 0) b.partial[(size_t)blockIdx.x * 8] = m;
-  if (!last_block(&ctl->cnt[0])) return;
-  double mm = 0.0;
-  for (int k = threadIdx.x; k < (int)gridDim.x; k += blockDim.x) mm = fmax(mm, __ldcg(&b.partial[(size_t)k * 8]));
-  mm = block_max(mm, sh);
-  if (threadIdx.x != 0) return;
-  // prepare_next_step: time, the step's pressure, volume pressure
+  if (!sc.fp32) {
+    b.upk[2 * (size_t)n] = make_float4(uh[0], uh[1], uh[2], 0.f);
+    b.upk[2 * (size_t)n + 1] = make_float4(ul[0], ul[1], ul[2], 0.f);
+  }
+  return __dadd_rn(__dadd_rn(__dmul_rn(d[0], d[0]), __dmul_rn(d[1], d[1])), __dmul_rn(d[2], d[2]));
+}
+
+// The scalar start of a step (one thread): prepare_next_step (time, the step's
+// pressure, cavity semi-axes, volume pressure) and check_increment(false) with
+// the predictor's largest |du|^2; sets the rebuild flag and the IF condition.
+__device__ void begin_step(Ctl* ctl, const StepConst& sc, double dt, double mm, const RebuildCond& rc) {
   ctl->time = __dadd_rn(ctl->time, dt);
   ctl->time_step += 1;
   double pr = sc.pressure_default;
@@ -418,6 +408,53 @@ __global__ void __launch_bounds__(kBlock) k_predict(DevBuf b, StepConst sc, Rebu
   }
   ctl->rebuild = (sc.contact && ctl->du_sum >= rebuild_tolerance(sc, ctl)) ? 1u : 0u;
   set_rebuild_cond(rc, ctl);
+}
+
+// u_pred, v_pred, positions and du_max of every node, then the step's scalar
+// start.  nodes_only: the predicted state alone, its largest |du|^2 left in
+// ctl->du2_pred for k_begin_step (the start of a run of fused steps).
+__global__ void __launch_bounds__(kBlock) k_predict(DevBuf b, StepConst sc, RebuildCond rc, int nodes_only) {
+  Ctl* ctl = b.ctl;
+  if (inactive(ctl)) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) set_rebuild_cond(rc, ctl);
+    return;
+  }
+  __shared__ double sh[kBlock / 32];
+  const uint32_t n = blockIdx.x * blockDim.x + threadIdx.x;
+  const double dt = sc.adapt_every ? ctl->dt_cur : sc.dt;
+  const double nm8 = sc.adapt_every ? ctl->nm[8] : sc.nm8, nm6 = sc.adapt_every ? ctl->nm[6] : sc.nm6;
+  double du2 = 0.0;
+  if (n < sc.V) {
+    const size_t k3 = 3 * (size_t)n;
+    const double u[3] = {b.u[k3], b.u[k3 + 1], b.u[k3 + 2]};
+    const double v[3] = {b.v[k3], b.v[k3 + 1], b.v[k3 + 2]};
+    const double a[3] = {b.a[k3], b.a[k3 + 1], b.a[k3 + 2]};
+    du2 = predict_node(b, sc, n, u, v, a, dt, nm8, nm6, b.p);
+  }
+  const double m = block_max(du2, sh);
+  if (threadIdx.x == 0) b.partial[(size_t)blockIdx.x * 8] = m;
+  if (!last_block(&ctl->cnt[0])) return;
+  double mm = 0.0;
+  for (int k = threadIdx.x; k < (int)gridDim.x; k += blockDim.x) mm = fmax(mm, __ldcg(&b.partial[(size_t)k * 8]));
+  mm = block_max(mm, sh);
+  if (threadIdx.x != 0) return;
+  if (nodes_only) {
+    ctl->du2_pred = mm;
+    return;
+  }
+  begin_step(ctl, sc, dt, mm, rc);
+}
+
+// the scalar start of a fused step: the nodes were predicted by the previous
+// step's corrector (k_gather_correct mode 3) or by k_predict(nodes_only)
+__global__ void k_begin_step(DevBuf b, StepConst sc, RebuildCond rc) {
+  Ctl* ctl = b.ctl;
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  if (inactive(ctl)) {
+    set_rebuild_cond(rc, ctl);
+    return;
+  }
+  begin_step(ctl, sc, sc.dt, ctl->du2_pred, rc);
 }
 
 // positions only (p = X + u_pred), for force evaluations at a given state
@@ -1351,7 +1388,10 @@ __device__ void cavity_totals(const DevBuf& b, const StepConst& sc, Ctl* ctl, do
 
 __global__ void __launch_bounds__(kBlock) k_gather_correct(DevBuf b, StepConst sc, int mode, double* f_out,
                                                            double* a_out, RebuildCond rc) {
-  // mode 0: eval (write f_out / a_out), mode 1: step corrector
+  // mode 0: eval (write f_out / a_out), mode 1: step corrector, mode 2: adaptive
+  // attempt, mode 3: step corrector fused with the next step's prediction (fixed
+  // dt): the step's predicted positions are read from b.pn and the next ones
+  // written there, the corrected positions go to b.p
   Ctl* ctl = b.ctl;
   if (inactive(ctl)) {
     if (blockIdx.x == 0 && threadIdx.x == 0) set_rebuild_cond(rc, ctl);
@@ -1359,7 +1399,7 @@ __global__ void __launch_bounds__(kBlock) k_gather_correct(DevBuf b, StepConst s
   }
   __shared__ double sh[kBlock / 32];
   const uint32_t n = blockIdx.x * blockDim.x + threadIdx.x;
-  double du2 = 0.0, ekin = 0.0;
+  double du2 = 0.0, ekin = 0.0, du2_next = 0.0;
   double c_nc = 0.0, c_e = 0.0, c_ef = 0.0, c_fn = 0.0;  // cavity: contacts, energy, friction energy, force
   if (n < sc.V) {
     double f[3] = {0.0, 0.0, 0.0};
@@ -1418,7 +1458,8 @@ __global__ void __launch_bounds__(kBlock) k_gather_correct(DevBuf b, StepConst s
       // interaction with the cavity (ShellSystem.C:1600-1723)
       const CavityGeom cg = cavity_geom(ctl->cav_R, sc);
       const size_t k3 = 3 * (size_t)n;
-      const double p[3] = {b.p[k3], b.p[k3 + 1], b.p[k3 + 2]};
+      const double* pp = mode == 3 ? b.pn : b.p;
+      const double p[3] = {pp[k3], pp[k3 + 1], pp[k3 + 2]};
       const double xr = (p[0] / cg.R_eff[0]) * (p[0] / cg.R_eff[0]);
       const double yr = (p[1] / cg.R_eff[1]) * (p[1] / cg.R_eff[1]);
       const double zr = (p[2] / cg.R_eff[2]) * (p[2] / cg.R_eff[2]);
@@ -1504,7 +1545,7 @@ __global__ void __launch_bounds__(kBlock) k_gather_correct(DevBuf b, StepConst s
       f[1] += b.fcorr[3 * (size_t)n + 1];
       f[2] += b.fcorr[3 * (size_t)n + 2];
     }
-    double d[3];
+    double d[3], un[3], vnn[3], an[3];
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
       const size_t k = 3 * (size_t)n + c;
@@ -1535,9 +1576,13 @@ __global__ void __launch_bounds__(kBlock) k_gather_correct(DevBuf b, StepConst s
         b.a[k] = ap;
         b.p[k] = __dadd_rn(b.X[k], up);
         ekin += vn * vn * b.M[k];
+        un[c] = up;
+        vnn[c] = vn;
+        an[c] = ap;
       }
     }
-    if (mode == 1) du2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+    if (mode == 1 || mode == 3) du2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+    if (mode == 3) du2_next = predict_node(b, sc, n, un, vnn, an, sc.dt, sc.nm8, sc.nm6, b.pn);
   }
   if (mode == 0) return;
   if (sc.cavity_contact) {
@@ -1598,18 +1643,25 @@ __global__ void __launch_bounds__(kBlock) k_gather_correct(DevBuf b, StepConst s
   }
   const double m = block_max(du2, sh);
   const double ek = block_sum(0.5 * ekin, sh);
+  const double mn = mode == 3 ? block_max(du2_next, sh) : 0.0;
   if (threadIdx.x == 0) {
     b.partial[(size_t)blockIdx.x * 8] = m;
     b.partial[(size_t)blockIdx.x * 8 + 1] = ek;
+    b.partial[(size_t)blockIdx.x * 8 + 6] = mn;
   }
   if (!last_block(&ctl->cnt[3])) return;
   if (sc.cavity_contact) cavity_totals(b, sc, ctl, sh);
-  double mm = 0.0;
-  for (int k = threadIdx.x; k < (int)gridDim.x; k += blockDim.x) mm = fmax(mm, __ldcg(&b.partial[(size_t)k * 8]));
+  double mm = 0.0, mmn = 0.0;
+  for (int k = threadIdx.x; k < (int)gridDim.x; k += blockDim.x) {
+    mm = fmax(mm, __ldcg(&b.partial[(size_t)k * 8]));
+    mmn = fmax(mmn, __ldcg(&b.partial[(size_t)k * 8 + 6]));
+  }
   mm = block_max(mm, sh);
+  if (mode == 3) mmn = block_max(mmn, sh);
   const double ekt = sum_partials(b.partial, 1, gridDim.x, sh);
   if (threadIdx.x != 0) return;
   ctl->Ekin = ekt;
+  if (mode == 3) ctl->du2_pred = mmn;  // check_increment(false) of the next step, in k_begin_step
   // check_increment(true)
   const double du_max = sqrt(mm);
   if (isfinite(du_max)) {
@@ -1849,8 +1901,11 @@ void launch_flush(void* buf, size_t bytes, uint32_t tag, cudaStream_t s) {
 // --------------------------------------------------------------- launch --
 static inline uint32_t nblk(uint32_t n) { return (n + kBlock - 1) / kBlock; }
 
-void launch_predict(const DevBuf& b, const StepConst& sc, RebuildCond rc, cudaStream_t s) {
-  k_predict<<<nblk(sc.V), kBlock, 0, s>>>(b, sc, rc);
+void launch_predict(const DevBuf& b, const StepConst& sc, RebuildCond rc, cudaStream_t s, bool nodes_only) {
+  k_predict<<<nblk(sc.V), kBlock, 0, s>>>(b, sc, rc, nodes_only ? 1 : 0);
+}
+void launch_begin_step(const DevBuf& b, const StepConst& sc, RebuildCond rc, cudaStream_t s) {
+  k_begin_step<<<1, 32, 0, s>>>(b, sc, rc);
 }
 void launch_positions(const DevBuf& b, const StepConst& sc, cudaStream_t s) {
   k_positions<<<nblk(sc.V), kBlock, 0, s>>>(b, sc);
@@ -1945,7 +2000,8 @@ void launch_contact_force(const DevBuf& b, const StepConst& sc, int, cudaStream_
 // mode 2: an adaptive attempt (a_pred and the error estimate); else correct ? step corrector : evaluation
 void launch_gather_correct(const DevBuf& b, const StepConst& sc, int mode, bool correct, double* f_out, double* a_out,
                            cudaStream_t s, RebuildCond rc) {
-  k_gather_correct<<<nblk(sc.V), kBlock, 0, s>>>(b, sc, mode == 2 ? 2 : (correct ? 1 : 0), f_out, a_out, rc);
+  const int m = (mode == 2 || mode == 3) ? mode : (correct ? 1 : 0);
+  k_gather_correct<<<nblk(sc.V), kBlock, 0, s>>>(b, sc, m, f_out, a_out, rc);
 }
 void launch_correct_adapt(const DevBuf& b, const StepConst& sc, cudaStream_t s, RebuildCond rc) {
   k_correct_adapt<<<(sc.V + kBlock - 1) / kBlock, kBlock, 0, s>>>(b, sc, rc);
