@@ -100,37 +100,42 @@ __device__ __forceinline__ bool last_block(uint32_t* counter) {
   return is_last;
 }
 
-// N block sums at once (the same order per sum as block_sum); the result is in thread 0
+// Block sums of N values per thread (kBlock threads), transposed through shared
+// memory: warp k adds column k (its lane's 8 values in order, then a shuffle
+// tree), so the FP64 adds and shuffles are N warps' worth instead of every
+// warp's.  Fixed order; the sums land in thread 0's x.
+struct TransposedSum {
+  double v[8][kBlock];
+  double res[8];
+};
 template <int N>
-__device__ __forceinline__ void block_sum_n(double* x, double (*sh)[kBlock / 32]) {
+__device__ __forceinline__ void block_sum_t(double* x, TransposedSum& sh) {
+  static_assert(N <= 8 && N * 32 <= kBlock, "one warp per value");
+  const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+  __syncthreads();  // the shared buffer may still be read by a previous call
 #pragma unroll
-  for (int k = 0; k < N; ++k)
-    for (int o = 16; o > 0; o >>= 1) x[k] += __shfl_down_sync(0xffffffffu, x[k], o);
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int k = 0; k < N; ++k) sh.v[k][t] = x[k];
   __syncthreads();
-  if (lane == 0)
+  if (warp < N) {
+    double a = sh.v[warp][lane];
 #pragma unroll
-    for (int k = 0; k < N; ++k) sh[k][warp] = x[k];
+    for (int i = 1; i < kBlock / 32; ++i) a += sh.v[warp][lane + 32 * i];
+    for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
+    if (lane == 0) sh.res[warp] = a;
+  }
   __syncthreads();
-  if (warp == 0)
+  if (t == 0)
 #pragma unroll
-    for (int k = 0; k < N; ++k) {
-      x[k] = (lane < (int)(blockDim.x >> 5)) ? sh[k][lane] : 0.0;
-      for (int o = 16; o > 0; o >>= 1) x[k] += __shfl_down_sync(0xffffffffu, x[k], o);
-    }
+    for (int k = 0; k < N; ++k) x[k] = sh.res[k];
 }
-
-// fields 0..N-1 of the per-block partials summed over the blocks in fixed order
-// (the same order per field as sum_partials; last block only, result in thread 0)
 template <int N>
-__device__ __forceinline__ void sum_partials_n(const double* partial, int nb, double (*sh)[kBlock / 32],
-                                               double* out) {
+__device__ __forceinline__ void sum_partials_t(const double* partial, int nb, TransposedSum& sh, double* out) {
 #pragma unroll
   for (int k = 0; k < N; ++k) out[k] = 0.0;
   for (int b = threadIdx.x; b < nb; b += blockDim.x)
 #pragma unroll
     for (int k = 0; k < N; ++k) out[k] += __ldcg(&partial[(size_t)b * 8 + k]);
-  block_sum_n<N>(out, sh);
+  block_sum_t<N>(out, sh);
 }
 
 // per-face measurement densities times area (E_tens, E_bend, kGauss, kMean) and the area
@@ -1233,18 +1238,18 @@ __global__ void __launch_bounds__(BS, MINB) k_elements(DevBuf b, StepConst sc, E
 __global__ void __launch_bounds__(kBlock) k_elem_totals(DevBuf b, StepConst sc) {
   Ctl* ctl = b.ctl;
   if (inactive(ctl)) return;
-  __shared__ double sh[5][kBlock / 32];
+  __shared__ TransposedSum sh;
   const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
   double v[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
   if (e < sc.F) face_totals(b, e, v);
-  block_sum_n<5>(v, sh);
+  block_sum_t<5>(v, sh);
   if (threadIdx.x == 0) {
     double* pp = b.partial + (size_t)blockIdx.x * 8;
     for (int k = 0; k < 5; ++k) pp[k] = v[k];
   }
   if (!last_block(&ctl->cnt[1])) return;
   double t[5];
-  sum_partials_n<5>(b.partial, gridDim.x, sh, t);
+  sum_partials_t<5>(b.partial, gridDim.x, sh, t);
   if (threadIdx.x == 0) {
     ctl->Etens = t[0]; ctl->Ebend = t[1]; ctl->kGauss = t[2]; ctl->kMean = t[3]; ctl->area = t[4];
   }
@@ -1403,6 +1408,20 @@ __global__ void __launch_bounds__(kBlock) k_gather_correct(DevBuf b, StepConst s
   double c_nc = 0.0, c_e = 0.0, c_ef = 0.0, c_fn = 0.0;  // cavity: contacts, energy, friction energy, force
   if (n < sc.V) {
     double f[3] = {0.0, 0.0, 0.0};
+    // the node's state, loaded ahead of (and independently of) the share sums
+    const size_t k3n = 3 * (size_t)n;
+    const bool corr = mode == 1 || mode == 3;
+    double s_vp[3], s_minv[3], s_c[3], s_up[3], s_u[3], s_x[3], s_m[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      s_vp[c] = b.vp[k3n + c];
+      s_minv[c] = b.Minv[k3n + c];
+      s_c[c] = b.C[k3n + c];
+      s_up[c] = corr ? b.up[k3n + c] : 0.0;
+      s_u[c] = corr ? b.u[k3n + c] : 0.0;
+      s_x[c] = corr ? b.X[k3n + c] : 0.0;
+      s_m[c] = corr ? b.M[k3n + c] : 0.0;
+    }
     if (sc.contact) {
       const uint32_t k0 = b.csr_ptr[n], k1 = b.csr_ptr[n + 1];
       for (uint32_t k = k0; k < k1; ++k) {
@@ -1435,7 +1454,7 @@ __global__ void __launch_bounds__(kBlock) k_gather_correct(DevBuf b, StepConst s
       // double-float shares: added as pairs on the FP32 pipe, converted once
       const float2* q2 = reinterpret_cast<const float2*>(b.qe);
       df2 s0 = dfv(0.f), s1 = dfv(0.f), s2 = dfv(0.f);
-#pragma unroll 4
+#pragma unroll 8
       for (uint32_t k = g0; k < g1; ++k) {
         const float2 x = q2[3 * (size_t)k], y = q2[3 * (size_t)k + 1], z = q2[3 * (size_t)k + 2];
         s0 += df2{x.x, x.y};
@@ -1549,8 +1568,8 @@ __global__ void __launch_bounds__(kBlock) k_gather_correct(DevBuf b, StepConst s
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
       const size_t k = 3 * (size_t)n + c;
-      const double vp = b.vp[k];
-      const double ap = b.Minv[k] * (f[c] - b.C[k] * vp);
+      const double vp = s_vp[c];
+      const double ap = s_minv[c] * (f[c] - s_c[c] * vp);
       if (mode == 2) {
         // adaptive attempt: keep a_pred; local-error and velocity norms (ShellSystem.C:1017-1040)
         b.ap[k] = ap;
@@ -1564,18 +1583,18 @@ __global__ void __launch_bounds__(kBlock) k_gather_correct(DevBuf b, StepConst s
       } else {
         double up, vn;
         if (sc.contact) {
-          up = __dadd_rn(__dmul_rn(sc.nm0, ap), b.up[k]);
+          up = __dadd_rn(__dmul_rn(sc.nm0, ap), s_up[c]);
           vn = __dadd_rn(__dmul_rn(sc.nm7, ap), vp);
         } else {
-          up = fma(sc.nm0, ap, b.up[k]);
+          up = fma(sc.nm0, ap, s_up[c]);
           vn = fma(sc.nm7, ap, vp);
         }
-        d[c] = __dsub_rn(up, b.u[k]);
+        d[c] = __dsub_rn(up, s_u[c]);
         b.u[k] = up;
         b.v[k] = vn;
         b.a[k] = ap;
-        b.p[k] = __dadd_rn(b.X[k], up);
-        ekin += vn * vn * b.M[k];
+        b.p[k] = __dadd_rn(s_x[c], up);
+        ekin += vn * vn * s_m[c];
         un[c] = up;
         vnn[c] = vn;
         an[c] = ap;
@@ -1761,7 +1780,7 @@ __global__ void __launch_bounds__(kBlock) k_volume_end(DevBuf b, StepConst sc, i
   }
   // the element kernel's per-face measurement totals (as k_elem_totals forms
   // them, bit for bit) and the enclosed volume, in one pass over the faces
-  __shared__ double sh[6][kBlock / 32];
+  __shared__ TransposedSum sh;
   const uint32_t f = blockIdx.x * blockDim.x + threadIdx.x;
   double v[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
   if (f < sc.F) {
@@ -1772,14 +1791,14 @@ __global__ void __launch_bounds__(kBlock) k_volume_end(DevBuf b, StepConst sc, i
     v[5] = q0[0] * (q1[1] * q2[2] - q2[1] * q1[2]) - q1[0] * (q0[1] * q2[2] - q2[1] * q0[2]) +
            q2[0] * (q0[1] * q1[2] - q1[1] * q0[2]);
   }
-  block_sum_n<6>(v, sh);
+  block_sum_t<6>(v, sh);
   if (threadIdx.x == 0) {
     double* pp = b.partial + (size_t)blockIdx.x * 8;
     for (int k = 0; k < 6; ++k) pp[k] = v[k];
   }
   if (!last_block(&ctl->cnt[4])) return;
   double t[6];
-  sum_partials_n<6>(b.partial, gridDim.x, sh, t);
+  sum_partials_t<6>(b.partial, gridDim.x, sh, t);
   if (threadIdx.x != 0) return;
   ctl->Etens = t[0]; ctl->Ebend = t[1]; ctl->kGauss = t[2]; ctl->kMean = t[3]; ctl->area = t[4];
   ctl->volume = fabs(t[5] / 6.0) - ctl->area * 0.5 * sc.thickness;
