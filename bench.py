@@ -41,12 +41,13 @@ from shell_gb300.workloads import (ALPHA, AMPL, DT, G12, MU, NU12, RAMP_STEPS, R
                                    classical_pressure, pressure, squashed_state, workload)
 
 FLUSH_BYTES = 512 << 20
-# library kernels per step with self-contact: predictor, element kernel, contact force,
-# gather/corrector, volume/measurement totals/end of step (predictor and corrector set the
-# conditions of the two rebuild IF nodes themselves); plus the 27 kernels of each
-# candidate-list rebuild that runs (10 pipeline + 3 x 3 scan + 8 contact CSR)
+# library kernels per step with self-contact: step start (k_begin_step, which also sets the
+# condition of the step's rebuild IF node), element kernel, contact force, gather/corrector
+# (which also predicts the next step), volume/measurement totals/end of step; plus, for each
+# rebuild, the body of the IF node: two linked-cell passes of 27 kernels (10 pipeline +
+# 3 x 3 scan + 8 contact CSR; the one not due returns at once) and the kernel between them
 LAUNCHES_PER_STEP_CONTACT = 5
-LAUNCHES_PER_REBUILD = 27
+LAUNCHES_PER_REBUILD = 55
 # element kernel (double-float FP64 path): per-face constants as float pairs
 # (38 fields x 8 B), patch ids, force shares (float pairs), element fields,
 # face permutation (bytes); per-node predicted displacement (bytes)

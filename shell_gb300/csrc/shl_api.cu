@@ -64,6 +64,9 @@ struct shl_ctx {
   // step.  pred_valid: the device holds that prediction for the current state
   // (set by graph steps, cleared by every entry point that may change the state)
   bool pred_valid = false;
+  // fused graph steps ran since the last collect: a corrector-side linked-cell
+  // pass may be pending on the device (made by the next step, or on host access)
+  bool maybe_pending = false;
   double* h_pin = nullptr;  // pinned staging buffer, 3V doubles x 3
   Ctl* h_ctl = nullptr;     // pinned copy of the device control block
   double* h_table = nullptr;  // pinned staging of the pressure table (kTableCap doubles)
@@ -156,11 +159,36 @@ shl_status check_launch(const char* where) {
   return SHL_OK;
 }
 
+
+
 #define SHL_TRY(expr)             \
   do {                            \
     shl_status s_ = (expr);       \
     if (s_ != SHL_OK) return s_;  \
   } while (0)
+
+// Makes the corrector-side linked-cell pass that fused steps may have left
+// pending, so the candidate list and du_sum are those of the unfused sequence
+// at this point (before the host reads or changes the state).
+shl_status flush_deferred_rebuild(shl_ctx* c) {
+  if (!c->maybe_pending) return SHL_OK;
+  c->maybe_pending = false;
+  if (!c->sc.contact) return SHL_OK;
+  Ctl h;
+  SHL_TRY(ctl_get(c, h));
+  if (!h.rebuild_pending) return SHL_OK;
+  launch_rebuild_first(c->b, c->stream);
+  launch_rebuild(c->b, c->sc, c->stream);
+  SHL_CUDA_TRY(cudaStreamSynchronize(c->stream));
+  return check_launch("deferred linked-cell pass");
+}
+
+// entry points that read the contact state or may change the step state
+shl_status host_access(shl_ctx* c) {
+  SHL_TRY(flush_deferred_rebuild(c));
+  c->pred_valid = false;
+  return SHL_OK;
+}
 
 bool validate(const shl_params& p, std::string& err) {
   if (!(p.shell_mass_density > 0)) { err = "shell_mass_density must be > 0"; return false; }
@@ -294,7 +322,7 @@ cudaError_t rebuild_cond_create(shl_ctx* c, RebuildCond* rc) {
   return cudaSuccess;
 }
 
-cudaError_t rebuild_if_node(shl_ctx* c, const RebuildCond& rc, const DevBuf& b) {
+cudaError_t rebuild_if_node(shl_ctx* c, const RebuildCond& rc, const DevBuf& b, const DevBuf* second) {
   cudaStreamCaptureStatus st;
   cudaGraph_t g = nullptr;
   const cudaGraphNode_t* deps = nullptr;
@@ -313,6 +341,10 @@ cudaError_t rebuild_if_node(shl_ctx* c, const RebuildCond& rc, const DevBuf& b) 
   e = cudaStreamBeginCaptureToGraph(c->side, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed);
   if (e != cudaSuccess) return e;
   launch_rebuild(b, c->sc, c->side);
+  if (second) {
+    launch_rebuild_second(b, c->sc, c->side);
+    launch_rebuild(*second, c->sc, c->side);
+  }
   e = cudaStreamEndCapture(c->side, &body);
   if (e != cudaSuccess) return e;
   return cudaStreamUpdateCaptureDependencies(c->stream, &node, nullptr, 1, cudaStreamSetCaptureDependencies);
@@ -321,9 +353,15 @@ cudaError_t rebuild_if_node(shl_ctx* c, const RebuildCond& rc, const DevBuf& b) 
 // the linked-cell pass after the kernel that decided it: an IF node in a graph
 // with conditional nodes, else the pipeline itself (its kernels return at once
 // when no rebuild is due); b.p = the positions it works on
-cudaError_t enqueue_rebuild(shl_ctx* c, const RebuildCond& rc, const DevBuf& b) {
-  if (rc.has) return rebuild_if_node(c, rc, b);
+// second: fused steps' pair of passes (b at the corrected positions, then
+// *second at the predicted ones, k_rebuild_second between them)
+cudaError_t enqueue_rebuild(shl_ctx* c, const RebuildCond& rc, const DevBuf& b, const DevBuf* second = nullptr) {
+  if (rc.has) return rebuild_if_node(c, rc, b, second);
   launch_rebuild(b, c->sc, c->stream);
+  if (second) {
+    launch_rebuild_second(b, c->sc, c->stream);
+    launch_rebuild(*second, c->sc, c->stream);
+  }
   return cudaSuccess;
 }
 
@@ -347,10 +385,11 @@ cudaError_t enqueue_step(shl_ctx* c, bool capturing = false, bool fused = false)
     launch_begin_step(b, sc, r1, s);
   else
     launch_predict(b, sc, r1, s);
-  if (sc.contact && (e = enqueue_rebuild(c, r1, bp)) != cudaSuccess) return e;
+  // fused: one IF node for the previous corrector's pass and this predictor's
+  if (sc.contact && (e = enqueue_rebuild(c, r1, fused ? b : bp, fused ? &bp : nullptr)) != cudaSuccess) return e;
   launch_elements(b, sc, elem_launch(c, sc), s, false);  // totals in k_volume_end
   if (sc.contact) launch_contact_force(bp, sc, 0, s);
-  if (cond && (e = rebuild_cond_create(c, &r2)) != cudaSuccess) return e;
+  if (cond && !fused && (e = rebuild_cond_create(c, &r2)) != cudaSuccess) return e;
   if (sc.adapt_every) {
     // one attempt: estimate, then correct only if accepted (ShellSystem.C:1010-1117)
     launch_gather_correct(b, sc, 2, false, nullptr, nullptr, s);
@@ -358,7 +397,7 @@ cudaError_t enqueue_step(shl_ctx* c, bool capturing = false, bool fused = false)
   } else {
     launch_gather_correct(b, sc, fused ? 3 : 0, true, nullptr, nullptr, s, r2);
   }
-  if (sc.contact && (e = enqueue_rebuild(c, r2, b)) != cudaSuccess) return e;
+  if (sc.contact && !fused && (e = enqueue_rebuild(c, r2, b)) != cudaSuccess) return e;
   launch_volume_end_step(b, sc, true, s);
   return cudaSuccess;
 }
@@ -872,7 +911,7 @@ shl_status shl_batch_layout(shl_ctx* c, uint32_t* n_shells, uint32_t* node_offse
 
 shl_status shl_set_state(shl_ctx* c, const double* u, const double* v, const double* a) {
   if (!c) return SHL_ERR_ARG;
-  c->pred_valid = false;  // may change what the step prediction was made from
+  SHL_TRY(host_access(c));  // pending linked-cell pass; the step prediction is rebuilt
   const size_t nd = 3 * (size_t)c->S.V;
   if (u) {
     SHL_TRY(upload(c, c->b.u, u, nd));
@@ -897,7 +936,7 @@ shl_status shl_get_state(shl_ctx* c, double* u, double* v, double* a) {
 
 shl_status shl_set_time(shl_ctx* c, double t, uint32_t step) {
   if (!c) return SHL_ERR_ARG;
-  c->pred_valid = false;  // may change what the step prediction was made from
+  SHL_TRY(host_access(c));  // pending linked-cell pass; the step prediction is rebuilt
   Ctl h;
   SHL_TRY(ctl_get(c, h));
   h.time = t;
@@ -964,7 +1003,7 @@ extern "C" {
 shl_status shl_eval_forces(shl_ctx* c, const double* u_pred, const double* v_pred, double pressure, double* f_out,
                            double* a_out, shl_energies* e) {
   if (!c || !u_pred || !v_pred) return SHL_ERR_ARG;
-  c->pred_valid = false;  // may change what the step prediction was made from
+  SHL_TRY(host_access(c));  // pending linked-cell pass; the step prediction is rebuilt
   const size_t nd = 3 * (size_t)c->S.V;
   SHL_TRY(upload(c, c->b.up, u_pred, nd));
   SHL_TRY(upload(c, c->b.vp, v_pred, nd));
@@ -1009,7 +1048,7 @@ shl_status initial_state(shl_ctx* c, Ctl& h) {
 
 shl_status shl_apply_initial_conditions(shl_ctx* c, const double* u0, double t0, double pressure_next) {
   if (!c || !u0) return SHL_ERR_ARG;
-  c->pred_valid = false;  // may change what the step prediction was made from
+  SHL_TRY(host_access(c));  // pending linked-cell pass; the step prediction is rebuilt
   const size_t nd = 3 * (size_t)c->S.V;
   SHL_TRY(upload(c, c->b.u, u0, nd));
   SHL_TRY(upload(c, c->b.up, u0, nd));
@@ -1038,7 +1077,7 @@ shl_status shl_apply_initial_conditions(shl_ctx* c, const double* u0, double t0,
 
 shl_status shl_apply_loaded_state(shl_ctx* c) {
   if (!c) return SHL_ERR_ARG;
-  c->pred_valid = false;  // may change what the step prediction was made from
+  SHL_TRY(host_access(c));  // pending linked-cell pass; the step prediction is rebuilt
   Ctl h;
   return initial_state(c, h);
 }
@@ -1059,6 +1098,7 @@ shl_status ensure_graphs(shl_ctx* c) {
 
 shl_status enqueue_steps(shl_ctx* c, uint32_t n, bool use_graph) {
   if (n == 0) return SHL_OK;
+  if (!use_graph || !fused_steps(c)) SHL_TRY(flush_deferred_rebuild(c));
   if (use_graph) {
     SHL_TRY(ensure_graphs(c));
     if (fused_steps(c) && !c->pred_valid) {
@@ -1070,6 +1110,7 @@ shl_status enqueue_steps(shl_ctx* c, uint32_t n, bool use_graph) {
     for (; k + kGraphSteps <= n; k += kGraphSteps) SHL_CUDA_TRY(cudaGraphLaunch(c->graph, c->stream));
     for (; k < n; ++k) SHL_CUDA_TRY(cudaGraphLaunch(c->graph1, c->stream));
     c->pred_valid = fused_steps(c);
+    c->maybe_pending = c->maybe_pending || (fused_steps(c) && c->sc.contact);
   } else {
     for (uint32_t k = 0; k < n; ++k) enqueue_step(c);
     c->pred_valid = false;
@@ -1104,6 +1145,16 @@ shl_status collect(shl_ctx* c, shl_step_report* report, const Ctl* fresh = nullp
     h = *fresh;
   else
     SHL_TRY(ctl_get(c, h));
+  if (c->maybe_pending) {
+    // a corrector-side linked-cell pass left pending by the last fused step
+    c->maybe_pending = false;
+    if (c->sc.contact && h.rebuild_pending) {
+      launch_rebuild_first(c->b, c->stream);
+      launch_rebuild(c->b, c->sc, c->stream);
+      SHL_TRY(check_launch("deferred linked-cell pass"));
+      SHL_TRY(ctl_get(c, h));
+    }
+  }
   if (report) {
     std::memset(report, 0, sizeof(*report));
     report->steps_done = h.steps_done;
@@ -1222,7 +1273,7 @@ shl_status shl_get_cavity_origins(shl_ctx* c, double* origins) {
 
 shl_status shl_set_cavity_origins(shl_ctx* c, const double* origins) {
   if (!c || !origins) return SHL_ERR_ARG;
-  c->pred_valid = false;  // may change what the step prediction was made from
+  SHL_TRY(host_access(c));  // pending linked-cell pass; the step prediction is rebuilt
   if (!c->b.cav_origin) return SHL_OK;  // nothing to keep without cavity contact
   SHL_TRY(upload(c, c->b.cav_origin, origins, 3 * (size_t)c->S.V));
   SHL_CUDA_TRY(cudaStreamSynchronize(c->stream));
@@ -1311,7 +1362,7 @@ shl_status shl_time_kernel(shl_ctx* c, int which, int reps, size_t flush_bytes, 
     if (flush_bytes) launch_flush(c->d_flush, flush_bytes, (uint32_t)r, c->stream);
     cudaEventRecord(e0, c->stream);
     if (which == 0)
-      launch_elements(c->b, c->sc, elem_launch(c, c->sc), c->stream);
+      launch_elements(c->b, c->sc, elem_launch(c, c->sc), c->stream, false);  // the element kernel alone
     else
       launch_gather_correct(c->b, c->sc, 0, false, c->d_fa, c->d_fa + nd, c->stream);
     cudaEventRecord(e1, c->stream);
@@ -1332,7 +1383,7 @@ shl_status shl_time_kernel(shl_ctx* c, int which, int reps, size_t flush_bytes, 
 
 shl_status shl_profile_step(shl_ctx* c, double pressure, size_t flush_bytes, double* ms_out) {
   if (!c || !ms_out) return SHL_ERR_ARG;
-  c->pred_valid = false;  // may change what the step prediction was made from
+  SHL_TRY(host_access(c));  // pending linked-cell pass; the step prediction is rebuilt
   if (flush_bytes > c->flush_bytes) {
     if (c->d_flush) cudaFree(c->d_flush);
     c->d_flush = nullptr;
@@ -1409,6 +1460,7 @@ shl_status shl_measure_fp64_peak(double* tflops) {
 shl_status shl_get_contact_state(shl_ctx* c, uint32_t* pairs, uint8_t* stick, double* spring_origin, double* d2,
                                  size_t cap, size_t* n_pairs, double* du_sum) {
   if (!c) return SHL_ERR_ARG;
+  SHL_TRY(flush_deferred_rebuild(c));
   Ctl h;
   SHL_TRY(ctl_get(c, h));
   if (n_pairs) *n_pairs = h.n_pairs;
@@ -1436,6 +1488,8 @@ shl_status shl_get_contact_pairs(shl_ctx* c, uint32_t* pairs, size_t cap, size_t
 
 shl_status shl_get_contact_coords(shl_ctx* c, double* x, size_t cap, size_t* n_pairs) {
   if (!c) return SHL_ERR_ARG;
+  SHL_TRY(flush_deferred_rebuild(c));
+  SHL_TRY(flush_deferred_rebuild(c));
   Ctl h;
   SHL_TRY(ctl_get(c, h));
   if (n_pairs) *n_pairs = h.n_pairs;
@@ -1450,7 +1504,7 @@ shl_status shl_get_contact_coords(shl_ctx* c, double* x, size_t cap, size_t* n_p
 
 shl_status shl_set_contact_coords(shl_ctx* c, const double* x, size_t n) {
   if (!c || (n && !x)) return SHL_ERR_ARG;
-  c->pred_valid = false;  // may change what the step prediction was made from
+  SHL_TRY(host_access(c));  // pending linked-cell pass; the step prediction is rebuilt
   if (!c->sc.smooth) { g_err = "closest-point coordinates are kept for SMOOTH contact only"; return SHL_ERR_ARG; }
   Ctl h;
   SHL_TRY(ctl_get(c, h));
@@ -1463,7 +1517,7 @@ shl_status shl_set_contact_coords(shl_ctx* c, const double* x, size_t n) {
 shl_status shl_set_contact_state(shl_ctx* c, const uint32_t* pairs, const uint8_t* stick, const double* spring_origin,
                                  const double* d2, size_t n, double du_sum) {
   if (!c) return SHL_ERR_ARG;
-  c->pred_valid = false;  // may change what the step prediction was made from
+  SHL_TRY(host_access(c));  // pending linked-cell pass; the step prediction is rebuilt
   if (!c->sc.contact) { g_err = "self-contact is off"; return SHL_ERR_ARG; }
   if (n > c->sc.pairs_cap) { g_err = "too many pairs"; return SHL_ERR_CAPACITY; }
   const uint32_t F = c->S.F;
@@ -1518,7 +1572,7 @@ shl_status shl_set_contact_state(shl_ctx* c, const uint32_t* pairs, const uint8_
 
 shl_status shl_rebuild_contacts(shl_ctx* c) {
   if (!c) return SHL_ERR_ARG;
-  c->pred_valid = false;  // may change what the step prediction was made from
+  SHL_TRY(host_access(c));  // pending linked-cell pass; the step prediction is rebuilt
   if (!c->sc.contact) return SHL_OK;
   Ctl h;
   SHL_TRY(ctl_get(c, h));
@@ -1546,7 +1600,7 @@ shl_status shl_get_element_fields(shl_ctx* c, double* kG, double* kM, double* et
 
 shl_status shl_residual(shl_ctx* c, double pressure, int flags, double* rel, double* f2, double* fext2) {
   if (!c) return SHL_ERR_ARG;
-  c->pred_valid = false;  // may change what the step prediction was made from
+  SHL_TRY(host_access(c));  // pending linked-cell pass; the step prediction is rebuilt
   const size_t nd = 3 * (size_t)c->S.V;
   const uint32_t ns = (uint32_t)c->node_off.size() - 1;
   const bool ctx32 = c->sc.fp32 != 0;
@@ -1806,7 +1860,7 @@ shl_status shl_get_element_variant(shl_ctx* c, int* variant, char* name, size_t 
 
 shl_status shl_scale_damping(shl_ctx* c, double factor) {
   if (!c || !(factor >= 0)) return SHL_ERR_ARG;
-  c->pred_valid = false;  // may change what the step prediction was made from
+  SHL_TRY(host_access(c));  // pending linked-cell pass; the step prediction is rebuilt
   const size_t nd = 3 * (size_t)c->S.V;
   std::vector<double> C(nd);
   for (size_t i = 0; i < nd; ++i) C[i] = factor * c->S.C[i];
@@ -1826,7 +1880,7 @@ shl_status shl_get_mass_damping(shl_ctx* c, double* Minv, double* C) {
 shl_status shl_internal_force_noalloc(shl_ctx* c, const double* u_dev, double pressure, double* f_dev,
                                       void* stream) {
   if (!c || !u_dev || !f_dev) { g_err = "null argument"; return SHL_ERR_ARG; }
-  c->pred_valid = false;  // may change what the step prediction was made from
+  SHL_TRY(host_access(c));  // pending linked-cell pass; the step prediction is rebuilt
   if (c->sc.contact || c->P.bulk_modulus != 0.0 || c->sc.fp32) {
     g_err = "shl_internal_force_noalloc: self-contact, bulk-modulus pressure and FP32 element forces are not "
             "evaluated here";

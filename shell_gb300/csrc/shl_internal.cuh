@@ -99,6 +99,8 @@ struct Ctl {
   double bmin[3], bmax[3];
   uint32_t ncd[3];
   uint32_t rebuild;        // rebuild requested for the next rebuild pass
+  uint32_t rebuild_pending; // fused steps: the corrector's pass, deferred to the next step's IF node
+  uint32_t rebuild_b;       // fused steps: the predictor-side pass of the same IF node
   uint32_t n_cells;
   uint32_t n_entries;      // (cell, face) entries of the current rebuild
   uint32_t n_pairs;        // pairs in the current list
@@ -288,6 +290,12 @@ struct RebuildCond {
 // the step's scalar start, which k_begin_step then makes (fused steps)
 void launch_predict(const DevBuf& b, const StepConst& sc, RebuildCond rc, cudaStream_t s, bool nodes_only = false);
 void launch_begin_step(const DevBuf& b, const StepConst& sc, RebuildCond rc, cudaStream_t s);
+// Fused steps make both linked-cell passes of a step boundary in one IF node:
+// the corrector's (deferred, at the corrected positions) and then the
+// predictor's; launch_rebuild_second sits between them.  launch_rebuild_first
+// turns a deferred pass into a due one (before a direct launch_rebuild).
+void launch_rebuild_second(const DevBuf& b, const StepConst& sc, cudaStream_t s);
+void launch_rebuild_first(const DevBuf& b, cudaStream_t s);
 // totals: also the fixed-order sums of the per-face measurements (k_elem_totals);
 // k_volume_end forms them too, so launches followed by it pass false
 void launch_elements(const DevBuf& b, const StepConst& sc, const ElemLaunch& el, cudaStream_t s, bool totals = true);

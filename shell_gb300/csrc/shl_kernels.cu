@@ -384,7 +384,11 @@ __device__ __forceinline__ double predict_node(const DevBuf& b, const StepConst&
 // The scalar start of a step (one thread): prepare_next_step (time, the step's
 // pressure, cavity semi-axes, volume pressure) and check_increment(false) with
 // the predictor's largest |du|^2; sets the rebuild flag and the IF condition.
-__device__ void begin_step(Ctl* ctl, const StepConst& sc, double dt, double mm, const RebuildCond& rc) {
+// fused: the IF node holds both passes of the step boundary.  With the previous
+// corrector's pass pending, that pass runs first and this check's du_sum update
+// follows it (k_rebuild_second); otherwise the second pass's flag is rebuild_b.
+__device__ void begin_step(Ctl* ctl, const StepConst& sc, double dt, double mm, const RebuildCond& rc,
+                           bool fused = false) {
   ctl->time = __dadd_rn(ctl->time, dt);
   ctl->time_step += 1;
   double pr = sc.pressure_default;
@@ -405,14 +409,50 @@ __device__ void begin_step(Ctl* ctl, const StepConst& sc, double dt, double mm, 
   }
   // check_increment(false)
   const double du_max = sqrt(mm);
-  if (isfinite(du_max)) {
-    ctl->du_sum = __dadd_rn(ctl->du_sum, __dmul_rn(2.0, du_max));
+  const bool finite = isfinite(du_max);
+  if (finite) {
     if (sc.contact && du_max > 0.5 * sc.thickness) register_problem(ctl, SHL_LARGE_DISP);
   } else {
     register_problem(ctl, SHL_NOT_FINITE);
   }
-  ctl->rebuild = (sc.contact && ctl->du_sum >= rebuild_tolerance(sc, ctl)) ? 1u : 0u;
+  if (fused && ctl->rebuild_pending) {
+    ctl->rebuild = 1u;
+    if (rc.has) cudaGraphSetConditional(rc.h, ctl->halted == 0 ? 1u : 0u);
+    return;
+  }
+  if (finite) ctl->du_sum = __dadd_rn(ctl->du_sum, __dmul_rn(2.0, du_max));
+  const uint32_t flag = (sc.contact && ctl->du_sum >= rebuild_tolerance(sc, ctl)) ? 1u : 0u;
+  if (fused) {
+    ctl->rebuild = 0u;
+    ctl->rebuild_b = flag;
+    if (rc.has) cudaGraphSetConditional(rc.h, (flag != 0 && ctl->halted == 0) ? 1u : 0u);
+    return;
+  }
+  ctl->rebuild = flag;
   set_rebuild_cond(rc, ctl);
+}
+
+// between the two passes of a fused step's IF node (one thread): the deferred
+// du_sum update of check_increment(false) (after the first pass reset du_sum
+// and the element size), then the second pass's flag
+__global__ void k_rebuild_second(DevBuf b, StepConst sc) {
+  Ctl* ctl = b.ctl;
+  if (threadIdx.x != 0 || blockIdx.x != 0 || ctl->halted != 0) return;
+  if (ctl->rebuild_pending) {
+    ctl->rebuild_pending = 0u;
+    const double du_max = sqrt(ctl->du2_pred);
+    if (isfinite(du_max)) ctl->du_sum = __dadd_rn(ctl->du_sum, __dmul_rn(2.0, du_max));
+    ctl->rebuild_b = (sc.contact && ctl->du_sum >= rebuild_tolerance(sc, ctl)) ? 1u : 0u;
+  }
+  ctl->rebuild = ctl->rebuild_b;
+  ctl->rebuild_b = 0u;
+}
+
+// a deferred corrector pass made due for a direct launch_rebuild
+__global__ void k_rebuild_first(Ctl* ctl) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  ctl->rebuild = ctl->rebuild_pending;
+  ctl->rebuild_pending = 0u;
 }
 
 // u_pred, v_pred, positions and du_max of every node, then the step's scalar
@@ -459,7 +499,7 @@ __global__ void k_begin_step(DevBuf b, StepConst sc, RebuildCond rc) {
     set_rebuild_cond(rc, ctl);
     return;
   }
-  begin_step(ctl, sc, sc.dt, ctl->du2_pred, rc);
+  begin_step(ctl, sc, sc.dt, ctl->du2_pred, rc, true);
 }
 
 // positions only (p = X + u_pred), for force evaluations at a given state
@@ -1693,7 +1733,12 @@ __global__ void __launch_bounds__(kBlock) k_gather_correct(DevBuf b, StepConst s
     register_problem(ctl, SHL_NOT_FINITE);
   }
   if (!isfinite(ekt)) register_problem(ctl, SHL_NOT_FINITE);
-  ctl->rebuild = (sc.contact && ctl->du_sum >= rebuild_tolerance(sc, ctl)) ? 1u : 0u;
+  const uint32_t flag = (sc.contact && ctl->du_sum >= rebuild_tolerance(sc, ctl)) ? 1u : 0u;
+  if (mode == 3) {
+    ctl->rebuild_pending = flag;  // made by the next step's IF node, before its own pass
+    return;
+  }
+  ctl->rebuild = flag;
   set_rebuild_cond(rc, ctl);
 }
 
@@ -1926,6 +1971,10 @@ void launch_predict(const DevBuf& b, const StepConst& sc, RebuildCond rc, cudaSt
 void launch_begin_step(const DevBuf& b, const StepConst& sc, RebuildCond rc, cudaStream_t s) {
   k_begin_step<<<1, 32, 0, s>>>(b, sc, rc);
 }
+void launch_rebuild_second(const DevBuf& b, const StepConst& sc, cudaStream_t s) {
+  k_rebuild_second<<<1, 32, 0, s>>>(b, sc);
+}
+void launch_rebuild_first(const DevBuf& b, cudaStream_t s) { k_rebuild_first<<<1, 32, 0, s>>>(b.ctl); }
 void launch_positions(const DevBuf& b, const StepConst& sc, cudaStream_t s) {
   k_positions<<<nblk(sc.V), kBlock, 0, s>>>(b, sc);
 }
