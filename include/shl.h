@@ -228,7 +228,12 @@ shl_status shl_eval_forces(shl_ctx* ctx, const double* u_pred, const double* v_p
  * time t + dt), or NULL to use params.pressure.  The steps run on the
  * device without host synchronisation (captured in a CUDA graph when
  * use_graph != 0); problems are recorded per step and the remaining steps are
- * skipped once a problem >= SHL_STOP_SIM is registered. */
+ * skipped once a problem >= SHL_STOP_SIM is registered.  Graph steps with a
+ * fixed dt are fused (each corrector also predicts the next step; the
+ * corrector's candidate-list pass, if due, is made at the start of the next
+ * step); the results are bit for bit those of use_graph = 0, and every call
+ * that returns or reads the state (this one, shl_step_collect, the getters of
+ * the contact state, the setters) first completes a pending pass. */
 shl_status shl_step(shl_ctx* ctx, uint32_t n_steps, const double* pressure_table,
                     int use_graph, shl_step_report* report);
 
@@ -240,7 +245,9 @@ shl_status shl_step(shl_ctx* ctx, uint32_t n_steps, const double* pressure_table
  *  shl_step_enqueue    enqueue n steps (graph replays) without synchronising;
  *                      step k uses table entry k since the last upload;
  *  shl_step_collect    wait for the stream and fill the report of every step
- *                      enqueued since the last collect (or shl_step). */
+ *                      enqueued since the last collect (or shl_step); it also
+ *                      completes a candidate-list pass that the last enqueued
+ *                      step left pending (see shl_step). */
 shl_status shl_get_stream(shl_ctx* ctx, void** stream);
 shl_status shl_upload_pressure_table(shl_ctx* ctx, const double* pressure_table, uint32_t n);
 shl_status shl_step_enqueue(shl_ctx* ctx, uint32_t n_steps);
