@@ -57,9 +57,9 @@ ELEM_BYTES_PER_NODE = 24
 # arithmetic in element_force<12>, fused multiply-add = 2)
 ELEM_FLOPS_PER_FACE = 1372
 # DRAM bytes (read + write) of one element-kernel launch on the level-6 shell,
-# from one ncu --set full capture with caches flushed (38.2 MB read, 3.4 MB
-# written; the force shares mostly stay in the 129 MB L2)
-ELEM_TRAFFIC_LEVEL6 = 41.6e6
+# from one ncu --set full capture with caches flushed (38.6 MB read, 3.4 MB
+# written; the force shares stay in the 129 MB L2 for the gather)
+ELEM_TRAFFIC_LEVEL6 = 42.0e6
 
 
 def ensemble_workload(L, n_shells=256, seed=0):
