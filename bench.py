@@ -450,7 +450,7 @@ def run_ours(args, rank, world, dist):
         "warmstart": warmstart,
         "e2e": {"value": e2e, "unit": "face-steps/s", "h2d_bytes_per_step": 3 * 3 * V * 8,
                 "d2h_bytes_per_step": 3 * 3 * V * 8,
-                "how": "per step: shl_set_state from pinned host, shl_step(1), shl_get_state"},
+                "how": "per step: shl_set_state from pinned host memory, shl_step(1), shl_get_state into pinned host memory (the library reads and writes mapped page-locked buffers with one kernel each way)"},
         "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm, "unit": "GB/s",
                      "frac": achieved_gbs / hbm,
                      "traffic": ELEM_TRAFFIC_LEVEL6 if args.level == 6 else None,

@@ -205,7 +205,9 @@ shl_status shl_apply_initial_conditions(shl_ctx* ctx, const double* u0, double t
                                         double pressure_next);
 
 /* State in and out (ShellSystem::save/load, ShellSystem.C:2956-3153).
- * shl_set_state also sets u_pred = u. */
+ * shl_set_state also sets u_pred = u.  When u, v and a all lie in page-locked
+ * host memory mapped into the device (cudaHostAlloc), one kernel reads or
+ * writes them over the host link; other pointers are copied. */
 shl_status shl_set_state(shl_ctx* ctx, const double* u, const double* v, const double* a);
 shl_status shl_get_state(shl_ctx* ctx, double* u, double* v, double* a);
 shl_status shl_set_time(shl_ctx* ctx, double time, uint32_t time_step);

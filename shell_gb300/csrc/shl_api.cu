@@ -909,10 +909,32 @@ shl_status shl_batch_layout(shl_ctx* c, uint32_t* n_shells, uint32_t* node_offse
   return SHL_OK;
 }
 
+namespace {
+// the device address of page-locked, mapped host memory, or null for any other pointer
+double* mapped_host(const void* p) {
+  if (!p) return nullptr;
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  if (at.type != cudaMemoryTypeHost || at.devicePointer == nullptr) return nullptr;
+  return static_cast<double*>(at.devicePointer);
+}
+}  // namespace
+
 shl_status shl_set_state(shl_ctx* c, const double* u, const double* v, const double* a) {
   if (!c) return SHL_ERR_ARG;
   SHL_TRY(host_access(c));  // pending linked-cell pass; the step prediction is rebuilt
   const size_t nd = 3 * (size_t)c->S.V;
+  double *du = mapped_host(u), *dv = mapped_host(v), *da = mapped_host(a);
+  if (du && dv && da) {
+    // all three in mapped page-locked memory: one kernel reads them over the host link
+    launch_state_host(c->b, c->sc, du, dv, da, true, c->stream);
+    launch_positions(c->b, c->sc, c->stream);
+    SHL_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    return check_launch("shl_set_state");
+  }
   if (u) {
     SHL_TRY(upload(c, c->b.u, u, nd));
     SHL_TRY(upload(c, c->b.up, u, nd));
@@ -927,6 +949,12 @@ shl_status shl_set_state(shl_ctx* c, const double* u, const double* v, const dou
 shl_status shl_get_state(shl_ctx* c, double* u, double* v, double* a) {
   if (!c) return SHL_ERR_ARG;
   const size_t bytes = 3 * (size_t)c->S.V * sizeof(double);
+  double *du = mapped_host(u), *dv = mapped_host(v), *da = mapped_host(a);
+  if (du && dv && da) {
+    launch_state_host(c->b, c->sc, du, dv, da, false, c->stream);
+    SHL_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    return check_launch("shl_get_state");
+  }
   if (u) SHL_CUDA_TRY(cudaMemcpyAsync(u, c->b.u, bytes, cudaMemcpyDeviceToHost, c->stream));
   if (v) SHL_CUDA_TRY(cudaMemcpyAsync(v, c->b.v, bytes, cudaMemcpyDeviceToHost, c->stream));
   if (a) SHL_CUDA_TRY(cudaMemcpyAsync(a, c->b.a, bytes, cudaMemcpyDeviceToHost, c->stream));

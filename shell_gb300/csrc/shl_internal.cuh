@@ -307,6 +307,9 @@ void launch_gather_correct(const DevBuf& b, const StepConst& sc, int mode, bool 
                            double* a_out, cudaStream_t s, RebuildCond rc = {0, 0});
 void launch_volume_end_step(const DevBuf& b, const StepConst& sc, bool end_step, cudaStream_t s);
 void launch_positions(const DevBuf& b, const StepConst& sc, cudaStream_t s);
+// u, v, a between the context and mapped page-locked host memory (device pointers of it)
+void launch_state_host(const DevBuf& b, const StepConst& sc, double* hu, double* hv, double* ha, bool load,
+                       cudaStream_t s);
 cudaError_t init_element_kernels();
 enum : uint32_t { kCtlReset = 1u, kCtlTable = 2u, kCtlArm = 4u };
 void launch_ctl_begin(Ctl* ctl, uint32_t n, uint32_t flags, cudaStream_t s);

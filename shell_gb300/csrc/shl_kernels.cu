@@ -502,6 +502,26 @@ __global__ void k_begin_step(DevBuf b, StepConst sc, RebuildCond rc) {
   begin_step(ctl, sc, sc.dt, ctl->du2_pred, rc, true);
 }
 
+// The state from (hu, hv, ha) or to them: host memory that the device reads and
+// writes directly (page-locked, mapped), one kernel instead of three copies each
+// way.  Loading also sets u_pred = u and the positions, as k_positions does.
+__global__ void k_state_host(DevBuf b, StepConst sc, double* hu, double* hv, double* ha, int load) {
+  const size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  const size_t nd = 3 * (size_t)sc.V;
+  if (k >= nd) return;
+  if (load) {
+    const double u = hu[k];
+    b.u[k] = u;
+    b.up[k] = u;
+    b.v[k] = hv[k];
+    b.a[k] = ha[k];
+  } else {
+    hu[k] = b.u[k];
+    hv[k] = b.v[k];
+    ha[k] = b.a[k];
+  }
+}
+
 // positions only (p = X + u_pred), for force evaluations at a given state
 __global__ void k_positions(DevBuf b, StepConst sc) {
   const uint32_t n = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1975,6 +1995,11 @@ void launch_rebuild_second(const DevBuf& b, const StepConst& sc, cudaStream_t s)
   k_rebuild_second<<<1, 32, 0, s>>>(b, sc);
 }
 void launch_rebuild_first(const DevBuf& b, cudaStream_t s) { k_rebuild_first<<<1, 32, 0, s>>>(b.ctl); }
+void launch_state_host(const DevBuf& b, const StepConst& sc, double* hu, double* hv, double* ha, bool load,
+                       cudaStream_t s) {
+  const size_t nd = 3 * (size_t)sc.V;
+  k_state_host<<<(unsigned)((nd + kBlock - 1) / kBlock), kBlock, 0, s>>>(b, sc, hu, hv, ha, load ? 1 : 0);
+}
 void launch_positions(const DevBuf& b, const StepConst& sc, cudaStream_t s) {
   k_positions<<<nblk(sc.V), kBlock, 0, s>>>(b, sc);
 }

@@ -93,3 +93,31 @@ def test_fused_steps_match_direct(cuda_ok, setup):
     g.step(2, table[22:24], use_graph=True)
     assert_same(snapshot(g), ref)
     g.close()
+
+
+def test_state_through_mapped_host_memory(cuda_ok, setup):
+    """shl_set_state / shl_get_state with page-locked (mapped) host buffers take the
+    one-kernel path; the results equal those of pageable buffers bit for bit."""
+    torch = pytest.importorskip("torch")
+    X, T, p, u0 = setup
+    rng = np.random.default_rng(11)
+    v0 = 1e-4 * rng.standard_normal(u0.shape)
+    a0 = 1e-3 * rng.standard_normal(u0.shape)
+    table = np.zeros(6)
+    out = []
+    for pinned in (False, True):
+        g = L.Shell(X, T, p)
+        if pinned:
+            hu, hv, ha = (torch.from_numpy(x.copy()).pin_memory().numpy() for x in (u0, v0, a0))
+        else:
+            hu, hv, ha = u0.copy(), v0.copy(), a0.copy()
+        g.set_state(hu, hv, ha)
+        g.rebuild_contacts()
+        for k in range(3):
+            g.step(2, table[2 * k:2 * k + 2])
+            g.get_state(out=(hu, hv, ha))
+            g.set_state(hu, hv, ha)
+        out.append([bits(x.copy()) for x in (hu, hv, ha)])
+        g.close()
+    for x, y in zip(out[0], out[1]):
+        assert np.array_equal(x, y)
