@@ -7,26 +7,42 @@ pressure ramped from 0 to 2x the classical buckling pressure over 20,000
 steps, seeded Gaussian normal imperfection of amplitude 1e-3 R, linear
 self-contact with Coulomb friction mu=0.3 and linked cells of 2h.  Inputs are
 synthetic (generated icosphere and seeded imperfection); there is no dataset.
+Over its first 20,000 steps this shell does not buckle: it has no contact
+pairs, and its candidate list is rebuilt about once every 20 steps.
 
 A step is one Newmark step (ShellSystem::advance) of that shell; the metric is
-face-steps per second.  Reported:
-  value      device throughput of the timed steps, each step launched as one
-             CUDA graph and bracketed by CUDA events on the library's stream,
-             with L2 evicted (a 512 MB write) before every step;
-  e2e        the same steps through the C ABI with host buffers: per step the
-             state (u, v, a) is copied from pinned host memory, one step runs,
-             and the state is copied back;
+face-steps per second.  The K timed steps are every S-th step of the run after
+W warm-up steps, S = max(1, 1000 // K): they sample the first 1,000 steps at
+an even stride, so candidate-list rebuilds enter at their rate.  Both arms
+(the library and the CPU reference arm) time exactly these steps.
+Reported:
+  value      device throughput of the timed steps, each launched as one CUDA
+             graph replay and bracketed by CUDA events on the library's
+             stream, with L2 evicted (a 512 MB write) before each; the steps
+             between them run untimed;
+  e2e        the same steps through the C ABI with host buffers: per timed
+             step the state (u, v, a) is copied in from pinned host memory,
+             the step runs, and the state is copied back;
+  run_value  the whole 10,000-step run, replayed back to back (16 steps per
+             graph replay), one pair of CUDA events around it;
+  parity     the 10,000-step run checked against the oracle every 100 steps
+             (same-state force, step and candidate-list checks; the first
+             1,000 steps also in lockstep), and the contact-heavy run;
   roofline   the element-force kernel timed live (events, cold L2) against
-             its algorithmic bytes and FP64 flops;
-  cpu_baseline  the CPU oracle on this host's cores on a bounded sample;
+             its algorithmic bytes, the FP64-equivalent flops and the
+             instruction issue rate;
+  cpu_baseline  the CPU oracle on this host's cores on the same timed steps,
+             with 3 threads (the reference launcher's setting) on a sample,
+             and the full 20,000-step level-3 run;
   contact_modes  LINEAR and SMOOTH self-contact at a squashed, contact-heavy
-             state of the same shell (10 steps each).
+             state of the same shell, with the CPU oracle on the same steps.
 
 python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--level L]
 """
 import argparse
 import json
 import os
+import platform
 import subprocess
 import sys
 import threading
@@ -41,6 +57,8 @@ from shell_gb300.workloads import (ALPHA, AMPL, DT, G12, MU, NU12, RAMP_STEPS, R
                                    classical_pressure, pressure, squashed_state, workload)
 
 FLUSH_BYTES = 512 << 20
+SAMPLE_SPAN = 1000   # the timed steps sample this many steps after the warm-up
+RUN_STEPS = 10000    # the length of the level-6 FP64 run
 # library kernels per step with self-contact: step start (k_begin_step, which also sets the
 # condition of the step's rebuild IF node), element kernel, contact force, gather/corrector
 # (which also predicts the next step), volume/measurement totals/end of step; plus, for each
@@ -48,11 +66,10 @@ FLUSH_BYTES = 512 << 20
 # 3 x 3 scan + 8 contact CSR; the one not due returns at once) and the kernel between them
 LAUNCHES_PER_STEP_CONTACT = 5
 LAUNCHES_PER_REBUILD = 55
-# element kernel (double-float FP64 path): per-face constants as float pairs
-# (38 fields x 8 B), patch ids, force shares (float pairs), element fields,
-# face permutation (bytes); per-node predicted displacement (bytes)
-ELEM_BYTES_PER_FACE = 38 * 8 + 12 * 4 + 36 * 8 + 5 * 8 + 4
-ELEM_BYTES_PER_NODE = 24
+# algorithmic bytes of one face-step of the FP64 path: vertex state u, v, a read and written
+# plus M^-1 and C (96 B per face), per-face constants (R, reference metric, forms, stiffness,
+# JxW: 264 B), connectivity and CSR (96 B); intermediate force shares are not counted
+STEP_BYTES_PER_FACE = 456
 # FP64 flops of one regular face in the element kernel (count of the
 # arithmetic in element_force<12>, fused multiply-add = 2)
 ELEM_FLOPS_PER_FACE = 1372
@@ -60,6 +77,45 @@ ELEM_FLOPS_PER_FACE = 1372
 # from one ncu --set full capture with caches flushed (38.6 MB read, 3.4 MB
 # written; the force shares stay in the 129 MB L2 for the gather)
 ELEM_TRAFFIC_LEVEL6 = 42.0e6
+# warp instructions of one element-kernel launch on the level-6 shell (ncu
+# smsp__inst_executed.sum of the same capture) and the issue peak: 4 schedulers
+# per SM, one warp instruction per cycle each
+ELEM_WARP_INST_LEVEL6 = 30.0e6
+ISSUE_PER_SM_PER_CYCLE = 4
+
+
+def stride_for(K):
+    return max(1, SAMPLE_SPAN // K)
+
+
+def line_config(level, F, V, K, W, world):
+    """The `config` of both arms (identical, so the two lines compare)."""
+    S = stride_for(K)
+    return {"workload": "single shell, level-%d icosphere (%d faces, %d nodes), FP64 element forces and state, "
+                        "self-contact + Coulomb friction (mu 0.3, linked cells 2h), pressure ramp to 2 p_cl over "
+                        "%d steps (dt 1e-4)" % (level, F, V, RAMP_STEPS),
+            "faces": F, "nodes": V,
+            "timed_steps": "%d steps: every %d-th step of steps %d-%d, after %d warm-up steps" % (
+                K, S, W + 1, W + S * K, W),
+            "parallelism": "replicas (one shell per GPU; rank 0 times the CPU arm)" if world > 1 else "single",
+            "l2": "GPU arm: evicted before every timed step (512 MB write); CPU arm: not applicable"}
+
+
+def cpu_model():
+    try:
+        for ln in open("/proc/cpuinfo"):
+            if ln.lower().startswith("model name"):
+                return ln.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    try:
+        out = subprocess.run(["lscpu"], stdout=subprocess.PIPE, text=True).stdout
+        for ln in out.splitlines():
+            if ln.lower().startswith("model name") or ln.lower().startswith("vendor id"):
+                return ln.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return platform.processor() or platform.machine()
 
 
 def ensemble_workload(L, n_shells=256, seed=0):
@@ -119,12 +175,15 @@ def time_ensemble(L, torch, K, W, flush):
             "steps": K, "status": int(status)}
 
 
-def time_contact_modes(L, torch, K, W, flush, level):
+def time_contact_modes(L, torch, K, W, flush, level, cpu=True):
     """Self-contact at a contact-heavy state: the level-`level` shell of the
     main workload squashed to a double layer (every face has candidates on the
     other layer), zero pressure, with the LINEAR (flat triangles) and SMOOTH
     (Loop limit surfaces) narrow phases: K timed steps each (L2 evicted before
-    every step) after W warm-up steps, and the first candidate-list build."""
+    every step) after W warm-up steps, and the first candidate-list build.
+    With `cpu`, the CPU oracle (all host threads) takes the same first build
+    and the first steps from the same state (one step for SMOOTH, whose CPU
+    step takes seconds)."""
     X, T, _, _ = workload(L, level)
     u = squashed_state(X)
     z = np.zeros_like(u)
@@ -159,6 +218,29 @@ def time_contact_modes(L, torch, K, W, flush, level):
                      "n_pairs": int(rep.last.n_pairs), "Nc": int(rep.last.Nc), "n_rebuilds": int(rep.n_rebuilds),
                      "first_build_s": build_s, "status": int(status)}
         g.close()
+        if cpu:
+            import oracle as O
+
+            lib = O.load()
+            o = O.Oracle(X, T, p, threads=os.cpu_count())
+            o.set_state(u, z, z)
+            t0 = time.perf_counter()
+            o.rebuild_contacts()
+            cpu_build = time.perf_counter() - t0
+            # one step with all host threads, one with 3 (the reference launcher's setting); the faster counts
+            times = {}
+            for k, t in enumerate(sorted({os.cpu_count(), min(3, os.cpu_count())}, reverse=True)):
+                lib.oracle_set_threads(t)
+                t0 = time.perf_counter()
+                r, _ = o.step(1, np.zeros(1))
+                times[t] = time.perf_counter() - t0
+            o.close()
+            best = min(times, key=times.get)
+            out[name].update(cpu_value=F / times[best], cpu_ms_per_step=times[best] * 1e3,
+                             cpu_first_build_s=cpu_build, cpu_threads=best,
+                             cpu_steps="steps 1-%d from the squashed state, one step per thread count (%s), "
+                                       "the faster counts" % (len(times), "/".join(str(t) for t in times)),
+                             cpu_n_pairs=int(r.last.n_pairs))
     return out
 
 
@@ -213,25 +295,85 @@ def fp32_accuracy(L, steps=1000, level=7):
     return out
 
 
-def cpu_sample(X, T, p, u0, seconds=10.0, threads=None):
-    """CPU oracle on the same workload: steps until about `seconds` elapsed."""
+def cpu_sampled(X, T, p, u0, K, W, threads=None):
+    """The CPU oracle on the timed steps of the benchmark: W warm-up steps,
+    then K timed steps, every S-th step, the steps between untimed.  Without
+    `threads`, the warm-up steps after the first try all host threads, half of
+    them and 3 (the reference launcher's OMP_NUM_THREADS, script.pl:54), one
+    step each, and the timed steps use the fastest: the oracle keeps the
+    reference's critical-section assembly, which can scale worse than linearly."""
     import oracle as O
 
-    threads = threads or os.cpu_count()
-    o = O.Oracle(X, T, p, threads=threads)
-    o.apply_initial_conditions(u0, 0.0, pressure(1))
-    o.step(1, pressure([1]))
-    t0 = time.perf_counter()
-    o.step(2, pressure([2, 3]))
-    per = (time.perf_counter() - t0) / 2
-    n = int(max(2, min(2000, seconds / max(per, 1e-6))))
-    t0 = time.perf_counter()
-    o.step(n, pressure(np.arange(4, 4 + n)))
-    dt = time.perf_counter() - t0
+    lib = O.load()
+    S = stride_for(K)
+    n = os.cpu_count()
+    cands = [threads] if threads else sorted({n, max(1, n // 2), min(3, n)}, reverse=True)
+    o = O.Oracle(X, T, p, threads=cands[0])
+    o.apply_initial_conditions(u0, 0.0, float(pressure(1)))
+    o.step(1, pressure(np.array([1])))
+    step, probe = 1, {}
+    for t in cands:
+        if step >= W:
+            break
+        lib.oracle_set_threads(t)
+        t0 = time.perf_counter()
+        o.step(1, pressure(np.array([step + 1])))
+        probe[t] = time.perf_counter() - t0
+        step += 1
+    best = min(probe, key=probe.get) if probe else cands[0]
+    lib.oracle_set_threads(best)
+    if step < W:
+        o.step(W - step, pressure(np.arange(step + 1, W + 1)))
+        step = W
+    secs, rebuilds, pairs = 0.0, 0, 0
+    for _ in range(K):
+        if S > 1:
+            o.step(S - 1, pressure(np.arange(step + 1, step + S)))
+            step += S - 1
+        t0 = time.perf_counter()
+        r, _ = o.step(1, pressure(np.array([step + 1])))
+        secs += time.perf_counter() - t0
+        step += 1
+        rebuilds += r.n_rebuilds
+        pairs = max(pairs, r.last.n_pairs)
     o.close()
-    return {"value": len(T) * n / dt, "unit": "face-steps/s", "cores": threads, "kind": "port",
-            "sample": "%d steps (steps 4-%d) of the level-%d workload, %.1f s, OpenMP %d threads"
-                      % (n, 3 + n, int(round(np.log(len(T) / 20) / np.log(4))), dt, threads)}
+    return {"value": len(T) * K / secs, "unit": "face-steps/s", "cores": best, "kind": "port",
+            "sample": "the %d timed steps of the benchmark (every %d-th step of steps %d-%d), %.2f s timed, "
+                      "OpenMP %d threads (fastest of %s on a warm-up step each)"
+                      % (K, S, W + 1, W + S * K, secs, best, "/".join(str(t) for t in cands)),
+            "thread_probe_s": {str(t): v for t, v in probe.items()},
+            "n_rebuilds_timed": int(rebuilds), "n_pairs": int(pairs)}
+
+
+def cpu_rate(X, T, p, u0, n_steps, threads, first_step=1, table=None):
+    """CPU oracle face-steps/s over n_steps consecutive steps from the initial conditions."""
+    import oracle as O
+
+    o = O.Oracle(X, T, p, threads=threads)
+    tbl = pressure(np.arange(first_step, first_step + n_steps)) if table is None else table
+    o.apply_initial_conditions(u0, 0.0, float(tbl[0]))
+    t0 = time.perf_counter()
+    r, st = o.step(n_steps, tbl)
+    secs = time.perf_counter() - t0
+    o.close()
+    return {"value": len(T) * n_steps / secs, "seconds": secs, "steps": int(r.steps_done), "threads": threads,
+            "n_rebuilds": int(r.n_rebuilds), "status": int(st)}
+
+
+def cpu_baseline_extras(api, level, threads_ref=3):
+    """The CPU figures beside the main sample: the level-`level` workload at
+    the reference launcher's 3 OpenMP threads (script.pl:54) on its first 100
+    steps, and the whole 20,000-step level-3 run with all threads and with 3."""
+    X, T, p, u0 = workload(api, level)
+    out = {"cpu_model": cpu_model(), "host_threads": os.cpu_count(),
+           "threads_%d" % threads_ref: dict(cpu_rate(X, T, p, u0, 100, threads_ref),
+                                            sample="steps 1-100 of the level-%d workload" % level)}
+    X3, T3, p3, u03 = workload(api, 3)
+    out["level3_full_run"] = {
+        "workload": "level-3 icosphere (1280 faces), same physics, all 20,000 steps of the ramp",
+        "all_threads": cpu_rate(X3, T3, p3, u03, RAMP_STEPS, os.cpu_count()),
+        "threads_%d" % threads_ref: cpu_rate(X3, T3, p3, u03, RAMP_STEPS, threads_ref)}
+    return out
 
 
 class ClockSampler:
@@ -291,26 +433,163 @@ class ClockSampler:
 
 def run_reference(args, rank, world):
     """The reference arm: the CPU restatement of the reference's step (the
-    reference itself does not build), all host threads, same workload."""
-    import shell_gb300.lib as L
-
+    reference itself does not build), all host threads, on the same timed
+    steps of the same workload.  Inputs come from the oracle's own generators,
+    so this process loads no part of the CUDA library."""
     if rank != 0:
         return
-    X, T, p, u0 = workload(L, args.level)
-    s = cpu_sample(X, T, p, u0, seconds=args.cpu_seconds)
+    import oracle as O
+    from oracle import inputs as I
+
+    O.build()
+    W, K = args.warmup, args.steps
+    X, T, p, u0 = workload(I, args.level)
+    s = cpu_sampled(X, T, p, u0, K, W)
     line = {"metric": "shell face-steps/sec at 1 GB300", "value": s["value"], "unit": "face-steps/s",
-            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+            "n_gpus": world, "steps": K, "warmup": W, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "impl": "reference",
-            "config": {"workload": "single shell, level-%d icosphere (%d faces), FP64, self-contact + friction"
-                                   % (args.level, len(T)), "faces": int(len(T)), "nodes": int(len(X)),
-                       "parallelism": "replicas", "l2": "n/a (CPU)"},
+            "config": line_config(args.level, len(T), len(X), K, W, world),
             "cpu_baseline": {"value": s["value"], "unit": s["unit"], "cores": s["cores"], "kind": "port",
-                             "sample": s["sample"]},
+                             "sample": s["sample"], "cpu_model": cpu_model()},
             "e2e": {"value": s["value"], "unit": "face-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "status": {"n_rebuilds_timed": s["n_rebuilds_timed"], "n_pairs": s["n_pairs"]},
             "note": "the reference needs an unpublished libMesh fork and muparser and misses Contact.C; "
                     "its CPU step is timed through the oracle restatement"}
     print(json.dumps(line), flush=True)
+
+
+def fresh_start(g, u0):
+    """The run from its initial conditions again: empty candidate list, time 0."""
+    g.set_contact_state(np.zeros((0, 2), dtype=np.uint32), du_sum=0.0)
+    g.set_time(0.0, 0)
+    g.apply_initial_conditions(u0, 0.0, float(pressure(1)))
+
+
+def census(g, u0, K, W):
+    """Candidate-list passes and pairs of every step of the sampled window
+    (untimed; a collect after every step, which completes a deferred pass
+    inside the step that asked for it)."""
+    S = stride_for(K)
+    n = W + S * K
+    fresh_start(g, u0)
+    g.upload_pressure_table(pressure(np.arange(1, n + 1)))
+    rebuilds = np.zeros(n + 1, dtype=np.int64)
+    pairs = np.zeros(n + 1, dtype=np.int64)
+    for s in range(1, n + 1):
+        g.step_enqueue(1)
+        r, _ = g.step_collect()
+        rebuilds[s], pairs[s] = r.n_rebuilds, r.last.n_pairs
+    return rebuilds, pairs
+
+
+def timed_sample(g, torch, u0, K, W, flush, dist=None, clock=None):
+    """W warm-up steps, then K timed steps (every S-th step; the steps between
+    run untimed), each one graph replay bracketed by CUDA events on the
+    library's stream after an L2-evicting write.  Returns per-step ms."""
+    S = stride_for(K)
+    fresh_start(g, u0)
+    g.upload_pressure_table(pressure(np.arange(1, W + S * K + 1)))
+    g.step_enqueue(W)
+    torch.cuda.synchronize()
+    g.step_collect()
+    stream = torch.cuda.ExternalStream(g.stream_handle())
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(K)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(K)]
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    if clock:
+        clock.__enter__()
+    with torch.cuda.stream(stream):
+        for k in range(K):
+            if S > 1:
+                g.step_enqueue(S - 1)
+            flush.fill_(k)
+            starts[k].record(stream)
+            g.step_enqueue(1)
+            ends[k].record(stream)
+    torch.cuda.synchronize()
+    if clock:
+        clock.__exit__()
+    if dist:
+        dist.barrier()
+    ms = [a.elapsed_time(e) for a, e in zip(starts, ends)]
+    report, status = g.step_collect()
+    return ms, report, status
+
+
+def e2e_sample(g, torch, u0, K, W):
+    """The timed steps through the C ABI with host buffers: per timed step,
+    shl_set_state from pinned host memory, shl_step(1), shl_get_state into
+    pinned host memory; the steps between run untimed."""
+    S = stride_for(K)
+    fresh_start(g, u0)
+    table = pressure(np.arange(1, W + S * K + 1))
+    g.step(W, table[:W])
+    u, v, a = g.get_state()
+    bufs = [torch.from_numpy(x).pin_memory() for x in (u, v, a)]
+    hu, hv, ha = (b.numpy() for b in bufs)
+    step, secs = W, 0.0
+    for _ in range(K):
+        if S > 1:
+            g.step(S - 1, table[step:step + S - 1])
+            step += S - 1
+            g.get_state(out=(hu, hv, ha))  # the host copy of the state before the timed step
+        t0 = time.perf_counter()
+        g.set_state(hu, hv, ha)
+        g.step(1, table[step:step + 1])
+        g.get_state(out=(hu, hv, ha))
+        secs += time.perf_counter() - t0
+        step += 1
+    return secs
+
+
+def run_value_leg(g, torch, u0, n_steps=RUN_STEPS):
+    """The whole run back to back (graph replays of 16 steps), warm L2."""
+    fresh_start(g, u0)
+    g.upload_pressure_table(pressure(np.arange(1, n_steps + 1)))
+    stream = torch.cuda.ExternalStream(g.stream_handle())
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    with torch.cuda.stream(stream):
+        e0.record(stream)
+        g.step_enqueue(n_steps)
+        e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    rep, st = g.step_collect()
+    return {"value": g.F * n_steps / (ms * 1e-3), "unit": "face-steps/s", "ms_per_step": ms / n_steps,
+            "steps": int(rep.steps_done), "n_rebuilds": int(rep.n_rebuilds), "n_pairs_last": int(rep.last.n_pairs),
+            "status": int(st), "how": "steps 1-%d of the run, %d graph replays of 16 steps, one pair of CUDA events, "
+                                      "warm L2" % (n_steps, (n_steps + 15) // 16)}
+
+
+def parity_leg(L, level, n_steps, lockstep_steps, contact_steps):
+    """The run checked against the oracle every 100 steps, and the
+    contact-heavy run from the squashed state every 25 steps (oracle.protocol)."""
+    import oracle as O
+    from oracle import protocol
+
+    X, T, p, u0 = workload(L, level)
+
+    def summary(r):
+        return {k: r[k] for k in ("steps", "checks", "check_every", "lockstep_steps", "same_state_bit_exact",
+                                  "lockstep_equal", "worst", "n_rebuilds", "n_rebuilds_oracle_lockstep",
+                                  "max_pairs", "max_Nc", "seconds")}
+
+    out = {"tolerances": "forces and accelerations at the same state 1e-12 relative; one step from the same state "
+                         "1e-12; pair lists, FP64 d^2 and stick flags bit for bit"}
+    r = protocol.run(L, O, X, T, p, u0=u0, n_steps=n_steps, check_every=100, lockstep_steps=lockstep_steps,
+                     pressure=pressure, threads=os.cpu_count())
+    out["run"] = summary(r)
+    if contact_steps > 0:
+        u = squashed_state(X)
+        z = np.zeros_like(u)
+        rc = protocol.run(L, O, X, T, p, state0=(u, z, z), n_steps=contact_steps, check_every=25,
+                          lockstep_steps=25, threads=os.cpu_count())
+        out["contact"] = dict(summary(rc), workload="the same shell squashed to a double layer, zero pressure")
+    return out
 
 
 def run_ours(args, rank, world, dist):
@@ -322,106 +601,59 @@ def run_ours(args, rank, world, dist):
     torch.cuda.set_device(dev)
     X, T, p, u0 = workload(L, args.level)
     F, V = len(T), len(X)
-    g = L.Shell(X, T, p)
-    g.apply_initial_conditions(u0, 0.0, pressure(1))
-    stream = torch.cuda.ExternalStream(g.stream_handle())
-    flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.int32, device="cuda")
     W, K = args.warmup, args.steps
-    g.upload_pressure_table(pressure(np.arange(1, 1 + W + K)))
-    # warm-up (graph instantiation, first rebuilds); the report then covers the timed steps only
-    g.step_enqueue(W)
-    torch.cuda.synchronize()
-    g.step_collect()
-    starts = [torch.cuda.Event(enable_timing=True) for _ in range(K)]
-    ends = [torch.cuda.Event(enable_timing=True) for _ in range(K)]
-    if dist:
-        dist.barrier()
-    torch.cuda.synchronize()
-    with ClockSampler(dev) as clk:
-        with torch.cuda.stream(stream):
-            for k in range(K):
-                flush.fill_(k)
-                starts[k].record(stream)
-                g.step_enqueue(1)
-                ends[k].record(stream)
-        torch.cuda.synchronize()
-    if dist:
-        dist.barrier()
-    ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
-    report, status = g.step_collect()
+    S = stride_for(K)
+    g = L.Shell(X, T, p)
+    flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.int32, device="cuda")
+    reb, pairs = census(g, u0, K, W)
+    timed_idx = W + S * (np.arange(K) + 1)
+    clk = ClockSampler(dev)
+    ms_list, report, status = timed_sample(g, torch, u0, K, W, flush, dist, clk)
+    ms = sum(ms_list)
     if dist:
         t = torch.tensor([ms], dtype=torch.float64, device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
     value = F * K * world / (ms * 1e-3)
+    rebuild_steps = np.zeros(K, dtype=bool)
+    rebuild_steps[:] = reb[timed_idx] > 0
+    ms_arr = np.array(ms_list)
+    window = {"n_rebuilds_timed": int(reb[timed_idx].sum()), "n_pairs_max": int(pairs[timed_idx].max()),
+              "ms_plain_step_median": float(np.median(ms_arr[~rebuild_steps])) if (~rebuild_steps).any() else None,
+              "ms_rebuild_step_median": float(np.median(ms_arr[rebuild_steps])) if rebuild_steps.any() else None,
+              "n_rebuilds_window": int(reb[W + 1:].sum())}
 
-    # the same workload with FP32 element forces (FP64 state and contact), cold L2 per step
+    # the same timed steps with FP32 element forces (FP64 state and contact)
     fp32_value = None
     if args.fp32:
         p32 = L.default_params(**{k: getattr(p, k) for k, _ in L._PARAM_FIELDS if not k.startswith("pad")})
         p32.precision = L.PREC_FP32
         g32 = L.Shell(X, T, p32)
-        g32.apply_initial_conditions(u0, 0.0, pressure(1))
-        s32 = torch.cuda.ExternalStream(g32.stream_handle())
-        g32.upload_pressure_table(pressure(np.arange(1, 1 + W + K)))
-        g32.step_enqueue(W)
-        torch.cuda.synchronize()
-        st32 = [torch.cuda.Event(enable_timing=True) for _ in range(K)]
-        en32 = [torch.cuda.Event(enable_timing=True) for _ in range(K)]
-        with torch.cuda.stream(s32):
-            for k in range(K):
-                flush.fill_(k)
-                st32[k].record(s32)
-                g32.step_enqueue(1)
-                en32[k].record(s32)
-        torch.cuda.synchronize()
-        ms32 = sum(a.elapsed_time(b) for a, b in zip(st32, en32))
-        g32.step_collect()
+        ms32, _, _ = timed_sample(g32, torch, u0, K, W, flush)
         g32.close()
-        fp32_value = F * K / (ms32 * 1e-3)
+        fp32_value = F * K / (sum(ms32) * 1e-3)
+
+    e2e_s = e2e_sample(g, torch, u0, K, W)
+    e2e = F * K * world / e2e_s
+    run_value = run_value_leg(g, torch, u0)
 
     ensemble = time_ensemble(L, torch, max(20, K // 4), W, flush) if args.ensemble else None
-    contact_modes = time_contact_modes(L, torch, 10, 2, flush, args.level) if args.contact_modes else None
+    contact_modes = (time_contact_modes(L, torch, 10, 2, flush, args.level, cpu=rank == 0)
+                     if args.contact_modes else None)
     accuracy = fp32_accuracy(L) if args.accuracy else None
     warmstart = None
     if args.warmstart:
         from shell_gb300 import warmstart as WS
         warmstart = WS.experiment(n_train=args.ws_train, n_test=args.ws_test, log=lambda m: print(m, file=sys.stderr))
 
-    # warm continuous throughput (informative): K steps back to back, one graph replay per 16 steps
-    g.upload_pressure_table(pressure(np.arange(1 + W + K, 1 + W + 2 * K)))
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with torch.cuda.stream(stream):
-        e0.record(stream)
-        g.step_enqueue(K)
-        e1.record(stream)
-    torch.cuda.synchronize()
-    warm = F * K / (e0.elapsed_time(e1) * 1e-3)
-    g.step_collect()
-
-    # e2e through the C ABI with pinned host buffers
-    u, v, a = g.get_state()
-    hu = torch.from_numpy(u).pin_memory()
-    hv = torch.from_numpy(v).pin_memory()
-    ha = torch.from_numpy(a).pin_memory()
-    nu_, nv_, na_ = hu.numpy(), hv.numpy(), ha.numpy()
-    Ke = max(8, K // 4)
-    pt = pressure(np.arange(1 + W + 2 * K, 1 + W + 2 * K + Ke))
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for k in range(Ke):
-        g.set_state(nu_, nv_, na_)
-        g.step(1, pt[k:k + 1])
-        g.get_state(out=(nu_, nv_, na_))
-    e2e_s = time.perf_counter() - t0
-    e2e = F * Ke * world / e2e_s
-
-    # roofline of the element kernel (live, cold L2)
+    # roofline of the element kernel (live, cold L2), at the state after the run
     elem_ms = g.time_kernel(0, reps=20, flush_bytes=FLUSH_BYTES)
     elem_variant = g.element_variant()[1]
     fp64_peak = L.measure_fp64_peak()
     g.close()
-    bytes_elem = F * ELEM_BYTES_PER_FACE + V * ELEM_BYTES_PER_NODE
+    parity = (parity_leg(L, args.level, args.parity_steps, args.parity_lockstep, args.parity_contact)
+              if args.parity_steps > 0 and rank == 0 else None)
+    bytes_elem = F * STEP_BYTES_PER_FACE
     achieved_gbs = bytes_elem / (elem_ms * 1e-3) / 1e9
     achieved_tf = F * ELEM_FLOPS_PER_FACE / (elem_ms * 1e-3) / 1e12
     peaks = {}
@@ -430,41 +662,58 @@ def run_ours(args, rank, world, dist):
     except (OSError, ValueError):
         pass
     hbm = peaks.get("hbm_gbs", 6800.0)
+    hbm_src = "MEASURED_PEAKS.json hbm_gbs (of measured)" if "hbm_gbs" in peaks else "fallback 6800 GB/s (of fallback)"
+    clocks = clk.summary()
+    sm_ghz = (clocks.get("sm_max_mhz") or 2070.0) / 1e3
+    issue_peak = ISSUE_PER_SM_PER_CYCLE * 152 * sm_ghz  # G warp instructions / s
     if rank != 0:
         return
-    cpu = cpu_sample(X, T, p, u0, seconds=args.cpu_seconds) if args.cpu_seconds > 0 else None
+    cpu = None
+    if args.cpu_baseline:
+        cpu = cpu_sampled(X, T, p, u0, K, W)
+        cpu["cpu_model"] = cpu_model()
+        cpu.update(cpu_baseline_extras(L, args.level))
     line = {
         "metric": "shell face-steps/sec at 1 GB300", "value": value, "unit": "face-steps/s", "n_gpus": world,
         "steps": K, "warmup": W, "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "single shell, level-%d icosphere (%d faces, %d nodes), FP64 element forces and "
-                               "state, self-contact + Coulomb friction, pressure ramp to 2 p_cl over %d steps, "
-                               "steps %d-%d of the run" % (args.level, F, V, RAMP_STEPS, W + 1, W + K),
-                   "faces": F, "nodes": V, "parallelism": "replicas (one shell per GPU)" if world > 1 else "single",
-                   "l2": "evicted before every timed step (512 MB write)"},
-        "warm_value": warm,
+        "config": line_config(args.level, F, V, K, W, world),
+        "window": window,
+        "run_value": run_value,
         "fp32_value": fp32_value,
         "ensemble": ensemble,
         "contact_modes": contact_modes,
         "fp32_accuracy": accuracy,
         "warmstart": warmstart,
+        "parity": parity,
         "e2e": {"value": e2e, "unit": "face-steps/s", "h2d_bytes_per_step": 3 * 3 * V * 8,
                 "d2h_bytes_per_step": 3 * 3 * V * 8,
-                "how": "per step: shl_set_state from pinned host memory, shl_step(1), shl_get_state into pinned host memory (the library reads and writes mapped page-locked buffers with one kernel each way)"},
+                "how": "per timed step: shl_set_state from pinned host memory, shl_step(1), shl_get_state into "
+                       "pinned host memory (the library reads and writes mapped page-locked buffers with one "
+                       "kernel each way)"},
         "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm, "unit": "GB/s",
                      "frac": achieved_gbs / hbm,
                      "traffic": ELEM_TRAFFIC_LEVEL6 if args.level == 6 else None,
                      "traffic_note": "bytes per launch, ncu capture of the level-6 element kernel",
+                     "algorithmic_bytes": "%d B per face-step x %d faces" % (STEP_BYTES_PER_FACE, F),
                      "kernel": "k_elements", "variant": elem_variant,
-                     "kernel_ms": elem_ms, "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)",
+                     "kernel_ms": elem_ms, "peak_source": hbm_src,
+                     "issue": {"warp_inst_per_launch": ELEM_WARP_INST_LEVEL6 if args.level == 6 else None,
+                               "achieved_ginst_s": (ELEM_WARP_INST_LEVEL6 / (elem_ms * 1e-3) / 1e9
+                                                    if args.level == 6 else None),
+                               "peak_ginst_s": issue_peak,
+                               "frac": (ELEM_WARP_INST_LEVEL6 / (elem_ms * 1e-3) / 1e9 / issue_peak
+                                        if args.level == 6 else None),
+                               "note": "instruction issue: the bound of the double-float element kernel "
+                                       "(4 warp instructions per SM per cycle at the sampled max SM clock)"},
                      "fp64": {"achieved_tflops": achieved_tf, "peak_tflops": fp64_peak,
                               "frac": achieved_tf / fp64_peak,
                               "flops": "FP64-equivalent flops of the element arithmetic (executed as float "
                                        "pairs on the FP32 pipe by the double-float variants)",
                               "peak_source": "DFMA register loop measured in this run"}},
         "cpu_baseline": cpu,
-        "clocks": clk.summary(),
-        "gpu_launches": LAUNCHES_PER_STEP_CONTACT * K + LAUNCHES_PER_REBUILD * report.n_rebuilds,
+        "clocks": clocks,
+        "gpu_launches": LAUNCHES_PER_STEP_CONTACT * S * K + LAUNCHES_PER_REBUILD * int(reb[W + 1:].sum()),
         "status": {"worst_problem": report.worst_problem, "steps_done": report.steps_done,
                    "n_rebuilds": report.n_rebuilds, "n_pairs": report.last.n_pairs},
     }
@@ -474,16 +723,20 @@ def run_ours(args, rank, world, dist):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=400)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--level", type=int, default=6)
-    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--cpu-baseline", type=int, default=1, help="time the CPU oracle beside the GPU (rank 0)")
     ap.add_argument("--fp32", type=int, default=1, help="also time the FP32 element-force mode")
     ap.add_argument("--ensemble", type=int, default=1, help="also time the 256-shell batched ensemble")
     ap.add_argument("--accuracy", type=int, default=1, help="also report the level-7 FP32-vs-FP64 accuracy")
     ap.add_argument("--contact-modes", type=int, default=1,
                     help="also time LINEAR and SMOOTH self-contact at a squashed (contact-heavy) state")
+    ap.add_argument("--parity-steps", type=int, default=RUN_STEPS,
+                    help="steps of the run checked against the oracle every 100 steps (0 = no parity leg)")
+    ap.add_argument("--parity-lockstep", type=int, default=1000, help="of these, steps also run by the oracle")
+    ap.add_argument("--parity-contact", type=int, default=100, help="steps of the contact-heavy parity run")
     ap.add_argument("--warmstart", type=int, default=0,
                     help="also run the learned warm-start study (level-5 shells; minutes of GPU time)")
     ap.add_argument("--ws-train", type=int, default=3584)
@@ -493,9 +746,10 @@ def main():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     dist = None
-    import __graft_entry__
+    if args.impl == "ours":
+        import __graft_entry__
 
-    __graft_entry__.build()
+        __graft_entry__.build()
     if world > 1:
         import torch
         import torch.distributed as tdist

@@ -305,12 +305,13 @@ shl_status shl_get_element_fields(shl_ctx* ctx, double* kGauss, double* kMean, d
 /* Element-kernel variants (launch shape; for FP64, the arithmetic of the two
  * basis contractions): shl_create times the shapes of the context's path on
  * its mesh and keeps the fastest (autotuning).  shl_set_element_variant forces
- * one (0-9 FP64, 10-12 FP32; 0 and 5 keep the displacement contraction in
- * FP64, 6-9 compute in double-float) or, with -1, tunes again; shl_get_element_variant
+ * one (0-10 FP64, 11-13 FP32; 0 and 5 keep the displacement contraction in
+ * FP64, 6-10 compute in double-float, 10 in one round of faces: one block of
+ * 544 threads per SM, a face per thread) or, with -1, tunes again; shl_get_element_variant
  * returns the choice, its name and the tuning times of all
  * SHL_ELEMENT_VARIANTS (ms, 0 = not timed; tuned_ms holds that many floats).
  * No counterpart in the reference. */
-enum { SHL_ELEMENT_VARIANTS = 13 };
+enum { SHL_ELEMENT_VARIANTS = 14 };
 shl_status shl_set_element_variant(shl_ctx* ctx, int variant);
 shl_status shl_get_element_variant(shl_ctx* ctx, int* variant, char* name, size_t cap, float* tuned_ms);
 
@@ -441,12 +442,15 @@ shl_status shl_gaussian_normal_imperfection(const double* xyz, uint32_t n_nodes,
  * f_dev (3*n_nodes doubles, device) receives f = pressure force - internal
  * force at the predicted displacement u_dev (3*n_nodes doubles, device), as
  * f_out of shl_eval_forces for a shell without self-contact and with
- * bulk_modulus = 0 (both are rejected here).  The set-up data are the
- * context's (read only); the per-(face, slot) force shares go to a scratch
- * array compiled into the library (a static device array of 36 doubles x
- * 32768 faces = 9 MiB that every GPU which loads the library holds until the
- * process exits), so shells above 32768 faces are rejected with
- * SHL_ERR_CAPACITY.  The context's own buffers and step state are untouched.
+ * bulk_modulus = 0 (both are rejected here).  Only the context's constant
+ * set-up data are read; its state, buffers and step prediction are untouched.
+ * The per-(face, patch node) force shares go to a scratch array compiled into
+ * the library: a static device array of 12 * 32768 slots of 3 doubles (9 MiB)
+ * that every GPU which loads the library holds until the process exits.  A
+ * face of a 12-node patch takes 12 slots, so shells of up to 32768 faces of
+ * regular patches fit; patches around vertices of valence N take N + 6 slots.
+ * Shells with more slots are rejected with SHL_ERR_CAPACITY.  The call must
+ * be made with the context's device current (else SHL_ERR_ARG).
  *
  * The first call on a device looks up the scratch address there (and may
  * make the CUDA runtime load the library's device code); make that first call

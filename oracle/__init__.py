@@ -33,7 +33,7 @@ def load():
         return _lib
     if not os.path.exists(LIB_PATH):
         build()
-    from shell_gb300.lib import ShlEnergies, ShlMesh, ShlParams, ShlStepReport
+    from shell_gb300.abi import ShlEnergies, ShlMesh, ShlParams, ShlStepReport
 
     lib = ctypes.CDLL(LIB_PATH)
     vp, d, u32, sz = ctypes.c_void_p, ctypes.c_double, ctypes.c_uint32, ctypes.c_size_t
@@ -91,13 +91,15 @@ class Oracle:
     """CPU restatement of one ShellSystem (FP64)."""
 
     def __init__(self, X, T, params, threads=None):
-        from shell_gb300.lib import make_mesh
+        from shell_gb300.abi import ShlMesh
 
         self.lib = load()
         if threads is not None:
             self.lib.oracle_set_threads(threads)
-        m, keep = make_mesh(X, T)
-        self.X, self.T = keep
+        X = np.ascontiguousarray(X, dtype=np.float64)
+        T = np.ascontiguousarray(T, dtype=np.uint32)
+        m = ShlMesh(X.shape[0], T.shape[0], X.ctypes.data, T.ctypes.data)
+        self.X, self.T = X, T
         self.V, self.F = self.X.shape[0], self.T.shape[0]
         self.params = params
         self.h = self.lib.oracle_create(ctypes.byref(m), ctypes.byref(params))
@@ -138,7 +140,7 @@ class Oracle:
         return t.value, s.value
 
     def eval_forces(self, u_pred, v_pred, pressure):
-        from shell_gb300.lib import ShlEnergies
+        from shell_gb300.abi import ShlEnergies
 
         u_pred = np.ascontiguousarray(u_pred, dtype=np.float64).reshape(-1)
         v_pred = np.ascontiguousarray(v_pred, dtype=np.float64).reshape(-1)
@@ -149,7 +151,7 @@ class Oracle:
         return f, a, e.as_dict(), st
 
     def step(self, n, pressure_table=None):
-        from shell_gb300.lib import ShlStepReport
+        from shell_gb300.abi import ShlStepReport
 
         r = ShlStepReport()
         pt = None if pressure_table is None else np.ascontiguousarray(pressure_table, dtype=np.float64)

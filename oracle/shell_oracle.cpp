@@ -38,8 +38,16 @@
  * irregular patch (the quadrature point (1/3,1/3) lies in the middle
  * sub-triangle after one step, as in SubdivEvaluation.C:170-187, 110-135).
  *
- * Build with -ffp-contract=off: the contact geometry must round like the
- * device code (shl_geom.h).
+ * The narrow phase (ShellShellContact::compute, ShellShellContact.C:35-145)
+ * and the friction law (Friction::apply, Friction.C:4-60) are restated here
+ * on the oracle's own vector type, in the reference's order of operations.
+ * The only contact code shared with the library is shl_distance.h: the two
+ * closest-point routines that the reference declares but does not ship
+ * (Contact.h:22-34, Contact.C missing).
+ *
+ * Build with -ffp-contract=off: every multiply and add is rounded on its own,
+ * as the device code does (__dmul_rn/__dadd_rn), so candidate lists agree bit
+ * for bit.
  */
 #include "oracle.h"
 
@@ -60,7 +68,10 @@
 #include "../shell_gb300/csrc/shl_expr.h"
 #include "../shell_gb300/csrc/shl_smooth.h"
 #include "../shell_gb300/csrc/shl_subdiv.h"
-#include "../shell_gb300/csrc/shl_geom.h"
+#include "../shell_gb300/csrc/shl_distance.h"
+#ifdef SHL_GEOM_H_
+#error "the oracle restates the narrow phase and friction; it must not compile the library's versions"
+#endif
 
 namespace {
 
@@ -93,6 +104,118 @@ struct Point {
 };
 inline Point operator*(Real s, const Point& p) { return p * s; }
 static_assert(sizeof(Point) == 3 * sizeof(Real), "positions are read as packed xyz");
+
+// ---- narrow phase: ShellShellContact::compute (ShellShellContact.C:35-57) ----
+// d2, the contact vector dc (element 1 -> element 2) and the barycentric
+// coordinates (v, w) of the closest points on both elements.
+struct PairGeom {
+  Real d2;
+  Point dc;
+  Real v[2], w[2];
+};
+
+// edge_edge_test (ShellShellContact.C:89-113): each edge of element 1 against
+// each edge of element 2, edge i running from node i to node mod3[i]; a pair of
+// edges replaces the current minimum only when strictly closer.
+void edge_edge_test(const Point* const p[2][3], PairGeom& c) {
+  static const unsigned int mod3[3] = {1, 2, 0};
+  Real st[2];
+  Point this_dc;
+  for (unsigned int i = 0; i < 3; ++i) {
+    for (unsigned int j = 0; j < 3; ++j) {
+      shl_segment_segment(p[0][i]->x, p[0][mod3[i]]->x, p[1][j]->x, p[1][mod3[j]]->x, this_dc.x, st);
+      const Real this_d2 = this_dc.size_sq();
+      if (this_d2 < c.d2) {
+        c.d2 = this_d2;
+        c.dc = this_dc;
+        c.v[0] = (i == 0) * st[0] + (i == 1) * (1 - st[0]);
+        c.w[0] = (i == 1) * st[0] + (i == 2) * (1 - st[0]);
+        c.v[1] = (j == 0) * st[1] + (j == 1) * (1 - st[1]);
+        c.w[1] = (j == 1) * st[1] + (j == 2) * (1 - st[1]);
+      }
+    }
+  }
+}
+
+// vertex_face_test (ShellShellContact.C:115-145): each vertex of each element
+// against the face of the other; dc is turned to point from element 1 to 2.
+void vertex_face_test(const Point* const p[2][3], PairGeom& c) {
+  Real vw[2];
+  Point this_dc;
+  for (unsigned int i = 0; i < 2; ++i) {
+    for (unsigned int j = 0; j < 3; ++j) {
+      shl_point_triangle(p[i][j]->x, p[1 - i][0]->x, p[1 - i][1]->x, p[1 - i][2]->x, this_dc.x, vw);
+      const Real this_d2 = this_dc.size_sq();
+      if (this_d2 < c.d2) {
+        c.d2 = this_d2;
+        c.dc = (i == 0 ? this_dc : -this_dc);
+        c.v[0] = (i == 0) * (j == 1) + (i == 1) * vw[0];
+        c.w[0] = (i == 0) * (j == 2) + (i == 1) * vw[1];
+        c.v[1] = (i == 1) * (j == 1) + (i == 0) * vw[0];
+        c.w[1] = (i == 1) * (j == 2) + (i == 0) * vw[1];
+      }
+    }
+  }
+}
+
+void shell_shell_compute(const Point* const p[2][3], PairGeom& c) {
+  c.d2 = std::numeric_limits<Real>::max();
+  c.dc = Point();
+  c.v[0] = c.v[1] = c.w[0] = c.w[1] = 0;
+  edge_edge_test(p, c);
+  vertex_face_test(p, c);
+}
+
+// ---- Friction::apply (Friction.C:4-60): Margolis slip-stick law -------------
+// f_contact is zero on entry (the callers' fresh vector); stick and
+// spring_origin are the contact's persistent state.
+void friction_apply(Real& Efric, Point& f_contact, Real f_normal, const Point& n, const Point& v, Real abs_v_normal,
+                    Real v_stop, Real spring_stiffness, Real mu_s, Real mu_d, Real damping, bool& stick,
+                    Point& spring_origin, const Point& contact_point) {
+  // tangential velocity
+  const Point v_normal = abs_v_normal * n;
+  const Point v_tangential = v - v_normal;
+  const Real abs_v_tangential = v_tangential.size();
+  const Real v_eps = 1e-8 * v_stop;
+  // static part
+  if (mu_s > 0 && abs_v_tangential <= v_stop) {
+    if (!stick) {
+      // a new spring, sized so that the force is continuous from dynamic to static
+      stick = true;
+      const Real prefactor = mu_d * f_normal / (spring_stiffness * (abs_v_tangential + v_eps)) - damping;
+      spring_origin = contact_point - prefactor * v_tangential;
+    }
+    Point u_spring = contact_point - spring_origin;
+    u_spring -= (u_spring * n) * n;  // tangential part of the spring
+    Efric = 0.5 * spring_stiffness * u_spring.size_sq();
+    f_contact = -spring_stiffness * u_spring;
+    f_contact -= damping * spring_stiffness * v_tangential;
+  }
+  // dynamic part
+  if (abs_v_tangential > v_stop || f_contact.size_sq() >= std::pow(mu_s * f_normal, 2)) {
+    spring_origin.zero();
+    stick = false;
+    Efric = 0;
+    f_contact = -mu_d * f_normal / (abs_v_tangential + v_eps) * v_tangential;
+  }
+}
+
+// The summation order of avg_elem_size (ShellSystem.C:2572, 2584).  The
+// reference leaves it to OpenMP; the library fixes it so that host and device
+// agree: 1024 lanes, lane l adding x[l], x[l + 1024], ... in index order, then
+// the lanes combined pairwise (strides 512, 256, ..., 1).
+Real fixed_order_sum(const Real* x, unsigned n) {
+  const unsigned lanes = 1024;
+  std::vector<Real> lane(lanes, 0.0);
+  for (unsigned l = 0; l < lanes; ++l) {
+    Real s = 0;
+    for (unsigned i = l; i < n; i += lanes) s = s + x[i];
+    lane[l] = s;
+  }
+  for (unsigned stride = lanes / 2; stride > 0; stride /= 2)
+    for (unsigned l = 0; l < stride; ++l) lane[l] = lane[l] + lane[l + stride];
+  return lane[0];
+}
 
 struct Tensor {  // 3x3, row major
   Real a[3][3];
@@ -367,6 +490,7 @@ struct oracle {
   Real dt_step = 0;       // dt of the last accepted step
   bool accepted = false;  // the last advance() accepted a step
   uint64_t rejections = 0;
+  uint64_t n_rebuilds = 0;  // candidate-list rebuilds made (forced or triggered)
   shl::expr::Expression pfun;  // pressure as an expression of t, when set
   bool has_pfun = false;
 
@@ -428,16 +552,13 @@ struct oracle {
       smooth_compute(c);
       return;
     }
-    const double* p1[3];
-    const double* p2[3];
-    for (int n = 0; n < 3; ++n) {
-      p1[n] = on_mesh ? X[tri[3 * c.eid[0] + n]].x : p[tri[3 * c.eid[0] + n]].x;
-      p2[n] = on_mesh ? X[tri[3 * c.eid[1] + n]].x : p[tri[3 * c.eid[1] + n]].x;
-    }
-    shl_pair_geom g;
-    shl_pair_compute(p1, p2, &g);
+    const Point* pp[2][3];
+    for (int e = 0; e < 2; ++e)
+      for (int n = 0; n < 3; ++n) pp[e][n] = on_mesh ? &X[tri[3 * c.eid[e] + n]] : &p[tri[3 * c.eid[e] + n]];
+    PairGeom g;
+    shell_shell_compute(pp, g);
     c.d2 = g.d2;
-    c.dc = Point(g.dc[0], g.dc[1], g.dc[2]);
+    c.dc = g.dc;
     c.v[0] = g.v[0]; c.v[1] = g.v[1]; c.w[0] = g.w[0]; c.w[1] = g.w[1];
   }
   Point contact_point(const Contact& c) const {  // ShellShellContact::point()
@@ -892,7 +1013,7 @@ void oracle::compute_bounding_box() {
     if (d2 > dmax) dmax = d2;
     sizes[eid] = dmax;
   }
-  avg_elem_size = shl_fixed_order_sum(sizes.data(), F) / F;
+  avg_elem_size = fixed_order_sum(sizes.data(), F) / F;
 }
 
 void oracle::compute_deformed_metrics() {
@@ -1067,10 +1188,10 @@ void oracle::add_cavity_force() {
       Point f_contact;
       if (cavity_friction) {
         Real Efric_node = 0;
-        int stick = cav_origin[nid].size_sq() != 0 ? 1 : 0;
-        shl_friction_apply(&Efric_node, f_contact.x, f_normal, n.x, vel.x, abs_v_normal, P.friction_stop_velocity,
-                           stiff_static_friction, P.mu_s_cavity, P.mu_d_cavity, P.cavity_friction_damping, &stick,
-                           cav_origin[nid].x, pp.x);
+        bool stick = cav_origin[nid].size_sq() != 0;
+        friction_apply(Efric_node, f_contact, f_normal, n, vel, abs_v_normal, P.friction_stop_velocity,
+                       stiff_static_friction, P.mu_s_cavity, P.mu_d_cavity, P.cavity_friction_damping, stick,
+                       cav_origin[nid], pp);
         Efric_sum += Efric_node;
         efric_vec[nid] += Efric_node / area_node;
       }
@@ -1131,12 +1252,12 @@ void oracle::add_shell_shell_contact_force() {
       const Real abs_v_normal = v_rel * n;
       Point f_contact;
       if (self_friction) {
-        int stick = contact->stick ? 1 : 0;
+        bool stick = contact->stick;
         const Point cp = contact_point(*contact);
-        shl_friction_apply(&Efric_contact, f_contact.x, f_normal, n.x, v_rel.x, abs_v_normal,
-                           P.friction_stop_velocity, stiff_static_friction, P.mu_s, P.mu_d,
-                           P.self_friction_damping, &stick, contact->spring_origin.x, cp.x);
-        contact->stick = stick != 0;
+        friction_apply(Efric_contact, f_contact, f_normal, n, v_rel, abs_v_normal, P.friction_stop_velocity,
+                       stiff_static_friction, P.mu_s, P.mu_d, P.self_friction_damping, stick,
+                       contact->spring_origin, cp);
+        contact->stick = stick;
         Efric_sum += Efric_contact;
       }
       f_normal -= P.self_damping * stiffness * abs_v_normal;
@@ -1255,6 +1376,7 @@ void oracle::compute_shell_shell_contact_candidates(bool force) {
   Real cell_size = P.cell_size_mult * avg_elem_size;
   Real tolerance = P.cell_margin * cell_size;
   if (!(force || du_sum >= tolerance)) return;
+  ++n_rebuilds;
   du_sum = 0;
   compute_bounding_box();
   cell_size = P.cell_size_mult * avg_elem_size;
@@ -1627,7 +1749,7 @@ int oracle_step(oracle* o, uint32_t n_steps, const double* pressure_table, shl_s
   std::memset(&rep, 0, sizeof(rep));
   int worst = 0;
   uint32_t done = 0;
-  const uint64_t rej0 = o->rejections;
+  const uint64_t rej0 = o->rejections, reb0 = o->n_rebuilds;
   for (uint32_t s = 0; s < n_steps; ++s) {
     o->current_problem = 0;
     ++o->time_step;
@@ -1663,6 +1785,7 @@ int oracle_step(oracle* o, uint32_t n_steps, const double* pressure_table, shl_s
   }
   rep.steps_done = done;
   rep.rejections = (uint32_t)(o->rejections - rej0);
+  rep.n_rebuilds = (uint32_t)(o->n_rebuilds - reb0);
   rep.worst_problem = worst;
   rep.time = o->time;
   rep.du_sum = o->du_sum;
@@ -1937,23 +2060,37 @@ void oracle_point_triangle(const double* p0, const double* p1, const double* p2,
 }
 
 void oracle_pair_compute(const double* p, double* out) {
-  const double* p1[3] = {p, p + 3, p + 6};
-  const double* p2[3] = {p + 9, p + 12, p + 15};
-  shl_pair_geom g;
-  shl_pair_compute(p1, p2, &g);
+  Point q[2][3];
+  const Point* pp[2][3];
+  for (int e = 0; e < 2; ++e)
+    for (int n = 0; n < 3; ++n) {
+      q[e][n] = Point(p[9 * e + 3 * n], p[9 * e + 3 * n + 1], p[9 * e + 3 * n + 2]);
+      pp[e][n] = &q[e][n];
+    }
+  PairGeom g;
+  shell_shell_compute(pp, g);
   out[0] = g.d2;
-  out[1] = g.dc[0]; out[2] = g.dc[1]; out[3] = g.dc[2];
+  out[1] = g.dc(0); out[2] = g.dc(1); out[3] = g.dc(2);
   out[4] = g.v[0]; out[5] = g.w[0]; out[6] = g.v[1]; out[7] = g.w[1];
 }
 
 void oracle_friction_apply(double* Efric, double* f_contact, double f_normal, const double* n, const double* v,
                            double abs_v_normal, double v_stop, double k, double mu_s, double mu_d,
                            double damping, int* stick, double* spring_origin, const double* contact_point) {
-  shl_friction_apply(Efric, f_contact, f_normal, n, v, abs_v_normal, v_stop, k, mu_s, mu_d, damping, stick,
-                     spring_origin, contact_point);
+  Point fc(f_contact[0], f_contact[1], f_contact[2]), so(spring_origin[0], spring_origin[1], spring_origin[2]);
+  bool st = *stick != 0;
+  Real E = *Efric;
+  friction_apply(E, fc, f_normal, Point(n[0], n[1], n[2]), Point(v[0], v[1], v[2]), abs_v_normal, v_stop, k, mu_s,
+                 mu_d, damping, st, so, Point(contact_point[0], contact_point[1], contact_point[2]));
+  *Efric = E;
+  *stick = st ? 1 : 0;
+  for (int c = 0; c < 3; ++c) {
+    f_contact[c] = fc(c);
+    spring_origin[c] = so(c);
+  }
 }
 
-double oracle_fixed_order_sum(const double* x, uint32_t n) { return shl_fixed_order_sum(x, n); }
+double oracle_fixed_order_sum(const double* x, uint32_t n) { return fixed_order_sum(x, n); }
 
 int oracle_fp_contract_off(void) {
   volatile double x = 1.0 + 1.0 / (1 << 30);  // x*x = 1 + 2^-29 + 2^-60

@@ -92,6 +92,12 @@ int bs_index(int block) { return block == 64 ? 0 : block == 128 ? 1 : 2; }
 ElemLaunch elem_launch(const shl_ctx* c, const StepConst& sc) {
   ElemLaunch el;
   el.variant = sc.fp32 ? c->var32 : c->var64;
+  if (el.variant == kFlatVariant) {
+    // one face per thread over the whole mesh; the groups are found by face index
+    el.blocks = (sc.F + kFlatBlock - 1) / kFlatBlock;
+    el.eg = c->eg_bs[0];
+    return el;
+  }
   const int k = bs_index(kElemVariants[el.variant].block);
   el.blocks = c->blocks_bs[k];
   el.eg = c->eg_bs[k];
@@ -1908,17 +1914,27 @@ shl_status shl_get_mass_damping(shl_ctx* c, double* Minv, double* C) {
 shl_status shl_internal_force_noalloc(shl_ctx* c, const double* u_dev, double pressure, double* f_dev,
                                       void* stream) {
   if (!c || !u_dev || !f_dev) { g_err = "null argument"; return SHL_ERR_ARG; }
-  SHL_TRY(host_access(c));  // pending linked-cell pass; the step prediction is rebuilt
   if (c->sc.contact || c->P.bulk_modulus != 0.0 || c->sc.fp32) {
     g_err = "shl_internal_force_noalloc: self-contact, bulk-modulus pressure and FP32 element forces are not "
             "evaluated here";
     return SHL_ERR_ARG;
   }
-  if (c->S.n_slots_total > 12 * noalloc_max_faces()) {
-    g_err = "shl_internal_force_noalloc: " + std::to_string(c->S.F) + " faces exceed the scratch limit of " +
-            std::to_string(noalloc_max_faces()) + " regular faces";
+  if (c->S.n_slots_total > noalloc_max_slots()) {
+    g_err = "shl_internal_force_noalloc: the shell has " + std::to_string(c->S.n_slots_total) +
+            " (face, patch node) slots, above the scratch limit of " + std::to_string(noalloc_max_slots()) +
+            " slots (32768 faces of 12-node patches)";
     return SHL_ERR_CAPACITY;
   }
+  int dev = -1;
+  SHL_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev != c->device) {
+    g_err = "shl_internal_force_noalloc: the current device (" + std::to_string(dev) +
+            ") is not the context's device (" + std::to_string(c->device) + ")";
+    return SHL_ERR_ARG;
+  }
+  // Only the context's constant set-up data are read (patches, face constants,
+  // basis, gather CSR): no step state, so a pending candidate-list pass or the
+  // stored prediction are neither needed nor changed.
   const double p = c->P.compat_zero_pressure ? pressure * 0.0 : pressure;
   cudaError_t e = launch_force_noalloc(c->b, c->sc, c->eg, c->elem_blocks, u_dev, p, f_dev, (cudaStream_t)stream);
   if (e != cudaSuccess) {

@@ -65,7 +65,11 @@ struct ElemVariant {
   const char* name;
 };
 constexpr int kNumElemVariants = SHL_ELEMENT_VARIANTS;
-constexpr int kFirstFp32Variant = 10;
+constexpr int kFirstFp32Variant = 11;
+// the one-round double-float element kernel (variant kFlatVariant): one block
+// of 544 threads (17 warps, 120 registers each) per SM, one face per thread
+constexpr int kFlatVariant = 10;
+constexpr int kFlatBlock = 544;
 extern const ElemVariant kElemVariants[kNumElemVariants];
 
 // The element launch of a context: variant, grid and patch-group block ranges for its block size.
@@ -315,7 +319,7 @@ enum : uint32_t { kCtlReset = 1u, kCtlTable = 2u, kCtlArm = 4u };
 void launch_ctl_begin(Ctl* ctl, uint32_t n, uint32_t flags, cudaStream_t s);
 void launch_fp64_peak(double* out, int blocks, int iters, cudaStream_t s);
 // allocation-free force evaluation (scratch in a static device array)
-uint32_t noalloc_max_faces();
+uint64_t noalloc_max_slots();
 cudaError_t launch_force_noalloc(const DevBuf& ctx_b, const StepConst& sc, const ElemGroups& eg, uint32_t n_blocks,
                                  const double* u, double pressure, double* f_out, cudaStream_t s);
 void launch_shell_norms(const double* f, const double* fext, const double* mass, const uint32_t* node_off,

@@ -21,6 +21,7 @@
 
 #include <algorithm>
 #include <cstdint>
+#include <mutex>
 
 #include "shl_geom.h"
 #include "shl_internal.cuh"
@@ -207,6 +208,12 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 // (hi and lo float4) of up to 12 patch slots per thread
 constexpr int kDfStageSlots = 12;
 constexpr size_t df_stage_bytes(int block) { return (size_t)kDfStageSlots * 2 * sizeof(float4) * block; }
+// the one-round kernel: staging columns of its block plus the basis tables
+// (hi and lo floats) of every patch group
+constexpr size_t flat_smem_bytes() {
+  return df_stage_bytes(kFlatBlock) + (size_t)kMaxGroups * 2 * kMaxSlots * 6 * sizeof(float);
+}
+static_assert(flat_smem_bytes() <= 232448, "the one-round element kernel exceeds the shared memory of a block");
 
 // ---------------------------------------------------------------- cavity --
 // effective semi-axes and friction scope (update_derived, ShellSystem.C:421-436)
@@ -954,13 +961,11 @@ __device__ __forceinline__ ElemOut element_force32(uint32_t i, int np_rt, uint32
 // and kMean already divided by the area.
 template <int NP>
 __device__ __forceinline__ ElemOut element_force_df(uint32_t i, int np_rt, uint32_t slot0,
-                                                    const double* __restrict__ B, const DevBuf& b,
-                                                    const StepConst& sc, double pressure_d, double vol_p_d,
-                                                    float4* __restrict__ su) {
+                                                    const float* __restrict__ Bh, const float* __restrict__ Bl,
+                                                    const DevBuf& b, const StepConst& sc, double pressure_d,
+                                                    double vol_p_d, float4* __restrict__ su) {
   const uint32_t F = sc.F;
   const int np = NP > 0 ? NP : np_rt;
-  const float* Bh = reinterpret_cast<const float*>(B + kMaxSlots * 6);
-  const float* Bl = Bh + kMaxSlots * 6;
   const uint32_t t = threadIdx.x, bs = blockDim.x;
   if (NP > 0) {
     // all patch ids, then all node displacements copied asynchronously into this
@@ -1207,13 +1212,58 @@ __global__ void __launch_bounds__(BS, MINB) k_elements_df(DevBuf b, StepConst sc
   const double pr = pressure * __ldg(&b.pscale[i]);
   ElemOut o;
   if (gd.n_slots == 12)
-    o = element_force_df<12>(i, 12, slot0, sB, b, sc, pr, vol_p, su);
+    o = element_force_df<12>(i, 12, slot0, sBh, sBl, b, sc, pr, vol_p, su);
   else if (gd.n_slots == 11)
-    o = element_force_df<11>(i, 11, slot0, sB, b, sc, pr, vol_p, su);
+    o = element_force_df<11>(i, 11, slot0, sBh, sBl, b, sc, pr, vol_p, su);
   else
-    o = element_force_df<0>(i, gd.n_slots, slot0, sB, b, sc, pr, vol_p, su);
+    o = element_force_df<0>(i, gd.n_slots, slot0, sBh, sBl, b, sc, pr, vol_p, su);
   const uint32_t e = __ldg(&b.perm[i]);
   b.area[e] = o.area;  // the other fields come per unit area
+  b.kG[e] = o.kg;
+  b.kM[e] = o.km;
+  b.etens[e] = o.etens;
+  b.ebend[e] = o.ebend;
+}
+
+// The double-float element kernel in one round of faces: thread t of block k
+// takes face k * BS + t of the whole mesh (all patch groups), so with one
+// 544-thread block per SM a level-6 shell (81,920 faces on 152 SMs) runs every
+// face at once.  The shapes above run 1.4 rounds there, and since a face is a
+// long dependent chain, the second, partly filled round costs as much as the
+// first.  Each thread picks its patch group (groups are contiguous face
+// ranges) and the basis tables of all groups sit in shared memory after the
+// staging columns.  The per-face arithmetic is that of k_elements_df.
+template <int BS>
+__global__ void __launch_bounds__(BS, 1) k_elements_df_flat(DevBuf b, StepConst sc, ElemGroups eg) {
+  Ctl* ctl = b.ctl;
+  if (inactive(ctl)) return;
+  extern __shared__ float4 su[];  // kDfStageSlots x 2 x BS staging, then per group the basis (hi, lo)
+  float* sBall = reinterpret_cast<float*>(su + (size_t)kDfStageSlots * 2 * BS);
+  for (int g = 0; g < eg.n; ++g) {
+    float* h = sBall + g * (2 * kMaxSlots * 6);
+    for (int k = threadIdx.x; k < eg.g[g].n_slots * 6; k += blockDim.x)
+      df_split(eg.basis[eg.g[g].basis_off + k], h[k], h[kMaxSlots * 6 + k]);
+  }
+  __syncthreads();
+  const uint32_t i = blockIdx.x * BS + threadIdx.x;
+  if (i >= sc.F) return;
+  int g = 0;
+  while (g + 1 < eg.n && i >= eg.g[g + 1].first) ++g;
+  const GroupDesc gd = eg.g[g];
+  const float* Bh = sBall + g * (2 * kMaxSlots * 6);
+  const float* Bl = Bh + kMaxSlots * 6;
+  const double pressure = ctl->pressure, vol_p = ctl->volume_pressure;
+  const uint32_t slot0 = gd.slot_base + (i - gd.first) * (uint32_t)gd.n_slots;
+  const double pr = pressure * __ldg(&b.pscale[i]);
+  ElemOut o;
+  if (gd.n_slots == 12)
+    o = element_force_df<12>(i, 12, slot0, Bh, Bl, b, sc, pr, vol_p, su);
+  else if (gd.n_slots == 11)
+    o = element_force_df<11>(i, 11, slot0, Bh, Bl, b, sc, pr, vol_p, su);
+  else
+    o = element_force_df<0>(i, gd.n_slots, slot0, Bh, Bl, b, sc, pr, vol_p, su);
+  const uint32_t e = __ldg(&b.perm[i]);
+  b.area[e] = o.area;
   b.kG[e] = o.kg;
   b.kM[e] = o.km;
   b.etens[e] = o.etens;
@@ -2041,7 +2091,7 @@ const ElemVariant kElemVariants[kNumElemVariants] = {
     {256, 0, "fp64 256x1"},        {256, 1, "fp64 256x1 pair-G"}, {128, 1, "fp64 128x3 pair-G"},
     {64, 1, "fp64 64x5 pair-G"},   {64, 1, "fp64 64x6 pair-G"},   {64, 0, "fp64 64x5"},
     {256, 2, "fp64 256x1 df"},     {128, 2, "fp64 128x3 df"},     {64, 2, "fp64 64x6 df"},
-    {64, 2, "fp64 64x8 df"},
+    {64, 2, "fp64 64x8 df"},       {kFlatBlock, 2, "fp64 544x1 df flat"},
     {256, 0, "fp32 256x2"},        {128, 0, "fp32 128x4"},        {64, 0, "fp32 64x8"}};
 
 // the double-float kernels take more than the default 48 KB of shared memory
@@ -2058,6 +2108,12 @@ cudaError_t init_element_kernels() {
   set((const void*)k_elements_df<128, 3>, 128);
   set((const void*)k_elements_df<64, 6>, 64);
   set((const void*)k_elements_df<64, 8>, 64);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute((const void*)k_elements_df_flat<kFlatBlock>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)flat_smem_bytes());
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute((const void*)k_elements_df_flat<kFlatBlock>,
+                             cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
   return e;
 }
 
@@ -2075,8 +2131,9 @@ void launch_elements(const DevBuf& b, const StepConst& sc, const ElemLaunch& el,
     case 7: k_elements_df<128, 3><<<nb, 128, df_stage_bytes(128), s>>>(b, sc, eg); break;
     case 8: k_elements_df<64, 6><<<nb, 64, df_stage_bytes(64), s>>>(b, sc, eg); break;
     case 9: k_elements_df<64, 8><<<nb, 64, df_stage_bytes(64), s>>>(b, sc, eg); break;
-    case 10: k_elements32<256, 2><<<nb, 256, 0, s>>>(b, sc, eg); break;
-    case 11: k_elements32<128, 4><<<nb, 128, 0, s>>>(b, sc, eg); break;
+    case 10: k_elements_df_flat<kFlatBlock><<<nb, kFlatBlock, flat_smem_bytes(), s>>>(b, sc, eg); break;
+    case 11: k_elements32<256, 2><<<nb, 256, 0, s>>>(b, sc, eg); break;
+    case 12: k_elements32<128, 4><<<nb, 128, 0, s>>>(b, sc, eg); break;
     default: k_elements32<64, 8><<<nb, 64, 0, s>>>(b, sc, eg); break;
   }
   if (totals) k_elem_totals<<<nblk(sc.F), kBlock, 0, s>>>(b, sc);
@@ -2109,31 +2166,35 @@ void launch_volume_end_step(const DevBuf& b, const StepConst& sc, bool end_step,
 // the per-(face, slot) force shares go to a file-scope scratch array instead of
 // a buffer of the context.  See shl_internal_force_noalloc in include/shl.h.
 
-// Largest shell this path accepts (faces).  The scratch holds 36 doubles per
-// face: 32768 faces -> 9 MiB, resident on every GPU that loads the library.
-constexpr uint32_t kNoAllocMaxFaces = 32768;
-static __device__ __align__(256) double g_noalloc_scratch[(size_t)kNoAllocMaxFaces * 36];
+// Largest shell this path accepts: 12 * 32768 (face, patch node) slots of 3
+// doubles each, i.e. 32768 faces of regular 12-node patches (fewer where
+// patches around vertices of valence above 6 have more nodes) -> 9 MiB,
+// resident on every GPU that loads the library.
+constexpr uint64_t kNoAllocMaxSlots = 12ull * 32768ull;
+static __device__ __align__(256) double g_noalloc_scratch[kNoAllocMaxSlots * 3];
 
 // Device address of the scratch array per device, looked up once per device
 // (cudaGetSymbolAddress on the host side; the array name itself is only a
-// host-side stand-in).
-static void* g_noalloc_ptr[64];
-static bool g_noalloc_ready[64];
+// host-side stand-in).  std::call_once orders first calls made by several
+// host threads on one device.
+constexpr int kNoAllocDevices = 64;
+static std::once_flag g_noalloc_once[kNoAllocDevices];
+static void* g_noalloc_ptr[kNoAllocDevices];
+static cudaError_t g_noalloc_err[kNoAllocDevices];
 
-uint32_t noalloc_max_faces() { return kNoAllocMaxFaces; }
+uint64_t noalloc_max_slots() { return kNoAllocMaxSlots; }
 
 cudaError_t noalloc_scratch(void** ptr) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
-  if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
-  if (!g_noalloc_ready[dev]) {
+  if (dev < 0 || dev >= kNoAllocDevices) return cudaErrorInvalidDevice;
+  std::call_once(g_noalloc_once[dev], [dev] {
     void* p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess) return e;
+    g_noalloc_err[dev] = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     g_noalloc_ptr[dev] = p;
-    g_noalloc_ready[dev] = true;
-  }
+  });
+  if (g_noalloc_err[dev] != cudaSuccess) return g_noalloc_err[dev];
   *ptr = g_noalloc_ptr[dev];
   return cudaSuccess;
 }

@@ -45,7 +45,7 @@
  *    f, or after SHL_SMOOTH_MAX_IT iterations.
  *
  * Every floating-point operation is rounded on its own (SHL_MUL / SHL_ADD of
- * shl_geom.h) or is an explicit fused multiply-add (fma, IEEE on both sides);
+ * shl_distance.h) or is an explicit fused multiply-add (fma, IEEE on both sides);
  * frexp / ldexp are exact, so host and device agree bit for bit.
  */
 #ifndef SHL_SMOOTH_H_
@@ -53,7 +53,7 @@
 
 #include <stdint.h>
 
-#include "shl_geom.h"
+#include "shl_distance.h"
 
 #ifndef __CUDACC__
 #include <math.h>

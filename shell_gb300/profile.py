@@ -3,10 +3,12 @@ kernel profilers (the CUDA graphs of shl_step hold conditional nodes, whose
 kernels profilers cannot replay one by one).
 
 python -m shell_gb300.profile [--level 6] [--warmup 3] [--steps 5] [--squashed] [--contact linear|smooth|none]
-    [--phases] [--variant V]
+    [--phases] [--variant V] [--start N]
 
 --squashed starts from the double-layer state of the contact-mode benchmark
-instead of the imperfect sphere; --phases also prints shl_profile_step's
+instead of the imperfect sphere; --start N first runs N steps of the ramp as
+graph replays (not profiled kernels: give ncu a kernel filter), so that the
+profiled steps lie later in the run; --phases also prints shl_profile_step's
 per-phase event times (predictor, linked cells, elements, contact, gather,
 volume) of one more step.
 """
@@ -28,6 +30,7 @@ def main(argv=None):
     ap.add_argument("--contact", default="linear", choices=["linear", "smooth", "none"])
     ap.add_argument("--phases", action="store_true")
     ap.add_argument("--variant", type=int, default=-1, help="element-kernel variant (-1: the autotuned one)")
+    ap.add_argument("--start", type=int, default=0, help="steps of the ramp run as graph replays first")
     a = ap.parse_args(argv)
     mode = {"linear": L.CONTACT_LINEAR, "smooth": L.CONTACT_SMOOTH, "none": L.CONTACT_NONE}[a.contact]
     X, T, p, u0 = workload(L, a.level, contact=mode)
@@ -42,7 +45,9 @@ def main(argv=None):
         table = np.zeros(a.warmup + a.steps + 1)
     else:
         g.apply_initial_conditions(u0, 0.0, pressure(1))
-        table = pressure(np.arange(1, a.warmup + a.steps + 2))
+        if a.start > 0:
+            g.step(a.start, pressure(np.arange(1, a.start + 1)), use_graph=True)
+        table = pressure(np.arange(a.start + 1, a.start + a.warmup + a.steps + 2))
     g.step(a.warmup, table[:a.warmup], use_graph=False)
     t0 = time.perf_counter()
     r, st = g.step(a.steps, table[a.warmup:a.warmup + a.steps], use_graph=False)

@@ -20,16 +20,23 @@ def classical_pressure():
     return 2 * E * H * H / np.sqrt(3 * (1 - nu * nu))
 
 
-def workload(L, level, contact=None):
-    """Mesh, parameters and initial displacement of the single-shell workload."""
-    X, T = L.icosphere(level)
+def workload(api, level, contact=None):
+    """Mesh, parameters and initial displacement of the single-shell workload.
+
+    `api` provides icosphere, default_params, gaussian_normal_imperfection and
+    the CONTACT_* constants: the library's binding (shell_gb300.lib) or the
+    oracle's own input generators (oracle.inputs), which give the same inputs
+    bit for bit without loading the CUDA library.  Every parameter whose
+    default differs between the two is set here."""
+    X, T = api.icosphere(level)
     P = X[T]
     cell_mult = 2 * H / (P.max(axis=1) - P.min(axis=1)).max(axis=1).mean()
-    p = L.default_params(shell_mass_density=RHO, shell_young_modulus=E1, shell_young_modulus2=E2,
-                         shell_poisson_ratio=NU12, shell_shear_modulus=G12, thickness=H, damping_alpha=ALPHA, dt=DT,
-                         shell_shell_contact=L.CONTACT_LINEAR if contact is None else contact, mu_s=MU, mu_d=MU,
-                         cell_size_mult=cell_mult)
-    u0 = L.gaussian_normal_imperfection(X, AMPL, SEED).reshape(-1)
+    p = api.default_params(shell_mass_density=RHO, shell_young_modulus=E1, shell_young_modulus2=E2,
+                           shell_poisson_ratio=NU12, shell_shear_modulus=G12, thickness=H, damping_alpha=ALPHA,
+                           dt=DT, shell_shell_contact=api.CONTACT_LINEAR if contact is None else contact, mu_s=MU,
+                           mu_d=MU, cell_size_mult=cell_mult, adapt_dt_every=0, rel_loc_err_min=5e-5,
+                           rel_loc_err_max=5e-4, shell_cavity_contact=0)
+    u0 = api.gaussian_normal_imperfection(X, AMPL, SEED).reshape(-1)
     return X, T, p, u0
 
 

@@ -29,6 +29,23 @@ def bits(x):
     return np.ascontiguousarray(x).view(np.uint64)
 
 
+def _mapped_device_pointer(host_ptr):
+    """Device address of a page-locked host buffer (driver API
+    cuPointerGetAttribute), or 0 when the buffer is not mapped host memory."""
+    import ctypes
+
+    cu = ctypes.CDLL("libcuda.so.1")
+    CU_POINTER_ATTRIBUTE_MEMORY_TYPE, CU_POINTER_ATTRIBUTE_DEVICE_POINTER, CU_MEMORYTYPE_HOST = 2, 3, 1
+    mtype, dptr = ctypes.c_uint(0), ctypes.c_uint64(0)
+    if cu.cuPointerGetAttribute(ctypes.byref(mtype), CU_POINTER_ATTRIBUTE_MEMORY_TYPE, ctypes.c_void_p(host_ptr)):
+        return 0
+    if mtype.value != CU_MEMORYTYPE_HOST:
+        return 0
+    if cu.cuPointerGetAttribute(ctypes.byref(dptr), CU_POINTER_ATTRIBUTE_DEVICE_POINTER, ctypes.c_void_p(host_ptr)):
+        return 0
+    return dptr.value
+
+
 def snapshot(g):
     u, v, a = g.get_state()
     c = g.contact_state()
@@ -109,6 +126,9 @@ def test_state_through_mapped_host_memory(cuda_ok, setup):
         g = L.Shell(X, T, p)
         if pinned:
             hu, hv, ha = (torch.from_numpy(x.copy()).pin_memory().numpy() for x in (u0, v0, a0))
+            # the library takes its one-kernel path only for mapped page-locked memory
+            for x in (hu, hv, ha):
+                assert _mapped_device_pointer(x.ctypes.data), "pinned buffer is not mapped into the device"
         else:
             hu, hv, ha = u0.copy(), v0.copy(), a0.copy()
         g.set_state(hu, hv, ha)

@@ -93,6 +93,30 @@ def test_eval_forces_valence_5_6_7(cuda_ok, precision):
     g.close()
 
 
+@pytest.mark.parametrize("variant", [6, 7, 8, 9, 10])
+def test_double_float_variants_match_oracle(cuda_ok, variant):
+    """Every launch shape of the double-float element kernel, forced, on a mesh
+    with valence-5, -6 and -7 patches (the one-round shape takes faces of all
+    patch groups in one block): forces and element fields within 1e-12."""
+    X, T = flipped_sphere(1)
+    rng = np.random.default_rng(21)
+    p = physics_params(contact=False)
+    g = L.Shell(X, T, p)
+    g.set_element_variant(variant)
+    assert g.element_variant()[0] == variant
+    o = O.Oracle(X, T, p, threads=4)
+    u = smooth_state(X, rng)
+    v = 1e-3 * rng.standard_normal(u.shape)
+    pres = -classical_pressure()
+    fg, ag, eg, _ = g.eval_forces(u, v, pres)
+    fo, ao, eo, _ = o.eval_forces(u, v, pres)
+    assert rel(fg, fo) < FORCE_TOL and rel(ag, ao) < FORCE_TOL
+    fe_g, fe_o = g.element_fields(), o.element_fields()
+    for k in ("etens", "ebend", "area"):
+        assert rel(fe_g[k], fe_o[k]) < 1e-11, k
+    g.close()
+
+
 def test_mass_damping_match(cuda_ok, meshes):
     X, T = meshes[3]
     p = physics_params(damping_beta=0.01, damping_gamma=0.002)
