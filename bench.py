@@ -53,7 +53,7 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-from shell_gb300.workloads import (ALPHA, AMPL, DT, G12, MU, NU12, RAMP_STEPS, RHO, SEED,  # noqa: E402
+from shell_gb300.workloads import (ALPHA, AMPL, DT, G12, MU, NU12, RAMP_STEPS, RHO, SEED, ensemble_workload,  # noqa: E402
                                    classical_pressure, pressure, squashed_state, workload)
 
 FLUSH_BYTES = 512 << 20
@@ -118,43 +118,9 @@ def cpu_model():
     return platform.processor() or platform.machine()
 
 
-def ensemble_workload(L, n_shells=256, seed=0):
-    """256 shells, levels uniform over 3/4/5, per-shell parameters from a seed:
-    E1/E2 log-uniform in [0.2, 5] (E1 E2 = 1), h/R log-uniform in [0.005, 0.05],
-    pressure ramp end uniform in [1.2, 3] p_cl of the shell, imperfection
-    amplitude log-uniform in [1e-4, 1e-2] R; FP32 element forces."""
-    rng = np.random.default_rng(seed)
-    meshes = {lv: L.icosphere(lv) for lv in (3, 4, 5)}
-    shells, params, scale, u0 = [], [], [], []
-    for k in range(n_shells):
-        lv = int(rng.integers(3, 6))
-        r = float(np.exp(rng.uniform(np.log(0.2), np.log(5.0))))
-        h = float(np.exp(rng.uniform(np.log(0.005), np.log(0.05))))
-        s = float(rng.uniform(1.2, 3.0))
-        amp = float(np.exp(rng.uniform(np.log(1e-4), np.log(1e-2))))
-        e1, e2 = np.sqrt(r), 1.0 / np.sqrt(r)
-        E = np.sqrt(e1 * e2)
-        nu = np.sqrt(NU12 * NU12 * e2 / e1)
-        p_cl = 2 * E * h * h / np.sqrt(3 * (1 - nu * nu))
-        X, T = meshes[lv]
-        params.append(L.default_params(shell_mass_density=RHO, shell_young_modulus=e1, shell_young_modulus2=e2,
-                                       shell_poisson_ratio=NU12, shell_shear_modulus=G12 * E, thickness=h,
-                                       damping_alpha=ALPHA, dt=DT, shell_shell_contact=L.CONTACT_NONE,
-                                       precision=L.PREC_FP32))
-        shells.append((X, T))
-        scale.append(s * p_cl)
-        u0.append(L.gaussian_normal_imperfection(X, amp, seed * 100000 + k).reshape(-1))
-    return shells, params, np.array(scale), np.concatenate(u0)
-
-
-def time_ensemble(L, torch, K, W, flush):
-    shells, params, scale, u0 = ensemble_workload(L)
-    b = L.Batch(shells, params, pressure_scale=scale)
-    ramp = lambda st: -np.asarray(st, dtype=np.float64) / RAMP_STEPS  # noqa: E731
-    b.apply_initial_conditions(u0, 0.0, ramp(1))
-    b.upload_pressure_table(ramp(np.arange(1, 1 + W + K)))
-    b.step_enqueue(W)
-    torch.cuda.synchronize()
+def _timed_batch_steps(b, torch, K, flush):
+    """K single-step graph replays of a batch, each bracketed by CUDA events on
+    the batch's stream with L2 evicted before it; returns the summed ms."""
     stream = torch.cuda.ExternalStream(b.stream_handle())
     st = [torch.cuda.Event(enable_timing=True) for _ in range(K)]
     en = [torch.cuda.Event(enable_timing=True) for _ in range(K)]
@@ -165,14 +131,54 @@ def time_ensemble(L, torch, K, W, flush):
             b.step_enqueue(1)
             en[k].record(stream)
     torch.cuda.synchronize()
-    ms = sum(a.elapsed_time(e) for a, e in zip(st, en))
+    return sum(a.elapsed_time(e) for a, e in zip(st, en))
+
+
+def time_ensemble(L, torch, K, W, flush):
+    """The 256-shell ensemble: K steps of its pressure ramp after W warm-up
+    steps (no shell is in contact yet; every shell's linked-cell trigger runs),
+    and K steps with every shell squashed to a double layer (zero pressure:
+    each shell's candidate list is long and rebuilt as it moves)."""
+    shells, params, scale, u0 = ensemble_workload(L)
+    b = L.Batch(shells, params, pressure_scale=scale)
+    ramp = lambda st: -np.asarray(st, dtype=np.float64) / RAMP_STEPS  # noqa: E731
+    b.apply_initial_conditions(u0, 0.0, ramp(1))
+    b.upload_pressure_table(ramp(np.arange(1, 1 + W + K)))
+    b.step_enqueue(W)
+    torch.cuda.synchronize()
+    ms = _timed_batch_steps(b, torch, K, flush)
     rep, status = b.step_collect()
+    _, nr0 = b.contact_stats()
+    n_pairs = len(b.contact_state()["pairs"])
+    # contact-heavy: every shell flattened to a double layer
+    rng = np.random.default_rng(7)
+    us = []
+    for X, _ in shells:
+        u = np.zeros_like(X)
+        u[:, 2] = (0.0042 - 1.0) * X[:, 2]
+        us.append((u + 2e-5 * rng.standard_normal(X.shape)).reshape(-1))
+    z = np.zeros(3 * b.V)
+    b.set_state(np.concatenate(us), z, z)
+    b.rebuild_contacts()
+    b.upload_pressure_table(np.zeros(W + K))
+    b.step_enqueue(W)
+    torch.cuda.synchronize()
+    _, nr1 = b.contact_stats()
+    ms_c = _timed_batch_steps(b, torch, K, flush)
+    rep_c, status_c = b.step_collect()
+    _, nr2 = b.contact_stats()
+    pairs_c = len(b.contact_state()["pairs"])
     F = b.F
     b.close()
     levels = [int(round(np.log(len(T) / 20) / np.log(4))) for _, T in shells]
     return {"value": F * K / (ms * 1e-3), "unit": "face-steps/s", "ms_per_step": ms / K, "shells": len(shells),
-            "faces": int(F), "levels": {str(lv): levels.count(lv) for lv in (3, 4, 5)}, "dtype": "f32 forces, f64 state",
-            "steps": K, "status": int(status)}
+            "faces": int(F), "levels": {str(lv): levels.count(lv) for lv in (3, 4, 5)},
+            "dtype": "f32 forces, f64 state and contact gaps", "contact": "linear + friction, per-shell linked cells",
+            "steps": K, "status": int(status), "n_pairs": int(n_pairs), "shell_rebuilds_total": int(nr0.sum()),
+            "contact_heavy": {"value": F * K / (ms_c * 1e-3), "ms_per_step": ms_c / K, "n_pairs": int(pairs_c),
+                              "shell_rebuilds_in_timed_steps": int((nr2 - nr1).sum()),
+                              "status": int(status_c),
+                              "state": "every shell squashed to a double layer, zero pressure"}}
 
 
 def time_contact_modes(L, torch, K, W, flush, level, cpu=True):

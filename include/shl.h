@@ -181,14 +181,25 @@ const char* shl_status_string(shl_status s);
  * per process).  Each shell has its own mesh and material/damping/thickness;
  * dt, the Newmark parameters, the precision and the pressure basis are
  * shared.  The pressure of shell k in a step is pressure_scale[k] times the
- * step's value (its ramp).  Self-contact and bulk-modulus pressure are
- * evaluated for single shells only (rejected here).  State vectors of a batch
+ * step's value (its ramp).  Bulk-modulus pressure is evaluated for single
+ * shells only (rejected here); self-contact is per shell (below).  State vectors of a batch
  * are the shells' node-major vectors concatenated; shl_batch_layout gives the
  * node and face offsets (n_shells + 1 entries each).  Energies and the volume
  * reported by shl_step are batch totals. */
 shl_status shl_batch_create(const shl_mesh* meshes, const shl_params* params, const double* pressure_scale,
                             uint32_t n_shells, shl_ctx** out);
 shl_status shl_batch_layout(shl_ctx* ctx, uint32_t* n_shells, uint32_t* node_offsets, uint32_t* face_offsets);
+/* Self-contact in a batch: every shell keeps its own linked cells -- its own
+ * rebuild trigger (check_increment, ShellSystem.C:2591-2652), bounds, cell
+ * size, d_max and cell grid (ShellSystem.C:1910-2135) -- so each shell's
+ * candidate list and contact forces are those of the shell run alone; the
+ * grids share one counting sort.  Shells must share the contact mode, the
+ * friction coefficients, the contact damping, the cell margin and a fixed dt.
+ * shl_batch_contact_stats gives each shell's du_sum and the number of its
+ * candidate-list rebuilds since creation (n_shells entries; either pointer may
+ * be NULL).  Pairs reported by shl_get_contact_pairs use batch face ids.
+ * No counterpart in the reference, which runs one shell per process. */
+shl_status shl_batch_contact_stats(shl_ctx* ctx, double* du_sum, uint32_t* n_rebuilds);
 
 /* Set-up: ShellSystem::set_parameters + build_cache + compute_mass_damping
  * (ShellSystem.C:170-418, 490-681, 762-852).  Computes the subdivision basis,
@@ -336,9 +347,13 @@ shl_status shl_get_mass_damping(shl_ctx* ctx, double* Minv, double* C);
  * context; SHL_RESIDUAL_CORRECT (FP32 context, with FP64) also stores the
  * defect f64 - f32 at this state, which the following steps add to their FP32
  * force (mixed-precision defect correction, so relaxation converges to the
- * FP64 equilibrium); SHL_RESIDUAL_CLEAR drops a stored defect.
+ * FP64 equilibrium); SHL_RESIDUAL_CLEAR drops a stored defect;
+ * SHL_RESIDUAL_CONTACT (self-contact on, no friction) adds the self-contact
+ * force of the current candidate list to f_int (its static part: the penalty
+ * force of ShellSystem.C:1803-1900 without the contact damping), for
+ * equilibria held by contact; the contact state is not changed.
  * No counterpart in the reference, which has no residual stop. */
-enum { SHL_RESIDUAL_FP64 = 1, SHL_RESIDUAL_CORRECT = 2, SHL_RESIDUAL_CLEAR = 4 };
+enum { SHL_RESIDUAL_FP64 = 1, SHL_RESIDUAL_CORRECT = 2, SHL_RESIDUAL_CLEAR = 4, SHL_RESIDUAL_CONTACT = 8 };
 shl_status shl_residual(shl_ctx* ctx, double pressure, int flags, double* rel, double* f2, double* fext2);
 
 /* The pressure as a config expression of t (the muparser language of the

@@ -82,6 +82,12 @@ struct shl_ctx {
   shl::expr::Op* d_rfun = nullptr;           // compiled cavity semi-axes (device), 3 programs
   std::string rfun_text[3];                  // the same, for evaluations started by the host
   double* f32 = nullptr;                     // FP32 force at the checked state (defect correction)
+  // batch with self-contact: per-shell constants (empty otherwise), the shell
+  // of each original face, and the shells' summed linked-cell estimates
+  std::vector<ShellCell> shc_host;
+  std::vector<uint32_t> face_shell;
+  uint64_t bc_cells = 0, bc_entries = 0, bc_cells_max = 0;
+  double bc_pairs = 0;
 };
 
 namespace {
@@ -183,7 +189,7 @@ shl_status flush_deferred_rebuild(shl_ctx* c) {
   Ctl h;
   SHL_TRY(ctl_get(c, h));
   if (!h.rebuild_pending) return SHL_OK;
-  launch_rebuild_first(c->b, c->stream);
+  launch_rebuild_first(c->b, c->sc, c->stream);
   launch_rebuild(c->b, c->sc, c->stream);
   SHL_CUDA_TRY(cudaStreamSynchronize(c->stream));
   return check_launch("deferred linked-cell pass");
@@ -642,15 +648,24 @@ shl_status create_common(shl_ctx* c, const std::vector<double>& pscale_orig, shl
   uint32_t n_cells_cap = 1, entries_cap = 1, pairs_cap = 1, csr_cap = 1, cand_cap = 1;
   if (contact) {
     double ppf = 16.0;
-    estimate_cells(S, *params, n_cells0, entries0, ppf);
-    const uint64_t want_cells = std::min<uint64_t>(S.n_cells_max, 1ull << 28);
+    const bool batch_contact = !c->shc_host.empty();
+    uint64_t cells_max = S.n_cells_max;
+    if (batch_contact) {  // the shells' own estimates, summed
+      n_cells0 = c->bc_cells;
+      entries0 = c->bc_entries;
+      cells_max = c->bc_cells_max;
+    } else {
+      estimate_cells(S, *params, n_cells0, entries0, ppf);
+    }
+    const uint64_t want_cells = std::min<uint64_t>(cells_max, 1ull << 28);
     n_cells_cap = (uint32_t)std::max<uint64_t>(std::min<uint64_t>(want_cells, std::max<uint64_t>(8 * n_cells0, 1u << 20)), 1);
     if (n_cells_cap < n_cells0) n_cells_cap = (uint32_t)std::min<uint64_t>(n_cells0, 1ull << 28);
     entries_cap = (uint32_t)std::min<uint64_t>(std::max<uint64_t>(8 * entries0, 1u << 20), 1ull << 30);
     // room for a shell folded onto itself everywhere (1.5 x the double-layer estimate);
     // csr entries hold pair * 8 + role, so at most 2^28 pairs
     const double per_face = std::max(16.0, 1.5 * ppf);
-    pairs_cap = (uint32_t)std::min<double>(std::max<double>(per_face * F, 65536.0), (double)(1u << 28));
+    const double pairs_want = batch_contact ? c->bc_pairs : per_face * F;
+    pairs_cap = (uint32_t)std::min<double>(std::max<double>(pairs_want, 65536.0), (double)(1u << 28));
     csr_cap = (uint32_t)std::min<uint64_t>((uint64_t)6 * pairs_cap, 0xFFFFFFF0u);
     // candidates before the distance test (SMOOTH skips the facet prefilter)
     cand_cap = (uint32_t)std::min<uint64_t>(std::max<uint64_t>((uint64_t)(smooth ? 3 : 2) * pairs_cap, 1u << 18),
@@ -680,6 +695,11 @@ shl_status create_common(shl_ctx* c, const std::vector<double>& pscale_orig, shl
       ALLOC(b.pvw[0], 4 * (size_t)pairs_cap); ALLOC(b.pvw[1], 4 * (size_t)pairs_cap);
       ALLOC(b.new_x, 4 * (size_t)pairs_cap); ALLOC(b.cand_x, 4 * (size_t)cand_cap);
       ALLOC(b.inv_perm, F); ALLOC(b.fsm, F);
+    }
+    if (batch_contact) {
+      ALLOC(b.shc, c->shc_host.size());
+      ALLOC(b.face_shell, F);
+      ALLOC(b.node_shell, V);
     }
   }
 #undef ALLOC
@@ -735,6 +755,14 @@ shl_status create_common(shl_ctx* c, const std::vector<double>& pscale_orig, shl
     }
     if ((st = upload(c, b.fsm, fsm.data(), F)) != SHL_OK) return fail(st);
     if ((st = upload(c, b.inv_perm, S.inv_perm.data(), F)) != SHL_OK) return fail(st);
+  }
+  if (contact && !c->shc_host.empty()) {
+    std::vector<uint32_t> node_shell(V);
+    for (size_t k = 0; k + 1 < c->node_off.size(); ++k)
+      for (uint32_t n = c->node_off[k]; n < c->node_off[k + 1]; ++n) node_shell[n] = (uint32_t)k;
+    if ((st = upload(c, b.shc, c->shc_host.data(), c->shc_host.size())) != SHL_OK) return fail(st);
+    if ((st = upload(c, b.face_shell, c->face_shell.data(), F)) != SHL_OK) return fail(st);
+    if ((st = upload(c, b.node_shell, node_shell.data(), V)) != SHL_OK) return fail(st);
   }
   if (contact) {
     if ((st = upload(c, b.close_ptr, S.close_ptr.data(), S.close_ptr.size())) != SHL_OK) return fail(st);
@@ -823,6 +851,7 @@ shl_status create_common(shl_ctx* c, const std::vector<double>& pscale_orig, shl
   sc.cav_damping = p.cavity_damping;
   sc.cav_fric_damping = p.cavity_friction_damping;
   sc.static_friction_tol = p.static_friction_tol;
+  sc.n_cs = contact ? (uint32_t)c->shc_host.size() : 0u;
 
   Ctl h;
   std::memset(&h, 0, sizeof(h));
@@ -875,8 +904,20 @@ shl_status shl_batch_create(const shl_mesh* meshes, const shl_params* params, co
   for (uint32_t k = 0; k < n_shells; ++k) {
     const shl_params& p = params[k];
     if (!validate(p, err)) { g_err = "shell " + std::to_string(k) + ": " + err; return SHL_ERR_ARG; }
-    if (p.shell_shell_contact != SHL_CONTACT_NONE || p.bulk_modulus != 0.0) {
-      g_err = "batched shells: self-contact and bulk-modulus pressure are evaluated per single shell only";
+    if (p.bulk_modulus != 0.0) {
+      g_err = "batched shells: bulk-modulus pressure is evaluated per single shell only";
+      return SHL_ERR_ARG;
+    }
+    // self-contact: each shell's own linked cells; the friction law and the
+    // cell margin are shared
+    if (p.shell_shell_contact != p0.shell_shell_contact ||
+        (p.shell_shell_contact != SHL_CONTACT_NONE &&
+         (p.mu_s != p0.mu_s || p.mu_d != p0.mu_d || p.self_damping != p0.self_damping ||
+          p.self_friction_damping != p0.self_friction_damping ||
+          p.friction_stop_velocity != p0.friction_stop_velocity || p.cell_margin != p0.cell_margin ||
+          p.adapt_dt_every != 0))) {
+      g_err = "batched shells with self-contact must share the contact mode, friction, damping and cell margin, "
+              "with a fixed dt";
       return SHL_ERR_ARG;
     }
     if (p.dt != p0.dt || p.newmark_beta != p0.newmark_beta || p.newmark_gamma != p0.newmark_gamma ||
@@ -895,14 +936,38 @@ shl_status shl_batch_create(const shl_mesh* meshes, const shl_params* params, co
     if (!ok[k]) { g_err = "shell " + std::to_string(k) + ": " + errs[k]; return SHL_ERR_ARG; }
   shl_ctx* c = new shl_ctx;
   c->P = p0;
-  std::vector<uint32_t> face_shell;
-  if (!merge_setups(shells, c->S, c->node_off, c->face_off, face_shell, err)) {
+  if (p0.shell_shell_contact != SHL_CONTACT_NONE) {
+    // per-shell constants and linked-cell estimates (before the merge moves the set-ups)
+    uint32_t f0 = 0;
+    for (uint32_t k = 0; k < n_shells; ++k) {
+      const Setup& S = shells[k];
+      ShellCell sc{};
+      sc.thickness = params[k].thickness;
+      sc.cell_size_mult = params[k].cell_size_mult;
+      sc.stiff_density = S.stiff_density;
+      sc.stiff_static_friction = S.stiff_static_friction;
+      sc.d2_friction = S.d2_friction;
+      sc.n_cells_max = S.n_cells_max;
+      sc.face_first = f0;
+      sc.face_end = f0 + S.F;
+      f0 += S.F;
+      c->shc_host.push_back(sc);
+      uint64_t nc = 0, ne = 0;
+      double ppf = 16.0;
+      estimate_cells(S, params[k], nc, ne, ppf);
+      c->bc_cells += nc;
+      c->bc_entries += ne;
+      c->bc_cells_max += S.n_cells_max;
+      c->bc_pairs += std::max(16.0, 1.5 * ppf) * S.F;
+    }
+  }
+  if (!merge_setups(shells, c->S, c->node_off, c->face_off, c->face_shell, err)) {
     g_err = err;
     delete c;
     return SHL_ERR_ARG;
   }
   std::vector<double> pscale(c->S.F);
-  for (uint32_t f = 0; f < c->S.F; ++f) pscale[f] = pressure_scale ? pressure_scale[face_shell[f]] : 1.0;
+  for (uint32_t f = 0; f < c->S.F; ++f) pscale[f] = pressure_scale ? pressure_scale[c->face_shell[f]] : 1.0;
   return create_common(c, pscale, out);
 }
 
@@ -912,6 +977,20 @@ shl_status shl_batch_layout(shl_ctx* c, uint32_t* n_shells, uint32_t* node_offse
   if (n_shells) *n_shells = n;
   if (node_offsets) std::copy(c->node_off.begin(), c->node_off.end(), node_offsets);
   if (face_offsets) std::copy(c->face_off.begin(), c->face_off.end(), face_offsets);
+  return SHL_OK;
+}
+
+shl_status shl_batch_contact_stats(shl_ctx* c, double* du_sum, uint32_t* n_rebuilds) {
+  if (!c) return SHL_ERR_ARG;
+  if (!c->sc.n_cs) { g_err = "not a batch with self-contact"; return SHL_ERR_ARG; }
+  SHL_TRY(flush_deferred_rebuild(c));
+  std::vector<ShellCell> h(c->sc.n_cs);
+  SHL_CUDA_TRY(cudaMemcpyAsync(h.data(), c->b.shc, h.size() * sizeof(ShellCell), cudaMemcpyDeviceToHost, c->stream));
+  SHL_CUDA_TRY(cudaStreamSynchronize(c->stream));
+  for (size_t k = 0; k < h.size(); ++k) {
+    if (du_sum) du_sum[k] = h[k].du_sum;
+    if (n_rebuilds) n_rebuilds[k] = h[k].n_rebuilds;
+  }
   return SHL_OK;
 }
 
@@ -1009,7 +1088,10 @@ shl_status begin_eval(shl_ctx* c, double pressure, bool allow_rebuild) {
   } else {
     h.rebuild = 0;
   }
-  return ctl_put(c, h);
+  SHL_TRY(ctl_put(c, h));
+  // a batch: each shell's own test (the control block gets the OR)
+  if (c->sc.n_cs) launch_batch_flags(c->b, c->sc, allow_rebuild ? 1 : 2, c->stream);
+  return SHL_OK;
 }
 
 shl_status eval_into(shl_ctx* c, double* d_f, double* d_a) {
@@ -1069,6 +1151,7 @@ shl_status initial_state(shl_ctx* c, Ctl& h) {
   h.volume_pressure = 0;
   h.rebuild = c->sc.contact ? 1u : 0u;  // compute_shell_shell_contact_candidates(true)
   SHL_TRY(ctl_put(c, h));
+  if (c->sc.n_cs) launch_batch_flags(c->b, c->sc, 0, c->stream);
   if (c->sc.contact) launch_rebuild(c->b, c->sc, c->stream);
   launch_elements(c->b, c->sc, elem_launch(c, c->sc), c->stream, false);
   launch_volume_end_step(c->b, c->sc, false, c->stream);
@@ -1183,7 +1266,7 @@ shl_status collect(shl_ctx* c, shl_step_report* report, const Ctl* fresh = nullp
     // a corrector-side linked-cell pass left pending by the last fused step
     c->maybe_pending = false;
     if (c->sc.contact && h.rebuild_pending) {
-      launch_rebuild_first(c->b, c->stream);
+      launch_rebuild_first(c->b, c->sc, c->stream);
       launch_rebuild(c->b, c->sc, c->stream);
       SHL_TRY(check_launch("deferred linked-cell pass"));
       SHL_TRY(ctl_get(c, h));
@@ -1553,6 +1636,7 @@ shl_status shl_set_contact_state(shl_ctx* c, const uint32_t* pairs, const uint8_
   if (!c) return SHL_ERR_ARG;
   SHL_TRY(host_access(c));  // pending linked-cell pass; the step prediction is rebuilt
   if (!c->sc.contact) { g_err = "self-contact is off"; return SHL_ERR_ARG; }
+  if (c->sc.n_cs) { g_err = "contact state files are written and read for single shells only"; return SHL_ERR_ARG; }
   if (n > c->sc.pairs_cap) { g_err = "too many pairs"; return SHL_ERR_CAPACITY; }
   const uint32_t F = c->S.F;
   std::vector<size_t> order(n);
@@ -1615,6 +1699,7 @@ shl_status shl_rebuild_contacts(shl_ctx* c) {
   h.halted = 0;
   h.error = 0;
   SHL_TRY(ctl_put(c, h));
+  if (c->sc.n_cs) launch_batch_flags(c->b, c->sc, 0, c->stream);
   launch_rebuild(c->b, c->sc, c->stream);
   SHL_TRY(check_launch("shl_rebuild_contacts"));
   return finish_status(c, h);
@@ -1640,6 +1725,11 @@ shl_status shl_residual(shl_ctx* c, double pressure, int flags, double* rel, dou
   const bool ctx32 = c->sc.fp32 != 0;
   const bool fp64 = (flags & SHL_RESIDUAL_FP64) || !ctx32;
   const bool correct = (flags & SHL_RESIDUAL_CORRECT) && ctx32 && fp64;
+  const bool with_contact = (flags & SHL_RESIDUAL_CONTACT) != 0;
+  if (with_contact && (!c->sc.contact || c->sc.friction)) {
+    g_err = "SHL_RESIDUAL_CONTACT needs self-contact without friction";
+    return SHL_ERR_ARG;
+  }
   if (!c->d_node_off) {
     SHL_TRY(dev_alloc(c, &c->d_node_off, ns + 1));
     SHL_TRY(dev_alloc(c, &c->d_norms, 2 * (size_t)ns));
@@ -1671,7 +1761,8 @@ shl_status shl_residual(shl_ctx* c, double pressure, int flags, double* rel, dou
   const double red = std::max((1.0 - static_cast<int>(h.time * 5.0) * 0.01), 0.5);
   h.volume_pressure = (c->P.bulk_modulus == 0 ? 0 : c->P.bulk_modulus * (h.volume0 * red / h.volume - 1));
   SHL_TRY(ctl_put(c, h));
-  // f = pressure force - internal force, then the pressure force alone (no contact, no damping)
+  // f = pressure force - internal force (- the static self-contact force), then
+  // the pressure force alone (no contact, no damping)
   StepConst sc = c->sc;
   sc.contact = 0;
   sc.cavity_contact = 0;
@@ -1681,7 +1772,31 @@ shl_status shl_residual(shl_ctx* c, double pressure, int flags, double* rel, dou
     bf.qe = c->qe64;
   }
   launch_elements(bf, sc, elem_launch(c, sc), c->stream);
-  launch_gather_correct(bf, sc, 0, false, c->d_fa, nullptr, c->stream);
+  if (with_contact) {
+    // the contact kernel at this state on copies of the per-pair state (the
+    // list's scratch side), without contact damping
+    StepConst scc = sc;
+    scc.contact = 1;
+    scc.self_damping = 0.0;
+    DevBuf bc = bf;
+    if (h.n_pairs) {
+      SHL_CUDA_TRY(cudaMemcpyAsync(b.pd2[1], b.pd2[0], h.n_pairs * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+      SHL_CUDA_TRY(cudaMemcpyAsync(b.pstick[1], b.pstick[0], h.n_pairs, cudaMemcpyDeviceToDevice, c->stream));
+      SHL_CUDA_TRY(cudaMemcpyAsync(b.porig[1], b.porig[0], 3 * h.n_pairs * sizeof(double), cudaMemcpyDeviceToDevice,
+                                   c->stream));
+      if (c->sc.smooth)
+        SHL_CUDA_TRY(cudaMemcpyAsync(b.pvw[1], b.pvw[0], 4 * h.n_pairs * sizeof(double), cudaMemcpyDeviceToDevice,
+                                     c->stream));
+    }
+    bc.pd2[0] = b.pd2[1];
+    bc.pstick[0] = b.pstick[1];
+    bc.porig[0] = b.porig[1];
+    bc.pvw[0] = b.pvw[1];
+    launch_contact_force(bc, scc, 0, c->stream);
+    launch_gather_correct(bc, scc, 0, false, c->d_fa, nullptr, c->stream);
+  } else {
+    launch_gather_correct(bf, sc, 0, false, c->d_fa, nullptr, c->stream);
+  }
   if (correct) {
     // the context's own FP32 force at the same state, and the defect the steps add to it
     StepConst s32 = c->sc;

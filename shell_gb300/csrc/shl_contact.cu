@@ -58,6 +58,57 @@ __device__ __forceinline__ void set_error(Ctl* ctl, int code) {
   ctl->rebuild = 0;
 }
 
+// The cell grid that face f is binned in: the control block's for a single
+// shell, its shell's for a batch with self-contact (ShellCell).
+struct GridView {
+  double cell_size, d_max, d2_max;
+  const double* bmin;
+  uint32_t ny, nz, base;
+};
+__device__ __forceinline__ GridView grid_of(const DevBuf& b, const StepConst& sc, uint32_t f) {
+  GridView g;
+  if (sc.n_cs) {
+    const ShellCell& s = b.shc[b.face_shell[f]];
+    g.cell_size = s.cell_size; g.d_max = s.d_max; g.d2_max = s.d2_max; g.bmin = s.bmin;
+    g.ny = s.ncd[1]; g.nz = s.ncd[2]; g.base = s.cell_base;
+  } else {
+    const Ctl* ctl = b.ctl;
+    g.cell_size = ctl->cell_size; g.d_max = ctl->d_max; g.d2_max = ctl->d2_max; g.bmin = ctl->bmin;
+    g.ny = ctl->ncd[1]; g.nz = ctl->ncd[2]; g.base = 0;
+  }
+  return g;
+}
+
+// face f takes part in the current pass (a batch rebuilds only the shells whose trigger fired)
+__device__ __forceinline__ bool face_in_pass(const DevBuf& b, const StepConst& sc, uint32_t f) {
+  return sc.n_cs == 0 || b.shc[b.face_shell[f]].rebuild != 0;
+}
+
+// Cell size, d_max and cell counts of a shell from its bounds and average
+// element size (ShellSystem.C:1929-1969), rounded operation by operation.
+// Returns the number of cells (0 with TOO_MANY_CELLS registered).
+__device__ uint64_t grid_setup(const double* bmin, const double* bmax, double avg, double cell_size_mult,
+                               double cell_margin, double thickness, int smooth, double* cell_size_out,
+                               double* d_max_out, uint32_t* ncd) {
+  double cell_size = __dmul_rn(cell_size_mult, avg);
+  const double tolerance = __dmul_rn(cell_margin, cell_size);
+  cell_size = __dadd_rn(cell_size, tolerance);
+  double d_max = __dadd_rn(thickness, tolerance);
+  // SMOOTH: the limit surfaces may be closer than the facets (ShellSystem.C:1940-1944)
+  if (smooth) d_max = __dadd_rn(d_max, avg);
+  *cell_size_out = cell_size;
+  *d_max_out = d_max;
+  uint64_t n_cells = 1;
+  for (int c = 0; c < 3; ++c) {
+    const double sz = __dsub_rn(bmax[c], bmin[c]);
+    const double q = __dadd_rn(__ddiv_rn(__dadd_rn(sz, d_max), cell_size), 1.0);
+    const int ncd_c = (q < 2147483647.0) ? (int)q : 2147483647;
+    ncd[c] = (uint32_t)ncd_c;
+    n_cells *= (uint64_t)(uint32_t)ncd_c;
+  }
+  return n_cells;
+}
+
 // ------------------------------------------------------------------ AABB --
 __global__ void __launch_bounds__(kBlock) k_rb_aabb(DevBuf b, StepConst sc) {
   Ctl* ctl = b.ctl;
@@ -85,6 +136,7 @@ __global__ void __launch_bounds__(kBlock) k_rb_aabb(DevBuf b, StepConst sc) {
     if (d2 > dmax) dmax = d2;
     b.fsize[f] = dmax;
   }
+  if (sc.n_cs) return;  // a batch: per-shell grids (k_rb_grids)
   for (int c = 0; c < 3; ++c) {
     sh_min[c][threadIdx.x] = lo[c];
     sh_max[c][threadIdx.x] = hi[c];
@@ -142,23 +194,9 @@ __global__ void __launch_bounds__(kBlock) k_rb_aabb(DevBuf b, StepConst sc) {
   }
   const double avg = __ddiv_rn(lanes[0], (double)sc.F);
   ctl->avg_elem_size = avg;
-  double cell_size = __dmul_rn(sc.cell_size_mult, avg);
-  const double tolerance = __dmul_rn(sc.cell_margin, cell_size);
-  cell_size = __dadd_rn(cell_size, tolerance);
-  double d_max = __dadd_rn(sc.thickness, tolerance);
-  // SMOOTH: the limit surfaces may be closer than the facets (ShellSystem.C:1940-1944)
-  if (sc.smooth) d_max = __dadd_rn(d_max, avg);
-  ctl->cell_size = cell_size;
-  ctl->d_max = d_max;
-  ctl->d2_max = __dmul_rn(d_max, d_max);
-  uint64_t n_cells = 1;
-  for (int c = 0; c < 3; ++c) {
-    const double sz = __dsub_rn(ctl->bmax[c], ctl->bmin[c]);
-    const double q = __dadd_rn(__ddiv_rn(__dadd_rn(sz, d_max), cell_size), 1.0);
-    const int ncd = (q < 2147483647.0) ? (int)q : 2147483647;
-    ctl->ncd[c] = (uint32_t)ncd;
-    n_cells *= (uint64_t)(uint32_t)ncd;
-  }
+  const uint64_t n_cells = grid_setup(ctl->bmin, ctl->bmax, avg, sc.cell_size_mult, sc.cell_margin, sc.thickness,
+                                      sc.smooth, &ctl->cell_size, &ctl->d_max, ctl->ncd);
+  ctl->d2_max = __dmul_rn(ctl->d_max, ctl->d_max);
   if (n_cells > sc.n_cells_max) {
     atomicMax(&ctl->problem, (int)SHL_TOO_MANY_CELLS);
     ctl->rebuild = 0;
@@ -169,6 +207,110 @@ __global__ void __launch_bounds__(kBlock) k_rb_aabb(DevBuf b, StepConst sc) {
     return;
   }
   ctl->n_cells = (uint32_t)n_cells;
+  ctl->n_old = ctl->n_pairs;
+  ctl->n_new = 0;
+  ctl->n_rebuilds += 1;
+}
+
+// ------------------------------------------------------- batch grids --
+// One block per shell of a batch with self-contact: the shell's bounds and
+// average element size (the fixed-order sum of shl_geom.h over the shell's own
+// faces, so every value equals that of the shell run alone), its cell size,
+// d_max and cell counts.  Shells whose trigger did not fire keep their list.
+__global__ void __launch_bounds__(kBlock) k_rb_grids(DevBuf b, StepConst sc) {
+  Ctl* ctl = b.ctl;
+  if (rb_off(ctl)) return;
+  ShellCell& S = b.shc[blockIdx.x];
+  if (!S.rebuild) {
+    if (threadIdx.x == 0) S.n_cells = 0;
+    return;
+  }
+  __shared__ double sh_min[3][kBlock], sh_max[3][kBlock];
+  __shared__ double lanes[SHL_SUM_LANES];
+  const uint32_t f0 = S.face_first, nf = S.face_end - S.face_first;
+  double lo[3] = {SHL_DBL_MAX, SHL_DBL_MAX, SHL_DBL_MAX}, hi[3] = {-SHL_DBL_MAX, -SHL_DBL_MAX, -SHL_DBL_MAX};
+  for (uint32_t i = threadIdx.x; i < nf; i += blockDim.x)
+    for (int c = 0; c < 3; ++c) {
+      lo[c] = fmin(lo[c], b.bmin[3 * (size_t)(f0 + i) + c]);
+      hi[c] = fmax(hi[c], b.bmax[3 * (size_t)(f0 + i) + c]);
+    }
+  for (int c = 0; c < 3; ++c) {
+    sh_min[c][threadIdx.x] = lo[c];
+    sh_max[c][threadIdx.x] = hi[c];
+  }
+  for (uint32_t l = threadIdx.x; l < SHL_SUM_LANES; l += blockDim.x) {
+    double s = 0.0;
+    for (uint32_t i = l; i < nf; i += SHL_SUM_LANES) s = __dadd_rn(s, b.fsize[f0 + i]);
+    lanes[l] = s;
+  }
+  __syncthreads();
+  for (int st = blockDim.x / 2; st > 0; st >>= 1) {
+    if ((int)threadIdx.x < st)
+      for (int c = 0; c < 3; ++c) {
+        sh_min[c][threadIdx.x] = fmin(sh_min[c][threadIdx.x], sh_min[c][threadIdx.x + st]);
+        sh_max[c][threadIdx.x] = fmax(sh_max[c][threadIdx.x], sh_max[c][threadIdx.x + st]);
+      }
+    __syncthreads();
+  }
+  for (uint32_t st = SHL_SUM_LANES / 2; st > 0; st >>= 1) {
+    for (uint32_t l = threadIdx.x; l < st; l += blockDim.x) lanes[l] = __dadd_rn(lanes[l], lanes[l + st]);
+    __syncthreads();
+  }
+  if (threadIdx.x != 0) return;
+  S.du_sum = 0.0;
+  for (int c = 0; c < 3; ++c) {
+    S.bmin[c] = sh_min[c][0];
+    S.bmax[c] = sh_max[c][0];
+  }
+  const double avg = __ddiv_rn(lanes[0], (double)nf);
+  S.avg_elem_size = avg;
+  const uint64_t n_cells = grid_setup(S.bmin, S.bmax, avg, S.cell_size_mult, sc.cell_margin, S.thickness, sc.smooth,
+                                      &S.cell_size, &S.d_max, S.ncd);
+  S.d2_max = __dmul_rn(S.d_max, S.d_max);
+  S.n_rebuilds += 1;
+  if (n_cells > S.n_cells_max) {
+    atomicMax(&ctl->problem, (int)SHL_TOO_MANY_CELLS);
+    ctl->rebuild = 0;
+    S.n_cells = 0;
+    return;
+  }
+  S.n_cells = n_cells > sc.n_cells_cap ? sc.n_cells_cap + 1u : (uint32_t)n_cells;
+}
+
+// first cell of each shell's grid (exclusive scan over the shells), the pass's
+// cell count and the list counters (one block)
+__global__ void __launch_bounds__(1024) k_rb_grid_scan(DevBuf b, StepConst sc) {
+  Ctl* ctl = b.ctl;
+  if (rb_off(ctl)) return;
+  const uint32_t n = sc.n_cs;
+  const uint32_t per = (n + blockDim.x - 1) / blockDim.x;
+  const uint32_t s0 = threadIdx.x * per;
+  uint64_t tot = 0;
+  for (uint32_t k = 0; k < per; ++k)
+    if (s0 + k < n) tot += b.shc[s0 + k].n_cells;
+  __shared__ unsigned long long sh[1024];
+  sh[threadIdx.x] = tot;
+  __syncthreads();
+  for (uint32_t o = 1; o < blockDim.x; o <<= 1) {
+    const unsigned long long y = threadIdx.x >= o ? sh[threadIdx.x - o] : 0ull;
+    __syncthreads();
+    sh[threadIdx.x] += y;
+    __syncthreads();
+  }
+  uint64_t run = sh[threadIdx.x] - tot;
+  for (uint32_t k = 0; k < per; ++k)
+    if (s0 + k < n) {
+      ShellCell& S = b.shc[s0 + k];
+      S.cell_base = run < 0xFFFFFFFFull ? (uint32_t)run : 0xFFFFFFFFu;
+      run += S.n_cells;
+    }
+  if (threadIdx.x != blockDim.x - 1) return;
+  const unsigned long long all = sh[blockDim.x - 1];
+  if (all > sc.n_cells_cap) {
+    set_error(ctl, SHL_ERR_CAPACITY);
+    return;
+  }
+  ctl->n_cells = (uint32_t)all;
   ctl->n_old = ctl->n_pairs;
   ctl->n_new = 0;
   ctl->n_rebuilds += 1;
@@ -194,11 +336,11 @@ __global__ void k_rb_clear(DevBuf b, StepConst sc) {
 }
 
 // cell index range of face f on axis c (ShellSystem.C:1982-1983)
-__device__ __forceinline__ void cell_range(const DevBuf& b, const Ctl* ctl, uint32_t f, int* lo, int* hi) {
-  const double cs = ctl->cell_size, dm = ctl->d_max;
+__device__ __forceinline__ void cell_range(const DevBuf& b, const GridView& g, uint32_t f, int* lo, int* hi) {
+  const double cs = g.cell_size, dm = g.d_max;
   for (int c = 0; c < 3; ++c) {
-    lo[c] = (int)__ddiv_rn(__dsub_rn(b.bmin[3 * (size_t)f + c], ctl->bmin[c]), cs);
-    hi[c] = (int)__ddiv_rn(__dadd_rn(__dsub_rn(b.bmax[3 * (size_t)f + c], ctl->bmin[c]), dm), cs);
+    lo[c] = (int)__ddiv_rn(__dsub_rn(b.bmin[3 * (size_t)f + c], g.bmin[c]), cs);
+    hi[c] = (int)__ddiv_rn(__dadd_rn(__dsub_rn(b.bmax[3 * (size_t)f + c], g.bmin[c]), dm), cs);
   }
 }
 
@@ -206,25 +348,29 @@ __device__ __forceinline__ void cell_range(const DevBuf& b, const Ctl* ctl, uint
 // one face t < F (cell ranges, histogram) or one old pair j = t - F (keep flag)
 __device__ __forceinline__ void rb_count_one(const DevBuf& b, const StepConst& sc, const Ctl* ctl, uint32_t t) {
   if (t < sc.F) {
+    if (!face_in_pass(b, sc, t)) return;
+    const GridView g = grid_of(b, sc, t);
     int lo[3], hi[3];
-    cell_range(b, ctl, t, lo, hi);
+    cell_range(b, g, t, lo, hi);
     for (int c = 0; c < 3; ++c) {
       b.cell_lo[3 * (size_t)t + c] = lo[c];
       b.cell_hi[3 * (size_t)t + c] = hi[c];
     }
-    const uint32_t ny = ctl->ncd[1], nz = ctl->ncd[2];
+    const uint32_t ny = g.ny, nz = g.nz;
     for (int cx = lo[0]; cx <= hi[0]; ++cx)
       for (int cy = lo[1]; cy <= hi[1]; ++cy)
         for (int cz = lo[2]; cz <= hi[2]; ++cz) {
-          const uint32_t cell = (uint32_t)cx * ny * nz + (uint32_t)cy * nz + (uint32_t)cz;
+          const uint32_t cell = g.base + (uint32_t)cx * ny * nz + (uint32_t)cy * nz + (uint32_t)cz;
           atomicAdd(&b.cell_count[cell], 1u);
         }
     return;
   }
   const uint32_t j = t - sc.F;
   if (j < ctl->n_old) {
-    // ShellSystem.C:2020: drop unless sticking or still within d_max
-    const bool keep = b.pstick[0][j] != 0 || !(b.pd2[0][j] > ctl->d2_max);
+    // ShellSystem.C:2020: drop unless sticking or still within d_max; a shell
+    // of a batch that is not rebuilt keeps its whole list
+    const uint32_t e1 = b.pe1[0][j];
+    const bool keep = !face_in_pass(b, sc, e1) || b.pstick[0][j] != 0 || !(b.pd2[0][j] > grid_of(b, sc, e1).d2_max);
     b.pkeep[j] = keep ? 1 : 0;
     if (keep) atomicAdd(&b.seg_count[b.pe1[0][j]], 1u);
   }
@@ -350,17 +496,18 @@ __global__ void __launch_bounds__(kBlock) k_rb_fill(DevBuf b, StepConst sc) {
   Ctl* ctl = b.ctl;
   if (rb_off(ctl)) return;
   const uint32_t f = blockIdx.x * blockDim.x + threadIdx.x;
-  if (f >= sc.F) return;
+  if (f >= sc.F || !face_in_pass(b, sc, f)) return;
   int lo[3], hi[3];
   for (int c = 0; c < 3; ++c) {
     lo[c] = b.cell_lo[3 * (size_t)f + c];
     hi[c] = b.cell_hi[3 * (size_t)f + c];
   }
-  const uint32_t ny = ctl->ncd[1], nz = ctl->ncd[2];
+  const GridView g = grid_of(b, sc, f);
+  const uint32_t ny = g.ny, nz = g.nz;
   for (int cx = lo[0]; cx <= hi[0]; ++cx)
     for (int cy = lo[1]; cy <= hi[1]; ++cy)
       for (int cz = lo[2]; cz <= hi[2]; ++cz) {
-        const uint32_t cell = (uint32_t)cx * ny * nz + (uint32_t)cy * nz + (uint32_t)cz;
+        const uint32_t cell = g.base + (uint32_t)cx * ny * nz + (uint32_t)cy * nz + (uint32_t)cz;
         const uint32_t pos = b.cell_start[cell] + atomicAdd(&b.cell_fill[cell], 1u);
         b.cell_items[pos] = f;
         b.entry_cell[pos] = cell;
@@ -425,9 +572,6 @@ __global__ void __launch_bounds__(kBlock) k_rb_cand(DevBuf b, StepConst sc) {
   if (rb_off(ctl)) return;
   const uint32_t n_entries = ctl->n_entries;
   const uint32_t stride = gridDim.x * blockDim.x;
-  const uint32_t ny = ctl->ncd[1], nz = ctl->ncd[2];
-  const double d_max = ctl->d_max;
-  const float d_max32 = (float)d_max;
   constexpr int kBuf = 8;
   uint32_t buf1[kBuf], buf2[kBuf];
   int nb = 0;
@@ -445,9 +589,14 @@ __global__ void __launch_bounds__(kBlock) k_rb_cand(DevBuf b, StepConst sc) {
     nb = 0;
   };
   for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n_entries; j += stride) {
-    const uint32_t cell = b.entry_cell[j];
     const uint32_t e1 = b.cell_items[j];
-    const uint32_t cz = cell % nz, cy = (cell / nz) % ny, cx = cell / (nz * ny);
+    const GridView g = grid_of(b, sc, e1);
+    const uint32_t ny = g.ny, nz = g.nz;
+    const double d_max = g.d_max;
+    const float d_max32 = (float)d_max;
+    const uint32_t cell = b.entry_cell[j];
+    const uint32_t local = cell - g.base;
+    const uint32_t cz = local % nz, cy = (local / nz) % ny, cx = local / (nz * ny);
     const int* lo1 = b.cell_lo + 3 * (size_t)e1;
     const int l10 = lo1[0], l11 = lo1[1], l12 = lo1[2];
     const uint32_t c0 = b.close_ptr[e1], c1 = b.close_ptr[e1 + 1];
@@ -494,9 +643,9 @@ __global__ void __launch_bounds__(kBlock) k_rb_narrow(DevBuf b, StepConst sc) {
   Ctl* ctl = b.ctl;
   if (rb_off(ctl)) return;
   const uint32_t n = min(ctl->n_cand, sc.cand_cap);
-  const double d2_max = ctl->d2_max;
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const uint32_t e1 = b.cand_e1[i], e2 = b.cand_e2[i];
+    const double d2_max = sc.n_cs ? b.shc[b.face_shell[e1]].d2_max : ctl->d2_max;
     const double* P1[3];
     const double* P2[3];
     for (int q = 0; q < 3; ++q) {
@@ -617,10 +766,14 @@ __global__ void k_rb_copyback(DevBuf b, StepConst sc) {
   for (uint32_t f = blockIdx.x * blockDim.x + threadIdx.x; f <= sc.F; f += stride) b.pair_ptr[0][f] = b.pair_ptr[1][f];
 }
 
-// flag flip after the copy-back (single thread, after all blocks are done)
-__global__ void k_rb_finish(DevBuf b) {
+// flag flip after the copy-back (after all blocks are done); a batch also
+// clears its shells' flags
+__global__ void k_rb_finish(DevBuf b, StepConst sc) {
   Ctl* ctl = b.ctl;
   if (rb_off(ctl)) return;
+  for (uint32_t s = threadIdx.x; s < sc.n_cs; s += blockDim.x) b.shc[s].rebuild = 0;
+  __syncthreads();
+  if (threadIdx.x != 0) return;
   ctl->n_pairs = ctl->n_next;
   ctl->rebuild = 0;
   ctl->csr_dirty = 1;
@@ -707,6 +860,10 @@ void launch_contact_csr(const DevBuf& b, const StepConst& sc, cudaStream_t s) {
 void launch_rebuild(const DevBuf& b, const StepConst& sc, cudaStream_t s) {
   const uint32_t gF = nblk(sc.F);
   k_rb_aabb<<<gF, kBlock, 0, s>>>(b, sc);
+  if (sc.n_cs) {
+    k_rb_grids<<<sc.n_cs, kBlock, 0, s>>>(b, sc);
+    k_rb_grid_scan<<<1, 1024, 0, s>>>(b, sc);
+  }
   {
     uint32_t g = nblk(sc.n_cells_cap > sc.F ? sc.n_cells_cap : sc.F);
     if (g > 16 * 152) g = 16 * 152;
@@ -742,7 +899,7 @@ void launch_rebuild(const DevBuf& b, const StepConst& sc, cudaStream_t s) {
     if (g > 8 * 152) g = 8 * 152;
     k_rb_copyback<<<g, kBlock, 0, s>>>(b, sc);
   }
-  k_rb_finish<<<1, 1, 0, s>>>(b);
+  k_rb_finish<<<1, sc.n_cs ? kBlock : 32, 0, s>>>(b, sc);
   launch_contact_csr(b, sc, s);
 }
 

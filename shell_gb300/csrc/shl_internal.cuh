@@ -140,6 +140,25 @@ struct Ctl {
   uint32_t cnt[16];
 };
 
+// Per-shell linked-cell state of a batch with self-contact.  The shells of a
+// batch are independent: each keeps the single-shell control block's
+// linked-cell fields (its own rebuild trigger, bounds, cell size, d_max and
+// cell grid) and its own contact constants, and the grids of all shells share
+// one counting sort (shell s owns cells cell_base .. cell_base + n_cells).
+// The control block's rebuild / rebuild_pending flags are the OR over shells.
+struct ShellCell {
+  // constants of the shell (ShellSystem.C:421-487 with its own thickness and moduli)
+  double thickness, cell_size_mult, stiff_density, stiff_static_friction, d2_friction;
+  uint64_t n_cells_max;
+  uint32_t face_first, face_end;  // original face ids of the shell
+  // linked-cell state (Ctl's fields of a single shell)
+  double du_sum, du2_pred, avg_elem_size, cell_size, d_max, d2_max;
+  double bmin[3], bmax[3];
+  unsigned long long du2_acc, du2n_acc;  // largest |du|^2 of a node pass (bits of non-negative doubles)
+  uint32_t ncd[3], cell_base, n_cells, n_rebuilds;
+  uint32_t rebuild, rebuild_pending, rebuild_b, pad;
+};
+
 // Step constants (captured by value in each launch).
 struct StepConst {
   double dt;
@@ -182,7 +201,9 @@ struct StepConst {
   double mu_s_cav, mu_d_cav, cav_damping, cav_fric_damping, static_friction_tol;
   const shl::expr::Op* rfun[3];  // semi-axes as compiled expressions of t, or null: cav_R
   int32_t rfun_len[3];
-  int32_t pad_rfun;
+  // shells of a batch with self-contact (per-shell linked cells, DevBuf::shc);
+  // 0 for a single shell, whose linked-cell state is the control block's
+  uint32_t n_cs;
 };
 
 // Device buffers of one context.
@@ -243,6 +264,10 @@ struct DevBuf {
   int32_t* fsm;                // per original face: valence | (position of the patch's first vertex) << 8
   double* stab;                // subdivision tables of the valences present
   uint32_t *csr_count, *csr_ptr, *csr_ent, *csr_fill;  // per-node contact CSR
+  // batch with self-contact: per-shell linked-cell state, shell of each
+  // original face and of each node (null for a single shell)
+  ShellCell* shc;
+  uint32_t *face_shell, *node_shell;
   Ctl* ctl;
   double* ptable;              // per-step pressure table (capacity)
   uint32_t ptable_cap;
@@ -299,7 +324,11 @@ void launch_begin_step(const DevBuf& b, const StepConst& sc, RebuildCond rc, cud
 // predictor's; launch_rebuild_second sits between them.  launch_rebuild_first
 // turns a deferred pass into a due one (before a direct launch_rebuild).
 void launch_rebuild_second(const DevBuf& b, const StepConst& sc, cudaStream_t s);
-void launch_rebuild_first(const DevBuf& b, cudaStream_t s);
+void launch_rebuild_first(const DevBuf& b, const StepConst& sc, cudaStream_t s);
+// batch with self-contact: the per-shell rebuild flags of a pass started by the
+// host (mode 0: every shell, 1: the shells whose du_sum reached their tolerance,
+// 2: none) and the control block's OR of them
+void launch_batch_flags(const DevBuf& b, const StepConst& sc, int mode, cudaStream_t s);
 // totals: also the fixed-order sums of the per-face measurements (k_elem_totals);
 // k_volume_end forms them too, so launches followed by it pass false
 void launch_elements(const DevBuf& b, const StepConst& sc, const ElemLaunch& el, cudaStream_t s, bool totals = true);

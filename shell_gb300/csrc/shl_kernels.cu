@@ -164,6 +164,118 @@ __device__ __forceinline__ double rebuild_tolerance(const StepConst& sc, const C
   return __dmul_rn(sc.cell_margin, cs);
 }
 
+// ---- batch with self-contact: the linked-cell trigger of every shell ----
+// (ShellCell; the same decisions as the single-shell code below, per shell)
+__device__ __forceinline__ double shell_tolerance(const StepConst& sc, const ShellCell& S) {
+  const double cs = __dmul_rn(S.cell_size_mult, S.avg_elem_size);
+  return __dmul_rn(sc.cell_margin, cs);
+}
+
+// Largest |du|^2 of a node pass, per shell (which: 0 du2_acc, 1 du2n_acc).
+// Called by every lane of a warp; a warp whose nodes belong to one shell makes
+// one atomic.  NaNs are skipped, as fmax skips them in the single-shell maximum.
+__device__ __forceinline__ void shell_max_acc(const DevBuf& b, const StepConst& sc, uint32_t n, double x, int which) {
+  const uint32_t s = n < sc.V ? b.node_shell[n] : 0xffffffffu;
+  const uint32_t s0 = __shfl_sync(0xffffffffu, s, 0);
+  if (s0 == 0xffffffffu) return;  // the whole warp is past the last node
+  const bool valid = n < sc.V && !isnan(x);
+  if (__all_sync(0xffffffffu, s == s0 || n >= sc.V)) {
+    double m = valid ? x : 0.0;
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) {
+      ShellCell& S = b.shc[s0];
+      atomicMax(which ? &S.du2n_acc : &S.du2_acc, (unsigned long long)__double_as_longlong(m));
+    }
+  } else if (valid) {
+    ShellCell& S = b.shc[s];
+    atomicMax(which ? &S.du2n_acc : &S.du2_acc, (unsigned long long)__double_as_longlong(x));
+  }
+}
+
+// takes (and clears) a shell's accumulated maximum
+__device__ __forceinline__ double shell_take_max(unsigned long long* acc) {
+  return __longlong_as_double((long long)atomicExch(acc, 0ull));
+}
+
+// check_increment(false) of every shell (all threads of one block; thread t
+// takes shells t, t + blockDim.x, ...): the largest |du|^2 of the pass that
+// just ran (from_acc), or that the fused corrector predicted (du2_pred).  The
+// control block gets the OR of the shells' flags and the IF condition, as
+// begin_step sets them for one shell.
+__device__ void batch_begin_check(const DevBuf& b, const StepConst& sc, const RebuildCond& rc, bool fused,
+                                  bool from_acc) {
+  Ctl* ctl = b.ctl;
+  int r = 0, rb = 0;
+  for (uint32_t s = threadIdx.x; s < sc.n_cs; s += blockDim.x) {
+    ShellCell& S = b.shc[s];
+    const double mm = from_acc ? shell_take_max(&S.du2_acc) : S.du2_pred;
+    const double du_max = sqrt(mm);
+    const bool finite = isfinite(du_max);
+    if (finite) {
+      if (du_max > 0.5 * S.thickness) register_problem(ctl, SHL_LARGE_DISP);
+    } else {
+      register_problem(ctl, SHL_NOT_FINITE);
+    }
+    if (fused && S.rebuild_pending) {  // the corrector's pass first; k_rebuild_second updates du_sum
+      S.rebuild = 1u;
+      r = 1;
+      continue;
+    }
+    if (finite) S.du_sum = __dadd_rn(S.du_sum, __dmul_rn(2.0, du_max));
+    const uint32_t flag = S.du_sum >= shell_tolerance(sc, S) ? 1u : 0u;
+    if (fused) {
+      S.rebuild = 0u;
+      S.rebuild_b = flag;
+      rb |= (int)flag;
+    } else {
+      S.rebuild = flag;
+      r |= (int)flag;
+    }
+  }
+  r = __syncthreads_or(r);
+  rb = __syncthreads_or(rb);
+  if (threadIdx.x != 0) return;
+  ctl->rebuild = r ? 1u : 0u;
+  if (fused) ctl->rebuild_b = rb ? 1u : 0u;
+  if (rc.has) cudaGraphSetConditional(rc.h, ((r || rb) && ctl->halted == 0) ? 1u : 0u);
+}
+
+// check_increment(true) of every shell after a corrector (all threads of one
+// block): fused (mode 3) leaves each shell's flag pending for the next step's
+// IF node and keeps the next prediction's maximum in du2_pred
+__device__ void batch_correct_check(const DevBuf& b, const StepConst& sc, const RebuildCond& rc, bool fused) {
+  Ctl* ctl = b.ctl;
+  int r = 0;
+  for (uint32_t s = threadIdx.x; s < sc.n_cs; s += blockDim.x) {
+    ShellCell& S = b.shc[s];
+    const double du_max = sqrt(shell_take_max(&S.du2_acc));
+    if (fused) S.du2_pred = shell_take_max(&S.du2n_acc);
+    if (isfinite(du_max)) {
+      S.du_sum = __dadd_rn(S.du_sum, __dmul_rn(2.0, du_max));
+      if (du_max == 0.0)
+        register_problem(ctl, SHL_NO_DISP_CHANGE);
+      else if (du_max > 0.5 * S.thickness)
+        register_problem(ctl, SHL_LARGE_DISP);
+    } else {
+      register_problem(ctl, SHL_NOT_FINITE);
+    }
+    const uint32_t flag = S.du_sum >= shell_tolerance(sc, S) ? 1u : 0u;
+    if (fused)
+      S.rebuild_pending = flag;
+    else
+      S.rebuild = flag;
+    r |= (int)flag;
+  }
+  r = __syncthreads_or(r);
+  if (threadIdx.x != 0) return;
+  if (fused) {
+    ctl->rebuild_pending = r ? 1u : 0u;
+    return;
+  }
+  ctl->rebuild = r ? 1u : 0u;
+  set_rebuild_cond(rc, ctl);
+}
+
 // ---- float-pair ("double-float") arithmetic for the FP64 path's two
 // basis contractions.  GB300 issues 64 FP32 FMAs per FP64 FMA, so a product
 // sum carried as an unevaluated pair hi + lo of floats (about 48 significant
@@ -394,8 +506,7 @@ __device__ __forceinline__ double predict_node(const DevBuf& b, const StepConst&
 // fused: the IF node holds both passes of the step boundary.  With the previous
 // corrector's pass pending, that pass runs first and this check's du_sum update
 // follows it (k_rebuild_second); otherwise the second pass's flag is rebuild_b.
-__device__ void begin_step(Ctl* ctl, const StepConst& sc, double dt, double mm, const RebuildCond& rc,
-                           bool fused = false) {
+__device__ void begin_step_scalar(Ctl* ctl, const StepConst& sc, double dt) {
   ctl->time = __dadd_rn(ctl->time, dt);
   ctl->time_step += 1;
   double pr = sc.pressure_default;
@@ -414,6 +525,11 @@ __device__ void begin_step(Ctl* ctl, const StepConst& sc, double dt, double mm, 
     if (ctl->time_step == 2) ctl->volume0 = ctl->volume;
     ctl->volume_pressure = (sc.bulk_modulus == 0.0) ? 0.0 : sc.bulk_modulus * (ctl->volume0 * red / ctl->volume - 1.0);
   }
+}
+
+__device__ void begin_step(Ctl* ctl, const StepConst& sc, double dt, double mm, const RebuildCond& rc,
+                           bool fused = false) {
+  begin_step_scalar(ctl, sc, dt);
   // check_increment(false)
   const double du_max = sqrt(mm);
   const bool finite = isfinite(du_max);
@@ -444,7 +560,30 @@ __device__ void begin_step(Ctl* ctl, const StepConst& sc, double dt, double mm, 
 // and the element size), then the second pass's flag
 __global__ void k_rebuild_second(DevBuf b, StepConst sc) {
   Ctl* ctl = b.ctl;
-  if (threadIdx.x != 0 || blockIdx.x != 0 || ctl->halted != 0) return;
+  if (blockIdx.x != 0 || ctl->halted != 0) return;
+  if (sc.n_cs) {  // per shell of a batch
+    int r = 0;
+    for (uint32_t s = threadIdx.x; s < sc.n_cs; s += blockDim.x) {
+      ShellCell& S = b.shc[s];
+      if (S.rebuild_pending) {
+        S.rebuild_pending = 0u;
+        const double du_max = sqrt(S.du2_pred);
+        if (isfinite(du_max)) S.du_sum = __dadd_rn(S.du_sum, __dmul_rn(2.0, du_max));
+        S.rebuild_b = S.du_sum >= shell_tolerance(sc, S) ? 1u : 0u;
+      }
+      S.rebuild = S.rebuild_b;
+      S.rebuild_b = 0u;
+      r |= (int)S.rebuild;
+    }
+    r = __syncthreads_or(r);
+    if (threadIdx.x == 0) {
+      ctl->rebuild_pending = 0u;
+      ctl->rebuild = r ? 1u : 0u;
+      ctl->rebuild_b = 0u;
+    }
+    return;
+  }
+  if (threadIdx.x != 0) return;
   if (ctl->rebuild_pending) {
     ctl->rebuild_pending = 0u;
     const double du_max = sqrt(ctl->du2_pred);
@@ -456,10 +595,41 @@ __global__ void k_rebuild_second(DevBuf b, StepConst sc) {
 }
 
 // a deferred corrector pass made due for a direct launch_rebuild
-__global__ void k_rebuild_first(Ctl* ctl) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+__global__ void k_rebuild_first(DevBuf b, StepConst sc) {
+  Ctl* ctl = b.ctl;
+  if (blockIdx.x != 0) return;
+  if (sc.n_cs) {
+    int r = 0;
+    for (uint32_t s = threadIdx.x; s < sc.n_cs; s += blockDim.x) {
+      ShellCell& S = b.shc[s];
+      S.rebuild = S.rebuild_pending;
+      S.rebuild_pending = 0u;
+      r |= (int)S.rebuild;
+    }
+    r = __syncthreads_or(r);
+    if (threadIdx.x == 0) {
+      ctl->rebuild = r ? 1u : 0u;
+      ctl->rebuild_pending = 0u;
+    }
+    return;
+  }
+  if (threadIdx.x != 0) return;
   ctl->rebuild = ctl->rebuild_pending;
   ctl->rebuild_pending = 0u;
+}
+
+// rebuild flags of a pass started by the host (batch with self-contact):
+// mode 0 every shell, 1 the shells whose du_sum reached their tolerance, 2 none
+__global__ void k_batch_flags(DevBuf b, StepConst sc, int mode) {
+  Ctl* ctl = b.ctl;
+  int r = 0;
+  for (uint32_t s = threadIdx.x; s < sc.n_cs; s += blockDim.x) {
+    ShellCell& S = b.shc[s];
+    S.rebuild = mode == 0 ? 1u : (mode == 1 && S.du_sum >= shell_tolerance(sc, S)) ? 1u : 0u;
+    r |= (int)S.rebuild;
+  }
+  r = __syncthreads_or(r);
+  if (threadIdx.x == 0) ctl->rebuild = r ? 1u : 0u;
 }
 
 // u_pred, v_pred, positions and du_max of every node, then the step's scalar
@@ -483,12 +653,23 @@ __global__ void __launch_bounds__(kBlock) k_predict(DevBuf b, StepConst sc, Rebu
     const double a[3] = {b.a[k3], b.a[k3 + 1], b.a[k3 + 2]};
     du2 = predict_node(b, sc, n, u, v, a, dt, nm8, nm6, b.p);
   }
+  if (sc.n_cs) shell_max_acc(b, sc, n, du2, 0);
   const double m = block_max(du2, sh);
   if (threadIdx.x == 0) b.partial[(size_t)blockIdx.x * 8] = m;
   if (!last_block(&ctl->cnt[0])) return;
   double mm = 0.0;
   for (int k = threadIdx.x; k < (int)gridDim.x; k += blockDim.x) mm = fmax(mm, __ldcg(&b.partial[(size_t)k * 8]));
   mm = block_max(mm, sh);
+  if (sc.n_cs) {  // a batch: each shell's own check
+    if (nodes_only) {
+      for (uint32_t s = threadIdx.x; s < sc.n_cs; s += blockDim.x) b.shc[s].du2_pred = shell_take_max(&b.shc[s].du2_acc);
+      return;
+    }
+    if (threadIdx.x == 0) begin_step_scalar(ctl, sc, dt);
+    __syncthreads();
+    batch_begin_check(b, sc, rc, false, true);
+    return;
+  }
   if (threadIdx.x != 0) return;
   if (nodes_only) {
     ctl->du2_pred = mm;
@@ -501,7 +682,18 @@ __global__ void __launch_bounds__(kBlock) k_predict(DevBuf b, StepConst sc, Rebu
 // step's corrector (k_gather_correct mode 3) or by k_predict(nodes_only)
 __global__ void k_begin_step(DevBuf b, StepConst sc, RebuildCond rc) {
   Ctl* ctl = b.ctl;
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  if (blockIdx.x != 0) return;
+  if (sc.n_cs) {  // a batch: each shell's own check (all threads of the block)
+    if (inactive(ctl)) {
+      if (threadIdx.x == 0) set_rebuild_cond(rc, ctl);
+      return;
+    }
+    if (threadIdx.x == 0) begin_step_scalar(ctl, sc, sc.dt);
+    __syncthreads();
+    batch_begin_check(b, sc, rc, true, false);
+    return;
+  }
+  if (threadIdx.x != 0) return;
   if (inactive(ctl)) {
     set_rebuild_cond(rc, ctl);
     return;
@@ -1382,9 +1574,14 @@ __global__ void __launch_bounds__(kBlock) k_contact_force(DevBuf b, StepConst sc
     return;
   }
   double eself = 0.0, efric = 0.0, nc = 0.0;
-  const double h = sc.thickness;
   for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n_pairs; j += gridDim.x * blockDim.x) {
     const uint32_t e[2] = {b.pe1[0][j], b.pe2[0][j]};
+    // the shell's contact constants (a pair of a batch lies within one shell)
+    const ShellCell* S = sc.n_cs ? &b.shc[b.face_shell[e[0]]] : nullptr;
+    const double h = S ? S->thickness : sc.thickness;
+    const double d2_friction = S ? S->d2_friction : sc.d2_friction;
+    const double stiff_density = S ? S->stiff_density : sc.stiff_density;
+    const double stiff_static_friction = S ? S->stiff_static_friction : sc.stiff_static_friction;
     const double* P1[3];
     const double* P2[3];
     uint32_t nid[2][3];
@@ -1407,13 +1604,13 @@ __global__ void __launch_bounds__(kBlock) k_contact_force(DevBuf b, StepConst sc
     b.pd2[0][j] = g.d2;
     if (g.d2 <= 0.0) register_problem(ctl, SHL_CONTACT_PROBLEM);
     double* out = b.pforce + kPairOut * (size_t)j;
-    if (g.d2 < sc.d2_friction) {
+    if (g.d2 < d2_friction) {
       const double area_min = fmin(b.area[e[0]], b.area[e[1]]);
       const double abs_dc = SHL_SQRT(g.d2);
       const double depth = SHL_SUB(h, abs_dc);
       double nrm[3];
       for (int c = 0; c < 3; ++c) nrm[c] = SHL_DIV(g.dc[c], abs_dc);
-      const double stiffness = SHL_MUL(sc.stiff_density, area_min);
+      const double stiffness = SHL_MUL(stiff_density, area_min);
       double f_normal = 0.0, es = 0.0, ef = 0.0;
       if (depth > 0.0) {
         nc += 1.0;
@@ -1445,7 +1642,7 @@ __global__ void __launch_bounds__(kBlock) k_contact_force(DevBuf b, StepConst sc
                           SHL_MUL(0.5, g.dc[c]));
         int stick = b.pstick[0][j];
         double orig[3] = {b.porig[0][3 * (size_t)j], b.porig[0][3 * (size_t)j + 1], b.porig[0][3 * (size_t)j + 2]};
-        shl_friction_apply(&ef, fcon, f_normal, nrm, vrel, abs_v_normal, sc.v_stop, sc.stiff_static_friction,
+        shl_friction_apply(&ef, fcon, f_normal, nrm, vrel, abs_v_normal, sc.v_stop, stiff_static_friction,
                            sc.mu_s, sc.mu_d, sc.self_friction_damping, &stick, orig, cp);
         b.pstick[0][j] = (uint8_t)stick;
         b.porig[0][3 * (size_t)j] = orig[0];
@@ -1714,6 +1911,10 @@ __global__ void __launch_bounds__(kBlock) k_gather_correct(DevBuf b, StepConst s
     if (mode == 3) du2_next = predict_node(b, sc, n, un, vnn, an, sc.dt, sc.nm8, sc.nm6, b.pn);
   }
   if (mode == 0) return;
+  if (sc.n_cs && (mode == 1 || mode == 3)) {
+    shell_max_acc(b, sc, n, du2, 0);
+    if (mode == 3) shell_max_acc(b, sc, n, du2_next, 1);
+  }
   if (sc.cavity_contact) {
     const double r0 = block_sum(c_nc, sh), r1 = block_sum(c_e, sh), r2 = block_sum(c_ef, sh),
                  r3 = block_sum(c_fn, sh);
@@ -1788,6 +1989,14 @@ __global__ void __launch_bounds__(kBlock) k_gather_correct(DevBuf b, StepConst s
   mm = block_max(mm, sh);
   if (mode == 3) mmn = block_max(mmn, sh);
   const double ekt = sum_partials(b.partial, 1, gridDim.x, sh);
+  if (sc.n_cs) {  // a batch: each shell's own check_increment(true)
+    if (threadIdx.x == 0) {
+      ctl->Ekin = ekt;
+      if (!isfinite(ekt)) register_problem(ctl, SHL_NOT_FINITE);
+    }
+    batch_correct_check(b, sc, rc, mode == 3);
+    return;
+  }
   if (threadIdx.x != 0) return;
   ctl->Ekin = ekt;
   if (mode == 3) ctl->du2_pred = mmn;  // check_increment(false) of the next step, in k_begin_step
@@ -2039,12 +2248,17 @@ void launch_predict(const DevBuf& b, const StepConst& sc, RebuildCond rc, cudaSt
   k_predict<<<nblk(sc.V), kBlock, 0, s>>>(b, sc, rc, nodes_only ? 1 : 0);
 }
 void launch_begin_step(const DevBuf& b, const StepConst& sc, RebuildCond rc, cudaStream_t s) {
-  k_begin_step<<<1, 32, 0, s>>>(b, sc, rc);
+  k_begin_step<<<1, sc.n_cs ? kBlock : 32, 0, s>>>(b, sc, rc);
 }
 void launch_rebuild_second(const DevBuf& b, const StepConst& sc, cudaStream_t s) {
-  k_rebuild_second<<<1, 32, 0, s>>>(b, sc);
+  k_rebuild_second<<<1, sc.n_cs ? kBlock : 32, 0, s>>>(b, sc);
 }
-void launch_rebuild_first(const DevBuf& b, cudaStream_t s) { k_rebuild_first<<<1, 32, 0, s>>>(b.ctl); }
+void launch_rebuild_first(const DevBuf& b, const StepConst& sc, cudaStream_t s) {
+  k_rebuild_first<<<1, sc.n_cs ? kBlock : 32, 0, s>>>(b, sc);
+}
+void launch_batch_flags(const DevBuf& b, const StepConst& sc, int mode, cudaStream_t s) {
+  k_batch_flags<<<1, kBlock, 0, s>>>(b, sc, mode);
+}
 void launch_state_host(const DevBuf& b, const StepConst& sc, double* hu, double* hv, double* ha, bool load,
                        cudaStream_t s) {
   const size_t nd = 3 * (size_t)sc.V;

@@ -657,7 +657,17 @@ bool merge_setups(std::vector<Setup>& shells, Setup& M, std::vector<uint32_t>& n
     for (int fld = 0; fld < 2 * F32_COUNT; ++fld) M.face_df[(size_t)fld * F + i] = S.face_df[(size_t)fld * S.F + si];
   }
   build_node_lists(M);
+  // topological exclusion sets (self-contact), face ids offset shell by shell
   M.close_ptr.assign(F + 1, 0);
+  M.close_list.clear();
+  for (size_t k = 0; k < n; ++k) {
+    const Setup& S = shells[k];
+    for (uint32_t f = 0; f < S.F; ++f) {
+      const uint32_t c0 = S.close_ptr.empty() ? 0 : S.close_ptr[f], c1 = S.close_ptr.empty() ? 0 : S.close_ptr[f + 1];
+      for (uint32_t q = c0; q < c1; ++q) M.close_list.push_back(S.close_list[q] + face_off[k]);
+      M.close_ptr[face_off[k] + f + 1] = (uint32_t)M.close_list.size();
+    }
+  }
   M.K = shells[0].K;
   M.D = shells[0].D;
   return true;

@@ -30,7 +30,7 @@ from shell_gb300.abi import (_PARAM_FIELDS, ShlEnergies, ShlMesh, ShlParams, Shl
 
 
 _lib = None
-RESIDUAL_FP64, RESIDUAL_CORRECT, RESIDUAL_CLEAR = 1, 2, 4
+RESIDUAL_FP64, RESIDUAL_CORRECT, RESIDUAL_CLEAR, RESIDUAL_CONTACT = 1, 2, 4, 8
 
 
 def load():
@@ -78,6 +78,7 @@ def load():
         "shl_profile_step": (_i32, [vp, _d, sz, vp]),
         "shl_batch_create": (_i32, [vp, vp, vp, _u32, ctypes.POINTER(vp)]),
         "shl_batch_layout": (_i32, [vp, ctypes.POINTER(_u32), vp, vp]),
+        "shl_batch_contact_stats": (_i32, [vp, vp, vp]),
         "shl_context_size": (_i32, [vp, ctypes.POINTER(_u32), ctypes.POINTER(_u32)]),
         "shl_context_mesh": (_i32, [vp, vp, vp]),
         "shl_get_node_fields": (_i32, [vp, vp, vp, vp, vp, vp]),
@@ -125,7 +126,8 @@ def exported_symbols():
             "shl_icosphere", "shl_icosphere_off", "shl_read_off", "shl_gaussian_normal_imperfection",
             "shl_params_default", "shl_get_stream", "shl_upload_pressure_table", "shl_step_enqueue",
             "shl_step_collect", "shl_time_kernel", "shl_measure_fp64_peak", "shl_internal_force_noalloc",
-            "shl_profile_step", "shl_batch_create", "shl_batch_layout", "shl_context_size", "shl_context_mesh",
+            "shl_profile_step", "shl_batch_create", "shl_batch_layout", "shl_batch_contact_stats", "shl_context_size",
+            "shl_context_mesh",
             "shl_get_node_fields", "shl_apply_loaded_state", "shl_save_state_file", "shl_load_state_file",
             "shl_write_vtu", "shl_get_energies", "shl_mlp_create", "shl_mlp_destroy", "shl_mlp_set_params",
             "shl_mlp_get_params", "shl_mlp_set_dataset", "shl_mlp_train", "shl_mlp_predict", "shl_mlp_gradients",
@@ -436,7 +438,7 @@ class Shell:
 
     def residual(self, pressure, flags=0):
         """Relative residual ||f_ext - f_int|| / ||f_ext|| of the stored state, per shell
-        (flags: RESIDUAL_FP64, RESIDUAL_CORRECT, RESIDUAL_CLEAR)."""
+        (flags: RESIDUAL_FP64, RESIDUAL_CORRECT, RESIDUAL_CLEAR, RESIDUAL_CONTACT)."""
         n = self.n_shells
         rel, f2, e2 = np.zeros(n), np.zeros(n), np.zeros(n)
         _check(self.lib.shl_residual(self.h, pressure, flags, rel.ctypes.data, f2.ctypes.data, e2.ctypes.data),
@@ -498,6 +500,20 @@ class Batch(Shell):
     def split(self, vec):
         """Per-shell views of a concatenated node-major vector."""
         return [vec[3 * self.node_off[k]:3 * self.node_off[k + 1]] for k in range(self.n_shells)]
+
+    def contact_stats(self):
+        """Per shell (self-contact on): du_sum and the candidate-list rebuilds since creation."""
+        du = np.zeros(self.n_shells)
+        nr = np.zeros(self.n_shells, dtype=np.uint32)
+        _check(self.lib.shl_batch_contact_stats(self.h, du.ctypes.data, nr.ctypes.data), "shl_batch_contact_stats",
+               False)
+        return du, nr
+
+    def split_pairs(self, pairs):
+        """Contact pairs (batch face ids) per shell, in each shell's own face ids."""
+        pairs = np.asarray(pairs, dtype=np.int64).reshape(-1, 2)
+        shell = np.searchsorted(self.face_off, pairs[:, 0], side="right") - 1
+        return [pairs[shell == k] - self.face_off[k] for k in range(self.n_shells)]
 
 
 def gemm_bf16(A_bits, B_bits):

@@ -4,8 +4,12 @@ The problem family (no counterpart in the reference, which always starts from
 the undeformed state): a closed level-5 icosphere shell (10,242 nodes, 20,480
 faces) with a geometric imperfection, under a uniform external pressure held
 constant, relaxed by the explicit Newmark solver with mass-proportional
-damping until the relative residual ||f_ext - f_int|| / ||f_ext|| (see
-shl_residual) falls below a tolerance.
+damping until the relative residual ||f_ext - f_int - f_contact|| / ||f_ext||
+(see shl_residual) falls below a tolerance.  Above the classical buckling
+pressure (pressure / p_cl in [1.2, 3]) the sphere collapses: its equilibrium
+is a buckled shape held by self-contact (linear, frictionless, so that the
+equilibrium does not depend on the path; linked cells of 2h), and f_contact is
+the static contact force of the current candidate list.
 
 Eight inputs per problem:
   log(E1/E2) with E1 E2 = 1, nu12, G12 / sqrt(E1 E2), log(h/R),
@@ -38,6 +42,7 @@ IMPERFECTION = 0.3        # amplitude of the imperfection in units of h
 DAMPING = 1.0             # mass-proportional damping of the relaxation
 DT = 4e-3                 # relaxation time step
 CHECK_EVERY = 100         # steps between residual checks
+S_RANGE = (1.2, 3.0)      # pressure / p_cl of the problems: the buckled (collapsed) regime
 
 
 def harmonics(X):
@@ -47,7 +52,7 @@ def harmonics(X):
     return np.stack([(3 * z * z - 1) / 2, np.sqrt(3.0) * x * z, x * (5 * z * z - 1) / 2], 1), n
 
 
-def sample_problems(n, seed, s_range=(0.15, 0.5)):
+def sample_problems(n, seed, s_range=S_RANGE):
     """n problems from a seed (material, thickness, pressure, imperfection)."""
     rng = np.random.default_rng(seed)
     return {
@@ -76,10 +81,13 @@ def classical_pressure(e1, e2, nu12, h):
     return 2 * E * h * h / np.sqrt(3 * (1 - nu * nu))
 
 
-def build_batch(pr, precision=L.PREC_FP32, level=LEVEL, dt=DT, damping=DAMPING):
-    """One batch context over the problems; returns (batch, h per shell)."""
+def build_batch(pr, precision=L.PREC_FP32, level=LEVEL, dt=DT, damping=DAMPING, contact=True):
+    """One batch context over the problems; returns (batch, h per shell).
+    contact: each shell with its own frictionless self-contact (linked cells of 2h)."""
     X0, T = L.icosphere(level)
     Y, nrm = harmonics(X0)
+    P = X0[T]
+    ext = (P.max(axis=1) - P.min(axis=1)).max(axis=1).mean()
     meshes, params, scale = [], [], []
     for k in range(len(pr["h"])):
         r, nu, g, h, s = (float(pr[q][k]) for q in ("ratio", "nu", "g", "h", "s"))
@@ -89,7 +97,8 @@ def build_batch(pr, precision=L.PREC_FP32, level=LEVEL, dt=DT, damping=DAMPING):
         params.append(L.default_params(shell_mass_density=1.0, shell_young_modulus=e1, shell_young_modulus2=e2,
                                        shell_poisson_ratio=nu, shell_shear_modulus=g * np.sqrt(e1 * e2),
                                        thickness=h, damping_alpha=damping, dt=dt,
-                                       shell_shell_contact=L.CONTACT_NONE, precision=precision))
+                                       shell_shell_contact=L.CONTACT_LINEAR if contact else L.CONTACT_NONE,
+                                       mu_s=0.0, mu_d=0.0, cell_size_mult=2 * h / ext, precision=precision))
         scale.append(s * classical_pressure(e1, e2, nu, h))
     return L.Batch(meshes, params, np.array(scale)), np.asarray(pr["h"], float)
 
@@ -105,6 +114,8 @@ def relax(batch, u_start, tol=1e-6, check_every=CHECK_EVERY, max_steps=40000, co
     residuals, the displacement at convergence and the wall time."""
     n = batch.n_shells
     flags = L.RESIDUAL_FP64 | (L.RESIDUAL_CORRECT if correct else L.RESIDUAL_CLEAR)
+    if batch.params.shell_shell_contact != L.CONTACT_NONE:
+        flags |= L.RESIDUAL_CONTACT
     t0 = time.perf_counter()
     batch.apply_initial_conditions(u_start, 0.0, -1.0)
     conv_step = np.full(n, -1, dtype=np.int64)
@@ -161,7 +172,8 @@ def standardizer(F):
     return mu.astype(np.float32), sd.astype(np.float32)
 
 
-def generate(problems, batch_size=512, precision=L.PREC_FP32, tol=5e-5, max_steps=10000, log=None, level=LEVEL):
+def generate(problems, batch_size=512, precision=L.PREC_FP32, tol=5e-5, max_steps=10000, log=None, level=LEVEL,
+             contact=True):
     """Equilibria of the problems by plain relaxation from zero, in batches.
     Returns (u_eq as n x 3V float64, conv_step, final residual, stats)."""
     n = len(problems["h"])
@@ -170,7 +182,7 @@ def generate(problems, batch_size=512, precision=L.PREC_FP32, tol=5e-5, max_step
     for s in range(0, n, batch_size):
         idx = np.arange(s, min(n, s + batch_size))
         t0 = time.perf_counter()
-        b, _ = build_batch(subset(problems, idx), precision=precision, level=level)
+        b, _ = build_batch(subset(problems, idx), precision=precision, level=level, contact=contact)
         stats["setup_s"] += time.perf_counter() - t0
         r = relax(b, np.zeros(3 * b.V), tol=tol, max_steps=max_steps)
         stats["wall_s"] += r["wall_s"]
@@ -223,14 +235,14 @@ def project(Y, mean, basis):
 
 
 def solve(pr, U_start, level, precision, tol, max_steps, polish_tol=None, polish_max=None, smooth_steps=0,
-          smooth_damping=200.0):
+          smooth_damping=200.0, contact=True):
     """Relaxation of a batch of problems from U_start (n x 3V).  With
     polish_tol, a second FP64 phase continues from the first phase's state
     (restarted at rest) down to polish_tol.  Returns per-shell steps to the
     final tolerance (-1: not reached), the final displacements, wall time and
     face-steps of each phase."""
     n = len(pr["h"])
-    b, _ = build_batch(pr, precision=precision, level=level)
+    b, _ = build_batch(pr, precision=precision, level=level, contact=contact)
     F = b.F
     r = relax(b, np.asarray(U_start, np.float64).reshape(-1), tol=tol, max_steps=max_steps, smooth_steps=smooth_steps,
               smooth_damping=smooth_damping)
@@ -241,7 +253,7 @@ def solve(pr, U_start, level, precision, tol, max_steps, polish_tol=None, polish
          "face_steps_per_s": F * r["steps"] / r["wall_s"], "reached": int((r["conv_step"] >= 0).sum())}]}
     if polish_tol is None:
         return out
-    b, _ = build_batch(pr, precision=L.PREC_FP64, level=level)
+    b, _ = build_batch(pr, precision=L.PREC_FP64, level=level, contact=contact)
     r2 = relax(b, np.concatenate(r["u"]), tol=polish_tol, max_steps=polish_max)
     b.close()
     ok = (r["conv_step"] >= 0) & (r2["conv_step"] >= 0)
@@ -259,8 +271,8 @@ def _stats(steps, mask):
 
 
 def experiment(n_train=2048, n_test=256, seed=0, batch_size=512, train_iters=4000, gen_tol=5e-5, gen_max=10000,
-               tol=1e-6, max_steps=15000, log=print, level=LEVEL, hidden=None, train_batch=256, s_range=(0.15, 0.5),
-               mixed=False, n_modes=32, smooth_steps=200, smooth_damping=200.0):
+               tol=1e-6, max_steps=15000, log=print, level=LEVEL, hidden=None, train_batch=256, s_range=S_RANGE,
+               mixed=False, n_modes=32, smooth_steps=200, smooth_damping=200.0, contact=True):
     """The warm-start study.  Equilibria of n_train seeded problems by plain
     FP32 relaxation (FP64 defect correction) to gen_tol train the network;
     n_test held-out problems are then solved to the FP64 residual tol from
@@ -275,7 +287,7 @@ def experiment(n_train=2048, n_test=256, seed=0, batch_size=512, train_iters=400
     pr = sample_problems(n_train + n_test, seed, s_range)
     F = features(pr)
     U, steps, rels, st = generate(subset(pr, np.arange(n_train)), batch_size, tol=gen_tol, max_steps=gen_max, log=log,
-                                  level=level)
+                                  level=level, contact=contact)
     ok = steps >= 0
     out["generation"] = {"converged": int(ok.sum()), "wall_s": st["wall_s"], "setup_s": st["setup_s"],
                          "fp32_face_steps_per_s": st["face_steps"] / st["wall_s"],
@@ -295,10 +307,10 @@ def experiment(n_train=2048, n_test=256, seed=0, batch_size=512, train_iters=400
     U_pred = project(U_raw / ht[:, None], mean, basis) * ht[:, None]
     V3 = U_pred.shape[1]
     res = {}
-    variants = [("fp64", dict(precision=L.PREC_FP64, tol=tol, max_steps=max_steps))]
+    variants = [("fp64", dict(precision=L.PREC_FP64, tol=tol, max_steps=max_steps, contact=contact))]
     if mixed:
         variants.append(("fp32+fp64", dict(precision=L.PREC_FP32, tol=gen_tol, max_steps=gen_max, polish_tol=tol,
-                                           polish_max=max_steps)))
+                                           polish_max=max_steps, contact=contact)))
     for name, kw in variants:
         plain = solve(test, np.zeros((n_test, V3)), level, **kw)
         warm = solve(test, U_pred, level, smooth_steps=smooth_steps, smooth_damping=smooth_damping, **kw)

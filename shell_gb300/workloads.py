@@ -52,3 +52,38 @@ def squashed_state(X, s=0.0042, seed=0):
     u = np.zeros_like(X)
     u[:, 2] = (s - 1.0) * X[:, 2]
     return (u + 2e-5 * rng.standard_normal(X.shape)).reshape(-1)
+
+
+def ensemble_workload(L, n_shells=256, seed=0):
+    """256 shells, levels uniform over 3/4/5, per-shell parameters from a seed:
+    E1/E2 log-uniform in [0.2, 5] (E1 E2 = 1), h/R log-uniform in [0.005, 0.05],
+    pressure ramp end uniform in [1.2, 3] p_cl of the shell, imperfection
+    amplitude log-uniform in [1e-4, 1e-2] R; FP32 element forces, FP64 state;
+    each shell with its own self-contact (linear, Coulomb friction mu = 0.3,
+    linked cells of 2h: contact gaps in FP64)."""
+    rng = np.random.default_rng(seed)
+    meshes = {lv: L.icosphere(lv) for lv in (3, 4, 5)}
+    ext = {}
+    for lv, (X, T) in meshes.items():
+        P = X[T]
+        ext[lv] = (P.max(axis=1) - P.min(axis=1)).max(axis=1).mean()
+    shells, params, scale, u0 = [], [], [], []
+    for k in range(n_shells):
+        lv = int(rng.integers(3, 6))
+        r = float(np.exp(rng.uniform(np.log(0.2), np.log(5.0))))
+        h = float(np.exp(rng.uniform(np.log(0.005), np.log(0.05))))
+        s = float(rng.uniform(1.2, 3.0))
+        amp = float(np.exp(rng.uniform(np.log(1e-4), np.log(1e-2))))
+        e1, e2 = np.sqrt(r), 1.0 / np.sqrt(r)
+        E = np.sqrt(e1 * e2)
+        nu = np.sqrt(NU12 * NU12 * e2 / e1)
+        p_cl = 2 * E * h * h / np.sqrt(3 * (1 - nu * nu))
+        X, T = meshes[lv]
+        params.append(L.default_params(shell_mass_density=RHO, shell_young_modulus=e1, shell_young_modulus2=e2,
+                                       shell_poisson_ratio=NU12, shell_shear_modulus=G12 * E, thickness=h,
+                                       damping_alpha=ALPHA, dt=DT, shell_shell_contact=L.CONTACT_LINEAR, mu_s=MU,
+                                       mu_d=MU, cell_size_mult=2 * h / ext[lv], precision=L.PREC_FP32))
+        shells.append((X, T))
+        scale.append(s * p_cl)
+        u0.append(L.gaussian_normal_imperfection(X, amp, seed * 100000 + k).reshape(-1))
+    return shells, params, np.array(scale), np.concatenate(u0)

@@ -103,3 +103,46 @@ def test_residual_fp64_in_fp32_context_and_defect_correction(cuda_ok):
     r_c, u_c = relax(b32, L.RESIDUAL_FP64 | L.RESIDUAL_CORRECT)
     assert np.all(np.abs(r_c - r_ref) <= 1e-3 * r_ref + 1e-7)
     assert np.abs(u_c - u_ref).max() < 1e-4 * np.abs(u_ref).max()
+
+
+def test_residual_with_self_contact_matches_oracle(cuda_ok):
+    """SHL_RESIDUAL_CONTACT: the static self-contact force of the current
+    candidate list joins f_int (frictionless contact, no contact damping).  At
+    rest (v = 0) it equals the oracle's force evaluation with contact at the
+    same state; the contact state is left as it was."""
+    from tests.common import cell_size_mult_for
+    X, T = L.icosphere(3)
+    rng = np.random.default_rng(6)
+    u = np.zeros_like(X)
+    u[:, 2] = (0.0042 - 1.0) * X[:, 2]
+    u = (u + 2e-5 * rng.standard_normal(X.shape)).reshape(-1)
+    p = physics_params(mu_s=0.0, mu_d=0.0, cell_size_mult=cell_size_mult_for(X, T, 0.01))
+    pres = -classical_pressure()
+    z = np.zeros_like(u)
+    g = L.Shell(X, T, p)
+    g.set_state(u, z, z)
+    g.rebuild_contacts()
+    before = g.contact_state()
+    assert len(before["pairs"]) > 1000
+    r_plain = g.residual(pres)
+    r = g.residual(pres, L.RESIDUAL_CONTACT)
+    after = g.contact_state()
+    for k in ("pairs", "stick", "origin", "d2"):
+        assert np.array_equal(np.asarray(before[k]), np.asarray(after[k])), k
+    o = O.Oracle(X, T, p, threads=4)
+    o.set_state(u, z, z)
+    o.rebuild_contacts()
+    f = o.eval_forces(u, z, pres)[0]
+    _, _, fe = _oracle_residual(X, T, physics_params(contact=False), u, pres)
+    m = 1.0 / o.mass_damping()[0].reshape(-1, 3)[:, :1]
+    x = f.reshape(-1, 3)
+    x = (x - m * (x.sum(0) / m.sum())).reshape(-1)
+    ro = np.linalg.norm(x) / np.linalg.norm(fe)
+    assert abs(r[0] - ro) <= 1e-10 * ro
+    assert abs(r[0] - r_plain[0]) > 1e-3 * r_plain[0]  # the contact force matters at this state
+    with pytest.raises(L.ShlError):  # friction makes the contact force path dependent
+        q = physics_params(cell_size_mult=cell_size_mult_for(X, T, 0.01))
+        g2 = L.Shell(X, T, q)
+        g2.set_state(u, z, z)
+        g2.residual(pres, L.RESIDUAL_CONTACT)
+    g.close()
