@@ -77,6 +77,13 @@ ELEM_FLOPS_PER_FACE = 1372
 # from one ncu --set full capture with caches flushed (38.6 MB read, 3.4 MB
 # written; the force shares stay in the 129 MB L2 for the gather)
 ELEM_TRAFFIC_LEVEL6 = 42.0e6
+# FP32 element path (the ensemble): about 300 algorithmic bytes per face-step with
+# FP32 per-face constants; DRAM bytes of one launch on the 256-shell ensemble and its
+# FP32-pipe utilisation, from one ncu --set full capture (673.4 MB read, 427.0 MB
+# written: the force shares do not fit in L2 at this size)
+ENS_BYTES_PER_FACE = 300
+ENS_ELEM_TRAFFIC = 1100.4e6
+ENS_ELEM_FP32_PIPE = 0.129
 # warp instructions of one element-kernel launch on the level-6 shell (ncu
 # smsp__inst_executed.sum of the same capture) and the issue peak: 4 schedulers
 # per SM, one warp instruction per cycle each
@@ -169,12 +176,27 @@ def time_ensemble(L, torch, K, W, flush):
     _, nr2 = b.contact_stats()
     pairs_c = len(b.contact_state()["pairs"])
     F = b.F
+    # the FP32 element kernel alone (CUDA events, L2 evicted before each launch)
+    elem_ms = b.time_kernel(0, reps=10, flush_bytes=FLUSH_BYTES)
+    elem_variant = b.element_variant()[1]
     b.close()
+    hbm = 6800.0
+    try:
+        hbm = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["hbm_gbs"]
+    except (OSError, ValueError, KeyError):
+        pass
+    ach = F * ENS_BYTES_PER_FACE / (elem_ms * 1e-3) / 1e9
     levels = [int(round(np.log(len(T) / 20) / np.log(4))) for _, T in shells]
     return {"value": F * K / (ms * 1e-3), "unit": "face-steps/s", "ms_per_step": ms / K, "shells": len(shells),
             "faces": int(F), "levels": {str(lv): levels.count(lv) for lv in (3, 4, 5)},
             "dtype": "f32 forces, f64 state and contact gaps", "contact": "linear + friction, per-shell linked cells",
             "steps": K, "status": int(status), "n_pairs": int(n_pairs), "shell_rebuilds_total": int(nr0.sum()),
+            "roofline": {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
+                         "traffic": ENS_ELEM_TRAFFIC, "kernel": "k_elements32", "variant": elem_variant,
+                         "kernel_ms": elem_ms, "fp32_pipe_frac": ENS_ELEM_FP32_PIPE,
+                         "algorithmic_bytes": "%d B per face-step x %d faces" % (ENS_BYTES_PER_FACE, F),
+                         "note": "the FP32 element kernel of the batched path, timed live; traffic and FP32-pipe "
+                                 "share from one ncu capture (the larger fraction, HBM, is the bound)"},
             "contact_heavy": {"value": F * K / (ms_c * 1e-3), "ms_per_step": ms_c / K, "n_pairs": int(pairs_c),
                               "shell_rebuilds_in_timed_steps": int((nr2 - nr1).sum()),
                               "status": int(status_c),
@@ -551,6 +573,48 @@ def e2e_sample(g, torch, u0, K, W):
     return secs
 
 
+def warmstart_leg(args):
+    """Time to equilibrium (relative residual 1e-6, FP64) of held-out shells,
+    relaxed from zero (plain) and from the learned prediction (warm), and
+    the FP32 batched form (FP32 relaxation with FP64 defect correction, then
+    an FP64 polish) against the plain FP64 form; the surrogate is trained on
+    the GPU by the library's own kernels on equilibria the batched solver
+    generates.  Pressures 0.15-0.5 p_cl: in the buckled range the collapsed
+    shells do not reach the residual (profiles/warmstart_buckled_probe.md)."""
+    from shell_gb300 import warmstart as WS
+    t0 = time.perf_counter()
+    lv = args.ws_level
+    r = WS.experiment(n_train=args.ws_train, n_test=args.ws_test, seed=1, batch_size=512, train_iters=1500,
+                      gen_tol=1e-5, gen_max=15000, tol=1e-6, max_steps=15000, level=lv, hidden=[512] * 4,
+                      train_batch=128, s_range=(0.15, 0.5), contact=False, mixed=True,
+                      log=lambda m: print(m, file=sys.stderr))
+    t64 = r["test"]["fp64"]
+    mix = r["test"]["fp32+fp64"]
+    plain, warm = t64["plain"], t64["warm"]
+    return {
+        "workload": "level-%d shells (%d faces each), %d training / %d held-out problems; constant pressure "
+                    "0.15-0.5 p_cl; explicit relaxation dt %g, mass damping %g; residual 1e-6 (FP64)"
+                    % (lv, 20 * 4 ** lv, args.ws_train, args.ws_test, WS.DT, WS.DAMPING),
+        "network": "8 -> 512 x 4 (GELU) -> %d, BF16 weights, FP32 accumulation, tcgen05 GEMMs" % (3 * (10 * 4 ** lv + 2)),
+        "time_to_equilibrium": {
+            "plain": {"median_steps": plain["median_steps"], "wall_s": plain["wall_s"],
+                      "converged": plain["converged"]},
+            "warm": {"median_steps": warm["median_steps"], "wall_s": warm["wall_s"], "converged": warm["converged"],
+                     "fallbacks": warm["fallbacks"],
+                     "equilibrium_within_1e-4_of_plain": warm["equilibrium_within_1e-4_of_plain"]},
+            "steps_saved": (None if plain["median_steps"] is None or warm["median_steps"] is None
+                            else 1.0 - warm["median_steps"] / plain["median_steps"])},
+        "fp32_batched_vs_fp64": {
+            "fp64_plain_face_steps_per_s": t64["plain"]["phases"][0]["face_steps_per_s"],
+            "fp32_phase_face_steps_per_s": mix["plain"]["phases"][0]["face_steps_per_s"],
+            "fp32_plus_fp64_wall_s": mix["plain"]["wall_s"], "fp64_wall_s": t64["plain"]["wall_s"],
+            "fp32_plus_fp64_median_steps": mix["plain"]["median_steps"],
+            "equilibrium_within_1e-4_of_fp64": mix.get("plain_vs_fp64_plain_within_1e-4")},
+        "prediction_error_over_h": t64.get("prediction_error_over_h"),
+        "training": r["training"], "generation": r["generation"],
+        "seconds": time.perf_counter() - t0}
+
+
 def run_value_leg(g, torch, u0, n_steps=RUN_STEPS):
     """The whole run back to back (graph replays of 16 steps), warm L2."""
     fresh_start(g, u0)
@@ -648,9 +712,8 @@ def run_ours(args, rank, world, dist):
                      if args.contact_modes else None)
     accuracy = fp32_accuracy(L) if args.accuracy else None
     warmstart = None
-    if args.warmstart:
-        from shell_gb300 import warmstart as WS
-        warmstart = WS.experiment(n_train=args.ws_train, n_test=args.ws_test, log=lambda m: print(m, file=sys.stderr))
+    if args.warmstart and rank == 0:
+        warmstart = warmstart_leg(args)
 
     # roofline of the element kernel (live, cold L2), at the state after the run
     elem_ms = g.time_kernel(0, reps=20, flush_bytes=FLUSH_BYTES)
@@ -743,10 +806,12 @@ def main():
                     help="steps of the run checked against the oracle every 100 steps (0 = no parity leg)")
     ap.add_argument("--parity-lockstep", type=int, default=1000, help="of these, steps also run by the oracle")
     ap.add_argument("--parity-contact", type=int, default=100, help="steps of the contact-heavy parity run")
-    ap.add_argument("--warmstart", type=int, default=0,
-                    help="also run the learned warm-start study (level-5 shells; minutes of GPU time)")
-    ap.add_argument("--ws-train", type=int, default=3584)
-    ap.add_argument("--ws-test", type=int, default=512)
+    ap.add_argument("--warmstart", type=int, default=1,
+                    help="also run the learned warm-start study: time to equilibrium, warm against plain start "
+                         "and FP32 batched against FP64 plain (level-4 shells by default)")
+    ap.add_argument("--ws-level", type=int, default=4)
+    ap.add_argument("--ws-train", type=int, default=448)
+    ap.add_argument("--ws-test", type=int, default=64)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     world = int(os.environ.get("WORLD_SIZE", "1"))

@@ -504,6 +504,10 @@ shl_status shl_mlp_gradients(shl_mlp* mlp, const float* X, const float* T, uint3
 /* C = A . B^T with the library's BF16 GEMM: A (M x K) and B (N x K) as BF16
  * bit patterns, K a multiple of 8; C is M x N FP32. */
 shl_status shl_gemm_bf16(const uint16_t* A, const uint16_t* B, uint32_t M, uint32_t N, uint32_t K, float* C);
+/* Average device time (ms, CUDA events over `reps` launches after a warm-up) of
+ * the same GEMM on device-resident operands of the given shape (pseudo-random
+ * values), for throughput figures. */
+shl_status shl_gemm_bf16_time(uint32_t M, uint32_t N, uint32_t K, int reps, double* avg_ms);
 
 /* Default parameters (ShellSystem constructor and set_parameters defaults). */
 void shl_params_default(shl_params* p);

@@ -10,15 +10,18 @@
 //   forward        Z  = H_prev . W^T        (A = H_prev,  B = W)
 //   input grad     dH = dZ . W              (A = dZ,      B = W^T)
 //   weight grad    dW = dZ^T . H_prev       (A = dZ^T,    B = H_prev^T)
-// The GEMM is a 128x128x32 block tile of eight warps, each a 64x32 warp tile
-// of mma.sync m16n8k16 BF16 products fed by ldmatrix from a two-stage
-// cp.async shared-memory pipeline.  Split-K writes FP32 partials that one
-// fixed-order kernel sums, so every result is deterministic.
+// The GEMM (k_gemm_tc) runs on the tcgen05 tensor cores: TMA loads of 128 x 64
+// operand tiles into a four-stage shared-memory ring, tcgen05.mma with the
+// accumulator in tensor memory, tcgen05.ld for the epilogue.  Split-K writes
+// FP32 partials that one fixed-order kernel sums, so every result is
+// deterministic.
 //
 // GELU is the erf form 0.5 x (1 + erf(x / sqrt 2)); the loss is the mean
 // squared error over the real (unpadded) outputs; the optimiser is Adam with
 // bias correction.  Feature dimensions are padded to multiples of 32 and the
 // batch to a multiple of 128; padded weights, inputs and targets are zero.
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -26,6 +29,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <mutex>
 #include <random>
 #include <string>
 #include <vector>
@@ -35,33 +39,111 @@
 
 namespace {
 
-constexpr int kBM = 128, kBN = 128, kBK = 32;
-constexpr int kLds = kBK + 8;  // padded shared row (bf16): 80 bytes, conflict-free ldmatrix
-constexpr int kGemmThreads = 256;
+// ---- the BF16 GEMM on the fifth-generation tensor cores ----
+// C[M,N] = A[M,K] . B[N,K]^T, both operands K-contiguous.  One CTA of four
+// warps per 128 x 128 output tile: thread 0 streams 128 x 64 tiles of A and B
+// into a four-stage shared-memory ring with TMA (128-byte swizzle, zero fill
+// past the matrix edges), thread 32 issues tcgen05.mma (M 128, N 128, K 16;
+// BF16 operands read from shared memory through matrix descriptors, FP32
+// accumulator in tensor memory) and releases each stage with tcgen05.commit,
+// and after the last K block all four warps read their 32 accumulator lanes
+// (rows) with tcgen05.ld for the epilogue.  Every wait on an mbarrier is
+// bounded in time: on expiry the kernel records an error, waits (bounded) for
+// its copies and products in flight, frees its tensor memory and returns.
+constexpr int kBM = 128, kBN = 128, kBK = 64;  // kBK bf16 = 128 bytes: one swizzle row
+constexpr int kStages = 4;
+constexpr int kGemmThreads = 128;
+constexpr int kTileBytes = kBM * kBK * 2;      // 16 KB per operand tile
+constexpr int kGemmSmem = kStages * 2 * kTileBytes + 1024;
+constexpr uint32_t kTmemCols = 128;            // FP32 accumulator: 128 lanes x 128 columns
+constexpr uint64_t kWaitNs = 2000000000ull;    // a wait gives up after 2 s
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
   return (uint32_t)__cvta_generic_to_shared(p);
 }
 
-__device__ __forceinline__ void cp_async16(uint32_t dst, const void* src, bool pred) {
-  const int n = pred ? 16 : 0;  // zero-fill outside the matrix
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(dst), "l"(src), "r"(n));
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::); }
-
-__device__ __forceinline__ void ldmatrix_x4(uint32_t addr, uint32_t& r0, uint32_t& r1, uint32_t& r2, uint32_t& r3) {
-  asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
-               : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
-               : "r"(addr));
+__device__ __forceinline__ uint64_t globaltimer() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
 }
 
-__device__ __forceinline__ void mma_bf16(float* d, const uint32_t* a, const uint32_t* b) {
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count));
+}
+
+__device__ __forceinline__ bool mbar_test(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
   asm volatile(
-      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-      "{%0,%1,%2,%3};\n"
-      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// wait for the phase of the given parity to complete; false after kWaitNs or
+// once *abort is set by another thread of the CTA
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int* abort) {
+  const uint64_t t0 = globaltimer();
+  for (uint32_t it = 0;; ++it) {
+    if (mbar_test(bar, parity)) return true;
+    if ((it & 63u) == 63u && (*abort || globaltimer() - t0 > kWaitNs)) return false;
+  }
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+// 2-D tiled TMA load of the box at (x = K element, y = row) into shared memory
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int x, int y, uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
+      ::"r"(dst), "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(bar)
+      : "memory");
+}
+
+// shared-memory matrix descriptor of a K-major operand tile written by TMA with
+// the 128-byte swizzle: rows of 128 bytes, 8-row groups 1024 bytes apart
+__device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t addr) {
+  uint64_t d = (uint64_t)((addr >> 4) & 0x3FFFu);  // start address
+  d |= (uint64_t)1 << 16;                          // leading byte offset (not used by swizzled K-major)
+  d |= (uint64_t)(1024 >> 4) << 32;                // stride byte offset between 8-row groups
+  d |= (uint64_t)1 << 46;                          // descriptor version of sm_100
+  d |= (uint64_t)2 << 61;                          // 128-byte swizzle
+  return d;
+}
+
+// instruction descriptor of kind::f16: FP32 accumulator, BF16 A and B, both K-major, M 128, N 128
+constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kBN >> 3) << 17) |
+                            ((uint32_t)(kBM >> 4) << 24);
+
+__device__ __forceinline__ void tc_mma(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
+      ::"r"(tmem_d), "l"(adesc), "l"(bdesc), "r"(kIdesc), "r"(accumulate));
+}
+
+__device__ __forceinline__ void tc_commit(uint32_t bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// 16 consecutive FP32 columns of this thread's accumulator lane
+__device__ __forceinline__ void tc_ld16(uint32_t taddr, float* v) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
 __device__ __forceinline__ float gelu(float x) { return 0.5f * x * (1.0f + erff(x * 0.70710678118654752f)); }
@@ -75,107 +157,149 @@ __device__ __forceinline__ float gelu_grad(float x) {
 enum { EPI_PARTIAL = 0, EPI_BIAS = 1, EPI_BIAS_GELU = 2 };
 
 struct GemmArgs {
-  const __nv_bfloat16* A;  // M x K, row stride lda
-  const __nv_bfloat16* B;  // N x K, row stride ldb
-  int M, N, K, lda, ldb;
-  int k_per_split;         // multiple of kBK
+  int M, N, K;
+  int kb_per_split;        // K blocks (kBK wide) per split-K slice (blockIdx.z)
   int mode;
   const float* bias;       // N (EPI_BIAS*)
   float* C;                // M x N fp32 (ldc) ; EPI_PARTIAL: split z writes C + z*M*ldc
   int ldc;
   __nv_bfloat16* Cb;       // optional bf16 copy of the activation (ldc)
+  int* error;              // set to 1 when a wait gave up
 };
 
-// C = A . B^T on a 128x128 block tile; blockIdx.z = split-K slice
-__global__ void __launch_bounds__(kGemmThreads) k_gemm_bf16(GemmArgs g) {
-  __shared__ __align__(16) __nv_bfloat16 sA[2][kBM * kLds];
-  __shared__ __align__(16) __nv_bfloat16 sB[2][kBN * kLds];
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int wm = warp >> 2, wn = warp & 3;  // 2 x 4 warps, warp tile 64 x 32
+__global__ void __launch_bounds__(kGemmThreads, 1)
+    k_gemm_tc(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b, GemmArgs g) {
+  extern __shared__ uint8_t smem_raw[];
+  __shared__ __align__(8) uint64_t full_bar[kStages], empty_bar[kStages], acc_bar;
+  __shared__ uint32_t tmem_base;
+  __shared__ int abort_flag;
+  __shared__ int issued[kStages];  // K blocks loaded into each stage (for the drain after an abort)
+  const uint32_t base = (smem_u32(smem_raw) + 1023u) & ~1023u;  // swizzled tiles start on 1024 bytes
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int m0 = blockIdx.y * kBM, n0 = blockIdx.x * kBN;
-  const int k_begin = blockIdx.z * g.k_per_split;
-  const int k_end = min(g.K, k_begin + g.k_per_split);
-  const int n_tiles = (k_end - k_begin + kBK - 1) / kBK;
-
-  float acc[4][4][4];
-#pragma unroll
-  for (int i = 0; i < 4; ++i)
-#pragma unroll
-    for (int j = 0; j < 4; ++j)
-#pragma unroll
-      for (int r = 0; r < 4; ++r) acc[i][j][r] = 0.f;
-
-  // each thread copies two 16-byte chunks of A and two of B per k tile
-  auto load_tile = [&](int stage, int kt) {
-    const int kb = k_begin + kt * kBK;
-#pragma unroll
-    for (int c = 0; c < 2; ++c) {
-      const int chunk = tid + c * kGemmThreads;  // 0..511
-      const int row = chunk >> 2, col = (chunk & 3) * 8;
-      const int gm = m0 + row, gk = kb + col;
-      const bool pa = gm < g.M && gk < k_end;
-      const __nv_bfloat16* srcA = g.A + (size_t)(pa ? gm : 0) * g.lda + (pa ? gk : 0);
-      cp_async16(smem_u32(&sA[stage][row * kLds + col]), srcA, pa);
-      const int gn = n0 + row;
-      const bool pb = gn < g.N && gk < k_end;
-      const __nv_bfloat16* srcB = g.B + (size_t)(pb ? gn : 0) * g.ldb + (pb ? gk : 0);
-      cp_async16(smem_u32(&sB[stage][row * kLds + col]), srcB, pb);
+  const int kb_total = (g.K + kBK - 1) / kBK;
+  const int kb0 = blockIdx.z * g.kb_per_split;
+  const int nkb = max(0, min(g.kb_per_split, kb_total - kb0));
+  volatile int* abort = &abort_flag;
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kStages; ++s) {
+      mbar_init(smem_u32(&full_bar[s]), 1);
+      mbar_init(smem_u32(&empty_bar[s]), 1);
+      issued[s] = 0;
     }
-    cp_async_commit();
-  };
-
-  if (n_tiles > 0) load_tile(0, 0);
-  for (int kt = 0; kt < n_tiles; ++kt) {
-    const int st = kt & 1;
-    cp_async_wait_all();
-    __syncthreads();
-    if (kt + 1 < n_tiles) load_tile(st ^ 1, kt + 1);
-#pragma unroll
-    for (int ks = 0; ks < kBK; ks += 16) {
-      uint32_t af[4][4], bfr[4][2];
-#pragma unroll
-      for (int i = 0; i < 4; ++i) {
-        const int r = wm * 64 + i * 16 + (lane & 15);
-        const int c = ks + (lane >> 4) * 8;
-        ldmatrix_x4(smem_u32(&sA[st][r * kLds + c]), af[i][0], af[i][1], af[i][2], af[i][3]);
-      }
-#pragma unroll
-      for (int j = 0; j < 4; j += 2) {
-        // lanes 0-7: n 0-7 k 0; 8-15: n 0-7 k 8; 16-23: n 8-15 k 0; 24-31: n 8-15 k 8
-        const int r = wn * 32 + j * 8 + (lane & 7) + ((lane >> 4) << 3);
-        const int c = ks + ((lane >> 3) & 1) * 8;
-        ldmatrix_x4(smem_u32(&sB[st][r * kLds + c]), bfr[j][0], bfr[j][1], bfr[j + 1][0], bfr[j + 1][1]);
-      }
-#pragma unroll
-      for (int i = 0; i < 4; ++i)
-#pragma unroll
-        for (int j = 0; j < 4; ++j) mma_bf16(acc[i][j], af[i], bfr[j]);
-    }
-    __syncthreads();
+    mbar_init(smem_u32(&acc_bar), 1);
+    abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   }
-
-  // epilogue: thread holds rows (lane/4, +8) and columns 2*(lane%4) + {0,1} of each 16x8 tile
-  const int gr = lane >> 2, gc = (lane & 3) * 2;
-  float* C = g.C + (g.mode == EPI_PARTIAL ? (size_t)blockIdx.z * g.M * g.ldc : 0);
-#pragma unroll
-  for (int i = 0; i < 4; ++i)
-#pragma unroll
-    for (int j = 0; j < 4; ++j)
-#pragma unroll
-      for (int h = 0; h < 2; ++h) {
-        const int row = m0 + wm * 64 + i * 16 + gr + h * 8;
-        if (row >= g.M) continue;
-#pragma unroll
-        for (int e = 0; e < 2; ++e) {
-          const int col = n0 + wn * 32 + j * 8 + gc + e;
-          if (col >= g.N) continue;
-          float v = acc[i][j][2 * h + e];
-          if (g.mode != EPI_PARTIAL) v += g.bias[col];
-          const size_t o = (size_t)row * g.ldc + col;
-          C[o] = v;
-          if (g.Cb) g.Cb[o] = __float2bfloat16_rn(g.mode == EPI_BIAS_GELU ? gelu(v) : v);
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
+                 "r"(kTmemCols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tmem_base;
+  bool mma_done = true;
+  if (nkb > 0) {
+    if (threadIdx.x == 0) {  // TMA producer
+      for (int kb = 0; kb < nkb; ++kb) {
+        const int s = kb % kStages;
+        const uint32_t ph = (uint32_t)(kb / kStages) & 1u;
+        if (!mbar_wait(smem_u32(&empty_bar[s]), ph ^ 1u, abort)) {
+          *abort = 1;
+          break;
         }
+        const uint32_t fb = smem_u32(&full_bar[s]);
+        mbar_expect_tx(fb, 2 * kTileBytes);
+        const int kx = (kb0 + kb) * kBK;
+        tma_load_2d(base + (uint32_t)s * 2 * kTileBytes, &map_a, kx, m0, fb);
+        tma_load_2d(base + (uint32_t)s * 2 * kTileBytes + kTileBytes, &map_b, kx, n0, fb);
+        issued[s] += 1;
       }
+    } else if (threadIdx.x == 32) {  // MMA issuer
+      for (int kb = 0; kb < nkb; ++kb) {
+        const int s = kb % kStages;
+        const uint32_t ph = (uint32_t)(kb / kStages) & 1u;
+        if (!mbar_wait(smem_u32(&full_bar[s]), ph, abort)) {
+          *abort = 1;
+          break;
+        }
+        tc_fence_after();
+        const uint32_t a_addr = base + (uint32_t)s * 2 * kTileBytes, b_addr = a_addr + kTileBytes;
+#pragma unroll
+        for (int k = 0; k < kBK / 16; ++k)  // K 16 per product: 32 bytes further along the swizzled rows
+          tc_mma(tmem, smem_desc_sw128(a_addr + 32u * k), smem_desc_sw128(b_addr + 32u * k), (kb | k) != 0 ? 1u : 0u);
+        tc_commit(smem_u32(&empty_bar[s]));
+      }
+      tc_commit(smem_u32(&acc_bar));  // completes once every product issued above has
+    }
+    __syncwarp();
+    // every thread: the accumulator is complete (bounded)
+    mma_done = mbar_wait(smem_u32(&acc_bar), 0u, abort);
+    if (!mma_done) *abort = 1;
+  }
+  tc_fence_after();
+  __syncthreads();
+  const bool failed = *abort != 0;
+  if (failed) {
+    if (threadIdx.x == 0) {
+      atomicExch(g.error, 1);
+      // drain: the last load issued into each stage lands (bounded) before the CTA's shared memory is released
+      for (int s = 0; s < kStages; ++s)
+        if (issued[s] > 0) {
+          const uint64_t t0 = globaltimer();
+          while (!mbar_test(smem_u32(&full_bar[s]), (uint32_t)(issued[s] - 1) & 1u) && globaltimer() - t0 < kWaitNs) {
+          }
+        }
+      const uint64_t t0 = globaltimer();
+      while (nkb > 0 && !mbar_test(smem_u32(&acc_bar), 0u) && globaltimer() - t0 < kWaitNs) {
+      }
+    }
+  } else {
+    // epilogue: warp w holds rows m0 + 32 w .. + 31 (accumulator lanes), 16 columns per load
+    const int row = m0 + warp * 32 + lane;
+    float* C = g.C + (g.mode == EPI_PARTIAL ? (size_t)blockIdx.z * g.M * g.ldc : 0);
+#pragma unroll 1
+    for (int c = 0; c < kBN; c += 16) {
+      float v[16];
+      if (nkb > 0) {
+        tc_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c, v);
+      } else {
+#pragma unroll
+        for (int i = 0; i < 16; ++i) v[i] = 0.f;
+      }
+      if (row >= g.M) continue;
+#pragma unroll
+      for (int i = 0; i < 16; ++i) {
+        const int col = n0 + c + i;
+        if (col >= g.N) break;
+        float x = v[i];
+        if (g.mode != EPI_PARTIAL) x += g.bias[col];
+        const size_t o = (size_t)row * g.ldc + col;
+        C[o] = x;
+        if (g.Cb) g.Cb[o] = __float2bfloat16_rn(g.mode == EPI_BIAS_GELU ? gelu(x) : x);
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols));
+  }
+}
+
+// pseudo-random bf16 values in [-1, 1) (hash of the index), operands of the GEMM timing
+__global__ void k_fill_bf16(__nv_bfloat16* p, size_t n, uint32_t seed) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    uint32_t h = (uint32_t)i * 2654435761u ^ seed;
+    h ^= h >> 15;
+    h *= 2246822519u;
+    h ^= h >> 13;
+    p[i] = __float2bfloat16_rn((float)(h >> 8) * (2.0f / 16777216.0f) - 1.0f);
+  }
 }
 
 // out[m, n] = sum over splits of part[s, m, n] (fixed order), optional bf16 copy
@@ -316,6 +440,7 @@ struct shl_mlp {
   __nv_bfloat16* dZ = nullptr;       // bf16 grads (max width)
   __nv_bfloat16* dZT = nullptr;
   float* part = nullptr;             // split-K partials
+  int* gemm_err = nullptr;           // set by a GEMM whose wait gave up
   size_t part_elems = 0;
   float* Tb = nullptr;
   double* loss_part = nullptr;
@@ -355,30 +480,92 @@ shl_status mlp_alloc(shl_mlp* m, T** p, size_t n) {
     if (s_ != SHL_OK) return s_;         \
   } while (0)
 
+// cuTensorMapEncodeTiled from the driver (no link-time dependency on libcuda)
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  });
+  return fn;
+}
+
+// TMA map of a K-contiguous BF16 operand (rows x K, row stride ld elements):
+// 64 x 128 boxes with the 128-byte swizzle, zeros past the edges
+shl_status operand_map(CUtensorMap* map, const __nv_bfloat16* ptr, int rows, int K, int ld) {
+  PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+  if (!enc) {
+    shl::set_error("cuTensorMapEncodeTiled is not available from the driver");
+    return SHL_ERR_CUDA;
+  }
+  if ((reinterpret_cast<uintptr_t>(ptr) & 15u) || (ld * 2) % 16 || rows < 1 || K < 1) {
+    shl::set_error("GEMM operand: 16-byte aligned base and row stride, non-empty extents");
+    return SHL_ERR_ARG;
+  }
+  const cuuint64_t dims[2] = {(cuuint64_t)K, (cuuint64_t)rows};
+  const cuuint64_t strides[1] = {(cuuint64_t)ld * 2};
+  const cuuint32_t box[2] = {(cuuint32_t)kBK, (cuuint32_t)kBM};
+  const cuuint32_t es[2] = {1, 1};
+  const CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<__nv_bfloat16*>(ptr), dims, strides, box,
+                         es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                         CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) {
+    shl::set_error("cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
+    return SHL_ERR_CUDA;
+  }
+  return SHL_OK;
+}
+
+cudaError_t gemm_kernel_attributes() {
+  static cudaError_t e = cudaFuncSetAttribute((const void*)k_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              kGemmSmem);
+  return e;
+}
+
 // C[M,N] = A[M,K] . B[N,K]^T with the chosen epilogue.  Products without an
 // epilogue split K when the output grid alone would leave SMs idle.
 shl_status gemm(shl_mlp* m, const __nv_bfloat16* A, int lda, const __nv_bfloat16* B, int ldb, int M, int N, int K,
                 int mode, const float* bias, float* C, __nv_bfloat16* Cb) {
+  MLP_TRY(gemm_kernel_attributes());
+  CUtensorMap ma, mb;
+  MLP_CHECK(operand_map(&ma, A, M, K, lda));
+  MLP_CHECK(operand_map(&mb, B, N, K, ldb));
   const int gx = (N + kBN - 1) / kBN, gy = (M + kBM - 1) / kBM;
-  const int k_tiles = (K + kBK - 1) / kBK;
+  const int k_blocks = (K + kBK - 1) / kBK;
   int splits = 1;
   if (mode == EPI_PARTIAL)
-    while (gx * gy * splits < 2 * 152 && k_tiles / (splits * 2) >= 8 &&
+    while (gx * gy * splits < 2 * 152 && k_blocks / (splits * 2) >= 4 &&
            (size_t)(splits * 2) * M * N <= m->part_elems)
       splits *= 2;
-  GemmArgs g{A, B, M, N, K, lda, ldb, 0, mode, bias, C, N, Cb};
+  GemmArgs g{M, N, K, k_blocks, mode, bias, C, N, Cb, m->gemm_err};
   if (splits == 1) {
-    g.k_per_split = k_tiles * kBK;
-    k_gemm_bf16<<<dim3(gx, gy, 1), kGemmThreads, 0, m->stream>>>(g);
+    k_gemm_tc<<<dim3(gx, gy, 1), kGemmThreads, kGemmSmem, m->stream>>>(ma, mb, g);
     return SHL_OK;
   }
-  const int tiles_per = (k_tiles + splits - 1) / splits;
-  g.k_per_split = tiles_per * kBK;
-  splits = (k_tiles + tiles_per - 1) / tiles_per;
+  const int per = (k_blocks + splits - 1) / splits;
+  g.kb_per_split = per;
+  splits = (k_blocks + per - 1) / per;
   g.C = m->part;
   g.Cb = nullptr;
-  k_gemm_bf16<<<dim3(gx, gy, splits), kGemmThreads, 0, m->stream>>>(g);
+  k_gemm_tc<<<dim3(gx, gy, splits), kGemmThreads, kGemmSmem, m->stream>>>(ma, mb, g);
   k_splitk_reduce<<<592, 256, 0, m->stream>>>(m->part, splits, (size_t)M * N, C, Cb);
+  return SHL_OK;
+}
+
+// SHL_ERR_TIMEOUT when a GEMM gave up waiting (the flag is cleared)
+shl_status gemm_status(shl_mlp* m) {
+  int e = 0;
+  MLP_TRY(cudaMemcpyAsync(&e, m->gemm_err, sizeof(int), cudaMemcpyDeviceToHost, m->stream));
+  MLP_TRY(cudaStreamSynchronize(m->stream));
+  if (e) {
+    MLP_TRY(cudaMemsetAsync(m->gemm_err, 0, sizeof(int), m->stream));
+    shl::set_error("tensor-core GEMM: a pipeline wait gave up");
+    return SHL_ERR_TIMEOUT;
+  }
   return SHL_OK;
 }
 
@@ -523,7 +710,7 @@ shl_status shl_mlp_create(const uint32_t* dims, uint32_t n_dims, uint32_t max_ba
   if ((s = mlp_alloc(m, &m->dH, (size_t)R * maxw)) || (s = mlp_alloc(m, &m->dZ, (size_t)R * maxw)) ||
       (s = mlp_alloc(m, &m->dZT, (size_t)R * maxw)) || (s = mlp_alloc(m, &m->part, m->part_elems)) ||
       (s = mlp_alloc(m, &m->Tb, (size_t)R * m->pad[L])) || (s = mlp_alloc(m, &m->loss_part, 592)) ||
-      (s = mlp_alloc(m, &m->idx, (size_t)R)))
+      (s = mlp_alloc(m, &m->idx, (size_t)R)) || (s = mlp_alloc(m, &m->gemm_err, 1)))
     return fail(s);
   if ((s = refresh_copies(m)) != SHL_OK) return fail(s);
   if (cudaStreamSynchronize(m->stream) != cudaSuccess) return fail(SHL_ERR_CUDA);
@@ -613,7 +800,7 @@ shl_status shl_mlp_train(shl_mlp* m, uint32_t iters, uint32_t batch, float lr0, 
   }
   MLP_TRY(cudaStreamSynchronize(m->stream));
   MLP_TRY(cudaGetLastError());
-  return SHL_OK;
+  return gemm_status(m);
 }
 
 shl_status shl_mlp_predict(shl_mlp* m, const float* X, uint32_t n, float* Y) {
@@ -647,7 +834,8 @@ shl_status shl_mlp_predict(shl_mlp* m, const float* X, uint32_t n, float* Y) {
   }
   cudaFreeAsync(dXtmp, m->stream);
   MLP_TRY(cudaStreamSynchronize(m->stream));
-  return st;
+  if (st != SHL_OK) return st;
+  return gemm_status(m);
 }
 
 shl_status shl_mlp_gradients(shl_mlp* m, const float* X, const float* T, uint32_t n, double* loss, float* const* dW,
@@ -673,6 +861,7 @@ shl_status shl_mlp_gradients(shl_mlp* m, const float* X, const float* T, uint32_
   m->dT = t;
   m->n_data = nd;
   if (st != SHL_OK) return st;
+  MLP_CHECK(gemm_status(m));
   for (int l = 0; l < L; ++l) {
     const int o = m->dim[l + 1], i = m->dim[l];
     if (dW && dW[l]) {
@@ -697,7 +886,7 @@ shl_status shl_gemm_bf16(const uint16_t* A, const uint16_t* B, uint32_t M, uint3
   tmp.part_elems = (size_t)M * N * 8;
   shl_status st = SHL_OK;
   if (mlp_alloc(&tmp, &dA, (size_t)M * K) || mlp_alloc(&tmp, &dB, (size_t)N * K) || mlp_alloc(&tmp, &dC, (size_t)M * N) ||
-      mlp_alloc(&tmp, &tmp.part, tmp.part_elems))
+      mlp_alloc(&tmp, &tmp.part, tmp.part_elems) || mlp_alloc(&tmp, &tmp.gemm_err, 1))
     st = SHL_ERR_OOM;
   if (st == SHL_OK) {
     cudaMemcpyAsync(dA, A, (size_t)M * K * 2, cudaMemcpyHostToDevice, tmp.stream);
@@ -705,8 +894,46 @@ shl_status shl_gemm_bf16(const uint16_t* A, const uint16_t* B, uint32_t M, uint3
     st = gemm(&tmp, dA, (int)K, dB, (int)K, (int)M, (int)N, (int)K, EPI_PARTIAL, nullptr, dC, nullptr);
     cudaMemcpyAsync(C, dC, (size_t)M * N * sizeof(float), cudaMemcpyDeviceToHost, tmp.stream);
     if (cudaStreamSynchronize(tmp.stream) != cudaSuccess || cudaGetLastError() != cudaSuccess) st = SHL_ERR_CUDA;
+    if (st == SHL_OK) st = gemm_status(&tmp);
   }
   for (void* p : tmp.allocs) cudaFree(p);
+  cudaStreamDestroy(tmp.stream);
+  return st;
+}
+
+shl_status shl_gemm_bf16_time(uint32_t M, uint32_t N, uint32_t K, int reps, double* avg_ms) {
+  // average device time of C = A . B^T on device-resident operands (CUDA events, reps launches after one warm-up)
+  if (!avg_ms || M == 0 || N == 0 || K == 0 || K % 8 != 0 || reps < 1) return SHL_ERR_ARG;
+  shl_mlp tmp;
+  MLP_TRY(cudaStreamCreateWithFlags(&tmp.stream, cudaStreamNonBlocking));
+  __nv_bfloat16 *dA = nullptr, *dB = nullptr;
+  float* dC = nullptr;
+  tmp.part_elems = (size_t)M * N * 8;
+  shl_status st = SHL_OK;
+  if (mlp_alloc(&tmp, &dA, (size_t)M * K) || mlp_alloc(&tmp, &dB, (size_t)N * K) || mlp_alloc(&tmp, &dC, (size_t)M * N) ||
+      mlp_alloc(&tmp, &tmp.part, tmp.part_elems) || mlp_alloc(&tmp, &tmp.gemm_err, 1))
+    st = SHL_ERR_OOM;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (st == SHL_OK && (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)) st = SHL_ERR_CUDA;
+  if (st == SHL_OK) {
+    k_fill_bf16<<<592, 256, 0, tmp.stream>>>(dA, (size_t)M * K, 1u);
+    k_fill_bf16<<<592, 256, 0, tmp.stream>>>(dB, (size_t)N * K, 2u);
+  }
+  if (st == SHL_OK) st = gemm(&tmp, dA, (int)K, dB, (int)K, (int)M, (int)N, (int)K, EPI_PARTIAL, nullptr, dC, nullptr);
+  if (st == SHL_OK) {
+    cudaEventRecord(e0, tmp.stream);
+    for (int r = 0; r < reps && st == SHL_OK; ++r)
+      st = gemm(&tmp, dA, (int)K, dB, (int)K, (int)M, (int)N, (int)K, EPI_PARTIAL, nullptr, dC, nullptr);
+    cudaEventRecord(e1, tmp.stream);
+    float ms = 0.f;
+    if (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) st = SHL_ERR_CUDA;
+    *avg_ms = ms / reps;
+  }
+  if (st == SHL_OK) st = gemm_status(&tmp);
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  cudaStreamSynchronize(tmp.stream);
+  for (void* q : tmp.allocs) cudaFree(q);
   cudaStreamDestroy(tmp.stream);
   return st;
 }

@@ -97,6 +97,7 @@ def load():
         "shl_mlp_predict": (_i32, [vp, vp, _u32, vp]),
         "shl_mlp_gradients": (_i32, [vp, vp, vp, _u32, ctypes.POINTER(_d), vp, vp]),
         "shl_gemm_bf16": (_i32, [vp, vp, _u32, _u32, _u32, vp]),
+        "shl_gemm_bf16_time": (_i32, [_u32, _u32, _u32, ctypes.c_int, ctypes.POINTER(_d)]),
         "shl_residual": (_i32, [vp, _d, ctypes.c_int, vp, vp, vp]),
         "shl_set_pressure_function": (_i32, [vp, ctypes.c_char_p]),
         "shl_get_dt": (_i32, [vp, ctypes.POINTER(_d), ctypes.POINTER(_u32)]),
@@ -131,7 +132,7 @@ def exported_symbols():
             "shl_get_node_fields", "shl_apply_loaded_state", "shl_save_state_file", "shl_load_state_file",
             "shl_write_vtu", "shl_get_energies", "shl_mlp_create", "shl_mlp_destroy", "shl_mlp_set_params",
             "shl_mlp_get_params", "shl_mlp_set_dataset", "shl_mlp_train", "shl_mlp_predict", "shl_mlp_gradients",
-            "shl_gemm_bf16", "shl_residual", "shl_set_pressure_function", "shl_eval_pressure_function",
+            "shl_gemm_bf16", "shl_gemm_bf16_time", "shl_residual", "shl_set_pressure_function", "shl_eval_pressure_function",
             "shl_get_dt", "shl_set_stop_function", "shl_set_cavity_functions", "shl_get_cavity_origins",
             "shl_set_cavity_origins", "shl_scale_damping", "shl_set_element_variant", "shl_get_element_variant",
             "shl_get_contact_coords", "shl_set_contact_coords"]
@@ -526,6 +527,14 @@ def gemm_bf16(A_bits, B_bits):
     C = np.zeros((M, N), dtype=np.float32)
     _check(lib.shl_gemm_bf16(A_bits.ctypes.data, B_bits.ctypes.data, M, N, K, C.ctypes.data), "shl_gemm_bf16", False)
     return C
+
+
+def gemm_bf16_time(M, N, K, reps=20):
+    """Average device ms of the library's BF16 GEMM (M x K) . (N x K)^T on device-resident operands."""
+    lib = load()
+    ms = _d()
+    _check(lib.shl_gemm_bf16_time(M, N, K, reps, ctypes.byref(ms)), "shl_gemm_bf16_time", False)
+    return ms.value
 
 
 class MLP:

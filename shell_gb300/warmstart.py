@@ -30,6 +30,7 @@ start does not converge.  With mass-proportional damping every underdamped
 mode decays at the same rate, so the steps to a residual tolerance grow with
 the logarithm of the initial residual, and that is what a warm start can save.
 """
+import json
 import time
 
 import numpy as np
@@ -355,6 +356,41 @@ def experiment(n_train=2048, n_test=256, seed=0, batch_size=512, train_iters=400
     return out
 
 
+def probe(n=32, seed=3, level=4, s_range=S_RANGE, contact=True, max_steps=80000, check_every=2000,
+          precision=L.PREC_FP32, log=print):
+    """Plain relaxation from zero of n seeded problems, the residual
+    (quartiles over the shells) and the candidate pairs recorded every
+    check_every steps: whether the problem family reaches equilibrium at all.
+    Returns a JSON-able record."""
+    pr = sample_problems(n, seed, s_range)
+    b, _ = build_batch(pr, precision=precision, level=level, contact=contact)
+    flags = L.RESIDUAL_FP64 | L.RESIDUAL_CORRECT | (L.RESIDUAL_CONTACT if contact else 0)
+    t0 = time.perf_counter()
+    b.apply_initial_conditions(np.zeros(3 * b.V), 0.0, -1.0)
+    table = np.full(check_every, -1.0)
+    conv = np.full(n, -1, dtype=np.int64)
+    hist, steps, worst = [], 0, 0
+    while steps < max_steps:
+        _, st = b.step(check_every, table)
+        worst = max(worst, int(st))
+        steps += check_every
+        rel = b.residual(-1.0, flags)
+        conv[(rel < 1e-6) & (conv < 0)] = steps
+        q = np.percentile(rel, [0, 25, 50, 75, 100])
+        rec = {"steps": steps, "wall_s": time.perf_counter() - t0, "pairs": len(b.contact_state()["pairs"]),
+               "converged": int((conv >= 0).sum()), "residual_quartiles": [float(x) for x in q], "status": int(st)}
+        hist.append(rec)
+        if log:
+            log(json.dumps(rec))
+        if st >= 3 or (conv >= 0).all():
+            break
+    b.close()
+    return {"level": level, "shells": n, "seed": seed, "pressure_over_p_cl": list(s_range),
+            "contact": "linear, frictionless, linked cells 2h" if contact else "none",
+            "relaxation": {"dt": DT, "damping_alpha": DAMPING, "precision": "fp32 forces + fp64 defect correction"},
+            "worst_status": worst, "converged": int((conv >= 0).sum()), "history": hist}
+
+
 def _jsonable(o):
     if isinstance(o, dict):
         return {str(k): _jsonable(v) for k, v in o.items()}
@@ -366,9 +402,9 @@ def _jsonable(o):
 
 
 def main(argv=None):
-    """python -m shell_gb300.warmstart --train N --test M --out study.json"""
+    """python -m shell_gb300.warmstart --train N --test M --out study.json
+    python -m shell_gb300.warmstart --probe --level 4 --shells 32 --out probe.json"""
     import argparse
-    import json
     ap = argparse.ArgumentParser(description="learned warm start study (level-5 shells)")
     ap.add_argument("--train", type=int, default=3584)
     ap.add_argument("--test", type=int, default=256)
@@ -376,7 +412,15 @@ def main(argv=None):
     ap.add_argument("--train-iters", type=int, default=6000)
     ap.add_argument("--max-steps", type=int, default=15000)
     ap.add_argument("--out", default="warmstart_study.json")
+    ap.add_argument("--probe", action="store_true", help="plain relaxation of the buckled family only")
+    ap.add_argument("--level", type=int, default=LEVEL)
+    ap.add_argument("--shells", type=int, default=32)
     a = ap.parse_args(argv)
+    if a.probe:
+        r = probe(n=a.shells, level=a.level, max_steps=a.max_steps, log=lambda m: print(m, flush=True))
+        with open(a.out, "w") as f:
+            json.dump(_jsonable(r), f, indent=1)
+        return
     t0 = time.perf_counter()
     r = experiment(n_train=a.train, n_test=a.test, seed=a.seed, batch_size=512, train_iters=a.train_iters,
                    max_steps=a.max_steps, log=lambda m: print("[%.0f s] %s" % (time.perf_counter() - t0, m),
