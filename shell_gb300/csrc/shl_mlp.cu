@@ -10,9 +10,10 @@
 //   forward        Z  = H_prev . W^T        (A = H_prev,  B = W)
 //   input grad     dH = dZ . W              (A = dZ,      B = W^T)
 //   weight grad    dW = dZ^T . H_prev       (A = dZ^T,    B = H_prev^T)
-// The GEMM (k_gemm_tc) runs on the tcgen05 tensor cores: TMA loads of 128 x 64
-// operand tiles into a four-stage shared-memory ring, tcgen05.mma with the
-// accumulator in tensor memory, tcgen05.ld for the epilogue.  Split-K writes
+// The GEMM (k_gemm_tc) runs on the tcgen05 tensor cores: a persistent,
+// warp-specialised kernel with TMA loads into a four-stage shared-memory ring,
+// tcgen05.mma into two tensor-memory accumulators and a tcgen05.ld epilogue
+// that overlaps the next tile's products.  Split-K writes
 // FP32 partials that one fixed-order kernel sums, so every result is
 // deterministic.
 //
@@ -40,22 +41,30 @@
 namespace {
 
 // ---- the BF16 GEMM on the fifth-generation tensor cores ----
-// C[M,N] = A[M,K] . B[N,K]^T, both operands K-contiguous.  One CTA of four
-// warps per 128 x 128 output tile: thread 0 streams 128 x 64 tiles of A and B
-// into a four-stage shared-memory ring with TMA (128-byte swizzle, zero fill
-// past the matrix edges), thread 32 issues tcgen05.mma (M 128, N 128, K 16;
-// BF16 operands read from shared memory through matrix descriptors, FP32
-// accumulator in tensor memory) and releases each stage with tcgen05.commit,
-// and after the last K block all four warps read their 32 accumulator lanes
-// (rows) with tcgen05.ld for the epilogue.  Every wait on an mbarrier is
-// bounded in time: on expiry the kernel records an error, waits (bounded) for
-// its copies and products in flight, frees its tensor memory and returns.
-constexpr int kBM = 128, kBN = 128, kBK = 64;  // kBK bf16 = 128 bytes: one swizzle row
+// C[M,N] = A[M,K] . B[N,K]^T, both operands K-contiguous, 128 x 256 output
+// tiles.  A persistent grid (one CTA per SM) takes the tiles in turn; each CTA
+// has six warps with fixed roles:
+//   warp 0     one thread streams 128 x 64 tiles of A and 256 x 64 tiles of B
+//              into a four-stage shared-memory ring with TMA (128-byte swizzle,
+//              zero fill past the matrix edges);
+//   warp 1     owns the tensor memory (two 256-column FP32 accumulators) and one
+//              thread issues tcgen05.mma (M 128, N 256, K 16; BF16 operands read
+//              from shared memory through matrix descriptors), releasing each
+//              stage with tcgen05.commit and signalling a finished accumulator;
+//   warps 2-5  the epilogue: each reads its 32 accumulator lanes (rows) with
+//              tcgen05.ld, adds the bias (and GELU), stores, and hands the
+//              accumulator back, so the next tile's products overlap it.
+// Every wait on an mbarrier is bounded in time: on expiry the kernel records an
+// error, stops its loops, waits (bounded) for its copies and products in flight,
+// frees its tensor memory and returns.
+constexpr int kBM = 128, kBN = 256, kBK = 64;  // kBK bf16 = 128 bytes: one swizzle row
 constexpr int kStages = 4;
-constexpr int kGemmThreads = 128;
-constexpr int kTileBytes = kBM * kBK * 2;      // 16 KB per operand tile
-constexpr int kGemmSmem = kStages * 2 * kTileBytes + 1024;
-constexpr uint32_t kTmemCols = 128;            // FP32 accumulator: 128 lanes x 128 columns
+constexpr int kGemmThreads = 192;
+constexpr int kTileA = kBM * kBK * 2;          // 16 KB
+constexpr int kTileB = kBN * kBK * 2;          // 32 KB
+constexpr int kStageBytes = kTileA + kTileB;
+constexpr int kGemmSmem = kStages * kStageBytes + 1024;
+constexpr uint32_t kTmemCols = 512;            // two FP32 accumulators of 128 lanes x 256 columns
 constexpr uint64_t kWaitNs = 2000000000ull;    // a wait gives up after 2 s
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -92,6 +101,17 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatil
   }
 }
 
+// bounded wait that ignores the abort flag (the drain after an abort)
+__device__ __forceinline__ void mbar_drain(uint32_t bar, uint32_t parity) {
+  const uint64_t t0 = globaltimer();
+  while (!mbar_test(bar, parity) && globaltimer() - t0 < kWaitNs) {
+  }
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
 __device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
 }
@@ -115,7 +135,7 @@ __device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t addr) {
   return d;
 }
 
-// instruction descriptor of kind::f16: FP32 accumulator, BF16 A and B, both K-major, M 128, N 128
+// instruction descriptor of kind::f16: FP32 accumulator, BF16 A and B, both K-major, M 128, N 256
 constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kBN >> 3) << 17) |
                             ((uint32_t)(kBM >> 4) << 24);
 
@@ -158,7 +178,8 @@ enum { EPI_PARTIAL = 0, EPI_BIAS = 1, EPI_BIAS_GELU = 2 };
 
 struct GemmArgs {
   int M, N, K;
-  int kb_per_split;        // K blocks (kBK wide) per split-K slice (blockIdx.z)
+  int kb_per_split;        // K blocks (kBK wide) per split-K slice
+  int gx, gy, splits;      // tiles along N, along M, K slices
   int mode;
   const float* bias;       // N (EPI_BIAS*)
   float* C;                // M x N fp32 (ldc) ; EPI_PARTIAL: split z writes C + z*M*ldc
@@ -167,32 +188,50 @@ struct GemmArgs {
   int* error;              // set to 1 when a wait gave up
 };
 
+// tile t of the persistent schedule: N block fastest, then M block, then K slice
+struct TileCoord {
+  int m0, n0, kb0, nkb, z;
+};
+__device__ __forceinline__ TileCoord tile_coord(const GemmArgs& g, int t) {
+  TileCoord c;
+  const int per_z = g.gx * g.gy;
+  c.z = t / per_z;
+  const int r = t - c.z * per_z;
+  c.m0 = (r / g.gx) * kBM;
+  c.n0 = (r % g.gx) * kBN;
+  const int kb_total = (g.K + kBK - 1) / kBK;
+  c.kb0 = c.z * g.kb_per_split;
+  c.nkb = max(0, min(g.kb_per_split, kb_total - c.kb0));
+  return c;
+}
+
 __global__ void __launch_bounds__(kGemmThreads, 1)
     k_gemm_tc(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b, GemmArgs g) {
   extern __shared__ uint8_t smem_raw[];
-  __shared__ __align__(8) uint64_t full_bar[kStages], empty_bar[kStages], acc_bar;
+  __shared__ __align__(8) uint64_t full_bar[kStages], empty_bar[kStages], tfull_bar[2], tempty_bar[2], done_bar;
   __shared__ uint32_t tmem_base;
   __shared__ int abort_flag;
-  __shared__ int issued[kStages];  // K blocks loaded into each stage (for the drain after an abort)
+  __shared__ int loads_issued;  // stage loads issued by the producer (for the drain after an abort)
   const uint32_t base = (smem_u32(smem_raw) + 1023u) & ~1023u;  // swizzled tiles start on 1024 bytes
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int m0 = blockIdx.y * kBM, n0 = blockIdx.x * kBN;
-  const int kb_total = (g.K + kBK - 1) / kBK;
-  const int kb0 = blockIdx.z * g.kb_per_split;
-  const int nkb = max(0, min(g.kb_per_split, kb_total - kb0));
+  const int n_tiles = g.gx * g.gy * g.splits;
   volatile int* abort = &abort_flag;
   if (threadIdx.x == 0) {
     for (int s = 0; s < kStages; ++s) {
       mbar_init(smem_u32(&full_bar[s]), 1);
       mbar_init(smem_u32(&empty_bar[s]), 1);
-      issued[s] = 0;
     }
-    mbar_init(smem_u32(&acc_bar), 1);
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(smem_u32(&tfull_bar[b]), 1);
+      mbar_init(smem_u32(&tempty_bar[b]), 4);  // one arrival per epilogue warp
+    }
+    mbar_init(smem_u32(&done_bar), 1);
     abort_flag = 0;
+    loads_issued = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   }
-  if (warp == 0) {
+  if (warp == 1) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
                  "r"(kTmemCols));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
@@ -201,91 +240,133 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = tmem_base;
-  bool mma_done = true;
-  if (nkb > 0) {
-    if (threadIdx.x == 0) {  // TMA producer
-      for (int kb = 0; kb < nkb; ++kb) {
-        const int s = kb % kStages;
-        const uint32_t ph = (uint32_t)(kb / kStages) & 1u;
-        if (!mbar_wait(smem_u32(&empty_bar[s]), ph ^ 1u, abort)) {
-          *abort = 1;
-          break;
+
+  if (warp == 0) {
+    if (lane == 0) {  // TMA producer
+      int it = 0;
+      for (int t = blockIdx.x; t < n_tiles && !*abort; t += gridDim.x) {
+        const TileCoord c = tile_coord(g, t);
+        for (int kb = 0; kb < c.nkb; ++kb, ++it) {
+          const int s = it % kStages;
+          const uint32_t ph = (uint32_t)(it / kStages) & 1u;
+          if (!mbar_wait(smem_u32(&empty_bar[s]), ph ^ 1u, abort)) {
+            *abort = 1;
+            break;
+          }
+          const uint32_t fb = smem_u32(&full_bar[s]);
+          mbar_expect_tx(fb, kStageBytes);
+          const int kx = (c.kb0 + kb) * kBK;
+          tma_load_2d(base + (uint32_t)s * kStageBytes, &map_a, kx, c.m0, fb);
+          tma_load_2d(base + (uint32_t)s * kStageBytes + kTileA, &map_b, kx, c.n0, fb);
+          loads_issued = it + 1;
         }
-        const uint32_t fb = smem_u32(&full_bar[s]);
-        mbar_expect_tx(fb, 2 * kTileBytes);
-        const int kx = (kb0 + kb) * kBK;
-        tma_load_2d(base + (uint32_t)s * 2 * kTileBytes, &map_a, kx, m0, fb);
-        tma_load_2d(base + (uint32_t)s * 2 * kTileBytes + kTileBytes, &map_b, kx, n0, fb);
-        issued[s] += 1;
       }
-    } else if (threadIdx.x == 32) {  // MMA issuer
-      for (int kb = 0; kb < nkb; ++kb) {
-        const int s = kb % kStages;
-        const uint32_t ph = (uint32_t)(kb / kStages) & 1u;
-        if (!mbar_wait(smem_u32(&full_bar[s]), ph, abort)) {
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {  // MMA issuer
+      int it = 0, tl = 0;
+      for (int t = blockIdx.x; t < n_tiles && !*abort; t += gridDim.x, ++tl) {
+        const TileCoord c = tile_coord(g, t);
+        const int acc = tl & 1;
+        const uint32_t aph = (uint32_t)(tl >> 1) & 1u;
+        if (!mbar_wait(smem_u32(&tempty_bar[acc]), aph ^ 1u, abort)) {
           *abort = 1;
           break;
         }
         tc_fence_after();
-        const uint32_t a_addr = base + (uint32_t)s * 2 * kTileBytes, b_addr = a_addr + kTileBytes;
-#pragma unroll
-        for (int k = 0; k < kBK / 16; ++k)  // K 16 per product: 32 bytes further along the swizzled rows
-          tc_mma(tmem, smem_desc_sw128(a_addr + 32u * k), smem_desc_sw128(b_addr + 32u * k), (kb | k) != 0 ? 1u : 0u);
-        tc_commit(smem_u32(&empty_bar[s]));
-      }
-      tc_commit(smem_u32(&acc_bar));  // completes once every product issued above has
-    }
-    __syncwarp();
-    // every thread: the accumulator is complete (bounded)
-    mma_done = mbar_wait(smem_u32(&acc_bar), 0u, abort);
-    if (!mma_done) *abort = 1;
-  }
-  tc_fence_after();
-  __syncthreads();
-  const bool failed = *abort != 0;
-  if (failed) {
-    if (threadIdx.x == 0) {
-      atomicExch(g.error, 1);
-      // drain: the last load issued into each stage lands (bounded) before the CTA's shared memory is released
-      for (int s = 0; s < kStages; ++s)
-        if (issued[s] > 0) {
-          const uint64_t t0 = globaltimer();
-          while (!mbar_test(smem_u32(&full_bar[s]), (uint32_t)(issued[s] - 1) & 1u) && globaltimer() - t0 < kWaitNs) {
+        const uint32_t d = tmem + (uint32_t)(acc * kBN);
+        bool ok = true;
+        for (int kb = 0; kb < c.nkb; ++kb, ++it) {
+          const int s = it % kStages;
+          const uint32_t ph = (uint32_t)(it / kStages) & 1u;
+          if (!mbar_wait(smem_u32(&full_bar[s]), ph, abort)) {
+            ok = false;
+            break;
           }
+          tc_fence_after();
+          const uint32_t a_addr = base + (uint32_t)s * kStageBytes, b_addr = a_addr + kTileA;
+#pragma unroll
+          for (int k = 0; k < kBK / 16; ++k)  // K 16 per product: 32 bytes further along the swizzled rows
+            tc_mma(d, smem_desc_sw128(a_addr + 32u * k), smem_desc_sw128(b_addr + 32u * k),
+                   (kb | k) != 0 ? 1u : 0u);
+          tc_commit(smem_u32(&empty_bar[s]));
         }
-      const uint64_t t0 = globaltimer();
-      while (nkb > 0 && !mbar_test(smem_u32(&acc_bar), 0u) && globaltimer() - t0 < kWaitNs) {
+        if (!ok) {
+          *abort = 1;
+          break;
+        }
+        if (c.nkb > 0)
+          tc_commit(smem_u32(&tfull_bar[acc]));  // arrives once the tile's products are complete
+        else
+          mbar_arrive(smem_u32(&tfull_bar[acc]));  // an empty K range: the epilogue writes zeros
       }
+      tc_commit(smem_u32(&done_bar));  // every product this thread issued has completed
     }
-  } else {
-    // epilogue: warp w holds rows m0 + 32 w .. + 31 (accumulator lanes), 16 columns per load
-    const int row = m0 + warp * 32 + lane;
-    float* C = g.C + (g.mode == EPI_PARTIAL ? (size_t)blockIdx.z * g.M * g.ldc : 0);
+  } else {  // epilogue warps 2-5: accumulator lanes 32 (warp % 4) .. + 31
+    const int q = warp & 3;
+    int tl = 0;
+    for (int t = blockIdx.x; t < n_tiles && !*abort; t += gridDim.x, ++tl) {
+      const TileCoord c = tile_coord(g, t);
+      const int acc = tl & 1;
+      const uint32_t aph = (uint32_t)(tl >> 1) & 1u;
+      if (!mbar_wait(smem_u32(&tfull_bar[acc]), aph, abort)) {
+        *abort = 1;
+        break;
+      }
+      tc_fence_after();
+      const int row = c.m0 + q * 32 + lane;
+      float* C = g.C + (g.mode == EPI_PARTIAL ? (size_t)c.z * g.M * g.ldc : 0);
+      const bool vec = (g.ldc & 3) == 0;
 #pragma unroll 1
-    for (int c = 0; c < kBN; c += 16) {
-      float v[16];
-      if (nkb > 0) {
-        tc_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c, v);
-      } else {
+      for (int col0 = 0; col0 < kBN; col0 += 16) {
+        if (c.n0 + col0 >= g.N) break;  // warp-uniform
+        float v[16];
+        if (c.nkb > 0) {
+          tc_ld16(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(acc * kBN + col0), v);
+        } else {
 #pragma unroll
-        for (int i = 0; i < 16; ++i) v[i] = 0.f;
-      }
-      if (row >= g.M) continue;
+          for (int i = 0; i < 16; ++i) v[i] = 0.f;
+        }
+        if (row >= g.M) continue;
+        const int cb = c.n0 + col0;
+        if (g.mode != EPI_PARTIAL) {
 #pragma unroll
-      for (int i = 0; i < 16; ++i) {
-        const int col = n0 + c + i;
-        if (col >= g.N) break;
-        float x = v[i];
-        if (g.mode != EPI_PARTIAL) x += g.bias[col];
-        const size_t o = (size_t)row * g.ldc + col;
-        C[o] = x;
-        if (g.Cb) g.Cb[o] = __float2bfloat16_rn(g.mode == EPI_BIAS_GELU ? gelu(x) : x);
+          for (int i = 0; i < 16; ++i)
+            if (cb + i < g.N) v[i] += g.bias[cb + i];
+        }
+        const size_t o = (size_t)row * g.ldc + cb;
+        if (vec && cb + 16 <= g.N) {
+#pragma unroll
+          for (int i = 0; i < 16; i += 4) *reinterpret_cast<float4*>(C + o + i) = make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]);
+        } else {
+#pragma unroll
+          for (int i = 0; i < 16; ++i)
+            if (cb + i < g.N) C[o + i] = v[i];
+        }
+        if (g.Cb) {
+#pragma unroll
+          for (int i = 0; i < 16; ++i)
+            if (cb + i < g.N) g.Cb[o + i] = __float2bfloat16_rn(g.mode == EPI_BIAS_GELU ? gelu(v[i]) : v[i]);
+        }
       }
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(smem_u32(&tempty_bar[acc]));
     }
   }
+  __syncwarp();
+  if (threadIdx.x == 32) mbar_drain(smem_u32(&done_bar), 0u);  // no product in flight past this point
   tc_fence_before();
   __syncthreads();
-  if (warp == 0) {
+  if (*abort && threadIdx.x == 0) {
+    atomicExch(g.error, 1);
+    // every load issued lands before the CTA's shared memory is released
+    const int n = loads_issued;
+    for (int it = max(0, n - kStages); it < n; ++it)
+      mbar_drain(smem_u32(&full_bar[it % kStages]), (uint32_t)(it / kStages) & 1u);
+  }
+  __syncthreads();
+  if (warp == 1) {
     tc_fence_after();
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols));
   }
@@ -495,8 +576,8 @@ PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
 }
 
 // TMA map of a K-contiguous BF16 operand (rows x K, row stride ld elements):
-// 64 x 128 boxes with the 128-byte swizzle, zeros past the edges
-shl_status operand_map(CUtensorMap* map, const __nv_bfloat16* ptr, int rows, int K, int ld) {
+// 64 x box_rows boxes with the 128-byte swizzle, zeros past the edges
+shl_status operand_map(CUtensorMap* map, const __nv_bfloat16* ptr, int rows, int K, int ld, int box_rows) {
   PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
   if (!enc) {
     shl::set_error("cuTensorMapEncodeTiled is not available from the driver");
@@ -508,7 +589,7 @@ shl_status operand_map(CUtensorMap* map, const __nv_bfloat16* ptr, int rows, int
   }
   const cuuint64_t dims[2] = {(cuuint64_t)K, (cuuint64_t)rows};
   const cuuint64_t strides[1] = {(cuuint64_t)ld * 2};
-  const cuuint32_t box[2] = {(cuuint32_t)kBK, (cuuint32_t)kBM};
+  const cuuint32_t box[2] = {(cuuint32_t)kBK, (cuuint32_t)box_rows};
   const cuuint32_t es[2] = {1, 1};
   const CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<__nv_bfloat16*>(ptr), dims, strides, box,
                          es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
@@ -527,32 +608,32 @@ cudaError_t gemm_kernel_attributes() {
 }
 
 // C[M,N] = A[M,K] . B[N,K]^T with the chosen epilogue.  Products without an
-// epilogue split K when the output grid alone would leave SMs idle.
+// epilogue split K when the output tiles alone would leave SMs idle.
 shl_status gemm(shl_mlp* m, const __nv_bfloat16* A, int lda, const __nv_bfloat16* B, int ldb, int M, int N, int K,
                 int mode, const float* bias, float* C, __nv_bfloat16* Cb) {
   MLP_TRY(gemm_kernel_attributes());
+  int dev = 0, sms = 0;
+  MLP_TRY(cudaGetDevice(&dev));
+  MLP_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   CUtensorMap ma, mb;
-  MLP_CHECK(operand_map(&ma, A, M, K, lda));
-  MLP_CHECK(operand_map(&mb, B, N, K, ldb));
+  MLP_CHECK(operand_map(&ma, A, M, K, lda, kBM));
+  MLP_CHECK(operand_map(&mb, B, N, K, ldb, kBN));
   const int gx = (N + kBN - 1) / kBN, gy = (M + kBM - 1) / kBM;
   const int k_blocks = (K + kBK - 1) / kBK;
   int splits = 1;
   if (mode == EPI_PARTIAL)
-    while (gx * gy * splits < 2 * 152 && k_blocks / (splits * 2) >= 4 &&
-           (size_t)(splits * 2) * M * N <= m->part_elems)
+    while (gx * gy * splits < sms && k_blocks / (splits * 2) >= 4 && (size_t)(splits * 2) * M * N <= m->part_elems)
       splits *= 2;
-  GemmArgs g{M, N, K, k_blocks, mode, bias, C, N, Cb, m->gemm_err};
-  if (splits == 1) {
-    k_gemm_tc<<<dim3(gx, gy, 1), kGemmThreads, kGemmSmem, m->stream>>>(ma, mb, g);
-    return SHL_OK;
-  }
   const int per = (k_blocks + splits - 1) / splits;
-  g.kb_per_split = per;
-  splits = (k_blocks + per - 1) / per;
-  g.C = m->part;
-  g.Cb = nullptr;
-  k_gemm_tc<<<dim3(gx, gy, splits), kGemmThreads, kGemmSmem, m->stream>>>(ma, mb, g);
-  k_splitk_reduce<<<592, 256, 0, m->stream>>>(m->part, splits, (size_t)M * N, C, Cb);
+  splits = std::max(1, (k_blocks + per - 1) / per);
+  GemmArgs g{M, N, K, per, gx, gy, splits, mode, bias, C, N, Cb, m->gemm_err};
+  if (splits > 1) {
+    g.C = m->part;
+    g.Cb = nullptr;
+  }
+  const int tiles = gx * gy * splits;
+  k_gemm_tc<<<std::min(tiles, sms), kGemmThreads, kGemmSmem, m->stream>>>(ma, mb, g);
+  if (splits > 1) k_splitk_reduce<<<592, 256, 0, m->stream>>>(m->part, splits, (size_t)M * N, C, Cb);
   return SHL_OK;
 }
 
