@@ -7,6 +7,7 @@
 //
 //   k_rb_aabb      per-face AABBs, shell bounds, avg_elem_size (fixed-order
 //                  sum), cell size, d_max, cell counts; TOO_MANY_CELLS check
+//                  (k_rb_grids and k_rb_grid_scan per shell for a batch)
 //   k_rb_clear     clear the cell histogram and the per-face counters
 //   k_rb_count     cell ranges per face, cell histogram (counting sort, pass 1);
 //                  keep flags of the old list (ShellSystem.C:2016-2027)
@@ -82,6 +83,27 @@ __device__ __forceinline__ GridView grid_of(const DevBuf& b, const StepConst& sc
 // face f takes part in the current pass (a batch rebuilds only the shells whose trigger fired)
 __device__ __forceinline__ bool face_in_pass(const DevBuf& b, const StepConst& sc, uint32_t f) {
   return sc.n_cs == 0 || b.shc[b.face_shell[f]].rebuild != 0;
+}
+
+// The lane sums of the fixed-order sum (shl_geom.h) of x[0..n): lane l adds
+// x[l], x[l + LANES], ... in index order into lanes[l].  Each thread carries
+// its LANES / blockDim lanes together so that the loads of several rounds are
+// in flight at once; the additions of every lane keep their order.
+template <int PER>
+__device__ __forceinline__ void lane_sums(const double* x, uint32_t n, double* lanes) {
+  double acc[PER];
+#pragma unroll
+  for (int k = 0; k < PER; ++k) acc[k] = 0.0;
+#pragma unroll 4
+  for (uint32_t i0 = 0; i0 < n; i0 += SHL_SUM_LANES) {
+#pragma unroll
+    for (int k = 0; k < PER; ++k) {
+      const uint32_t i = i0 + threadIdx.x + (uint32_t)k * blockDim.x;
+      if (i < n) acc[k] = __dadd_rn(acc[k], __ldcg(&x[i]));
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < PER; ++k) lanes[threadIdx.x + (uint32_t)k * blockDim.x] = acc[k];
 }
 
 // Cell size, d_max and cell counts of a shell from its bounds and average
@@ -176,11 +198,7 @@ __global__ void __launch_bounds__(kBlock) k_rb_aabb(DevBuf b, StepConst sc) {
     __syncthreads();
   }
   // avg_elem_size: the fixed-order sum of shl_geom.h (1024 lanes, then a tree)
-  for (uint32_t l = threadIdx.x; l < SHL_SUM_LANES; l += blockDim.x) {
-    double s = 0.0;
-    for (uint32_t i = l; i < sc.F; i += SHL_SUM_LANES) s = __dadd_rn(s, __ldcg(&b.fsize[i]));
-    lanes[l] = s;
-  }
+  lane_sums<SHL_SUM_LANES / kBlock>(b.fsize, sc.F, lanes);
   __syncthreads();
   for (uint32_t st = SHL_SUM_LANES / 2; st > 0; st >>= 1) {
     for (uint32_t l = threadIdx.x; l < st; l += blockDim.x) lanes[l] = __dadd_rn(lanes[l], lanes[l + st]);
@@ -238,11 +256,7 @@ __global__ void __launch_bounds__(kBlock) k_rb_grids(DevBuf b, StepConst sc) {
     sh_min[c][threadIdx.x] = lo[c];
     sh_max[c][threadIdx.x] = hi[c];
   }
-  for (uint32_t l = threadIdx.x; l < SHL_SUM_LANES; l += blockDim.x) {
-    double s = 0.0;
-    for (uint32_t i = l; i < nf; i += SHL_SUM_LANES) s = __dadd_rn(s, b.fsize[f0 + i]);
-    lanes[l] = s;
-  }
+  lane_sums<SHL_SUM_LANES / kBlock>(b.fsize + f0, nf, lanes);
   __syncthreads();
   for (int st = blockDim.x / 2; st > 0; st >>= 1) {
     if ((int)threadIdx.x < st)
@@ -537,36 +551,77 @@ __device__ __forceinline__ uint32_t sorted_find(const uint32_t* a, uint32_t lo, 
 }
 
 // ---------------------------------------------------------------- pairs --
-// Conservative separating-axis test along the line of centroids, in FP32 on
-// FP32 copies of the positions: true only when the triangles are certainly
-// farther apart than d_max.  The bound on the rounding error of the FP32
-// projections (including the rounding of the positions to FP32) is
-// 32 eps32 |d| S with S the largest coordinate magnitude, and the remaining
-// relative margin (1e-5) is far above the rounding of the FP64 closest-point
-// solve, so the test never removes a pair that the exact path would accept
-// (or that the AABB test would keep and the closest-point test accept).
-__device__ __forceinline__ bool certainly_apart32(const float* const* P1, const float* const* P2, float d_max) {
-  float d[3], S = 0.f;
+// Conservative separating-axis tests in FP32 on FP32 copies of the positions:
+// true only when the triangles are certainly farther apart than d_max.  For an
+// axis a (any vector, unnormalised, |a| = L) the projections of the two
+// triangles onto a are separated by more than d_max L, allowing for the
+// rounding of the FP32 projections (including the rounding of the positions to
+// FP32): at most 32 eps32 L S with S the largest coordinate magnitude.  The
+// remaining relative margin (1e-5) is far above the rounding of the FP64
+// closest-point solve, so a pair rejected here is one the exact path would
+// reject too (d^2 > d_max^2).  The axes: the line of centroids, the two face
+// normals and the in-plane normals of the six edges (n x e), which separate
+// neighbouring, nearly coplanar faces of a smooth surface.
+__device__ __forceinline__ bool apart_on_axis(const float* a, const float* const* P1, const float* const* P2,
+                                              float d_max, float S) {
+  const float L2 = a[0] * a[0] + a[1] * a[1] + a[2] * a[2];
+  if (!(L2 > 0.f)) return false;
+  float mn1 = 3.0e38f, mx1 = -3.0e38f, mn2 = 3.0e38f, mx2 = -3.0e38f;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const float q1 = a[0] * P1[k][0] + a[1] * P1[k][1] + a[2] * P1[k][2];
+    const float q2 = a[0] * P2[k][0] + a[1] * P2[k][1] + a[2] * P2[k][2];
+    mn1 = fminf(mn1, q1);
+    mx1 = fmaxf(mx1, q1);
+    mn2 = fminf(mn2, q2);
+    mx2 = fmaxf(mx2, q2);
+  }
+  const float L = sqrtf(L2);
+  const float gap = fmaxf(mn2 - mx1, mn1 - mx2) - 32.f * 5.9604645e-8f * L * S;
+  return gap > d_max * L * (1.f + 1e-5f);
+}
+
+// the line of centroids (S: the largest coordinate magnitude, for the next test)
+__device__ __forceinline__ bool apart_centroids32(const float* const* P1, const float* const* P2, float d_max,
+                                                  float& S) {
+  float d[3];
+  S = 0.f;
   for (int c = 0; c < 3; ++c) {
     d[c] = (P2[0][c] + P2[1][c] + P2[2][c]) - (P1[0][c] + P1[1][c] + P1[2][c]);
     for (int k = 0; k < 3; ++k) S = fmaxf(S, fmaxf(fabsf(P1[k][c]), fabsf(P2[k][c])));
   }
-  const float L2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
-  if (!(L2 > 0.f)) return false;
-  float mx1 = -3.0e38f, mn2 = 3.0e38f;
-  for (int k = 0; k < 3; ++k) {
-    mx1 = fmaxf(mx1, d[0] * P1[k][0] + d[1] * P1[k][1] + d[2] * P1[k][2]);
-    mn2 = fminf(mn2, d[0] * P2[k][0] + d[1] * P2[k][1] + d[2] * P2[k][2]);
+  return apart_on_axis(d, P1, P2, d_max, S);
+}
+
+// the face normals and the in-plane edge normals
+__device__ __forceinline__ bool apart_faces32(const float* const* P1, const float* const* P2, float d_max, float S) {
+  const float* const* T[2] = {P1, P2};
+#pragma unroll
+  for (int t = 0; t < 2; ++t) {
+    const float* const* P = T[t];
+    float e[3][3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) e[k][c] = P[(k + 1) % 3][c] - P[k][c];
+    const float n[3] = {e[0][1] * e[2][2] - e[0][2] * e[2][1], e[0][2] * e[2][0] - e[0][0] * e[2][2],
+                        e[0][0] * e[2][1] - e[0][1] * e[2][0]};
+    if (apart_on_axis(n, P1, P2, d_max, S)) return true;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const float m[3] = {n[1] * e[k][2] - n[2] * e[k][1], n[2] * e[k][0] - n[0] * e[k][2],
+                          n[0] * e[k][1] - n[1] * e[k][0]};
+      if (apart_on_axis(m, P1, P2, d_max, S)) return true;
+    }
   }
-  const float L = sqrtf(L2);
-  const float gap = (mn2 - mx1) - 32.f * 5.9604645e-8f * L * S;
-  return gap > d_max * L * (1.f + 1e-5f);
+  return false;
 }
 
 // Candidate pairs of one (cell, face) entry: faces e2 > e1 in the cell, emitted
 // from the lowest shared cell only, not topologically close, not in the kept
 // list, not AABB-apart by d_max (ShellSystem.C:2047-2060), and not certainly
-// apart.  Buffered per thread, appended with one atomic per flush.
+// apart by the separating-axis tests.  Buffered per thread, appended with one
+// atomic per flush.
 __global__ void __launch_bounds__(kBlock) k_rb_cand(DevBuf b, StepConst sc) {
   Ctl* ctl = b.ctl;
   if (rb_off(ctl)) return;
@@ -603,32 +658,44 @@ __global__ void __launch_bounds__(kBlock) k_rb_cand(DevBuf b, StepConst sc) {
     const uint32_t o0 = b.pair_ptr[0][e1], o1 = b.pair_ptr[0][e1 + 1];
     double mn1[3], mx1[3];
     const float* Q1[3];
+    uint32_t t1[3];
     for (int c = 0; c < 3; ++c) {
       mn1[c] = b.bmin[3 * (size_t)e1 + c];
       mx1[c] = b.bmax[3 * (size_t)e1 + c];
-      Q1[c] = b.p32 + 3 * (size_t)b.tri[3 * (size_t)e1 + c];
+      t1[c] = b.tri[3 * (size_t)e1 + c];
+      Q1[c] = b.p32 + 3 * (size_t)t1[c];
     }
     const uint32_t s0 = b.cell_start[cell], cnt = b.cell_count[cell];
+    // The filters are conjunctive, so their order leaves the result unchanged;
+    // the cheap and decisive ones come first.
     for (uint32_t k = 0; k < cnt; ++k) {
       const uint32_t e2 = b.cell_items[s0 + k];
       if (e2 <= e1) continue;
       const int* lo2 = b.cell_lo + 3 * (size_t)e2;
       if ((uint32_t)max(l10, lo2[0]) != cx || (uint32_t)max(l11, lo2[1]) != cy || (uint32_t)max(l12, lo2[2]) != cz)
         continue;
-      if (!sc.smooth) {  // a facet bound; SMOOTH distances are between limit surfaces
-        const float* Q2[3];
-        for (int q = 0; q < 3; ++q) Q2[q] = b.p32 + 3 * (size_t)b.tri[3 * (size_t)e2 + q];
-        if (certainly_apart32(Q1, Q2, d_max32)) continue;
-      }
-      if (sorted_contains(b.close_list, c0, c1, e2)) continue;
-      const uint32_t at = sorted_find(b.pe2[0], o0, o1, e2);
-      if (at < o1 && b.pkeep[at]) continue;
+      // faces sharing a node are neighbours in the mesh, always in the close list (ShellSystem.C:657-678)
+      uint32_t t2[3];
+      for (int q = 0; q < 3; ++q) t2[q] = b.tri[3 * (size_t)e2 + q];
+      bool shared = false;
+      for (int q = 0; q < 3; ++q) shared = shared || t2[q] == t1[0] || t2[q] == t1[1] || t2[q] == t1[2];
+      if (shared) continue;
       bool apart = false;
       for (int c = 0; c < 3; ++c) {
         const double mn2 = b.bmin[3 * (size_t)e2 + c], mx2 = b.bmax[3 * (size_t)e2 + c];
         apart = apart || mn1[c] > __dadd_rn(mx2, d_max) || mn2 > __dadd_rn(mx1[c], d_max);
       }
       if (apart) continue;
+      const float* Q2[3];
+      float S = 0.f;
+      if (!sc.smooth) {  // facet bounds; SMOOTH distances are between limit surfaces
+        for (int q = 0; q < 3; ++q) Q2[q] = b.p32 + 3 * (size_t)t2[q];
+        if (apart_centroids32(Q1, Q2, d_max32, S)) continue;
+      }
+      if (sorted_contains(b.close_list, c0, c1, e2)) continue;
+      const uint32_t at = sorted_find(b.pe2[0], o0, o1, e2);
+      if (at < o1 && b.pkeep[at]) continue;
+      if (!sc.smooth && apart_faces32(Q1, Q2, d_max32, S)) continue;
       buf1[nb] = e1;
       buf2[nb] = e2;
       if (++nb == kBuf) flush();
