@@ -587,7 +587,7 @@ shl_status create_common(shl_ctx* c, const std::vector<double>& pscale_orig, shl
   const bool fp32 = params->precision == SHL_PREC_FP32;
   if (fp32) {
     ALLOC(b.qe32, 3 * (size_t)S.n_slots_total);
-    ALLOC(b.up32, nd);
+    ALLOC(b.up32, (size_t)V);
     ALLOC(b.face32, (size_t)F32_COUNT * F);
   } else {
     ALLOC(b.face_df, (size_t)2 * F32_COUNT * F);

@@ -622,7 +622,7 @@ __device__ __forceinline__ bool apart_faces32(const float* const* P1, const floa
 // list, not AABB-apart by d_max (ShellSystem.C:2047-2060), and not certainly
 // apart by the separating-axis tests.  Buffered per thread, appended with one
 // atomic per flush.
-__global__ void __launch_bounds__(kBlock) k_rb_cand(DevBuf b, StepConst sc) {
+__global__ void __launch_bounds__(kBlock, 4) k_rb_cand(DevBuf b, StepConst sc) {
   Ctl* ctl = b.ctl;
   if (rb_off(ctl)) return;
   const uint32_t n_entries = ctl->n_entries;
@@ -692,10 +692,10 @@ __global__ void __launch_bounds__(kBlock) k_rb_cand(DevBuf b, StepConst sc) {
         for (int q = 0; q < 3; ++q) Q2[q] = b.p32 + 3 * (size_t)t2[q];
         if (apart_centroids32(Q1, Q2, d_max32, S)) continue;
       }
+      if (!sc.smooth && apart_faces32(Q1, Q2, d_max32, S)) continue;
       if (sorted_contains(b.close_list, c0, c1, e2)) continue;
       const uint32_t at = sorted_find(b.pe2[0], o0, o1, e2);
       if (at < o1 && b.pkeep[at]) continue;
-      if (!sc.smooth && apart_faces32(Q1, Q2, d_max32, S)) continue;
       buf1[nb] = e1;
       buf2[nb] = e2;
       if (++nb == kBuf) flush();

@@ -223,7 +223,7 @@ struct DevBuf {
   float* face32;      // F32_COUNT * F (FP32 element path)
   float* face_df;     // 2 * F32_COUNT * F: the same constants as float pairs (double-float FP64 path)
   float* qe32;        // 3 per element-force slot, in gather order (FP32 element path)
-  float* up32;        // 3V, FP32 copy of u_pred (FP32 element path)
+  float4* up32;       // V, FP32 copy of u_pred (x, y, z, 0; FP32 element path)
   float4* upk;        // 2V, u_pred as float pairs: [2n] = hi (x, y, z, 0), [2n + 1] = lo (the FP64 path's contractions)
   // element force shares are stored in gather order (node by node, ascending
   // element-force slot): slot_pos maps a (face, slot) to its place, and node n's

@@ -470,7 +470,7 @@ __device__ __forceinline__ double predict_node(const DevBuf& b, const StepConst&
                                                const double* v, const double* a, double dt, double nm8, double nm6,
                                                double* pos) {
   double d[3];
-  float uh[3], ul[3];
+  float uh[3], ul[3], u32[3];
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
     const size_t k = 3 * (size_t)n + c;
@@ -486,14 +486,16 @@ __device__ __forceinline__ double predict_node(const DevBuf& b, const StepConst&
     }
     b.up[k] = up;
     if (sc.fp32)
-      b.up32[k] = (float)up;
+      u32[c] = (float)up;
     else
       df_split(up, uh[c], ul[c]);
     b.vp[k] = vp;
     pos[k] = __dadd_rn(b.X[k], up);
     d[c] = __dsub_rn(up, u[c]);
   }
-  if (!sc.fp32) {
+  if (sc.fp32) {
+    b.up32[n] = make_float4(u32[0], u32[1], u32[2], 0.f);
+  } else {
     b.upk[2 * (size_t)n] = make_float4(uh[0], uh[1], uh[2], 0.f);
     b.upk[2 * (size_t)n + 1] = make_float4(ul[0], ul[1], ul[2], 0.f);
   }
@@ -729,9 +731,11 @@ __global__ void k_positions(DevBuf b, StepConst sc) {
   for (int c = 0; c < 3; ++c) {
     const size_t k = 3 * (size_t)n + c;
     b.p[k] = __dadd_rn(b.X[k], b.up[k]);
-    if (sc.fp32) b.up32[k] = (float)b.up[k];
     df_split(b.up[k], uh[c], ul[c]);
   }
+  if (sc.fp32)
+    b.up32[n] = make_float4((float)b.up[3 * (size_t)n], (float)b.up[3 * (size_t)n + 1], (float)b.up[3 * (size_t)n + 2],
+                            0.f);
   b.upk[2 * (size_t)n] = make_float4(uh[0], uh[1], uh[2], 0.f);
   b.upk[2 * (size_t)n + 1] = make_float4(ul[0], ul[1], ul[2], 0.f);
 }
@@ -976,9 +980,8 @@ __device__ __forceinline__ ElemOut element_force32(uint32_t i, int np_rt, uint32
   for (int s = 0; s < (NP > 0 ? NP : kMaxSlots); ++s) {
     if (NP == 0 && s >= np) break;
     const int nd = __ldg(&b.patch[(size_t)s * F + i]);
-    const float ux = __ldg(&b.up32[3 * (size_t)nd]);
-    const float uy = __ldg(&b.up32[3 * (size_t)nd + 1]);
-    const float uz = __ldg(&b.up32[3 * (size_t)nd + 2]);
+    const float4 un = __ldg(&b.up32[nd]);
+    const float ux = un.x, uy = un.y, uz = un.z;
 #pragma unroll
     for (int k = 0; k < 6; ++k) {
       const float w = B[6 * s + k];
