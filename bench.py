@@ -73,10 +73,10 @@ STEP_BYTES_PER_FACE = 456
 # FP64 flops of one regular face in the element kernel (count of the
 # arithmetic in element_force<12>, fused multiply-add = 2)
 ELEM_FLOPS_PER_FACE = 1372
-# DRAM bytes (read + write) of one element-kernel launch on the level-6 shell,
-# from one ncu --set full capture with caches flushed (38.6 MB read, 3.4 MB
-# written; the force shares stay in the 129 MB L2 for the gather)
-ELEM_TRAFFIC_LEVEL6 = 42.0e6
+# DRAM bytes (read + write) of one launch of the tuned element kernel (the
+# one-round double-float shape, 544 threads per SM) on the level-6 shell, from
+# one ncu --set full capture with caches flushed (46.3 MB read, 15.9 MB written)
+ELEM_TRAFFIC_LEVEL6 = 62.2e6
 # FP32 element path (the ensemble): about 300 algorithmic bytes per face-step with
 # FP32 per-face constants; DRAM bytes of one launch on the 256-shell ensemble and its
 # FP32-pipe utilisation, from one ncu --set full capture (673.4 MB read, 427.0 MB
@@ -87,7 +87,7 @@ ENS_ELEM_FP32_PIPE = 0.129
 # warp instructions of one element-kernel launch on the level-6 shell (ncu
 # smsp__inst_executed.sum of the same capture) and the issue peak: 4 schedulers
 # per SM, one warp instruction per cycle each
-ELEM_WARP_INST_LEVEL6 = 30.0e6
+ELEM_WARP_INST_LEVEL6 = 30.7e6
 ISSUE_PER_SM_PER_CYCLE = 4
 
 

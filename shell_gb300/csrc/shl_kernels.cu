@@ -1734,6 +1734,9 @@ __global__ void __launch_bounds__(kBlock) k_gather_correct(DevBuf b, StepConst s
     }
     if (sc.contact) {
       const uint32_t k0 = b.csr_ptr[n], k1 = b.csr_ptr[n + 1];
+      // unrolled so that the loads of several entries are in flight; the
+      // additions keep the list's order
+#pragma unroll 4
       for (uint32_t k = k0; k < k1; ++k) {
         const uint32_t ent = b.csr_ent[k];
         const uint32_t j = ent >> 3, role = ent & 7u;
