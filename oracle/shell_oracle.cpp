@@ -38,12 +38,17 @@
  * irregular patch (the quadrature point (1/3,1/3) lies in the middle
  * sub-triangle after one step, as in SubdivEvaluation.C:170-187, 110-135).
  *
- * The narrow phase (ShellShellContact::compute, ShellShellContact.C:35-145)
- * and the friction law (Friction::apply, Friction.C:4-60) are restated here
- * on the oracle's own vector type, in the reference's order of operations.
- * The only contact code shared with the library is shl_distance.h: the two
- * closest-point routines that the reference declares but does not ship
- * (Contact.h:22-34, Contact.C missing).
+ * The narrow phase (ShellShellContact::compute, ShellShellContact.C:35-145),
+ * the friction law (Friction::apply, Friction.C:4-60) and the SMOOTH
+ * closest-point search (SmoothShellShellContact.C:16-204, with the minimiser
+ * the reference does not ship restated as the library documents it) are
+ * restated here on the oracle's own code, in the reference's order of
+ * operations.  The only contact code shared with the library is
+ * shl_distance.h: the two closest-point routines that the reference declares
+ * but does not ship (Contact.h:22-34, Contact.C missing); for SMOOTH contact
+ * the limit-surface evaluation (shl_limit.h, SubdivEvaluation.C:14-187) and its
+ * subdivision tables (shl_subdiv.h, the reference's PAnArray) are shared too,
+ * pinned by explicit Loop subdivision in the tests.
  *
  * Build with -ffp-contract=off: every multiply and add is rounded on its own,
  * as the device code does (__dmul_rn/__dadd_rn), so candidate lists agree bit
@@ -66,7 +71,7 @@
 #endif
 
 #include "../shell_gb300/csrc/shl_expr.h"
-#include "../shell_gb300/csrc/shl_smooth.h"
+#include "../shell_gb300/csrc/shl_limit.h"
 #include "../shell_gb300/csrc/shl_subdiv.h"
 #include "../shell_gb300/csrc/shl_distance.h"
 #ifdef SHL_GEOM_H_
@@ -375,6 +380,339 @@ void irregular_stencil(int N, std::vector<double>& S) {
   edge(11, a, nl, b, nl2);
 }
 
+
+/* ------------------------------------------------------------------------
+ * SmoothShellShellContact::compute (SmoothShellShellContact.C:16-60): the
+ * closest points of the limit surfaces of two faces, minimising
+ * f(x) = |p2(v2, w2) - p1(v1, w1)|^2 over x = (v1, w1, v2, w2) subject to
+ * v, w >= 0 and v + w <= 1 per face, from the pair's previous solution.  The
+ * constraint hooks are the reference's: apply_constraints (:155-179),
+ * update_constraint_bitmap (:139-152, activity within 100 eps) and
+ * find_max_alpha (:96-136).  The minimiser (ConstrainedMinimizer.h) is not in
+ * the reference's sources; it is restated here, on the oracle's own code, as
+ * the active-set projected Newton method that the library documents: exact
+ * Hessian from the limit surface's second derivatives, Jacobi-scaled and
+ * shifted by mu I until its Cholesky factor exists on the free subspace of the
+ * working set (multiplier signs of the active constraints), Armijo
+ * backtracking capped by find_max_alpha; stops on a projected gradient below
+ * 1e-9 of the gradient, a Newton decrement below 1e-15 of f, a short full
+ * Newton step (1e-6), a vanishing step (1e-14), a failed line search or 40
+ * iterations.  Only the limit evaluation (shl_limit.h) is shared with the
+ * library.  Every operation is rounded on its own (-ffp-contract=off).
+ * ------------------------------------------------------------------------ */
+namespace smooth {
+
+const double kEps = 2.220446049250313e-16;
+const double kActiveTol = 100 * kEps;
+const int kMaxIt = 40, kMaxHalvings = 30;
+const double kStepTol = 1e-14, kDecrementTol = 1e-15, kQuadTol = 1e-6, kKktTol = 1e-9;
+
+inline double dot(const double* a, const double* b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+
+// apply_constraints: clip to v, w >= 0, then pull the larger coordinate back
+// when v + w exceeds 1
+void apply_constraints(double* x) {
+  for (int i = 0; i < 4; ++i) x[i] = std::fmax(x[i], 0.0);
+  for (int e = 0; e < 2; ++e) {
+    const double u = (1.0 - x[2 * e]) - x[2 * e + 1];
+    if (u < 0.0) {
+      double& big = x[2 * e] > x[2 * e + 1] ? x[2 * e] : x[2 * e + 1];
+      big = big + (u - kEps);
+    }
+  }
+}
+
+// update_constraint_bitmap: bits 0..3 coordinate i at 0, bits 4, 5 v + w at 1
+unsigned bitmap(const double* x) {
+  unsigned m = 0;
+  for (int i = 0; i < 4; ++i)
+    if (x[i] < kActiveTol) m |= 1u << i;
+  if (x[0] + x[1] > 1.0 - kActiveTol) m |= 1u << 4;
+  if (x[2] + x[3] > 1.0 - kActiveTol) m |= 1u << 5;
+  return m;
+}
+
+// find_max_alpha: the longest feasible step along d (the largest double if none limits it)
+double max_alpha(const double* x, const double* d) {
+  double a = std::numeric_limits<double>::max();
+  for (int i = 0; i < 4; ++i)
+    if (d[i] < 0.0) a = std::fmin(a, -x[i] / d[i]);
+  for (int e = 0; e < 2; ++e) {
+    const double ds = d[2 * e] + d[2 * e + 1];
+    if (ds > 0.0) a = std::fmin(a, ((1.0 - x[2 * e]) - x[2 * e + 1]) / ds);
+  }
+  return a;
+}
+
+// the working constraints of one face (1: v = 0, 2: w = 0, 4: v + w = 1) among
+// its active ones, kept where the first-order multiplier is non-negative
+unsigned working(unsigned act, double gv, double gw) {
+  const double mu_v = gv, mu_w = gw, mu_s = -(gv + gw);
+  switch (act) {
+    case 3u:  // corner (0, 0)
+      if (mu_v >= 0.0 && mu_w >= 0.0) return 3u;
+      return mu_v >= 0.0 ? 1u : (mu_w >= 0.0 ? 2u : 0u);
+    case 5u: {  // corner (0, 1): g = a (1, 0) + b (-1, -1)
+      const double a = gv - gw, b = -gw;
+      if (a >= 0.0 && b >= 0.0) return 5u;
+      if (a >= 0.0) return mu_v >= 0.0 ? 1u : 0u;
+      if (b >= 0.0) return mu_s >= 0.0 ? 4u : 0u;
+      return 0u;
+    }
+    case 6u: {  // corner (1, 0): g = a (0, 1) + b (-1, -1)
+      const double a = gw - gv, b = -gv;
+      if (a >= 0.0 && b >= 0.0) return 6u;
+      if (a >= 0.0) return mu_w >= 0.0 ? 2u : 0u;
+      if (b >= 0.0) return mu_s >= 0.0 ? 4u : 0u;
+      return 0u;
+    }
+    case 1u: return mu_v >= 0.0 ? 1u : 0u;
+    case 2u: return mu_w >= 0.0 ? 2u : 0u;
+    case 4u: return mu_s >= 0.0 ? 4u : 0u;
+    default: return 0u;
+  }
+}
+
+// f, its gradient and Hessian at x (limit points and derivatives of both faces)
+double value_grad_hess(const shl_limit_patch* A, const shl_limit_patch* B, const double* x, double* g,
+                       double H[4][4], double* p1, double* p2) {
+  double a[6][3], b[6][3];
+  shl_limit_eval(A, x[0], x[1], 2, a);
+  shl_limit_eval(B, x[2], x[3], 2, b);
+  double r[3], dr[4][3];  // r = p2 - p1 and its derivatives along x
+  for (int c = 0; c < 3; ++c) {
+    r[c] = b[0][c] - a[0][c];
+    dr[0][c] = -a[1][c];
+    dr[1][c] = -a[2][c];
+    dr[2][c] = b[1][c];
+    dr[3][c] = b[2][c];
+    p1[c] = a[0][c];
+    p2[c] = b[0][c];
+  }
+  for (int i = 0; i < 4; ++i) g[i] = 2.0 * dot(r, dr[i]);
+  // r . (second derivatives of r): -p1's within face 1, p2's within face 2
+  const double s00 = -dot(r, a[3]), s11 = -dot(r, a[4]), s01 = -dot(r, a[5]);
+  const double s22 = dot(r, b[3]), s33 = dot(r, b[4]), s23 = dot(r, b[5]);
+  for (int i = 0; i < 4; ++i)
+    for (int j = i; j < 4; ++j) {
+      double h = dot(dr[i], dr[j]);
+      if (i == 0 && j == 0) h = h + s00;
+      if (i == 1 && j == 1) h = h + s11;
+      if (i == 0 && j == 1) h = h + s01;
+      if (i == 2 && j == 2) h = h + s22;
+      if (i == 3 && j == 3) h = h + s33;
+      if (i == 2 && j == 3) h = h + s23;
+      H[i][j] = 2.0 * h;
+      H[j][i] = H[i][j];
+    }
+  return dot(r, r);
+}
+
+double value(const shl_limit_patch* A, const shl_limit_patch* B, const double* x, double* p1, double* p2) {
+  double a[6][3], b[6][3];
+  shl_limit_eval(A, x[0], x[1], 0, a);
+  shl_limit_eval(B, x[2], x[3], 0, b);
+  double r[3];
+  for (int c = 0; c < 3; ++c) {
+    r[c] = b[0][c] - a[0][c];
+    p1[c] = a[0][c];
+    p2[c] = b[0][c];
+  }
+  return dot(r, r);
+}
+
+// Newton direction on the free subspace of the working set; true when the
+// reduced Hessian had to be shifted (f not convex there)
+bool newton_direction(const double* g, double H[4][4], const unsigned* work, double* d) {
+  // basis of the free subspace, face by face
+  double Z[4][4];
+  int m = 0;
+  for (int e = 0; e < 2; ++e) {
+    const int iv = 2 * e, iw = 2 * e + 1;
+    auto push = [&](double zv, double zw) {
+      for (int i = 0; i < 4; ++i) Z[m][i] = 0.0;
+      Z[m][iv] = zv;
+      Z[m][iw] = zw;
+      ++m;
+    };
+    switch (work[e]) {
+      case 0u: push(1.0, 0.0); push(0.0, 1.0); break;
+      case 1u: push(0.0, 1.0); break;   // v = 0: w free
+      case 2u: push(1.0, 0.0); break;   // w = 0: v free
+      case 4u: push(1.0, -1.0); break;  // v + w = 1
+      default: break;
+    }
+  }
+  for (int i = 0; i < 4; ++i) d[i] = 0.0;
+  if (m == 0) return false;
+  double Hz[4][4], rg[4], rh[4][4];
+  for (int a = 0; a < m; ++a) {
+    double s = 0.0;
+    for (int i = 0; i < 4; ++i) s = s + Z[a][i] * g[i];
+    rg[a] = s;
+    for (int i = 0; i < 4; ++i) {
+      double t = 0.0;
+      for (int j = 0; j < 4; ++j) t = t + H[i][j] * Z[a][j];
+      Hz[a][i] = t;
+    }
+  }
+  for (int a = 0; a < m; ++a)
+    for (int c = 0; c < m; ++c) {
+      double s = 0.0;
+      for (int i = 0; i < 4; ++i) s = s + Z[a][i] * Hz[c][i];
+      rh[a][c] = s;
+    }
+  // unit diagonal: the free directions' scales differ by powers of 2 next to an irregular vertex
+  double sc[4];
+  for (int a = 0; a < m; ++a) {
+    const double h = std::fabs(rh[a][a]);
+    sc[a] = h > 0.0 ? 1.0 / std::sqrt(h) : 1.0;
+  }
+  for (int a = 0; a < m; ++a) {
+    rg[a] = sc[a] * rg[a];
+    for (int c = 0; c < m; ++c) rh[a][c] = (sc[a] * rh[a][c]) * sc[c];
+  }
+  double shift = 0.0, L[4][4], y[4];
+  for (int attempt = 0; attempt < 24; ++attempt) {
+    bool factored = true;
+    for (int a = 0; a < m && factored; ++a)
+      for (int c = 0; c <= a; ++c) {
+        double s = rh[a][c];
+        if (a == c) s = s + shift;
+        for (int k = 0; k < c; ++k) s = s - L[a][k] * L[c][k];
+        if (a == c) {
+          if (!(s > 1e-14)) {
+            factored = false;
+            break;
+          }
+          L[a][a] = std::sqrt(s);
+        } else {
+          L[a][c] = s / L[c][c];
+        }
+      }
+    if (factored) {
+      for (int a = 0; a < m; ++a) {  // forward: L y = -rg
+        double s = -rg[a];
+        for (int k = 0; k < a; ++k) s = s - L[a][k] * y[k];
+        y[a] = s / L[a][a];
+      }
+      for (int a = m - 1; a >= 0; --a) {  // backward: L^T y = y
+        double s = y[a];
+        for (int k = a + 1; k < m; ++k) s = s - L[k][a] * y[k];
+        y[a] = s / L[a][a];
+      }
+      for (int i = 0; i < 4; ++i) {
+        double s = 0.0;
+        for (int a = 0; a < m; ++a) s = s + Z[a][i] * (sc[a] * y[a]);
+        d[i] = s;
+      }
+      return shift > 0.0;
+    }
+    shift = shift == 0.0 ? 1e-10 : shift * 10.0;
+  }
+  for (int i = 0; i < 4; ++i) {  // scaled projected steepest descent
+    double s = 0.0;
+    for (int a = 0; a < m; ++a) s = s + Z[a][i] * (sc[a] * -rg[a]);
+    d[i] = s;
+  }
+  return true;
+}
+
+// the closest points of the limit patches A (face 1) and B (face 2) from x;
+// x becomes the minimiser, d2 = |p2 - p1|^2 and dc = p2 - p1
+int closest(const shl_limit_patch* A, const shl_limit_patch* B, double* x, double* d2, double* dc) {
+  apply_constraints(x);
+  double p1[3], p2[3], g[4], H[4][4];
+  double f = value_grad_hess(A, B, x, g, H, p1, p2);
+  int it = 0;
+  for (; it < kMaxIt; ++it) {
+    const unsigned bm = bitmap(x);
+    unsigned act[2], work[2];
+    for (int e = 0; e < 2; ++e) {
+      act[e] = ((bm >> (2 * e)) & 1u) | (((bm >> (2 * e + 1)) & 1u) << 1) | (((bm >> (4 + e)) & 1u) << 2);
+      work[e] = working(act[e], g[2 * e], g[2 * e + 1]);
+    }
+    // first-order optimality on the working set
+    double pg = 0.0, gmax = 0.0;
+    for (int e = 0; e < 2; ++e) {
+      const double gv = g[2 * e], gw = g[2 * e + 1];
+      gmax = std::fmax(gmax, std::fmax(std::fabs(gv), std::fabs(gw)));
+      switch (work[e]) {
+        case 0u: pg = std::fmax(pg, std::fmax(std::fabs(gv), std::fabs(gw))); break;
+        case 1u: pg = std::fmax(pg, std::fabs(gw)); break;
+        case 2u: pg = std::fmax(pg, std::fabs(gv)); break;
+        case 4u: pg = std::fmax(pg, 0.5 * std::fabs(gv - gw)); break;
+        default: break;
+      }
+    }
+    if (pg <= kKktTol * gmax) break;
+    double d[4];
+    bool shifted = false;
+    // a constraint left out of the working set must not be violated by the step:
+    // each round adds one back
+    for (int round = 0; round < 6; ++round) {
+      shifted = newton_direction(g, H, work, d);
+      bool added = false;
+      for (int e = 0; e < 2; ++e) {
+        const unsigned freed = act[e] & ~work[e];
+        unsigned add = 0;
+        if ((freed & 1u) && d[2 * e] < 0.0) add |= 1u;
+        if ((freed & 2u) && d[2 * e + 1] < 0.0) add |= 2u;
+        if ((freed & 4u) && d[2 * e] + d[2 * e + 1] > 0.0) add |= 4u;
+        if (add) {
+          work[e] |= add;
+          added = true;
+        }
+      }
+      if (!added) break;
+    }
+    double dmax = 0.0, gd = 0.0;
+    for (int i = 0; i < 4; ++i) {
+      dmax = std::fmax(dmax, std::fabs(d[i]));
+      gd = gd + g[i] * d[i];
+    }
+    if (!(dmax > 0.0) || !(gd < 0.0) || -gd <= kDecrementTol * f) break;
+    const double amax = max_alpha(x, d);
+    double alpha = (shifted || amax < 1.0) ? amax : 1.0;
+    if (!(alpha > 0.0)) break;
+    double xt[4], q1[3], q2[3], ft = 0.0;
+    bool accepted = false;
+    for (int ls = 0; ls < kMaxHalvings; ++ls) {
+      for (int i = 0; i < 4; ++i) xt[i] = x[i] + alpha * d[i];
+      apply_constraints(xt);
+      ft = value(A, B, xt, q1, q2);
+      if (ft <= f + (1e-4 * alpha) * gd) {
+        accepted = true;
+        break;
+      }
+      const double half = alpha * 0.5;
+      alpha = (ls == 0 && shifted) ? std::fmin(half, 0.05 / dmax) : half;
+    }
+    if (!accepted) break;
+    double step = 0.0;
+    for (int i = 0; i < 4; ++i) {
+      step = std::fmax(step, std::fabs(xt[i] - x[i]));
+      x[i] = xt[i];
+    }
+    const bool full_newton = !shifted && alpha == 1.0;
+    if (step <= kStepTol || (full_newton && step <= kQuadTol)) {
+      f = ft;
+      for (int c = 0; c < 3; ++c) {
+        p1[c] = q1[c];
+        p2[c] = q2[c];
+      }
+      ++it;
+      break;
+    }
+    f = value_grad_hess(A, B, x, g, H, p1, p2);
+  }
+  *d2 = f;
+  for (int c = 0; c < 3; ++c) dc[c] = p2[c] - p1[c];
+  return it;
+}
+
+}  // namespace smooth
+
 /* ------------------------------------------------------------------------ */
 
 struct SurfaceMetric {  // ShellSystem.h:56-63
@@ -534,7 +872,7 @@ struct oracle {
     limit_patch(c.eid[0], A);
     limit_patch(c.eid[1], B);
     double d2, dc[3];
-    shl_smooth_closest(&A, &B, c.x, &d2, dc);
+    smooth::closest(&A, &B, c.x, &d2, dc);
     c.d2 = d2;
     c.dc = Point(dc[0], dc[1], dc[2]);
     for (int e = 0; e < 2; ++e) {
@@ -1946,7 +2284,7 @@ int oracle_smooth_closest(oracle* o, uint32_t e1, uint32_t e2, double* x, double
   shl_limit_patch A, B;
   o->limit_patch(e1, A);
   o->limit_patch(e2, B);
-  return shl_smooth_closest(&A, &B, x, d2, dc);
+  return smooth::closest(&A, &B, x, d2, dc);
 }
 
 size_t oracle_subdiv_table(int N, double* out, size_t cap) {

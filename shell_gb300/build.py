@@ -19,7 +19,7 @@ RUN = os.path.join(OUT, "shl_run")  # the command-line driver (csrc/shl_run.cpp)
 
 CU_SOURCES = ["shl_kernels.cu", "shl_contact.cu", "shl_api.cu", "shl_mlp.cu"]
 CPP_SOURCES = ["shl_setup.cpp", "shl_host.cpp", "shl_io.cpp"]
-HEADERS = ["shl_geom.h", "shl_distance.h", "shl_setup.h", "shl_internal.cuh", "shl_expr.h", "shl_smooth.h", "shl_subdiv.h",
+HEADERS = ["shl_geom.h", "shl_distance.h", "shl_limit.h", "shl_setup.h", "shl_internal.cuh", "shl_expr.h", "shl_smooth.h", "shl_subdiv.h",
            os.path.join("..", "..", "include", "shl.h")]
 
 NVCC = os.environ.get("NVCC", "nvcc")

@@ -1,0 +1,216 @@
+/*
+ * shl_limit.h -- Loop limit-surface evaluation at any (v, w) of a face, shared
+ * bit for bit by the CUDA kernels and the host code (library set-up, CPU
+ * oracle).
+ *
+ * Reference behaviour (file:line):
+ *  - SubdivEvaluation::evaluate / evaluate_deriv (SubdivEvaluation.C:14-165):
+ *    a regular patch (first vertex of valence 6) is evaluated with Stam's 12
+ *    box splines; an irregular patch is subdivided n times around its
+ *    irregular vertex, n = floor(1 - log2(v + w)) after clamping points closer
+ *    than irregular_tol = 1e-10 to the vertex (rescale_irregular_coords,
+ *    SubdivEvaluation.C:168-187), and evaluated in one of the three regular
+ *    children of the n-th step: k = 0 for v > 1/2 with local (2v - 1, 2w),
+ *    k = 2 for w > 1/2 with (2v, 2w - 1), else the middle child k = 1 with
+ *    (1 - 2v, 1 - 2w).  The children's control points are fixed linear
+ *    combinations of the patch nodes (the tables of shl_subdiv.h; the
+ *    reference's PAnArray, SubdivEvaluation.h:14-96, holds the same matrices in
+ *    libMesh's node order, at most max_A_exponent = 34 levels).
+ *    Derivatives: d/dv of the local coordinates is 2^n for k = 0, 2 and -2^n
+ *    for the middle child (chain rule through the n-1 rescalings by 2 and the
+ *    child map).  SubdivEvaluation.C:125 uses (-2)^n for the middle child,
+ *    whose sign differs for even n; this restatement follows the chain rule,
+ *    so its tangents are the derivatives of its positions everywhere.
+ *
+ * Every floating-point operation is rounded on its own (SHL_MUL / SHL_ADD of
+ * shl_distance.h) or is an explicit fused multiply-add (fma, IEEE on both sides);
+ * frexp / ldexp are exact, so host and device agree bit for bit.
+ */
+#ifndef SHL_LIMIT_H_
+#define SHL_LIMIT_H_
+
+#include <stdint.h>
+
+#include "shl_distance.h"
+
+#ifndef __CUDACC__
+#include <math.h>
+#endif
+
+#define SHL_SMOOTH_LEVELS 34        /* max_A_exponent = floor(1 - log2(irregular_tol)) */
+#define SHL_IRREGULAR_TOL 1e-10
+#define SHL_SMOOTH_MAX_SLOTS 18     /* patch nodes of the largest valence (12) */
+/* Stam's box splines (J. Stam, "Evaluation of Loop subdivision surfaces",
+ * SIGGRAPH'98 course notes) expanded into monomials of (v, w) with
+ * u = 1 - v - w: basis s = (1/12) sum_m C[s][m] v^p w^q over the monomials
+ * m = (p, q) in the order (0,0) (0,1) .. (0,4) (1,0) .. (1,3) (2,0) (2,1) (2,2)
+ * (3,0) (3,1) (4,0).  Integer coefficients, exact in double. */
+#define SHL_BOX_COEFFS                                                        \
+  {{1, -4, 6, -4, 1, -2, 6, -6, 2, 0, 0, 0, 2, -2, -1},                       \
+   {1, -2, 0, 2, -1, -4, 6, 0, -2, 6, -6, 0, -4, 2, 1},                       \
+   {1, -2, 0, 2, -1, 2, -6, 6, -2, 0, 0, 0, -4, 4, 2},                        \
+   {6, 0, -12, 8, -1, 0, -12, 12, -2, -12, 12, 0, 8, -2, -1},                 \
+   {1, 2, 0, -4, 2, -2, -6, 0, 4, 0, 6, 0, 2, -2, -1},                        \
+   {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 2, -2, -1},                           \
+   {1, 2, 0, -4, 2, 4, 6, -12, 4, 6, -6, 0, -4, -2, -1},                      \
+   {1, 4, 6, -4, -1, 2, 6, -6, -2, 0, -12, 0, -4, 4, 2},                      \
+   {0, 0, 0, 2, -1, 0, 0, 0, -2, 0, 0, 0, 0, 0, 0},                           \
+   {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 2, 1},                             \
+   {0, 0, 0, 2, -1, 0, 0, 6, -2, 0, 6, 0, 2, -2, -1},                         \
+   {0, 0, 0, 0, 1, 0, 0, 0, 2, 0, 0, 0, 0, 0, 0}}
+#define SHL_BOX_P {0, 0, 0, 0, 0, 1, 1, 1, 1, 2, 2, 2, 3, 3, 4}
+#define SHL_BOX_Q {0, 1, 2, 3, 4, 0, 1, 2, 3, 0, 1, 2, 0, 1, 0}
+/* patch slot (this library's regular-patch order) of Stam node s */
+#define SHL_STAM_SLOT {5, 4, 6, 0, 3, 9, 1, 2, 11, 8, 7, 10}
+
+#ifdef __CUDACC__
+static __constant__ signed char kShlBoxC_d[12][15] = SHL_BOX_COEFFS;
+static __constant__ signed char kShlBoxP_d[15] = SHL_BOX_P;
+static __constant__ signed char kShlBoxQ_d[15] = SHL_BOX_Q;
+static __constant__ signed char kShlStamSlot_d[12] = SHL_STAM_SLOT;
+#endif
+static const signed char kShlBoxC_h[12][15] = SHL_BOX_COEFFS;
+static const signed char kShlBoxP_h[15] = SHL_BOX_P;
+static const signed char kShlBoxQ_h[15] = SHL_BOX_Q;
+static const signed char kShlStamSlot_h[12] = SHL_STAM_SLOT;
+
+#ifdef __CUDA_ARCH__
+#define SHL_BOXC kShlBoxC_d
+#define SHL_BOXP kShlBoxP_d
+#define SHL_BOXQ kShlBoxQ_d
+#define SHL_STAMSLOT kShlStamSlot_d
+#else
+#define SHL_BOXC kShlBoxC_h
+#define SHL_BOXP kShlBoxP_h
+#define SHL_BOXQ kShlBoxQ_h
+#define SHL_STAMSLOT kShlStamSlot_h
+#endif
+
+/* rescale_irregular_coords (SubdivEvaluation.C:168-187): returns n and scales
+ * (v, w) by 2^(n-1) so that v + w lies in (1/2, 1].  n = floor(1 - log2(v+w))
+ * is computed exactly from the binary exponent. */
+SHL_HD int shl_rescale_irregular(double* v, double* w)
+{
+  if (SHL_ADD(*v, *w) < SHL_IRREGULAR_TOL) {
+    *v = fmax(*v, SHL_IRREGULAR_TOL);
+    *w = fmax(*w, 0.0);
+  }
+  const double s = SHL_ADD(*v, *w);
+  int e = 0;
+  const double fr = frexp(s, &e);  /* s = fr 2^e, fr in [1/2, 1) */
+  int m = -e + (fr == 0.5 ? 1 : 0);  /* floor(-log2 s) */
+  /* n in [1, SHL_SMOOTH_LEVELS] for any input (v + w rounded above 1, NaN) */
+  if (!(m >= 0)) m = 0;
+  if (m > SHL_SMOOTH_LEVELS - 1) m = SHL_SMOOTH_LEVELS - 1;
+  *v = ldexp(*v, m);
+  *w = ldexp(*w, m);
+  return m + 1;
+}
+
+/* A face's limit patch: its node positions in this library's patch order
+ * (a, b, c, the remaining ring of a, d, b_far0, b_far1, c_far0, c_far1) as
+ * base + 3 * ids[j * stride], the valence N of its first vertex, and for
+ * N != 6 the subdivision table of valence N (shl_subdiv.h layout: [level n-1]
+ * [child k][Stam node s][slot]). */
+typedef struct {
+  const double* base;
+  const uint32_t* ids;
+  uint32_t stride;
+  int N;
+  const double* tab;
+} shl_limit_patch;
+
+#define SHL_FMA(a, b, c) fma((a), (b), (c))
+
+/* Limit surface of a patch at (v, w): out[0] the point, out[1] d/dv, out[2]
+ * d/dw (order >= 1), out[3] d2/dv2, out[4] d2/dw2, out[5] d2/dvdw (order 2).
+ * The twelve control points of the regular (sub-)patch are formed one at a
+ * time and contracted with the box splines as they are evaluated (12 times
+ * the splines, scaled by 1/12 at the end), in fused multiply-adds; fma is
+ * IEEE on host and device, so both round alike. */
+SHL_HD void shl_limit_eval(const shl_limit_patch* pt, double v, double w, int order, double out[6][3])
+{
+  double j1 = 1.0;
+  int n = 0, k = 0;
+  if (pt->N != 6) {
+    n = shl_rescale_irregular(&v, &w);
+    if (v > 0.5) {
+      k = 0;
+      v = SHL_SUB(SHL_MUL(2.0, v), 1.0);
+      w = SHL_MUL(2.0, w);
+      j1 = ldexp(1.0, n);
+    } else if (w > 0.5) {
+      k = 2;
+      v = SHL_MUL(2.0, v);
+      w = SHL_SUB(SHL_MUL(2.0, w), 1.0);
+      j1 = ldexp(1.0, n);
+    } else {
+      k = 1;
+      v = SHL_SUB(1.0, SHL_MUL(2.0, v));
+      w = SHL_SUB(1.0, SHL_MUL(2.0, w));
+      j1 = -ldexp(1.0, n);
+    }
+  }
+  const int np = pt->N + 6;
+  const double* T = pt->N == 6 ? 0 : pt->tab + (size_t)((n - 1) * 3 + k) * 12 * (size_t)np;
+  double vp[5], wp[5];
+  vp[0] = 1.0;
+  wp[0] = 1.0;
+  for (int i = 1; i < 5; ++i) {
+    vp[i] = SHL_MUL(vp[i - 1], v);
+    wp[i] = SHL_MUL(wp[i - 1], w);
+  }
+  const int nq = order >= 2 ? 6 : (order >= 1 ? 3 : 1);
+  double acc[6][3];
+  for (int q = 0; q < 6; ++q) acc[q][0] = acc[q][1] = acc[q][2] = 0.0;
+  for (int s = 0; s < 12; ++s) {
+    /* control point s */
+    double Q0, Q1, Q2;
+    if (T == 0) {
+      const double* x = pt->base + 3 * (size_t)pt->ids[(size_t)SHL_STAMSLOT[s] * pt->stride];
+      Q0 = x[0];
+      Q1 = x[1];
+      Q2 = x[2];
+    } else {
+      Q0 = Q1 = Q2 = 0.0;
+      for (int j = 0; j < np; ++j) {
+        const double t = T[s * np + j];
+        if (t == 0.0) continue;
+        const double* x = pt->base + 3 * (size_t)pt->ids[(size_t)j * pt->stride];
+        Q0 = SHL_FMA(t, x[0], Q0);
+        Q1 = SHL_FMA(t, x[1], Q1);
+        Q2 = SHL_FMA(t, x[2], Q2);
+      }
+    }
+    /* box spline s and its derivatives, times 12 */
+    double bs[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    for (int m = 0; m < 15; ++m) {
+      const int c = SHL_BOXC[s][m];
+      if (c == 0) continue;
+      const int p = SHL_BOXP[m], q = SHL_BOXQ[m];
+      bs[0] = SHL_FMA((double)c, SHL_MUL(vp[p], wp[q]), bs[0]);
+      if (nq > 1) {
+        if (p >= 1) bs[1] = SHL_FMA((double)(c * p), SHL_MUL(vp[p - 1], wp[q]), bs[1]);
+        if (q >= 1) bs[2] = SHL_FMA((double)(c * q), SHL_MUL(vp[p], wp[q - 1]), bs[2]);
+      }
+      if (nq > 3) {
+        if (p >= 2) bs[3] = SHL_FMA((double)(c * p * (p - 1)), SHL_MUL(vp[p - 2], wp[q]), bs[3]);
+        if (q >= 2) bs[4] = SHL_FMA((double)(c * q * (q - 1)), SHL_MUL(vp[p], wp[q - 2]), bs[4]);
+        if (p >= 1 && q >= 1) bs[5] = SHL_FMA((double)(c * p * q), SHL_MUL(vp[p - 1], wp[q - 1]), bs[5]);
+      }
+    }
+    for (int q = 0; q < nq; ++q) {
+      acc[q][0] = SHL_FMA(bs[q], Q0, acc[q][0]);
+      acc[q][1] = SHL_FMA(bs[q], Q1, acc[q][1]);
+      acc[q][2] = SHL_FMA(bs[q], Q2, acc[q][2]);
+    }
+  }
+  const double twelfth = 1.0 / 12.0;
+  for (int q = 0; q < nq; ++q) {
+    const double sc = q == 0 ? twelfth : (q < 3 ? SHL_MUL(j1, twelfth) : SHL_MUL(SHL_MUL(j1, j1), twelfth));
+    for (int c = 0; c < 3; ++c) out[q][c] = SHL_MUL(acc[q][c], sc);
+  }
+}
+
+
+#endif /* SHL_LIMIT_H_ */

@@ -1,9 +1,11 @@
 """SMOOTH self-contact on the GPU against the CPU oracle.
 
-The closest-point searches between limit surfaces use the same shared header
-(shl_smooth.h) with separately rounded operations on both sides, and the same
-subdivision tables (shl_subdiv.h), so the candidate list, the squared
-distances and the searches' coordinates are bit-exact at a given state; forces
+The closest-point search between limit surfaces is the library's
+shl_smooth.h on the GPU and the oracle's own restatement of the same
+projected-Newton method on the CPU, both over the shared limit evaluation
+(shl_limit.h) and subdivision tables (shl_subdiv.h) with separately rounded
+operations, so the candidate list, the squared distances and the searches'
+coordinates are bit-exact at a given state; forces
 within 1e-12 relative (the element kernel's fused multiply-adds); 24-step
 trajectories within 1e-10 (u) and 1e-7 (v): the searches stop within their
 convergence tolerance, which a 1e-13 force difference can shift.

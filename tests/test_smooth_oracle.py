@@ -1,6 +1,6 @@
 """SMOOTH self-contact on the CPU: the Loop limit-surface evaluation at any
-point of a face (shl_smooth.h / shl_subdiv.h, through the oracle) and the
-closest-point search between two limit patches.
+point of a face (shl_limit.h / shl_subdiv.h, through the oracle) and the
+oracle's closest-point search between two limit patches.
 
 The reference's own evaluation (libMesh's FESubdivision and the missing
 ConstrainedMinimizer.h) cannot run here, so these are known-answer tests:
