@@ -704,15 +704,27 @@ __global__ void __launch_bounds__(kBlock, 4) k_rb_cand(DevBuf b, StepConst sc) {
   flush();
 }
 
+// the acceptance of a candidate at squared distance d2 (ShellSystem.C:2082)
+__device__ __forceinline__ void narrow_accept(const DevBuf& b, const StepConst& sc, Ctl* ctl, uint32_t i, uint32_t e1,
+                                              double d2) {
+  const double d2_max = sc.n_cs ? b.shc[b.face_shell[e1]].d2_max : ctl->d2_max;
+  if (d2 <= 0.0) atomicMax(&ctl->problem, (int)SHL_CONTACT_PROBLEM);
+  const bool ok = !(d2 > d2_max);
+  b.cand_d2[i] = d2;
+  b.cand_ok[i] = ok ? 1 : 0;
+  if (ok) {
+    atomicAdd(&b.new_cnt[e1], 1u);
+    atomicAdd(&b.seg_count[e1], 1u);
+  }
+}
+
 // closest-point test of each candidate (rounded operation by operation)
-template <bool SMOOTH>
 __global__ void __launch_bounds__(kBlock) k_rb_narrow(DevBuf b, StepConst sc) {
   Ctl* ctl = b.ctl;
   if (rb_off(ctl)) return;
   const uint32_t n = min(ctl->n_cand, sc.cand_cap);
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const uint32_t e1 = b.cand_e1[i], e2 = b.cand_e2[i];
-    const double d2_max = sc.n_cs ? b.shc[b.face_shell[e1]].d2_max : ctl->d2_max;
     const double* P1[3];
     const double* P2[3];
     for (int q = 0; q < 3; ++q) {
@@ -720,20 +732,100 @@ __global__ void __launch_bounds__(kBlock) k_rb_narrow(DevBuf b, StepConst sc) {
       P2[q] = b.p + 3 * (size_t)b.tri[3 * (size_t)e2 + q];
     }
     shl_pair_geom g;
-    if (SMOOTH) {  // a new SmoothShellShellContact starts at (1/3, 1/3) (SmoothShellShellContact.C:9-14)
-      double x[4] = {1.0 / 3.0, 1.0 / 3.0, 1.0 / 3.0, 1.0 / 3.0};
-      smooth_pair(b, sc, e1, e2, x, &g);
-      for (int k = 0; k < 4; ++k) b.cand_x[4 * (size_t)i + k] = x[k];
-    } else {
-      shl_pair_compute(P1, P2, &g);
+    shl_pair_compute(P1, P2, &g);
+    narrow_accept(b, sc, ctl, i, e1, g.d2);
+  }
+}
+
+// SMOOTH closest-point searches with lane refill.  A search takes from one to
+// several hundred limit evaluations (most of a squashed shell's pairs end after
+// one to three, a few run the line search to its limit), so one thread per
+// pair would hold each warp until its longest search ends.  Here each lane
+// runs its search as a resumable state (shl_smooth_state): per trip a warp
+// evaluates one point of both limit patches per lane and advances the
+// searches, and a lane whose search has ended takes the next pair from a queue
+// shared by the grid (ctl->cnt[7]; the last warp to leave resets it), so that
+// the lanes stay busy until the queue is empty.  A search's result does not
+// depend on the lane or the order that runs it.
+//   REBUILD: the candidates of a linked-cell pass, each from (1/3, 1/3, 1/3,
+//   1/3) as a new SmoothShellShellContact (SmoothShellShellContact.C:9-14),
+//   then k_rb_narrow's acceptance;
+//   else: the pairs of the list from their previous solution; x, d2 and
+//   dc = p2 - p1 go to pvw, pd2 and the pair's force slots 0-2 for
+//   k_contact_force.
+constexpr int kSearchBlock = 128;
+template <bool REBUILD>
+__global__ void __launch_bounds__(kSearchBlock) k_smooth_search(DevBuf b, StepConst sc) {
+  Ctl* ctl = b.ctl;
+  uint32_t* queue = &ctl->cnt[7];
+  uint32_t* left = &ctl->cnt[8];
+  const bool off = REBUILD ? rb_off(ctl) : (ctl->halted != 0 || ctl->paused != 0);
+  const uint32_t n = off ? 0u : (REBUILD ? min(ctl->n_cand, sc.cand_cap) : ctl->n_pairs);
+  const unsigned lane = threadIdx.x & 31u;
+  const unsigned below = (1u << lane) - 1u;
+  bool busy = false, more = n > 0;
+  uint32_t j = 0, e1 = 0;
+  shl_limit_patch A, B;
+  shl_smooth_state st;
+  for (;;) {
+    const unsigned idle = __ballot_sync(0xffffffffu, !busy);
+    if (more && idle) {
+      const int leader = __ffs(idle) - 1;
+      const uint32_t want = (uint32_t)__popc(idle);
+      uint32_t base = 0;
+      if ((int)lane == leader) base = atomicAdd(queue, want);
+      base = __shfl_sync(0xffffffffu, base, leader);
+      if (!(base + want < n)) more = false;  // the queue is empty for every warp
+      if (!busy) {
+        const uint32_t i = base + (uint32_t)__popc(idle & below);
+        if (i < n) {
+          busy = true;
+          j = i;
+          double x0[4];
+          uint32_t e2;
+          if (REBUILD) {
+            e1 = b.cand_e1[i];
+            e2 = b.cand_e2[i];
+            for (int k = 0; k < 4; ++k) x0[k] = 1.0 / 3.0;
+          } else {
+            e1 = b.pe1[0][i];
+            e2 = b.pe2[0][i];
+            for (int k = 0; k < 4; ++k) x0[k] = b.pvw[0][4 * (size_t)i + k];
+          }
+          smooth_patch(b, sc, e1, A);
+          smooth_patch(b, sc, e2, B);
+          shl_smooth_start(&st, x0);
+        }
+      }
     }
-    if (g.d2 <= 0.0) atomicMax(&ctl->problem, (int)SHL_CONTACT_PROBLEM);
-    const bool ok = !(g.d2 > d2_max);  // ShellSystem.C:2082
-    b.cand_d2[i] = g.d2;
-    b.cand_ok[i] = ok ? 1 : 0;
-    if (ok) {
-      atomicAdd(&b.new_cnt[e1], 1u);
-      atomicAdd(&b.seg_count[e1], 1u);
+    if (!__any_sync(0xffffffffu, busy)) break;
+    if (busy) {
+      const double* pt = shl_smooth_point(&st);
+      const int order = shl_smooth_order(&st);
+      double ev1[6][3], ev2[6][3];
+      shl_limit_eval(&A, pt[0], pt[1], order, ev1);
+      shl_limit_eval(&B, pt[2], pt[3], order, ev2);
+      shl_smooth_take(&st, ev1, ev2);
+      if (st.phase == SHL_SMOOTH_DONE) {
+        busy = false;
+        if (REBUILD) {
+          for (int k = 0; k < 4; ++k) b.cand_x[4 * (size_t)j + k] = st.x[k];
+          narrow_accept(b, sc, ctl, j, e1, st.f);
+        } else {
+          for (int k = 0; k < 4; ++k) b.pvw[0][4 * (size_t)j + k] = st.x[k];
+          b.pd2[0][j] = st.f;
+          double* out = b.pforce + kPairOut * (size_t)j;
+          for (int c = 0; c < 3; ++c) out[c] = SHL_SUB(st.p2[c], st.p1[c]);
+        }
+      }
+    }
+  }
+  if (lane == 0) {
+    __threadfence();
+    const uint32_t warps = gridDim.x * (kSearchBlock / 32);
+    if (atomicAdd(left, 1u) == warps - 1) {
+      atomicExch(queue, 0u);
+      atomicExch(left, 0u);
     }
   }
 }
@@ -911,6 +1003,26 @@ inline uint32_t nblk(uint32_t n, uint32_t bs = kBlock) { return n == 0 ? 1 : (n 
 
 }  // namespace
 
+// a grid that the SMs hold at once (the queue hands out the pairs)
+template <bool REBUILD>
+static uint32_t search_grid() {
+  static const uint32_t g = [] {
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_smooth_search<REBUILD>, kSearchBlock, 0);
+    return (uint32_t)(sms > 0 ? sms : 152) * (uint32_t)(per_sm > 0 ? per_sm : 1);
+  }();
+  return g;
+}
+
+void launch_smooth_search(const DevBuf& b, const StepConst& sc, bool rebuild, cudaStream_t s) {
+  if (rebuild)
+    k_smooth_search<true><<<search_grid<true>(), kSearchBlock, 0, s>>>(b, sc);
+  else
+    k_smooth_search<false><<<search_grid<false>(), kSearchBlock, 0, s>>>(b, sc);
+}
+
 void launch_contact_csr(const DevBuf& b, const StepConst& sc, cudaStream_t s) {
   const uint32_t gV = nblk(sc.V);
   uint32_t gP = nblk(sc.pairs_cap);
@@ -951,9 +1063,9 @@ void launch_rebuild(const DevBuf& b, const StepConst& sc, cudaStream_t s) {
     uint32_t gc = nblk(sc.cand_cap);
     if (gc > 16 * 152) gc = 16 * 152;
     if (sc.smooth)
-      k_rb_narrow<true><<<gc, kBlock, 0, s>>>(b, sc);
+      launch_smooth_search(b, sc, true, s);
     else
-      k_rb_narrow<false><<<gc, kBlock, 0, s>>>(b, sc);
+      k_rb_narrow<<<gc, kBlock, 0, s>>>(b, sc);
     launch_scan(&b.ctl->rebuild, b.ctl, b.new_cnt, b.new_off, nullptr, sc.F, sc.F, b.scan_block, &b.ctl->n_new,
                 false, sc.pairs_cap, true, s);
     k_rb_scatter_new<<<gc, kBlock, 0, s>>>(b, sc);

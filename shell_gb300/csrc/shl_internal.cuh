@@ -285,15 +285,11 @@ __device__ __forceinline__ void smooth_patch(const DevBuf& b, const StepConst& s
   lp.tab = N == 6 ? nullptr : b.stab + sc.stab_off[N];
 }
 
-// Closest points of the limit patches of a pair from the start x[4] (patch
-// frames); fills the pair geometry with the coordinates in each face's own node
-// order (the force distribution's u, v, w of tri[0..2]).
-__device__ __forceinline__ void smooth_pair(const DevBuf& b, const StepConst& sc, uint32_t e1, uint32_t e2,
-                                            double* x, shl_pair_geom* g) {
-  shl_limit_patch A, B;
-  smooth_patch(b, sc, e1, A);
-  smooth_patch(b, sc, e2, B);
-  shl_smooth_closest(&A, &B, x, &g->d2, g->dc);
+// The pair geometry's coordinates in each face's own node order (the force
+// distribution's u, v, w of tri[0..2]) from the closest-point search's
+// x = (v1, w1, v2, w2) in the patch frames.
+__device__ __forceinline__ void smooth_coords(const DevBuf& b, uint32_t e1, uint32_t e2, const double* x,
+                                              shl_pair_geom* g) {
   const uint32_t e[2] = {e1, e2};
   for (int t = 0; t < 2; ++t) {
     const int r = b.fsm[e[t]] >> 8;
@@ -308,6 +304,11 @@ __device__ __forceinline__ void smooth_pair(const DevBuf& b, const StepConst& sc
 #endif
 
 // ---- launchers (shl_kernels.cu) ----
+// SMOOTH closest-point searches (shl_contact.cu): rebuild = the candidates of a
+// linked-cell pass (then k_rb_narrow's acceptance), else the pairs of the list
+// from their previous solution (x to pvw, d2 to pd2, dc to the pair's force
+// slots 0-2, which k_contact_force reads and overwrites)
+void launch_smooth_search(const DevBuf& b, const StepConst& sc, bool rebuild, cudaStream_t s);
 // The condition of a graph IF node around a linked-cell pass, set to
 // (ctl->rebuild && !ctl->halted) by the last block of the kernel that decides
 // the rebuild (has = 0: launched outside a graph, or no IF node follows).

@@ -1596,17 +1596,18 @@ __global__ void __launch_bounds__(kBlock) k_contact_force(DevBuf b, StepConst sc
       P2[k] = b.p + 3 * (size_t)nid[1][k];
     }
     shl_pair_geom g;
-    if (SMOOTH) {  // SmoothShellShellContact::compute from the pair's previous solution
+    double* out = b.pforce + kPairOut * (size_t)j;
+    if (SMOOTH) {  // SmoothShellShellContact::compute: the search of k_smooth_search from the previous solution
       double x[4];
       for (int k = 0; k < 4; ++k) x[k] = b.pvw[0][4 * (size_t)j + k];
-      smooth_pair(b, sc, e[0], e[1], x, &g);
-      for (int k = 0; k < 4; ++k) b.pvw[0][4 * (size_t)j + k] = x[k];
+      g.d2 = b.pd2[0][j];
+      for (int c = 0; c < 3; ++c) g.dc[c] = out[c];
+      smooth_coords(b, e[0], e[1], x, &g);
     } else {
       shl_pair_compute(P1, P2, &g);
+      b.pd2[0][j] = g.d2;
     }
-    b.pd2[0][j] = g.d2;
     if (g.d2 <= 0.0) register_problem(ctl, SHL_CONTACT_PROBLEM);
-    double* out = b.pforce + kPairOut * (size_t)j;
     if (g.d2 < d2_friction) {
       const double area_min = fmin(b.area[e[0]], b.area[e[1]]);
       const double abs_dc = SHL_SQRT(g.d2);
@@ -2362,9 +2363,10 @@ void launch_contact_force(const DevBuf& b, const StepConst& sc, int, cudaStream_
   uint32_t nb = nblk(sc.pairs_cap);
   if (nb > 4 * 152) nb = 4 * 152;
   if (nb == 0) nb = 1;
-  if (sc.smooth)
+  if (sc.smooth) {
+    launch_smooth_search(b, sc, false, s);
     k_contact_force<true><<<nb, kBlock, 0, s>>>(b, sc);
-  else
+  } else
     k_contact_force<false><<<nb, kBlock, 0, s>>>(b, sc);
 }
 // mode 2: an adaptive attempt (a_pred and the error estimate); else correct ? step corrector : evaluation

@@ -63,27 +63,15 @@
 /* patch slot (this library's regular-patch order) of Stam node s */
 #define SHL_STAM_SLOT {5, 4, 6, 0, 3, 9, 1, 2, 11, 8, 7, 10}
 
-#ifdef __CUDACC__
-static __constant__ signed char kShlBoxC_d[12][15] = SHL_BOX_COEFFS;
-static __constant__ signed char kShlBoxP_d[15] = SHL_BOX_P;
-static __constant__ signed char kShlBoxQ_d[15] = SHL_BOX_Q;
-static __constant__ signed char kShlStamSlot_d[12] = SHL_STAM_SLOT;
-#endif
-static const signed char kShlBoxC_h[12][15] = SHL_BOX_COEFFS;
-static const signed char kShlBoxP_h[15] = SHL_BOX_P;
-static const signed char kShlBoxQ_h[15] = SHL_BOX_Q;
-static const signed char kShlStamSlot_h[12] = SHL_STAM_SLOT;
-
+/* Device loops over the twelve splines and fifteen monomials unroll fully, so
+ * that the tables fold into the code (no table loads, no dynamically indexed
+ * arrays); the host runs the same loops, operation for operation. */
 #ifdef __CUDA_ARCH__
-#define SHL_BOXC kShlBoxC_d
-#define SHL_BOXP kShlBoxP_d
-#define SHL_BOXQ kShlBoxQ_d
-#define SHL_STAMSLOT kShlStamSlot_d
+#define SHL_UNROLL _Pragma("unroll")
+#define SHL_TABLE const
 #else
-#define SHL_BOXC kShlBoxC_h
-#define SHL_BOXP kShlBoxP_h
-#define SHL_BOXQ kShlBoxQ_h
-#define SHL_STAMSLOT kShlStamSlot_h
+#define SHL_UNROLL
+#define SHL_TABLE static const
 #endif
 
 /* rescale_irregular_coords (SubdivEvaluation.C:168-187): returns n and scales
@@ -151,6 +139,10 @@ SHL_HD void shl_limit_eval(const shl_limit_patch* pt, double v, double w, int or
       j1 = -ldexp(1.0, n);
     }
   }
+  SHL_TABLE signed char BC[12][15] = SHL_BOX_COEFFS;
+  SHL_TABLE signed char BP[15] = SHL_BOX_P;
+  SHL_TABLE signed char BQ[15] = SHL_BOX_Q;
+  SHL_TABLE signed char SLOT[12] = SHL_STAM_SLOT;
   const int np = pt->N + 6;
   const double* T = pt->N == 6 ? 0 : pt->tab + (size_t)((n - 1) * 3 + k) * 12 * (size_t)np;
   double vp[5], wp[5];
@@ -163,11 +155,12 @@ SHL_HD void shl_limit_eval(const shl_limit_patch* pt, double v, double w, int or
   const int nq = order >= 2 ? 6 : (order >= 1 ? 3 : 1);
   double acc[6][3];
   for (int q = 0; q < 6; ++q) acc[q][0] = acc[q][1] = acc[q][2] = 0.0;
+  SHL_UNROLL
   for (int s = 0; s < 12; ++s) {
     /* control point s */
     double Q0, Q1, Q2;
     if (T == 0) {
-      const double* x = pt->base + 3 * (size_t)pt->ids[(size_t)SHL_STAMSLOT[s] * pt->stride];
+      const double* x = pt->base + 3 * (size_t)pt->ids[(size_t)SLOT[s] * pt->stride];
       Q0 = x[0];
       Q1 = x[1];
       Q2 = x[2];
@@ -184,10 +177,11 @@ SHL_HD void shl_limit_eval(const shl_limit_patch* pt, double v, double w, int or
     }
     /* box spline s and its derivatives, times 12 */
     double bs[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    SHL_UNROLL
     for (int m = 0; m < 15; ++m) {
-      const int c = SHL_BOXC[s][m];
+      const int c = BC[s][m];
       if (c == 0) continue;
-      const int p = SHL_BOXP[m], q = SHL_BOXQ[m];
+      const int p = BP[m], q = BQ[m];
       bs[0] = SHL_FMA((double)c, SHL_MUL(vp[p], wp[q]), bs[0]);
       if (nq > 1) {
         if (p >= 1) bs[1] = SHL_FMA((double)(c * p), SHL_MUL(vp[p - 1], wp[q]), bs[1]);
@@ -199,7 +193,9 @@ SHL_HD void shl_limit_eval(const shl_limit_patch* pt, double v, double w, int or
         if (p >= 1 && q >= 1) bs[5] = SHL_FMA((double)(c * p * q), SHL_MUL(vp[p - 1], wp[q - 1]), bs[5]);
       }
     }
-    for (int q = 0; q < nq; ++q) {
+    SHL_UNROLL
+    for (int q = 0; q < 6; ++q) {
+      if (q >= nq) break;
       acc[q][0] = SHL_FMA(bs[q], Q0, acc[q][0]);
       acc[q][1] = SHL_FMA(bs[q], Q1, acc[q][1]);
       acc[q][2] = SHL_FMA(bs[q], Q2, acc[q][2]);
