@@ -694,6 +694,7 @@ shl_status create_common(shl_ctx* c, const std::vector<double>& pscale_orig, shl
     if (smooth) {
       ALLOC(b.pvw[0], 4 * (size_t)pairs_cap); ALLOC(b.pvw[1], 4 * (size_t)pairs_cap);
       ALLOC(b.new_x, 4 * (size_t)pairs_cap); ALLOC(b.cand_x, 4 * (size_t)cand_cap);
+      ALLOC(b.lcoef, SHL_LIMIT_NCOEF * (size_t)F);
       ALLOC(b.inv_perm, F); ALLOC(b.fsm, F);
     }
     if (batch_contact) {

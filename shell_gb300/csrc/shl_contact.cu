@@ -753,6 +753,32 @@ __global__ void __launch_bounds__(kBlock) k_rb_narrow(DevBuf b, StepConst sc) {
 //   else: the pairs of the list from their previous solution; x, d2 and
 //   dc = p2 - p1 go to pvw, pd2 and the pair's force slots 0-2 for
 //   k_contact_force.
+// the power form of each regular patch at the current positions (irregular
+// patches are evaluated from their subdivision tables in the search)
+__global__ void __launch_bounds__(kBlock) k_limit_coeffs(DevBuf b, StepConst sc, bool rebuild) {
+  const Ctl* ctl = b.ctl;
+  if (rebuild ? rb_off(ctl) : (ctl->halted != 0 || ctl->paused != 0)) return;
+  for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < sc.F; e += gridDim.x * blockDim.x) {
+    if ((b.fsm[e] & 0xff) != 6) continue;
+    shl_limit_patch lp;
+    smooth_patch(b, sc, e, lp);
+    double P[15][3];
+    shl_limit_coeffs_regular(&lp, P);
+    double* out = b.lcoef + SHL_LIMIT_NCOEF * (size_t)e;
+    for (int m = 0; m < 15; ++m)
+      for (int c = 0; c < 3; ++c) out[3 * m + c] = P[m][c];
+  }
+}
+
+// a patch's limit surface at (v, w): the stored power form of a regular patch
+__device__ __forceinline__ void limit_at(const DevBuf& b, uint32_t e, const shl_limit_patch& lp, double v, double w,
+                                         int order, double out[6][3]) {
+  if (lp.N == 6)
+    shl_limit_poly(reinterpret_cast<const double(*)[3]>(b.lcoef + SHL_LIMIT_NCOEF * (size_t)e), v, w, order, 1.0, out);
+  else
+    shl_limit_eval(&lp, v, w, order, out);
+}
+
 constexpr int kSearchBlock = 128;
 template <bool REBUILD>
 __global__ void __launch_bounds__(kSearchBlock) k_smooth_search(DevBuf b, StepConst sc) {
@@ -764,7 +790,7 @@ __global__ void __launch_bounds__(kSearchBlock) k_smooth_search(DevBuf b, StepCo
   const unsigned lane = threadIdx.x & 31u;
   const unsigned below = (1u << lane) - 1u;
   bool busy = false, more = n > 0;
-  uint32_t j = 0, e1 = 0;
+  uint32_t j = 0, e1 = 0, e2 = 0;
   shl_limit_patch A, B;
   shl_smooth_state st;
   for (;;) {
@@ -782,7 +808,6 @@ __global__ void __launch_bounds__(kSearchBlock) k_smooth_search(DevBuf b, StepCo
           busy = true;
           j = i;
           double x0[4];
-          uint32_t e2;
           if (REBUILD) {
             e1 = b.cand_e1[i];
             e2 = b.cand_e2[i];
@@ -803,8 +828,8 @@ __global__ void __launch_bounds__(kSearchBlock) k_smooth_search(DevBuf b, StepCo
       const double* pt = shl_smooth_point(&st);
       const int order = shl_smooth_order(&st);
       double ev1[6][3], ev2[6][3];
-      shl_limit_eval(&A, pt[0], pt[1], order, ev1);
-      shl_limit_eval(&B, pt[2], pt[3], order, ev2);
+      limit_at(b, e1, A, pt[0], pt[1], order, ev1);
+      limit_at(b, e2, B, pt[2], pt[3], order, ev2);
       shl_smooth_take(&st, ev1, ev2);
       if (st.phase == SHL_SMOOTH_DONE) {
         busy = false;
@@ -976,21 +1001,56 @@ __global__ void k_csr_fill(DevBuf b, StepConst sc) {
   }
 }
 
-// sort each node's entries (deterministic order for the gather) and clear the flag
-__global__ void k_csr_sort(DevBuf b, StepConst sc) {
+// sort each node's entries (deterministic order for the gather): one warp per
+// node, a bitonic sort of the entries padded to a power of two in shared
+// memory (a node has a few hundred entries in a contact-heavy state, about a
+// thousand with SMOOTH contact); a node with more than kCsrSortCap entries is
+// sorted in place by one lane
+constexpr int kCsrSortWarps = 4;
+constexpr uint32_t kCsrSortCap = 2048;
+__global__ void __launch_bounds__(32 * kCsrSortWarps) k_csr_sort(DevBuf b, StepConst sc) {
   Ctl* ctl = b.ctl;
   if (csr_off(ctl)) return;
-  const uint32_t nd = blockIdx.x * blockDim.x + threadIdx.x;
-  if (nd >= sc.V) return;
-  const uint32_t k0 = b.csr_ptr[nd], k1 = b.csr_ptr[nd + 1];
-  for (uint32_t k = k0 + 1; k < k1; ++k) {
-    const uint32_t x = b.csr_ent[k];
-    uint32_t q = k;
-    while (q > k0 && b.csr_ent[q - 1] > x) {
-      b.csr_ent[q] = b.csr_ent[q - 1];
-      --q;
+  __shared__ uint32_t buf[kCsrSortWarps][kCsrSortCap];
+  const uint32_t lane = threadIdx.x & 31u, w = threadIdx.x >> 5;
+  uint32_t* sh = buf[w];
+  for (uint32_t nd = blockIdx.x * kCsrSortWarps + w; nd < sc.V; nd += gridDim.x * kCsrSortWarps) {
+    const uint32_t k0 = b.csr_ptr[nd], k1 = b.csr_ptr[nd + 1];
+    const uint32_t n = k1 - k0;
+    if (n < 2) continue;
+    if (n > kCsrSortCap) {
+      if (lane == 0)
+        for (uint32_t k = k0 + 1; k < k1; ++k) {
+          const uint32_t x = b.csr_ent[k];
+          uint32_t q = k;
+          while (q > k0 && b.csr_ent[q - 1] > x) {
+            b.csr_ent[q] = b.csr_ent[q - 1];
+            --q;
+          }
+          b.csr_ent[q] = x;
+        }
+      __syncwarp();
+      continue;
     }
-    b.csr_ent[q] = x;
+    uint32_t P = 32;
+    while (P < n) P <<= 1;
+    for (uint32_t i = lane; i < P; i += 32) sh[i] = i < n ? b.csr_ent[k0 + i] : 0xffffffffu;
+    __syncwarp();
+    for (uint32_t k = 2; k <= P; k <<= 1)
+      for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+        // compare-exchange t: the pair (i, i + j) with bit j of i clear
+        for (uint32_t t = lane; t < P / 2; t += 32) {
+          const uint32_t i = ((t & ~(j - 1)) << 1) | (t & (j - 1));
+          const uint32_t x = sh[i], y = sh[i + j];
+          if (((i & k) == 0) == (x > y)) {
+            sh[i] = y;
+            sh[i + j] = x;
+          }
+        }
+        __syncwarp();
+      }
+    for (uint32_t i = lane; i < n; i += 32) b.csr_ent[k0 + i] = sh[i];
+    __syncwarp();
   }
 }
 
@@ -1017,6 +1077,9 @@ static uint32_t search_grid() {
 }
 
 void launch_smooth_search(const DevBuf& b, const StepConst& sc, bool rebuild, cudaStream_t s) {
+  uint32_t g = nblk(sc.F);
+  if (g > 8 * 152) g = 8 * 152;
+  k_limit_coeffs<<<g, kBlock, 0, s>>>(b, sc, rebuild);
   if (rebuild)
     k_smooth_search<true><<<search_grid<true>(), kSearchBlock, 0, s>>>(b, sc);
   else
@@ -1032,7 +1095,11 @@ void launch_contact_csr(const DevBuf& b, const StepConst& sc, cudaStream_t s) {
   launch_scan(&b.ctl->csr_dirty, b.ctl, b.csr_count, b.csr_ptr, nullptr, sc.V, sc.V, b.scan_block, &b.ctl->n_csr,
               true, sc.csr_cap, true, s);
   k_csr_fill<<<gP, kBlock, 0, s>>>(b, sc);
-  k_csr_sort<<<gV, kBlock, 0, s>>>(b, sc);
+  {
+    uint32_t g = (sc.V + kCsrSortWarps - 1) / kCsrSortWarps;
+    if (g > 16 * 152) g = 16 * 152;
+    k_csr_sort<<<g ? g : 1, 32 * kCsrSortWarps, 0, s>>>(b, sc);
+  }
   k_csr_finish<<<1, 1, 0, s>>>(b);
 }
 

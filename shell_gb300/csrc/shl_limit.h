@@ -109,19 +109,138 @@ typedef struct {
 } shl_limit_patch;
 
 #define SHL_FMA(a, b, c) fma((a), (b), (c))
+#define SHL_LIMIT_NCOEF 45  /* power-form coefficients of a regular patch: 15 monomials x 3 */
 
-/* Limit surface of a patch at (v, w): out[0] the point, out[1] d/dv, out[2]
- * d/dw (order >= 1), out[3] d2/dv2, out[4] d2/dw2, out[5] d2/dvdw (order 2).
- * The twelve control points of the regular (sub-)patch are formed one at a
- * time and contracted with the box splines as they are evaluated (12 times
- * the splines, scaled by 1/12 at the end), in fused multiply-adds; fma is
- * IEEE on host and device, so both round alike. */
+/* The limit surface of a regular (sub-)patch over its triangle is a quartic
+ * polynomial: sum_s B_s(v, w) Q_s = sum_m P_m v^p w^q with the power-form
+ * coefficients P_m = (1/12) sum_s C[s][m] Q_s of its twelve control points Q_s
+ * (Stam node order; m in the monomial order of SHL_BOX_P / SHL_BOX_Q).
+ * shl_limit_add_point adds control point s to the coefficients (s ascending,
+ * fused multiply-adds from zero, so P_m's rounding does not depend on how
+ * the points are formed); shl_limit_scale applies the 1/12. */
+SHL_HD void shl_limit_add_point(double P[15][3], int s, double q0, double q1, double q2)
+{
+  SHL_TABLE signed char BC[12][15] = SHL_BOX_COEFFS;
+  SHL_UNROLL
+  for (int m = 0; m < 15; ++m) {
+    const int c = BC[s][m];
+    if (c == 0) continue;
+    P[m][0] = SHL_FMA((double)c, q0, P[m][0]);
+    P[m][1] = SHL_FMA((double)c, q1, P[m][1]);
+    P[m][2] = SHL_FMA((double)c, q2, P[m][2]);
+  }
+}
+
+SHL_HD void shl_limit_scale(double P[15][3])
+{
+  const double twelfth = 1.0 / 12.0;
+  SHL_UNROLL
+  for (int m = 0; m < 15; ++m) {
+    P[m][0] = SHL_MUL(P[m][0], twelfth);
+    P[m][1] = SHL_MUL(P[m][1], twelfth);
+    P[m][2] = SHL_MUL(P[m][2], twelfth);
+  }
+}
+
+/* Power-form coefficients of a regular patch (N = 6) from its nodes. */
+SHL_HD void shl_limit_coeffs_regular(const shl_limit_patch* pt, double P[15][3])
+{
+  SHL_TABLE signed char SLOT[12] = SHL_STAM_SLOT;
+  SHL_UNROLL
+  for (int m = 0; m < 15; ++m) P[m][0] = P[m][1] = P[m][2] = 0.0;
+  SHL_UNROLL
+  for (int s = 0; s < 12; ++s) {
+    const double* x = pt->base + 3 * (size_t)pt->ids[(size_t)SLOT[s] * pt->stride];
+    shl_limit_add_point(P, s, x[0], x[1], x[2]);
+  }
+  shl_limit_scale(P);
+}
+
+/* Evaluation of the power form at (v, w) of the (sub-)patch's triangle:
+ * out[0] the point, out[1] d/dv, out[2] d/dw (order >= 1), out[3] d2/dv2,
+ * out[4] d2/dw2, out[5] d2/dvdw (order 2), the derivatives times j1 and j1^2
+ * (the chain rule of an irregular patch's sub-patch map; j1 = 1 for a regular
+ * patch, a power of two otherwise, so the scaling is exact).  Each sum runs
+ * over the monomials in order; the integer factors of the derivatives scale
+ * the monomials. */
+SHL_HD void shl_limit_poly(const double P[15][3], double v, double w, int order, double j1, double out[6][3])
+{
+  SHL_TABLE signed char BP[15] = SHL_BOX_P;
+  SHL_TABLE signed char BQ[15] = SHL_BOX_Q;
+  double vp[5], wp[5];
+  vp[0] = 1.0;
+  wp[0] = 1.0;
+  SHL_UNROLL
+  for (int i = 1; i < 5; ++i) {
+    vp[i] = SHL_MUL(vp[i - 1], v);
+    wp[i] = SHL_MUL(wp[i - 1], w);
+  }
+  double a0 = 0.0, a1 = 0.0, a2 = 0.0;
+  SHL_UNROLL
+  for (int m = 0; m < 15; ++m) {
+    const double t = SHL_MUL(vp[BP[m]], wp[BQ[m]]);
+    a0 = SHL_FMA(P[m][0], t, a0);
+    a1 = SHL_FMA(P[m][1], t, a1);
+    a2 = SHL_FMA(P[m][2], t, a2);
+  }
+  out[0][0] = a0;
+  out[0][1] = a1;
+  out[0][2] = a2;
+  if (order < 1) return;
+  double d[5][3];
+  SHL_UNROLL
+  for (int q = 0; q < 5; ++q) d[q][0] = d[q][1] = d[q][2] = 0.0;
+  SHL_UNROLL
+  for (int m = 0; m < 15; ++m) {
+    const int p = BP[m], q = BQ[m];
+    if (p >= 1) {
+      const double t = SHL_MUL((double)p, SHL_MUL(vp[p - 1], wp[q]));
+      for (int c = 0; c < 3; ++c) d[0][c] = SHL_FMA(P[m][c], t, d[0][c]);
+    }
+    if (q >= 1) {
+      const double t = SHL_MUL((double)q, SHL_MUL(vp[p], wp[q - 1]));
+      for (int c = 0; c < 3; ++c) d[1][c] = SHL_FMA(P[m][c], t, d[1][c]);
+    }
+    if (order < 2) continue;
+    if (p >= 2) {
+      const double t = SHL_MUL((double)(p * (p - 1)), SHL_MUL(vp[p - 2], wp[q]));
+      for (int c = 0; c < 3; ++c) d[2][c] = SHL_FMA(P[m][c], t, d[2][c]);
+    }
+    if (q >= 2) {
+      const double t = SHL_MUL((double)(q * (q - 1)), SHL_MUL(vp[p], wp[q - 2]));
+      for (int c = 0; c < 3; ++c) d[3][c] = SHL_FMA(P[m][c], t, d[3][c]);
+    }
+    if (p >= 1 && q >= 1) {
+      const double t = SHL_MUL((double)(p * q), SHL_MUL(vp[p - 1], wp[q - 1]));
+      for (int c = 0; c < 3; ++c) d[4][c] = SHL_FMA(P[m][c], t, d[4][c]);
+    }
+  }
+  const double j2 = SHL_MUL(j1, j1);
+  for (int c = 0; c < 3; ++c) {
+    out[1][c] = SHL_MUL(d[0][c], j1);
+    out[2][c] = SHL_MUL(d[1][c], j1);
+  }
+  if (order < 2) return;
+  for (int c = 0; c < 3; ++c) {
+    out[3][c] = SHL_MUL(d[2][c], j2);
+    out[4][c] = SHL_MUL(d[3][c], j2);
+    out[5][c] = SHL_MUL(d[4][c], j2);
+  }
+}
+
+/* Limit surface of a patch at (v, w) (outputs as shl_limit_poly).  An
+ * irregular patch is evaluated in the regular child of the n-th subdivision
+ * step that holds (v, w), whose control points are table rows of the patch
+ * nodes (each formed by fused multiply-adds over the nonzero weights). */
 SHL_HD void shl_limit_eval(const shl_limit_patch* pt, double v, double w, int order, double out[6][3])
 {
+  double P[15][3];
   double j1 = 1.0;
-  int n = 0, k = 0;
-  if (pt->N != 6) {
-    n = shl_rescale_irregular(&v, &w);
+  if (pt->N == 6) {
+    shl_limit_coeffs_regular(pt, P);
+  } else {
+    const int n = shl_rescale_irregular(&v, &w);
+    int k;
     if (v > 0.5) {
       k = 0;
       v = SHL_SUB(SHL_MUL(2.0, v), 1.0);
@@ -138,34 +257,12 @@ SHL_HD void shl_limit_eval(const shl_limit_patch* pt, double v, double w, int or
       w = SHL_SUB(1.0, SHL_MUL(2.0, w));
       j1 = -ldexp(1.0, n);
     }
-  }
-  SHL_TABLE signed char BC[12][15] = SHL_BOX_COEFFS;
-  SHL_TABLE signed char BP[15] = SHL_BOX_P;
-  SHL_TABLE signed char BQ[15] = SHL_BOX_Q;
-  SHL_TABLE signed char SLOT[12] = SHL_STAM_SLOT;
-  const int np = pt->N + 6;
-  const double* T = pt->N == 6 ? 0 : pt->tab + (size_t)((n - 1) * 3 + k) * 12 * (size_t)np;
-  double vp[5], wp[5];
-  vp[0] = 1.0;
-  wp[0] = 1.0;
-  for (int i = 1; i < 5; ++i) {
-    vp[i] = SHL_MUL(vp[i - 1], v);
-    wp[i] = SHL_MUL(wp[i - 1], w);
-  }
-  const int nq = order >= 2 ? 6 : (order >= 1 ? 3 : 1);
-  double acc[6][3];
-  for (int q = 0; q < 6; ++q) acc[q][0] = acc[q][1] = acc[q][2] = 0.0;
-  SHL_UNROLL
-  for (int s = 0; s < 12; ++s) {
-    /* control point s */
-    double Q0, Q1, Q2;
-    if (T == 0) {
-      const double* x = pt->base + 3 * (size_t)pt->ids[(size_t)SLOT[s] * pt->stride];
-      Q0 = x[0];
-      Q1 = x[1];
-      Q2 = x[2];
-    } else {
-      Q0 = Q1 = Q2 = 0.0;
+    const int np = pt->N + 6;
+    const double* T = pt->tab + (size_t)((n - 1) * 3 + k) * 12 * (size_t)np;
+    for (int m = 0; m < 15; ++m) P[m][0] = P[m][1] = P[m][2] = 0.0;
+    SHL_UNROLL
+    for (int s = 0; s < 12; ++s) {
+      double Q0 = 0.0, Q1 = 0.0, Q2 = 0.0;
       for (int j = 0; j < np; ++j) {
         const double t = T[s * np + j];
         if (t == 0.0) continue;
@@ -174,38 +271,11 @@ SHL_HD void shl_limit_eval(const shl_limit_patch* pt, double v, double w, int or
         Q1 = SHL_FMA(t, x[1], Q1);
         Q2 = SHL_FMA(t, x[2], Q2);
       }
+      shl_limit_add_point(P, s, Q0, Q1, Q2);
     }
-    /* box spline s and its derivatives, times 12 */
-    double bs[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
-    SHL_UNROLL
-    for (int m = 0; m < 15; ++m) {
-      const int c = BC[s][m];
-      if (c == 0) continue;
-      const int p = BP[m], q = BQ[m];
-      bs[0] = SHL_FMA((double)c, SHL_MUL(vp[p], wp[q]), bs[0]);
-      if (nq > 1) {
-        if (p >= 1) bs[1] = SHL_FMA((double)(c * p), SHL_MUL(vp[p - 1], wp[q]), bs[1]);
-        if (q >= 1) bs[2] = SHL_FMA((double)(c * q), SHL_MUL(vp[p], wp[q - 1]), bs[2]);
-      }
-      if (nq > 3) {
-        if (p >= 2) bs[3] = SHL_FMA((double)(c * p * (p - 1)), SHL_MUL(vp[p - 2], wp[q]), bs[3]);
-        if (q >= 2) bs[4] = SHL_FMA((double)(c * q * (q - 1)), SHL_MUL(vp[p], wp[q - 2]), bs[4]);
-        if (p >= 1 && q >= 1) bs[5] = SHL_FMA((double)(c * p * q), SHL_MUL(vp[p - 1], wp[q - 1]), bs[5]);
-      }
-    }
-    SHL_UNROLL
-    for (int q = 0; q < 6; ++q) {
-      if (q >= nq) break;
-      acc[q][0] = SHL_FMA(bs[q], Q0, acc[q][0]);
-      acc[q][1] = SHL_FMA(bs[q], Q1, acc[q][1]);
-      acc[q][2] = SHL_FMA(bs[q], Q2, acc[q][2]);
-    }
+    shl_limit_scale(P);
   }
-  const double twelfth = 1.0 / 12.0;
-  for (int q = 0; q < nq; ++q) {
-    const double sc = q == 0 ? twelfth : (q < 3 ? SHL_MUL(j1, twelfth) : SHL_MUL(SHL_MUL(j1, j1), twelfth));
-    for (int c = 0; c < 3; ++c) out[q][c] = SHL_MUL(acc[q][c], sc);
-  }
+  shl_limit_poly(P, v, w, order, j1, out);
 }
 
 
