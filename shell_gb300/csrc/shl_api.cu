@@ -568,6 +568,10 @@ shl_status create_common(shl_ctx* c, const std::vector<double>& pscale_orig, shl
     g_err = std::string("element kernel attributes: ") + cudaGetErrorString(e);
     return fail(SHL_ERR_CUDA);
   }
+  if (cudaError_t e = init_contact_kernels(); e != cudaSuccess) {
+    g_err = std::string("contact kernel attributes: ") + cudaGetErrorString(e);
+    return fail(SHL_ERR_CUDA);
+  }
   const Setup& S = c->S;
   const uint32_t V = S.V, F = S.F;
   DevBuf& b = c->b;

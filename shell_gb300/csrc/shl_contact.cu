@@ -873,11 +873,9 @@ __global__ void __launch_bounds__(kBlock) k_rb_scatter_new(DevBuf b, StepConst s
 }
 
 // -------------------------------------------------------------- assemble --
-__global__ void __launch_bounds__(kBlock) k_rb_assemble(DevBuf b, StepConst sc) {
-  Ctl* ctl = b.ctl;
-  if (rb_off(ctl)) return;
-  const uint32_t e1 = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e1 >= sc.F) return;
+// one face's segment of the new list, serially: the face's new pairs sorted
+// by e2 in place (insertion sort), merged with its kept old pairs
+__device__ void assemble_serial(const DevBuf& b, const StepConst& sc, uint32_t e1) {
   uint32_t dst = b.pair_ptr[1][e1];
   const uint32_t o0 = b.pair_ptr[0][e1], o1 = b.pair_ptr[0][e1 + 1];
   const uint32_t nn = b.new_cnt[e1];
@@ -885,7 +883,6 @@ __global__ void __launch_bounds__(kBlock) k_rb_assemble(DevBuf b, StepConst sc) 
   uint32_t* ne2 = b.new_e2 + off;
   double* nd2 = b.new_d2 + off;
   double* nx = sc.smooth ? b.new_x + 4 * (size_t)off : nullptr;
-  // insertion sort of this face's new pairs by e2 (the segment belongs to this thread)
   for (uint32_t k = 1; k < nn; ++k) {
     const uint32_t x = ne2[k];
     const double d = nd2[k];
@@ -930,6 +927,108 @@ __global__ void __launch_bounds__(kBlock) k_rb_assemble(DevBuf b, StepConst sc) 
       ++in;
     }
     ++dst;
+  }
+}
+
+// The new list, face by face (segments of eid1): the kept old pairs (in e2
+// order already) merged with the face's new pairs sorted by e2, a new pair
+// before an old one of the same e2.  One warp per face: the new pairs' keys
+// (e2, index) are sorted in shared memory (bitonic), and every pair's place
+// follows from ranks, an old pair's = its rank among the kept old ones + the
+// new pairs of e2 <= its e2, a new pair's = its rank among the new ones + the
+// kept old pairs of e2 < its e2; the same list as the serial merge, which
+// takes a face with more than kAsmCap old or new pairs.
+constexpr int kAsmWarps = 4;
+constexpr uint32_t kAsmCap = 512;
+__global__ void __launch_bounds__(32 * kAsmWarps) k_rb_assemble(DevBuf b, StepConst sc) {
+  Ctl* ctl = b.ctl;
+  if (rb_off(ctl)) return;
+  __shared__ unsigned long long skey[kAsmWarps][kAsmCap];
+  __shared__ uint32_t skept[kAsmWarps][kAsmCap + 1];
+  const uint32_t lane = threadIdx.x & 31u, w = threadIdx.x >> 5;
+  unsigned long long* key = skey[w];
+  uint32_t* kept = skept[w];
+  for (uint32_t e1 = blockIdx.x * kAsmWarps + w; e1 < sc.F; e1 += gridDim.x * kAsmWarps) {
+    const uint32_t o0 = b.pair_ptr[0][e1], o1 = b.pair_ptr[0][e1 + 1];
+    const uint32_t no = o1 - o0;
+    const uint32_t nn = b.new_cnt[e1];
+    if (nn > kAsmCap || no > kAsmCap) {
+      if (lane == 0) assemble_serial(b, sc, e1);
+      __syncwarp();
+      continue;
+    }
+    const uint32_t dst = b.pair_ptr[1][e1];
+    const uint32_t off = nn ? b.new_off[e1] : 0u;
+    // the new pairs' keys, sorted
+    uint32_t P = 32;
+    while (P < nn) P <<= 1;
+    for (uint32_t i = lane; i < P; i += 32)
+      key[i] = i < nn ? ((unsigned long long)b.new_e2[off + i] << 32) | i : ~0ull;
+    __syncwarp();
+    if (nn > 1)
+      for (uint32_t k = 2; k <= P; k <<= 1)
+        for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+          for (uint32_t t = lane; t < P / 2; t += 32) {
+            const uint32_t i = ((t & ~(j - 1)) << 1) | (t & (j - 1));
+            const unsigned long long x = key[i], y = key[i + j];
+            if (((i & k) == 0) == (x > y)) {
+              key[i] = y;
+              key[i + j] = x;
+            }
+          }
+          __syncwarp();
+        }
+    // kept old pairs before each old position (exclusive prefix count)
+    uint32_t run = 0;
+    for (uint32_t base = 0; base < no; base += 32) {
+      const uint32_t i = base + lane;
+      const bool kp = i < no && b.pkeep[o0 + i];
+      const unsigned m = __ballot_sync(0xffffffffu, kp);
+      if (i < no) kept[i] = run + (uint32_t)__popc(m & ((1u << lane) - 1u));
+      run += (uint32_t)__popc(m);
+    }
+    if (lane == 0) kept[no] = run;
+    __syncwarp();
+    // kept old pairs
+    for (uint32_t i = lane; i < no; i += 32) {
+      const uint32_t io = o0 + i;
+      if (!b.pkeep[io]) continue;
+      const uint32_t x = b.pe2[0][io];
+      uint32_t lo = 0, hi = nn;  // new pairs with e2 <= x
+      while (lo < hi) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if ((uint32_t)(key[mid] >> 32) <= x) lo = mid + 1;
+        else hi = mid;
+      }
+      const uint32_t d = dst + kept[i] + lo;
+      b.pe1[1][d] = e1;
+      b.pe2[1][d] = x;
+      b.pstick[1][d] = b.pstick[0][io];
+      b.pd2[1][d] = b.pd2[0][io];
+      for (int c = 0; c < 3; ++c) b.porig[1][3 * (size_t)d + c] = b.porig[0][3 * (size_t)io + c];
+      if (sc.smooth)
+        for (int c = 0; c < 4; ++c) b.pvw[1][4 * (size_t)d + c] = b.pvw[0][4 * (size_t)io + c];
+    }
+    // new pairs
+    for (uint32_t r = lane; r < nn; r += 32) {
+      const unsigned long long kr = key[r];
+      const uint32_t x = (uint32_t)(kr >> 32), k = off + (uint32_t)(kr & 0xffffffffu);
+      uint32_t lo = 0, hi = no;  // old pairs (kept or not) with e2 < x
+      while (lo < hi) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (b.pe2[0][o0 + mid] < x) lo = mid + 1;
+        else hi = mid;
+      }
+      const uint32_t d = dst + r + kept[lo];
+      b.pe1[1][d] = e1;
+      b.pe2[1][d] = x;
+      b.pstick[1][d] = 0;
+      b.pd2[1][d] = b.new_d2[k];
+      for (int c = 0; c < 3; ++c) b.porig[1][3 * (size_t)d + c] = 0.0;
+      if (sc.smooth)
+        for (int c = 0; c < 4; ++c) b.pvw[1][4 * (size_t)d + c] = b.new_x[4 * (size_t)k + c];
+    }
+    __syncwarp();
   }
 }
 
@@ -1001,13 +1100,62 @@ __global__ void k_csr_fill(DevBuf b, StepConst sc) {
   }
 }
 
-// sort each node's entries (deterministic order for the gather): one warp per
-// node, a bitonic sort of the entries padded to a power of two in shared
-// memory (a node has a few hundred entries in a contact-heavy state, about a
-// thousand with SMOOTH contact); a node with more than kCsrSortCap entries is
-// sorted in place by one lane
+// sort each node's entries (deterministic order for the gather): a bitonic
+// sort of the entries padded to a power of two in shared memory, by one warp
+// for a node of up to kCsrSortCap entries (a few hundred in a contact-heavy
+// state, about a thousand with SMOOTH contact), by a block of k_csr_sort_big
+// up to kCsrSortBigCap, in place by one thread beyond
 constexpr int kCsrSortWarps = 4;
 constexpr uint32_t kCsrSortCap = 2048;
+constexpr uint32_t kCsrSortBigCap = 16384;
+constexpr int kCsrSortBigBlock = 1024;
+
+__device__ void csr_sort_serial(const DevBuf& b, uint32_t k0, uint32_t k1) {
+  for (uint32_t k = k0 + 1; k < k1; ++k) {
+    const uint32_t x = b.csr_ent[k];
+    uint32_t q = k;
+    while (q > k0 && b.csr_ent[q - 1] > x) {
+      b.csr_ent[q] = b.csr_ent[q - 1];
+      --q;
+    }
+    b.csr_ent[q] = x;
+  }
+}
+
+__global__ void __launch_bounds__(kCsrSortBigBlock) k_csr_sort_big(DevBuf b, StepConst sc) {
+  Ctl* ctl = b.ctl;
+  if (csr_off(ctl)) return;
+  extern __shared__ uint32_t big[];
+  for (uint32_t nd = blockIdx.x; nd < sc.V; nd += gridDim.x) {
+    const uint32_t k0 = b.csr_ptr[nd], k1 = b.csr_ptr[nd + 1];
+    const uint32_t n = k1 - k0;
+    if (n <= kCsrSortCap) continue;
+    if (n > kCsrSortBigCap) {
+      if (threadIdx.x == 0) csr_sort_serial(b, k0, k1);
+      __syncthreads();
+      continue;
+    }
+    uint32_t P = kCsrSortCap;
+    while (P < n) P <<= 1;
+    for (uint32_t i = threadIdx.x; i < P; i += blockDim.x) big[i] = i < n ? b.csr_ent[k0 + i] : 0xffffffffu;
+    __syncthreads();
+    for (uint32_t k = 2; k <= P; k <<= 1)
+      for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+        for (uint32_t t = threadIdx.x; t < P / 2; t += blockDim.x) {
+          const uint32_t i = ((t & ~(j - 1)) << 1) | (t & (j - 1));
+          const uint32_t x = big[i], y = big[i + j];
+          if (((i & k) == 0) == (x > y)) {
+            big[i] = y;
+            big[i + j] = x;
+          }
+        }
+        __syncthreads();
+      }
+    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) b.csr_ent[k0 + i] = big[i];
+    __syncthreads();
+  }
+}
+
 __global__ void __launch_bounds__(32 * kCsrSortWarps) k_csr_sort(DevBuf b, StepConst sc) {
   Ctl* ctl = b.ctl;
   if (csr_off(ctl)) return;
@@ -1017,21 +1165,7 @@ __global__ void __launch_bounds__(32 * kCsrSortWarps) k_csr_sort(DevBuf b, StepC
   for (uint32_t nd = blockIdx.x * kCsrSortWarps + w; nd < sc.V; nd += gridDim.x * kCsrSortWarps) {
     const uint32_t k0 = b.csr_ptr[nd], k1 = b.csr_ptr[nd + 1];
     const uint32_t n = k1 - k0;
-    if (n < 2) continue;
-    if (n > kCsrSortCap) {
-      if (lane == 0)
-        for (uint32_t k = k0 + 1; k < k1; ++k) {
-          const uint32_t x = b.csr_ent[k];
-          uint32_t q = k;
-          while (q > k0 && b.csr_ent[q - 1] > x) {
-            b.csr_ent[q] = b.csr_ent[q - 1];
-            --q;
-          }
-          b.csr_ent[q] = x;
-        }
-      __syncwarp();
-      continue;
-    }
+    if (n < 2 || n > kCsrSortCap) continue;
     uint32_t P = 32;
     while (P < n) P <<= 1;
     for (uint32_t i = lane; i < P; i += 32) sh[i] = i < n ? b.csr_ent[k0 + i] : 0xffffffffu;
@@ -1086,6 +1220,13 @@ void launch_smooth_search(const DevBuf& b, const StepConst& sc, bool rebuild, cu
     k_smooth_search<false><<<search_grid<false>(), kSearchBlock, 0, s>>>(b, sc);
 }
 
+// k_csr_sort_big takes more than the default 48 KB of shared memory; called
+// once per device before its first launch
+cudaError_t init_contact_kernels() {
+  return cudaFuncSetAttribute((const void*)k_csr_sort_big, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)(kCsrSortBigCap * 4));
+}
+
 void launch_contact_csr(const DevBuf& b, const StepConst& sc, cudaStream_t s) {
   const uint32_t gV = nblk(sc.V);
   uint32_t gP = nblk(sc.pairs_cap);
@@ -1099,6 +1240,7 @@ void launch_contact_csr(const DevBuf& b, const StepConst& sc, cudaStream_t s) {
     uint32_t g = (sc.V + kCsrSortWarps - 1) / kCsrSortWarps;
     if (g > 16 * 152) g = 16 * 152;
     k_csr_sort<<<g ? g : 1, 32 * kCsrSortWarps, 0, s>>>(b, sc);
+    k_csr_sort_big<<<152, kCsrSortBigBlock, kCsrSortBigCap * 4, s>>>(b, sc);
   }
   k_csr_finish<<<1, 1, 0, s>>>(b);
 }
@@ -1139,7 +1281,11 @@ void launch_rebuild(const DevBuf& b, const StepConst& sc, cudaStream_t s) {
   }
   launch_scan(&b.ctl->rebuild, b.ctl, b.seg_count, b.pair_ptr[1], nullptr, sc.F, sc.F, b.scan_block, &b.ctl->n_next,
               true, sc.pairs_cap, true, s);
-  k_rb_assemble<<<gF, kBlock, 0, s>>>(b, sc);
+  {
+    uint32_t g = (sc.F + kAsmWarps - 1) / kAsmWarps;
+    if (g > 16 * 152) g = 16 * 152;
+    k_rb_assemble<<<g ? g : 1, 32 * kAsmWarps, 0, s>>>(b, sc);
+  }
   {
     uint32_t g = nblk(sc.pairs_cap > sc.F + 1 ? sc.pairs_cap : sc.F + 1);
     if (g > 8 * 152) g = 8 * 152;

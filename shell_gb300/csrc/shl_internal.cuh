@@ -347,6 +347,7 @@ void launch_positions(const DevBuf& b, const StepConst& sc, cudaStream_t s);
 void launch_state_host(const DevBuf& b, const StepConst& sc, double* hu, double* hv, double* ha, bool load,
                        cudaStream_t s);
 cudaError_t init_element_kernels();
+cudaError_t init_contact_kernels();
 enum : uint32_t { kCtlReset = 1u, kCtlTable = 2u, kCtlArm = 4u };
 void launch_ctl_begin(Ctl* ctl, uint32_t n, uint32_t flags, cudaStream_t s);
 void launch_fp64_peak(double* out, int blocks, int iters, cudaStream_t s);
