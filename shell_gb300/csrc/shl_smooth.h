@@ -170,57 +170,51 @@ SHL_HD double shl_smooth_f_from(const double e1[6][3], const double e2[6][3], do
 
 /* Newton direction on the free subspace of the working set (Z columns), the
  * reduced Hessian shifted by mu I until its Cholesky factorisation succeeds.
- * Returns 1 when a shift was needed (f is not convex on the free subspace). */
+ * Returns 1 when a shift was needed (f is not convex on the free subspace).
+ * The columns of Z are unit vectors e_k (a free coordinate) or e_k - e_(k+1)
+ * (along an active edge v + w = 1), so the reduced gradient Z^T g and Hessian
+ * Z^T H Z are single entries or differences: each is formed as the sum over
+ * the four coordinates from zero would round it (the zero products add
+ * nothing; a zero result is +0). */
 SHL_HD int shl_smooth_direction(const double* g, double H[4][4], const unsigned* work, double* d)
 {
-  double Z[4][4];
+  int zk[4], zd[4];  /* column a of Z: e_zk, minus e_(zk+1) when zd */
   int m = 0;
   for (int t = 0; t < 2; ++t) {
     const unsigned wk = work[t];
-    double z0[4] = {0, 0, 0, 0}, z1[4] = {0, 0, 0, 0};
-    int nz = 0;
     if (wk == 0) {
-      z0[2 * t] = 1.0;
-      z1[2 * t + 1] = 1.0;
-      nz = 2;
+      zk[m] = 2 * t;
+      zd[m++] = 0;
+      zk[m] = 2 * t + 1;
+      zd[m++] = 0;
     } else if (wk == 1u) {  /* v = 0: w free */
-      z0[2 * t + 1] = 1.0;
-      nz = 1;
+      zk[m] = 2 * t + 1;
+      zd[m++] = 0;
     } else if (wk == 2u) {  /* w = 0: v free */
-      z0[2 * t] = 1.0;
-      nz = 1;
+      zk[m] = 2 * t;
+      zd[m++] = 0;
     } else if (wk == 4u) {  /* v + w = 1: along (1, -1) */
-      z0[2 * t] = 1.0;
-      z0[2 * t + 1] = -1.0;
-      nz = 1;
-    }
-    if (nz >= 1) {
-      for (int i = 0; i < 4; ++i) Z[m][i] = z0[i];
-      ++m;
-    }
-    if (nz == 2) {
-      for (int i = 0; i < 4; ++i) Z[m][i] = z1[i];
-      ++m;
+      zk[m] = 2 * t;
+      zd[m++] = 1;
     }
   }
   for (int i = 0; i < 4; ++i) d[i] = 0.0;
   if (m == 0) return 0;
   double Hr[4][4], gr[4], HZ[4][4];
   for (int a = 0; a < m; ++a) {
-    double s = 0.0;
-    for (int i = 0; i < 4; ++i) s = SHL_ADD(s, SHL_MUL(Z[a][i], g[i]));
-    gr[a] = s;
+    const int k = zk[a];
+    gr[a] = SHL_ADD(0.0, g[k]);
+    if (zd[a]) gr[a] = SHL_SUB(gr[a], g[k + 1]);
     for (int i = 0; i < 4; ++i) {
-      double t = 0.0;
-      for (int j = 0; j < 4; ++j) t = SHL_ADD(t, SHL_MUL(H[i][j], Z[a][j]));
-      HZ[a][i] = t;
+      HZ[a][i] = SHL_ADD(0.0, H[i][k]);
+      if (zd[a]) HZ[a][i] = SHL_SUB(HZ[a][i], H[i][k + 1]);
     }
   }
   for (int a = 0; a < m; ++a)
     for (int b = 0; b < m; ++b) {
-      double s = 0.0;
-      for (int i = 0; i < 4; ++i) s = SHL_ADD(s, SHL_MUL(Z[a][i], HZ[b][i]));
-      Hr[a][b] = s;
+      const int k = zk[a];
+      Hr[a][b] = SHL_ADD(0.0, HZ[b][k]);
+      if (zd[a]) Hr[a][b] = SHL_SUB(Hr[a][b], HZ[b][k + 1]);
     }
   /* Jacobi scaling: the free directions can differ in scale by many orders
    * (the limit surface's parametric derivatives grow like 2^n next to an
@@ -261,20 +255,21 @@ SHL_HD int shl_smooth_direction(const double* g, double H[4][4], const unsigned*
         for (int k = a + 1; k < m; ++k) s = SHL_SUB(s, SHL_MUL(L[k][a], y[k]));
         y[a] = SHL_DIV(s, L[a][a]);
       }
-      for (int i = 0; i < 4; ++i) {
-        double s = 0.0;
-        for (int a = 0; a < m; ++a) s = SHL_ADD(s, SHL_MUL(Z[a][i], SHL_MUL(S[a], y[a])));
-        d[i] = s;
+      /* d = Z S y: each coordinate is one column's share (or +0) */
+      for (int a = 0; a < m; ++a) {
+        const double sy = SHL_MUL(S[a], y[a]);
+        d[zk[a]] = SHL_ADD(0.0, sy);
+        if (zd[a]) d[zk[a] + 1] = SHL_ADD(0.0, -sy);
       }
       return mu > 0.0 ? 1 : 0;
     }
     mu = mu == 0.0 ? 1e-10 : SHL_MUL(mu, 10.0);
   }
   /* not reached for finite input: scaled projected steepest descent */
-  for (int i = 0; i < 4; ++i) {
-    double s = 0.0;
-    for (int a = 0; a < m; ++a) s = SHL_ADD(s, SHL_MUL(Z[a][i], SHL_MUL(S[a], -gr[a])));
-    d[i] = s;
+  for (int a = 0; a < m; ++a) {
+    const double sg = SHL_MUL(S[a], -gr[a]);
+    d[zk[a]] = SHL_ADD(0.0, sg);
+    if (zd[a]) d[zk[a] + 1] = SHL_ADD(0.0, -sg);
   }
   return 1;
 }
