@@ -948,87 +948,99 @@ __global__ void __launch_bounds__(32 * kAsmWarps) k_rb_assemble(DevBuf b, StepCo
   const uint32_t lane = threadIdx.x & 31u, w = threadIdx.x >> 5;
   unsigned long long* key = skey[w];
   uint32_t* kept = skept[w];
-  for (uint32_t e1 = blockIdx.x * kAsmWarps + w; e1 < sc.F; e1 += gridDim.x * kAsmWarps) {
-    const uint32_t o0 = b.pair_ptr[0][e1], o1 = b.pair_ptr[0][e1 + 1];
-    const uint32_t no = o1 - o0;
-    const uint32_t nn = b.new_cnt[e1];
-    if (nn > kAsmCap || no > kAsmCap) {
-      if (lane == 0) assemble_serial(b, sc, e1);
+  // each warp reads the segments of 32 consecutive faces at once and merges
+  // the faces that have old or new pairs, one after the other
+  for (uint32_t fbase = (blockIdx.x * kAsmWarps + w) * 32; fbase < sc.F; fbase += gridDim.x * kAsmWarps * 32) {
+    const uint32_t mine = fbase + lane;
+    uint32_t my_o0 = 0, my_no = 0, my_nn = 0;
+    if (mine < sc.F) {
+      my_o0 = b.pair_ptr[0][mine];
+      my_no = b.pair_ptr[0][mine + 1] - my_o0;
+      my_nn = b.new_cnt[mine];
+    }
+    const bool big = my_nn > kAsmCap || my_no > kAsmCap;
+    if (big) assemble_serial(b, sc, mine);
+    unsigned todo = __ballot_sync(0xffffffffu, !big && (my_no > 0 || my_nn > 0));
+    while (todo) {
+      const int src = __ffs(todo) - 1;
+      todo &= todo - 1;
+      const uint32_t e1 = fbase + (uint32_t)src;
+      const uint32_t o0 = __shfl_sync(0xffffffffu, my_o0, src);
+      const uint32_t no = __shfl_sync(0xffffffffu, my_no, src);
+      const uint32_t nn = __shfl_sync(0xffffffffu, my_nn, src);
+      const uint32_t dst = b.pair_ptr[1][e1];
+      const uint32_t off = nn ? b.new_off[e1] : 0u;
+      // the new pairs' keys, sorted
+      uint32_t P = 32;
+      while (P < nn) P <<= 1;
+      for (uint32_t i = lane; i < P; i += 32)
+        key[i] = i < nn ? ((unsigned long long)b.new_e2[off + i] << 32) | i : ~0ull;
       __syncwarp();
-      continue;
-    }
-    const uint32_t dst = b.pair_ptr[1][e1];
-    const uint32_t off = nn ? b.new_off[e1] : 0u;
-    // the new pairs' keys, sorted
-    uint32_t P = 32;
-    while (P < nn) P <<= 1;
-    for (uint32_t i = lane; i < P; i += 32)
-      key[i] = i < nn ? ((unsigned long long)b.new_e2[off + i] << 32) | i : ~0ull;
-    __syncwarp();
-    if (nn > 1)
-      for (uint32_t k = 2; k <= P; k <<= 1)
-        for (uint32_t j = k >> 1; j > 0; j >>= 1) {
-          for (uint32_t t = lane; t < P / 2; t += 32) {
-            const uint32_t i = ((t & ~(j - 1)) << 1) | (t & (j - 1));
-            const unsigned long long x = key[i], y = key[i + j];
-            if (((i & k) == 0) == (x > y)) {
-              key[i] = y;
-              key[i + j] = x;
+      if (nn > 1)
+        for (uint32_t k = 2; k <= P; k <<= 1)
+          for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+            for (uint32_t t = lane; t < P / 2; t += 32) {
+              const uint32_t i = ((t & ~(j - 1)) << 1) | (t & (j - 1));
+              const unsigned long long x = key[i], y = key[i + j];
+              if (((i & k) == 0) == (x > y)) {
+                key[i] = y;
+                key[i + j] = x;
+              }
             }
+            __syncwarp();
           }
-          __syncwarp();
+      // kept old pairs before each old position (exclusive prefix count)
+      uint32_t run = 0;
+      for (uint32_t base = 0; base < no; base += 32) {
+        const uint32_t i = base + lane;
+        const bool kp = i < no && b.pkeep[o0 + i];
+        const unsigned m = __ballot_sync(0xffffffffu, kp);
+        if (i < no) kept[i] = run + (uint32_t)__popc(m & ((1u << lane) - 1u));
+        run += (uint32_t)__popc(m);
+      }
+      if (lane == 0) kept[no] = run;
+      __syncwarp();
+      // kept old pairs
+      for (uint32_t i = lane; i < no; i += 32) {
+        const uint32_t io = o0 + i;
+        if (!b.pkeep[io]) continue;
+        const uint32_t x = b.pe2[0][io];
+        uint32_t lo = 0, hi = nn;  // new pairs with e2 <= x
+        while (lo < hi) {
+          const uint32_t mid = (lo + hi) >> 1;
+          if ((uint32_t)(key[mid] >> 32) <= x) lo = mid + 1;
+          else hi = mid;
         }
-    // kept old pairs before each old position (exclusive prefix count)
-    uint32_t run = 0;
-    for (uint32_t base = 0; base < no; base += 32) {
-      const uint32_t i = base + lane;
-      const bool kp = i < no && b.pkeep[o0 + i];
-      const unsigned m = __ballot_sync(0xffffffffu, kp);
-      if (i < no) kept[i] = run + (uint32_t)__popc(m & ((1u << lane) - 1u));
-      run += (uint32_t)__popc(m);
-    }
-    if (lane == 0) kept[no] = run;
-    __syncwarp();
-    // kept old pairs
-    for (uint32_t i = lane; i < no; i += 32) {
-      const uint32_t io = o0 + i;
-      if (!b.pkeep[io]) continue;
-      const uint32_t x = b.pe2[0][io];
-      uint32_t lo = 0, hi = nn;  // new pairs with e2 <= x
-      while (lo < hi) {
-        const uint32_t mid = (lo + hi) >> 1;
-        if ((uint32_t)(key[mid] >> 32) <= x) lo = mid + 1;
-        else hi = mid;
+        const uint32_t d = dst + kept[i] + lo;
+        b.pe1[1][d] = e1;
+        b.pe2[1][d] = x;
+        b.pstick[1][d] = b.pstick[0][io];
+        b.pd2[1][d] = b.pd2[0][io];
+        for (int c = 0; c < 3; ++c) b.porig[1][3 * (size_t)d + c] = b.porig[0][3 * (size_t)io + c];
+        if (sc.smooth)
+          for (int c = 0; c < 4; ++c) b.pvw[1][4 * (size_t)d + c] = b.pvw[0][4 * (size_t)io + c];
       }
-      const uint32_t d = dst + kept[i] + lo;
-      b.pe1[1][d] = e1;
-      b.pe2[1][d] = x;
-      b.pstick[1][d] = b.pstick[0][io];
-      b.pd2[1][d] = b.pd2[0][io];
-      for (int c = 0; c < 3; ++c) b.porig[1][3 * (size_t)d + c] = b.porig[0][3 * (size_t)io + c];
-      if (sc.smooth)
-        for (int c = 0; c < 4; ++c) b.pvw[1][4 * (size_t)d + c] = b.pvw[0][4 * (size_t)io + c];
-    }
-    // new pairs
-    for (uint32_t r = lane; r < nn; r += 32) {
-      const unsigned long long kr = key[r];
-      const uint32_t x = (uint32_t)(kr >> 32), k = off + (uint32_t)(kr & 0xffffffffu);
-      uint32_t lo = 0, hi = no;  // old pairs (kept or not) with e2 < x
-      while (lo < hi) {
-        const uint32_t mid = (lo + hi) >> 1;
-        if (b.pe2[0][o0 + mid] < x) lo = mid + 1;
-        else hi = mid;
+      // new pairs
+      for (uint32_t r = lane; r < nn; r += 32) {
+        const unsigned long long kr = key[r];
+        const uint32_t x = (uint32_t)(kr >> 32), k = off + (uint32_t)(kr & 0xffffffffu);
+        uint32_t lo = 0, hi = no;  // old pairs (kept or not) with e2 < x
+        while (lo < hi) {
+          const uint32_t mid = (lo + hi) >> 1;
+          if (b.pe2[0][o0 + mid] < x) lo = mid + 1;
+          else hi = mid;
+        }
+        const uint32_t d = dst + r + kept[lo];
+        b.pe1[1][d] = e1;
+        b.pe2[1][d] = x;
+        b.pstick[1][d] = 0;
+        b.pd2[1][d] = b.new_d2[k];
+        for (int c = 0; c < 3; ++c) b.porig[1][3 * (size_t)d + c] = 0.0;
+        if (sc.smooth)
+          for (int c = 0; c < 4; ++c) b.pvw[1][4 * (size_t)d + c] = b.new_x[4 * (size_t)k + c];
       }
-      const uint32_t d = dst + r + kept[lo];
-      b.pe1[1][d] = e1;
-      b.pe2[1][d] = x;
-      b.pstick[1][d] = 0;
-      b.pd2[1][d] = b.new_d2[k];
-      for (int c = 0; c < 3; ++c) b.porig[1][3 * (size_t)d + c] = 0.0;
-      if (sc.smooth)
-        for (int c = 0; c < 4; ++c) b.pvw[1][4 * (size_t)d + c] = b.new_x[4 * (size_t)k + c];
+      __syncwarp();
     }
-    __syncwarp();
   }
 }
 
@@ -1067,6 +1079,7 @@ __device__ __forceinline__ bool csr_off(const Ctl* ctl) { return ctl->csr_dirty 
 
 __global__ void k_csr_clear(DevBuf b, StepConst sc) {
   if (csr_off(b.ctl)) return;
+  if (blockIdx.x == 0 && threadIdx.x == 0) b.ctl->cnt[9] = 0;  // k_csr_sort's list of large nodes
   const uint32_t stride = gridDim.x * blockDim.x;
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < sc.V; i += stride) {
     b.csr_count[i] = 0;
@@ -1122,14 +1135,16 @@ __device__ void csr_sort_serial(const DevBuf& b, uint32_t k0, uint32_t k1) {
   }
 }
 
+// the nodes that k_csr_sort listed (in csr_fill, free after k_csr_fill; count in ctl->cnt[9])
 __global__ void __launch_bounds__(kCsrSortBigBlock) k_csr_sort_big(DevBuf b, StepConst sc) {
   Ctl* ctl = b.ctl;
   if (csr_off(ctl)) return;
   extern __shared__ uint32_t big[];
-  for (uint32_t nd = blockIdx.x; nd < sc.V; nd += gridDim.x) {
+  const uint32_t n_big = min(ctl->cnt[9], sc.V);
+  for (uint32_t q = blockIdx.x; q < n_big; q += gridDim.x) {
+    const uint32_t nd = b.csr_fill[q];
     const uint32_t k0 = b.csr_ptr[nd], k1 = b.csr_ptr[nd + 1];
     const uint32_t n = k1 - k0;
-    if (n <= kCsrSortCap) continue;
     if (n > kCsrSortBigCap) {
       if (threadIdx.x == 0) csr_sort_serial(b, k0, k1);
       __syncthreads();
@@ -1162,29 +1177,41 @@ __global__ void __launch_bounds__(32 * kCsrSortWarps) k_csr_sort(DevBuf b, StepC
   __shared__ uint32_t buf[kCsrSortWarps][kCsrSortCap];
   const uint32_t lane = threadIdx.x & 31u, w = threadIdx.x >> 5;
   uint32_t* sh = buf[w];
-  for (uint32_t nd = blockIdx.x * kCsrSortWarps + w; nd < sc.V; nd += gridDim.x * kCsrSortWarps) {
-    const uint32_t k0 = b.csr_ptr[nd], k1 = b.csr_ptr[nd + 1];
-    const uint32_t n = k1 - k0;
-    if (n < 2 || n > kCsrSortCap) continue;
-    uint32_t P = 32;
-    while (P < n) P <<= 1;
-    for (uint32_t i = lane; i < P; i += 32) sh[i] = i < n ? b.csr_ent[k0 + i] : 0xffffffffu;
-    __syncwarp();
-    for (uint32_t k = 2; k <= P; k <<= 1)
-      for (uint32_t j = k >> 1; j > 0; j >>= 1) {
-        // compare-exchange t: the pair (i, i + j) with bit j of i clear
-        for (uint32_t t = lane; t < P / 2; t += 32) {
-          const uint32_t i = ((t & ~(j - 1)) << 1) | (t & (j - 1));
-          const uint32_t x = sh[i], y = sh[i + j];
-          if (((i & k) == 0) == (x > y)) {
-            sh[i] = y;
-            sh[i + j] = x;
+  // each warp reads the segments of 32 consecutive nodes at once and sorts the
+  // ones with two or more entries; larger ones than the buffer go to the list
+  for (uint32_t base = (blockIdx.x * kCsrSortWarps + w) * 32; base < sc.V; base += gridDim.x * kCsrSortWarps * 32) {
+    const uint32_t me = base + lane;
+    uint32_t k0 = 0, n = 0;
+    if (me < sc.V) {
+      k0 = b.csr_ptr[me];
+      n = b.csr_ptr[me + 1] - k0;
+    }
+    if (n > kCsrSortCap) b.csr_fill[atomicAdd(&ctl->cnt[9], 1u)] = me;
+    unsigned todo = __ballot_sync(0xffffffffu, n >= 2 && n <= kCsrSortCap);
+    while (todo) {
+      const int src = __ffs(todo) - 1;
+      todo &= todo - 1;
+      const uint32_t s0 = __shfl_sync(0xffffffffu, k0, src), sn = __shfl_sync(0xffffffffu, n, src);
+      uint32_t P = 32;
+      while (P < sn) P <<= 1;
+      for (uint32_t i = lane; i < P; i += 32) sh[i] = i < sn ? b.csr_ent[s0 + i] : 0xffffffffu;
+      __syncwarp();
+      for (uint32_t k = 2; k <= P; k <<= 1)
+        for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+          // compare-exchange t: the pair (i, i + j) with bit j of i clear
+          for (uint32_t t = lane; t < P / 2; t += 32) {
+            const uint32_t i = ((t & ~(j - 1)) << 1) | (t & (j - 1));
+            const uint32_t x = sh[i], y = sh[i + j];
+            if (((i & k) == 0) == (x > y)) {
+              sh[i] = y;
+              sh[i + j] = x;
+            }
           }
+          __syncwarp();
         }
-        __syncwarp();
-      }
-    for (uint32_t i = lane; i < n; i += 32) b.csr_ent[k0 + i] = sh[i];
-    __syncwarp();
+      for (uint32_t i = lane; i < sn; i += 32) b.csr_ent[s0 + i] = sh[i];
+      __syncwarp();
+    }
   }
 }
 
@@ -1237,7 +1264,7 @@ void launch_contact_csr(const DevBuf& b, const StepConst& sc, cudaStream_t s) {
               true, sc.csr_cap, true, s);
   k_csr_fill<<<gP, kBlock, 0, s>>>(b, sc);
   {
-    uint32_t g = (sc.V + kCsrSortWarps - 1) / kCsrSortWarps;
+    uint32_t g = (sc.V + 32 * kCsrSortWarps - 1) / (32 * kCsrSortWarps);
     if (g > 16 * 152) g = 16 * 152;
     k_csr_sort<<<g ? g : 1, 32 * kCsrSortWarps, 0, s>>>(b, sc);
     k_csr_sort_big<<<152, kCsrSortBigBlock, kCsrSortBigCap * 4, s>>>(b, sc);
@@ -1282,7 +1309,7 @@ void launch_rebuild(const DevBuf& b, const StepConst& sc, cudaStream_t s) {
   launch_scan(&b.ctl->rebuild, b.ctl, b.seg_count, b.pair_ptr[1], nullptr, sc.F, sc.F, b.scan_block, &b.ctl->n_next,
               true, sc.pairs_cap, true, s);
   {
-    uint32_t g = (sc.F + kAsmWarps - 1) / kAsmWarps;
+    uint32_t g = (sc.F + 32 * kAsmWarps - 1) / (32 * kAsmWarps);
     if (g > 16 * 152) g = 16 * 152;
     k_rb_assemble<<<g ? g : 1, 32 * kAsmWarps, 0, s>>>(b, sc);
   }
