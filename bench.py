@@ -548,27 +548,40 @@ def timed_sample(g, torch, u0, K, W, flush, dist=None, clock=None):
 
 
 def e2e_sample(g, torch, u0, K, W):
-    """The timed steps through the C ABI with host buffers: per timed step,
-    shl_set_state from pinned host memory, shl_step(1), shl_get_state into
-    pinned host memory; the steps between run untimed."""
+    """The timed steps through the C ABI with host buffers, called as a host
+    program binds it (ctypes calls with the buffers' addresses): per timed
+    step shl_set_state from pinned host memory, shl_step(1) and shl_get_state
+    into pinned host memory; the steps between run untimed."""
+    import ctypes
+
+    from shell_gb300.lib import ShlError, ShlStepReport
+
     S = stride_for(K)
     fresh_start(g, u0)
-    table = pressure(np.arange(1, W + S * K + 1))
+    table = np.ascontiguousarray(pressure(np.arange(1, W + S * K + 1)), dtype=np.float64)
     g.step(W, table[:W])
     u, v, a = g.get_state()
     bufs = [torch.from_numpy(x).pin_memory() for x in (u, v, a)]
     hu, hv, ha = (b.numpy() for b in bufs)
+    lib, h = g.lib, g.h
+    pu, pv, pa = (ctypes.c_void_p(x.ctypes.data) for x in (hu, hv, ha))
+    rep = ShlStepReport()
+    rref = ctypes.byref(rep)
     step, secs = W, 0.0
     for _ in range(K):
         if S > 1:
             g.step(S - 1, table[step:step + S - 1])
             step += S - 1
             g.get_state(out=(hu, hv, ha))  # the host copy of the state before the timed step
+        tp = ctypes.c_void_p(table.ctypes.data + 8 * step)
         t0 = time.perf_counter()
-        g.set_state(hu, hv, ha)
-        g.step(1, table[step:step + 1])
-        g.get_state(out=(hu, hv, ha))
+        s1 = lib.shl_set_state(h, pu, pv, pa)
+        s2 = lib.shl_step(h, 1, tp, 1, rref)
+        s3 = lib.shl_get_state(h, pu, pv, pa)
         secs += time.perf_counter() - t0
+        for st, where in ((s1, "shl_set_state"), (s2, "shl_step"), (s3, "shl_get_state")):
+            if st >= 100 or (st != 0 and where != "shl_step"):
+                raise ShlError(st, where)
         step += 1
     return secs
 

@@ -1020,8 +1020,8 @@ shl_status shl_set_state(shl_ctx* c, const double* u, const double* v, const dou
   double *du = mapped_host(u), *dv = mapped_host(v), *da = mapped_host(a);
   if (du && dv && da) {
     // all three in mapped page-locked memory: one kernel reads them over the host link
+    // and sets the positions
     launch_state_host(c->b, c->sc, du, dv, da, true, c->stream);
-    launch_positions(c->b, c->sc, c->stream);
     SHL_CUDA_TRY(cudaStreamSynchronize(c->stream));
     return check_launch("shl_set_state");
   }

@@ -703,41 +703,52 @@ __global__ void k_begin_step(DevBuf b, StepConst sc, RebuildCond rc) {
   begin_step(ctl, sc, sc.dt, ctl->du2_pred, rc, true);
 }
 
+// positions p = X + u_pred of node n and the packed copies of u_pred that the
+// element kernels read (float pairs; FP32 for the FP32 path)
+__device__ __forceinline__ void set_positions(const DevBuf& b, const StepConst& sc, uint32_t n, const double* up) {
+  float uh[3], ul[3];
+  for (int c = 0; c < 3; ++c) {
+    const size_t k = 3 * (size_t)n + c;
+    b.p[k] = __dadd_rn(b.X[k], up[c]);
+    df_split(up[c], uh[c], ul[c]);
+  }
+  if (sc.fp32) b.up32[n] = make_float4((float)up[0], (float)up[1], (float)up[2], 0.f);
+  b.upk[2 * (size_t)n] = make_float4(uh[0], uh[1], uh[2], 0.f);
+  b.upk[2 * (size_t)n + 1] = make_float4(ul[0], ul[1], ul[2], 0.f);
+}
+
 // The state from (hu, hv, ha) or to them: host memory that the device reads and
 // writes directly (page-locked, mapped), one kernel instead of three copies each
-// way.  Loading also sets u_pred = u and the positions, as k_positions does.
+// way.  Loading (one thread per node) also sets u_pred = u and the positions.
 __global__ void k_state_host(DevBuf b, StepConst sc, double* hu, double* hv, double* ha, int load) {
-  const size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-  const size_t nd = 3 * (size_t)sc.V;
-  if (k >= nd) return;
   if (load) {
-    const double u = hu[k];
-    b.u[k] = u;
-    b.up[k] = u;
-    b.v[k] = hv[k];
-    b.a[k] = ha[k];
-  } else {
-    hu[k] = b.u[k];
-    hv[k] = b.v[k];
-    ha[k] = b.a[k];
+    const uint32_t n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= sc.V) return;
+    double u[3];
+    for (int c = 0; c < 3; ++c) {
+      const size_t k = 3 * (size_t)n + c;
+      u[c] = hu[k];
+      b.u[k] = u[c];
+      b.up[k] = u[c];
+      b.v[k] = hv[k];
+      b.a[k] = ha[k];
+    }
+    set_positions(b, sc, n, u);
+    return;
   }
+  const size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (k >= 3 * (size_t)sc.V) return;
+  hu[k] = b.u[k];
+  hv[k] = b.v[k];
+  ha[k] = b.a[k];
 }
 
 // positions only (p = X + u_pred), for force evaluations at a given state
 __global__ void k_positions(DevBuf b, StepConst sc) {
   const uint32_t n = blockIdx.x * blockDim.x + threadIdx.x;
   if (n >= sc.V) return;
-  float uh[3], ul[3];
-  for (int c = 0; c < 3; ++c) {
-    const size_t k = 3 * (size_t)n + c;
-    b.p[k] = __dadd_rn(b.X[k], b.up[k]);
-    df_split(b.up[k], uh[c], ul[c]);
-  }
-  if (sc.fp32)
-    b.up32[n] = make_float4((float)b.up[3 * (size_t)n], (float)b.up[3 * (size_t)n + 1], (float)b.up[3 * (size_t)n + 2],
-                            0.f);
-  b.upk[2 * (size_t)n] = make_float4(uh[0], uh[1], uh[2], 0.f);
-  b.upk[2 * (size_t)n + 1] = make_float4(ul[0], ul[1], ul[2], 0.f);
+  const double up[3] = {b.up[3 * (size_t)n], b.up[3 * (size_t)n + 1], b.up[3 * (size_t)n + 2]};
+  set_positions(b, sc, n, up);
 }
 
 // ------------------------------------------------------------- elements --
@@ -2268,8 +2279,8 @@ void launch_batch_flags(const DevBuf& b, const StepConst& sc, int mode, cudaStre
 }
 void launch_state_host(const DevBuf& b, const StepConst& sc, double* hu, double* hv, double* ha, bool load,
                        cudaStream_t s) {
-  const size_t nd = 3 * (size_t)sc.V;
-  k_state_host<<<(unsigned)((nd + kBlock - 1) / kBlock), kBlock, 0, s>>>(b, sc, hu, hv, ha, load ? 1 : 0);
+  const size_t n = load ? (size_t)sc.V : 3 * (size_t)sc.V;  // load: one thread per node
+  k_state_host<<<(unsigned)((n + kBlock - 1) / kBlock), kBlock, 0, s>>>(b, sc, hu, hv, ha, load ? 1 : 0);
 }
 void launch_positions(const DevBuf& b, const StepConst& sc, cudaStream_t s) {
   k_positions<<<nblk(sc.V), kBlock, 0, s>>>(b, sc);
