@@ -676,7 +676,7 @@ shl_status create_common(shl_ctx* c, const std::vector<double>& pscale_orig, shl
                                             1u << 30);
     ALLOC(b.close_ptr, F + 1);
     ALLOC(b.close_list, S.close_list.size());
-    ALLOC(b.bmin, 3 * (size_t)F); ALLOC(b.bmax, 3 * (size_t)F); ALLOC(b.fsize, F);
+    ALLOC(b.bmin, 3 * (size_t)F); ALLOC(b.bmax, 3 * (size_t)F); ALLOC(b.fsize, F); ALLOC(b.sum_lanes, SHL_SUM_LANES);
     ALLOC(b.cell_lo, 3 * (size_t)F); ALLOC(b.cell_hi, 3 * (size_t)F);
     ALLOC(b.cell_count, n_cells_cap); ALLOC(b.cell_start, n_cells_cap + 1); ALLOC(b.cell_fill, n_cells_cap);
     ALLOC(b.cell_items, entries_cap);

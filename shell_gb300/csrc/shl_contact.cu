@@ -5,9 +5,10 @@
 // immediately unless the device flag ctl->rebuild is set (so the pipeline can
 // be captured into a CUDA graph and skipped on device):
 //
-//   k_rb_aabb      per-face AABBs, shell bounds, avg_elem_size (fixed-order
-//                  sum), cell size, d_max, cell counts; TOO_MANY_CELLS check
-//                  (k_rb_grids and k_rb_grid_scan per shell for a batch)
+//   k_rb_aabb      per-face AABBs and sizes, per-block bounds
+//   k_rb_bounds    shell bounds, avg_elem_size (fixed-order sum), cell size,
+//                  d_max, cell counts; TOO_MANY_CELLS check (k_rb_grids and
+//                  k_rb_grid_scan per shell for a batch)
 //   k_rb_clear     clear the cell histogram and the per-face counters
 //   k_rb_count     cell ranges per face, cell histogram (counting sort, pass 1);
 //                  keep flags of the old list (ShellSystem.C:2016-2027)
@@ -17,7 +18,8 @@
 //                  from the lowest shared cell only, not topologically close, not
 //                  in the kept list, not AABB-apart by d_max, not certainly apart
 //                  along the line of centroids (a conservative prefilter)
-//   k_rb_narrow    per candidate: closest points, accept d2 <= d2_max
+//   k_rb_narrow    per candidate: closest points, accept d2 <= d2_max (SMOOTH:
+//                  k_limit_coeffs and k_smooth_search)
 //   scan, k_rb_scatter_new  accepted pairs grouped by eid1 (counting sort)
 //   scan           per-face pair counts -> segment offsets
 //   k_rb_assemble  kept old pairs + new pairs of each face, merged in e2 order
@@ -136,7 +138,6 @@ __global__ void __launch_bounds__(kBlock) k_rb_aabb(DevBuf b, StepConst sc) {
   Ctl* ctl = b.ctl;
   if (rb_off(ctl)) return;
   __shared__ double sh_min[3][kBlock], sh_max[3][kBlock];
-  __shared__ double lanes[SHL_SUM_LANES];
   const uint32_t f = blockIdx.x * blockDim.x + threadIdx.x;
   double lo[3] = {SHL_DBL_MAX, SHL_DBL_MAX, SHL_DBL_MAX}, hi[3] = {-SHL_DBL_MAX, -SHL_DBL_MAX, -SHL_DBL_MAX};
   if (f < sc.F) {
@@ -177,11 +178,35 @@ __global__ void __launch_bounds__(kBlock) k_rb_aabb(DevBuf b, StepConst sc) {
       b.partial[(size_t)blockIdx.x * 8 + c] = sh_min[c][0];
       b.partial[(size_t)blockIdx.x * 8 + 3 + c] = sh_max[c][0];
     }
+}
+
+// The shell's bounds, average element size and cell grid (ShellSystem.C:1910-1969)
+// from k_rb_aabb's per-block bounds and face sizes.  The 1024 lanes of the
+// fixed-order sum of shl_geom.h are added on kBoundsBlocks SMs (a lane's sum
+// is a chain of F / 1024 FP64 additions: on one SM the 1024 chains took most of
+// a pass's bounds step); the last block adds the lanes in the fixed tree and
+// makes the grid.
+constexpr int kBoundsBlocks = 16;
+__global__ void __launch_bounds__(kBlock) k_rb_bounds(DevBuf b, StepConst sc, uint32_t n_parts) {
+  Ctl* ctl = b.ctl;
+  if (rb_off(ctl) || sc.n_cs) return;  // a batch: per-shell grids (k_rb_grids)
+  __shared__ double sh_min[3][kBlock], sh_max[3][kBlock];
+  __shared__ double lanes[SHL_SUM_LANES];
+  {
+    constexpr uint32_t per_block = SHL_SUM_LANES / kBoundsBlocks;
+    const uint32_t l = blockIdx.x * per_block + threadIdx.x;
+    if (threadIdx.x < per_block) {
+      double acc = 0.0;
+#pragma unroll 4
+      for (uint32_t i = l; i < sc.F; i += SHL_SUM_LANES) acc = __dadd_rn(acc, __ldcg(&b.fsize[i]));
+      b.sum_lanes[l] = acc;
+    }
+  }
   if (!last_block_rb(&ctl->cnt[5])) return;
   // shell bounds (exact min/max)
   for (int c = 0; c < 3; ++c) {
     double mn = SHL_DBL_MAX, mx = -SHL_DBL_MAX;
-    for (uint32_t k = threadIdx.x; k < gridDim.x; k += blockDim.x) {
+    for (uint32_t k = threadIdx.x; k < n_parts; k += blockDim.x) {
       mn = fmin(mn, __ldcg(&b.partial[(size_t)k * 8 + c]));
       mx = fmax(mx, __ldcg(&b.partial[(size_t)k * 8 + 3 + c]));
     }
@@ -198,7 +223,7 @@ __global__ void __launch_bounds__(kBlock) k_rb_aabb(DevBuf b, StepConst sc) {
     __syncthreads();
   }
   // avg_elem_size: the fixed-order sum of shl_geom.h (1024 lanes, then a tree)
-  lane_sums<SHL_SUM_LANES / kBlock>(b.fsize, sc.F, lanes);
+  for (uint32_t l = threadIdx.x; l < SHL_SUM_LANES; l += blockDim.x) lanes[l] = __ldcg(&b.sum_lanes[l]);
   __syncthreads();
   for (uint32_t st = SHL_SUM_LANES / 2; st > 0; st >>= 1) {
     for (uint32_t l = threadIdx.x; l < st; l += blockDim.x) lanes[l] = __dadd_rn(lanes[l], lanes[l + st]);
@@ -1275,6 +1300,7 @@ void launch_contact_csr(const DevBuf& b, const StepConst& sc, cudaStream_t s) {
 void launch_rebuild(const DevBuf& b, const StepConst& sc, cudaStream_t s) {
   const uint32_t gF = nblk(sc.F);
   k_rb_aabb<<<gF, kBlock, 0, s>>>(b, sc);
+  if (!sc.n_cs) k_rb_bounds<<<kBoundsBlocks, kBlock, 0, s>>>(b, sc, gF);
   if (sc.n_cs) {
     k_rb_grids<<<sc.n_cs, kBlock, 0, s>>>(b, sc);
     k_rb_grid_scan<<<1, 1024, 0, s>>>(b, sc);

@@ -260,6 +260,7 @@ struct DevBuf {
   double* pvw[2];              // 4 per pair: the closest-point search's (v1, w1, v2, w2), patch frames
   double* new_x;               // 4 per new pair of a rebuild
   double* cand_x;              // 4 per candidate
+  double* sum_lanes;           // SHL_SUM_LANES lane sums of the face sizes (linked-cell pass)
   double* lcoef;               // per original face with a regular patch: the limit surface's power form
                                // (SHL_LIMIT_NCOEF), made before each search from the current positions
   uint32_t* inv_perm;          // original -> internal face
