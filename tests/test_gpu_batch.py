@@ -116,3 +116,47 @@ def test_batch_self_contact_equals_single_shells(cuda_ok, use_graph):
         assert c["du_sum"] == du_b[k]
         assert rg.n_rebuilds >= 1 and nr_b[k] == rg.n_rebuilds + 1  # + the rebuild before the steps
         g.close()
+
+
+def test_batch_smooth_contact_equals_single_shells(cuda_ok):
+    """SMOOTH self-contact in a batch: the limit patches (valence tables, patch
+    frames) and the closest-point searches of each shell equal those of the
+    shell run alone, bit for bit (pairs, d2, search coordinates, state)."""
+    specs = [(3, 0.01, {}, 3), (3, 0.015, dict(shell_young_modulus2=2.0), 5)]
+    meshes, params, u0s = [], [], []
+    for lv, h, kw, seed in specs:
+        X, T = L.icosphere(lv)
+        meshes.append((X, T))
+        params.append(physics_params(thickness=h, cell_size_mult=cell_size_mult_for(X, T, h),
+                                     shell_shell_contact=L.CONTACT_SMOOTH, **kw))
+        u0s.append(_squashed(X, seed))
+    n = 8
+    table = np.zeros(n)
+    b = L.Batch(meshes, params)
+    z = np.zeros(3 * b.V)
+    b.set_state(np.concatenate(u0s), z, z)
+    b.rebuild_contacts()
+    rb, sb = b.step(n, table)
+    assert rb.steps_done == n
+    ub, vb, ab = b.get_state()
+    cb = b.contact_state()
+    xb = b.contact_coords()
+    pairs_b = b.split_pairs(cb["pairs"])
+    shell_of_pair = np.searchsorted(b.face_off, cb["pairs"].reshape(-1, 2)[:, 0], side="right") - 1
+    b.close()
+    for k, ((X, T), p, u0) in enumerate(zip(meshes, params, u0s)):
+        g = L.Shell(X, T, p)
+        zz = np.zeros_like(u0)
+        g.set_state(u0, zz, zz)
+        g.rebuild_contacts()
+        g.step(n, table)
+        u, v, a = g.get_state()
+        for x, y in ((u, b.split(ub)[k]), (v, b.split(vb)[k]), (a, b.split(ab)[k])):
+            assert np.array_equal(_bits(x), _bits(y))
+        c = g.contact_state()
+        assert len(c["pairs"]) > 0, "the squashed shell is in contact"
+        assert np.array_equal(np.asarray(c["pairs"]).reshape(-1, 2), pairs_b[k])
+        sel = shell_of_pair == k
+        assert np.array_equal(_bits(c["d2"]), _bits(cb["d2"][sel]))
+        assert np.array_equal(_bits(g.contact_coords()), _bits(xb[sel]))
+        g.close()
