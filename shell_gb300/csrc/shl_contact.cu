@@ -762,22 +762,6 @@ __global__ void __launch_bounds__(kBlock) k_rb_narrow(DevBuf b, StepConst sc) {
   }
 }
 
-// SMOOTH closest-point searches with lane refill.  A search takes from one to
-// several hundred limit evaluations (most of a squashed shell's pairs end after
-// one to three, a few run the line search to its limit), so one thread per
-// pair would hold each warp until its longest search ends.  Here each lane
-// runs its search as a resumable state (shl_smooth_state): per trip a warp
-// evaluates one point of both limit patches per lane and advances the
-// searches, and a lane whose search has ended takes the next pair from a queue
-// shared by the grid (ctl->cnt[7]; the last warp to leave resets it), so that
-// the lanes stay busy until the queue is empty.  A search's result does not
-// depend on the lane or the order that runs it.
-//   REBUILD: the candidates of a linked-cell pass, each from (1/3, 1/3, 1/3,
-//   1/3) as a new SmoothShellShellContact (SmoothShellShellContact.C:9-14),
-//   then k_rb_narrow's acceptance;
-//   else: the pairs of the list from their previous solution; x, d2 and
-//   dc = p2 - p1 go to pvw, pd2 and the pair's force slots 0-2 for
-//   k_contact_force.
 // the power form of each regular patch at the current positions (irregular
 // patches are evaluated from their subdivision tables in the search)
 __global__ void __launch_bounds__(kBlock) k_limit_coeffs(DevBuf b, StepConst sc, bool rebuild) {
@@ -804,6 +788,22 @@ __device__ __forceinline__ void limit_at(const DevBuf& b, uint32_t e, const shl_
     shl_limit_eval(&lp, v, w, order, out);
 }
 
+// SMOOTH closest-point searches with lane refill.  A search takes from one to
+// several hundred limit evaluations (most of a squashed shell's pairs end after
+// one to three, a few run the line search to its limit), so one thread per
+// pair would hold each warp until its longest search ends.  Here each lane
+// runs its search as a resumable state (shl_smooth_state): per trip a warp
+// evaluates one point of both limit patches per lane and advances the
+// searches, and a lane whose search has ended takes the next pair from a queue
+// shared by the grid (ctl->cnt[7]; the last warp to leave resets it), so that
+// the lanes stay busy until the queue is empty.  A search's result does not
+// depend on the lane or the order that runs it.
+//   REBUILD: the candidates of a linked-cell pass, each from (1/3, 1/3, 1/3,
+//   1/3) as a new SmoothShellShellContact (SmoothShellShellContact.C:9-14),
+//   then k_rb_narrow's acceptance;
+//   else: the pairs of the list from their previous solution; x, d2 and
+//   dc = p2 - p1 go to pvw, pd2 and the pair's force slots 0-2 for
+//   k_contact_force.
 constexpr int kSearchBlock = 128;
 template <bool REBUILD>
 __global__ void __launch_bounds__(kSearchBlock) k_smooth_search(DevBuf b, StepConst sc) {
