@@ -425,7 +425,7 @@ __global__ void __launch_bounds__(kBlock) k_rb_count(DevBuf b, StepConst sc) {
 
 // ----------------------------------------------------------------- scan --
 // Exclusive scan of in[0..n) into out[0..n) (+ out[n] = total if with_end),
-// gated by *gate; three launches, fixed grids sized by capacity.
+// gated by *gate; two launches, fixed grids sized by capacity.
 __global__ void __launch_bounds__(kBlock) k_scan_tiles(const uint32_t* gate, const Ctl* ctl, const uint32_t* in,
                                                        uint32_t* out, const uint32_t* n_ptr, uint32_t n_const,
                                                        uint32_t* tile_sums) {
@@ -469,53 +469,45 @@ __global__ void __launch_bounds__(kBlock) k_scan_tiles(const uint32_t* gate, con
   if (threadIdx.x == kBlock - 1) tile_sums[blockIdx.x] = excl + sum;
 }
 
-__global__ void __launch_bounds__(1024) k_scan_sums(const uint32_t* gate, Ctl* ctl, uint32_t* out,
-                                                     const uint32_t* n_ptr, uint32_t n_const, uint32_t* tile_sums,
-                                                     uint32_t* total, int with_end, uint32_t cap, int cap_error) {
-  if (*gate == 0 || ctl->halted) return;
-  const uint32_t n = n_ptr ? *n_ptr : n_const;
-  const uint32_t nt = (n + kScanTile - 1) / kScanTile;
-  const uint32_t per = (nt + blockDim.x - 1) / blockDim.x;
-  const uint32_t t0 = threadIdx.x * per;
-  uint32_t s = 0;
-  for (uint32_t k = 0; k < per; ++k)
-    if (t0 + k < nt) s += tile_sums[t0 + k];
-  __shared__ uint32_t sh[1024];
-  sh[threadIdx.x] = s;
-  __syncthreads();
-  for (uint32_t o = 1; o < blockDim.x; o <<= 1) {
-    const uint32_t y = threadIdx.x >= o ? sh[threadIdx.x - o] : 0u;
-    __syncthreads();
-    sh[threadIdx.x] += y;
-    __syncthreads();
-  }
-  uint32_t run = sh[threadIdx.x] - s;
-  for (uint32_t k = 0; k < per; ++k)
-    if (t0 + k < nt) {
-      const uint32_t x = tile_sums[t0 + k];
-      tile_sums[t0 + k] = run;
-      run += x;
-    }
-  if (threadIdx.x == blockDim.x - 1) {
-    const uint32_t tot = sh[blockDim.x - 1];
-    *total = tot;
-    if (with_end) out[n] = tot;
-    if (cap_error && tot > cap) {
-      atomicMax(&ctl->error, (int)SHL_ERR_CAPACITY);
-      ctl->rebuild = 0;
-      ctl->csr_dirty = 0;
-    }
-  }
-}
-
-__global__ void __launch_bounds__(kBlock) k_scan_add(const uint32_t* gate, const Ctl* ctl, uint32_t* out,
+// Each tile's offset is the sum of the tiles before it, added up by the tile's
+// own block (a few hundred tile sums at most); block 0 adds all of them: the
+// total, out[n] and the capacity check.
+__global__ void __launch_bounds__(kBlock) k_scan_add(const uint32_t* gate, Ctl* ctl, uint32_t* out,
                                                      const uint32_t* n_ptr, uint32_t n_const,
-                                                     const uint32_t* tile_sums) {
+                                                     const uint32_t* tile_sums, uint32_t* total, int with_end,
+                                                     uint32_t cap, int cap_error) {
   if (*gate == 0 || ctl->halted) return;
   const uint32_t n = n_ptr ? *n_ptr : n_const;
   const uint32_t base = blockIdx.x * kScanTile;
-  if (base >= n || blockIdx.x == 0) return;
-  const uint32_t add = tile_sums[blockIdx.x];
+  if (blockIdx.x != 0 && base >= n) return;
+  const uint32_t upto = blockIdx.x == 0 ? (n + kScanTile - 1) / kScanTile : blockIdx.x;
+  uint32_t s = 0;
+  for (uint32_t t = threadIdx.x; t < upto; t += blockDim.x) s += tile_sums[t];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  __shared__ uint32_t wsum[kBlock / 32];
+  __shared__ uint32_t offset;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) wsum[warp] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t t = 0;
+    for (int w = 0; w < kBlock / 32; ++w) t += wsum[w];
+    offset = t;
+  }
+  __syncthreads();
+  const uint32_t add = offset;
+  if (blockIdx.x == 0) {
+    if (threadIdx.x == 0) {
+      *total = add;
+      if (with_end) out[n] = add;
+      if (cap_error && add > cap) {
+        atomicMax(&ctl->error, (int)SHL_ERR_CAPACITY);
+        ctl->rebuild = 0;
+        ctl->csr_dirty = 0;
+      }
+    }
+    return;
+  }
   for (uint32_t i = base + threadIdx.x; i < base + kScanTile && i < n; i += blockDim.x) out[i] += add;
 }
 
@@ -525,9 +517,8 @@ void launch_scan(const uint32_t* gate, Ctl* ctl, const uint32_t* in, uint32_t* o
   const uint32_t nt = (n_cap + kScanTile - 1) / kScanTile;
   const uint32_t grid = nt > 0 ? nt : 1;
   k_scan_tiles<<<grid, kBlock, 0, s>>>(gate, ctl, in, out, n_ptr, n_const, tile_sums);
-  k_scan_sums<<<1, 1024, 0, s>>>(gate, ctl, out, n_ptr, n_const, tile_sums, total, with_end ? 1 : 0, cap,
-                                 cap_error ? 1 : 0);
-  k_scan_add<<<grid, kBlock, 0, s>>>(gate, ctl, out, n_ptr, n_const, tile_sums);
+  k_scan_add<<<grid, kBlock, 0, s>>>(gate, ctl, out, n_ptr, n_const, tile_sums, total, with_end ? 1 : 0, cap,
+                                     cap_error ? 1 : 0);
 }
 
 // ----------------------------------------------------------------- fill --
