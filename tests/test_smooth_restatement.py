@@ -8,10 +8,11 @@ oracle/shell_oracle.cpp), both over the shared limit evaluation
 (shl_limit.h), must agree bit for bit: minimiser, squared distance, contact
 vector and iteration count.  The library's host build of the headers is
 compiled here into a small harness (g++, -ffp-contract=off, as the library's
-host code is built).  Inputs: pairs of faces of a squashed icosphere
-(regular and irregular patches, faces near and far apart) from the face
-centres, from random interior starts and from starts on the edges and
-vertices of the triangles.
+host code is built).  Inputs: pairs of faces of a squashed icosphere and of
+a squashed sphere with valence-5 and valence-7 patches (regular and
+irregular patches, faces near and far apart) from the face centres, from
+random interior starts and from starts on the edges and vertices of the
+triangles.
 """
 import ctypes
 import os
@@ -22,7 +23,7 @@ import pytest
 
 from shell_gb300 import lib as L
 import oracle as O
-from tests.common import cell_size_mult_for, physics_params
+from tests.common import cell_size_mult_for, flipped_sphere, physics_params
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 HARNESS = r'''
@@ -62,9 +63,9 @@ def harness(tmp_path_factory, built):
     return lib
 
 
-@pytest.fixture(scope="module")
-def state(built):
-    X, T = L.icosphere(3)
+@pytest.fixture(scope="module", params=["ico3", "flip"])
+def state(request, built):
+    X, T = L.icosphere(3) if request.param == "ico3" else flipped_sphere(1)
     p = physics_params(shell_shell_contact=L.CONTACT_SMOOTH, cell_size_mult=cell_size_mult_for(X, T, 0.01))
     o = O.Oracle(X, T, p, threads=2)
     rng = np.random.default_rng(17)
@@ -139,4 +140,4 @@ def test_search_equals_oracle_restatement(harness, state):
             assert it == ito
             n_checked += 1
             n_irr += (e1 in irregular) or (e2 in irregular)
-    assert n_checked > 200 and n_irr > 50
+    assert n_checked > 150 and n_irr > 50
